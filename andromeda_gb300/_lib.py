@@ -1,0 +1,66 @@
+"""ctypes binding of libandromeda_gb300.so (the C ABI in include/andromeda_gb300.h).
+
+The shared library is built in-tree by :mod:`andromeda_gb300.build`.  There is
+no fallback: if the library is missing or cannot be loaded, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libandromeda_gb300.so")
+
+# Every symbol the header declares, with its ctypes signature.
+dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+lp = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+vp = C.c_void_p
+I = C.c_int
+D = C.c_double
+PI = C.POINTER(C.c_int)
+
+SIGNATURES = {
+    "agb_version": ([], C.c_char_p),
+    "agb_create": ([C.POINTER(vp), I], I),
+    "agb_destroy": ([vp], I),
+    "agb_last_error": ([vp], C.c_char_p),
+    "agb_set_mesh": ([vp, I, dp, I, ip, ip, ip], I),
+    "agb_set_problem": ([vp, I, I, ip, dp, D, ip, I, I], I),
+    "agb_get_geometry": ([vp, dp, dp, dp], I),
+    "agb_system_size": ([vp, PI, PI], I),
+    "agb_assemble": ([vp, I], I),
+    "agb_get_system": ([vp, I, vp, vp], I),
+    "agb_rhs": ([vp, I, dp, dp], I),
+    "agb_solve": ([vp, I, dp, dp, I, D, I, ip, ip], I),
+    "agb_force_torque": ([vp, I, dp, I, dp], I),
+    "agb_resistance_tensor": ([vp, I, I, I, I, D, I, dp, ip, dp], I),
+    "agb_lsqr_precon": ([I, I, C.c_int64, dp, lp, ip, dp], I),
+    "agb_lsqr_solve": ([I, I, C.c_int64, PI, D, PI, PI, dp, lp, ip, dp, dp, dp], I),
+}
+
+_lib = None
+
+
+class AgbError(RuntimeError):
+    pass
+
+
+def load(path: str | None = None):
+    """Load the CUDA library (raises if it is absent: no CPU fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise AgbError(f"{p} is missing: build it with `python -m andromeda_gb300.build` "
+                       "(the GPU path has no fallback)")
+    L = C.CDLL(p)
+    for name, (args, res) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L

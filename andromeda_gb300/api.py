@@ -1,0 +1,175 @@
+"""Host-side front end of the GB300 BEM hot path.
+
+Mirrors the reference's operator interface for this path:
+
+* :func:`lsqr_precon` / :func:`lsqr_solve` -- the exact argument meaning of
+  ``lsqr_precon(m,n,nnz,q,ia,ja,a)`` and
+  ``lsqr_solve(m,n,nnz,maxit,eps,nit,ierr,q,ia,ja,a,b,x)`` (src/lib_lsqr.f:131,33):
+  1-based CRS, ``a`` scaled in place, ``x`` warm start in / solution out.
+* :class:`Context` -- mesh + one subdomain + BCs (the mMesh/mEqns module state),
+  assembly of the system on the GPU (CoR_Integrals + sdSetUpSysMrhsM_CRS /
+  stokesFormCRSsysMrhsM + lsqr_precon), right-hand sides, block LSQR solve,
+  force/torque (getForceIntegrateFluxes / getTorqueIntegrateFluxes) and the
+  resistance-tensor workflow (StokesInlet3sides*CRS).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import AgbError, load
+
+LAPLACE, STOKES = 1, 2
+FP64, MIXED = 0, 1
+BC_FUNCTION, BC_FLUX, BC_CONTACT = 1, 2, 3
+
+
+def _check(rc, ctx_ptr=None):
+    if rc != 0:
+        L = load()
+        msg = L.agb_last_error(ctx_ptr).decode()
+        raise AgbError(f"andromeda_gb300 error {rc}: {msg}")
+
+
+def version() -> str:
+    return load().agb_version().decode()
+
+
+def lsqr_precon(m, n, ia, ja, a, q=None):
+    """Column scaling q_j = 1/||A(:,j)|| and A <- A diag(q), on the GPU.
+
+    ``a`` (float64) is modified in place like the reference does; returns q.
+    """
+    L = load()
+    ia = np.ascontiguousarray(ia, dtype=np.int64)
+    ja = np.ascontiguousarray(ja, dtype=np.int32)
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    if q is None:
+        q = np.zeros(n)
+    _check(L.agb_lsqr_precon(int(m), int(n), len(a), q, ia, ja, a))
+    return q
+
+
+def lsqr_solve(m, n, ia, ja, a, q, b, x, maxit=0, eps=1e-8):
+    """LSQR with the reference's warm start and stopping rules, on the GPU.
+
+    ``x`` (float64) holds the initial guess and receives the solution.
+    Returns (nit, ierr) like the Fortran out-arguments.
+    """
+    L = load()
+    ia = np.ascontiguousarray(ia, dtype=np.int64)
+    ja = np.ascontiguousarray(ja, dtype=np.int32)
+    mi, nit, ierr = C.c_int(int(maxit)), C.c_int(0), C.c_int(0)
+    assert x.dtype == np.float64 and x.flags.c_contiguous
+    _check(L.agb_lsqr_solve(int(m), int(n), len(a), C.byref(mi), float(eps), C.byref(nit), C.byref(ierr),
+                            np.ascontiguousarray(q, dtype=np.float64), ia, ja,
+                            np.ascontiguousarray(a, dtype=np.float64), np.ascontiguousarray(b, dtype=np.float64), x))
+    return nit.value, ierr.value
+
+
+class Context:
+    """One GPU context: mesh, subdomain/BCs, resident system matrix."""
+
+    def __init__(self, device: int = 0):
+        self._L = load()
+        h = C.c_void_p()
+        rc = self._L.agb_create(C.byref(h), int(device))
+        if rc != 0:
+            raise AgbError(f"agb_create failed ({rc}): {self._L.agb_last_error(None).decode()}")
+        self.h = h
+        self.kind = None
+        self.mesh = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.agb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, rc):
+        _check(rc, self.h)
+
+    def set_mesh(self, mesh):
+        self.mesh = mesh
+        xyz = np.ascontiguousarray(mesh["xyz"], dtype=np.float64).ravel()
+        et = np.ascontiguousarray(mesh["etype"], dtype=np.int32)
+        con = np.ascontiguousarray(mesh["con"], dtype=np.int32).ravel()
+        bc = np.ascontiguousarray(mesh["bcid"], dtype=np.int32)
+        self.nnodes, self.nelem = len(mesh["xyz"]), len(et)
+        self._ck(self._L.agb_set_mesh(self.h, self.nnodes, xyz, self.nelem, et, con, bc))
+
+    def set_problem(self, kind, walls, known, normMul=None, diff=1.0, itri=5, iqud=4):
+        walls = np.ascontiguousarray(walls, dtype=np.int32)
+        nm = np.ones(len(walls)) if normMul is None else np.ascontiguousarray(normMul, dtype=np.float64)
+        kn = np.ascontiguousarray(known, dtype=np.int32).ravel()
+        self.kind = kind
+        self.neq = 3 if kind == STOKES else 1
+        self._ck(self._L.agb_set_problem(self.h, int(kind), len(walls), walls, nm, float(diff), kn, int(itri), int(iqud)))
+        m, n = C.c_int(), C.c_int()
+        self._ck(self._L.agb_system_size(self.h, C.byref(m), C.byref(n)))
+        self.m, self.n = m.value, n.value
+
+    def geometry(self):
+        nrm = np.zeros(3 * self.nelem)
+        area = np.zeros(self.nelem)
+        cen = np.zeros(3 * self.nelem)
+        self._ck(self._L.agb_get_geometry(self.h, nrm, area, cen))
+        return nrm.reshape(-1, 3), area, cen.reshape(-1, 3)
+
+    def assemble(self, precision=FP64):
+        self._ck(self._L.agb_assemble(self.h, int(precision)))
+
+    def system(self, scaled=False):
+        A = np.zeros((self.m, self.n))
+        q = np.zeros(self.n)
+        self._ck(self._L.agb_get_system(self.h, int(bool(scaled)), A.ctypes.data_as(C.c_void_p),
+                                        q.ctypes.data_as(C.c_void_p)))
+        return A, q
+
+    def rhs(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        nrhs = u.shape[0]
+        out = np.zeros((nrhs, self.m))
+        self._ck(self._L.agb_rhs(self.h, nrhs, u.ravel(), out.reshape(-1)))
+        return out
+
+    def solve(self, u, x0=None, maxit=0, eps=1e-8, refine=0):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        nrhs = u.shape[0]
+        x = np.zeros((nrhs, self.n)) if x0 is None else np.array(x0, dtype=np.float64, copy=True).reshape(nrhs, self.n)
+        nit = np.zeros(nrhs, np.int32)
+        istop = np.zeros(nrhs, np.int32)
+        self._ck(self._L.agb_solve(self.h, nrhs, u.ravel(), x.reshape(-1), int(maxit), float(eps), int(refine), nit, istop))
+        return x, nit, istop
+
+    def force_torque(self, x, wall):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        nrhs = x.shape[0]
+        ft = np.zeros((nrhs, 6))
+        self._ck(self._L.agb_force_torque(self.h, nrhs, x.reshape(-1), int(wall), ft.reshape(-1)))
+        return ft
+
+    def resistance_tensor(self, precision=MIXED, particle_wall=1, outer_wall=2, maxit=0, eps=1e-8, refine=0):
+        R = np.zeros((6, 6))
+        nit = np.zeros(6, np.int32)
+        t = np.zeros(5)
+        self._ck(self._L.agb_resistance_tensor(self.h, int(precision), int(particle_wall), int(outer_wall), int(maxit),
+                                               float(eps), int(refine), R.reshape(-1), nit, t))
+        return R, nit, {"assemble_ms": t[0], "rhs_ms": t[1], "solve_ms": t[2], "reduce_ms": t[3], "total_ms": t[4]}
+
+
+def dirichlet_known(kind, nwalls):
+    neq = 3 if kind == STOKES else 1
+    return np.full((neq, nwalls), BC_FUNCTION, dtype=np.int32)

@@ -1,0 +1,645 @@
+// C ABI of the GB300 BEM hot path: context, mesh/problem state, fused
+// assembly, block LSQR solve and the resistance-tensor workflow.
+#include "../../include/andromeda_gb300.h"
+#include "agb_assembly.cuh"
+#include "agb_lsqr.cuh"
+#include "quad_tables.h"
+
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+namespace agb {
+cudaError_t upload_gauss_tables();
+}
+
+using namespace agb;
+
+struct agb_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // mesh (host)
+  int nnodes = 0, nelem = 0;
+  std::vector<double> xyz;
+  std::vector<int> etype, con, bcid;
+  bool has_mesh = false;
+  // problem
+  int kind = 0, neq = 0;
+  std::vector<int> walls;
+  std::vector<double> normMul;
+  double diff = 1.0;
+  std::vector<int> known;
+  int itri = 5, iqud = 4;
+  bool has_problem = false;
+  // subdomain order
+  std::vector<int> elemList, posOfElem, wallIdx;
+  int ne = 0;
+  bool all_dirichlet = false, all_tri = false;
+  // device state
+  double* d_xyz = nullptr;
+  int *d_etype = nullptr, *d_con = nullptr, *d_wall = nullptr;
+  double* d_normMul = nullptr;
+  ElemGeom* d_geom = nullptr;
+  RuleDev rule;
+  // assembled system
+  int prec = -1;
+  void* d_A = nullptr;
+  int64_t lda = 0;
+  int m = 0, n = 0;
+  double* d_q = nullptr;
+  bool assembled = false;
+  DenseLsqr lsqr;
+  // scratch
+  void* d_pts = nullptr;
+  void* d_src = nullptr;
+  void* d_nrm = nullptr;
+  void* d_colscale = nullptr;
+  double *d_u = nullptr, *d_rhs = nullptr, *d_x = nullptr, *d_ft = nullptr;
+  int *d_active = nullptr;
+  unsigned char* d_rowact = nullptr;
+  size_t cap_u = 0, cap_rhs = 0, cap_x = 0, cap_act = 0;
+};
+
+namespace {
+thread_local std::string g_free_err;
+
+int fail(agb_context* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  else g_free_err = msg;
+  return code;
+}
+#define CUDA_OR_FAIL(ctx, expr)                                                               \
+  do {                                                                                        \
+    cudaError_t e_ = (expr);                                                                  \
+    if (e_ != cudaSuccess) return fail(ctx, AGB_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename P>
+void dfree(P*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+
+// Wandzura-Xiao orbit expansion into barycentric points on the reference
+// equilateral triangle (the construction of WandzuratXiaoBary,
+// mod_trikotnik.f90:682-781): every orbit point and its images under the two
+// maps of Table 1 of the paper, then barycentric coordinates w.r.t. the
+// vertices (-1/2, sqrt3/2), (-1/2, -sqrt3/2), (1, 0).
+void expand_rule(int itri, std::vector<double>& l, std::vector<double>& w) {
+  const int o0 = agb_tables::kWxOrbitOffset[itri - 1], o1 = agb_tables::kWxOrbitOffset[itri];
+  const double pi = 4.0 * std::atan(1.0);
+  const double s = std::sin(2.0 / 3.0 * pi), c = std::cos(2.0 / 3.0 * pi);
+  const double s4 = std::sin(4.0 / 3.0 * pi), c4 = std::cos(4.0 / 3.0 * pi);
+  std::vector<double> X, Y;
+  w.clear();
+  auto images = [&](double x, double y, double cc, double ss, double wt) {
+    const double xb = x * cc - y * ss, yb = -x * ss - y * cc;
+    const double xc = xb * cc + yb * ss, yc = -xb * ss + yb * cc;
+    X.insert(X.end(), {x, xb, xc});
+    Y.insert(Y.end(), {y, yb, yc});
+    w.insert(w.end(), {wt, wt, wt});
+  };
+  for (int j = o0; j < o1; ++j) {
+    const auto& ob = agb_tables::kWxOrbits[j];
+    if (ob.m == 1) {
+      X.push_back(ob.x); Y.push_back(ob.y); w.push_back(ob.w);
+    } else {
+      images(ob.x, ob.y, c, s, ob.w);
+      if (ob.m == 6) images(ob.x, -ob.y, c4, s4, ob.w);
+    }
+  }
+  const int Q = (int)X.size();
+  l.assign(3 * Q, 0.0);
+  const double x1 = -0.5, y1 = 0.5 * std::sqrt(3.0), x2 = -0.5, y2 = -0.5 * std::sqrt(3.0), x3 = 1.0, y3 = 0.0;
+  for (int i = 0; i < Q; ++i) {
+    const double v0x = x2 - x1, v0y = y2 - y1, v1x = x3 - x1, v1y = y3 - y1, v2x = X[i] - x1, v2y = Y[i] - y1;
+    const double d00 = v0x * v0x + v0y * v0y, d01 = v0x * v1x + v0y * v1y, d11 = v1x * v1x + v1y * v1y;
+    const double d20 = v2x * v0x + v2y * v0y, d21 = v2x * v1x + v2y * v1y;
+    const double den = d00 * d11 - d01 * d01;
+    const double a = (d11 * d20 - d01 * d21) / den, b = (d00 * d21 - d01 * d20) / den;
+    l[i] = a;
+    l[Q + i] = b;
+    l[2 * Q + i] = 1.0 - a - b;
+  }
+}
+
+template <typename T>
+cudaError_t ensure(T*& p, size_t& cap, size_t count) {
+  if (count <= cap && p) return cudaSuccess;
+  if (p) cudaFree(p);
+  p = nullptr;
+  cap = 0;
+  cudaError_t e = cudaMalloc((void**)&p, std::max<size_t>(count, 1) * sizeof(T));
+  if (e == cudaSuccess) cap = count;
+  return e;
+}
+
+void free_system(agb_context* c) {
+  dfree(c->d_A);
+  dfree(c->d_q);
+  dfree(c->d_pts);
+  dfree(c->d_src);
+  dfree(c->d_nrm);
+  dfree(c->d_colscale);
+  c->lsqr.release();
+  c->assembled = false;
+  c->prec = -1;
+}
+void free_problem(agb_context* c) {
+  free_system(c);
+  dfree(c->d_etype);
+  dfree(c->d_con);
+  dfree(c->d_wall);
+  dfree(c->d_normMul);
+  dfree(c->d_geom);
+  dfree(c->rule.l);
+  dfree(c->rule.w);
+  c->has_problem = false;
+}
+
+int check_ctx(agb_context* c, bool need_problem) {
+  if (!c) return AGB_ERR_ARG;
+  if (!c->has_mesh) return fail(c, AGB_ERR_STATE, "no mesh set (agb_set_mesh)");
+  if (need_problem && !c->has_problem) return fail(c, AGB_ERR_STATE, "no problem set (agb_set_problem)");
+  return AGB_OK;
+}
+
+// Upload u fields [nrhs][neq][nnodes]; mark active elements (any nonzero
+// nodal value) and rows whose own element is active.
+int stage_u(agb_context* c, int nrhs, const double* u, int* na_out) {
+  const size_t cnt = (size_t)nrhs * c->neq * c->nnodes;
+  CUDA_OR_FAIL(c, ensure(c->d_u, c->cap_u, cnt));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_u, u, cnt * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  std::vector<char> nz(c->nnodes, 0);
+  for (size_t t = 0; t < cnt; ++t)
+    if (u[t] != 0.0) nz[t % c->nnodes] = 1;
+  std::vector<int> act;
+  std::vector<unsigned char> rowact(c->ne, 0);
+  for (int p = 0; p < c->ne; ++p) {
+    const int e = c->elemList[p];
+    const int nno = (c->etype[e] == AGB_TRI) ? 3 : 4;
+    bool a = false;
+    for (int k = 0; k < nno; ++k) a = a || nz[c->con[4 * e + k]];
+    if (a) { act.push_back(p); rowact[p] = 1; }
+  }
+  CUDA_OR_FAIL(c, ensure(c->d_active, c->cap_act, std::max<size_t>(act.size(), (size_t)c->ne)));
+  if (!c->d_rowact) CUDA_OR_FAIL(c, cudaMalloc(&c->d_rowact, std::max(c->ne, 1)));
+  if (!act.empty())
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_active, act.data(), act.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_rowact, rowact.data(), c->ne, cudaMemcpyHostToDevice, c->stream));
+  // the host vectors above are freed on return: make the copies complete
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  *na_out = (int)act.size();
+  return AGB_OK;
+}
+
+// rhs on the device for nrhs fields already staged in d_u
+int device_rhs(agb_context* c, int nrhs, int na) {
+  CUDA_OR_FAIL(c, ensure(c->d_rhs, c->cap_rhs, (size_t)nrhs * c->m));
+  if (c->kind == AGB_STOKES) {
+    StokesRhsArgs a;
+    a.ne = c->ne; a.Q = c->rule.Q; a.ldp = 0; a.k = nrhs; a.nnodes = c->nnodes;
+    a.geom = c->d_geom; a.rule_l = c->rule.l; a.rule_w = c->rule.w; a.u = c->d_u;
+    a.active = c->d_active; a.na = na; a.row_active = c->d_rowact; a.rhs = c->d_rhs;
+    if (c->prec == AGB_MIXED) CUDA_OR_FAIL(c, launch_stokes_rhs<float>(a, c->stream));
+    else CUDA_OR_FAIL(c, launch_stokes_rhs<double>(a, c->stream));
+  } else {
+    LaplaceArgs a;
+    a.ne = c->ne; a.Q = c->rule.Q; a.k = nrhs; a.nnodes = c->nnodes; a.iqud = c->iqud;
+    a.geom = c->d_geom; a.rule_l = c->rule.l; a.rule_w = c->rule.w; a.u = c->d_u; a.diff = c->diff;
+    a.A = nullptr; a.lda = c->lda; a.rhs = c->d_rhs;
+    cudaError_t e = launch_laplace_system(a, c->stream);
+    CUDA_OR_FAIL(c, e);
+  }
+  return AGB_OK;
+}
+
+int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int refine, int* nit, int* istop) {
+  if (!c->lsqr.A || c->lsqr.k != nrhs) {
+    if (!c->lsqr.setup(c->d_A, c->prec == AGB_MIXED, c->m, c->n, c->lda, nrhs, c->stream))
+      return fail(c, AGB_ERR_CUDA, "lsqr setup: " + c->lsqr.err);
+  }
+  std::vector<int> nt(nrhs, 0), is(nrhs, 0);
+  for (int pass = 0; pass <= refine; ++pass) {
+    if (!c->lsqr.solve(c->d_rhs, d_x, c->d_q, eps, maxit, nt.data(), is.data()))
+      return fail(c, AGB_ERR_CUDA, "lsqr: " + c->lsqr.err);
+    for (int r = 0; r < nrhs; ++r) {
+      if (nit) nit[r] = (pass == 0 ? 0 : nit[r]) + nt[r];
+      if (istop) istop[r] = is[r];
+    }
+  }
+  return AGB_OK;
+}
+}  // namespace
+
+extern "C" {
+
+const char* agb_version(void) { return "andromeda_gb300 0.1 (sm_103a)"; }
+
+int agb_create(agb_context** out, int device) {
+  if (!out) return AGB_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    g_free_err = std::string("no CUDA device: ") + cudaGetErrorString(e);
+    return AGB_ERR_CUDA;
+  }
+  if (device < 0 || device >= ndev) {
+    g_free_err = "device index out of range";
+    return AGB_ERR_ARG;
+  }
+  agb_context* c = new agb_context();
+  c->device = device;
+  e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = upload_gauss_tables();
+  if (e != cudaSuccess) {
+    g_free_err = std::string("agb_create: ") + cudaGetErrorString(e);
+    delete c;
+    return AGB_ERR_CUDA;
+  }
+  *out = c;
+  return AGB_OK;
+}
+
+int agb_destroy(agb_context* c) {
+  if (!c) return AGB_OK;
+  cudaSetDevice(c->device);
+  free_problem(c);
+  dfree(c->d_xyz);
+  dfree(c->d_u);
+  dfree(c->d_rhs);
+  dfree(c->d_x);
+  dfree(c->d_ft);
+  dfree(c->d_active);
+  dfree(c->d_rowact);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return AGB_OK;
+}
+
+const char* agb_last_error(const agb_context* c) { return c ? c->err.c_str() : g_free_err.c_str(); }
+
+int agb_set_mesh(agb_context* c, int nnodes, const double* xyz, int nelem, const int* etype, const int* con,
+                 const int* bcid) {
+  if (!c) return AGB_ERR_ARG;
+  if (nnodes <= 0 || nelem <= 0 || !xyz || !etype || !con || !bcid) return fail(c, AGB_ERR_ARG, "empty mesh");
+  for (int e = 0; e < nelem; ++e) {
+    if (etype[e] != AGB_TRI && etype[e] != AGB_QUAD) return fail(c, AGB_ERR_ARG, "element type must be 2 or 3");
+    const int nno = etype[e] == AGB_TRI ? 3 : 4;
+    for (int k = 0; k < nno; ++k)
+      if (con[4 * e + k] < 0 || con[4 * e + k] >= nnodes) return fail(c, AGB_ERR_ARG, "connectivity out of range");
+  }
+  cudaSetDevice(c->device);
+  free_problem(c);
+  c->nnodes = nnodes;
+  c->nelem = nelem;
+  c->xyz.assign(xyz, xyz + 3 * (size_t)nnodes);
+  c->etype.assign(etype, etype + nelem);
+  c->con.assign(con, con + 4 * (size_t)nelem);
+  c->bcid.assign(bcid, bcid + nelem);
+  dfree(c->d_xyz);
+  CUDA_OR_FAIL(c, cudaMalloc(&c->d_xyz, c->xyz.size() * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_xyz, c->xyz.data(), c->xyz.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                  c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  c->has_mesh = true;
+  return AGB_OK;
+}
+
+int agb_set_problem(agb_context* c, int kind, int nwalls, const int* walls, const double* normMul, double diff,
+                    const int* known, int itri, int iqud) {
+  int rc = check_ctx(c, false);
+  if (rc) return rc;
+  if (kind != AGB_LAPLACE && kind != AGB_STOKES) return fail(c, AGB_ERR_ARG, "kind must be AGB_LAPLACE or AGB_STOKES");
+  if (nwalls <= 0 || !walls || !known) return fail(c, AGB_ERR_ARG, "no walls");
+  if (itri < 1 || itri > 5) return fail(c, AGB_ERR_ARG, "itri must be 1..5");
+  if (iqud < 1 || iqud > 8) return fail(c, AGB_ERR_ARG, "iqud must be 1..8");
+  if (!(diff != 0.0) || !std::isfinite(diff)) return fail(c, AGB_ERR_ARG, "diff must be finite and nonzero");
+  cudaSetDevice(c->device);
+  free_problem(c);
+  c->kind = kind;
+  c->neq = (kind == AGB_STOKES) ? 3 : 1;
+  c->walls.assign(walls, walls + nwalls);
+  c->normMul.assign(nwalls, 1.0);
+  if (normMul) c->normMul.assign(normMul, normMul + nwalls);
+  c->diff = diff;
+  c->known.assign(known, known + c->neq * nwalls);
+  c->itri = itri;
+  c->iqud = iqud;
+  // subdomain element order: walls in list order, then element index (SetUpSubdomains)
+  c->elemList.clear();
+  c->wallIdx.clear();
+  c->posOfElem.assign(c->nelem, -1);
+  for (int k = 0; k < nwalls; ++k)
+    for (int e = 0; e < c->nelem; ++e)
+      if (c->bcid[e] == walls[k] && c->posOfElem[e] < 0) {
+        c->posOfElem[e] = (int)c->elemList.size();
+        c->elemList.push_back(e);
+        c->wallIdx.push_back(k);
+      }
+  c->ne = (int)c->elemList.size();
+  if (c->ne == 0) return fail(c, AGB_ERR_ARG, "no element belongs to the subdomain walls");
+  c->all_dirichlet = true;
+  for (int v : c->known)
+    if (v != AGB_BC_FUNCTION) c->all_dirichlet = false;
+  c->all_tri = true;
+  for (int e : c->elemList)
+    if (c->etype[e] != AGB_TRI) c->all_tri = false;
+  // device copies in subdomain order
+  std::vector<int> et(c->ne), cn(4 * (size_t)c->ne);
+  for (int p = 0; p < c->ne; ++p) {
+    const int e = c->elemList[p];
+    et[p] = c->etype[e];
+    for (int k = 0; k < 4; ++k) cn[4 * p + k] = c->con[4 * e + k];
+  }
+  CUDA_OR_FAIL(c, cudaMalloc(&c->d_etype, c->ne * sizeof(int)));
+  CUDA_OR_FAIL(c, cudaMalloc(&c->d_con, 4 * (size_t)c->ne * sizeof(int)));
+  CUDA_OR_FAIL(c, cudaMalloc(&c->d_wall, c->ne * sizeof(int)));
+  CUDA_OR_FAIL(c, cudaMalloc(&c->d_normMul, nwalls * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMalloc(&c->d_geom, c->ne * sizeof(ElemGeom)));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_etype, et.data(), c->ne * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_con, cn.data(), cn.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_wall, c->wallIdx.data(), c->ne * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_normMul, c->normMul.data(), nwalls * sizeof(double), cudaMemcpyHostToDevice,
+                                  c->stream));
+  CUDA_OR_FAIL(c, launch_geometry(c->ne, c->d_xyz, c->d_etype, c->d_con, c->d_wall, c->d_normMul, c->d_geom, c->stream));
+  std::vector<double> l, w;
+  expand_rule(itri, l, w);
+  c->rule.Q = (int)w.size();
+  CUDA_OR_FAIL(c, cudaMalloc(&c->rule.l, l.size() * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMalloc(&c->rule.w, w.size() * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->rule.l, l.data(), l.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->rule.w, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  c->m = c->n = c->neq * c->ne;
+  c->has_problem = true;
+  return AGB_OK;
+}
+
+int agb_get_geometry(agb_context* c, double* normal, double* area, double* centroid) {
+  int rc = check_ctx(c, true);
+  if (rc) return rc;
+  cudaSetDevice(c->device);
+  std::vector<ElemGeom> g(c->ne);
+  CUDA_OR_FAIL(c, cudaMemcpy(g.data(), c->d_geom, c->ne * sizeof(ElemGeom), cudaMemcpyDeviceToHost));
+  if (normal) std::fill(normal, normal + 3 * (size_t)c->nelem, 0.0);
+  if (area) std::fill(area, area + c->nelem, 0.0);
+  if (centroid) std::fill(centroid, centroid + 3 * (size_t)c->nelem, 0.0);
+  for (int p = 0; p < c->ne; ++p) {
+    const int e = c->elemList[p];
+    for (int i = 0; i < 3; ++i) {
+      if (normal) normal[3 * e + i] = g[p].n[i];
+      if (centroid) centroid[3 * e + i] = g[p].c[i];
+    }
+    if (area) area[e] = g[p].area;
+  }
+  return AGB_OK;
+}
+
+int agb_system_size(agb_context* c, int* m, int* n) {
+  int rc = check_ctx(c, true);
+  if (rc) return rc;
+  if (m) *m = c->m;
+  if (n) *n = c->n;
+  return AGB_OK;
+}
+
+int agb_assemble(agb_context* c, int precision) {
+  int rc = check_ctx(c, true);
+  if (rc) return rc;
+  if (precision != AGB_FP64 && precision != AGB_MIXED) return fail(c, AGB_ERR_ARG, "precision must be AGB_FP64 or AGB_MIXED");
+  if (!c->all_dirichlet)
+    return fail(c, AGB_ERR_UNSUPPORTED, "agb_assemble: only walls with known function values are supported");
+  if (c->kind == AGB_LAPLACE && precision != AGB_FP64)
+    return fail(c, AGB_ERR_UNSUPPORTED, "Laplace systems are assembled in FP64 only");
+  if (c->kind == AGB_STOKES && !c->all_tri)
+    return fail(c, AGB_ERR_UNSUPPORTED, "Stokes fused assembly needs a triangle mesh");
+  cudaSetDevice(c->device);
+  free_system(c);
+  c->prec = precision;
+  const bool f32 = (precision == AGB_MIXED);
+  const size_t tsz = f32 ? sizeof(float) : sizeof(double);
+  c->lda = ((int64_t)c->n + 31) / 32 * 32;
+  CUDA_OR_FAIL(c, cudaMalloc(&c->d_A, (size_t)c->m * c->lda * tsz));
+  if (c->lda > c->n)
+    CUDA_OR_FAIL(c, cudaMemset2DAsync((char*)c->d_A + c->n * tsz, c->lda * tsz, 0, (c->lda - c->n) * tsz, c->m,
+                                      c->stream));
+  CUDA_OR_FAIL(c, cudaMalloc(&c->d_q, c->lda * sizeof(double)));
+  if (c->kind == AGB_STOKES) {
+    const int ldp = (c->ne + 31) / 32 * 32;
+    const int Q = c->rule.Q;
+    CUDA_OR_FAIL(c, cudaMalloc(&c->d_pts, (size_t)Q * ldp * (f32 ? sizeof(QPt<float>) : sizeof(QPt<double>))));
+    CUDA_OR_FAIL(c, cudaMalloc(&c->d_src, 3 * (size_t)ldp * tsz));
+    CUDA_OR_FAIL(c, cudaMalloc(&c->d_nrm, 3 * (size_t)ldp * tsz));
+    CUDA_OR_FAIL(c, cudaMalloc(&c->d_colscale, (size_t)ldp * tsz));
+    std::vector<double> cs(ldp, 0.0);
+    for (int p = 0; p < c->ne; ++p) cs[p] = -c->normMul[c->wallIdx[p]] / c->diff;
+    if (f32) {
+      std::vector<float> csf(cs.begin(), cs.end());
+      CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_colscale, csf.data(), ldp * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+      CUDA_OR_FAIL(c, launch_expand_points<float>(c->ne, ldp, c->d_geom, c->rule, (QPt<float>*)c->d_pts,
+                                                  (float*)c->d_src, (float*)c->d_nrm, c->stream));
+      CUDA_OR_FAIL(c, launch_stokes_G<float>(c->ne, Q, ldp, (const QPt<float>*)c->d_pts, (const float*)c->d_src,
+                                             (const float*)c->d_colscale, (float*)c->d_A, c->lda, c->stream));
+      CUDA_OR_FAIL(c, launch_stokes_self<float>(c->ne, c->d_geom, c->diff, (float*)c->d_A, c->lda, c->stream));
+    } else {
+      CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_colscale, cs.data(), ldp * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+      CUDA_OR_FAIL(c, launch_expand_points<double>(c->ne, ldp, c->d_geom, c->rule, (QPt<double>*)c->d_pts,
+                                                   (double*)c->d_src, (double*)c->d_nrm, c->stream));
+      CUDA_OR_FAIL(c, launch_stokes_G<double>(c->ne, Q, ldp, (const QPt<double>*)c->d_pts, (const double*)c->d_src,
+                                              (const double*)c->d_colscale, (double*)c->d_A, c->lda, c->stream));
+      CUDA_OR_FAIL(c, launch_stokes_self<double>(c->ne, c->d_geom, c->diff, (double*)c->d_A, c->lda, c->stream));
+    }
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  } else {
+    LaplaceArgs a;
+    a.ne = c->ne; a.Q = c->rule.Q; a.k = 0; a.nnodes = c->nnodes; a.iqud = c->iqud;
+    a.geom = c->d_geom; a.rule_l = c->rule.l; a.rule_w = c->rule.w; a.u = nullptr; a.diff = c->diff;
+    a.A = (double*)c->d_A; a.lda = c->lda; a.rhs = nullptr;
+    CUDA_OR_FAIL(c, launch_laplace_system(a, c->stream));
+  }
+  // column scaling of lsqr_precon
+  if (!c->lsqr.setup(c->d_A, f32, c->m, c->n, c->lda, 1, c->stream)) return fail(c, AGB_ERR_CUDA, c->lsqr.err);
+  if (!c->lsqr.precon(c->d_A, c->d_q)) return fail(c, AGB_ERR_CUDA, c->lsqr.err);
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  c->assembled = true;
+  return AGB_OK;
+}
+
+int agb_get_system(agb_context* c, int scaled, double* A, double* q) {
+  int rc = check_ctx(c, true);
+  if (rc) return rc;
+  if (!c->assembled) return fail(c, AGB_ERR_STATE, "system not assembled");
+  cudaSetDevice(c->device);
+  std::vector<double> qh(c->lda);
+  CUDA_OR_FAIL(c, cudaMemcpy(qh.data(), c->d_q, c->lda * sizeof(double), cudaMemcpyDeviceToHost));
+  if (q) std::copy(qh.begin(), qh.begin() + c->n, q);
+  if (A) {
+    const bool f32 = c->prec == AGB_MIXED;
+    std::vector<char> buf((size_t)c->lda * (f32 ? 4 : 8));
+    for (int r = 0; r < c->m; ++r) {
+      CUDA_OR_FAIL(c, cudaMemcpy(buf.data(), (char*)c->d_A + (size_t)r * c->lda * (f32 ? 4 : 8), buf.size(),
+                                 cudaMemcpyDeviceToHost));
+      for (int j = 0; j < c->n; ++j) {
+        double v = f32 ? (double)((float*)buf.data())[j] : ((double*)buf.data())[j];
+        A[(size_t)r * c->n + j] = scaled ? v : v / qh[j];
+      }
+    }
+  }
+  return AGB_OK;
+}
+
+int agb_rhs(agb_context* c, int nrhs, const double* u, double* rhs) {
+  int rc = check_ctx(c, true);
+  if (rc) return rc;
+  if (!c->assembled) return fail(c, AGB_ERR_STATE, "system not assembled");
+  if (nrhs < 1 || nrhs > AGB_MAX_RHS || !u) return fail(c, AGB_ERR_ARG, "nrhs must be 1..8");
+  cudaSetDevice(c->device);
+  int na = 0;
+  if ((rc = stage_u(c, nrhs, u, &na))) return rc;
+  if ((rc = device_rhs(c, nrhs, na))) return rc;
+  if (rhs)
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(rhs, c->d_rhs, (size_t)nrhs * c->m * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  return AGB_OK;
+}
+
+int agb_solve(agb_context* c, int nrhs, const double* u, double* x, int maxit, double eps, int refine, int* nit,
+              int* istop) {
+  int rc = check_ctx(c, true);
+  if (rc) return rc;
+  if (!c->assembled) return fail(c, AGB_ERR_STATE, "system not assembled");
+  if (nrhs < 1 || nrhs > AGB_MAX_RHS || !u || !x) return fail(c, AGB_ERR_ARG, "nrhs must be 1..8");
+  if (maxit < 0 || !(eps >= 0.0) || refine < 0) return fail(c, AGB_ERR_ARG, "bad solver parameters");
+  cudaSetDevice(c->device);
+  int na = 0;
+  if ((rc = stage_u(c, nrhs, u, &na))) return rc;
+  if ((rc = device_rhs(c, nrhs, na))) return rc;
+  CUDA_OR_FAIL(c, ensure(c->d_x, c->cap_x, (size_t)nrhs * c->n));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_x, x, (size_t)nrhs * c->n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if ((rc = do_solve(c, nrhs, c->d_x, maxit, eps, refine, nit, istop))) return rc;
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(x, c->d_x, (size_t)nrhs * c->n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  return AGB_OK;
+}
+
+int agb_force_torque(agb_context* c, int nrhs, const double* x, int wall, double* ft) {
+  int rc = check_ctx(c, true);
+  if (rc) return rc;
+  if (c->kind != AGB_STOKES) return fail(c, AGB_ERR_UNSUPPORTED, "force/torque needs a Stokes problem");
+  if (nrhs < 1 || nrhs > AGB_MAX_RHS || !x || !ft) return fail(c, AGB_ERR_ARG, "bad arguments");
+  int widx = -1;
+  for (size_t k = 0; k < c->walls.size(); ++k)
+    if (c->walls[k] == wall) widx = (int)k;
+  if (widx < 0) return fail(c, AGB_ERR_ARG, "wall not in the subdomain");
+  cudaSetDevice(c->device);
+  CUDA_OR_FAIL(c, ensure(c->d_x, c->cap_x, (size_t)nrhs * c->n));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_x, x, (size_t)nrhs * c->n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (!c->d_ft) CUDA_OR_FAIL(c, cudaMalloc(&c->d_ft, 6 * AGB_MAX_RHS * sizeof(double)));
+  CUDA_OR_FAIL(c, launch_force_torque(c->ne, nrhs, c->d_geom, c->d_x, widx, c->d_ft, c->stream));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(ft, c->d_ft, 6 * (size_t)nrhs * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  return AGB_OK;
+}
+
+int agb_resistance_tensor(agb_context* c, int precision, int particle_wall, int outer_wall, int maxit, double eps,
+                          int refine, double* R, int* nit, double* times_ms) {
+  int rc = check_ctx(c, true);
+  if (rc) return rc;
+  if (c->kind != AGB_STOKES) return fail(c, AGB_ERR_UNSUPPORTED, "resistance tensor needs a Stokes problem");
+  if (!R) return fail(c, AGB_ERR_ARG, "R is NULL");
+  int pidx = -1, oidx = -1;
+  for (size_t k = 0; k < c->walls.size(); ++k) {
+    if (c->walls[k] == particle_wall) pidx = (int)k;
+    if (c->walls[k] == outer_wall) oidx = (int)k;
+  }
+  if (pidx < 0 || oidx < 0) return fail(c, AGB_ERR_ARG, "particle/outer wall not in the subdomain");
+  cudaSetDevice(c->device);
+  using clk = std::chrono::steady_clock;
+  auto ms = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
+  auto t0 = clk::now();
+  if ((rc = agb_assemble(c, precision))) return rc;
+  auto t1 = clk::now();
+  // six rigid motions of the container, particle at rest
+  const int k = 6;
+  std::vector<double> u((size_t)k * 3 * c->nnodes, 0.0);
+  std::vector<char> onOuter(c->nnodes, 0);
+  for (int p = 0; p < c->ne; ++p)
+    if (c->wallIdx[p] == oidx) {
+      const int e = c->elemList[p];
+      for (int kk = 0; kk < 3; ++kk) onOuter[c->con[4 * e + kk]] = 1;
+    }
+  for (int i = 0; i < c->nnodes; ++i) {
+    if (!onOuter[i]) continue;
+    const double* x = &c->xyz[3 * i];
+    for (int a = 0; a < 3; ++a) u[((size_t)a * 3 + a) * c->nnodes + i] = 1.0;
+    // e_a x r
+    const double w[3][3] = {{0, -x[2], x[1]}, {x[2], 0, -x[0]}, {-x[1], x[0], 0}};
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) u[((size_t)(3 + a) * 3 + b) * c->nnodes + i] = w[a][b];
+  }
+  int na = 0;
+  if ((rc = stage_u(c, k, u.data(), &na))) return rc;
+  if ((rc = device_rhs(c, k, na))) return rc;
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  auto t2 = clk::now();
+  CUDA_OR_FAIL(c, ensure(c->d_x, c->cap_x, (size_t)k * c->n));
+  CUDA_OR_FAIL(c, cudaMemsetAsync(c->d_x, 0, (size_t)k * c->n * sizeof(double), c->stream));
+  std::vector<int> nt(k), is(k);
+  if ((rc = do_solve(c, k, c->d_x, maxit, eps, refine, nt.data(), is.data()))) return rc;
+  auto t3 = clk::now();
+  if (!c->d_ft) CUDA_OR_FAIL(c, cudaMalloc(&c->d_ft, 6 * AGB_MAX_RHS * sizeof(double)));
+  CUDA_OR_FAIL(c, launch_force_torque(c->ne, k, c->d_geom, c->d_x, pidx, c->d_ft, c->stream));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(R, c->d_ft, 36 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  auto t4 = clk::now();
+  if (nit)
+    for (int r = 0; r < k; ++r) nit[r] = nt[r];
+  if (times_ms) {
+    times_ms[0] = ms(t0, t1);
+    times_ms[1] = ms(t1, t2);
+    times_ms[2] = ms(t2, t3);
+    times_ms[3] = ms(t3, t4);
+    times_ms[4] = ms(t0, t4);
+  }
+  for (int r = 0; r < k; ++r)
+    if (is[r] > 3) return fail(c, AGB_ERR_NUMERIC, "LSQR stopped with istop > 3 (iteration limit or ill conditioning)");
+  return AGB_OK;
+}
+
+// The CRS is checked on the host before it reaches the GPU: 1-based,
+// nondecreasing row starts ia(1) = 1, ia(m+1) = nnz+1, 1 <= ja <= n.
+static bool crs_valid(int m, int n, int64_t nnz, const int64_t* ia, const int* ja) {
+  if (ia[0] != 1 || ia[m] != nnz + 1) return false;
+  for (int r = 0; r < m; ++r)
+    if (ia[r + 1] < ia[r]) return false;
+  for (int64_t t = 0; t < nnz; ++t)
+    if (ja[t] < 1 || ja[t] > n) return false;
+  return true;
+}
+
+int agb_lsqr_precon(int m, int n, int64_t nnz, double* q, const int64_t* ia, const int* ja, double* a) {
+  if (m <= 0 || n <= 0 || nnz < 0 || !q || !ia || !ja || !a) return fail(nullptr, AGB_ERR_ARG, "bad CRS arguments");
+  if (!crs_valid(m, n, nnz, ia, ja)) return fail(nullptr, AGB_ERR_ARG, "malformed CRS (ia/ja out of range)");
+  std::string err;
+  if (!crs_lsqr_precon(m, n, nnz, q, ia, ja, a, err)) return fail(nullptr, AGB_ERR_CUDA, err);
+  return AGB_OK;
+}
+
+int agb_lsqr_solve(int m, int n, int64_t nnz, int* maxit, double eps, int* nit, int* ierr, const double* q,
+                   const int64_t* ia, const int* ja, double* a, const double* b, double* x) {
+  if (m <= 0 || n <= 0 || nnz < 0 || !maxit || !nit || !ierr || !q || !ia || !ja || !a || !b || !x)
+    return fail(nullptr, AGB_ERR_ARG, "bad CRS arguments");
+  if (!crs_valid(m, n, nnz, ia, ja)) return fail(nullptr, AGB_ERR_ARG, "malformed CRS (ia/ja out of range)");
+  std::string err;
+  if (!crs_lsqr_solve(m, n, nnz, *maxit, eps, *nit, *ierr, q, ia, ja, a, b, x, err)) return fail(nullptr, AGB_ERR_CUDA, err);
+  return AGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,940 @@
+// Block LSQR on the GPU: dense sweeps over an HBM-resident matrix shared by up
+// to 8 right-hand sides, plus the CRS solver behind the lsqr_solve drop-in.
+//
+// The recurrence is Paige & Saunders' LSQR exactly as the reference runs it
+// (src/lib_lsqr.f:470-1231, damp = 0, no standard errors), with the reference's
+// column scaling (lsqr_precon, :131-167) and warm start (lsqr_solve, :33-127).
+// Each right-hand side keeps its own scalars and stopping test; the matrix
+// products of all of them are computed in one pass over A per sweep:
+//   sweep 1  Y = A V + gamma Y        (one warp per 4 rows, V staged in smem)
+//   sweep 2  Z = A^T Y                (one thread per 4 columns, row groups
+//                                      reduced in a fixed order -> bitwise
+//                                      reproducible)
+// Vector norms are reduced from per-CTA partials in index order in FP64.
+#include "agb_lsqr.cuh"
+#include <cstdio>
+#include <cstring>
+#include <algorithm>
+
+namespace agb {
+
+#define CK(x)                                                                    \
+  do {                                                                           \
+    cudaError_t e_ = (x);                                                        \
+    if (e_ != cudaSuccess) {                                                     \
+      err = std::string(#x) + ": " + cudaGetErrorString(e_);                     \
+      return false;                                                              \
+    }                                                                            \
+  } while (0)
+
+constexpr int K8 = AGB_MAX_RHS;
+constexpr int kThreads = 256;
+
+template <typename T> struct Vec;
+template <> struct Vec<float> { using V = float4; static constexpr int N = 4; };
+template <> struct Vec<double> { using V = double2; static constexpr int N = 2; };
+
+template <typename T>
+__device__ __forceinline__ void unpack(const typename Vec<T>::V& v, T* o);
+template <>
+__device__ __forceinline__ void unpack<float>(const float4& v, float* o) { o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w; }
+template <>
+__device__ __forceinline__ void unpack<double>(const double2& v, double* o) { o[0] = v.x; o[1] = v.y; }
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Sweep 1: Y[r][c] = s1 * (A Vin)[r][c] + g_c * Yold[r][c]
+//   AccT: accumulation type inside a 1024-column chunk (T), chunk sums added
+//   in FP64.  VT: type of the staged V (T, or double for the FP64-accumulated
+//   refinement residual).  Writes Y (FP64), Ys (T copy) and per-CTA partial
+//   sums of Y^2 (part[blockIdx.x][c]).
+// ---------------------------------------------------------------------------
+constexpr int AV_RR = 4;                 // rows per warp
+constexpr int AV_ROWS = AV_RR * (kThreads / 32);
+
+template <typename T, typename VT>
+__global__ void __launch_bounds__(kThreads) k_av(const T* __restrict__ A, int64_t lda, int m, int ncols,
+                                                  const VT* __restrict__ Vin, double s1, const LsqrScalars* sc,
+                                                  int use_gamma, const double* __restrict__ Yold, double* __restrict__ Y,
+                                                  T* __restrict__ Ys, double* __restrict__ part) {
+  using AccT = typename std::conditional<std::is_same<VT, double>::value, double, T>::type;
+  constexpr int VN = Vec<T>::N;
+  constexpr int CH = 4096 / sizeof(VT);  // columns per smem chunk (32 KB of V)
+  __shared__ __align__(16) VT sV[CH * K8];
+  __shared__ double sPart[kThreads / 32][K8];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row0 = blockIdx.x * AV_ROWS + warp * AV_RR;
+  double acc[AV_RR][K8];
+#pragma unroll
+  for (int r = 0; r < AV_RR; ++r)
+#pragma unroll
+    for (int c = 0; c < K8; ++c) acc[r][c] = 0.0;
+
+  for (int64_t j0 = 0; j0 < lda; j0 += CH) {
+    const int cw = (int)((lda - j0) < (int64_t)CH ? (lda - j0) : (int64_t)CH);
+    __syncthreads();
+    for (int t = threadIdx.x; t < cw * K8; t += kThreads) sV[t] = Vin[j0 * K8 + t];
+    __syncthreads();
+    AccT part_acc[AV_RR][K8];
+#pragma unroll
+    for (int r = 0; r < AV_RR; ++r)
+#pragma unroll
+      for (int c = 0; c < K8; ++c) part_acc[r][c] = AccT(0);
+    for (int jj = lane * VN; jj < cw; jj += 32 * VN) {
+      T a[AV_RR][VN];
+#pragma unroll
+      for (int r = 0; r < AV_RR; ++r) {
+        const int row = row0 + r;
+        if (row < m) {
+          typename Vec<T>::V v = *reinterpret_cast<const typename Vec<T>::V*>(A + (int64_t)row * lda + j0 + jj);
+          unpack<T>(v, a[r]);
+        } else {
+#pragma unroll
+          for (int q = 0; q < VN; ++q) a[r][q] = T(0);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < VN; ++q) {
+        VT vv[K8];
+#pragma unroll
+        for (int c = 0; c < K8; ++c) vv[c] = sV[(jj + q) * K8 + c];
+#pragma unroll
+        for (int r = 0; r < AV_RR; ++r)
+#pragma unroll
+          for (int c = 0; c < K8; ++c) part_acc[r][c] += (AccT)a[r][q] * (AccT)vv[c];
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < AV_RR; ++r)
+#pragma unroll
+      for (int c = 0; c < K8; ++c) acc[r][c] += (double)part_acc[r][c];
+  }
+  // lane c finalises column c of each row (no lane reads what another writes)
+  double ssq = 0.0;
+#pragma unroll
+  for (int r = 0; r < AV_RR; ++r) {
+    const int row = row0 + r;
+#pragma unroll
+    for (int c = 0; c < K8; ++c) {
+      double s = warp_sum(acc[r][c]);
+      if (row < m && lane == c) {
+        double g = use_gamma ? sc[c].gamma : 1.0;
+        double y = s1 * s + (Yold ? g * Yold[(int64_t)row * K8 + c] : 0.0);
+        Y[(int64_t)row * K8 + c] = y;
+        Ys[(int64_t)row * K8 + c] = (T)y;
+        ssq += y * y;
+      }
+    }
+  }
+  if (lane < K8) sPart[warp][lane] = ssq;
+  __syncthreads();
+  if (threadIdx.x < K8) {
+    double s = 0.0;
+    for (int w = 0; w < kThreads / 32; ++w) s += sPart[w][threadIdx.x];
+    part[(int64_t)blockIdx.x * K8 + threadIdx.x] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Sweep 2: Zp[g][j][c] = sum_{r in group g} A[r][j] Us[r][c]
+// Each thread owns VN consecutive columns; rows of the group are streamed with
+// U staged in smem 256 rows at a time (T accumulation per chunk, FP64 across
+// chunks).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_atu(const T* __restrict__ A, int64_t lda, int m, const T* __restrict__ Us,
+                                                   int rows_per_group, double* __restrict__ Zp) {
+  constexpr int VN = Vec<T>::N;
+  constexpr int RCH = 256;
+  __shared__ __align__(16) T sU[RCH * K8];
+  const int64_t col = ((int64_t)blockIdx.x * kThreads + threadIdx.x) * VN;
+  const int g = blockIdx.y;
+  const int r0 = g * rows_per_group, r1 = min(m, r0 + rows_per_group);
+  double acc[VN][K8];
+#pragma unroll
+  for (int q = 0; q < VN; ++q)
+#pragma unroll
+    for (int c = 0; c < K8; ++c) acc[q][c] = 0.0;
+  for (int rb = r0; rb < r1; rb += RCH) {
+    const int nr = min(RCH, r1 - rb);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nr * K8; t += kThreads) sU[t] = Us[(int64_t)rb * K8 + t];
+    __syncthreads();
+    if (col < lda) {
+      T pa[VN][K8];
+#pragma unroll
+      for (int q = 0; q < VN; ++q)
+#pragma unroll
+        for (int c = 0; c < K8; ++c) pa[q][c] = T(0);
+      const T* ap = A + (int64_t)rb * lda + col;
+#pragma unroll 4
+      for (int r = 0; r < nr; ++r) {
+        typename Vec<T>::V v = *reinterpret_cast<const typename Vec<T>::V*>(ap + (int64_t)r * lda);
+        T a[VN];
+        unpack<T>(v, a);
+        const T* u = sU + r * K8;
+#pragma unroll
+        for (int q = 0; q < VN; ++q)
+#pragma unroll
+          for (int c = 0; c < K8; ++c) pa[q][c] += a[q] * u[c];
+      }
+#pragma unroll
+      for (int q = 0; q < VN; ++q)
+#pragma unroll
+        for (int c = 0; c < K8; ++c) acc[q][c] += (double)pa[q][c];
+    }
+  }
+  if (col < lda) {
+#pragma unroll
+    for (int q = 0; q < VN; ++q)
+#pragma unroll
+      for (int c = 0; c < K8; ++c) Zp[((int64_t)g * lda + col + q) * K8 + c] = acc[q][c];
+  }
+}
+
+// V <- Z/beta - beta V (Z = sum of group partials, in order); partial ||V||^2.
+// On the initial call (init=1) the old V is taken as zero.
+__global__ void k_atu_reduce(const double* __restrict__ Zp, int groups, int64_t lda, int n, const LsqrScalars* sc,
+                             int init, double* __restrict__ V, double* __restrict__ part) {
+  __shared__ double sP[kThreads / 32][K8];
+  const int64_t t = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  const int64_t j = t / K8;
+  const int c = (int)(t % K8);
+  double vn = 0.0;
+  if (j < n) {
+    double z = 0.0;
+    for (int g = 0; g < groups; ++g) z += Zp[((int64_t)g * lda + j) * K8 + c];
+    const double beta = sc[c].beta;
+    if (sc[c].active && beta > 0.0) {
+      vn = z / beta - (init ? 0.0 : beta * V[j * K8 + c]);
+      V[j * K8 + c] = vn;
+    } else {
+      vn = V[j * K8 + c];
+      if (!sc[c].active) vn = 0.0;
+    }
+  }
+  // reduce vn^2 per c: lanes with equal c are 8 apart
+  double s = vn * vn;
+  s += __shfl_xor_sync(0xffffffffu, s, 8);
+  s += __shfl_xor_sync(0xffffffffu, s, 16);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane < K8) sP[warp][lane] = s;
+  __syncthreads();
+  if (threadIdx.x < K8) {
+    double a = 0.0;
+    for (int w = 0; w < kThreads / 32; ++w) a += sP[w][threadIdx.x];
+    part[(int64_t)blockIdx.x * K8 + threadIdx.x] = a;
+  }
+}
+
+// Vector update of one iteration: V <- V/alpha; X += t1 W; W <- t2 W + V;
+// dknorm partial += (t3 W_old)^2; Vs = (T)V.  init=1: W <- V, X <- 0.
+template <typename T>
+__global__ void k_update(int n, int64_t lda, const LsqrScalars* sc, int init, double* __restrict__ V,
+                         double* __restrict__ W, double* __restrict__ X, T* __restrict__ Vs, double* __restrict__ part) {
+  __shared__ double sP[kThreads / 32][K8];
+  const int64_t t = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  const int64_t j = t / K8;
+  const int c = (int)(t % K8);
+  double dk = 0.0;
+  if (j < lda) {
+    const int64_t id = j * K8 + c;
+    if (j >= n) {
+      V[id] = 0.0; W[id] = 0.0; X[id] = 0.0; Vs[id] = T(0);
+    } else {
+      if (sc[c].active) {
+        double v = V[id];
+        if (sc[c].alpha > 0.0) v = v / sc[c].alpha;
+        V[id] = v;
+        if (init) {
+          W[id] = v;
+          X[id] = 0.0;
+        } else {
+          double w = W[id];
+          X[id] = sc[c].t1 * w + X[id];
+          W[id] = sc[c].t2 * w + v;
+          double q = sc[c].t3 * w;
+          dk = q * q;
+        }
+      } else if (init) {
+        W[id] = 0.0; X[id] = 0.0;
+      }
+      Vs[id] = (T)V[id];
+    }
+  }
+  double s = dk;
+  s += __shfl_xor_sync(0xffffffffu, s, 8);
+  s += __shfl_xor_sync(0xffffffffu, s, 16);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane < K8) sP[warp][lane] = s;
+  __syncthreads();
+  if (threadIdx.x < K8) {
+    double a = 0.0;
+    for (int w = 0; w < kThreads / 32; ++w) a += sP[w][threadIdx.x];
+    part[(int64_t)blockIdx.x * K8 + threadIdx.x] = a;
+  }
+}
+
+__device__ double d2norm(double a, double b) {
+  double scale = fabs(a) + fabs(b);
+  if (scale == 0.0) return 0.0;
+  return scale * sqrt((a / scale) * (a / scale) + (b / scale) * (b / scale));
+}
+__device__ double sum_part(const double* part, int nb, int c) {
+  double s = 0.0;
+  for (int b = 0; b < nb; ++b) s += part[b * K8 + c];
+  return s;
+}
+
+// Scalar phases (one thread per right-hand side).
+// phase 0: beta0 = ||r||; bnorm.       phase 1: alpha0; init recurrences.
+// phase 2: beta = ||Y|| after sweep 1; anorm.
+// phase 3: alpha after sweep 2; plane rotations; t1,t2,t3; gamma for next sweep.
+// phase 4: after the x/w update: dnorm, xnorm, residual estimates, stopping tests.
+__global__ void k_scalars(LsqrScalars* sc, int k, int phase, const double* part, int nb, int* nactive) {
+  const int c = threadIdx.x;
+  if (c >= K8) return;
+  LsqrScalars& s = sc[c];
+  if (c >= k) { s.active = 0; return; }
+  if (phase == 0) {
+    s.beta = sqrt(sum_part(part, nb, c));
+    return;
+  }
+  if (!s.active) return;
+  if (phase == 1) {
+    s.alpha = sqrt(sum_part(part, nb, c));
+    if (s.beta <= 0.0) s.alpha = 0.0;
+    s.rhobar = s.alpha;
+    s.phibar = s.beta;
+    s.bnorm = s.beta;
+    s.rnorm = s.beta;
+    s.arnorm = s.alpha * s.beta;
+    s.anorm = s.acond = s.dnorm = s.dxmax = s.res2 = s.xnorm = s.xnorm1 = s.z = s.sn2 = 0.0;
+    s.cs2 = -1.0;
+    s.itn = 0;
+    s.istop = 0;
+    s.gamma = (s.beta > 0.0) ? -s.alpha / s.beta : 0.0;
+    if (s.arnorm == 0.0) s.active = 0;  // lsqr: GOTO 800 with istop = 0
+    return;
+  }
+  if (phase == 2) {
+    s.itn += 1;
+    s.beta = sqrt(sum_part(part, nb, c));
+    double temp = d2norm(s.alpha, s.beta);
+    temp = d2norm(temp, 0.0);
+    s.anorm = d2norm(s.anorm, temp);
+    return;
+  }
+  if (phase == 3) {
+    if (s.beta > 0.0) {
+      s.alpha = sqrt(sum_part(part, nb, c));
+    }
+    double rhbar1 = s.rhobar;
+    double rho = d2norm(rhbar1, s.beta);
+    double cs = rhbar1 / rho, sn = s.beta / rho;
+    double theta = sn * s.alpha;
+    s.rhobar = -cs * s.alpha;
+    double phi = cs * s.phibar;
+    s.phibar = sn * s.phibar;
+    double tau = sn * phi;
+    s.t1 = phi / rho;
+    s.t2 = -theta / rho;
+    s.t3 = 1.0 / rho;
+    // second rotation and norm estimates (depend only on scalars)
+    double delta = s.sn2 * rho, gambar = -s.cs2 * rho;
+    double rhs = phi - delta * s.z;
+    double zbar = rhs / gambar;
+    s.xnorm = d2norm(s.xnorm1, zbar);
+    double gamma = d2norm(gambar, theta);
+    s.cs2 = gambar / gamma;
+    s.sn2 = theta / gamma;
+    s.z = rhs / gamma;
+    s.xnorm1 = d2norm(s.xnorm1, s.z);
+    s.res2 = d2norm(s.res2, 0.0);
+    s.rnorm = d2norm(s.res2, s.phibar);
+    s.arnorm = s.alpha * fabs(tau);
+    // stash phi for the dxk monitor
+    s.dxmax = fmax(s.dxmax, 0.0);
+    s.acond = phi;  // temporary (phi), replaced in phase 4
+    return;
+  }
+  if (phase == 4) {
+    const double phi = s.acond;
+    double dknorm = sqrt(sum_part(part, nb, c));
+    s.dnorm = d2norm(s.dnorm, dknorm);
+    double dxk = fabs(phi * dknorm);
+    if (s.dxmax < dxk) s.dxmax = dxk;
+    s.acond = s.anorm * s.dnorm;
+    const double one = 1.0, zero = 0.0;
+    double test1 = s.rnorm / s.bnorm;
+    double test2 = zero;
+    if (s.rnorm > zero) test2 = s.arnorm / (s.anorm * s.rnorm);
+    double test3 = one / s.acond;
+    double t1 = test1 / (one + s.anorm * s.xnorm / s.bnorm);
+    double rtol = s.btol + s.atol * s.anorm * s.xnorm / s.bnorm;
+    double t3 = one + test3, t2 = one + test2;
+    t1 = one + t1;
+    int istop = 0;
+    if (s.itn >= s.itnlim) istop = 5;
+    if (t3 <= one) istop = 4;
+    if (t2 <= one) istop = 2;
+    if (t1 <= one) istop = 1;
+    if (test3 <= s.ctol) istop = 4;
+    if (test2 <= s.atol) istop = 2;
+    if (test1 <= rtol) istop = 1;
+    s.istop = istop;
+    if (istop != 0) s.active = 0;
+    s.gamma = (s.beta > 0.0) ? -s.alpha / s.beta : 0.0;
+    if (s.beta <= 0.0) s.active = 0;
+    if (s.active) atomicAdd(nactive, 1);
+  }
+}
+
+
+// ---------------------------------------------------------------------------
+// Column scaling (lsqr_precon): partial column sums of squares per row group,
+// then q_j = 1/sqrt(sum) and A <- A diag(q).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_colsq(const T* __restrict__ A, int64_t lda, int m, int rows_per_group, double* __restrict__ P) {
+  constexpr int VN = Vec<T>::N;
+  const int64_t col = ((int64_t)blockIdx.x * kThreads + threadIdx.x) * VN;
+  const int g = blockIdx.y;
+  const int r0 = g * rows_per_group, r1 = min(m, r0 + rows_per_group);
+  if (col >= lda) return;
+  double acc[VN];
+#pragma unroll
+  for (int q = 0; q < VN; ++q) acc[q] = 0.0;
+  for (int r = r0; r < r1; ++r) {
+    typename Vec<T>::V v = *reinterpret_cast<const typename Vec<T>::V*>(A + (int64_t)r * lda + col);
+    T a[VN];
+    unpack<T>(v, a);
+#pragma unroll
+    for (int q = 0; q < VN; ++q) acc[q] += (double)a[q] * (double)a[q];
+  }
+#pragma unroll
+  for (int q = 0; q < VN; ++q) P[(int64_t)g * lda + col + q] = acc[q];
+}
+__global__ void k_colsq_finish(const double* __restrict__ P, int groups, int64_t lda, int n, double* __restrict__ q) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= lda) return;
+  double s = 0.0;
+  for (int g = 0; g < groups; ++g) s += P[(int64_t)g * lda + j];
+  q[j] = (j < n) ? 1.0 / sqrt(s) : 0.0;
+}
+template <typename T>
+__global__ void k_scale_cols(T* __restrict__ A, int64_t lda, int m, const double* __restrict__ q) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t tot = (int64_t)m * lda;
+  for (int64_t i = idx; i < tot; i += (int64_t)gridDim.x * blockDim.x) A[i] = (T)((double)A[i] * q[i % lda]);
+}
+
+// Pack column-major (rows x k) into [rows_pad][8] (zero padding); optional
+// element-wise divide by d (x/q warm start).
+__global__ void k_pack(const double* __restrict__ src, int rows, int k, int64_t rows_pad, const double* __restrict__ d,
+                       double* __restrict__ dst) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= rows_pad * K8) return;
+  const int64_t r = t / K8;
+  const int c = (int)(t % K8);
+  double v = 0.0;
+  if (r < rows && c < k) {
+    v = src[(int64_t)c * rows + r];
+    if (d) v = v / d[r];
+  }
+  dst[t] = v;
+}
+// x_out(:,c) = q .* X(:,c) + x0(:,c)
+__global__ void k_finish_x(const double* __restrict__ X, const double* __restrict__ q, const double* __restrict__ X0,
+                           int n, int k, const LsqrScalars* sc, double* __restrict__ xout) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n * k) return;
+  const int c = (int)(t / n);
+  const int64_t j = t % n;
+  xout[(int64_t)c * n + j] = q[j] * X[j * K8 + c] + X0[j * K8 + c];
+}
+__global__ void k_sumsq_rows(const double* __restrict__ B, int rows, double* __restrict__ part) {
+  __shared__ double sP[kThreads / 32][K8];
+  const int64_t t = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  double v = (t < (int64_t)rows * K8) ? B[t] : 0.0;
+  double s = v * v;
+  s += __shfl_xor_sync(0xffffffffu, s, 8);
+  s += __shfl_xor_sync(0xffffffffu, s, 16);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane < K8) sP[warp][lane] = s;
+  __syncthreads();
+  if (threadIdx.x < K8) {
+    double a = 0.0;
+    for (int w = 0; w < kThreads / 32; ++w) a += sP[w][threadIdx.x];
+    part[(int64_t)blockIdx.x * K8 + threadIdx.x] = a;
+  }
+}
+// tolerances of lsqr_solve: atol = eps, btol = eps*||b||/||r0||, conlim 1e8
+__global__ void k_setup_tol(LsqrScalars* sc, int k, const double* part_b, int nb_b, double eps, int itnlim) {
+  const int c = threadIdx.x;
+  if (c >= K8) return;
+  LsqrScalars& s = sc[c];
+  if (c >= k) { s.active = 0; return; }
+  const double nrm_b = sqrt(sum_part(part_b, nb_b, c));
+  s.atol = eps;
+  s.btol = eps * nrm_b / s.beta;
+  s.ctol = 1.0 / 1.0e8;
+  s.itnlim = itnlim;
+  s.active = (s.beta > 0.0) ? 1 : 0;
+  s.istop = 0;
+  s.itn = 0;
+  s.alpha = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Host driver
+// ---------------------------------------------------------------------------
+static inline unsigned cdiv(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
+
+void DenseLsqr::release() {
+  cudaFree(Y); cudaFree(V); cudaFree(W); cudaFree(X); cudaFree(Z); cudaFree(Ys); cudaFree(Vs);
+  cudaFree(part); cudaFree(Zp); cudaFree(sc); cudaFree(nactive);
+  if (h_nactive) cudaFreeHost(h_nactive);
+  Y = V = W = X = Z = nullptr; Ys = Vs = nullptr; part = Zp = nullptr; sc = nullptr; nactive = nullptr;
+  h_nactive = nullptr;
+}
+DenseLsqr::~DenseLsqr() { release(); }
+
+bool DenseLsqr::setup(const void* A_dev, bool is_fp32, int m_, int n_, int64_t lda_, int k_, cudaStream_t s) {
+  release();
+  A = A_dev; fp32 = is_fp32; m = m_; n = n_; lda = lda_; k = k_; stream = s;
+  if (k < 1 || k > K8) { err = "number of right-hand sides must be 1..8"; return false; }
+  if (lda % 32 != 0 || lda < n) { err = "lda must be a multiple of 32 and >= n"; return false; }
+  const size_t tsz = fp32 ? sizeof(float) : sizeof(double);
+  const int64_t mpad = ((int64_t)m + 255) / 256 * 256;
+  CK(cudaMalloc(&Y, mpad * K8 * sizeof(double)));
+  CK(cudaMalloc(&Ys, mpad * K8 * tsz));
+  CK(cudaMalloc(&V, lda * K8 * sizeof(double)));
+  CK(cudaMalloc(&W, lda * K8 * sizeof(double)));
+  CK(cudaMalloc(&X, lda * K8 * sizeof(double)));
+  CK(cudaMalloc(&Z, std::max<int64_t>(lda, mpad) * K8 * sizeof(double)));  // b / x0 staging
+  CK(cudaMalloc(&Vs, lda * K8 * sizeof(double)));                            // T copy, or FP64 for residual
+  // row groups for sweep 2: aim for >= 4 CTAs per SM
+  const int vn = fp32 ? 4 : 2;
+  const int colblocks = (int)cdiv(lda, kThreads * vn);
+  int groups = std::max(1, std::min((int)cdiv(m, 256), (int)cdiv(152 * 8, colblocks)));
+  zgroups = groups;
+  CK(cudaMalloc(&Zp, (int64_t)groups * lda * K8 * sizeof(double)));
+  const int64_t nbmax = std::max<int64_t>({(int64_t)cdiv(m, AV_ROWS), (int64_t)cdiv(lda * K8, kThreads),
+                                           (int64_t)cdiv(mpad * K8, kThreads)});
+  part_cap = (size_t)nbmax * K8 * 2;
+  CK(cudaMalloc(&part, part_cap * sizeof(double)));
+  CK(cudaMalloc(&sc, K8 * sizeof(LsqrScalars)));
+  CK(cudaMemsetAsync(sc, 0, K8 * sizeof(LsqrScalars), stream));
+  CK(cudaMalloc(&nactive, sizeof(int)));
+  CK(cudaMallocHost(&h_nactive, sizeof(int)));
+  CK(cudaMemsetAsync(Vs, 0, lda * K8 * sizeof(double), stream));
+  CK(cudaMemsetAsync(Y, 0, mpad * K8 * sizeof(double), stream));
+  CK(cudaMemsetAsync(Ys, 0, mpad * K8 * tsz, stream));
+  CK(cudaMemsetAsync(V, 0, lda * K8 * sizeof(double), stream));
+  CK(cudaMemsetAsync(W, 0, lda * K8 * sizeof(double), stream));
+  CK(cudaMemsetAsync(X, 0, lda * K8 * sizeof(double), stream));
+  return true;
+}
+
+bool DenseLsqr::precon(void* A_dev, double* q_dev) {
+  const int vn = fp32 ? 4 : 2;
+  dim3 g(cdiv(lda, kThreads * vn), zgroups);
+  const int rpg = (int)cdiv(m, zgroups);
+  if (fp32) k_colsq<float><<<g, kThreads, 0, stream>>>((const float*)A_dev, lda, m, rpg, Zp);
+  else k_colsq<double><<<g, kThreads, 0, stream>>>((const double*)A_dev, lda, m, rpg, Zp);
+  k_colsq_finish<<<cdiv(lda, 256), 256, 0, stream>>>(Zp, zgroups, lda, n, q_dev);
+  const int64_t tot = (int64_t)m * lda;
+  unsigned blocks = (unsigned)std::min<int64_t>(cdiv(tot, 256), 152 * 64);
+  if (fp32) k_scale_cols<float><<<blocks, 256, 0, stream>>>((float*)A_dev, lda, m, q_dev);
+  else k_scale_cols<double><<<blocks, 256, 0, stream>>>((double*)A_dev, lda, m, q_dev);
+  CK(cudaGetLastError());
+  return true;
+}
+
+template <typename T>
+static void launch_av(const DenseLsqr& L, const void* Vin, bool vin_fp64, double s1, int use_gamma,
+                      const double* Yold) {
+  const unsigned nb = cdiv(L.m, AV_ROWS);
+  if (vin_fp64)
+    k_av<T, double><<<nb, kThreads, 0, L.stream>>>((const T*)L.A, L.lda, L.m, L.n, (const double*)Vin, s1, L.sc,
+                                                   use_gamma, Yold, L.Y, (T*)L.Ys, L.part);
+  else
+    k_av<T, T><<<nb, kThreads, 0, L.stream>>>((const T*)L.A, L.lda, L.m, L.n, (const T*)Vin, s1, L.sc, use_gamma,
+                                              Yold, L.Y, (T*)L.Ys, L.part);
+}
+template <typename T>
+static void launch_atu(const DenseLsqr& L) {
+  constexpr int vn = Vec<T>::N;
+  dim3 g(cdiv(L.lda, kThreads * vn), L.zgroups);
+  const int rpg = (int)((cdiv(L.m, L.zgroups) + 255) / 256 * 256);
+  k_atu<T><<<g, kThreads, 0, L.stream>>>((const T*)L.A, L.lda, L.m, (const T*)L.Ys, rpg, L.Zp);
+}
+
+bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, double eps, int maxit, int* nit_host,
+                      int* istop_host, double* rnorm_host, int check_every) {
+  if (maxit == 0) maxit = 10 * (m + n + 50);
+  const int64_t mpad = ((int64_t)m + 255) / 256 * 256;
+  const unsigned nb_av = cdiv(m, AV_ROWS);
+  const unsigned nb_red = cdiv((int64_t)n * K8, kThreads);
+  const unsigned nb_upd = cdiv(lda * K8, kThreads);
+  // stage: b -> Z (as [m][8]); x0 -> X0 buffer (as [n][8]); xs = x0/q -> Vs (FP64)
+  double* Bp = Z;
+  k_pack<<<cdiv(mpad * K8, 256), 256, 0, stream>>>(b_dev, m, k, mpad, nullptr, Bp);
+  k_sumsq_rows<<<cdiv(mpad * K8, kThreads), kThreads, 0, stream>>>(Bp, (int)mpad, part);
+  const int nb_b = (int)cdiv(mpad * K8, kThreads);
+  // ||b|| partials are consumed right after the residual is known; keep them
+  // in the upper half of `part`
+  double* part_b = part + (part_cap / 2);
+  if ((size_t)nb_b * K8 > part_cap / 2) { err = "partial buffer too small"; return false; }
+  CK(cudaMemcpyAsync(part_b, part, (size_t)nb_b * K8 * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+  k_pack<<<cdiv(lda * K8, 256), 256, 0, stream>>>(x_dev, n, k, lda, q_dev, (double*)Vs);
+  // residual Y = b - A (x0/q), FP64 accumulation
+  if (fp32) launch_av<float>(*this, Vs, true, -1.0, 0, Bp);
+  else launch_av<double>(*this, Vs, true, -1.0, 0, Bp);
+  k_scalars<<<1, 32, 0, stream>>>(sc, k, 0, part, nb_av, nactive);
+  k_setup_tol<<<1, 32, 0, stream>>>(sc, k, part_b, nb_b, eps, maxit);
+  // keep x0 (packed) for the final update: in X0 = W (W is rewritten by the init update,
+  // so copy x0 to Bp region first: Bp is no longer needed)
+  k_pack<<<cdiv(lda * K8, 256), 256, 0, stream>>>(x_dev, n, k, lda, nullptr, Bp);
+  // A^T r, alpha0, w = v
+  if (fp32) launch_atu<float>(*this); else launch_atu<double>(*this);
+  k_atu_reduce<<<nb_red, kThreads, 0, stream>>>(Zp, zgroups, lda, n, sc, 1, V, part);
+  k_scalars<<<1, 32, 0, stream>>>(sc, k, 1, part, nb_red, nactive);
+  if (fp32) k_update<float><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 1, V, W, X, (float*)Vs, part);
+  else k_update<double><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 1, V, W, X, (double*)Vs, part);
+  CK(cudaGetLastError());
+
+  auto iteration = [&]() {
+    if (fp32) launch_av<float>(*this, Vs, false, 1.0, 1, Y);
+    else launch_av<double>(*this, Vs, false, 1.0, 1, Y);
+    k_scalars<<<1, 32, 0, stream>>>(sc, k, 2, part, nb_av, nactive);
+    if (fp32) launch_atu<float>(*this); else launch_atu<double>(*this);
+    k_atu_reduce<<<nb_red, kThreads, 0, stream>>>(Zp, zgroups, lda, n, sc, 0, V, part);
+    k_scalars<<<1, 32, 0, stream>>>(sc, k, 3, part, nb_red, nactive);
+    if (fp32) k_update<float><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 0, V, W, X, (float*)Vs, part);
+    else k_update<double><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 0, V, W, X, (double*)Vs, part);
+    cudaMemsetAsync(nactive, 0, sizeof(int), stream);
+    k_scalars<<<1, 32, 0, stream>>>(sc, k, 4, part, nb_upd, nactive);
+  };
+  // capture check_every iterations in one graph
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+  for (int i = 0; i < check_every; ++i) iteration();
+  CK(cudaStreamEndCapture(stream, &graph));
+  CK(cudaGraphInstantiate(&gexec, graph, 0));
+  // initial activity
+  LsqrScalars hs[K8];
+  CK(cudaMemcpyAsync(hs, sc, sizeof(hs), cudaMemcpyDeviceToHost, stream));
+  CK(cudaStreamSynchronize(stream));
+  int act = 0;
+  for (int c = 0; c < k; ++c) act += hs[c].active;
+  int iters = 0;
+  while (act > 0 && iters < maxit + check_every) {
+    CK(cudaGraphLaunch(gexec, stream));
+    CK(cudaMemcpyAsync(h_nactive, nactive, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    iters += check_every;
+    act = *h_nactive;
+  }
+  cudaGraphExecDestroy(gexec);
+  cudaGraphDestroy(graph);
+  // x = q .* dx + x0
+  k_finish_x<<<cdiv((int64_t)n * k, 256), 256, 0, stream>>>(X, q_dev, Bp, n, k, sc, x_dev);
+  CK(cudaMemcpyAsync(hs, sc, sizeof(hs), cudaMemcpyDeviceToHost, stream));
+  CK(cudaStreamSynchronize(stream));
+  CK(cudaGetLastError());
+  for (int c = 0; c < k; ++c) {
+    if (nit_host) nit_host[c] = hs[c].itn;
+    if (istop_host) istop_host[c] = hs[c].istop;
+    if (rnorm_host) rnorm_host[c] = hs[c].rnorm;
+  }
+  return true;
+}
+
+bool DenseLsqr::residual(const double* b_dev, const double* x_dev, const double* q_dev, double* r_dev) {
+  const int64_t mpad = ((int64_t)m + 255) / 256 * 256;
+  k_pack<<<cdiv(mpad * K8, 256), 256, 0, stream>>>(b_dev, m, k, mpad, nullptr, Z);
+  k_pack<<<cdiv(lda * K8, 256), 256, 0, stream>>>(x_dev, n, k, lda, q_dev, (double*)Vs);
+  if (fp32) launch_av<float>(*this, Vs, true, -1.0, 0, Z);
+  else launch_av<double>(*this, Vs, true, -1.0, 0, Z);
+  // unpack Y -> r (column-major)
+  for (int c = 0; c < k; ++c)
+    CK(cudaMemcpy2DAsync(r_dev + (int64_t)c * m, sizeof(double), Y + c, K8 * sizeof(double), sizeof(double), m,
+                         cudaMemcpyDeviceToDevice, stream));
+  CK(cudaGetLastError());
+  return true;
+}
+
+
+// ---------------------------------------------------------------------------
+// CRS LSQR (the lsqr_precon / lsqr_solve drop-ins).  1-based CRS as the
+// reference passes it.  The transpose is built on the device by a stable sort
+// of the column indices, so both products -- and the column norms of the
+// preconditioner -- sum their terms in the reference's order.
+// ---------------------------------------------------------------------------
+}  // namespace agb
+#include <cub/device/device_radix_sort.cuh>
+namespace agb {
+
+__global__ void k_iota_cols(int64_t nnz, const int* __restrict__ ja, int* __restrict__ key, int64_t* __restrict__ val) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nnz) return;
+  key[t] = ja[t] - 1;
+  val[t] = t;
+}
+__global__ void k_row_of(int m, const int64_t* __restrict__ ia, int* __restrict__ rowof) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= m) return;
+  for (int64_t t = ia[r] - 1; t < ia[r + 1] - 1; ++t) rowof[t] = r;
+}
+__global__ void k_colptr(int64_t nnz, int n, const int* __restrict__ skey, int64_t* __restrict__ cp) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t > nnz) return;
+  const int prev = (t == 0) ? -1 : skey[t - 1];
+  const int cur = (t == nnz) ? n : skey[t];
+  for (int c = prev + 1; c <= cur; ++c) cp[c] = t;
+}
+// y = s1 * A x + g y_old (warp per row); x, y in the [.][8] layout, column 0
+__global__ void k_csr_av(int m, const int64_t* __restrict__ ia, const int* __restrict__ ja, const double* __restrict__ a,
+                         const double* __restrict__ x, double s1, const LsqrScalars* sc, int use_gamma,
+                         const double* __restrict__ yold, double* __restrict__ Y, double* __restrict__ Ys,
+                         double* __restrict__ part) {
+  __shared__ double sP[kThreads / 32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = blockIdx.x * (kThreads / 32) + warp;
+  double ssq = 0.0;
+  if (r < m) {
+    double s = 0.0;
+    for (int64_t t = ia[r] - 1 + lane; t < ia[r + 1] - 1; t += 32) s += a[t] * x[(int64_t)(ja[t] - 1) * K8];
+    s = warp_sum(s);
+    const double g = use_gamma ? sc[0].gamma : 1.0;
+    const double y = s1 * s + (yold ? g * yold[(int64_t)r * K8] : 0.0);
+    if (lane == 0) {
+      Y[(int64_t)r * K8] = y;
+      Ys[(int64_t)r * K8] = y;
+    }
+    ssq = y * y;
+  }
+  if (lane == 0) sP[warp] = ssq;
+  __syncthreads();
+  if (threadIdx.x < K8) {
+    double acc = 0.0;
+    if (threadIdx.x == 0)
+      for (int w = 0; w < kThreads / 32; ++w) acc += sP[w];
+    part[(int64_t)blockIdx.x * K8 + threadIdx.x] = acc;
+  }
+}
+// Z(:,0) = A^T y via the transpose (CSC, rows ascending)
+__global__ void k_csc_atu(int n, const int64_t* __restrict__ cp, const int* __restrict__ rows,
+                          const double* __restrict__ av, const double* __restrict__ Ys, double* __restrict__ Zp) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  double s = 0.0;
+  for (int64_t t = cp[warp] + lane; t < cp[warp + 1]; t += 32) s += av[t] * Ys[(int64_t)rows[t] * K8];
+  s = warp_sum(s);
+  if (lane < K8) Zp[(int64_t)warp * K8 + lane] = (lane == 0) ? s : 0.0;
+}
+// column sums of squares in row order, q = 1/sqrt
+__global__ void k_csc_colnorm(int n, const int64_t* __restrict__ cp, const double* __restrict__ av,
+                              double* __restrict__ q) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  double s = 0.0;
+  for (int64_t t = cp[j]; t < cp[j + 1]; ++t) s += av[t] * av[t];
+  q[j] = 1.0 / sqrt(s);
+}
+__global__ void k_crs_scale(int64_t nnz, const int* __restrict__ ja, const double* __restrict__ q, double* __restrict__ a) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nnz) a[t] *= q[ja[t] - 1];
+}
+__global__ void k_gather(int64_t nnz, const int64_t* __restrict__ perm, const double* __restrict__ a,
+                         const int* __restrict__ rowof, double* __restrict__ av, int* __restrict__ rows) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nnz) return;
+  av[t] = a[perm[t]];
+  rows[t] = rowof[perm[t]];
+}
+
+struct CrsDev {
+  int m = 0, n = 0;
+  int64_t nnz = 0;
+  int64_t* ia = nullptr;
+  int* ja = nullptr;
+  double* a = nullptr;
+  int64_t* cp = nullptr;   // n+1
+  int64_t* perm = nullptr;
+  int* rows = nullptr;     // CSC row index per entry
+  double* av = nullptr;    // CSC values
+  std::string err;
+  ~CrsDev() {
+    cudaFree(ia); cudaFree(ja); cudaFree(a); cudaFree(cp); cudaFree(perm); cudaFree(rows); cudaFree(av);
+  }
+  bool upload(int m_, int n_, int64_t nnz_, const int64_t* ia_h, const int* ja_h, const double* a_h, cudaStream_t s) {
+    m = m_; n = n_; nnz = nnz_;
+    CK(cudaMalloc(&ia, (m + 1) * sizeof(int64_t)));
+    CK(cudaMalloc(&ja, std::max<int64_t>(nnz, 1) * sizeof(int)));
+    CK(cudaMalloc(&a, std::max<int64_t>(nnz, 1) * sizeof(double)));
+    CK(cudaMemcpyAsync(ia, ia_h, (m + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ja, ja_h, nnz * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(a, a_h, nnz * sizeof(double), cudaMemcpyHostToDevice, s));
+    return true;
+  }
+  // build the CSC structure (values gathered from the current a)
+  bool transpose(cudaStream_t s) {
+    int *key = nullptr, *skey = nullptr, *rowof = nullptr;
+    int64_t* val = nullptr;
+    CK(cudaMalloc(&key, std::max<int64_t>(nnz, 1) * sizeof(int)));
+    CK(cudaMalloc(&skey, std::max<int64_t>(nnz, 1) * sizeof(int)));
+    CK(cudaMalloc(&val, std::max<int64_t>(nnz, 1) * sizeof(int64_t)));
+    CK(cudaMalloc(&perm, std::max<int64_t>(nnz, 1) * sizeof(int64_t)));
+    CK(cudaMalloc(&rowof, std::max<int64_t>(nnz, 1) * sizeof(int)));
+    CK(cudaMalloc(&rows, std::max<int64_t>(nnz, 1) * sizeof(int)));
+    CK(cudaMalloc(&av, std::max<int64_t>(nnz, 1) * sizeof(double)));
+    CK(cudaMalloc(&cp, (n + 1) * sizeof(int64_t)));
+    k_iota_cols<<<cdiv(nnz, 256), 256, 0, s>>>(nnz, ja, key, val);
+    k_row_of<<<cdiv(m, 256), 256, 0, s>>>(m, ia, rowof);
+    size_t tmpb = 0;
+    int bits = 1;
+    while ((1 << bits) <= n && bits < 31) ++bits;
+    cub::DeviceRadixSort::SortPairs(nullptr, tmpb, key, skey, val, perm, nnz, 0, bits, s);
+    void* tmp = nullptr;
+    CK(cudaMalloc(&tmp, std::max<size_t>(tmpb, 1)));
+    CK(cub::DeviceRadixSort::SortPairs(tmp, tmpb, key, skey, val, perm, nnz, 0, bits, s));
+    k_colptr<<<cdiv(nnz + 1, 256), 256, 0, s>>>(nnz, n, skey, cp);
+    k_gather<<<cdiv(nnz, 256), 256, 0, s>>>(nnz, perm, a, rowof, av, rows);
+    CK(cudaStreamSynchronize(s));
+    cudaFree(tmp); cudaFree(key); cudaFree(skey); cudaFree(val); cudaFree(rowof);
+    CK(cudaGetLastError());
+    return true;
+  }
+};
+
+bool crs_lsqr_precon(int m, int n, int64_t nnz, double* q_h, const int64_t* ia_h, const int* ja_h, double* a_h,
+                     std::string& err) {
+  cudaStream_t s;
+  CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  {
+    CrsDev D;
+    if (!D.upload(m, n, nnz, ia_h, ja_h, a_h, s) || !D.transpose(s)) { err = D.err; cudaStreamDestroy(s); return false; }
+    double* q = nullptr;
+    CK(cudaMalloc(&q, std::max(n, 1) * sizeof(double)));
+    k_csc_colnorm<<<cdiv(n, 256), 256, 0, s>>>(n, D.cp, D.av, q);
+    k_crs_scale<<<cdiv(nnz, 256), 256, 0, s>>>(nnz, D.ja, q, D.a);
+    CK(cudaMemcpyAsync(q_h, q, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(a_h, D.a, nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    CK(cudaGetLastError());
+    cudaFree(q);
+  }
+  cudaStreamDestroy(s);
+  return true;
+}
+
+bool crs_lsqr_solve(int m, int n, int64_t nnz, int& maxit, double eps, int& nit, int& ierr, const double* q_h,
+                    const int64_t* ia_h, const int* ja_h, const double* a_h, const double* b_h, double* x_h,
+                    std::string& err) {
+  if (maxit == 0) maxit = 10 * (m + n + 50);
+  cudaStream_t s;
+  CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  CrsDev D;
+  if (!D.upload(m, n, nnz, ia_h, ja_h, a_h, s) || !D.transpose(s)) { err = D.err; cudaStreamDestroy(s); return false; }
+  const int64_t lda = ((int64_t)n + 31) / 32 * 32;
+  const int64_t mpad = ((int64_t)m + 255) / 256 * 256;
+  double *q, *b, *x, *Y, *Ys, *V, *W, *X, *Vs, *Bp, *X0, *Zp, *part;
+  LsqrScalars* sc;
+  int* nact;
+  CK(cudaMalloc(&q, lda * sizeof(double)));
+  CK(cudaMalloc(&b, std::max(m, 1) * sizeof(double)));
+  CK(cudaMalloc(&x, lda * sizeof(double)));
+  CK(cudaMalloc(&Y, mpad * K8 * sizeof(double)));
+  CK(cudaMalloc(&Ys, mpad * K8 * sizeof(double)));
+  CK(cudaMalloc(&Bp, mpad * K8 * sizeof(double)));
+  CK(cudaMalloc(&V, lda * K8 * sizeof(double)));
+  CK(cudaMalloc(&W, lda * K8 * sizeof(double)));
+  CK(cudaMalloc(&X, lda * K8 * sizeof(double)));
+  CK(cudaMalloc(&X0, lda * K8 * sizeof(double)));
+  CK(cudaMalloc(&Vs, lda * K8 * sizeof(double)));
+  CK(cudaMalloc(&Zp, lda * K8 * sizeof(double)));
+  const int64_t nbmax = std::max<int64_t>({(int64_t)cdiv(m, kThreads / 32), (int64_t)cdiv(lda * K8, kThreads),
+                                           (int64_t)cdiv(mpad * K8, kThreads)});
+  CK(cudaMalloc(&part, 2 * nbmax * K8 * sizeof(double)));
+  CK(cudaMalloc(&sc, K8 * sizeof(LsqrScalars)));
+  CK(cudaMalloc(&nact, sizeof(int)));
+  CK(cudaMemsetAsync(sc, 0, K8 * sizeof(LsqrScalars), s));
+  CK(cudaMemsetAsync(q, 0, lda * sizeof(double), s));
+  CK(cudaMemsetAsync(x, 0, lda * sizeof(double), s));
+  CK(cudaMemsetAsync(Ys, 0, mpad * K8 * sizeof(double), s));
+  CK(cudaMemsetAsync(Y, 0, mpad * K8 * sizeof(double), s));
+  CK(cudaMemsetAsync(V, 0, lda * K8 * sizeof(double), s));
+  CK(cudaMemsetAsync(W, 0, lda * K8 * sizeof(double), s));
+  CK(cudaMemsetAsync(X, 0, lda * K8 * sizeof(double), s));
+  CK(cudaMemcpyAsync(q, q_h, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b, b_h, m * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(x, x_h, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  const unsigned nb_av = cdiv(m, kThreads / 32);
+  const unsigned nb_red = cdiv((int64_t)n * K8, kThreads);
+  const unsigned nb_upd = cdiv(lda * K8, kThreads);
+  const int nb_b = (int)cdiv(mpad * K8, kThreads);
+  double* part_b = part + nbmax * K8;
+  k_pack<<<cdiv(mpad * K8, 256), 256, 0, s>>>(b, m, 1, mpad, nullptr, Bp);
+  k_sumsq_rows<<<nb_b, kThreads, 0, s>>>(Bp, (int)mpad, part_b);
+  k_pack<<<cdiv(lda * K8, 256), 256, 0, s>>>(x, n, 1, lda, q, Vs);
+  k_pack<<<cdiv(lda * K8, 256), 256, 0, s>>>(x, n, 1, lda, nullptr, X0);
+  k_csr_av<<<nb_av, kThreads, 0, s>>>(m, D.ia, D.ja, D.a, Vs, -1.0, sc, 0, Bp, Y, Ys, part);
+  k_scalars<<<1, 32, 0, s>>>(sc, 1, 0, part, nb_av, nact);
+  k_setup_tol<<<1, 32, 0, s>>>(sc, 1, part_b, nb_b, eps, maxit);
+  k_csc_atu<<<cdiv((int64_t)n * 32, kThreads), kThreads, 0, s>>>(n, D.cp, D.rows, D.av, Ys, Zp);
+  k_atu_reduce<<<nb_red, kThreads, 0, s>>>(Zp, 1, lda, n, sc, 1, V, part);
+  k_scalars<<<1, 32, 0, s>>>(sc, 1, 1, part, nb_red, nact);
+  k_update<double><<<nb_upd, kThreads, 0, s>>>(n, lda, sc, 1, V, W, X, Vs, part);
+  CK(cudaGetLastError());
+  LsqrScalars hs;
+  int act = 1;
+  CK(cudaMemcpyAsync(&hs, sc, sizeof(hs), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  act = hs.active;
+  const int chunk = 16;
+  cudaGraph_t graph;
+  cudaGraphExec_t gexec;
+  CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  for (int it = 0; it < chunk; ++it) {
+    k_csr_av<<<nb_av, kThreads, 0, s>>>(m, D.ia, D.ja, D.a, Vs, 1.0, sc, 1, Y, Y, Ys, part);
+    k_scalars<<<1, 32, 0, s>>>(sc, 1, 2, part, nb_av, nact);
+    k_csc_atu<<<cdiv((int64_t)n * 32, kThreads), kThreads, 0, s>>>(n, D.cp, D.rows, D.av, Ys, Zp);
+    k_atu_reduce<<<nb_red, kThreads, 0, s>>>(Zp, 1, lda, n, sc, 0, V, part);
+    k_scalars<<<1, 32, 0, s>>>(sc, 1, 3, part, nb_red, nact);
+    k_update<double><<<nb_upd, kThreads, 0, s>>>(n, lda, sc, 0, V, W, X, Vs, part);
+    cudaMemsetAsync(nact, 0, sizeof(int), s);
+    k_scalars<<<1, 32, 0, s>>>(sc, 1, 4, part, nb_upd, nact);
+  }
+  CK(cudaStreamEndCapture(s, &graph));
+  CK(cudaGraphInstantiate(&gexec, graph, 0));
+  int iters = 0;
+  while (act > 0 && iters < maxit + chunk) {
+    CK(cudaGraphLaunch(gexec, s));
+    CK(cudaMemcpyAsync(&act, nact, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    iters += chunk;
+  }
+  cudaGraphExecDestroy(gexec);
+  cudaGraphDestroy(graph);
+  k_finish_x<<<cdiv(n, 256), 256, 0, s>>>(X, q, X0, n, 1, sc, x);
+  CK(cudaMemcpyAsync(x_h, x, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&hs, sc, sizeof(hs), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  nit = hs.itn;
+  ierr = (hs.istop > 3) ? hs.istop : 0;
+  cudaFree(q); cudaFree(b); cudaFree(x); cudaFree(Y); cudaFree(Ys); cudaFree(Bp); cudaFree(V); cudaFree(W);
+  cudaFree(X); cudaFree(X0); cudaFree(Vs); cudaFree(Zp); cudaFree(part); cudaFree(sc); cudaFree(nact);
+  cudaStreamDestroy(s);
+  return true;
+}
+
+}  // namespace agb

@@ -1,0 +1,58 @@
+// Block LSQR on a dense row-major matrix resident in HBM (host-side driver).
+#pragma once
+#include "agb_common.cuh"
+#include <vector>
+#include <string>
+
+namespace agb {
+
+// Per right-hand-side LSQR recurrence state (lib_lsqr.f:900-1231), FP64.
+struct LsqrScalars {
+  double alpha, beta, rhobar, phibar, anorm, dnorm, res2, xnorm, xnorm1, cs2, sn2, z, bnorm, rnorm, arnorm, acond;
+  double atol, btol, ctol;
+  double t1, t2, t3;       // x/w update coefficients of the current iteration
+  double gamma;            // coefficient of Y_old in Y = A V + gamma Y_old
+  double dxmax;
+  int itn, istop, active, itnlim;
+};
+
+// Dense block LSQR.  A is m x n row-major with leading dimension lda (lda is
+// a multiple of 32 and columns n..lda-1 are zero).  T = float (mixed path)
+// or double (FP64 path).  Up to AGB_MAX_RHS right-hand sides share every
+// sweep over A.
+struct DenseLsqr {
+  int m = 0, n = 0, k = 0;
+  int64_t lda = 0;
+  bool fp32 = false;
+  const void* A = nullptr;     // device, T
+  cudaStream_t stream = 0;
+  // device work buffers (FP64 unless noted)
+  double *Y = nullptr, *V = nullptr, *W = nullptr, *X = nullptr, *Z = nullptr;
+  void *Ys = nullptr, *Vs = nullptr;  // T copies used by the sweeps
+  double* part = nullptr;      // per-CTA partial sums
+  double* Zp = nullptr;        // per-row-group partial products of A^T Y
+  LsqrScalars* sc = nullptr;   // k entries
+  int* nactive = nullptr;      // device counter
+  int* h_nactive = nullptr;    // pinned host mirror
+  int zgroups = 0;
+  size_t part_cap = 0;
+  std::string err;
+
+  ~DenseLsqr();
+  bool setup(const void* A_dev, bool is_fp32, int m, int n, int64_t lda, int k, cudaStream_t s);
+  // Column scaling of lsqr_precon: q_j = 1/||A(:,j)||, A <- A diag(q) (in place).
+  bool precon(void* A_dev, double* q_dev);
+  // lsqr_solve semantics per column c: x0 = X_in(:,c) warm start, b(:,c);
+  // x_out = q .* dx + x0.  b and x are device FP64, column-major n x k / m x k.
+  bool solve(const double* b_dev, double* x_dev, const double* q_dev, double eps, int maxit, int* nit_host,
+             int* istop_host, double* rnorm_host = nullptr, int check_every = 8);
+  // r = b - A (x ./ q) with FP64 accumulation (refinement residual).
+  bool residual(const double* b_dev, const double* x_dev, const double* q_dev, double* r_dev);
+  void release();
+};
+
+bool crs_lsqr_precon(int m, int n, int64_t nnz, double* q, const int64_t* ia, const int* ja, double* a, std::string& err);
+bool crs_lsqr_solve(int m, int n, int64_t nnz, int& maxit, double eps, int& nit, int& ierr, const double* q,
+                    const int64_t* ia, const int* ja, const double* a, const double* b, double* x, std::string& err);
+
+}  // namespace agb

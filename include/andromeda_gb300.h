@@ -1,0 +1,152 @@
+/*
+ * andromeda_gb300 -- C ABI of the GB300-native BEM hot path (assembly of the
+ * Laplace/Stokes influence matrices and their LSQR solve).
+ *
+ * Every entry point takes plain pointers and sizes, returns 0 (AGB_OK) on
+ * success and a nonzero status otherwise; agb_last_error() then describes the
+ * failure.  No exception and no CUDA/torch type crosses the boundary.  Arrays
+ * are owned by the caller; the library copies what it needs.
+ *
+ * The entry points replace the following reference routines (Fortran,
+ * src/ of WildSmilodon/Andromeda):
+ *
+ *   agb_set_mesh        mMesh module state built by ReadMesh, CalMeshArea
+ *                       (lib_mesh.f90:956), CalMeshNormals (lib_mesh.f90:695) and
+ *                       CalQMesh (lib_mesh.f90:577)
+ *   agb_set_problem     subdomain/BC state of ReadsdBIC + SetUpSubdomains
+ *                       (lib_sdBem.f90:319) + sdSetUpXandB (lib_sdBem.f90:4) and
+ *                       StokesBigSystemXB (lib_Stokes.f90:1180); the ITRI/IQUD
+ *                       rules of ReadParameters (mod_par.f90:230-234)
+ *   agb_assemble        CoR_Integrals (lib_int.f90:4) / CoR_Integrals_Stokes
+ *                       (lib_Stokes.f90:2664) fused with the BC routing of
+ *                       sdSetUpSysMrhsM_CRS (lib_CRS.f90:148) /
+ *                       stokesFormCRSsysMrhsM (lib_Stokes.f90:475) and the column
+ *                       scaling lsqr_precon (lib_lsqr.f:131); the system matrix
+ *                       stays resident on the GPU
+ *   agb_rhs             formStokesLeftRightHandSideVectors (lib_StokesFull.f90:379)
+ *                       + CRSxV(rhsM, b) (lib_CRS.f90:764); Laplace: CRSxV(rhsM,-b)
+ *   agb_solve           lsqr_solve (lib_lsqr.f:33) for nrhs right-hand sides in
+ *                       one block solve, + StokesDistributeUnknowns
+ *                       (lib_StokesFull.f90:446) numbering of the result
+ *   agb_force_torque    getForceIntegrateFluxes / getTorqueIntegrateFluxes
+ *                       (lib_particle.f90:1751,1793)
+ *   agb_resistance_tensor  the 3-sides resistance workflows
+ *                       StokesInlet3sidesForceCRS / ...TorqueOmegaCRS
+ *                       (lib_particle.f90:341,176) as one 6-RHS solve
+ *   agb_lsqr_precon     lsqr_precon(m,n,nnz,q,ia,ja,a)      (lib_lsqr.f:131)
+ *   agb_lsqr_solve      lsqr_solve(m,n,nnz,maxit,eps,nit,ierr,q,ia,ja,a,b,x)
+ *                                                           (lib_lsqr.f:33)
+ */
+#ifndef ANDROMEDA_GB300_H
+#define ANDROMEDA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct agb_context agb_context;
+
+/* status codes */
+#define AGB_OK 0
+#define AGB_ERR_ARG 1
+#define AGB_ERR_CUDA 2
+#define AGB_ERR_STATE 3
+#define AGB_ERR_UNSUPPORTED 4
+#define AGB_ERR_NUMERIC 5
+
+/* problem kinds (PRTY of and.inp) */
+#define AGB_LAPLACE 1
+#define AGB_STOKES 2
+
+/* precision of the assembled system */
+#define AGB_FP64 0  /* everything FP64 (the reference's arithmetic) */
+#define AGB_MIXED 1 /* FP32 regular quadrature + FP32 matrix; FP64 singular
+                       integrals, free-term row sums, norms/recurrences and
+                       the refinement residual */
+
+/* boundary-condition types (mod_mesh.f90:110) */
+#define AGB_BC_FUNCTION 1
+#define AGB_BC_FLUX 2
+#define AGB_BC_CONTACT 3
+
+/* Library version string. */
+const char* agb_version(void);
+
+/* Create a context bound to CUDA device `device` (one stream per context). */
+int agb_create(agb_context** ctx, int device);
+int agb_destroy(agb_context* ctx);
+/* Text of the last failure on this context ("" if none).  ctx may be NULL for
+ * the context-free entry points (agb_lsqr_*), whose last error is per thread. */
+const char* agb_last_error(const agb_context* ctx);
+
+/* Mesh.  xyz: 3*nnodes doubles (node-major: x,y,z of node 0, then node 1 ...).
+ * etype: 2 = 3-node triangle, 3 = 4-node quad.  con: 4*nelem 0-based node ids
+ * (4th entry ignored for triangles).  bcid: wall id of each element. */
+int agb_set_mesh(agb_context* ctx, int nnodes, const double* xyz, int nelem, const int* etype, const int* con,
+                 const int* bcid);
+
+/* One subdomain made of `nwalls` walls (ids `walls`), normal multipliers
+ * normMul (NORMMUL of the .bic file, 1.0 by default), diffusivity/viscosity
+ * diff, and known[en*nwalls + k] = BC type of equation en (0 for Laplace;
+ * 0,1,2 = x,y,z for Stokes) on wall walls[k].  itri = 1..5 (triangle rule),
+ * iqud = 1..8 (Gauss rule index for quads). */
+int agb_set_problem(agb_context* ctx, int kind, int nwalls, const int* walls, const double* normMul, double diff,
+                    const int* known, int itri, int iqud);
+
+/* Element geometry in global element order (normal 3*nelem, area nelem,
+ * centroid 3*nelem); elements outside the subdomain are zero. */
+int agb_get_geometry(agb_context* ctx, double* normal, double* area, double* centroid);
+
+/* Size of the assembled system: m rows (equations), n unknowns.  For the
+ * all-Dirichlet problems m == n == nelem (Laplace) or 3*nelem (Stokes), in the
+ * reference numbering: rows source-major/component-minor, unknowns
+ * component-major (x of every element, then y, then z). */
+int agb_system_size(agb_context* ctx, int* m, int* n);
+
+/* Assemble the system matrix on the GPU in the given precision and apply the
+ * reference's column scaling (lsqr_precon).  Current scope: every wall has
+ * known function values (all-Dirichlet), triangles for AGB_MIXED. */
+int agb_assemble(agb_context* ctx, int precision);
+
+/* Copy the assembled system to the host (m x n row-major), with (scaled=1) or
+ * without (scaled=0) the column scaling; and the scaling q (n) if not NULL. */
+int agb_get_system(agb_context* ctx, int scaled, double* A, double* q);
+
+/* Right-hand sides for nrhs known nodal fields u[r][en][nnodes]:
+ * rhs[r][m] = rhsM * b (Stokes) / rhsM * (-b) (Laplace). */
+int agb_rhs(agb_context* ctx, int nrhs, const double* u, double* rhs);
+
+/* Solve for nrhs fields at once.  x[r][n] holds the warm start on entry (the
+ * reference warm-starts from the previous solution) and the unknowns on exit.
+ * maxit = 0 -> 10*(m+n+50); eps as the SOLVER line.  refine = number of extra
+ * residual-correction passes (FP64 residual of the stored matrix).
+ * nit[r], istop[r] per right-hand side. */
+int agb_solve(agb_context* ctx, int nrhs, const double* u, double* x, int maxit, double eps, int refine, int* nit,
+              int* istop);
+
+/* Force (3) and torque (3, about the origin) of the tractions x[r][n] on the
+ * elements of wall `wall`: ft[r][6]. */
+int agb_force_torque(agb_context* ctx, int nrhs, const double* x, int wall, double* ft);
+
+/* Resistance tensor of the body on `particle_wall` inside the container
+ * `outer_wall`: assembles (precision), imposes the six rigid motions on the
+ * container (unit translations e_x,e_y,e_z, then rotations e_i x r), solves the
+ * six right-hand sides in one block LSQR and integrates force and torque on
+ * the particle.  R[r][6] = (F, T) of motion r.  times_ms (may be NULL):
+ * {assemble, rhs, solve, reduce, total}. */
+int agb_resistance_tensor(agb_context* ctx, int precision, int particle_wall, int outer_wall, int maxit, double eps,
+                          int refine, double* R, int* nit, double* times_ms);
+
+/* Drop-ins with the reference signatures (1-based CRS, int64 row pointers).
+ * agb_lsqr_precon scales a in place like lsqr_precon; agb_lsqr_solve
+ * warm-starts from x like lsqr_solve.  Both run on the current CUDA device. */
+int agb_lsqr_precon(int m, int n, int64_t nnz, double* q, const int64_t* ia, const int* ja, double* a);
+int agb_lsqr_solve(int m, int n, int64_t nnz, int* maxit, double eps, int* nit, int* ierr, const double* q,
+                   const int64_t* ia, const int* ja, double* a, const double* b, double* x);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ANDROMEDA_GB300_H */

@@ -1,0 +1,1603 @@
+// =============================================================================
+// CPU FP64 ORACLE of the Andromeda BEM hot path -- TEST INFRASTRUCTURE ONLY.
+//
+// This file restates, routine by routine, the reference Fortran algorithms of
+// WildSmilodon/Andromeda (src/*.f90, src/lib_lsqr.f) in plain C++ double
+// precision.  It is the checker for the CUDA library in andromeda_gb300/ and
+// the timed CPU baseline; it is never linked into the product.  Only the tests,
+// __graft_entry__.smoke() and bench.py's CPU legs load it (liborc.so).
+//
+// Parity pin: the reference cannot be compiled here (no Fortran compiler, LIS
+// or MPI).  The restatement is pinned against the reference's own known
+// answers -- the Triangle_TestIntegration analytic values
+// (src/mod_trikotnik.f90:124-154), the built-in rigid-body/free-term
+// diagnostics (src/lib_sdBem.f90:566-581,714-718; src/lib_Stokes.f90:1781-1812,
+// 2153-2178) and the analytic sphere resistances (src/lib_particle.f90:1961-1976)
+// -- see tests/test_oracle_golden.py.
+//
+// Index conventions: all arrays passed in from outside are 0-based; element
+// connectivity is 4 ints per element (unused 4th = -1 for triangles); wall ids
+// (bcid) are the user's integers.  Dense matrices of the reference
+// (Hmat(nsp,nnodes) etc.) are stored column-major exactly like Fortran.
+// =============================================================================
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#include <string>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../andromeda_gb300/csrc/quad_tables.h"
+
+namespace orc {
+
+static const double PI = 3.141592653589793238462643383;  // mCommon pi (mod_common.f90:7)
+enum { iFunction = 1, iFlux = 2, iContact = 3 };        // mod_mesh.f90:110
+
+// -----------------------------------------------------------------------------
+// Quadrature
+// -----------------------------------------------------------------------------
+struct TriRule {
+  int n = 0;
+  std::vector<double> l1, l2, l3, w;
+};
+
+// Triangle_GetBarycentricCoordinates (mod_trikotnik.f90:236-279)
+static void bary(double x1, double y1, double z1, double x2, double y2, double z2,
+                 double x3, double y3, double z3, double px, double py, double pz,
+                 double& l1, double& l2, double& l3) {
+  double v0x = x2 - x1, v0y = y2 - y1, v0z = z2 - z1;
+  double v1x = x3 - x1, v1y = y3 - y1, v1z = z3 - z1;
+  double v2x = px - x1, v2y = py - y1, v2z = pz - z1;
+  double d00 = v0x * v0x + v0y * v0y + v0z * v0z;
+  double d01 = v0x * v1x + v0y * v1y + v0z * v1z;
+  double d11 = v1x * v1x + v1y * v1y + v1z * v1z;
+  double d20 = v2x * v0x + v2y * v0y + v2z * v0z;
+  double d21 = v2x * v1x + v2y * v1y + v2z * v1z;
+  double denom = d00 * d11 - d01 * d01;
+  l1 = (d11 * d20 - d01 * d21) / denom;
+  l2 = (d00 * d21 - d01 * d20) / denom;
+  l3 = 1.0 - l1 - l2;
+}
+
+// Triangle_IntegrationInit + WandzuratXiaoBary (mod_trikotnik.f90:282-781)
+static TriRule wx_rule(int itri) {
+  TriRule r;
+  if (itri < 1 || itri > 5) return r;
+  const int o0 = agb_tables::kWxOrbitOffset[itri - 1], o1 = agb_tables::kWxOrbitOffset[itri];
+  const double x1 = -0.5, y1 = +0.5 * std::sqrt(3.0), x2 = -0.5, y2 = -0.5 * std::sqrt(3.0), x3 = 1.0, y3 = 0.0;
+  const double pi = 4.0 * std::atan(1.0);
+  const double s = std::sin(2.0 / 3.0 * pi), c = std::cos(2.0 / 3.0 * pi);
+  const double s4 = std::sin(4.0 / 3.0 * pi), c4 = std::cos(4.0 / 3.0 * pi);
+  std::vector<double> X, Y;
+  for (int j = o0; j < o1; ++j) {
+    const auto& ob = agb_tables::kWxOrbits[j];
+    auto push3 = [&](double x, double y, double cc, double ss) {
+      double xa = x, ya = y;
+      double xb = xa * cc - ya * ss, yb = -xa * ss - ya * cc;
+      double xc = xb * cc + yb * ss, yc = -xb * ss + yb * cc;
+      X.push_back(xa); Y.push_back(ya); r.w.push_back(ob.w);
+      X.push_back(xb); Y.push_back(yb); r.w.push_back(ob.w);
+      X.push_back(xc); Y.push_back(yc); r.w.push_back(ob.w);
+    };
+    if (ob.m == 1) {
+      X.push_back(ob.x); Y.push_back(ob.y); r.w.push_back(ob.w);
+    } else if (ob.m == 3) {
+      push3(ob.x, ob.y, c, s);
+    } else if (ob.m == 6) {
+      push3(ob.x, ob.y, c, s);
+      push3(ob.x, -ob.y, c4, s4);
+    }
+  }
+  r.n = (int)X.size();
+  r.l1.resize(r.n); r.l2.resize(r.n); r.l3.resize(r.n);
+  for (int i = 0; i < r.n; ++i)
+    bary(x1, y1, 0.0, x2, y2, 0.0, x3, y3, 0.0, X[i], Y[i], 0.0, r.l1[i], r.l2[i], r.l3[i]);
+  return r;
+}
+
+// Gauss table (mod_gauss.f90:33-393), 1-based ranges.
+static inline double GI(int i) { return agb_tables::kGaussGi[i - 1]; }
+static inline double OME(int i) { return agb_tables::kGaussOme[i - 1]; }
+
+// Triangle_Area, Heron (mod_trikotnik.f90:786-802) == tri_area (mod_singInt.f90:394-413)
+static double tri_area(double x1, double y1, double z1, double x2, double y2, double z2,
+                       double x3, double y3, double z3) {
+  double a = std::sqrt((x1 - x2) * (x1 - x2) + (y1 - y2) * (y1 - y2) + (z1 - z2) * (z1 - z2));
+  double b = std::sqrt((x3 - x2) * (x3 - x2) + (y3 - y2) * (y3 - y2) + (z3 - z2) * (z3 - z2));
+  double c = std::sqrt((x1 - x3) * (x1 - x3) + (y1 - y3) * (y1 - y3) + (z1 - z3) * (z1 - z3));
+  double p = 0.5 * (a + b + c);
+  return std::sqrt(p * (p - a) * (p - b) * (p - c));
+}
+
+// -----------------------------------------------------------------------------
+// Ren & Chan (2015) / Ravnik (2022) analytic singular integrals
+// (mod_singInt.f90:34-1157)
+// -----------------------------------------------------------------------------
+static double sq(double v) { return std::sqrt(v); }
+static double p15(double v) { return std::pow(v, 1.5); }
+
+static double getXi100(double a, double b, double c) {
+  double d = 2.0 * sq(b) * sq(a + b - c) + 2.0 * b - c;
+  double e = 2.0 * sq(a) * sq(b) - c;
+  return std::log(d / e) / sq(b);
+}
+static double getXi010(double a, double b, double c) {
+  double d = 2.0 * sq(a) * sq(a + b - c) + 2.0 * a - c;
+  double e = 2.0 * sq(a) * sq(b) - c;
+  return std::log(d / e) / sq(a);
+}
+static double getXi000(double a, double b, double c) {
+  double d = 2.0 * sq(a) * sq(a + b - c) + 2.0 * a - c;
+  double e = 2.0 * sq(b) * sq(a + b - c) - 2.0 * b + c;
+  return std::log(d / e) / sq(a + b - c);
+}
+static double getXi13130(double a, double b, double c) {
+  double d = 4.0 * a + 2.0 * b + 2.0 * sq(4.0 * a + b - 2.0 * c) * sq(a + b - c) - 3.0 * c;
+  double e = -2.0 * a - 4.0 * b + 2.0 * sq(a + 4.0 * b - 2.0 * c) * sq(a + b - c) + 3.0 * c;
+  double t1 = std::log(d / e) / sq(a + b - c);
+  d = 4.0 * a + 2.0 * sq(4.0 * a + b - 2.0 * c) * sq(a) - c;
+  e = -2.0 * a - c + 2.0 * sq(a + b + c) * sq(a);
+  double t2 = std::log(d / e) / sq(a);
+  d = (4.0 * b + 2.0 * sq(a + 4.0 * b - 2.0 * c) * sq(b) - c) * (2.0 * b + 2.0 * sq(a + b + c) * sq(b) + c);
+  e = (b + sq(4.0 * a + b - 2.0 * c) * sq(b) - c) * (-b + sq(4.0 * a + b - 2.0 * c) * sq(b) + c);
+  double t3 = std::log(d / e) / sq(b);
+  return (t1 + t2 + t3) / 3.0;
+}
+// Eq. (34) of Ren & Chan: tensor part for the centroid source (getXi13130G)
+static double getXi13130G(double a, double b, double c, double d, double e, double f) {
+  double G = 0.0, st, im;
+  st = 2.0 * sq(b) * (b * c * d + a * c * e - 2.0 * a * b * f) * (sq(a + b + c) - sq(4.0 * a + b - 2.0 * c));
+  im = a * (4.0 * a * b - c * c);
+  G += st / im;
+  st = 2.0 * sq(b) * (b * (2.0 * b - c) * d - a * (2.0 * b * e + c * e - 2.0 * b * f) + c * (c * e - b * f)) *
+       (sq(a + 4.0 * b - 2.0 * c) - sq(4.0 * a + b - 2.0 * c));
+  im = (a + b - c) * (4.0 * a * b - c * c);
+  G += st / im;
+  st = 4.0 * a + 2.0 * b + 2.0 * sq(4.0 * a + b - 2.0 * c) * sq(a + b - c) - 3.0 * c;
+  im = -2.0 * a - 4.0 * b + 2.0 * sq(a + 4.0 * b - 2.0 * c) * sq(a + b - c) + 3.0 * c;
+  G += e * sq(b) * std::log(st / im) / sq(a + b - c);
+  G += sq(b) * (b * d - a * e + c * e - b * f) * std::log(st / im) / p15(a + b - c);
+  st = 4.0 * a + 2.0 * sq(a) * sq(4.0 * a + b - 2.0 * c) - c;
+  im = -2.0 * a - c + 2.0 * sq(a) * sq(a + b + c);
+  G += e * sq(b) * std::log(st / im) / sq(a);
+  G += sq(b) * (b * d - a * e) * std::log(st / im) / p15(a);
+  st = (4.0 * b + 2.0 * sq(b) * sq(a + 4.0 * b - 2.0 * c) - c) * (2.0 * b + 2.0 * sq(b) * sq(a + b + c) + c);
+  im = 4.0 * (b + sq(b) * sq(4.0 * a + b - 2.0 * c) - c) * (-b + sq(b) * sq(4.0 * a + b - 2.0 * c) + c);
+  G += e * std::log(st / im);
+  G += e * std::log(4.0);
+  G /= (3.0 * p15(b));
+  return G;
+}
+static double getXi000G(double a, double b, double c, double d, double e, double f) {
+  double abc = a + b - c, q = 4 * a * b - c * c;
+  return (-4 * a * b * e + c * c * e +
+          (2 * b * (2 * b * b * d + c * (-a + c) * e - b * (2 * a * (e - f) + c * (d + f)))) / abc +
+          (2 * sq(a) * sq(b) * (-2 * b * b * d + (a - c) * c * e + b * (2 * a * (e - f) + c * (d + f)))) / abc +
+          (p15(b) * q * (d + e - f) * std::log(2 * a + 2 * sq(a) * sq(abc) - c)) / p15(abc) +
+          (-2 * p15(b) * c * d - 2 * a * sq(b) * c * e + 4 * a * p15(b) * f +
+           sq(a) * (-4 * a * b + c * c) * e * (-1 + std::log(2 * sq(a) * sq(b) + c))) / sq(a) +
+          4 * a * b * e * std::log(2 * sq(a) * sq(b) + c) - c * c * e * std::log(2 * sq(a) * sq(b) + c) -
+          (p15(b) * q * (d + e - f) * std::log(-2 * b + 2 * sq(b) * sq(abc) + c)) / p15(abc)) /
+         (p15(b) * q);
+}
+static double getXi100G(double a, double b, double c, double d, double e, double f) {
+  double abc = a + b - c, q = 4 * a * b - c * c;
+  return (2 * sq(b) * (b * sq(abc) * c * d - p15(a) * (c * e + 2 * b * (e - f)) + a * sq(abc) * (c * e - 2 * b * f) +
+                       sq(a) * (2 * b * b * d + c * c * e - b * c * (d + f))) -
+          sq(a) * sq(abc) * q * e * (std::log(2 * sq(a) * sq(b) - c) - std::log(2 * b + 2 * sq(b) * sq(abc) - c))) /
+         (sq(a) * p15(b) * sq(abc) * q);
+}
+static double getXi010G(double a, double b, double c, double d, double e, double f) {
+  double abc = a + b - c, q = 4 * a * b - c * c;
+  double t1 = (2 * sq(b) * (-2 * b * b * d + (a - c) * c * e + b * (2 * a * (e - f) + c * (d + f))) +
+               sq(abc) * q * e * (-1 + std::log(-2 * b + 2 * sq(b) * sq(abc) + c))) / sq(abc);
+  double t2 =
+      (p15(b) * sq(abc) * (-4 * a * b + c * c) * d * std::log(2 * sq(a) * sq(b) - c) +
+       p15(b) * sq(abc) * q * d * std::log(2 * a + 2 * sq(a) * sq(abc) - c) +
+       sq(a) * (2 * p15(b) * c * (-b + sq(b) * sq(abc) + c) * d +
+                a * a * (4 * b * sq(abc) * e - 2 * sq(b) * c * e + 4 * p15(b) * f) +
+                a * (2 * b * sq(abc) * c * e + 2 * sq(b) * c * c * e - sq(abc) * c * c * e + 4 * std::pow(b, 2.5) * f -
+                     4 * b * b * sq(abc) * f - 2 * p15(b) * c * (d + e + 2 * f)) +
+                a * sq(abc) * (-4 * a * b + c * c) * e * std::log(-2 * b + 2 * sq(b) * sq(abc) + c))) /
+      (p15(a) * sq(abc));
+  return (t1 + t2) / (p15(b) * q);
+}
+
+// siCrossProduct a = b x c (mod_singInt.f90:1114-1123)
+static void cross(double a[3], const double b[3], const double c[3]) {
+  a[0] = b[1] * c[2] - b[2] * c[1];
+  a[1] = -b[0] * c[2] + b[2] * c[0];
+  a[2] = b[0] * c[1] - b[1] * c[0];
+}
+// siNormVector (mod_singInt.f90:1141-1155); its uninitialised accumulator is
+// taken as zero (the value an optimising gfortran build produces).
+static void normv(double a[3]) {
+  double n = 0.0;
+  for (int i = 0; i < 3; ++i) n += a[i] * a[i];
+  n = std::sqrt(n);
+  for (int i = 0; i < 3; ++i) a[i] /= n;
+}
+// getMrot (mod_singInt.f90:905-946): rows of Mrot are the in-plane unit
+// vectors ov1, ov2 and the normal ov3.
+static void getMrot(const double rr1[3], const double rr2[3], const double rr3[3], double M[3][3]) {
+  double ov1[3], ov2[3], ov3[3], ov4[3];
+  for (int i = 0; i < 3; ++i) { ov1[i] = rr2[i] - rr1[i]; ov4[i] = rr3[i] - rr1[i]; }
+  cross(ov3, ov4, ov1);
+  cross(ov2, ov3, ov1);
+  normv(ov1); normv(ov2); normv(ov3);
+  for (int j = 0; j < 3; ++j) { M[0][j] = ov1[j]; M[1][j] = ov2[j]; M[2][j] = ov3[j]; }
+}
+// getrcABC / getABCDEF (mod_singInt.f90:1010-1108) + getABC/getDEF (:952-1004)
+struct Frame { double a, b, c, dxx, exx, fxx, dxy, exy, fxy, dyy, eyy, fyy; double M[3][3]; };
+static Frame getFrame(const double v[9]) {
+  Frame F;
+  double r1[3] = {v[0], v[1], v[2]}, r2[3] = {v[3], v[4], v[5]}, r3[3] = {v[6], v[7], v[8]};
+  double cc[3], rr1[3], rr2[3], rr3[3], q1[3], q2[3], q3[3];
+  for (int i = 0; i < 3; ++i) cc[i] = (r1[i] + r2[i] + r3[i]) / 3.0;
+  for (int i = 0; i < 3; ++i) { rr1[i] = r1[i] - cc[i]; rr2[i] = r2[i] - cc[i]; rr3[i] = r3[i] - cc[i]; }
+  getMrot(rr1, rr2, rr3, F.M);
+  for (int i = 0; i < 3; ++i) {
+    q1[i] = F.M[i][0] * rr1[0] + F.M[i][1] * rr1[1] + F.M[i][2] * rr1[2];
+    q2[i] = F.M[i][0] * rr2[0] + F.M[i][1] * rr2[1] + F.M[i][2] * rr2[2];
+    q3[i] = F.M[i][0] * rr3[0] + F.M[i][1] * rr3[1] + F.M[i][2] * rr3[2];
+  }
+  double A11 = q1[0] - q3[0], A12 = q2[0] - q3[0], A21 = q1[1] - q3[1], A22 = q2[1] - q3[1];
+  F.a = A11 * A11 + A21 * A21;
+  F.b = A12 * A12 + A22 * A22;
+  F.c = 2.0 * (A11 * A12 + A21 * A22);
+  F.dxx = A11 * A11; F.exx = A12 * A12; F.fxx = 2.0 * A11 * A12;
+  F.dyy = A21 * A21; F.eyy = A22 * A22; F.fyy = 2.0 * A21 * A22;
+  F.dxy = A11 * A21; F.exy = A12 * A22; F.fxy = A11 * A22 + A21 * A12;
+  return F;
+}
+// si_tri_lap (mod_singInt.f90:127-167)
+static double si_tri_lap(const double v[9], double area, int isrc) {
+  Frame F = getFrame(v);
+  double f;
+  switch (isrc) {
+    case 1: f = getXi100(F.a, F.b, F.c); break;
+    case 2: f = getXi010(F.a, F.b, F.c); break;
+    case 3: f = getXi000(F.a, F.b, F.c); break;
+    case 4: f = getXi13130(F.a, F.b, F.c); break;
+    default: fprintf(stderr, "Error in si_tri_lap\n"); return NAN;
+  }
+  double jac = 2.0 * area;
+  return 0.25 / PI * jac * f;
+}
+// si_tri_stk (mod_singInt.f90:34-123): G = {xx,xy,xz,yy,yz,zz}
+static void si_tri_stk(const double v[9], double area, int isrc, double G[6]) {
+  Frame F = getFrame(v);
+  double ff, gxx, gxy, gyy;
+  double (*fg)(double, double, double, double, double, double) = nullptr;
+  switch (isrc) {
+    case 1: ff = getXi100(F.a, F.b, F.c); fg = getXi100G; break;
+    case 2: ff = getXi010(F.a, F.b, F.c); fg = getXi010G; break;
+    case 3: ff = getXi000(F.a, F.b, F.c); fg = getXi000G; break;
+    case 4: ff = getXi13130(F.a, F.b, F.c); fg = getXi13130G; break;
+    default: fprintf(stderr, "Error in si_tri_stk\n"); for (int i = 0; i < 6; ++i) G[i] = NAN; return;
+  }
+  gxx = fg(F.a, F.b, F.c, F.dxx, F.exx, F.fxx);
+  gxy = fg(F.a, F.b, F.c, F.dxy, F.exy, F.fxy);
+  gyy = fg(F.a, F.b, F.c, F.dyy, F.eyy, F.fyy);
+  double mat[3][3] = {{2.0 * area * (ff + gxx), 2.0 * area * gxy, 0.0},
+                      {2.0 * area * gxy, 2.0 * area * (ff + gyy), 0.0},
+                      {0.0, 0.0, 2.0 * area * ff}};
+  // mat = MrotT * mat * Mrot
+  double t[3][3], o[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 3; ++k) s += F.M[k][i] * mat[k][j];
+      t[i][j] = s;
+    }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 3; ++k) s += t[i][k] * F.M[k][j];
+      o[i][j] = s;
+    }
+  G[0] = o[0][0]; G[1] = o[0][1]; G[2] = o[0][2]; G[3] = o[1][1]; G[4] = o[1][2]; G[5] = o[2][2];
+}
+static void tri9(double* v, const double* a, const double* b, const double* c) {
+  for (int i = 0; i < 3; ++i) { v[i] = a[i]; v[3 + i] = b[i]; v[6 + i] = c[i]; }
+}
+// si_qua_lap (mod_singInt.f90:172-260): split at the source vertex/centre
+static double si_qua_lap(const double q[12], int isrc) {
+  const double* P[5];
+  double p5[3];
+  for (int k = 0; k < 4; ++k) P[k] = q + 3 * k;
+  double v[9];
+  auto one = [&](int i, int j, int k) {
+    tri9(v, P[i], P[j], P[k]);
+    double ar = tri_area(v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], v[8]);
+    return si_tri_lap(v, ar, 1);
+  };
+  switch (isrc) {
+    case 1: return one(0, 1, 2) + one(0, 2, 3);
+    case 2: return one(1, 2, 3) + one(1, 3, 0);
+    case 3: return one(2, 3, 0) + one(2, 0, 1);
+    case 4: return one(3, 0, 1) + one(3, 1, 2);
+    case 5: {
+      for (int i = 0; i < 3; ++i) p5[i] = 0.25 * (q[i] + q[3 + i] + q[6 + i] + q[9 + i]);
+      P[4] = p5;
+      double s1 = one(4, 0, 1), s2 = one(4, 1, 2), s3 = one(4, 2, 3), s4 = one(4, 3, 0);
+      return s1 + s2 + s3 + s4;
+    }
+  }
+  fprintf(stderr, "ERROR in si_qua_lap\n");
+  return NAN;
+}
+// si_qua_stk (mod_singInt.f90:266-387)
+static void si_qua_stk(const double q[12], int isrc, double G[6]) {
+  const double* P[5];
+  double p5[3];
+  for (int k = 0; k < 4; ++k) P[k] = q + 3 * k;
+  double v[9], g1[6], g2[6], g3[6], g4[6];
+  auto one = [&](int i, int j, int k, double* g) {
+    tri9(v, P[i], P[j], P[k]);
+    double ar = tri_area(v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], v[8]);
+    si_tri_stk(v, ar, 1, g);
+  };
+  switch (isrc) {
+    case 1: one(0, 1, 2, g1); one(0, 2, 3, g2); break;
+    case 2: one(1, 2, 3, g1); one(1, 3, 0, g2); break;
+    case 3: one(2, 3, 0, g1); one(2, 0, 1, g2); break;
+    case 4: one(3, 0, 1, g1); one(3, 1, 2, g2); break;
+    case 5:
+      for (int i = 0; i < 3; ++i) p5[i] = 0.25 * (q[i] + q[3 + i] + q[6 + i] + q[9 + i]);
+      P[4] = p5;
+      one(4, 0, 1, g1); one(4, 1, 2, g2); one(4, 2, 3, g3); one(4, 3, 0, g4);
+      for (int i = 0; i < 6; ++i) G[i] = g1[i] + g2[i] + g3[i] + g4[i];
+      return;
+    default: fprintf(stderr, "ERROR in si_qua_stk\n"); for (int i = 0; i < 6; ++i) G[i] = NAN; return;
+  }
+  for (int i = 0; i < 6; ++i) G[i] = g1[i] + g2[i];
+}
+
+// -----------------------------------------------------------------------------
+// Kernels and regular integrators
+// -----------------------------------------------------------------------------
+// BemKernel (lib_sdBem.f90:911-936)
+static inline void bem_kernel(double sx, double sy, double sz, double fx, double fy, double fz,
+                              double nx, double ny, double nz, double& G, double& H) {
+  double RX = -fx + sx, RY = -fy + sy, RZ = -fz + sz;
+  double RA = std::sqrt(RX * RX + RY * RY + RZ * RZ);
+  double IRA2 = 1.0 / (RA * RA);
+  G = 0.25 / (PI * RA);
+  H = (RX * nx + RY * ny + RZ * nz) * IRA2 * G;
+}
+// Triangle_3DLapInt (lib_sdBem.f90:859-905); accumulates into out[0..3]
+static void tri_lap_regular(const TriRule& R, const double v[9], const double s[3], const double n[3],
+                            double area, double out[4]) {
+  for (int i = 0; i < R.n; ++i) {
+    double x = R.l1[i] * v[0] + R.l2[i] * v[3] + R.l3[i] * v[6];
+    double y = R.l1[i] * v[1] + R.l2[i] * v[4] + R.l3[i] * v[7];
+    double z = R.l1[i] * v[2] + R.l2[i] * v[5] + R.l3[i] * v[8];
+    double G, H;
+    bem_kernel(s[0], s[1], s[2], x, y, z, n[0], n[1], n[2], G, H);
+    out[0] += R.w[i] * G * area;
+    out[1] += R.w[i] * H * area * R.l1[i];
+    out[2] += R.w[i] * H * area * R.l2[i];
+    out[3] += R.w[i] * H * area * R.l3[i];
+  }
+}
+// Quad_BEMIntNum (lib_intAna.f90:219-344); out[0]=G, out[1..4]=H at nodes
+static void quad_lap_regular(int iqud, const double q[12], const double s[3], double multi, double out[5]) {
+  const double *P1 = q, *P2 = q + 3, *P3 = q + 6, *P4 = q + 9;
+  int ng1 = agb_tables::kGaussNg1[iqud - 1], ng2 = agb_tables::kGaussNg2[iqud - 1];
+  for (int k = 0; k < 5; ++k) out[k] = 0.0;
+  const double minedge = 1.0;
+  auto dist = [](const double* a, const double* b) {
+    return std::sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]));
+  };
+  double d1 = dist(P1, P2), d2 = dist(P2, P3), d3 = dist(P3, P4), d4 = dist(P4, P1);
+  double d13 = std::max(d1, d3), d24 = std::max(d2, d4);
+  int ndx = std::max(2, (int)(d13 / minedge + 0.5));
+  int nde = std::max(2, (int)(d24 / minedge + 0.5));
+  for (int ix = 1; ix <= ndx; ++ix)
+    for (int ie = 1; ie <= nde; ++ie) {
+      double a = -1.0 + (ix - 1) * 2.0 / ndx, b = -1.0 + ix * 2.0 / ndx;
+      double c = -1.0 + (ie - 1) * 2.0 / nde, d = -1.0 + ie * 2.0 / nde;
+      double dex = 0.25 * (b - a) * (d - c);
+      for (int i = ng1; i <= ng2; ++i) {
+        double gii = a + 0.5 * (GI(i) + 1.0) * (b - a);
+        double e1m = 1.0 - gii, e1p = 1.0 + gii;
+        for (int j = ng1; j <= ng2; ++j) {
+          double gij = c + 0.5 * (GI(j) + 1.0) * (d - c);
+          double e2m = 1.0 - gij, e2p = 1.0 + gij;
+          double f4[4] = {0.25 * e1m * e2m, 0.25 * e1p * e2m, 0.25 * e1p * e2p, 0.25 * e1m * e2p};
+          double X[3], KS[3], ET[3];
+          for (int k = 0; k < 3; ++k) {
+            X[k] = f4[0] * P1[k] + f4[1] * P2[k] + f4[2] * P3[k] + f4[3] * P4[k];
+            KS[k] = 0.25 * (-e2m * P1[k] + e2m * P2[k] + e2p * P3[k] - e2p * P4[k]);
+            ET[k] = 0.25 * (-e1m * P1[k] - e1p * P2[k] + e1p * P3[k] + e1m * P4[k]);
+          }
+          double anx = KS[1] * ET[2] - ET[1] * KS[2];
+          double any = ET[0] * KS[2] - KS[0] * ET[2];
+          double anz = KS[0] * ET[1] - ET[0] * KS[1];
+          double ajac = 1.0 / std::sqrt(anx * anx + any * any + anz * anz);
+          double n1 = multi * anx * ajac, n2 = multi * any * ajac, n3 = multi * anz * ajac;
+          ajac = dex * OME(i) * OME(j) / ajac;
+          double G, H;
+          bem_kernel(s[0], s[1], s[2], X[0], X[1], X[2], n1, n2, n3, G, H);
+          for (int k = 0; k < 4; ++k) out[1 + k] += H * ajac * f4[k];
+          out[0] += G * ajac;
+        }
+      }
+    }
+}
+
+// StokesKernel (lib_Stokes.f90:2450-2544).  G,T as 3x3; prG, prT 3-vectors.
+static inline void stokes_kernel(const double s[3], const double f[3], const double n[3], double G[3][3],
+                                 double T[3][3], double prG[3], double prT[3]) {
+  double rx = f[0] - s[0], ry = f[1] - s[1], rz = f[2] - s[2];
+  double rxx = rx * rx, rxy = rx * ry, rxz = rx * rz, ryy = ry * ry, ryz = ry * rz, rzz = rz * rz;
+  double ir2 = 1.0 / (rxx + ryy + rzz);
+  double ir = std::sqrt(ir2);
+  double ir3 = ir2 * ir;
+  G[0][0] = ir * (1.0 + rxx * ir2); G[0][1] = rxy * ir3; G[0][2] = rxz * ir3;
+  G[1][0] = G[0][1]; G[1][1] = ir * (1.0 + ryy * ir2); G[1][2] = ryz * ir3;
+  G[2][0] = G[0][2]; G[2][1] = G[1][2]; G[2][2] = ir * (1.0 + rzz * ir2);
+  double c = -6.0 * ir2 * ir3 * (rx * n[0] + ry * n[1] + rz * n[2]);
+  T[0][0] = c * rxx; T[0][1] = c * rxy; T[0][2] = c * rxz;
+  T[1][0] = T[0][1]; T[1][1] = c * ryy; T[1][2] = c * ryz;
+  T[2][0] = T[0][2]; T[2][1] = T[1][2]; T[2][2] = c * rzz;
+  c = 2.0 * ir3;
+  prG[0] = c * rx; prG[1] = c * ry; prG[2] = c * rz;
+  c = 4.0 * ir3;
+  prT[0] = c * ((-1.0 + 3.0 * rxx * ir2) * n[0] + 3.0 * rxy * ir2 * n[1] + 3.0 * rxz * ir2 * n[2]);
+  prT[1] = c * (3.0 * rxy * ir2 * n[0] + (-1.0 + 3.0 * ryy * ir2) * n[1] + 3.0 * ryz * ir2 * n[2]);
+  prT[2] = c * (3.0 * rxz * ir2 * n[0] + 3.0 * ryz * ir2 * n[1] + (-1.0 + 3.0 * rzz * ir2) * n[2]);
+}
+
+// Per-element Stokes result: G[6] (xx,xy,xz,yy,yz,zz), prG[3],
+// T[6][4] (component x local node), prT[3][4].
+struct StkElem {
+  double G[6], prG[3], T[6][4], prT[3][4];
+  void zero() { std::memset(this, 0, sizeof(*this)); }
+};
+static const int kSym[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
+
+// Triangle_3DStokesInt (lib_Stokes.f90:2341-2446)
+static void tri_stk_regular(const TriRule& R, const double v[9], const double s[3], const double n[3], double area,
+                            StkElem& E) {
+  double G[3][3], T[3][3], prG[3], prT[3], f[3];
+  for (int i = 0; i < R.n; ++i) {
+    f[0] = R.l1[i] * v[0] + R.l2[i] * v[3] + R.l3[i] * v[6];
+    f[1] = R.l1[i] * v[1] + R.l2[i] * v[4] + R.l3[i] * v[7];
+    f[2] = R.l1[i] * v[2] + R.l2[i] * v[5] + R.l3[i] * v[8];
+    stokes_kernel(s, f, n, G, T, prG, prT);
+    double w = R.w[i] * area;
+    double wl[3] = {w * R.l1[i], w * R.l2[i], w * R.l3[i]};
+    for (int k = 0; k < 6; ++k) E.G[k] += w * G[kSym[k][0]][kSym[k][1]];
+    for (int k = 0; k < 3; ++k) E.prG[k] += w * prG[k];
+    for (int k = 0; k < 6; ++k)
+      for (int j = 0; j < 3; ++j) E.T[k][j] += wl[j] * T[kSym[k][0]][kSym[k][1]];
+    for (int k = 0; k < 3; ++k)
+      for (int j = 0; j < 3; ++j) E.prT[k][j] += wl[j] * prT[k];
+  }
+}
+// Quad_StokesIntNum (lib_Stokes.f90:3754-3940): fixed 3x3 subcells
+static void quad_stk_regular(int iqud, const double q[12], const double s[3], double multi, StkElem& E) {
+  const double *P1 = q, *P2 = q + 3, *P3 = q + 6, *P4 = q + 9;
+  int ng1 = agb_tables::kGaussNg1[iqud - 1], ng2 = agb_tables::kGaussNg2[iqud - 1];
+  E.zero();
+  const int ndx = 3, nde = 3;
+  double G[3][3], T[3][3], prG[3], prT[3];
+  for (int ix = 1; ix <= ndx; ++ix)
+    for (int ie = 1; ie <= nde; ++ie) {
+      double a = -1.0 + (ix - 1) * 2.0 / ndx, b = -1.0 + ix * 2.0 / ndx;
+      double c = -1.0 + (ie - 1) * 2.0 / nde, d = -1.0 + ie * 2.0 / nde;
+      double dex = 0.25 * (b - a) * (d - c);
+      for (int i = ng1; i <= ng2; ++i) {
+        double gii = a + 0.5 * (GI(i) + 1.0) * (b - a);
+        double e1m = 1.0 - gii, e1p = 1.0 + gii;
+        for (int j = ng1; j <= ng2; ++j) {
+          double gij = c + 0.5 * (GI(j) + 1.0) * (d - c);
+          double e2m = 1.0 - gij, e2p = 1.0 + gij;
+          double f4[4] = {0.25 * e1m * e2m, 0.25 * e1p * e2m, 0.25 * e1p * e2p, 0.25 * e1m * e2p};
+          double X[3], KS[3], ET[3];
+          for (int k = 0; k < 3; ++k) {
+            X[k] = f4[0] * P1[k] + f4[1] * P2[k] + f4[2] * P3[k] + f4[3] * P4[k];
+            KS[k] = 0.25 * (-e2m * P1[k] + e2m * P2[k] + e2p * P3[k] - e2p * P4[k]);
+            ET[k] = 0.25 * (-e1m * P1[k] - e1p * P2[k] + e1p * P3[k] + e1m * P4[k]);
+          }
+          double anx = KS[1] * ET[2] - ET[1] * KS[2];
+          double any = ET[0] * KS[2] - KS[0] * ET[2];
+          double anz = KS[0] * ET[1] - ET[0] * KS[1];
+          double ajac = 1.0 / std::sqrt(anx * anx + any * any + anz * anz);
+          double nn[3] = {multi * anx * ajac, multi * any * ajac, multi * anz * ajac};
+          ajac = dex * OME(i) * OME(j) / ajac;
+          stokes_kernel(s, X, nn, G, T, prG, prT);
+          double w = ajac;
+          for (int k = 0; k < 6; ++k) E.G[k] += w * G[kSym[k][0]][kSym[k][1]];
+          for (int k = 0; k < 3; ++k) E.prG[k] += w * prG[k];
+          for (int isip = 0; isip < 4; ++isip) {
+            double ww = ajac * f4[isip];
+            for (int k = 0; k < 6; ++k) E.T[k][isip] += ww * T[kSym[k][0]][kSym[k][1]];
+            for (int k = 0; k < 3; ++k) E.prT[k][isip] += ww * prT[k];
+          }
+        }
+      }
+    }
+}
+
+// -----------------------------------------------------------------------------
+// Problem state: mesh + single subdomain + boundary conditions
+// -----------------------------------------------------------------------------
+struct CRS {
+  int neq = 0;
+  int64_t nnz = 0;
+  std::vector<int64_t> i;  // 1-based row starts (neq+1)
+  std::vector<int> j;      // 1-based columns
+  std::vector<double> v;
+};
+
+struct Eqn {
+  int nx = 0, nb = 0, neq = 0;
+  std::vector<int> col, qcol;  // 1-based numbering, -999 = not set
+  std::vector<double> u, q, x, b, pivot;
+  CRS sys, rhs;
+};
+
+struct Problem {
+  int kind = 1;  // 1 Laplace, 2 Stokes
+  int neq = 1;
+  // mesh (lib_mesh / mod_mesh)
+  int nnodes = 0, nelem = 0;
+  std::vector<double> x;       // 3*nnodes
+  std::vector<int> type, nno;  // type 2 tri, 3 quad
+  std::vector<int> con;        // 4*nelem, 0-based
+  std::vector<int> bcid;       // wall id per element
+  std::vector<double> normal, area, qx;
+  // subdomain
+  std::vector<int> loWalls;
+  std::vector<double> normMul;
+  double diff = 1.0;
+  std::vector<int> known;  // [neq][nw] BC type per equation and subdomain wall
+  std::vector<int> elementList, qnodeList, qbcidList, nodeList, BCidList;
+  int sd_nnodes = 0, sd_nqnodes = 0, nsp = 0;
+  // quadrature
+  TriRule tri;
+  int iqud = 4;
+  // integral matrices
+  std::vector<double> H, G;   // Laplace: nsp x sd_nnodes / nsp x sd_nqnodes, column-major
+  std::vector<double> M[18];  // Stokes: Txx..Tzz, prTx..prTz (nsp x nn), Gxx..Gzz, prGx..prGz (nsp x nq)
+  double fspCerr = 0, qspCerr = 0;
+  // equations
+  std::vector<Eqn> eqn;
+  Eqn stk;  // Stokes big system (col/qcol are 3*nnodes / 3*nqnodes)
+  int knownOf(int en, int wall) const {
+    for (size_t k = 0; k < loWalls.size(); ++k)
+      if (loWalls[k] == wall) return known[en * loWalls.size() + k];
+    return 0;
+  }
+  double multiOf(int wall) const {
+    double m = 1.0;
+    for (size_t k = 0; k < loWalls.size(); ++k)
+      if (loWalls[k] == wall) m = normMul[k];
+    return m;
+  }
+};
+
+// CalElementNormal (lib_mesh.f90:716-769), CalElementArea (lib_int.f90:606-721),
+// CalQMesh (lib_mesh.f90:577-629)
+static void geometry(Problem& P) {
+  P.normal.assign(3 * P.nelem, 0.0);
+  P.area.assign(P.nelem, 0.0);
+  P.qx.assign(3 * P.nelem, 0.0);
+  for (int e = 0; e < P.nelem; ++e) {
+    const double* t1 = &P.x[3 * P.con[4 * e + 0]];
+    const double* t2 = &P.x[3 * P.con[4 * e + 1]];
+    const double* t3 = &P.x[3 * P.con[4 * e + 2]];
+    double v1[3] = {t2[0] - t1[0], t2[1] - t1[1], t2[2] - t1[2]};
+    double v2[3] = {t3[0] - t1[0], t3[1] - t1[1], t3[2] - t1[2]};
+    double n[3] = {v1[1] * v2[2] - v1[2] * v2[1], -v1[0] * v2[2] + v1[2] * v2[0], v1[0] * v2[1] - v1[1] * v2[0]};
+    double d = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (int i = 0; i < 3; ++i) P.normal[3 * e + i] = n[i] / d;
+    if (P.type[e] == 2) {
+      P.area[e] = tri_area(t1[0], t1[1], t1[2], t2[0], t2[1], t2[2], t3[0], t3[1], t3[2]);
+      for (int j = 0; j < 3; ++j) {
+        double s = 0.0;
+        for (int k = 0; k < 3; ++k) s += (1.0 / 3.0) * P.x[3 * P.con[4 * e + k] + j];
+        P.qx[3 * e + j] = s;
+      }
+    } else {
+      const double* t4 = &P.x[3 * P.con[4 * e + 3]];
+      const double* Q[4] = {t1, t2, t3, t4};
+      int ng1 = agb_tables::kGaussNg1[3], ng2 = agb_tables::kGaussNg2[3];
+      double integral = 0.0, a = -1, b = 1, c = -1, dd = 1, dex = 0.25 * (b - a) * (dd - c);
+      for (int i = ng1; i <= ng2; ++i) {
+        double gii = a + 0.5 * (GI(i) + 1.0) * (b - a);
+        double e1m = 1.0 - gii, e1p = 1.0 + gii;
+        for (int j = ng1; j <= ng2; ++j) {
+          double gij = c + 0.5 * (GI(j) + 1.0) * (dd - c);
+          double e2m = 1.0 - gij, e2p = 1.0 + gij;
+          double f4[4] = {0.25 * e1m * e2m, 0.25 * e1p * e2m, 0.25 * e1p * e2p, 0.25 * e1m * e2p};
+          double KS[3], ET[3];
+          for (int k = 0; k < 3; ++k) {
+            KS[k] = 0.25 * (-e2m * Q[0][k] + e2m * Q[1][k] + e2p * Q[2][k] - e2p * Q[3][k]);
+            ET[k] = 0.25 * (-e1m * Q[0][k] - e1p * Q[1][k] + e1p * Q[2][k] + e1m * Q[3][k]);
+          }
+          double anx = KS[1] * ET[2] - ET[1] * KS[2];
+          double any = ET[0] * KS[2] - KS[0] * ET[2];
+          double anz = KS[0] * ET[1] - ET[0] * KS[1];
+          double ajac = dex * OME(i) * OME(j) * std::sqrt(anx * anx + any * any + anz * anz);
+          for (int isip = 0; isip < 4; ++isip) integral += ajac * f4[isip];
+        }
+      }
+      P.area[e] = integral;
+      for (int j = 0; j < 3; ++j) {
+        double s = 0.0;
+        for (int k = 0; k < 4; ++k) s += 0.25 * P.x[3 * P.con[4 * e + k] + j];
+        P.qx[3 * e + j] = s;
+      }
+    }
+  }
+}
+
+// SetUpSubdomains (lib_sdBem.f90:319-430), single subdomain
+static void setup_subdomain(Problem& P) {
+  P.elementList.clear();
+  for (int w : P.loWalls)
+    for (int e = 0; e < P.nelem; ++e)
+      if (P.bcid[e] == w) P.elementList.push_back(e);
+  P.sd_nqnodes = (int)P.elementList.size();
+  P.qnodeList = P.elementList;
+  P.qbcidList.resize(P.sd_nqnodes);
+  for (int i = 0; i < P.sd_nqnodes; ++i) P.qbcidList[i] = P.bcid[P.elementList[i]];
+  std::vector<int> tmp(P.nnodes, 0);
+  std::vector<char> has(P.nnodes, 0);
+  for (int e : P.elementList)
+    for (int j = 0; j < P.nno[e]; ++j) { tmp[P.con[4 * e + j]] = P.bcid[e]; has[P.con[4 * e + j]] = 1; }
+  P.nodeList.clear(); P.BCidList.clear();
+  for (int i = 0; i < P.nnodes; ++i)
+    if (has[i]) { P.nodeList.push_back(i); P.BCidList.push_back(tmp[i]); }
+  P.sd_nnodes = (int)P.nodeList.size();
+  P.nsp = P.sd_nnodes + P.sd_nqnodes;
+}
+
+// Elements of the subdomain in the reference's traversal order: walls of the
+// subdomain in list order, then element index (lib_sdBem.f90:471-474).
+static void element_vertices(const Problem& P, int e, double* v) {
+  for (int k = 0; k < P.nno[e]; ++k)
+    for (int i = 0; i < 3; ++i) v[3 * k + i] = P.x[3 * P.con[4 * e + k] + i];
+}
+
+// sdIntRowU (lib_sdBem.f90:438-584): source at node irow (global index)
+static void lap_row_u(const Problem& P, int irow, double* rowH, double* rowG, double& err) {
+  std::fill(rowH, rowH + P.nnodes, 0.0);
+  std::fill(rowG, rowG + P.nelem, 0.0);
+  const double s[3] = {P.x[3 * irow], P.x[3 * irow + 1], P.x[3 * irow + 2]};
+  for (size_t jj = 0; jj < P.loWalls.size(); ++jj) {
+    int iWall = P.loWalls[jj];
+    double mm = P.normMul[jj];
+    for (int ie = 0; ie < P.nelem; ++ie) {
+      if (P.bcid[ie] != iWall) continue;
+      int isrc = 0;
+      for (int j = 0; j < P.nno[ie]; ++j)
+        if (irow == P.con[4 * ie + j]) isrc = j + 1;
+      double v[12], integ = 0.0, inteH[4] = {0, 0, 0, 0};
+      element_vertices(P, ie, v);
+      if (P.type[ie] == 2) {
+        double n[3] = {mm * P.normal[3 * ie], mm * P.normal[3 * ie + 1], mm * P.normal[3 * ie + 2]};
+        if (isrc == 0) {
+          double out[4] = {0, 0, 0, 0};
+          tri_lap_regular(P.tri, v, s, n, P.area[ie], out);
+          integ = out[0]; inteH[0] = out[1]; inteH[1] = out[2]; inteH[2] = out[3];
+        } else {
+          integ = si_tri_lap(v, P.area[ie], isrc);
+        }
+      } else {
+        if (isrc == 0) {
+          double out[5];
+          quad_lap_regular(P.iqud, v, s, mm, out);
+          integ = out[0];
+          for (int k = 0; k < 4; ++k) inteH[k] = out[1 + k];
+        } else {
+          integ = si_qua_lap(v, isrc);
+        }
+      }
+      for (int j = 0; j < P.nno[ie]; ++j) rowH[P.con[4 * ie + j]] += inteH[j];
+      rowG[ie] = integ;
+    }
+  }
+  double c = 0.0;
+  for (int i = 0; i < P.nnodes; ++i) c -= rowH[i];
+  rowH[irow] += c;
+  for (int j = 0; j < 3; ++j) {
+    c = 0.0;
+    for (int i = 0; i < P.nnodes; ++i) c += rowH[i] * P.x[3 * i + j];
+    for (int i = 0; i < P.nelem; ++i) c -= rowG[i] * P.normal[3 * i + j] * P.multiOf(P.bcid[i]);
+    err = std::max(err, std::fabs(c));
+  }
+}
+// sdIntRowQ (lib_sdBem.f90:589-733): source at centroid of element irow
+static void lap_row_q(const Problem& P, int irow, double* rowH, double* rowG, double& err) {
+  std::fill(rowH, rowH + P.nnodes, 0.0);
+  std::fill(rowG, rowG + P.nelem, 0.0);
+  const double s[3] = {P.qx[3 * irow], P.qx[3 * irow + 1], P.qx[3 * irow + 2]};
+  for (size_t jj = 0; jj < P.loWalls.size(); ++jj) {
+    int iWall = P.loWalls[jj];
+    double mm = P.normMul[jj];
+    for (int ie = 0; ie < P.nelem; ++ie) {
+      if (P.bcid[ie] != iWall) continue;
+      int isrc = 0;
+      if (ie == irow) isrc = (P.type[ie] == 2) ? 4 : 5;
+      double v[12], integ = 0.0, inteH[4] = {0, 0, 0, 0};
+      element_vertices(P, ie, v);
+      if (P.type[ie] == 2) {
+        double n[3] = {mm * P.normal[3 * ie], mm * P.normal[3 * ie + 1], mm * P.normal[3 * ie + 2]};
+        if (isrc == 0) {
+          double out[4] = {0, 0, 0, 0};
+          tri_lap_regular(P.tri, v, s, n, P.area[ie], out);
+          integ = out[0]; inteH[0] = out[1]; inteH[1] = out[2]; inteH[2] = out[3];
+        } else {
+          integ = si_tri_lap(v, P.area[ie], isrc);
+        }
+      } else {
+        if (isrc == 0) {
+          double out[5];
+          quad_lap_regular(P.iqud, v, s, mm, out);
+          integ = out[0];
+          for (int k = 0; k < 4; ++k) inteH[k] = out[1 + k];
+        } else {
+          integ = si_qua_lap(v, isrc);
+        }
+      }
+      for (int j = 0; j < P.nno[ie]; ++j) rowH[P.con[4 * ie + j]] += inteH[j];
+      rowG[ie] = integ;
+    }
+  }
+  double c = 0.0;
+  for (int i = 0; i < P.nnodes; ++i) c -= rowH[i];
+  err = std::max(err, std::fabs(0.5 - c));
+  double shpf = (P.type[irow] == 2) ? 1.0 / 3.0 : 0.25;
+  for (int j = 0; j < P.nno[irow]; ++j) rowH[P.con[4 * irow + j]] += shpf * c;
+}
+
+// sdFormIntegralMatrices (lib_int.f90:225-323)
+static void lap_form_matrices(Problem& P) {
+  P.H.assign((size_t)P.nsp * P.sd_nnodes, 0.0);
+  P.G.assign((size_t)P.nsp * P.sd_nqnodes, 0.0);
+  double errU = 0.0, errQ = 0.0;
+#pragma omp parallel
+  {
+    std::vector<double> rowH(P.nnodes), rowG(P.nelem);
+    double eu = 0.0, eq = 0.0;
+#pragma omp for schedule(dynamic, 4)
+    for (int r = 0; r < P.nsp; ++r) {
+      if (r < P.sd_nnodes) lap_row_u(P, P.nodeList[r], rowH.data(), rowG.data(), eu);
+      else lap_row_q(P, P.qnodeList[r - P.sd_nnodes], rowH.data(), rowG.data(), eq);
+      for (int j = 0; j < P.sd_nnodes; ++j) P.H[(size_t)j * P.nsp + r] = rowH[P.nodeList[j]];
+      for (int j = 0; j < P.sd_nqnodes; ++j) P.G[(size_t)j * P.nsp + r] = rowG[P.qnodeList[j]];
+    }
+#pragma omp critical
+    { errU = std::max(errU, eu); errQ = std::max(errQ, eq); }
+  }
+  P.fspCerr = errU;
+  P.qspCerr = errQ;
+}
+
+// Stokes rows. Row arrays laid out [comp][n]: T comps 0..5 (xx,xy,xz,yy,yz,zz),
+// prT 6..8 over nnodes; G comps 0..5 and prG 6..8 over nelem.
+struct StkRow {
+  std::vector<double> T, G;  // 9*nnodes, 9*nelem
+  int nn, ne;
+  StkRow(int nn_, int ne_) : T(9 * (size_t)nn_), G(9 * (size_t)ne_), nn(nn_), ne(ne_) {}
+  double& t(int c, int i) { return T[(size_t)c * nn + i]; }
+  double& g(int c, int i) { return G[(size_t)c * ne + i]; }
+};
+
+static void stk_element(const Problem& P, int ie, const double s[3], int isrc, double mm, StkElem& E) {
+  double v[12];
+  element_vertices(P, ie, v);
+  E.zero();
+  if (P.type[ie] == 2) {
+    if (isrc == 0) {
+      double n[3] = {mm * P.normal[3 * ie], mm * P.normal[3 * ie + 1], mm * P.normal[3 * ie + 2]};
+      tri_stk_regular(P.tri, v, s, n, P.area[ie], E);
+    } else {
+      si_tri_stk(v, P.area[ie], isrc, E.G);  // T, prT, prG stay zero (lib_intAna.f90:136-148)
+    }
+  } else {
+    if (isrc == 0) quad_stk_regular(P.iqud, v, s, mm, E);
+    else si_qua_stk(v, isrc, E.G);  // Quad_StokesIntAna (lib_intAna.f90:43-82)
+  }
+}
+
+// sdIntRowQStokes (lib_Stokes.f90:1562-1897)
+static void stk_row_q(const Problem& P, int irow, StkRow& R, double& err) {
+  std::fill(R.T.begin(), R.T.end(), 0.0);
+  std::fill(R.G.begin(), R.G.end(), 0.0);
+  const double osemPi = (double)std::atan(1.0f) * 4.0 * 8.0;  // single-precision ATAN(1.0)
+  const double s[3] = {P.qx[3 * irow], P.qx[3 * irow + 1], P.qx[3 * irow + 2]};
+  StkElem E;
+  for (size_t jj = 0; jj < P.loWalls.size(); ++jj) {
+    int iWall = P.loWalls[jj];
+    double mm = P.normMul[jj];
+    for (int ie = 0; ie < P.nelem; ++ie) {
+      if (P.bcid[ie] != iWall) continue;
+      int isrc = 0;
+      if (ie == irow) isrc = (P.type[ie] == 2) ? 4 : 5;
+      stk_element(P, ie, s, isrc, mm, E);
+      for (int j = 0; j < P.nno[ie]; ++j)
+        for (int k = 0; k < 6; ++k) R.t(k, P.con[4 * ie + j]) += E.T[k][j];
+      for (int k = 0; k < 6; ++k) R.g(k, ie) = E.G[k];
+      if (isrc == 0) {
+        for (int j = 0; j < P.nno[ie]; ++j)
+          for (int k = 0; k < 3; ++k) R.t(6 + k, P.con[4 * ie + j]) += E.prT[k][j];
+        for (int k = 0; k < 3; ++k) R.g(6 + k, ie) = E.prG[k];
+      }
+    }
+  }
+  err = -9.99;
+  double cx = 0, cy = 0, cz = 0;
+  for (int i = 0; i < P.nnodes; ++i) { cx -= R.t(1, i); cy -= R.t(4, i); cz -= R.t(2, i); }
+  err = std::max(err, std::fabs(cx)); err = std::max(err, std::fabs(cy)); err = std::max(err, std::fabs(cz));
+  cx = cy = cz = 0;
+  for (int i = 0; i < P.nnodes; ++i) { cx -= R.t(0, i); cy -= R.t(3, i); cz -= R.t(5, i); }
+  err = std::max(err, std::fabs(cx - 0.5 * osemPi));
+  err = std::max(err, std::fabs(cy - 0.5 * osemPi));
+  err = std::max(err, std::fabs(cz - 0.5 * osemPi));
+  int ie = irow;
+  double shpf = (P.type[ie] == 2) ? 1.0 / 3.0 : 0.25;
+  for (int j = 0; j < P.nno[ie]; ++j) {
+    int nd = P.con[4 * ie + j];
+    R.t(0, nd) += shpf * cx; R.t(3, nd) += shpf * cy; R.t(5, nd) += shpf * cz;
+  }
+  cx = cy = cz = 0;
+  for (int j = 0; j < P.nnodes; ++j) { cx += R.t(6, j); cy += R.t(7, j); cz += R.t(8, j); }
+  for (int j = 0; j < P.nno[irow]; ++j) {
+    int nd = P.con[4 * irow + j];
+    R.t(6, nd) -= cx / P.nno[irow]; R.t(7, nd) -= cy / P.nno[irow]; R.t(8, nd) -= cz / P.nno[irow];
+  }
+}
+// sdIntRowUStokes (lib_Stokes.f90:1904-2245)
+static void stk_row_u(const Problem& P, int irow, StkRow& R, double& err) {
+  std::fill(R.T.begin(), R.T.end(), 0.0);
+  std::fill(R.G.begin(), R.G.end(), 0.0);
+  const double s[3] = {P.x[3 * irow], P.x[3 * irow + 1], P.x[3 * irow + 2]};
+  StkElem E;
+  for (size_t jj = 0; jj < P.loWalls.size(); ++jj) {
+    int iWall = P.loWalls[jj];
+    double mm = P.normMul[jj];
+    for (int ie = 0; ie < P.nelem; ++ie) {
+      if (P.bcid[ie] != iWall) continue;
+      int isrc = 0;
+      for (int j = 0; j < P.nno[ie]; ++j)
+        if (irow == P.con[4 * ie + j]) isrc = j + 1;
+      stk_element(P, ie, s, isrc, mm, E);
+      for (int j = 0; j < P.nno[ie]; ++j) {
+        int nd = P.con[4 * ie + j];
+        for (int k = 0; k < 6; ++k) R.t(k, nd) += E.T[k][j];
+        for (int k = 0; k < 3; ++k) R.t(6 + k, nd) += E.prT[k][j];
+      }
+      for (int k = 0; k < 6; ++k) R.g(k, ie) = E.G[k];
+      for (int k = 0; k < 3; ++k) R.g(6 + k, ie) = E.prG[k];
+    }
+  }
+  err = -9.99;
+  double cx = 0, cy = 0, cz = 0;
+  for (int i = 0; i < P.nnodes; ++i) { cx -= R.t(0, i); cy -= R.t(3, i); cz -= R.t(5, i); }
+  R.t(0, irow) += cx; R.t(3, irow) += cy; R.t(5, irow) += cz;
+  cx = cy = cz = 0;
+  for (int i = 0; i < P.nelem; ++i) {
+    double m = P.multiOf(P.bcid[i]);
+    const double* n = &P.normal[3 * i];
+    cx = cx - R.g(0, i) * n[0] * m - R.g(1, i) * n[1] * m - R.g(2, i) * n[2] * m;
+    cy = cy - R.g(1, i) * n[0] * m - R.g(3, i) * n[1] * m - R.g(4, i) * n[2] * m;
+    cz = cz - R.g(2, i) * n[0] * m - R.g(4, i) * n[1] * m - R.g(5, i) * n[2] * m;
+  }
+  err = std::max(err, std::fabs(cx)); err = std::max(err, std::fabs(cy)); err = std::max(err, std::fabs(cz));
+}
+
+// sdFormIntegralMatricesStokes (lib_Stokes.f90:1391-1555).  Matrix order in
+// P.M: 0..5 T(xx,xy,xz,yy,yz,zz), 6..8 prT, 9..14 G, 15..17 prG.
+static void stk_form_matrices(Problem& P) {
+  for (int k = 0; k < 9; ++k) P.M[k].assign((size_t)P.nsp * P.sd_nnodes, 0.0);
+  for (int k = 9; k < 18; ++k) P.M[k].assign((size_t)P.nsp * P.sd_nqnodes, 0.0);
+  double errU = -1e300, errQ = -1e300;
+#pragma omp parallel
+  {
+    StkRow R(P.nnodes, P.nelem);
+    double eu = -1e300, eq = -1e300;
+#pragma omp for schedule(dynamic, 4)
+    for (int r = 0; r < P.nsp; ++r) {
+      double e;
+      if (r < P.sd_nnodes) { stk_row_u(P, P.nodeList[r], R, e); eu = std::max(eu, e); }
+      else { stk_row_q(P, P.qnodeList[r - P.sd_nnodes], R, e); eq = std::max(eq, e); }
+      for (int k = 0; k < 9; ++k)
+        for (int j = 0; j < P.sd_nnodes; ++j) P.M[k][(size_t)j * P.nsp + r] = R.t(k, P.nodeList[j]);
+      for (int k = 0; k < 9; ++k)
+        for (int j = 0; j < P.sd_nqnodes; ++j) P.M[9 + k][(size_t)j * P.nsp + r] = R.g(k, P.qnodeList[j]);
+    }
+#pragma omp critical
+    { errU = std::max(errU, eu); errQ = std::max(errQ, eq); }
+  }
+  P.fspCerr = errU;
+  P.qspCerr = errQ;
+}
+
+// sdSetUpXandB (lib_sdBem.f90:4-107)
+static void setup_xb(Problem& P) {
+  const int notSet = -999;
+  P.eqn.assign(P.neq, Eqn());
+  for (int en = 0; en < P.neq; ++en) {
+    Eqn& E = P.eqn[en];
+    E.col.assign(P.nnodes, notSet);
+    E.qcol.assign(P.nelem, notSet);
+    for (int i = 0; i < P.sd_nnodes; ++i) {
+      int isp = P.nodeList[i], bc = P.knownOf(en, P.BCidList[i]);
+      if (bc == iFunction) { E.nb++; E.col[isp] = E.nb; }
+      else if (bc == iFlux) { E.nx++; E.col[isp] = E.nx; E.neq++; }
+      else if (bc == iContact) { E.neq++; if (E.col[isp] == notSet) { E.nx++; E.col[isp] = E.nx; } }
+    }
+    for (int i = 0; i < P.sd_nqnodes; ++i) {
+      int isp = P.qnodeList[i], bc = P.knownOf(en, P.qbcidList[i]);
+      if (bc == iFunction) { E.nx++; E.qcol[isp] = E.nx; E.neq++; }
+      else if (bc == iFlux) { E.nb++; E.qcol[isp] = E.nb; }
+      else if (bc == iContact) { E.neq++; if (E.qcol[isp] == notSet) { E.nx++; E.qcol[isp] = E.nx; } }
+    }
+    E.x.assign(E.nx, 0.0);
+    E.pivot.assign(E.nx, 0.0);
+    E.b.assign(E.nb, 0.0);
+    E.u.assign(P.nnodes, 0.0);
+    E.q.assign(P.nelem, 0.0);
+  }
+}
+
+// sdSetUpSysMrhsM_CRS (lib_CRS.f90:148-343): Laplace, no zero dropping
+static void lap_form_crs(Problem& P, int en) {
+  Eqn& E = P.eqn[en];
+  CRS &S = E.sys, &Rm = E.rhs;
+  S = CRS(); Rm = CRS();
+  S.neq = Rm.neq = E.neq;
+  S.i.assign(E.neq + 1, 0); Rm.i.assign(E.neq + 1, 0);
+  int row = 0, r = 0;
+  auto emitH = [&](int rr) {
+    for (int j = 0; j < P.sd_nnodes; ++j) {
+      int col = E.col[P.nodeList[j]], bc = P.knownOf(en, P.BCidList[j]);
+      double val = P.H[(size_t)j * P.nsp + rr];
+      if (bc == iFunction) { Rm.v.push_back(val); Rm.j.push_back(col); }
+      if (bc == iFlux || bc == iContact) { S.v.push_back(val); S.j.push_back(col); }
+    }
+    for (int j = 0; j < P.sd_nqnodes; ++j) {
+      int col = E.qcol[P.qnodeList[j]], wallC = P.qbcidList[j], bc = P.knownOf(en, wallC);
+      double val = P.multiOf(wallC) / P.diff * P.G[(size_t)j * P.nsp + rr];
+      if (bc == iFunction || bc == iContact) { S.v.push_back(val); S.j.push_back(col); }
+      if (bc == iFlux) { Rm.v.push_back(val); Rm.j.push_back(col); }
+    }
+  };
+  for (int i = 0; i < P.sd_nnodes; ++i, ++r) {
+    int bc = P.knownOf(en, P.BCidList[i]);
+    if (bc == iFlux || bc == iContact) {
+      S.i[row] = (int64_t)S.v.size() + 1; Rm.i[row] = (int64_t)Rm.v.size() + 1; row++;
+      emitH(r);
+    }
+  }
+  for (int i = 0; i < P.sd_nqnodes; ++i, ++r) {
+    int bc = P.knownOf(en, P.qbcidList[i]);
+    if (bc == iFunction || bc == iContact) {
+      S.i[row] = (int64_t)S.v.size() + 1; Rm.i[row] = (int64_t)Rm.v.size() + 1; row++;
+      emitH(r);
+    }
+  }
+  S.i[row] = (int64_t)S.v.size() + 1;
+  Rm.i[row] = (int64_t)Rm.v.size() + 1;
+  S.nnz = (int64_t)S.v.size();
+  Rm.nnz = (int64_t)Rm.v.size();
+}
+
+// StokesBigSystemXB (lib_Stokes.f90:1180-1276)
+static void stk_setup_xb(Problem& P) {
+  Eqn& S = P.stk;
+  S = Eqn();
+  S.col.assign(3 * P.nnodes, -999);
+  S.qcol.assign(3 * P.nelem, -999);
+  for (int i = 0; i < P.sd_nnodes; ++i) {
+    int isp = P.nodeList[i], wall = P.BCidList[i];
+    S.nx = S.nb = S.neq = 0;
+    for (int en = 0; en < 3; ++en) {
+      int ispL = isp + en * P.nnodes, bc = P.knownOf(en, wall);
+      if (bc == iFunction) S.col[ispL] = P.eqn[en].col[isp] + S.nb;
+      else if (bc == iFlux || bc == iContact) S.col[ispL] = P.eqn[en].col[isp] + S.nx;
+      S.nx += P.eqn[en].nx; S.nb += P.eqn[en].nb; S.neq += P.eqn[en].neq;
+    }
+  }
+  for (int i = 0; i < P.sd_nqnodes; ++i) {
+    int isp = P.qnodeList[i], wall = P.qbcidList[i];
+    S.nx = S.nb = S.neq = 0;
+    for (int en = 0; en < 3; ++en) {
+      int ispL = isp + en * P.nelem, bc = P.knownOf(en, wall);
+      if (bc == iFunction || bc == iContact) S.qcol[ispL] = P.eqn[en].qcol[isp] + S.nx;
+      else if (bc == iFlux) S.qcol[ispL] = P.eqn[en].qcol[isp] + S.nb;
+      S.nx += P.eqn[en].nx; S.nb += P.eqn[en].nb; S.neq += P.eqn[en].neq;
+    }
+  }
+  S.x.assign(S.nx, 0.0);
+  S.pivot.assign(S.nx, 0.0);
+  S.b.assign(S.nb, 0.0);
+}
+
+// Index of the Stokes component matrix for (een, en): T uses 0..5, G uses 9..14
+static int symIndex(int a, int b) {
+  if (a > b) std::swap(a, b);
+  static const int tab[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+  return tab[a][b];
+}
+
+// formQrow / formUrow (lib_StokesFull.f90:4-167): one row of sysM and rhsM
+static void stk_form_row(const Problem& P, int een, int r, std::vector<double>& sysRow, std::vector<double>& rhsRow) {
+  const Eqn& S = P.stk;
+  std::fill(sysRow.begin(), sysRow.end(), 0.0);
+  std::fill(rhsRow.begin(), rhsRow.end(), 0.0);
+  for (int j = 0; j < P.sd_nnodes; ++j) {
+    int wallC = P.BCidList[j], isp = P.nodeList[j];
+    for (int en = 0; en < 3; ++en) {
+      int col = S.col[isp + en * P.nnodes], bc = P.knownOf(en, wallC);
+      double val = P.M[symIndex(een, en)][(size_t)j * P.nsp + r];
+      if (bc == iFunction) rhsRow[col - 1] = val;
+      if (bc == iFlux || bc == iContact) sysRow[col - 1] = -val;
+    }
+  }
+  for (int j = 0; j < P.sd_nqnodes; ++j) {
+    int wallC = P.qbcidList[j], isp = P.qnodeList[j];
+    for (int en = 0; en < 3; ++en) {
+      int col = S.qcol[isp + en * P.nelem], bc = P.knownOf(en, wallC);
+      double val = P.M[9 + symIndex(een, en)][(size_t)j * P.nsp + r];
+      val = P.multiOf(wallC) / P.diff * val;
+      if (bc == iFunction || bc == iContact) sysRow[col - 1] = -val;
+      if (bc == iFlux) rhsRow[col - 1] = val;
+    }
+  }
+}
+
+// stokesFormCRSsysMrhsM (lib_Stokes.f90:475-637): CRS with exact zeros dropped
+static void stk_form_crs(Problem& P) {
+  Eqn& S = P.stk;
+  S.neq = 0;
+  for (int en = 0; en < 3; ++en) S.neq += P.eqn[en].neq;
+  CRS &A = S.sys, &B = S.rhs;
+  A = CRS(); B = CRS();
+  A.neq = B.neq = S.neq;
+  A.i.assign(S.neq + 1, 0); B.i.assign(S.neq + 1, 0);
+  std::vector<double> sysRow(S.neq > S.nx ? S.neq : S.nx), rhsRow(std::max(S.nb, 1));
+  sysRow.assign(std::max(S.neq, S.nx), 0.0);
+  int row = 0, r = 0;
+  auto emit = [&](int een, int rr) {
+    A.i[row] = (int64_t)A.v.size() + 1; B.i[row] = (int64_t)B.v.size() + 1; row++;
+    stk_form_row(P, een, rr, sysRow, rhsRow);
+    for (int col = 0; col < S.nx; ++col)
+      if (sysRow[col] != 0.0) { A.v.push_back(sysRow[col]); A.j.push_back(col + 1); }
+    for (int col = 0; col < S.nb; ++col)
+      if (rhsRow[col] != 0.0) { B.v.push_back(rhsRow[col]); B.j.push_back(col + 1); }
+  };
+  for (int i = 0; i < P.sd_nnodes; ++i, ++r)
+    for (int een = 0; een < 3; ++een) {
+      int bc = P.knownOf(een, P.BCidList[i]);
+      if (bc == iFlux || bc == iContact) emit(een, r);
+    }
+  for (int i = 0; i < P.sd_nqnodes; ++i, ++r)
+    for (int een = 0; een < 3; ++een) {
+      int bc = P.knownOf(een, P.qbcidList[i]);
+      if (bc == iFunction || bc == iContact) emit(een, r);
+    }
+  A.i[row] = (int64_t)A.v.size() + 1;
+  B.i[row] = (int64_t)B.v.size() + 1;
+  A.nnz = (int64_t)A.v.size();
+  B.nnz = (int64_t)B.v.size();
+}
+
+// CRSxV (lib_CRS.f90:764-787)
+static void crs_x_v(const CRS& M, const double* vek, double* rez) {
+  for (int i = 0; i < M.neq; ++i) {
+    double s = 0.0;
+    for (int64_t j = M.i[i]; j <= M.i[i + 1] - 1; ++j) s += M.v[j - 1] * vek[M.j[j - 1] - 1];
+    rez[i] = s;
+  }
+}
+
+// -----------------------------------------------------------------------------
+// LSQR (lib_lsqr.f) with reference-BLAS level-1 semantics
+// -----------------------------------------------------------------------------
+// dnrm2: scaled sum of squares (reference BLAS 3.x algorithm)
+static double dnrm2(int n, const double* x) {
+  if (n < 1) return 0.0;
+  if (n == 1) return std::fabs(x[0]);
+  double scale = 0.0, ssq = 1.0;
+  for (int i = 0; i < n; ++i) {
+    if (x[i] != 0.0) {
+      double a = std::fabs(x[i]);
+      if (scale < a) { ssq = 1.0 + ssq * (scale / a) * (scale / a); scale = a; }
+      else ssq += (a / scale) * (a / scale);
+    }
+  }
+  return scale * std::sqrt(ssq);
+}
+static void dscal(int n, double a, double* x) { for (int i = 0; i < n; ++i) x[i] *= a; }
+// lsqr_d2norm (lib_lsqr.f:1236-1263)
+static double d2norm(double a, double b) {
+  double scale = std::fabs(a) + std::fabs(b);
+  if (scale == 0.0) return 0.0;
+  return scale * std::sqrt((a / scale) * (a / scale) + (b / scale) * (b / scale));
+}
+struct CrsView { int m, n; int64_t nnz; const int64_t* ia; const int* ja; double* a; };
+// lsqr_matvec1: y = y + A x (lib_lsqr.f:203-233)
+static void matvec1(const CrsView& A, const double* x, double* y) {
+  for (int i = 0; i < A.m; ++i) {
+    double s = 0.0;
+    for (int64_t j = A.ia[i]; j <= A.ia[i + 1] - 1; ++j) s += A.a[j - 1] * x[A.ja[j - 1] - 1];
+    y[i] += s;
+  }
+}
+// lsqr_tmatvec2: x = x + A^T y (lib_lsqr.f:237-263)
+static void tmatvec2(const CrsView& A, const double* y, double* x) {
+  for (int j = 0; j < A.m; ++j)
+    for (int64_t i = A.ia[j]; i <= A.ia[j + 1] - 1; ++i) x[A.ja[i - 1] - 1] += A.a[i - 1] * y[j];
+}
+
+struct LsqrStats { int istop, itn; double anorm, acond, rnorm, arnorm, xnorm; };
+
+// lsqr_LSQR (lib_lsqr.f:470-1231), damp = 0, wantse = false
+static LsqrStats lsqr_core(const CrsView& A, double* u, double* x, double* v, double* w, double atol, double btol,
+                           double conlim, int itnlim) {
+  const int m = A.m, n = A.n;
+  LsqrStats S{};
+  const double zero = 0.0, one = 1.0, damp = 0.0;
+  int itn = 0, istop = 0, nstop = 0;
+  double ctol = zero;
+  if (conlim > zero) ctol = one / conlim;
+  double anorm = 0, acond = 0, dnorm = 0, dxmax = 0, res2 = 0, psi = 0, xnorm = 0, xnorm1 = 0, cs2 = -one, sn2 = 0, z = 0;
+  for (int i = 0; i < n; ++i) { v[i] = zero; x[i] = zero; }
+  double alpha = zero, beta = dnrm2(m, u);
+  if (beta > zero) {
+    dscal(m, one / beta, u);
+    tmatvec2(A, u, v);
+    alpha = dnrm2(n, v);
+  }
+  if (alpha > zero) {
+    dscal(n, one / alpha, v);
+    for (int i = 0; i < n; ++i) w[i] = v[i];
+  }
+  double arnorm = alpha * beta;
+  double rnorm = beta, bnorm = beta, rhobar = alpha, phibar = beta;
+  if (arnorm == zero) goto done;
+  for (;;) {
+    itn++;
+    dscal(m, -alpha, u);
+    matvec1(A, v, u);
+    beta = dnrm2(m, u);
+    {
+      double temp = d2norm(alpha, beta);
+      temp = d2norm(temp, damp);
+      anorm = d2norm(anorm, temp);
+    }
+    if (beta > zero) {
+      dscal(m, one / beta, u);
+      dscal(n, -beta, v);
+      tmatvec2(A, u, v);
+      alpha = dnrm2(n, v);
+      if (alpha > zero) dscal(n, one / alpha, v);
+    }
+    double rhbar1 = rhobar;
+    double rho = d2norm(rhbar1, beta);
+    double cs = rhbar1 / rho, sn = beta / rho;
+    double theta = sn * alpha;
+    rhobar = -cs * alpha;
+    double phi = cs * phibar;
+    phibar = sn * phibar;
+    double tau = sn * phi;
+    double t1 = phi / rho, t2 = -theta / rho, t3 = one / rho, dknorm = zero;
+    for (int i = 0; i < n; ++i) {
+      double t = w[i];
+      x[i] = t1 * t + x[i];
+      w[i] = t2 * t + v[i];
+      dknorm = (t3 * t) * (t3 * t) + dknorm;
+    }
+    dknorm = std::sqrt(dknorm);
+    dnorm = d2norm(dnorm, dknorm);
+    double dxk = std::fabs(phi * dknorm);
+    if (dxmax < dxk) dxmax = dxk;
+    double delta = sn2 * rho, gambar = -cs2 * rho;
+    double rhs = phi - delta * z;
+    double zbar = rhs / gambar;
+    xnorm = d2norm(xnorm1, zbar);
+    double gamma = d2norm(gambar, theta);
+    cs2 = gambar / gamma;
+    sn2 = theta / gamma;
+    z = rhs / gamma;
+    xnorm1 = d2norm(xnorm1, z);
+    acond = anorm * dnorm;
+    res2 = d2norm(res2, psi);
+    rnorm = d2norm(res2, phibar);
+    arnorm = alpha * std::fabs(tau);
+    double test1 = rnorm / bnorm;
+    double test2 = zero;
+    if (rnorm > zero) test2 = arnorm / (anorm * rnorm);
+    double test3 = one / acond;
+    double tt1 = test1 / (one + anorm * xnorm / bnorm);
+    double rtol = btol + atol * anorm * xnorm / bnorm;
+    double tt3 = one + test3, tt2 = one + test2;
+    tt1 = one + tt1;
+    if (itn >= itnlim) istop = 5;
+    if (tt3 <= one) istop = 4;
+    if (tt2 <= one) istop = 2;
+    if (tt1 <= one) istop = 1;
+    if (test3 <= ctol) istop = 4;
+    if (test2 <= atol) istop = 2;
+    if (test1 <= rtol) istop = 1;
+    if (istop == 0) nstop = 0;
+    else {
+      int nconv = 1;
+      nstop++;
+      if (nstop < nconv && itn < itnlim) istop = 0;
+    }
+    if (istop != 0) break;
+  }
+done:
+  S.istop = istop; S.itn = itn; S.anorm = anorm; S.acond = acond; S.rnorm = rnorm; S.arnorm = arnorm; S.xnorm = xnorm;
+  return S;
+}
+
+// lsqr_precon (lib_lsqr.f:131-167): q = 1/||A(:,j)||, A <- A diag(q) in place
+static void lsqr_precon(int m, int n, int64_t nnz, double* q, const int64_t* ia, const int* ja, double* a) {
+  (void)nnz;
+  for (int i = 0; i < n; ++i) q[i] = 0.0;
+  for (int j = 0; j < m; ++j)
+    for (int64_t i = ia[j]; i <= ia[j + 1] - 1; ++i) q[ja[i - 1] - 1] += a[i - 1] * a[i - 1];
+  for (int i = 0; i < n; ++i) q[i] = 1.0 / std::sqrt(q[i]);
+  for (int i = 0; i < m; ++i)
+    for (int64_t ij = ia[i]; ij <= ia[i + 1] - 1; ++ij) a[ij - 1] *= q[ja[ij - 1] - 1];
+}
+
+// lsqr_solve (lib_lsqr.f:33-127)
+static LsqrStats lsqr_solve(int m, int n, int64_t nnz, int& maxit, double eps, int& nit, int& ierr, const double* q,
+                            const int64_t* ia, const int* ja, double* a, const double* b, double* x) {
+  std::vector<double> x0(n), wm(m, 0.0), u(m), v(n), w(n);
+  const double conlim = 1.0e8;
+  if (maxit == 0) maxit = 10 * (m + n + 50);
+  for (int i = 0; i < n; ++i) x0[i] = x[i];
+  for (int i = 0; i < n; ++i) x[i] = x[i] / q[i];
+  CrsView A{m, n, nnz, ia, ja, a};
+  matvec1(A, x, wm.data());
+  for (int i = 0; i < m; ++i) u[i] = b[i] - wm[i];
+  double nrm_r = dnrm2(m, u.data()), nrm_b = dnrm2(m, b);
+  double atol = eps, btol = eps * nrm_b / nrm_r;
+  LsqrStats S = lsqr_core(A, u.data(), x, v.data(), w.data(), atol, btol, conlim, maxit);
+  nit = S.itn;
+  for (int i = 0; i < n; ++i) x[i] = q[i] * x[i];
+  for (int i = 0; i < n; ++i) x[i] = x0[i] + x[i];
+  ierr = (S.istop > 3) ? S.istop : 0;
+  return S;
+}
+
+// CalFluxIntegralSingleWall (lib_particle.f90:1880-1904) and
+// getTorqueIntegrateFluxes (lib_particle.f90:1793-1831)
+static void force_torque(const Problem& P, const double* qx, const double* qy, const double* qz, int wall, double F[3],
+                         double T[3]) {
+  F[0] = F[1] = F[2] = 0.0;
+  T[0] = T[1] = T[2] = 0.0;
+  for (int i = 0; i < P.nelem; ++i)
+    if (P.bcid[i] == wall) {
+      F[0] += P.area[i] * qx[i]; F[1] += P.area[i] * qy[i]; F[2] += P.area[i] * qz[i];
+    }
+  for (int i = 0; i < P.nelem; ++i) {
+    if (P.bcid[i] != wall) continue;
+    double q[3] = {qx[i], qy[i], qz[i]}, r[3] = {0, 0, 0}, cp[3];
+    for (int in = 0; in < P.nno[i]; ++in)
+      for (int j = 0; j < 3; ++j) r[j] += P.x[3 * P.con[4 * i + in] + j];
+    for (int j = 0; j < 3; ++j) r[j] /= (double)P.nno[i];
+    cp[0] = r[1] * q[2] - r[2] * q[1];
+    cp[1] = -r[0] * q[2] + r[2] * q[0];
+    cp[2] = r[0] * q[1] - r[1] * q[0];
+    for (int j = 0; j < 3; ++j) T[j] += P.area[i] * cp[j];
+  }
+}
+
+}  // namespace orc
+
+using namespace orc;
+
+// =============================================================================
+// C API used by the tests (ctypes)
+// =============================================================================
+extern "C" {
+
+int orc_wx_rule(int itri, double* l1, double* l2, double* l3, double* w) {
+  TriRule r = wx_rule(itri);
+  for (int i = 0; i < r.n; ++i) { l1[i] = r.l1[i]; l2[i] = r.l2[i]; l3[i] = r.l3[i]; w[i] = r.w[i]; }
+  return r.n;
+}
+
+// Triangle_TestIntegration (mod_trikotnik.f90:108-191): out = integ1..integ4
+void orc_triangle_test(int itri, double out[4]) {
+  TriRule R = wx_rule(itri);
+  double x1 = 0, y1 = 0, z1 = 1, x2 = 2, y2 = 0, z2 = 1, x3 = 2, y3 = 2, z3 = 1, sx = 0, sy = 0, sz = 1;
+  double area = tri_area(x1, y1, z1, x2, y2, z2, x3, y3, z3);
+  double i1 = 0, i2 = 0, i3 = 0, i4 = 0;
+  for (int i = 0; i < R.n; ++i) {
+    double x = R.l1[i] * x1 + R.l2[i] * x2 + R.l3[i] * x3;
+    double y = R.l1[i] * y1 + R.l2[i] * y2 + R.l3[i] * y3;
+    double z = R.l1[i] * z1 + R.l2[i] * z2 + R.l3[i] * z3;
+    i1 += R.w[i] * std::pow(x, 10) * std::pow(y, 10);
+    i2 += R.w[i] * std::sin(x * y);
+    i3 += R.w[i] * std::exp(-x * y);
+    i4 += R.w[i] / std::sqrt((x - sx) * (x - sx) + (y - sy) * (y - sy) + (z - sz) * (z - sz));
+  }
+  out[0] = i1 * area; out[1] = i2 * area; out[2] = i3 * area;
+  out[3] = i4 * area / (16.0 * std::atan(1.0));
+}
+
+double orc_tri_area(const double v[9]) { return tri_area(v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], v[8]); }
+double orc_si_tri_lap(const double v[9], int isrc) { return si_tri_lap(v, orc_tri_area(v), isrc); }
+void orc_si_tri_stk(const double v[9], int isrc, double G[6]) { si_tri_stk(v, orc_tri_area(v), isrc, G); }
+double orc_si_qua_lap(const double q[12], int isrc) { return si_qua_lap(q, isrc); }
+void orc_si_qua_stk(const double q[12], int isrc, double G[6]) { si_qua_stk(q, isrc, G); }
+
+// Regular (non-singular) element integrals, for kernel-level checks.
+// Triangle Laplace: out = {G, H1, H2, H3}; n is the (already multiplied) normal.
+void orc_tri_lap_regular(int itri, const double v[9], const double s[3], const double n[3], double out[4]) {
+  TriRule R = wx_rule(itri);
+  for (int k = 0; k < 4; ++k) out[k] = 0.0;
+  tri_lap_regular(R, v, s, n, orc_tri_area(v), out);
+}
+// Triangle Stokes: out = G[6], prG[3], T[6][3], prT[3][3]
+void orc_tri_stk_regular(int itri, const double v[9], const double s[3], const double n[3], double out[36]) {
+  TriRule R = wx_rule(itri);
+  StkElem E;
+  E.zero();
+  tri_stk_regular(R, v, s, n, orc_tri_area(v), E);
+  int p = 0;
+  for (int k = 0; k < 6; ++k) out[p++] = E.G[k];
+  for (int k = 0; k < 3; ++k) out[p++] = E.prG[k];
+  for (int k = 0; k < 6; ++k) for (int j = 0; j < 3; ++j) out[p++] = E.T[k][j];
+  for (int k = 0; k < 3; ++k) for (int j = 0; j < 3; ++j) out[p++] = E.prT[k][j];
+}
+
+// ---- problem object ----------------------------------------------------------
+// kind 1 = Laplace (1 equation), 2 = Stokes (3 equations).  known[en*nwalls+k]
+// is the BC type (1 function, 2 flux, 3 contact) of equation en on wall walls[k].
+void* orc_problem_create(int kind, int nnodes, const double* xyz, int nelem, const int* etype, const int* con,
+                         const int* bcid, int nwalls, const int* walls, const double* normMul, double diff,
+                         const int* known, int itri, int iqud) {
+  Problem* P = new Problem();
+  P->kind = kind;
+  P->neq = (kind == 2) ? 3 : 1;
+  P->nnodes = nnodes;
+  P->nelem = nelem;
+  P->x.assign(xyz, xyz + 3 * (size_t)nnodes);
+  P->type.assign(etype, etype + nelem);
+  P->nno.resize(nelem);
+  for (int e = 0; e < nelem; ++e) P->nno[e] = (etype[e] == 2) ? 3 : 4;
+  P->con.assign(con, con + 4 * (size_t)nelem);
+  P->bcid.assign(bcid, bcid + nelem);
+  P->loWalls.assign(walls, walls + nwalls);
+  P->normMul.assign(normMul, normMul + nwalls);
+  P->diff = diff;
+  P->known.assign(known, known + P->neq * nwalls);
+  P->tri = wx_rule(itri);
+  P->iqud = iqud;
+  geometry(*P);
+  setup_subdomain(*P);
+  setup_xb(*P);
+  if (kind == 2) stk_setup_xb(*P);
+  return P;
+}
+void orc_problem_destroy(void* h) { delete (Problem*)h; }
+
+// sizes: [nsp, sd_nnodes, sd_nqnodes, neq_rows, nx, nb] of the (big) system
+void orc_problem_sizes(void* h, int out[6]) {
+  Problem* P = (Problem*)h;
+  out[0] = P->nsp; out[1] = P->sd_nnodes; out[2] = P->sd_nqnodes;
+  if (P->kind == 2) {
+    int neq = 0;
+    for (int en = 0; en < 3; ++en) neq += P->eqn[en].neq;
+    out[3] = neq; out[4] = P->stk.nx; out[5] = P->stk.nb;
+  } else {
+    out[3] = P->eqn[0].neq; out[4] = P->eqn[0].nx; out[5] = P->eqn[0].nb;
+  }
+}
+void orc_geometry(void* h, double* normal, double* area, double* centroid) {
+  Problem* P = (Problem*)h;
+  std::copy(P->normal.begin(), P->normal.end(), normal);
+  std::copy(P->area.begin(), P->area.end(), area);
+  std::copy(P->qx.begin(), P->qx.end(), centroid);
+}
+void orc_lists(void* h, int* nodeList, int* qnodeList) {
+  Problem* P = (Problem*)h;
+  std::copy(P->nodeList.begin(), P->nodeList.end(), nodeList);
+  std::copy(P->qnodeList.begin(), P->qnodeList.end(), qnodeList);
+}
+
+// CoR_Integrals: fills the dense integral matrices; errs = {fspCerr, qspCerr}
+void orc_form_integrals(void* h, double errs[2]) {
+  Problem* P = (Problem*)h;
+  if (P->kind == 2) stk_form_matrices(*P);
+  else lap_form_matrices(*P);
+  errs[0] = P->fspCerr;
+  errs[1] = P->qspCerr;
+}
+// Copy one integral matrix (column-major nsp x ncols).  Laplace: 0 H, 1 G.
+// Stokes: 0..17 in the order Txx,Txy,Txz,Tyy,Tyz,Tzz,prTx,prTy,prTz,Gxx..Gzz,prGx..prGz.
+void orc_get_integral_matrix(void* h, int which, double* out) {
+  Problem* P = (Problem*)h;
+  const std::vector<double>& M = (P->kind == 2) ? P->M[which] : (which == 0 ? P->H : P->G);
+  std::copy(M.begin(), M.end(), out);
+}
+// One row of integrals for a source point (row r of the nsp rows), full-length
+// over global nodes / elements.  Laplace: rowH(nnodes), rowG(nelem).
+// Stokes: rowT(9*nnodes) rowG(9*nelem) in the component order above.
+double orc_integral_row(void* h, int r, double* rowT, double* rowG) {
+  Problem* P = (Problem*)h;
+  double err = 0.0;
+  if (P->kind == 2) {
+    StkRow R(P->nnodes, P->nelem);
+    if (r < P->sd_nnodes) stk_row_u(*P, P->nodeList[r], R, err);
+    else stk_row_q(*P, P->qnodeList[r - P->sd_nnodes], R, err);
+    std::copy(R.T.begin(), R.T.end(), rowT);
+    std::copy(R.G.begin(), R.G.end(), rowG);
+  } else {
+    if (r < P->sd_nnodes) lap_row_u(*P, P->nodeList[r], rowT, rowG, err);
+    else lap_row_q(*P, P->qnodeList[r - P->sd_nnodes], rowT, rowG, err);
+  }
+  return err;
+}
+
+// System formation (CRS, 1-based) -- Laplace: per equation 0; Stokes: big system
+void orc_form_system(void* h) {
+  Problem* P = (Problem*)h;
+  if (P->kind == 2) stk_form_crs(*P);
+  else lap_form_crs(*P, 0);
+}
+static CRS& pick_crs(Problem* P, int which) {
+  Eqn& E = (P->kind == 2) ? P->stk : P->eqn[0];
+  return which == 0 ? E.sys : E.rhs;
+}
+int64_t orc_crs_nnz(void* h, int which) { return pick_crs((Problem*)h, which).nnz; }
+void orc_get_crs(void* h, int which, int64_t* ia, int* ja, double* a) {
+  CRS& C = pick_crs((Problem*)h, which);
+  std::copy(C.i.begin(), C.i.end(), ia);
+  std::copy(C.j.begin(), C.j.end(), ja);
+  std::copy(C.v.begin(), C.v.end(), a);
+}
+
+// Plain lsqr_precon / lsqr_solve with the reference signature (1-based CRS).
+void orc_lsqr_precon(int m, int n, int64_t nnz, double* q, const int64_t* ia, const int* ja, double* a) {
+  lsqr_precon(m, n, nnz, q, ia, ja, a);
+}
+void orc_lsqr_solve(int m, int n, int64_t nnz, int* maxit, double eps, int* nit, int* ierr, const double* q,
+                    const int64_t* ia, const int* ja, double* a, const double* b, double* x, double stats[7]) {
+  LsqrStats S = lsqr_solve(m, n, nnz, *maxit, eps, *nit, *ierr, q, ia, ja, a, b, x);
+  if (stats) {
+    stats[0] = S.istop; stats[1] = S.itn; stats[2] = S.anorm; stats[3] = S.acond; stats[4] = S.rnorm;
+    stats[5] = S.arnorm; stats[6] = S.xnorm;
+  }
+}
+
+// Laplace solve (laplace.f90:1-52 + sdSolveCRS lib_CRS.f90:4-142) for known
+// nodal u (function walls) / element q (flux walls).  u_io(nnodes), q_io(nelem)
+// hold the known values and the initial guess; on return the unknowns.
+int orc_laplace_solve(void* h, double* u_io, double* q_io, int maxit, double eps, int* nit) {
+  Problem* P = (Problem*)h;
+  if (P->kind != 1) return -1;
+  if (P->H.empty()) { double e[2]; orc_form_integrals(h, e); }
+  lap_form_crs(*P, 0);
+  Eqn& E = P->eqn[0];
+  E.u.assign(u_io, u_io + P->nnodes);
+  E.q.assign(q_io, q_io + P->nelem);
+  for (int i = 0; i < P->sd_nnodes; ++i) {
+    int isp = P->nodeList[i], bc = P->knownOf(0, P->BCidList[i]);
+    if (bc == iFunction) E.b[E.col[isp] - 1] = E.u[isp];
+    else E.x[E.col[isp] - 1] = E.u[isp];
+  }
+  for (int i = 0; i < P->sd_nqnodes; ++i) {
+    int isp = P->qnodeList[i], bc = P->knownOf(0, P->qbcidList[i]);
+    if (bc == iFlux) E.b[E.qcol[isp] - 1] = E.q[isp];
+    else E.x[E.qcol[isp] - 1] = E.q[isp];
+  }
+  std::vector<double> nb(E.nb), b(E.neq);
+  for (int i = 0; i < E.nb; ++i) nb[i] = -E.b[i];
+  crs_x_v(E.rhs, nb.data(), b.data());
+  lsqr_precon(E.sys.neq, E.nx, E.sys.nnz, E.pivot.data(), E.sys.i.data(), E.sys.j.data(), E.sys.v.data());
+  int ierr = 0, mi = maxit;
+  lsqr_solve(E.sys.neq, E.nx, E.sys.nnz, mi, eps, *nit, ierr, E.pivot.data(), E.sys.i.data(), E.sys.j.data(),
+             E.sys.v.data(), b.data(), E.x.data());
+  for (int i = 0; i < P->sd_nnodes; ++i) {
+    int isp = P->nodeList[i], bc = P->knownOf(0, P->BCidList[i]);
+    E.u[isp] = (bc == iFunction) ? E.b[E.col[isp] - 1] : E.x[E.col[isp] - 1];
+  }
+  for (int i = 0; i < P->sd_nqnodes; ++i) {
+    int isp = P->qnodeList[i], bc = P->knownOf(0, P->qbcidList[i]);
+    E.q[isp] = (bc == iFlux) ? E.b[E.qcol[isp] - 1] : E.x[E.qcol[isp] - 1];
+  }
+  std::copy(E.u.begin(), E.u.end(), u_io);
+  std::copy(E.q.begin(), E.q.end(), q_io);
+  return ierr;
+}
+
+// Stokes: form CRS and precondition once (stokes.f90:109-110); then solve for
+// a sequence of boundary states like the 3-sides workflows
+// (lib_particle.f90:6-476): u_io[nrhs][3][nnodes] known velocities,
+// q_io[nrhs][3][nelem] receives tractions.  x is warm-started from the previous
+// right-hand side's solution exactly as the reference does through eqn%q.
+// Returns F and T on wall `fwall` per rhs: ft[nrhs][6].
+int orc_stokes_solve_sequence(void* h, int nrhs, const double* u_in, double* q_out, int maxit, double eps,
+                              int fwall, double* ft, int* nits) {
+  Problem* P = (Problem*)h;
+  if (P->kind != 2) return -1;
+  if (P->M[0].empty()) { double e[2]; orc_form_integrals(h, e); }
+  stk_form_crs(*P);
+  Eqn& S = P->stk;
+  lsqr_precon(S.sys.neq, S.nx, S.sys.nnz, S.pivot.data(), S.sys.i.data(), S.sys.j.data(), S.sys.v.data());
+  for (int en = 0; en < 3; ++en) { P->eqn[en].q.assign(P->nelem, 0.0); }
+  int ierr_all = 0;
+  for (int r = 0; r < nrhs; ++r) {
+    for (int en = 0; en < 3; ++en)
+      P->eqn[en].u.assign(u_in + ((size_t)r * 3 + en) * P->nnodes, u_in + ((size_t)r * 3 + en + 1) * P->nnodes);
+    // formStokesLeftRightHandSideVectors (lib_StokesFull.f90:379-438)
+    for (int i = 0; i < P->sd_nnodes; ++i) {
+      int isp = P->nodeList[i], wall = P->BCidList[i];
+      for (int en = 0; en < 3; ++en) {
+        int ispL = isp + en * P->nnodes, bc = P->knownOf(en, wall);
+        if (bc == iFunction) S.b[S.col[ispL] - 1] = P->eqn[en].u[isp];
+        else S.x[S.col[ispL] - 1] = P->eqn[en].u[isp];
+      }
+    }
+    for (int i = 0; i < P->sd_nqnodes; ++i) {
+      int isp = P->qnodeList[i], wall = P->qbcidList[i];
+      for (int en = 0; en < 3; ++en) {
+        int ispL = isp + en * P->nelem, bc = P->knownOf(en, wall);
+        if (bc == iFlux) S.b[S.qcol[ispL] - 1] = P->eqn[en].q[isp];
+        else S.x[S.qcol[ispL] - 1] = P->eqn[en].q[isp];
+      }
+    }
+    std::vector<double> b(S.sys.neq);
+    crs_x_v(S.rhs, S.b.data(), b.data());
+    int ierr = 0, nit = 0, mi = maxit;
+    lsqr_solve(S.sys.neq, S.nx, S.sys.nnz, mi, eps, nit, ierr, S.pivot.data(), S.sys.i.data(), S.sys.j.data(),
+               S.sys.v.data(), b.data(), S.x.data());
+    if (nits) nits[r] = nit;
+    if (ierr) ierr_all = ierr;
+    // StokesDistributeUnknowns (lib_StokesFull.f90:446-501)
+    for (int i = 0; i < P->sd_nqnodes; ++i) {
+      int isp = P->qnodeList[i], wall = P->qbcidList[i];
+      for (int en = 0; en < 3; ++en) {
+        int ispL = isp + en * P->nelem, bc = P->knownOf(en, wall);
+        P->eqn[en].q[isp] = (bc == iFlux) ? S.b[S.qcol[ispL] - 1] : S.x[S.qcol[ispL] - 1];
+      }
+    }
+    for (int en = 0; en < 3; ++en)
+      std::copy(P->eqn[en].q.begin(), P->eqn[en].q.end(), q_out + ((size_t)r * 3 + en) * P->nelem);
+    if (ft) force_torque(*P, P->eqn[0].q.data(), P->eqn[1].q.data(), P->eqn[2].q.data(), fwall, ft + 6 * r, ft + 6 * r + 3);
+  }
+  return ierr_all;
+}
+
+// Force and torque of a traction field on one wall (lib_particle.f90:1751-1904)
+void orc_force_torque(void* h, const double* qx, const double* qy, const double* qz, int wall, double ft[6]) {
+  force_torque(*(Problem*)h, qx, qy, qz, wall, ft, ft + 3);
+}
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
+}  // extern "C"

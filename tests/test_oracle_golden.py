@@ -1,0 +1,197 @@
+"""CPU tests: pin the FP64 oracle against the reference's own known answers.
+
+The reference ships no golden output files; what it does ship are
+* the analytic integrals of Triangle_TestIntegration (src/mod_trikotnik.f90:124-154),
+* the rigid-body / free-term self-checks it logs as fSP/qSP errors
+  (src/lib_sdBem.f90:566-581,714-718; src/lib_Stokes.f90:1781-1812,2153-2178),
+* analytic resistances (src/lib_particle.f90:1910-1976).
+The analytic singular integrals are pinned independently by Duffy-transformed
+Gauss quadrature, and tests/golden/oracle_values.json freezes oracle outputs
+(generated by tests/golden/make_golden.py) against regressions.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from andromeda_gb300 import mesh as M
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+# Triangle_TestIntegration analytic values (mod_trikotnik.f90:145-154)
+ANAL = [2097152.0 / 121.0, 1.0522458619541769455, 0.98364468921563619296, 0.14027496308479503178]
+
+
+def test_wx_rules_sizes_and_weights(orc):
+    for itri, q in zip(range(1, 6), (7, 25, 54, 85, 126)):
+        l1, l2, l3, w = orc.wx_rule(itri)
+        assert len(w) == q
+        assert abs(w.sum() - 1.0) < 1e-14
+        assert np.all(np.abs(l1 + l2 + l3 - 1) < 1e-14)
+
+
+@pytest.mark.parametrize("itri,tol", [(1, [0.46, 1e-2, 2e-3, 0.06]), (2, [1e-3, 2e-6, 1e-8, 0.006]),
+                                      (3, [5e-8, 1e-10, 5e-12, 0.009]), (4, [1e-13, 1e-13, 1e-14, 0.006]),
+                                      (5, [1e-13, 1e-14, 1e-14, 0.004])])
+def test_triangle_test_integration(orc, itri, tol):
+    """Polynomial of degree 20 is exact for the order-20/25 rules (ITRI 4, 5)."""
+    r = orc.triangle_test(itri)
+    for k in range(4):
+        assert abs(r[k] - ANAL[k]) / ANAL[k] <= tol[k], (itri, k, r[k])
+
+
+def _duffy(P0, P1, P2, f, n=120):
+    x, w = np.polynomial.legendre.leggauss(n)
+    u, wu = 0.5 * (x + 1), 0.5 * w
+    U, V = np.meshgrid(u, u, indexing="ij")
+    W = np.outer(wu, wu)
+    X = P0 + U[..., None] * (P1 - P0) + (U * V)[..., None] * (P2 - P1)
+    J = U * np.linalg.norm(np.cross(P1 - P0, P2 - P1))
+    return np.tensordot(W * J, f(X), axes=([0, 1], [0, 1]))
+
+
+def _lap(s):
+    return lambda X: 1 / (4 * np.pi * np.linalg.norm(X - s, axis=-1))
+
+
+def _stk(s):
+    def f(X):
+        r = X - s
+        R = np.linalg.norm(r, axis=-1)
+        G = np.eye(3)[None, None] / R[..., None, None] + r[..., :, None] * r[..., None, :] / R[..., None, None] ** 3
+        return G[..., [0, 0, 0, 1, 1, 2], [0, 1, 2, 1, 2, 2]]
+    return f
+
+
+def _numeric_self(v, isrc, f):
+    if isrc < 4:
+        s = v[isrc - 1]
+        return _duffy(s, v[isrc % 3], v[(isrc + 1) % 3], f(s))
+    s = v.mean(0)
+    return sum(_duffy(s, v[k], v[(k + 1) % 3], f(s)) for k in range(3))
+
+
+@pytest.mark.parametrize("isrc", [1, 2, 3, 4])
+@pytest.mark.parametrize("tri", [
+    [[0.1, 0.2, 0.3], [1.3, 0.1, 0.5], [0.4, 1.1, 0.2]],
+    [[0.0, 0.0, 1.0], [2.0, 0.0, 1.0], [2.0, 2.0, 1.0]],
+    [[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.02, 0.05, 0.3]],   # skinny
+])
+def test_ren_chan_vs_duffy(orc, isrc, tri):
+    v = np.array(tri, dtype=float)
+    a = orc.si_tri_lap(v, isrc)
+    b = orc.si_tri_stk(v, isrc)
+    na = _numeric_self(v, isrc, _lap)
+    nb = _numeric_self(v, isrc, _stk)
+    assert abs(a - na) / abs(na) < 1e-12
+    assert np.max(np.abs(b - nb)) / np.max(np.abs(nb)) < 1e-11
+
+
+def test_quad_singular_is_triangle_fan(orc):
+    q = np.array([[0, 0, 0], [1.2, 0.1, 0], [1.1, 0.9, 0.2], [-0.1, 1.0, 0.1]], dtype=float)
+    # corner 1: triangles (1,2,3)+(1,3,4)
+    exp = orc.si_tri_lap(q[[0, 1, 2]], 1) + orc.si_tri_lap(q[[0, 2, 3]], 1)
+    assert abs(orc.si_qua_lap(q, 1) - exp) < 1e-15
+    c = q.mean(0)
+    exp5 = sum(orc.si_tri_lap(np.array([c, q[k], q[(k + 1) % 4]]), 1) for k in range(4))
+    assert abs(orc.si_qua_lap(q, 5) - exp5) < 1e-14
+    g = orc.si_qua_stk(q, 2)
+    eg = orc.si_tri_stk(q[[1, 2, 3]], 1) + orc.si_tri_stk(q[[1, 3, 0]], 1)
+    assert np.max(np.abs(g - eg)) < 1e-14
+
+
+def test_mesh_generators_counts():
+    m3 = M.icosphere(3)
+    assert len(m3["xyz"]) == 642 and len(m3["etype"]) == 1280
+    m5 = M.icosphere(5)
+    assert len(m5["xyz"]) == 10242 and len(m5["etype"]) == 20480
+    se = M.superellipsoid(1.0, 0.5, 0.25, 0.6, 1.4, 160, 320)
+    assert len(se["etype"]) == 102400
+    # every triangle non-degenerate and outward oriented
+    p = se["xyz"][se["con"][:, :3]]
+    n = np.cross(p[:, 1] - p[:, 0], p[:, 2] - p[:, 0])
+    assert np.all(np.linalg.norm(n, axis=1) > 0)
+    assert np.all(np.einsum("ij,ij->i", n, p.mean(1)) > 0)
+
+
+def test_laplace_c1_diagnostics_and_flux(orc):
+    """Config 1: unit icosphere L3, u = x+2y+3z; q = -n.(1,2,3) (q = -diff du/dn)."""
+    m = M.icosphere(3)
+    P = orc.Problem(1, m, walls=[1], known=[[1]], itri=5)
+    errs = P.form_integrals()
+    assert errs[0] < 1e-12      # u-row rigid-body residual (lib_sdBem.f90:566-581)
+    assert errs[1] < 1e-7       # q-row |0.5 - c| (lib_sdBem.f90:714-718)
+    n, a, c = P.geometry()
+    u = m["xyz"] @ np.array([1.0, 2.0, 3.0])
+    _, q, nit, ierr = P.laplace_solve(u, np.zeros(P.nelem), maxit=0, eps=1e-12)
+    qex = -(n @ np.array([1.0, 2.0, 3.0]))
+    assert ierr == 0
+    assert np.linalg.norm(q - qex) / np.linalg.norm(qex) < 1e-7
+
+
+def _sphere_in_sphere(level_in=1, level_out=1, a=1.0, b=8.0):
+    return M.particle_in_sphere(M.icosphere(level_in, a, inward=True), outer_level=level_out, outer_radius=b)
+
+
+def _rigid_fields(m, outer_wall=2):
+    nn = len(m["xyz"])
+    on = np.zeros(nn, bool)
+    for e in np.where(m["bcid"] == outer_wall)[0]:
+        on[m["con"][e, :3]] = True
+    U = np.zeros((6, 3, nn))
+    for i in range(3):
+        U[i, i, on] = 1.0
+        w = np.zeros(3)
+        w[i] = 1.0
+        U[3 + i][:, on] = np.cross(w, m["xyz"][on]).T
+    return U
+
+
+def test_stokes_concentric_spheres(orc):
+    """Drag / torque of a fixed sphere inside a moving container against the
+    concentric-sphere solutions (flat elements: O(h^2) discretisation error)."""
+    a, b = 1.0, 8.0
+    m = _sphere_in_sphere(2, 1, a, b)
+    P = orc.Problem(2, m, walls=[1, 2], known=np.ones((3, 2)), itri=5)
+    errs = P.form_integrals()
+    assert errs[1] < 1e-2   # q-row diagonal 4 pi / off-diagonal 0 (lib_Stokes.f90:1781-1812)
+    q, ft, nits, ierr = P.stokes_solve_sequence(_rigid_fields(m), maxit=0, eps=1e-10, fwall=1)
+    assert ierr == 0
+    lam = a / b
+    K = (1 - lam ** 5) / (1 - 9 / 4 * lam + 5 / 2 * lam ** 3 - 9 / 4 * lam ** 5 + lam ** 6)
+    F = ft[:3, :3] / (6 * np.pi * a * K)
+    T = ft[3:, 3:] / (8 * np.pi * a ** 3 / (1 - lam ** 3))
+    assert np.allclose(np.diag(F), np.diag(F)[0], rtol=1e-6)
+    assert 0.95 < F[0, 0] < 1.01
+    assert 0.90 < T[0, 0] < 1.01
+    R = ft.T  # rows: F,T components; columns: motions
+    assert np.max(np.abs(R - R.T)) / np.max(np.abs(R)) < 1e-3  # reciprocal theorem
+
+
+def test_lsqr_oracle_small_system(orc):
+    rng = np.random.default_rng(7)
+    A = rng.normal(size=(40, 25))
+    ia = np.arange(0, 40 * 25 + 1, 25, dtype=np.int64) + 1
+    ja = np.tile(np.arange(1, 26, dtype=np.int32), 40)
+    a = A.ravel().copy()
+    q = orc.lsqr_precon(40, 25, ia, ja, a)
+    assert np.allclose(q, 1 / np.linalg.norm(A, axis=0))
+    xt = rng.normal(size=25)
+    b = A @ xt
+    x = np.zeros(25)
+    nit, ierr, st = orc.lsqr_solve(40, 25, ia, ja, a, q, b, x, maxit=0, eps=1e-14)
+    assert ierr == 0
+    assert np.linalg.norm(x - xt) / np.linalg.norm(xt) < 1e-10
+
+
+def test_golden_values_frozen(orc):
+    """Oracle outputs frozen in tests/golden/oracle_values.json."""
+    with open(os.path.join(GOLDEN, "oracle_values.json")) as f:
+        g = json.load(f)
+    v = np.array(g["triangle"])
+    for isrc in (1, 2, 3, 4):
+        assert abs(orc.si_tri_lap(v, isrc) - g["si_tri_lap"][isrc - 1]) <= 1e-14 * abs(g["si_tri_lap"][isrc - 1])
+        assert np.allclose(orc.si_tri_stk(v, isrc), g["si_tri_stk"][isrc - 1], rtol=1e-13, atol=0)
+    for itri in range(1, 6):
+        assert np.allclose(orc.triangle_test(itri), g["triangle_test"][itri - 1], rtol=1e-13, atol=0)
