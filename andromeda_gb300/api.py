@@ -161,6 +161,13 @@ class Context:
         self._ck(self._L.agb_force_torque(self.h, nrhs, x.reshape(-1), int(wall), ft.reshape(-1)))
         return ft
 
+    def kernel_times(self, reset=False):
+        """Cumulative live kernel times (ms) and launch counts since the last reset."""
+        out = np.zeros(8)
+        self._ck(self._L.agb_kernel_times(self.h, int(bool(reset)), out))
+        return {"av_ms": out[0], "av_launches": int(out[1]), "atu_ms": out[2], "atu_launches": int(out[3]),
+                "assemble_ms": out[4], "assemble_launches": int(out[5]), "rhs_ms": out[6], "rhs_calls": int(out[7])}
+
     def resistance_tensor(self, precision=MIXED, particle_wall=1, outer_wall=2, maxit=0, eps=1e-8, refine=0):
         R = np.zeros((6, 6))
         nit = np.zeros(6, np.int32)

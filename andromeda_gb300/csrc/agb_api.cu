@@ -62,6 +62,10 @@ struct agb_context {
   int *d_active = nullptr;
   unsigned char* d_rowact = nullptr;
   size_t cap_u = 0, cap_rhs = 0, cap_x = 0, cap_act = 0;
+  // live kernel timing (CUDA events on the context stream)
+  cudaEvent_t tev[4] = {};
+  double t_asm = 0.0, t_rhs = 0.0;
+  long n_asm = 0, n_rhs = 0;
 };
 
 namespace {
@@ -205,8 +209,14 @@ int device_rhs(agb_context* c, int nrhs, int na) {
     a.ne = c->ne; a.Q = c->rule.Q; a.ldp = 0; a.k = nrhs; a.nnodes = c->nnodes;
     a.geom = c->d_geom; a.rule_l = c->rule.l; a.rule_w = c->rule.w; a.u = c->d_u;
     a.active = c->d_active; a.na = na; a.row_active = c->d_rowact; a.rhs = c->d_rhs;
+    cudaEventRecord(c->tev[2], c->stream);
     if (c->prec == AGB_MIXED) CUDA_OR_FAIL(c, launch_stokes_rhs<float>(a, c->stream));
     else CUDA_OR_FAIL(c, launch_stokes_rhs<double>(a, c->stream));
+    cudaEventRecord(c->tev[3], c->stream);
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->tev[2], c->tev[3]) == cudaSuccess) { c->t_rhs += ms; ++c->n_rhs; }
+    (void)cudaGetLastError();
   } else {
     LaplaceArgs a;
     a.ne = c->ne; a.Q = c->rule.Q; a.k = nrhs; a.nnodes = c->nnodes; a.iqud = c->iqud;
@@ -258,6 +268,7 @@ int agb_create(agb_context** out, int device) {
   e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = upload_gauss_tables();
+  for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->tev[i]);
   if (e != cudaSuccess) {
     g_free_err = std::string("agb_create: ") + cudaGetErrorString(e);
     delete c;
@@ -278,6 +289,8 @@ int agb_destroy(agb_context* c) {
   dfree(c->d_ft);
   dfree(c->d_active);
   dfree(c->d_rowact);
+  for (int i = 0; i < 4; ++i)
+    if (c->tev[i]) cudaEventDestroy(c->tev[i]);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return AGB_OK;
@@ -445,18 +458,25 @@ int agb_assemble(agb_context* c, int precision) {
       CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_colscale, csf.data(), ldp * sizeof(float), cudaMemcpyHostToDevice, c->stream));
       CUDA_OR_FAIL(c, launch_expand_points<float>(c->ne, ldp, c->d_geom, c->rule, (QPt<float>*)c->d_pts,
                                                   (float*)c->d_src, (float*)c->d_nrm, c->stream));
+      cudaEventRecord(c->tev[0], c->stream);
       CUDA_OR_FAIL(c, launch_stokes_G<float>(c->ne, Q, ldp, (const QPt<float>*)c->d_pts, (const float*)c->d_src,
                                              (const float*)c->d_colscale, (float*)c->d_A, c->lda, c->stream));
+      cudaEventRecord(c->tev[1], c->stream);
       CUDA_OR_FAIL(c, launch_stokes_self<float>(c->ne, c->d_geom, c->diff, (float*)c->d_A, c->lda, c->stream));
     } else {
       CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_colscale, cs.data(), ldp * sizeof(double), cudaMemcpyHostToDevice, c->stream));
       CUDA_OR_FAIL(c, launch_expand_points<double>(c->ne, ldp, c->d_geom, c->rule, (QPt<double>*)c->d_pts,
                                                    (double*)c->d_src, (double*)c->d_nrm, c->stream));
+      cudaEventRecord(c->tev[0], c->stream);
       CUDA_OR_FAIL(c, launch_stokes_G<double>(c->ne, Q, ldp, (const QPt<double>*)c->d_pts, (const double*)c->d_src,
                                               (const double*)c->d_colscale, (double*)c->d_A, c->lda, c->stream));
+      cudaEventRecord(c->tev[1], c->stream);
       CUDA_OR_FAIL(c, launch_stokes_self<double>(c->ne, c->d_geom, c->diff, (double*)c->d_A, c->lda, c->stream));
     }
     CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->tev[0], c->tev[1]) == cudaSuccess) { c->t_asm += ms; ++c->n_asm; }
+    (void)cudaGetLastError();
   } else {
     LaplaceArgs a;
     a.ne = c->ne; a.Q = c->rule.Q; a.k = 0; a.nnodes = c->nnodes; a.iqud = c->iqud;
@@ -639,6 +659,23 @@ int agb_lsqr_solve(int m, int n, int64_t nnz, int* maxit, double eps, int* nit, 
   if (!crs_valid(m, n, nnz, ia, ja)) return fail(nullptr, AGB_ERR_ARG, "malformed CRS (ia/ja out of range)");
   std::string err;
   if (!crs_lsqr_solve(m, n, nnz, *maxit, eps, *nit, *ierr, q, ia, ja, a, b, x, err)) return fail(nullptr, AGB_ERR_CUDA, err);
+  return AGB_OK;
+}
+
+int agb_kernel_times(agb_context* c, int reset, double* out) {
+  if (!c) return AGB_ERR_ARG;
+  if (out) {
+    out[0] = c->lsqr.t_av;  out[1] = (double)c->lsqr.n_av;
+    out[2] = c->lsqr.t_atu; out[3] = (double)c->lsqr.n_atu;
+    out[4] = c->t_asm;      out[5] = (double)c->n_asm;
+    out[6] = c->t_rhs;      out[7] = (double)c->n_rhs;
+  }
+  if (reset) {
+    c->lsqr.t_av = c->lsqr.t_atu = 0.0;
+    c->lsqr.n_av = c->lsqr.n_atu = 0;
+    c->t_asm = c->t_rhs = 0.0;
+    c->n_asm = c->n_rhs = 0;
+  }
   return AGB_OK;
 }
 

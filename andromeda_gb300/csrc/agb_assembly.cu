@@ -306,10 +306,15 @@ __global__ void k_stokes_rhs(StokesRhsArgs a) {
     const ElemGeom& G = a.geom[e];
     const T nx = (T)(G.multi * G.n[0]), ny = (T)(G.multi * G.n[1]), nz = (T)(G.multi * G.n[2]);
     T uv[AGB_MAX_RHS][3][3];  // [c][comp][local node]
-    for (int c = 0; c < a.k; ++c)
+#pragma unroll
+    for (int c = 0; c < AGB_MAX_RHS; ++c)
+#pragma unroll
       for (int b = 0; b < 3; ++b)
-        for (int kk = 0; kk < 3; ++kk) uv[c][b][kk] = (T)a.u[((int64_t)c * 3 + b) * a.nnodes + G.con[kk]];
+#pragma unroll
+        for (int kk = 0; kk < 3; ++kk)
+          uv[c][b][kk] = (c < a.k) ? (T)a.u[((int64_t)c * 3 + b) * a.nnodes + G.con[kk]] : T(0);
     T pe[AGB_MAX_RHS][3];
+#pragma unroll
     for (int c = 0; c < AGB_MAX_RHS; ++c) pe[c][0] = pe[c][1] = pe[c][2] = T(0);
     for (int q = 0; q < Q; ++q) {
       const double l1 = a.rule_l[q], l2 = a.rule_l[Q + q], l3 = a.rule_l[2 * Q + q];
@@ -323,69 +328,115 @@ __global__ void k_stokes_rhs(StokesRhsArgs a) {
       const T ir2 = ir * ir;
       const T cn = T(-6) * w * (rx * nx + ry * ny + rz * nz) * (ir2 * ir2 * ir);
       const T L1 = (T)l1, L2 = (T)l2, L3 = (T)l3;
-      for (int c = 0; c < a.k; ++c) {
-        const T ux = L1 * uv[c][0][0] + L2 * uv[c][0][1] + L3 * uv[c][0][2];
-        const T uy = L1 * uv[c][1][0] + L2 * uv[c][1][1] + L3 * uv[c][1][2];
-        const T uz = L1 * uv[c][2][0] + L2 * uv[c][2][1] + L3 * uv[c][2][2];
-        const T f = cn * (rx * ux + ry * uy + rz * uz);
-        pe[c][0] += f * rx;
-        pe[c][1] += f * ry;
-        pe[c][2] += f * rz;
+#pragma unroll
+      for (int c = 0; c < AGB_MAX_RHS; ++c) {
+        if (c < a.k) {
+          const T ux = L1 * uv[c][0][0] + L2 * uv[c][0][1] + L3 * uv[c][0][2];
+          const T uy = L1 * uv[c][1][0] + L2 * uv[c][1][1] + L3 * uv[c][1][2];
+          const T uz = L1 * uv[c][2][0] + L2 * uv[c][2][1] + L3 * uv[c][2][2];
+          const T f = cn * (rx * ux + ry * uy + rz * uz);
+          pe[c][0] += f * rx;
+          pe[c][1] += f * ry;
+          pe[c][2] += f * rz;
+        }
       }
     }
-    for (int c = 0; c < a.k; ++c)
+#pragma unroll
+    for (int c = 0; c < AGB_MAX_RHS; ++c)
+#pragma unroll
       for (int b = 0; b < 3; ++b) acc[c][b] += (double)pe[c][b];
   }
-  // (B) free term: c_aa = -sum over all elements of int T_aa (FP64 sums)
-  double ca[3] = {0.0, 0.0, 0.0};
-  const bool row_act = a.row_active[i] != 0;
-  if (row_act) {
-    for (int e = lane; e < a.ne; e += 32) {
-      if (e == i) continue;
-      const ElemGeom& G = a.geom[e];
-      const T nx = (T)(G.multi * G.n[0]), ny = (T)(G.multi * G.n[1]), nz = (T)(G.multi * G.n[2]);
-      T s0 = T(0), s1 = T(0), s2 = T(0);
-      for (int q = 0; q < Q; ++q) {
-        const double l1 = a.rule_l[q], l2 = a.rule_l[Q + q], l3 = a.rule_l[2 * Q + q];
-        const T px = (T)(l1 * G.v[0][0] + l2 * G.v[1][0] + l3 * G.v[2][0]);
-        const T py = (T)(l1 * G.v[0][1] + l2 * G.v[1][1] + l3 * G.v[2][1]);
-        const T pz = (T)(l1 * G.v[0][2] + l2 * G.v[1][2] + l3 * G.v[2][2]);
-        const T w = (T)(a.rule_w[q] * G.area);
-        const T rx = px - sx, ry = py - sy, rz = pz - sz;
-        const T r2 = rx * rx + ry * ry + rz * rz;
-        const T ir = rsq<T>(r2);
-        const T ir2 = ir * ir;
-        const T cn = T(-6) * w * (rx * nx + ry * ny + rz * nz) * (ir2 * ir2 * ir);
-        s0 += cn * rx * rx;
-        s1 += cn * ry * ry;
-        s2 += cn * rz * rz;
-      }
-      ca[0] += (double)s0; ca[1] += (double)s1; ca[2] += (double)s2;
-    }
-    for (int b = 0; b < 3; ++b) ca[b] = -wsum(ca[b]);
-  }
-  for (int c = 0; c < a.k; ++c)
+#pragma unroll
+  for (int c = 0; c < AGB_MAX_RHS; ++c)
+#pragma unroll
     for (int b = 0; b < 3; ++b) acc[c][b] = wsum(acc[c][b]);
   if (lane == 0) {
-    const double shpf = (Gi.type == AGB_TRI) ? 1.0 / 3.0 : 0.25;
-    for (int c = 0; c < a.k; ++c)
-      for (int b = 0; b < 3; ++b) {
-        double v = acc[c][b];
-        if (row_act) {
-          double su = 0.0;
-          for (int kk = 0; kk < Gi.nno; ++kk) su += a.u[((int64_t)c * 3 + b) * a.nnodes + Gi.con[kk]];
-          v += shpf * ca[b] * su;
-        }
-        a.rhs[(int64_t)c * 3 * a.ne + 3 * i + b] = v;
-      }
+#pragma unroll
+    for (int c = 0; c < AGB_MAX_RHS; ++c)
+      if (c < a.k)
+        for (int b = 0; b < 3; ++b) a.rhs[(int64_t)c * 3 * a.ne + 3 * i + b] = acc[c][b];
   }
+}
+
+// Free term of the rows whose own element carries velocity: c_aa(i) =
+// -sum over all elements e != i of int_e T_aa(x_i, y) dy, accumulated in FP64
+// from per-element sums.  Grid: (active row, element chunk); partials per
+// (row, chunk) are reduced in chunk order by k_stokes_freeterm_apply.
+constexpr int FT_CHUNK = 2048;
+template <typename T>
+__global__ void __launch_bounds__(256) k_stokes_freeterm(StokesRhsArgs a, double* __restrict__ partial) {
+  const int t = blockIdx.x;  // index into the active list
+  const int i = a.active[t];
+  const int e0 = blockIdx.y * FT_CHUNK;
+  const ElemGeom& Gi = a.geom[i];
+  const T sx = (T)Gi.c[0], sy = (T)Gi.c[1], sz = (T)Gi.c[2];
+  const int Q = a.Q;
+  double ca[3] = {0.0, 0.0, 0.0};
+  for (int e = e0 + threadIdx.x; e < min(a.ne, e0 + FT_CHUNK); e += blockDim.x) {
+    if (e == i) continue;
+    const ElemGeom& G = a.geom[e];
+    const T nx = (T)(G.multi * G.n[0]), ny = (T)(G.multi * G.n[1]), nz = (T)(G.multi * G.n[2]);
+    T s0 = T(0), s1 = T(0), s2 = T(0);
+    for (int q = 0; q < Q; ++q) {
+      const double l1 = a.rule_l[q], l2 = a.rule_l[Q + q], l3 = a.rule_l[2 * Q + q];
+      const T px = (T)(l1 * G.v[0][0] + l2 * G.v[1][0] + l3 * G.v[2][0]);
+      const T py = (T)(l1 * G.v[0][1] + l2 * G.v[1][1] + l3 * G.v[2][1]);
+      const T pz = (T)(l1 * G.v[0][2] + l2 * G.v[1][2] + l3 * G.v[2][2]);
+      const T w = (T)(a.rule_w[q] * G.area);
+      const T rx = px - sx, ry = py - sy, rz = pz - sz;
+      const T r2 = rx * rx + ry * ry + rz * rz;
+      const T ir = rsq<T>(r2);
+      const T ir2 = ir * ir;
+      const T cn = T(-6) * w * (rx * nx + ry * ny + rz * nz) * (ir2 * ir2 * ir);
+      s0 += cn * rx * rx;
+      s1 += cn * ry * ry;
+      s2 += cn * rz * rz;
+    }
+    ca[0] += (double)s0; ca[1] += (double)s1; ca[2] += (double)s2;
+  }
+  __shared__ double sh[3][256];
+  for (int b = 0; b < 3; ++b) sh[b][threadIdx.x] = ca[b];
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int b = 0; b < 3; ++b) sh[b][threadIdx.x] += sh[b][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x < 3) partial[((int64_t)t * gridDim.y + blockIdx.y) * 3 + threadIdx.x] = sh[threadIdx.x][0];
+}
+// rhs(3i+b, c) += shpf * c_bb(i) * sum over the nodes of element i of u_b
+__global__ void k_stokes_freeterm_apply(StokesRhsArgs a, const double* __restrict__ partial, int nchunks) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= a.na) return;
+  const int i = a.active[t];
+  const ElemGeom& Gi = a.geom[i];
+  double ca[3] = {0.0, 0.0, 0.0};
+  for (int k = 0; k < nchunks; ++k)
+    for (int b = 0; b < 3; ++b) ca[b] += partial[((int64_t)t * nchunks + k) * 3 + b];
+  const double shpf = (Gi.type == AGB_TRI) ? 1.0 / 3.0 : 0.25;
+  for (int c = 0; c < a.k; ++c)
+    for (int b = 0; b < 3; ++b) {
+      double su = 0.0;
+      for (int kk = 0; kk < Gi.nno; ++kk) su += a.u[((int64_t)c * 3 + b) * a.nnodes + Gi.con[kk]];
+      a.rhs[(int64_t)c * 3 * a.ne + 3 * i + b] += shpf * (-ca[b]) * su;
+    }
 }
 
 template <typename T>
 cudaError_t launch_stokes_rhs(const StokesRhsArgs& a, cudaStream_t s) {
   const int threads = 128;
   k_stokes_rhs<T><<<cdiv((int64_t)a.ne * 32, threads), threads, 0, s>>>(a);
-  return cudaGetLastError();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || a.na == 0) return e;
+  const int nchunks = (int)cdiv(a.ne, FT_CHUNK);
+  double* partial = nullptr;
+  e = cudaMallocAsync(&partial, (size_t)a.na * nchunks * 3 * sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  k_stokes_freeterm<T><<<dim3(a.na, nchunks), 256, 0, s>>>(a, partial);
+  k_stokes_freeterm_apply<<<cdiv(a.na, 128), 128, 0, s>>>(a, partial, nchunks);
+  e = cudaGetLastError();
+  cudaFreeAsync(partial, s);
+  return e;
 }
 template cudaError_t launch_stokes_rhs<float>(const StokesRhsArgs&, cudaStream_t);
 template cudaError_t launch_stokes_rhs<double>(const StokesRhsArgs&, cudaStream_t);

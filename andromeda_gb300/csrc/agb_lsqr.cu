@@ -196,6 +196,278 @@ __global__ void __launch_bounds__(kThreads) k_atu(const T* __restrict__ A, int64
   }
 }
 
+// ---------------------------------------------------------------------------
+// Tuned sweeps of the LSQR iteration.
+//
+// k_av2: Y = A V + gamma Y.  A warp owns RR rows; lanes stream 16-byte
+// vectors of each row (coalesced 512 B per warp and row).  V is kept
+// RHS-major ([8][lda]) and staged chunk by chunk into shared memory by 1-D
+// TMA bulk copies (cp.async.bulk + mbarrier, double buffered), so a lane's
+// 16-byte reads of V hit 32 consecutive banks.  FP32 path: products are
+// accumulated in FP32 within a 1024-column chunk, then reduce-scattered across
+// the warp (31 shuffles) so that lane l keeps the FP64 running sum of
+// (row l/8, rhs l%8) -- one FP64 register per lane instead of 32.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: after ~2^22 failed tries the barrier is reported through
+// errflag and the wait gives up (the copy is in bounds by construction, so
+// this only guards against a hang)
+__device__ __forceinline__ void mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* errflag) {
+  uint32_t tries = 0;
+  while (!mbar_try_wait(bar, parity)) {
+    if (++tries > (1u << 22)) {
+      if (errflag) atomicExch(errflag, 1);
+      break;
+    }
+  }
+}
+
+template <typename T> struct AV2;
+template <> struct AV2<float> { static constexpr int RR = 4, WARPS = 16, CH = 1024; };
+template <> struct AV2<double> { static constexpr int RR = 2, WARPS = 8, CH = 512; };
+
+template <typename T>
+__global__ void __launch_bounds__(AV2<T>::WARPS * 32) k_av2(const T* __restrict__ A, int64_t lda, int m,
+                                                            const T* __restrict__ Vt, const LsqrScalars* sc,
+                                                            double* __restrict__ Y, T* __restrict__ Ys,
+                                                            double* __restrict__ part, int* errflag) {
+  constexpr int RR = AV2<T>::RR, WARPS = AV2<T>::WARPS, CH = AV2<T>::CH, VN = 16 / sizeof(T);
+  extern __shared__ __align__(128) unsigned char av2_smem[];
+  T* sV = reinterpret_cast<T*>(av2_smem);  // [2][8][CH]
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ double sPart[WARPS][K8];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row0 = blockIdx.x * (WARPS * RR) + warp * RR;
+  const int nch = (int)((lda + CH - 1) / CH);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int k) {
+    const int64_t j0 = (int64_t)k * CH;
+    const int cw = (int)((lda - j0) < (int64_t)CH ? (lda - j0) : (int64_t)CH);
+    uint64_t* b = &bar[k & 1];
+    T* dst = sV + (size_t)(k & 1) * K8 * CH;
+    mbar_expect_tx(b, (uint32_t)(K8 * cw * sizeof(T)));
+#pragma unroll
+    for (int c = 0; c < K8; ++c) bulk_g2s(dst + c * CH, Vt + (int64_t)c * lda + j0, (uint32_t)(cw * sizeof(T)), b);
+  };
+  if (threadIdx.x == 0) issue(0);
+
+  using Acc = T;
+  Acc acc[RR][K8];
+  double dacc = 0.0;                // float path: lane's (row, rhs) running sum
+  double dfull[RR][K8];             // double path
+#pragma unroll
+  for (int r = 0; r < RR; ++r)
+#pragma unroll
+    for (int c = 0; c < K8; ++c) { acc[r][c] = Acc(0); dfull[r][c] = 0.0; }
+
+  for (int k = 0; k < nch; ++k) {
+    if (threadIdx.x == 0 && k + 1 < nch) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(k + 1);
+    }
+    mbar_wait_bounded(&bar[k & 1], (uint32_t)((k >> 1) & 1), errflag);
+    const T* cv = sV + (size_t)(k & 1) * K8 * CH;
+    const int64_t j0 = (int64_t)k * CH;
+    const int cw = (int)((lda - j0) < (int64_t)CH ? (lda - j0) : (int64_t)CH);
+    for (int jj = lane * VN; jj < cw; jj += 32 * VN) {
+      T a[RR][VN];
+#pragma unroll
+      for (int r = 0; r < RR; ++r) {
+        const int row = row0 + r;
+        if (row < m) {
+          typename Vec<T>::V v = *reinterpret_cast<const typename Vec<T>::V*>(A + (int64_t)row * lda + j0 + jj);
+          unpack<T>(v, a[r]);
+        } else {
+#pragma unroll
+          for (int q = 0; q < VN; ++q) a[r][q] = T(0);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < K8; ++c) {
+        typename Vec<T>::V vv = *reinterpret_cast<const typename Vec<T>::V*>(cv + c * CH + jj);
+        T v[VN];
+        unpack<T>(vv, v);
+#pragma unroll
+        for (int r = 0; r < RR; ++r)
+#pragma unroll
+          for (int q = 0; q < VN; ++q) acc[r][c] += a[r][q] * v[q];
+      }
+    }
+    if constexpr (sizeof(T) == 4) {
+      // reduce-scatter the 32 chunk partials: lane l ends with index l = r*8+c
+      float v[32];
+#pragma unroll
+      for (int r = 0; r < RR; ++r)
+#pragma unroll
+        for (int c = 0; c < K8; ++c) { v[r * K8 + c] = acc[r][c]; acc[r][c] = 0.f; }
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) {
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < o; ++i) {
+          const float send = upper ? v[i] : v[i + o];
+          const float keep = upper ? v[i + o] : v[i];
+          v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+      }
+      dacc += (double)v[0];
+    } else {
+#pragma unroll
+      for (int r = 0; r < RR; ++r)
+#pragma unroll
+        for (int c = 0; c < K8; ++c) { dfull[r][c] += (double)acc[r][c]; acc[r][c] = Acc(0); }
+    }
+    __syncthreads();  // everyone is done with this buffer before it is refilled
+  }
+  double ssq = 0.0;
+  if constexpr (sizeof(T) == 4) {
+    const int r = lane >> 3, c = lane & 7, row = row0 + r;
+    if (row < m) {
+      const double y = dacc + sc[c].gamma * Y[(int64_t)row * K8 + c];
+      Y[(int64_t)row * K8 + c] = y;
+      Ys[(int64_t)row * K8 + c] = (T)y;
+      ssq = y * y;
+    }
+    // lanes with equal c: l, l^8, l^16, l^24
+    ssq += __shfl_xor_sync(0xffffffffu, ssq, 8);
+    ssq += __shfl_xor_sync(0xffffffffu, ssq, 16);
+  } else {
+#pragma unroll
+    for (int r = 0; r < RR; ++r) {
+      const int row = row0 + r;
+#pragma unroll
+      for (int c = 0; c < K8; ++c) {
+        const double s = warp_sum(dfull[r][c]);
+        if (row < m && lane == c) {
+          const double y = s + sc[c].gamma * Y[(int64_t)row * K8 + c];
+          Y[(int64_t)row * K8 + c] = y;
+          Ys[(int64_t)row * K8 + c] = (T)y;
+          ssq += y * y;
+        }
+      }
+    }
+  }
+  if (lane < K8) sPart[warp][lane] = ssq;
+  __syncthreads();
+  if (threadIdx.x < K8) {
+    double a = 0.0;
+    for (int w = 0; w < WARPS; ++w) a += sPart[w][threadIdx.x];
+    part[(int64_t)blockIdx.x * K8 + threadIdx.x] = a;
+  }
+}
+
+// k_atu2: Zp[g][j][c] = sum_{r in group g} A[r][j] U[r][c].  A thread owns VN
+// consecutive columns and streams the rows of its group 8 at a time (8
+// independent 16-byte loads in flight per thread); U rows are broadcast from
+// shared memory.  FP32 path: FP32 partials over 256 rows are added into FP64
+// per-thread accumulators kept in shared memory.
+constexpr int ATU_THREADS = 256;
+template <typename T>
+__global__ void __launch_bounds__(ATU_THREADS) k_atu2(const T* __restrict__ A, int64_t lda, int m,
+                                                      const T* __restrict__ Us, int rows_per_group,
+                                                      double* __restrict__ Zp) {
+  constexpr int VN = Vec<T>::N;
+  constexpr int RCH = 256;
+  constexpr int UNR = 8;
+  extern __shared__ __align__(16) unsigned char atu_smem[];
+  T* sU = reinterpret_cast<T*>(atu_smem);                                  // [RCH][8]
+  double* sD = reinterpret_cast<double*>(atu_smem + RCH * K8 * sizeof(T));  // [VN*8][threads] (FP32 path)
+  const int64_t col = ((int64_t)blockIdx.x * ATU_THREADS + threadIdx.x) * VN;
+  const int g = blockIdx.y;
+  const int r0 = g * rows_per_group, r1 = min(m, r0 + rows_per_group);
+  const bool live = col < lda;
+  T acc[VN][K8];
+#pragma unroll
+  for (int q = 0; q < VN; ++q)
+#pragma unroll
+    for (int c = 0; c < K8; ++c) acc[q][c] = T(0);
+  if constexpr (sizeof(T) == 4) {
+#pragma unroll
+    for (int t = 0; t < VN * K8; ++t) sD[t * ATU_THREADS + threadIdx.x] = 0.0;
+  }
+  for (int rb = r0; rb < r1; rb += RCH) {
+    const int nr = min(RCH, r1 - rb);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nr * K8; t += ATU_THREADS) sU[t] = Us[(int64_t)rb * K8 + t];
+    __syncthreads();
+    if (live) {
+      const T* ap = A + (int64_t)rb * lda + col;
+      int r = 0;
+      for (; r + UNR <= nr; r += UNR) {
+        typename Vec<T>::V v[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) v[u] = *reinterpret_cast<const typename Vec<T>::V*>(ap + (int64_t)(r + u) * lda);
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+          T a[VN];
+          unpack<T>(v[u], a);
+          const T* uu = sU + (r + u) * K8;
+#pragma unroll
+          for (int q = 0; q < VN; ++q)
+#pragma unroll
+            for (int c = 0; c < K8; ++c) acc[q][c] += a[q] * uu[c];
+        }
+      }
+      for (; r < nr; ++r) {
+        typename Vec<T>::V v = *reinterpret_cast<const typename Vec<T>::V*>(ap + (int64_t)r * lda);
+        T a[VN];
+        unpack<T>(v, a);
+        const T* uu = sU + r * K8;
+#pragma unroll
+        for (int q = 0; q < VN; ++q)
+#pragma unroll
+          for (int c = 0; c < K8; ++c) acc[q][c] += a[q] * uu[c];
+      }
+      if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int q = 0; q < VN; ++q)
+#pragma unroll
+          for (int c = 0; c < K8; ++c) {
+            sD[(q * K8 + c) * ATU_THREADS + threadIdx.x] += (double)acc[q][c];
+            acc[q][c] = T(0);
+          }
+      }
+    }
+  }
+  if (live) {
+#pragma unroll
+    for (int q = 0; q < VN; ++q)
+#pragma unroll
+      for (int c = 0; c < K8; ++c) {
+        double v;
+        if constexpr (sizeof(T) == 4) v = sD[(q * K8 + c) * ATU_THREADS + threadIdx.x];
+        else v = (double)acc[q][c];
+        Zp[((int64_t)g * lda + col + q) * K8 + c] = v;
+      }
+  }
+}
+
 // V <- Z/beta - beta V (Z = sum of group partials, in order); partial ||V||^2.
 // On the initial call (init=1) the old V is taken as zero.
 __global__ void k_atu_reduce(const double* __restrict__ Zp, int groups, int64_t lda, int n, const LsqrScalars* sc,
@@ -235,7 +507,8 @@ __global__ void k_atu_reduce(const double* __restrict__ Zp, int groups, int64_t 
 // dknorm partial += (t3 W_old)^2; Vs = (T)V.  init=1: W <- V, X <- 0.
 template <typename T>
 __global__ void k_update(int n, int64_t lda, const LsqrScalars* sc, int init, double* __restrict__ V,
-                         double* __restrict__ W, double* __restrict__ X, T* __restrict__ Vs, double* __restrict__ part) {
+                         double* __restrict__ W, double* __restrict__ X, T* __restrict__ Vs, double* __restrict__ part,
+                         int vs_rhs_major) {
   __shared__ double sP[kThreads / 32][K8];
   const int64_t t = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   const int64_t j = t / K8;
@@ -244,7 +517,7 @@ __global__ void k_update(int n, int64_t lda, const LsqrScalars* sc, int init, do
   if (j < lda) {
     const int64_t id = j * K8 + c;
     if (j >= n) {
-      V[id] = 0.0; W[id] = 0.0; X[id] = 0.0; Vs[id] = T(0);
+      V[id] = 0.0; W[id] = 0.0; X[id] = 0.0; Vs[vs_rhs_major ? (int64_t)c * lda + j : id] = T(0);
     } else {
       if (sc[c].active) {
         double v = V[id];
@@ -263,7 +536,7 @@ __global__ void k_update(int n, int64_t lda, const LsqrScalars* sc, int init, do
       } else if (init) {
         W[id] = 0.0; X[id] = 0.0;
       }
-      Vs[id] = (T)V[id];
+      Vs[vs_rhs_major ? (int64_t)c * lda + j : id] = (T)V[id];
     }
   }
   double s = dk;
@@ -495,9 +768,47 @@ __global__ void k_setup_tol(LsqrScalars* sc, int k, const double* part_b, int nb
 // ---------------------------------------------------------------------------
 static inline unsigned cdiv(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
 
+template <typename T>
+static void launch_resid(const DenseLsqr& L, const double* Xs, const double* Bp) {
+  const unsigned nb = cdiv(L.m, AV_ROWS);
+  k_av<T, double><<<nb, kThreads, 0, L.stream>>>((const T*)L.A, L.lda, L.m, L.n, Xs, -1.0, L.sc, 0, Bp, L.Y,
+                                                 (T*)L.Ys, L.part);
+}
+template <typename T>
+static unsigned av2_blocks(const DenseLsqr& L) { return cdiv(L.m, AV2<T>::WARPS * AV2<T>::RR); }
+template <typename T>
+static void launch_av2(const DenseLsqr& L) {
+  const size_t smem = 2 * K8 * AV2<T>::CH * sizeof(T);
+  k_av2<T><<<av2_blocks<T>(L), AV2<T>::WARPS * 32, smem, L.stream>>>((const T*)L.A, L.lda, L.m, (const T*)L.Vs, L.sc,
+                                                                     L.Y, (T*)L.Ys, L.part, L.errflag);
+}
+template <typename T>
+static size_t atu2_smem() {
+  return 256 * K8 * sizeof(T) + (sizeof(T) == 4 ? (size_t)Vec<T>::N * K8 * ATU_THREADS * sizeof(double) : 0);
+}
+template <typename T>
+static void launch_atu(const DenseLsqr& L) {
+  constexpr int vn = Vec<T>::N;
+  dim3 g(cdiv(L.lda, ATU_THREADS * vn), L.zgroups);
+  const int rpg = (int)((cdiv(L.m, L.zgroups) + 255) / 256 * 256);
+  k_atu2<T><<<g, ATU_THREADS, atu2_smem<T>(), L.stream>>>((const T*)L.A, L.lda, L.m, (const T*)L.Ys, rpg, L.Zp);
+}
+template <typename T>
+static cudaError_t set_sweep_attrs() {
+  cudaError_t e = cudaFuncSetAttribute(k_av2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(2 * K8 * AV2<T>::CH * sizeof(T)));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_atu2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)atu2_smem<T>());
+  return e;
+}
+
 void DenseLsqr::release() {
+  if (pev_ready)
+    for (int i = 0; i < 4 * 32; ++i) cudaEventDestroy(pev[i]);
+  pev_ready = false;
   cudaFree(Y); cudaFree(V); cudaFree(W); cudaFree(X); cudaFree(Z); cudaFree(Ys); cudaFree(Vs);
-  cudaFree(part); cudaFree(Zp); cudaFree(sc); cudaFree(nactive);
+  cudaFree(part); cudaFree(Zp); cudaFree(sc); cudaFree(nactive); cudaFree(XsD); cudaFree(errflag);
+  XsD = nullptr; errflag = nullptr;
   if (h_nactive) cudaFreeHost(h_nactive);
   Y = V = W = X = Z = nullptr; Ys = Vs = nullptr; part = Zp = nullptr; sc = nullptr; nactive = nullptr;
   h_nactive = nullptr;
@@ -520,12 +831,36 @@ bool DenseLsqr::setup(const void* A_dev, bool is_fp32, int m_, int n_, int64_t l
   CK(cudaMalloc(&Vs, lda * K8 * sizeof(double)));                            // T copy, or FP64 for residual
   // row groups for sweep 2: aim for >= 4 CTAs per SM
   const int vn = fp32 ? 4 : 2;
-  const int colblocks = (int)cdiv(lda, kThreads * vn);
-  int groups = std::max(1, std::min((int)cdiv(m, 256), (int)cdiv(152 * 8, colblocks)));
+  const int colblocks = (int)cdiv(lda, ATU_THREADS * vn);
+  // row groups of sweep 2: fill whole waves of resident CTAs
+  CK(fp32 ? set_sweep_attrs<float>() : set_sweep_attrs<double>());
+  int per_sm = 1, nsm = 152;
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (fp32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_atu2<float>, ATU_THREADS, atu2_smem<float>());
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_atu2<double>, ATU_THREADS, atu2_smem<double>());
+    per_sm = std::max(per_sm, 1);
+  }
+  const int slots = nsm * per_sm;
+  const int gmax = std::max(1, std::min((int)cdiv(m, 256), 64));
+  int groups = 1;
+  double best = -1.0;
+  for (int G = 1; G <= gmax; ++G) {
+    const int64_t items = (int64_t)colblocks * G;
+    const double eff = (double)items / (double)(cdiv(items, slots) * (int64_t)slots);
+    const double score = eff - 0.002 * G;  // prefer fewer partial sums at equal fill
+    if (items >= slots / 2 && score > best) { best = score; groups = G; }
+    if (best < 0 && G == gmax) groups = G;
+  }
   zgroups = groups;
+  CK(cudaMalloc(&XsD, lda * K8 * sizeof(double)));
+  CK(cudaMalloc(&errflag, sizeof(int)));
+  CK(cudaMemsetAsync(errflag, 0, sizeof(int), stream));
   CK(cudaMalloc(&Zp, (int64_t)groups * lda * K8 * sizeof(double)));
-  const int64_t nbmax = std::max<int64_t>({(int64_t)cdiv(m, AV_ROWS), (int64_t)cdiv(lda * K8, kThreads),
-                                           (int64_t)cdiv(mpad * K8, kThreads)});
+  const int64_t nbmax = std::max<int64_t>({(int64_t)cdiv(m, 16), (int64_t)cdiv(m, AV_ROWS),
+                                           (int64_t)cdiv(lda * K8, kThreads), (int64_t)cdiv(mpad * K8, kThreads)});
   part_cap = (size_t)nbmax * K8 * 2;
   CK(cudaMalloc(&part, part_cap * sizeof(double)));
   CK(cudaMalloc(&sc, K8 * sizeof(LsqrScalars)));
@@ -556,30 +891,13 @@ bool DenseLsqr::precon(void* A_dev, double* q_dev) {
   return true;
 }
 
-template <typename T>
-static void launch_av(const DenseLsqr& L, const void* Vin, bool vin_fp64, double s1, int use_gamma,
-                      const double* Yold) {
-  const unsigned nb = cdiv(L.m, AV_ROWS);
-  if (vin_fp64)
-    k_av<T, double><<<nb, kThreads, 0, L.stream>>>((const T*)L.A, L.lda, L.m, L.n, (const double*)Vin, s1, L.sc,
-                                                   use_gamma, Yold, L.Y, (T*)L.Ys, L.part);
-  else
-    k_av<T, T><<<nb, kThreads, 0, L.stream>>>((const T*)L.A, L.lda, L.m, L.n, (const T*)Vin, s1, L.sc, use_gamma,
-                                              Yold, L.Y, (T*)L.Ys, L.part);
-}
-template <typename T>
-static void launch_atu(const DenseLsqr& L) {
-  constexpr int vn = Vec<T>::N;
-  dim3 g(cdiv(L.lda, kThreads * vn), L.zgroups);
-  const int rpg = (int)((cdiv(L.m, L.zgroups) + 255) / 256 * 256);
-  k_atu<T><<<g, kThreads, 0, L.stream>>>((const T*)L.A, L.lda, L.m, (const T*)L.Ys, rpg, L.Zp);
-}
-
 bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, double eps, int maxit, int* nit_host,
                       int* istop_host, double* rnorm_host, int check_every) {
   if (maxit == 0) maxit = 10 * (m + n + 50);
   const int64_t mpad = ((int64_t)m + 255) / 256 * 256;
-  const unsigned nb_av = cdiv(m, AV_ROWS);
+  const unsigned nb_av = cdiv(m, AV_ROWS);  // residual sweep
+  const unsigned nb_av2 = fp32 ? av2_blocks<float>(*this) : av2_blocks<double>(*this);
+  CK(fp32 ? set_sweep_attrs<float>() : set_sweep_attrs<double>());
   const unsigned nb_red = cdiv((int64_t)n * K8, kThreads);
   const unsigned nb_upd = cdiv(lda * K8, kThreads);
   // stage: b -> Z (as [m][8]); x0 -> X0 buffer (as [n][8]); xs = x0/q -> Vs (FP64)
@@ -592,10 +910,10 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
   double* part_b = part + (part_cap / 2);
   if ((size_t)nb_b * K8 > part_cap / 2) { err = "partial buffer too small"; return false; }
   CK(cudaMemcpyAsync(part_b, part, (size_t)nb_b * K8 * sizeof(double), cudaMemcpyDeviceToDevice, stream));
-  k_pack<<<cdiv(lda * K8, 256), 256, 0, stream>>>(x_dev, n, k, lda, q_dev, (double*)Vs);
+  k_pack<<<cdiv(lda * K8, 256), 256, 0, stream>>>(x_dev, n, k, lda, q_dev, XsD);
   // residual Y = b - A (x0/q), FP64 accumulation
-  if (fp32) launch_av<float>(*this, Vs, true, -1.0, 0, Bp);
-  else launch_av<double>(*this, Vs, true, -1.0, 0, Bp);
+  if (fp32) launch_resid<float>(*this, XsD, Bp);
+  else launch_resid<double>(*this, XsD, Bp);
   k_scalars<<<1, 32, 0, stream>>>(sc, k, 0, part, nb_av, nactive);
   k_setup_tol<<<1, 32, 0, stream>>>(sc, k, part_b, nb_b, eps, maxit);
   // keep x0 (packed) for the final update: in X0 = W (W is rewritten by the init update,
@@ -605,19 +923,30 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
   if (fp32) launch_atu<float>(*this); else launch_atu<double>(*this);
   k_atu_reduce<<<nb_red, kThreads, 0, stream>>>(Zp, zgroups, lda, n, sc, 1, V, part);
   k_scalars<<<1, 32, 0, stream>>>(sc, k, 1, part, nb_red, nactive);
-  if (fp32) k_update<float><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 1, V, W, X, (float*)Vs, part);
-  else k_update<double><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 1, V, W, X, (double*)Vs, part);
+  if (fp32) k_update<float><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 1, V, W, X, (float*)Vs, part, 1);
+  else k_update<double><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 1, V, W, X, (double*)Vs, part, 1);
   CK(cudaGetLastError());
 
+  if (check_every > 32) check_every = 32;
+  if (!pev_ready) {
+    for (int i = 0; i < 4 * 32; ++i) CK(cudaEventCreate(&pev[i]));
+    pev_ready = true;
+  }
+  int it_in_graph = 0;
   auto iteration = [&]() {
-    if (fp32) launch_av<float>(*this, Vs, false, 1.0, 1, Y);
-    else launch_av<double>(*this, Vs, false, 1.0, 1, Y);
-    k_scalars<<<1, 32, 0, stream>>>(sc, k, 2, part, nb_av, nactive);
+    const int e = 4 * it_in_graph++;
+    cudaEventRecordWithFlags(pev[e], stream, cudaEventRecordExternal);
+    if (fp32) launch_av2<float>(*this);
+    else launch_av2<double>(*this);
+    cudaEventRecordWithFlags(pev[e + 1], stream, cudaEventRecordExternal);
+    k_scalars<<<1, 32, 0, stream>>>(sc, k, 2, part, nb_av2, nactive);
+    cudaEventRecordWithFlags(pev[e + 2], stream, cudaEventRecordExternal);
     if (fp32) launch_atu<float>(*this); else launch_atu<double>(*this);
+    cudaEventRecordWithFlags(pev[e + 3], stream, cudaEventRecordExternal);
     k_atu_reduce<<<nb_red, kThreads, 0, stream>>>(Zp, zgroups, lda, n, sc, 0, V, part);
     k_scalars<<<1, 32, 0, stream>>>(sc, k, 3, part, nb_red, nactive);
-    if (fp32) k_update<float><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 0, V, W, X, (float*)Vs, part);
-    else k_update<double><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 0, V, W, X, (double*)Vs, part);
+    if (fp32) k_update<float><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 0, V, W, X, (float*)Vs, part, 1);
+    else k_update<double><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 0, V, W, X, (double*)Vs, part, 1);
     cudaMemsetAsync(nactive, 0, sizeof(int), stream);
     k_scalars<<<1, 32, 0, stream>>>(sc, k, 4, part, nb_upd, nactive);
   };
@@ -639,6 +968,12 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
     CK(cudaGraphLaunch(gexec, stream));
     CK(cudaMemcpyAsync(h_nactive, nactive, sizeof(int), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
+    for (int i = 0; i < check_every; ++i) {
+      float a = 0.f, b = 0.f;
+      if (cudaEventElapsedTime(&a, pev[4 * i], pev[4 * i + 1]) == cudaSuccess) { t_av += a; ++n_av; }
+      if (cudaEventElapsedTime(&b, pev[4 * i + 2], pev[4 * i + 3]) == cudaSuccess) { t_atu += b; ++n_atu; }
+    }
+    (void)cudaGetLastError();  // a timing query must not leak into the error checks
     iters += check_every;
     act = *h_nactive;
   }
@@ -649,6 +984,9 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
   CK(cudaMemcpyAsync(hs, sc, sizeof(hs), cudaMemcpyDeviceToHost, stream));
   CK(cudaStreamSynchronize(stream));
   CK(cudaGetLastError());
+  int hflag = 0;
+  CK(cudaMemcpy(&hflag, errflag, sizeof(int), cudaMemcpyDeviceToHost));
+  if (hflag) { err = "a bounded barrier wait in the A*V sweep gave up"; return false; }
   for (int c = 0; c < k; ++c) {
     if (nit_host) nit_host[c] = hs[c].itn;
     if (istop_host) istop_host[c] = hs[c].istop;
@@ -660,9 +998,9 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
 bool DenseLsqr::residual(const double* b_dev, const double* x_dev, const double* q_dev, double* r_dev) {
   const int64_t mpad = ((int64_t)m + 255) / 256 * 256;
   k_pack<<<cdiv(mpad * K8, 256), 256, 0, stream>>>(b_dev, m, k, mpad, nullptr, Z);
-  k_pack<<<cdiv(lda * K8, 256), 256, 0, stream>>>(x_dev, n, k, lda, q_dev, (double*)Vs);
-  if (fp32) launch_av<float>(*this, Vs, true, -1.0, 0, Z);
-  else launch_av<double>(*this, Vs, true, -1.0, 0, Z);
+  k_pack<<<cdiv(lda * K8, 256), 256, 0, stream>>>(x_dev, n, k, lda, q_dev, XsD);
+  if (fp32) launch_resid<float>(*this, XsD, Z);
+  else launch_resid<double>(*this, XsD, Z);
   // unpack Y -> r (column-major)
   for (int c = 0; c < k; ++c)
     CK(cudaMemcpy2DAsync(r_dev + (int64_t)c * m, sizeof(double), Y + c, K8 * sizeof(double), sizeof(double), m,
@@ -892,7 +1230,7 @@ bool crs_lsqr_solve(int m, int n, int64_t nnz, int& maxit, double eps, int& nit,
   k_csc_atu<<<cdiv((int64_t)n * 32, kThreads), kThreads, 0, s>>>(n, D.cp, D.rows, D.av, Ys, Zp);
   k_atu_reduce<<<nb_red, kThreads, 0, s>>>(Zp, 1, lda, n, sc, 1, V, part);
   k_scalars<<<1, 32, 0, s>>>(sc, 1, 1, part, nb_red, nact);
-  k_update<double><<<nb_upd, kThreads, 0, s>>>(n, lda, sc, 1, V, W, X, Vs, part);
+  k_update<double><<<nb_upd, kThreads, 0, s>>>(n, lda, sc, 1, V, W, X, Vs, part, 0);
   CK(cudaGetLastError());
   LsqrScalars hs;
   int act = 1;
@@ -909,7 +1247,7 @@ bool crs_lsqr_solve(int m, int n, int64_t nnz, int& maxit, double eps, int& nit,
     k_csc_atu<<<cdiv((int64_t)n * 32, kThreads), kThreads, 0, s>>>(n, D.cp, D.rows, D.av, Ys, Zp);
     k_atu_reduce<<<nb_red, kThreads, 0, s>>>(Zp, 1, lda, n, sc, 0, V, part);
     k_scalars<<<1, 32, 0, s>>>(sc, 1, 3, part, nb_red, nact);
-    k_update<double><<<nb_upd, kThreads, 0, s>>>(n, lda, sc, 0, V, W, X, Vs, part);
+    k_update<double><<<nb_upd, kThreads, 0, s>>>(n, lda, sc, 0, V, W, X, Vs, part, 0);
     cudaMemsetAsync(nact, 0, sizeof(int), s);
     k_scalars<<<1, 32, 0, s>>>(sc, 1, 4, part, nb_upd, nact);
   }

@@ -28,13 +28,21 @@ struct DenseLsqr {
   cudaStream_t stream = 0;
   // device work buffers (FP64 unless noted)
   double *Y = nullptr, *V = nullptr, *W = nullptr, *X = nullptr, *Z = nullptr;
-  void *Ys = nullptr, *Vs = nullptr;  // T copies used by the sweeps
+  void *Ys = nullptr, *Vs = nullptr;  // T copies used by the sweeps (Ys [m][8], Vs [8][lda])
+  double* XsD = nullptr;       // x0./q packed [lda][8] for the FP64-accumulated residual
+  int* errflag = nullptr;      // set by a kernel whose bounded wait gave up
   double* part = nullptr;      // per-CTA partial sums
   double* Zp = nullptr;        // per-row-group partial products of A^T Y
   LsqrScalars* sc = nullptr;   // k entries
   int* nactive = nullptr;      // device counter
   int* h_nactive = nullptr;    // pinned host mirror
   int zgroups = 0;
+  // live per-kernel timing of the two sweeps (CUDA events recorded inside the
+  // iteration graph on the solver stream)
+  cudaEvent_t pev[4 * 32] = {};
+  bool pev_ready = false;
+  double t_av = 0.0, t_atu = 0.0;
+  long n_av = 0, n_atu = 0;
   size_t part_cap = 0;
   std::string err;
 

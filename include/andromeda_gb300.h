@@ -139,6 +139,15 @@ int agb_force_torque(agb_context* ctx, int nrhs, const double* x, int wall, doub
 int agb_resistance_tensor(agb_context* ctx, int precision, int particle_wall, int outer_wall, int maxit, double eps,
                           int refine, double* R, int* nit, double* times_ms);
 
+/* Live kernel timing (instrumentation; plays the role of the reference's
+ * TIMER stopwatches, stokes.f90:88-92, at kernel granularity).  Cumulative
+ * CUDA-event times on the context stream since the last reset:
+ * out[0] ms in the A*V sweep, out[1] its launches, out[2] ms in the A^T*U
+ * sweep, out[3] its launches, out[4] ms in the Stokes single-layer assembly
+ * kernel, out[5] its launches, out[6] ms building right-hand sides, out[7]
+ * its calls.  reset != 0 zeroes the counters after reading. */
+int agb_kernel_times(agb_context* ctx, int reset, double* out);
+
 /* Drop-ins with the reference signatures (1-based CRS, int64 row pointers).
  * agb_lsqr_precon scales a in place like lsqr_precon; agb_lsqr_solve
  * warm-starts from x like lsqr_solve.  Both run on the current CUDA device. */
