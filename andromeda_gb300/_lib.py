@@ -36,7 +36,7 @@ SIGNATURES = {
     "agb_rhs": ([vp, I, dp, dp], I),
     "agb_solve": ([vp, I, dp, dp, I, D, I, ip, ip], I),
     "agb_force_torque": ([vp, I, dp, I, dp], I),
-    "agb_resistance_tensor": ([vp, I, I, I, I, D, I, dp, ip, dp], I),
+    "agb_resistance_tensor": ([vp, I, I, I, I, D, I, dp, ip, ip, dp], I),
     "agb_kernel_times": ([vp, I, dp], I),
     "agb_lsqr_precon": ([I, I, C.c_int64, dp, lp, ip, dp], I),
     "agb_lsqr_solve": ([I, I, C.c_int64, PI, D, PI, PI, dp, lp, ip, dp, dp, dp], I),

@@ -163,18 +163,23 @@ class Context:
 
     def kernel_times(self, reset=False):
         """Cumulative live kernel times (ms) and launch counts since the last reset."""
-        out = np.zeros(8)
+        out = np.zeros(10)
         self._ck(self._L.agb_kernel_times(self.h, int(bool(reset)), out))
         return {"av_ms": out[0], "av_launches": int(out[1]), "atu_ms": out[2], "atu_launches": int(out[3]),
-                "assemble_ms": out[4], "assemble_launches": int(out[5]), "rhs_ms": out[6], "rhs_calls": int(out[7])}
+                "assemble_ms": out[4], "assemble_launches": int(out[5]), "rhs_ms": out[6], "rhs_calls": int(out[7]),
+                "launches": int(out[8])}
 
     def resistance_tensor(self, precision=MIXED, particle_wall=1, outer_wall=2, maxit=0, eps=1e-8, refine=0):
+        """Returns (R[6,6], nit[6], info): R[r] = (F, T) on the particle for rigid
+        motion r of the container (e_x, e_y, e_z translations, then rotations)."""
         R = np.zeros((6, 6))
         nit = np.zeros(6, np.int32)
-        t = np.zeros(5)
+        istop = np.zeros(6, np.int32)
+        t = np.zeros(6)
         self._ck(self._L.agb_resistance_tensor(self.h, int(precision), int(particle_wall), int(outer_wall), int(maxit),
-                                               float(eps), int(refine), R.reshape(-1), nit, t))
-        return R, nit, {"assemble_ms": t[0], "rhs_ms": t[1], "solve_ms": t[2], "reduce_ms": t[3], "total_ms": t[4]}
+                                               float(eps), int(refine), R.reshape(-1), nit, istop, t))
+        return R, nit, {"assemble_ms": t[0], "rhs_ms": t[1], "solve_ms": t[2], "reduce_ms": t[3], "total_ms": t[4],
+                        "device_ms": t[5], "istop": istop.tolist()}
 
 
 def dirichlet_known(kind, nwalls):

@@ -66,6 +66,8 @@ struct agb_context {
   cudaEvent_t tev[4] = {};
   double t_asm = 0.0, t_rhs = 0.0;
   long n_asm = 0, n_rhs = 0;
+  long nlaunch = 0;  // kernels launched outside the solver
+  long lsqr_prev_launches = 0;  // launches of solver instances since replaced
 };
 
 namespace {
@@ -213,6 +215,7 @@ int device_rhs(agb_context* c, int nrhs, int na) {
     if (c->prec == AGB_MIXED) CUDA_OR_FAIL(c, launch_stokes_rhs<float>(a, c->stream));
     else CUDA_OR_FAIL(c, launch_stokes_rhs<double>(a, c->stream));
     cudaEventRecord(c->tev[3], c->stream);
+    c->nlaunch += (na > 0) ? 3 : 1;
     CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, c->tev[2], c->tev[3]) == cudaSuccess) { c->t_rhs += ms; ++c->n_rhs; }
@@ -223,6 +226,7 @@ int device_rhs(agb_context* c, int nrhs, int na) {
     a.geom = c->d_geom; a.rule_l = c->rule.l; a.rule_w = c->rule.w; a.u = c->d_u; a.diff = c->diff;
     a.A = nullptr; a.lda = c->lda; a.rhs = c->d_rhs;
     cudaError_t e = launch_laplace_system(a, c->stream);
+    c->nlaunch += 1;
     CUDA_OR_FAIL(c, e);
   }
   return AGB_OK;
@@ -382,6 +386,7 @@ int agb_set_problem(agb_context* c, int kind, int nwalls, const int* walls, cons
   CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_normMul, c->normMul.data(), nwalls * sizeof(double), cudaMemcpyHostToDevice,
                                   c->stream));
   CUDA_OR_FAIL(c, launch_geometry(c->ne, c->d_xyz, c->d_etype, c->d_con, c->d_wall, c->d_normMul, c->d_geom, c->stream));
+  c->nlaunch += 1;
   std::vector<double> l, w;
   expand_rule(itri, l, w);
   c->rule.Q = (int)w.size();
@@ -463,6 +468,7 @@ int agb_assemble(agb_context* c, int precision) {
                                              (const float*)c->d_colscale, (float*)c->d_A, c->lda, c->stream));
       cudaEventRecord(c->tev[1], c->stream);
       CUDA_OR_FAIL(c, launch_stokes_self<float>(c->ne, c->d_geom, c->diff, (float*)c->d_A, c->lda, c->stream));
+      c->nlaunch += 3;  // expand, single layer, self blocks
     } else {
       CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_colscale, cs.data(), ldp * sizeof(double), cudaMemcpyHostToDevice, c->stream));
       CUDA_OR_FAIL(c, launch_expand_points<double>(c->ne, ldp, c->d_geom, c->rule, (QPt<double>*)c->d_pts,
@@ -472,6 +478,7 @@ int agb_assemble(agb_context* c, int precision) {
                                               (const double*)c->d_colscale, (double*)c->d_A, c->lda, c->stream));
       cudaEventRecord(c->tev[1], c->stream);
       CUDA_OR_FAIL(c, launch_stokes_self<double>(c->ne, c->d_geom, c->diff, (double*)c->d_A, c->lda, c->stream));
+      c->nlaunch += 3;
     }
     CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
     float ms = 0.f;
@@ -483,6 +490,7 @@ int agb_assemble(agb_context* c, int precision) {
     a.geom = c->d_geom; a.rule_l = c->rule.l; a.rule_w = c->rule.w; a.u = nullptr; a.diff = c->diff;
     a.A = (double*)c->d_A; a.lda = c->lda; a.rhs = nullptr;
     CUDA_OR_FAIL(c, launch_laplace_system(a, c->stream));
+    c->nlaunch += 1;
   }
   // column scaling of lsqr_precon
   if (!c->lsqr.setup(c->d_A, f32, c->m, c->n, c->lda, 1, c->stream)) return fail(c, AGB_ERR_CUDA, c->lsqr.err);
@@ -563,13 +571,14 @@ int agb_force_torque(agb_context* c, int nrhs, const double* x, int wall, double
   CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_x, x, (size_t)nrhs * c->n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   if (!c->d_ft) CUDA_OR_FAIL(c, cudaMalloc(&c->d_ft, 6 * AGB_MAX_RHS * sizeof(double)));
   CUDA_OR_FAIL(c, launch_force_torque(c->ne, nrhs, c->d_geom, c->d_x, widx, c->d_ft, c->stream));
+  c->nlaunch += 1;
   CUDA_OR_FAIL(c, cudaMemcpyAsync(ft, c->d_ft, 6 * (size_t)nrhs * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
   return AGB_OK;
 }
 
 int agb_resistance_tensor(agb_context* c, int precision, int particle_wall, int outer_wall, int maxit, double eps,
-                          int refine, double* R, int* nit, double* times_ms) {
+                          int refine, double* R, int* nit, int* istop, double* times_ms) {
   int rc = check_ctx(c, true);
   if (rc) return rc;
   if (c->kind != AGB_STOKES) return fail(c, AGB_ERR_UNSUPPORTED, "resistance tensor needs a Stokes problem");
@@ -583,6 +592,10 @@ int agb_resistance_tensor(agb_context* c, int precision, int particle_wall, int 
   cudaSetDevice(c->device);
   using clk = std::chrono::steady_clock;
   auto ms = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
+  cudaEvent_t d0 = nullptr, d1 = nullptr;
+  CUDA_OR_FAIL(c, cudaEventCreate(&d0));
+  CUDA_OR_FAIL(c, cudaEventCreate(&d1));
+  CUDA_OR_FAIL(c, cudaEventRecord(d0, c->stream));
   auto t0 = clk::now();
   if ((rc = agb_assemble(c, precision))) return rc;
   auto t1 = clk::now();
@@ -616,20 +629,27 @@ int agb_resistance_tensor(agb_context* c, int precision, int particle_wall, int 
   auto t3 = clk::now();
   if (!c->d_ft) CUDA_OR_FAIL(c, cudaMalloc(&c->d_ft, 6 * AGB_MAX_RHS * sizeof(double)));
   CUDA_OR_FAIL(c, launch_force_torque(c->ne, k, c->d_geom, c->d_x, pidx, c->d_ft, c->stream));
+  c->nlaunch += 1;
   CUDA_OR_FAIL(c, cudaMemcpyAsync(R, c->d_ft, 36 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaEventRecord(d1, c->stream));
   CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
   auto t4 = clk::now();
-  if (nit)
-    for (int r = 0; r < k; ++r) nit[r] = nt[r];
+  float dev_ms = 0.f;
+  CUDA_OR_FAIL(c, cudaEventElapsedTime(&dev_ms, d0, d1));
+  cudaEventDestroy(d0);
+  cudaEventDestroy(d1);
+  for (int r = 0; r < k; ++r) {
+    if (nit) nit[r] = nt[r];
+    if (istop) istop[r] = is[r];
+  }
   if (times_ms) {
     times_ms[0] = ms(t0, t1);
     times_ms[1] = ms(t1, t2);
     times_ms[2] = ms(t2, t3);
     times_ms[3] = ms(t3, t4);
     times_ms[4] = ms(t0, t4);
+    times_ms[5] = dev_ms;
   }
-  for (int r = 0; r < k; ++r)
-    if (is[r] > 3) return fail(c, AGB_ERR_NUMERIC, "LSQR stopped with istop > 3 (iteration limit or ill conditioning)");
   return AGB_OK;
 }
 
@@ -669,12 +689,17 @@ int agb_kernel_times(agb_context* c, int reset, double* out) {
     out[2] = c->lsqr.t_atu; out[3] = (double)c->lsqr.n_atu;
     out[4] = c->t_asm;      out[5] = (double)c->n_asm;
     out[6] = c->t_rhs;      out[7] = (double)c->n_rhs;
+    out[8] = (double)(c->nlaunch + c->lsqr.launches + c->lsqr_prev_launches);
+    out[9] = 0.0;
   }
   if (reset) {
     c->lsqr.t_av = c->lsqr.t_atu = 0.0;
     c->lsqr.n_av = c->lsqr.n_atu = 0;
     c->t_asm = c->t_rhs = 0.0;
     c->n_asm = c->n_rhs = 0;
+    c->nlaunch = 0;
+    c->lsqr.launches = 0;
+    c->lsqr_prev_launches = 0;
   }
   return AGB_OK;
 }

@@ -887,6 +887,7 @@ bool DenseLsqr::precon(void* A_dev, double* q_dev) {
   unsigned blocks = (unsigned)std::min<int64_t>(cdiv(tot, 256), 152 * 64);
   if (fp32) k_scale_cols<float><<<blocks, 256, 0, stream>>>((float*)A_dev, lda, m, q_dev);
   else k_scale_cols<double><<<blocks, 256, 0, stream>>>((double*)A_dev, lda, m, q_dev);
+  launches += 3;
   CK(cudaGetLastError());
   return true;
 }
@@ -925,6 +926,7 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
   k_scalars<<<1, 32, 0, stream>>>(sc, k, 1, part, nb_red, nactive);
   if (fp32) k_update<float><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 1, V, W, X, (float*)Vs, part, 1);
   else k_update<double><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 1, V, W, X, (double*)Vs, part, 1);
+  launches += 11;
   CK(cudaGetLastError());
 
   if (check_every > 32) check_every = 32;
@@ -966,6 +968,7 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
   int iters = 0;
   while (act > 0 && iters < maxit + check_every) {
     CK(cudaGraphLaunch(gexec, stream));
+    launches += 7L * check_every;
     CK(cudaMemcpyAsync(h_nactive, nactive, sizeof(int), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
     for (int i = 0; i < check_every; ++i) {
@@ -981,6 +984,7 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
   cudaGraphDestroy(graph);
   // x = q .* dx + x0
   k_finish_x<<<cdiv((int64_t)n * k, 256), 256, 0, stream>>>(X, q_dev, Bp, n, k, sc, x_dev);
+  launches += 1;
   CK(cudaMemcpyAsync(hs, sc, sizeof(hs), cudaMemcpyDeviceToHost, stream));
   CK(cudaStreamSynchronize(stream));
   CK(cudaGetLastError());

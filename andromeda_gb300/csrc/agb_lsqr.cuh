@@ -43,6 +43,7 @@ struct DenseLsqr {
   bool pev_ready = false;
   double t_av = 0.0, t_atu = 0.0;
   long n_av = 0, n_atu = 0;
+  long launches = 0;           // kernels launched by precon/solve
   size_t part_cap = 0;
   std::string err;
 

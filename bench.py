@@ -1,0 +1,375 @@
+#!/usr/bin/env python3
+"""Stokes resistance-tensor solves/s on GB300 (one JSON line on stdout).
+
+Workload (configuration 2 of the benchmark plan): a rigid sphere of radius
+a = 1 meshed as an icosahedral sphere of level 5 (20480 flat triangles,
+10242 nodes), inside a spherical container of radius 200 (level 2, 320
+triangles) -- the bounded geometry every particle case of the reference
+uses.  Viscosity 1, ITRI 5 (126-point Wandzura-Xiao rule), all walls with
+known velocity, six right-hand sides = the container's unit translations and
+rotations.  One solve = assembly of the 62400 x 62400 single-layer system,
+its right-hand sides, block LSQR of the six fields to eps, force and torque
+on the sphere (the 6x6 resistance tensor).  Inputs: synthetic meshes built
+in-process (no dataset); the 15.6 GB system matrix is far larger than L2, so
+no L2 flush is needed between timed steps.
+
+--impl ours (default): the mixed-precision GPU path through the C ABI.
+--impl reference: the reference's algorithm on the host cores (the FP64 C++
+restatement in oracle/, since the Fortran reference cannot be compiled on
+this image or the GPU machine), timed on a bounded sample and scaled to one solve.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Stokes resistance-tensor solves/s at <=1e-6 rel err: mixed/batched vs FP64 GPU"
+GOLDEN_TRUTH = os.path.join(ROOT, "tests", "golden", "c2_fp64_tensor.json")
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "lsqr_sweeps_traffic.json")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--level", type=int, default=5)
+    ap.add_argument("--outer-level", type=int, default=2)
+    ap.add_argument("--outer-radius", type=float, default=200.0)
+    ap.add_argument("--eps", type=float, default=1e-7)
+    ap.add_argument("--fp64-iters", type=int, default=16, help="FP64 comparator LSQR sample (iterations)")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    return ap.parse_args()
+
+
+def workload(args):
+    from andromeda_gb300 import mesh as M
+    p = M.icosphere(args.level, 1.0, inward=True)
+    m = M.particle_in_sphere(p, outer_level=args.outer_level, outer_radius=args.outer_radius)
+    name = (f"Stokes sphere a=1 icosphere L{args.level} ({len(p['etype'])} tri) in L{args.outer_level} container "
+            f"r={args.outer_radius:g} ({len(m['etype']) - len(p['etype'])} tri), 6 RHS, ITRI 5, mu=1, "
+            f"LSQR eps {args.eps:g}")
+    return m, name
+
+
+def rigid_fields(m, outer_wall=2):
+    import numpy as np
+    nn = len(m["xyz"])
+    on = np.zeros(nn, bool)
+    for e in np.where(m["bcid"] == outer_wall)[0]:
+        on[m["con"][e, :3]] = True
+    U = np.zeros((6, 3, nn))
+    for i in range(3):
+        U[i, i, on] = 1.0
+        w = np.zeros(3)
+        w[i] = 1.0
+        U[3 + i][:, on] = np.cross(w, m["xyz"][on]).T
+    return U
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+
+    def __init__(self, index=0):
+        self.cmd = ["nvidia-smi", "-i", str(index),
+                    "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                    "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                    "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                    "--format=csv,noheader,nounits", "-lms", "200"]
+        self.p = None
+        self.out = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(self.cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+                self.out, _ = self.p.communicate()
+
+    def summary(self):
+        if not self.out:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the FP64 restatement of the reference on the host cores
+# ---------------------------------------------------------------------------
+def cpu_baseline(m, nit_total, budget_s):
+    """Time a bounded sample of the reference algorithm and scale it to one
+    resistance-tensor solve of the same workload:
+      * integration: CoR_Integrals_Stokes computes all nsp = nnodes + nelem
+        rows (u- and q-source points, 18 component matrices); a slice of
+        rows is timed with all host threads and scaled by nsp;
+      * LSQR: the reference's serial CRS lsqr_solve; iterations on a smaller
+        system of the same kind are timed per nonzero and scaled to the
+        62400^2 system and to the iterations the solve needs (sum over the six
+        sequential right-hand sides)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from andromeda_gb300 import mesh as M
+    threads = os.cpu_count() or 1
+    P = oracle.Problem(2, m, walls=[1, 2], known=np.ones((3, 2)), itri=5)
+    nsp = P.nsp
+    # rows: start from the q-source rows (the used ones) -- same cost per row
+    t_row, rows = 0.0, 0
+    r0 = P.sd_nnodes
+    chunk = threads
+    t_start = time.perf_counter()
+    while time.perf_counter() - t_start < 0.5 * budget_s and rows < 4 * threads * 8:
+        t, _ = P.time_rows(r0 + rows, r0 + rows + chunk, threads, )
+        t_row += t
+        rows += chunk
+    P.close()
+    t_integration = t_row / rows * nsp
+    # LSQR on a smaller problem of the same kind (level-3 sphere in container)
+    ms = M.particle_in_sphere(M.icosphere(3, 1.0, inward=True), outer_level=2, outer_radius=200.0)
+    Ps = oracle.Problem(2, ms, walls=[1, 2], known=np.ones((3, 2)), itri=1)
+    Ps.form_integrals()
+    Ps.form_system()
+    ia, ja, a = Ps.crs(0)
+    q = oracle.lsqr_precon(Ps.neq_rows, Ps.nx, ia, ja, a)
+    b = np.random.default_rng(0).normal(size=Ps.neq_rows)
+    it = 8
+    while True:
+        x = np.zeros(Ps.nx)
+        t0 = time.perf_counter()
+        oracle.lsqr_solve(Ps.neq_rows, Ps.nx, ia, ja, a, q, b, x, maxit=it, eps=1e-30)
+        dt = time.perf_counter() - t0
+        if dt > 0.25 * budget_s or it >= 4096:
+            break
+        it *= 2
+    per_nnz_iter = dt / (it * len(a))
+    nnz_full = float(3 * len(m["etype"])) ** 2
+    t_lsqr = per_nnz_iter * nnz_full * nit_total
+    total = t_integration + t_lsqr
+    sample = (f"{rows} of {nsp} integration rows on {threads} threads (scaled by nsp) + {it} serial CRS LSQR "
+              f"iterations on a {Ps.neq_rows}^2 system of the same kind (scaled by nnz to {3 * len(m['etype'])}^2 and "
+              f"to {nit_total} iterations = sum over the 6 sequential right-hand sides)")
+    return {"value": 1.0 / total, "unit": "solves/s", "cores": threads, "kind": "port", "sample": sample,
+            "seconds_per_solve": total, "integration_s": t_integration, "lsqr_s": t_lsqr,
+            "lsqr_threads": 1}
+
+
+# LSQR iterations of this workload at eps 1e-7, measured on the GPU path
+# (763 per translation, 250 per rotation); the reference solves the six
+# right-hand sides one after another, so its iteration total is their sum.
+C2_NIT_EPS1E7 = [763, 763, 763, 250, 251, 250]
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    m, name = workload(args)
+    nit_total = sum(C2_NIT_EPS1E7) if (args.level == 5 and abs(args.eps - 1e-7) < 1e-12) else 6 * 500
+    vals = []
+    info = None
+    for _ in range(args.steps):
+        info = cpu_baseline(m, nit_total, args.cpu_seconds)
+        vals.append(info["value"])
+    v = statistics.median(vals)
+    line = {"metric": METRIC, "value": v, "unit": "solves/s", "impl": "reference", "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": name, "iterations_assumed": nit_total},
+            "cpu_baseline": {k: info[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    import numpy as np
+    import andromeda_gb300 as A
+    from andromeda_gb300 import build as B
+    if not os.path.exists(A.LIB_PATH):
+        B.build()
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    m, name = workload(args)
+    C = A.Context(local if world > 1 else 0)
+    C.set_mesh(m)
+    C.set_problem(A.STOKES, [1, 2], A.dirichlet_known(A.STOKES, 2), itri=5)
+
+    def step():
+        return C.resistance_tensor(A.MIXED, 1, 2, eps=args.eps)
+
+    for _ in range(args.warmup):
+        step()
+    C.kernel_times(reset=True)
+    if dist is not None:
+        dist.barrier()
+    dev_ms, host_ms, Rs, nits = [], [], [], []
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            R, nit, info = step()
+            dev_ms.append(info["device_ms"])
+            Rs.append(R)
+            nits.append(nit)
+        t1 = time.perf_counter()
+    kt = C.kernel_times(reset=True)
+    elapsed = sum(dev_ms) / 1000.0
+    if dist is not None:
+        import torch
+        t = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    value = world * args.steps / elapsed
+    R = Rs[-1]
+    nit = nits[-1]
+
+    # accuracy against the FP64 GPU path (frozen truth of this workload)
+    rel_err = None
+    if os.path.exists(GOLDEN_TRUTH):
+        with open(GOLDEN_TRUTH) as f:
+            g = json.load(f)
+        if g.get("workload") == name.split(", LSQR")[0]:
+            Rt = np.array(g["R"])
+            rel_err = float(np.max(np.abs(R - Rt)) / np.max(np.abs(Rt)))
+    lam = 1.0 / args.outer_radius
+    K = (1 - lam ** 5) / (1 - 9 / 4 * lam + 5 / 2 * lam ** 3 - 9 / 4 * lam ** 5 + lam ** 6)
+    drag_ratio = float(np.mean(np.diag(R[:3, :3])) / (6 * np.pi * K))
+    torque_ratio = float(np.mean(np.diag(R[3:, 3:])) / (8 * np.pi / (1 - lam ** 3)))
+
+    # roofline of the dominant kernel (A*V sweep of LSQR), live CUDA-event timing
+    peak, peak_kind = measured_peaks()
+    lda = (C.n + 31) // 32 * 32
+    a_bytes = C.m * lda * 4
+    av_ms = kt["av_ms"] / max(kt["av_launches"], 1)
+    atu_ms = kt["atu_ms"] / max(kt["atu_launches"], 1)
+    traffic = None
+    if os.path.exists(PROFILE_TRAFFIC):
+        with open(PROFILE_TRAFFIC) as f:
+            pt = json.load(f)
+        traffic = pt.get("k_av2_bytes_per_launch_c2")
+    roofline = {"bound": "hbm", "kernel": "k_av2 (LSQR A*V sweep, FP32 A, 8 RHS)",
+                "achieved": a_bytes / (av_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                "frac": a_bytes / (av_ms * 1e-3) / 1e9 / peak, "traffic": traffic, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": a_bytes,
+                "other_sweep": {"kernel": "k_atu2 (A^T*U)", "achieved": a_bytes / (atu_ms * 1e-3) / 1e9,
+                                "frac": a_bytes / (atu_ms * 1e-3) / 1e9 / peak}}
+
+    # end to end through the C ABI with host buffers (mesh upload + solve + R back)
+    e2e_vals = []
+    h2d = (m["xyz"].nbytes + m["etype"].nbytes + m["con"].nbytes + m["bcid"].nbytes +
+           6 * 3 * len(m["xyz"]) * 8 + 2 * 4 + 2 * 8 + 6 * 4)
+    d2h = 36 * 8 + 6 * 4 * 2 + 6 * 8
+    for _ in range(args.e2e_steps):
+        t2 = time.perf_counter()
+        C2 = A.Context(local if world > 1 else 0)
+        C2.set_mesh(m)
+        C2.set_problem(A.STOKES, [1, 2], A.dirichlet_known(A.STOKES, 2), itri=5)
+        C2.resistance_tensor(A.MIXED, 1, 2, eps=args.eps)
+        C2.close()
+        e2e_vals.append(time.perf_counter() - t2)
+    e2e = {"value": world / statistics.median(e2e_vals), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h)}
+
+    # plain FP64 GPU comparator: full FP64 assembly + a sample of FP64 LSQR
+    # iterations, scaled to the iteration count of the solve
+    fp64 = None
+    if args.fp64_iters > 0 and rank == 0:
+        C.kernel_times(reset=True)
+        R64, nit64, info64 = C.resistance_tensor(A.FP64, 1, 2, maxit=args.fp64_iters, eps=args.eps)
+        kt64 = C.kernel_times(reset=True)
+        per_it = (kt64["av_ms"] + kt64["atu_ms"]) / max(kt64["av_launches"], 1)
+        nmax = int(max(nit))
+        est_ms = info64["assemble_ms"] + info64["rhs_ms"] + info64["reduce_ms"] + per_it * nmax
+        fp64 = {"solves_per_s_est": 1000.0 / est_ms, "assemble_ms": info64["assemble_ms"],
+                "ms_per_iteration_sweeps": per_it, "iterations_scaled_to": nmax,
+                "sample_iterations": int(max(nit64)),
+                "ratio_mixed_over_fp64": value / world / (1000.0 / est_ms)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            cb = cpu_baseline(m, int(np.sum(nit)), args.cpu_seconds)
+            cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        except Exception as ex:  # the baseline must not hide the GPU line
+            cpu = {"value": None, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"failed: {ex}"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (fp64 singular/free-term/reductions)",
+                "data": "synthetic (meshes generated in-process)",
+                "config": {"workload": name, "precision": "mixed", "unknowns": C.n,
+                           "parallelism": "replicas" if world > 1 else "single GPU",
+                           "l2": "inputs larger than L2 (15.6 GB matrix), no flush"},
+                "rel_err_vs_fp64": rel_err, "drag_over_analytic": drag_ratio, "torque_over_analytic": torque_ratio,
+                "nit": [int(v) for v in nit], "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+                "clocks": clk.summary(), "gpu_launches": kt["launches"] * world,
+                "kernel_ms": {"assemble_single_layer": kt["assemble_ms"] / max(kt["assemble_launches"], 1),
+                              "rhs": kt["rhs_ms"] / max(kt["rhs_calls"], 1), "av_sweep": av_ms,
+                              "atu_sweep": atu_ms},
+                "host_s": t1 - t0, "fp64_gpu": fp64}
+        print(json.dumps(line), flush=True)
+    C.close()
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -134,10 +134,13 @@ int agb_force_torque(agb_context* ctx, int nrhs, const double* x, int wall, doub
  * `outer_wall`: assembles (precision), imposes the six rigid motions on the
  * container (unit translations e_x,e_y,e_z, then rotations e_i x r), solves the
  * six right-hand sides in one block LSQR and integrates force and torque on
- * the particle.  R[r][6] = (F, T) of motion r.  times_ms (may be NULL):
- * {assemble, rhs, solve, reduce, total}. */
+ * the particle.  R[r][6] = (F, T) of motion r; nit[6], istop[6] per motion
+ * (istop > 3: iteration or condition limit -- reported, not an error, as the
+ * reference only logs it).  times_ms (may be NULL, 6 doubles): host
+ * {assemble, rhs, solve, reduce, total} and [5] the device time of the whole
+ * call between two CUDA events on the context stream. */
 int agb_resistance_tensor(agb_context* ctx, int precision, int particle_wall, int outer_wall, int maxit, double eps,
-                          int refine, double* R, int* nit, double* times_ms);
+                          int refine, double* R, int* nit, int* istop, double* times_ms);
 
 /* Live kernel timing (instrumentation; plays the role of the reference's
  * TIMER stopwatches, stokes.f90:88-92, at kernel granularity).  Cumulative
@@ -145,7 +148,9 @@ int agb_resistance_tensor(agb_context* ctx, int precision, int particle_wall, in
  * out[0] ms in the A*V sweep, out[1] its launches, out[2] ms in the A^T*U
  * sweep, out[3] its launches, out[4] ms in the Stokes single-layer assembly
  * kernel, out[5] its launches, out[6] ms building right-hand sides, out[7]
- * its calls.  reset != 0 zeroes the counters after reading. */
+ * its calls, out[8] number of kernels this library launched, out[9] = 0
+ * (reserved).  out holds 10 doubles.  reset != 0 zeroes the counters after
+ * reading. */
 int agb_kernel_times(agb_context* ctx, int reset, double* out);
 
 /* Drop-ins with the reference signatures (1-based CRS, int64 row pointers).

@@ -1585,6 +1585,44 @@ void orc_force_torque(void* h, const double* qx, const double* qy, const double*
   force_torque(*(Problem*)h, qx, qy, qz, wall, ft, ft + 3);
 }
 
+// CPU baseline sample: integrate rows [r0, r1) of the reference's nsp rows
+// (u-source rows first, then q-source rows) with nthreads OpenMP threads and
+// return the elapsed seconds; a checksum of the rows keeps the work observable.
+double orc_time_rows(void* h, int r0, int r1, int nthreads, double* checksum) {
+  Problem* P = (Problem*)h;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+  const double t0 = omp_get_wtime();
+#else
+  (void)nthreads;
+#endif
+  double cs = 0.0;
+#pragma omp parallel reduction(+ : cs)
+  {
+    StkRow R(P->nnodes, P->nelem);
+    std::vector<double> rh(P->nnodes), rg(P->nelem);
+#pragma omp for schedule(dynamic, 1)
+    for (int r = r0; r < r1; ++r) {
+      double e = 0.0;
+      if (P->kind == 2) {
+        if (r < P->sd_nnodes) stk_row_u(*P, P->nodeList[r], R, e);
+        else stk_row_q(*P, P->qnodeList[r - P->sd_nnodes], R, e);
+        cs += R.T[r % R.T.size()] + R.G[r % R.G.size()];
+      } else {
+        if (r < P->sd_nnodes) lap_row_u(*P, P->nodeList[r], rh.data(), rg.data(), e);
+        else lap_row_q(*P, P->qnodeList[r - P->sd_nnodes], rh.data(), rg.data(), e);
+        cs += rh[r % rh.size()] + rg[r % rg.size()];
+      }
+    }
+  }
+  if (checksum) *checksum = cs;
+#ifdef _OPENMP
+  return omp_get_wtime() - t0;
+#else
+  return 0.0;
+#endif
+}
+
 int orc_num_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

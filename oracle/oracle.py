@@ -70,6 +70,8 @@ def lib():
         L.orc_stokes_solve_sequence.argtypes = [C.c_void_p, C.c_int, dp, dp, C.c_int, C.c_double, C.c_int, dp, ip]
         L.orc_stokes_solve_sequence.restype = C.c_int
         L.orc_force_torque.argtypes = [C.c_void_p, dp, dp, dp, C.c_int, dp]
+        L.orc_time_rows.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
+        L.orc_time_rows.restype = C.c_double
         L.orc_num_threads.restype = C.c_int
         L.orc_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -225,6 +227,11 @@ class Problem:
         ierr = lib().orc_stokes_solve_sequence(self.h, nrhs, u_fields.ravel(), q.reshape(-1), maxit, eps, fwall,
                                                ft.reshape(-1), nits)
         return q, ft, nits, ierr
+
+    def time_rows(self, r0, r1, nthreads):
+        cs = C.c_double(0.0)
+        t = lib().orc_time_rows(self.h, int(r0), int(r1), int(nthreads), C.byref(cs))
+        return t, cs.value
 
     def force_torque(self, q3, wall):
         ft = np.zeros(6)
