@@ -40,6 +40,7 @@ SIGNATURES = {
     "agb_kernel_times": ([vp, I, dp], I),
     "agb_lsqr_precon": ([I, I, C.c_int64, dp, lp, ip, dp], I),
     "agb_lsqr_solve": ([I, I, C.c_int64, PI, D, PI, PI, dp, lp, ip, dp, dp, dp], I),
+    "agb_lsqr_precon_dense_noalloc": ([I, I, C.c_int64, vp, vp], I),
 }
 
 _lib = None

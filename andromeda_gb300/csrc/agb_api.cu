@@ -72,6 +72,9 @@ struct agb_context {
 
 namespace {
 thread_local std::string g_free_err;
+}
+__attribute__((visibility("hidden"))) void agb_set_free_error(const std::string& msg) { g_free_err = msg; }
+namespace {
 
 int fail(agb_context* c, int code, const std::string& msg) {
   if (c) c->err = msg;

@@ -160,6 +160,24 @@ int agb_lsqr_precon(int m, int n, int64_t nnz, double* q, const int64_t* ia, con
 int agb_lsqr_solve(int m, int n, int64_t nnz, int* maxit, double eps, int* nit, int* ierr, const double* q,
                    const int64_t* ia, const int* ja, double* a, const double* b, double* x);
 
+/* Allocation-free column scaling for callers that cannot call cudaMalloc (a
+ * host program that owns all device memory through its own pool or an
+ * OpenACC runtime, code in an allocation-free phase, an embedding whose device
+ * memory is fully reserved).  No counterpart in the reference: it is the
+ * lsqr_precon column scaling (q_j = 1/||A(:,j)||, A <- A diag(q)) applied to a
+ * dense row-major m x n matrix the caller already holds on the current device
+ * (leading dimension lda >= n, FP64), writing q (n doubles, device).  It
+ * allocates nothing: its scratch is a fixed 8 MiB array in the library's
+ * device image (held by every GPU that loads the library until exit), so n is
+ * limited to AGB_NOALLOC_MAX_COLUMNS and larger n is rejected with
+ * AGB_ERR_ARG.  The first call on a device looks up the array's device address
+ * (make it before any stream capture).  All calls on a device share the array:
+ * calls that overlap on the GPU race on it.  Runs on the legacy default stream
+ * and returns after the work is done; errors via agb_last_error(NULL). */
+#define AGB_NOALLOC_SCRATCH_DOUBLES (1 << 20)
+#define AGB_NOALLOC_MAX_COLUMNS AGB_NOALLOC_SCRATCH_DOUBLES
+int agb_lsqr_precon_dense_noalloc(int m, int n, int64_t lda, double* A, double* q);
+
 #ifdef __cplusplus
 }
 #endif
