@@ -322,8 +322,8 @@ def main():
         C2.resistance_tensor(A.MIXED, 1, 2, eps=args.eps)
         C2.close()
         e2e_vals.append(time.perf_counter() - t2)
-    e2e = {"value": world / statistics.median(e2e_vals), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
-           "d2h_bytes_per_step": int(d2h)}
+    e2e = {"value": (world / statistics.median(e2e_vals)) if e2e_vals else None, "unit": "solves/s",
+           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": len(e2e_vals)}
 
     # plain FP64 GPU comparator: full FP64 assembly + a sample of FP64 LSQR
     # iterations, scaled to the iteration count of the solve
