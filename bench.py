@@ -31,7 +31,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Stokes resistance-tensor solves/s at <=1e-6 rel err: mixed/batched vs FP64 GPU"
 GOLDEN_TRUTH = os.path.join(ROOT, "tests", "golden", "c2_fp64_tensor.json")
-PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "lsqr_sweeps_traffic.json")
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "k_av2_k_atu2_k_stokes_G_l4.md")
 
 
 def parse():
@@ -298,10 +298,11 @@ def main():
     av_ms = kt["av_ms"] / max(kt["av_launches"], 1)
     atu_ms = kt["atu_ms"] / max(kt["atu_launches"], 1)
     traffic = None
-    if os.path.exists(PROFILE_TRAFFIC):
+    if os.path.exists(PROFILE_TRAFFIC) and args.level == 5:
         with open(PROFILE_TRAFFIC) as f:
-            pt = json.load(f)
-        traffic = pt.get("k_av2_bytes_per_launch_c2")
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch_k_av2_c2:"):
+                    traffic = float(line.split(":")[1])
     roofline = {"bound": "hbm", "kernel": "k_av2 (LSQR A*V sweep, FP32 A, 8 RHS)",
                 "achieved": a_bytes / (av_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                 "frac": a_bytes / (av_ms * 1e-3) / 1e9 / peak, "traffic": traffic, "peak_source": peak_kind,
