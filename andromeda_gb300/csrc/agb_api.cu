@@ -235,14 +235,15 @@ int device_rhs(agb_context* c, int nrhs, int na) {
   return AGB_OK;
 }
 
-int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int refine, int* nit, int* istop) {
+int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int refine, int* nit, int* istop,
+             bool x0_zero) {
   if (!c->lsqr.A || c->lsqr.k != nrhs) {
     if (!c->lsqr.setup(c->d_A, c->prec == AGB_MIXED, c->m, c->n, c->lda, nrhs, c->stream))
       return fail(c, AGB_ERR_CUDA, "lsqr setup: " + c->lsqr.err);
   }
   std::vector<int> nt(nrhs, 0), is(nrhs, 0);
   for (int pass = 0; pass <= refine; ++pass) {
-    if (!c->lsqr.solve(c->d_rhs, d_x, c->d_q, eps, maxit, nt.data(), is.data()))
+    if (!c->lsqr.solve(c->d_rhs, d_x, c->d_q, eps, maxit, nt.data(), is.data(), nullptr, 8, x0_zero && pass == 0))
       return fail(c, AGB_ERR_CUDA, "lsqr: " + c->lsqr.err);
     for (int r = 0; r < nrhs; ++r) {
       if (nit) nit[r] = (pass == 0 ? 0 : nit[r]) + nt[r];
@@ -554,7 +555,9 @@ int agb_solve(agb_context* c, int nrhs, const double* u, double* x, int maxit, d
   if ((rc = device_rhs(c, nrhs, na))) return rc;
   CUDA_OR_FAIL(c, ensure(c->d_x, c->cap_x, (size_t)nrhs * c->n));
   CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_x, x, (size_t)nrhs * c->n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  if ((rc = do_solve(c, nrhs, c->d_x, maxit, eps, refine, nit, istop))) return rc;
+  bool zero = true;
+  for (size_t t = 0; t < (size_t)nrhs * c->n && zero; ++t) zero = (x[t] == 0.0);
+  if ((rc = do_solve(c, nrhs, c->d_x, maxit, eps, refine, nit, istop, zero))) return rc;
   CUDA_OR_FAIL(c, cudaMemcpyAsync(x, c->d_x, (size_t)nrhs * c->n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
   return AGB_OK;
@@ -628,7 +631,7 @@ int agb_resistance_tensor(agb_context* c, int precision, int particle_wall, int 
   CUDA_OR_FAIL(c, ensure(c->d_x, c->cap_x, (size_t)k * c->n));
   CUDA_OR_FAIL(c, cudaMemsetAsync(c->d_x, 0, (size_t)k * c->n * sizeof(double), c->stream));
   std::vector<int> nt(k), is(k);
-  if ((rc = do_solve(c, k, c->d_x, maxit, eps, refine, nt.data(), is.data()))) return rc;
+  if ((rc = do_solve(c, k, c->d_x, maxit, eps, refine, nt.data(), is.data(), true))) return rc;
   auto t3 = clk::now();
   if (!c->d_ft) CUDA_OR_FAIL(c, cudaMalloc(&c->d_ft, 6 * AGB_MAX_RHS * sizeof(double)));
   CUDA_OR_FAIL(c, launch_force_torque(c->ne, k, c->d_geom, c->d_x, pidx, c->d_ft, c->stream));

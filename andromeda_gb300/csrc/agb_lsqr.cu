@@ -286,6 +286,17 @@ __global__ void __launch_bounds__(AV2<T>::WARPS * 32) k_av2(const T* __restrict_
 #pragma unroll
     for (int c = 0; c < K8; ++c) { acc[r][c] = Acc(0); dfull[r][c] = 0.0; }
 
+  // software pipeline over the A stream: the vectors of step s+1 are in flight
+  // while step s is multiplied (rows beyond m read row m-1; those products are
+  // discarded)
+  typename Vec<T>::V an[RR];
+  const T* arow[RR];
+#pragma unroll
+  for (int r = 0; r < RR; ++r) arow[r] = A + (int64_t)min(row0 + r, m - 1) * lda;
+  if (lane * VN < lda) {
+#pragma unroll
+    for (int r = 0; r < RR; ++r) an[r] = __ldcs(reinterpret_cast<const typename Vec<T>::V*>(arow[r] + lane * VN));
+  }
   for (int k = 0; k < nch; ++k) {
     if (threadIdx.x == 0 && k + 1 < nch) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -298,15 +309,14 @@ __global__ void __launch_bounds__(AV2<T>::WARPS * 32) k_av2(const T* __restrict_
     for (int jj = lane * VN; jj < cw; jj += 32 * VN) {
       T a[RR][VN];
 #pragma unroll
-      for (int r = 0; r < RR; ++r) {
-        const int row = row0 + r;
-        if (row < m) {
-          typename Vec<T>::V v = *reinterpret_cast<const typename Vec<T>::V*>(A + (int64_t)row * lda + j0 + jj);
-          unpack<T>(v, a[r]);
-        } else {
+      for (int r = 0; r < RR; ++r) unpack<T>(an[r], a[r]);
+      // next step of this lane: further along the chunk, or the first step of
+      // the next chunk (A does not depend on V, so it is fetched ahead of the
+      // chunk barrier)
+      const int64_t jn = (jj + 32 * VN < cw) ? j0 + jj + 32 * VN : j0 + cw + lane * VN;
+      if (jn < lda) {
 #pragma unroll
-          for (int q = 0; q < VN; ++q) a[r][q] = T(0);
-        }
+        for (int r = 0; r < RR; ++r) an[r] = __ldcs(reinterpret_cast<const typename Vec<T>::V*>(arow[r] + jn));
       }
 #pragma unroll
       for (int c = 0; c < K8; ++c) {
@@ -568,18 +578,39 @@ __device__ double sum_part(const double* part, int nb, int c) {
 // phase 2: beta = ||Y|| after sweep 1; anorm.
 // phase 3: alpha after sweep 2; plane rotations; t1,t2,t3; gamma for next sweep.
 // phase 4: after the x/w update: dnorm, xnorm, residual estimates, stopping tests.
-__global__ void k_scalars(LsqrScalars* sc, int k, int phase, const double* part, int nb, int* nactive) {
+// The partial sums of the producing kernel are reduced by the whole block in
+// a fixed order (thread t sums blocks t/8, t/8+32, ... of column t%8, then the
+// 32 per-thread sums are added in index order): deterministic and O(nb/32)
+// dependent loads instead of O(nb).
+constexpr int SCAL_THREADS = 256;
+__global__ void __launch_bounds__(SCAL_THREADS) k_scalars(LsqrScalars* sc, int k, int phase, const double* part,
+                                                          int nb, int* nactive) {
+  __shared__ double sred[SCAL_THREADS];
+  __shared__ double ssum[K8];
+  {
+    const int t = threadIdx.x, cc = t % K8;
+    double a = 0.0;
+      for (int b = t / K8; b < nb; b += SCAL_THREADS / K8) a += part[(int64_t)b * K8 + cc];
+    sred[t] = a;
+    __syncthreads();
+    if (t < K8) {
+      double tot = 0.0;
+      for (int i = t; i < SCAL_THREADS; i += K8) tot += sred[i];
+      ssum[t] = tot;
+    }
+    __syncthreads();
+  }
   const int c = threadIdx.x;
   if (c >= K8) return;
   LsqrScalars& s = sc[c];
   if (c >= k) { s.active = 0; return; }
   if (phase == 0) {
-    s.beta = sqrt(sum_part(part, nb, c));
+    s.beta = sqrt(ssum[c]);
     return;
   }
   if (!s.active) return;
   if (phase == 1) {
-    s.alpha = sqrt(sum_part(part, nb, c));
+    s.alpha = sqrt(ssum[c]);
     if (s.beta <= 0.0) s.alpha = 0.0;
     s.rhobar = s.alpha;
     s.phibar = s.beta;
@@ -596,7 +627,7 @@ __global__ void k_scalars(LsqrScalars* sc, int k, int phase, const double* part,
   }
   if (phase == 2) {
     s.itn += 1;
-    s.beta = sqrt(sum_part(part, nb, c));
+    s.beta = sqrt(ssum[c]);
     double temp = d2norm(s.alpha, s.beta);
     temp = d2norm(temp, 0.0);
     s.anorm = d2norm(s.anorm, temp);
@@ -604,7 +635,7 @@ __global__ void k_scalars(LsqrScalars* sc, int k, int phase, const double* part,
   }
   if (phase == 3) {
     if (s.beta > 0.0) {
-      s.alpha = sqrt(sum_part(part, nb, c));
+      s.alpha = sqrt(ssum[c]);
     }
     double rhbar1 = s.rhobar;
     double rho = d2norm(rhbar1, s.beta);
@@ -637,7 +668,7 @@ __global__ void k_scalars(LsqrScalars* sc, int k, int phase, const double* part,
   }
   if (phase == 4) {
     const double phi = s.acond;
-    double dknorm = sqrt(sum_part(part, nb, c));
+    double dknorm = sqrt(ssum[c]);
     s.dnorm = d2norm(s.dnorm, dknorm);
     double dxk = fabs(phi * dknorm);
     if (s.dxmax < dxk) s.dxmax = dxk;
@@ -892,8 +923,16 @@ bool DenseLsqr::precon(void* A_dev, double* q_dev) {
   return true;
 }
 
+template <typename T>
+__global__ void k_init_y(const double* __restrict__ Bp, int64_t count, double* __restrict__ Y, T* __restrict__ Ys) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  Y[t] = Bp[t];
+  Ys[t] = (T)Bp[t];
+}
+
 bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, double eps, int maxit, int* nit_host,
-                      int* istop_host, double* rnorm_host, int check_every) {
+                      int* istop_host, double* rnorm_host, int check_every, bool x0_zero) {
   if (maxit == 0) maxit = 10 * (m + n + 50);
   const int64_t mpad = ((int64_t)m + 255) / 256 * 256;
   const unsigned nb_av = cdiv(m, AV_ROWS);  // residual sweep
@@ -911,11 +950,18 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
   double* part_b = part + (part_cap / 2);
   if ((size_t)nb_b * K8 > part_cap / 2) { err = "partial buffer too small"; return false; }
   CK(cudaMemcpyAsync(part_b, part, (size_t)nb_b * K8 * sizeof(double), cudaMemcpyDeviceToDevice, stream));
-  k_pack<<<cdiv(lda * K8, 256), 256, 0, stream>>>(x_dev, n, k, lda, q_dev, XsD);
-  // residual Y = b - A (x0/q), FP64 accumulation
-  if (fp32) launch_resid<float>(*this, XsD, Bp);
-  else launch_resid<double>(*this, XsD, Bp);
-  k_scalars<<<1, 32, 0, stream>>>(sc, k, 0, part, nb_av, nactive);
+  if (x0_zero) {
+    // r0 = b: no sweep over A; ||r0|| from the partials of ||b||
+    if (fp32) k_init_y<float><<<cdiv((int64_t)m * K8, 256), 256, 0, stream>>>(Bp, (int64_t)m * K8, Y, (float*)Ys);
+    else k_init_y<double><<<cdiv((int64_t)m * K8, 256), 256, 0, stream>>>(Bp, (int64_t)m * K8, Y, (double*)Ys);
+    k_scalars<<<1, SCAL_THREADS, 0, stream>>>(sc, k, 0, part_b, nb_b, nactive);
+  } else {
+    k_pack<<<cdiv(lda * K8, 256), 256, 0, stream>>>(x_dev, n, k, lda, q_dev, XsD);
+    // residual Y = b - A (x0/q), FP64 accumulation
+    if (fp32) launch_resid<float>(*this, XsD, Bp);
+    else launch_resid<double>(*this, XsD, Bp);
+    k_scalars<<<1, SCAL_THREADS, 0, stream>>>(sc, k, 0, part, nb_av, nactive);
+  }
   k_setup_tol<<<1, 32, 0, stream>>>(sc, k, part_b, nb_b, eps, maxit);
   // keep x0 (packed) for the final update: in X0 = W (W is rewritten by the init update,
   // so copy x0 to Bp region first: Bp is no longer needed)
@@ -923,10 +969,10 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
   // A^T r, alpha0, w = v
   if (fp32) launch_atu<float>(*this); else launch_atu<double>(*this);
   k_atu_reduce<<<nb_red, kThreads, 0, stream>>>(Zp, zgroups, lda, n, sc, 1, V, part);
-  k_scalars<<<1, 32, 0, stream>>>(sc, k, 1, part, nb_red, nactive);
+  k_scalars<<<1, SCAL_THREADS, 0, stream>>>(sc, k, 1, part, nb_red, nactive);
   if (fp32) k_update<float><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 1, V, W, X, (float*)Vs, part, 1);
   else k_update<double><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 1, V, W, X, (double*)Vs, part, 1);
-  launches += 11;
+  launches += x0_zero ? 10 : 11;
   CK(cudaGetLastError());
 
   if (check_every > 32) check_every = 32;
@@ -941,16 +987,16 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
     if (fp32) launch_av2<float>(*this);
     else launch_av2<double>(*this);
     cudaEventRecordWithFlags(pev[e + 1], stream, cudaEventRecordExternal);
-    k_scalars<<<1, 32, 0, stream>>>(sc, k, 2, part, nb_av2, nactive);
+    k_scalars<<<1, SCAL_THREADS, 0, stream>>>(sc, k, 2, part, nb_av2, nactive);
     cudaEventRecordWithFlags(pev[e + 2], stream, cudaEventRecordExternal);
     if (fp32) launch_atu<float>(*this); else launch_atu<double>(*this);
     cudaEventRecordWithFlags(pev[e + 3], stream, cudaEventRecordExternal);
     k_atu_reduce<<<nb_red, kThreads, 0, stream>>>(Zp, zgroups, lda, n, sc, 0, V, part);
-    k_scalars<<<1, 32, 0, stream>>>(sc, k, 3, part, nb_red, nactive);
+    k_scalars<<<1, SCAL_THREADS, 0, stream>>>(sc, k, 3, part, nb_red, nactive);
     if (fp32) k_update<float><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 0, V, W, X, (float*)Vs, part, 1);
     else k_update<double><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 0, V, W, X, (double*)Vs, part, 1);
     cudaMemsetAsync(nactive, 0, sizeof(int), stream);
-    k_scalars<<<1, 32, 0, stream>>>(sc, k, 4, part, nb_upd, nactive);
+    k_scalars<<<1, SCAL_THREADS, 0, stream>>>(sc, k, 4, part, nb_upd, nactive);
   };
   // capture check_every iterations in one graph
   cudaGraph_t graph = nullptr;
@@ -1229,11 +1275,11 @@ bool crs_lsqr_solve(int m, int n, int64_t nnz, int& maxit, double eps, int& nit,
   k_pack<<<cdiv(lda * K8, 256), 256, 0, s>>>(x, n, 1, lda, q, Vs);
   k_pack<<<cdiv(lda * K8, 256), 256, 0, s>>>(x, n, 1, lda, nullptr, X0);
   k_csr_av<<<nb_av, kThreads, 0, s>>>(m, D.ia, D.ja, D.a, Vs, -1.0, sc, 0, Bp, Y, Ys, part);
-  k_scalars<<<1, 32, 0, s>>>(sc, 1, 0, part, nb_av, nact);
+  k_scalars<<<1, SCAL_THREADS, 0, s>>>(sc, 1, 0, part, nb_av, nact);
   k_setup_tol<<<1, 32, 0, s>>>(sc, 1, part_b, nb_b, eps, maxit);
   k_csc_atu<<<cdiv((int64_t)n * 32, kThreads), kThreads, 0, s>>>(n, D.cp, D.rows, D.av, Ys, Zp);
   k_atu_reduce<<<nb_red, kThreads, 0, s>>>(Zp, 1, lda, n, sc, 1, V, part);
-  k_scalars<<<1, 32, 0, s>>>(sc, 1, 1, part, nb_red, nact);
+  k_scalars<<<1, SCAL_THREADS, 0, s>>>(sc, 1, 1, part, nb_red, nact);
   k_update<double><<<nb_upd, kThreads, 0, s>>>(n, lda, sc, 1, V, W, X, Vs, part, 0);
   CK(cudaGetLastError());
   LsqrScalars hs;
@@ -1247,13 +1293,13 @@ bool crs_lsqr_solve(int m, int n, int64_t nnz, int& maxit, double eps, int& nit,
   CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   for (int it = 0; it < chunk; ++it) {
     k_csr_av<<<nb_av, kThreads, 0, s>>>(m, D.ia, D.ja, D.a, Vs, 1.0, sc, 1, Y, Y, Ys, part);
-    k_scalars<<<1, 32, 0, s>>>(sc, 1, 2, part, nb_av, nact);
+    k_scalars<<<1, SCAL_THREADS, 0, s>>>(sc, 1, 2, part, nb_av, nact);
     k_csc_atu<<<cdiv((int64_t)n * 32, kThreads), kThreads, 0, s>>>(n, D.cp, D.rows, D.av, Ys, Zp);
     k_atu_reduce<<<nb_red, kThreads, 0, s>>>(Zp, 1, lda, n, sc, 0, V, part);
-    k_scalars<<<1, 32, 0, s>>>(sc, 1, 3, part, nb_red, nact);
+    k_scalars<<<1, SCAL_THREADS, 0, s>>>(sc, 1, 3, part, nb_red, nact);
     k_update<double><<<nb_upd, kThreads, 0, s>>>(n, lda, sc, 0, V, W, X, Vs, part, 0);
     cudaMemsetAsync(nact, 0, sizeof(int), s);
-    k_scalars<<<1, 32, 0, s>>>(sc, 1, 4, part, nb_upd, nact);
+    k_scalars<<<1, SCAL_THREADS, 0, s>>>(sc, 1, 4, part, nb_upd, nact);
   }
   CK(cudaStreamEndCapture(s, &graph));
   CK(cudaGraphInstantiate(&gexec, graph, 0));

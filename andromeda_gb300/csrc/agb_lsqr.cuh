@@ -53,8 +53,10 @@ struct DenseLsqr {
   bool precon(void* A_dev, double* q_dev);
   // lsqr_solve semantics per column c: x0 = X_in(:,c) warm start, b(:,c);
   // x_out = q .* dx + x0.  b and x are device FP64, column-major n x k / m x k.
+  // x0_zero: the caller guarantees a zero warm start, so r0 = b and the
+  // FP64-accumulated residual sweep over A is skipped.
   bool solve(const double* b_dev, double* x_dev, const double* q_dev, double eps, int maxit, int* nit_host,
-             int* istop_host, double* rnorm_host = nullptr, int check_every = 8);
+             int* istop_host, double* rnorm_host = nullptr, int check_every = 8, bool x0_zero = false);
   // r = b - A (x ./ q) with FP64 accumulation (refinement residual).
   bool residual(const double* b_dev, const double* x_dev, const double* q_dev, double* r_dev);
   void release();
