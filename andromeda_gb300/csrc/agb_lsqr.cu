@@ -12,6 +12,7 @@
 //                                      reproducible)
 // Vector norms are reduced from per-CTA partials in index order in FP64.
 #include "agb_lsqr.cuh"
+#include <cudaTypedefs.h>
 #include <cstdio>
 #include <cstring>
 #include <algorithm>
@@ -478,6 +479,230 @@ __global__ void __launch_bounds__(ATU_THREADS) k_atu2(const T* __restrict__ A, i
   }
 }
 
+// ---------------------------------------------------------------------------
+// TMA-fed FP32 sweeps.  A is streamed through a 3-stage shared-memory ring by
+// 2-D tensor-map copies (cp.async.bulk.tensor, one elected thread issues,
+// mbarrier full/empty handshakes with bounded waits); the warps compute from
+// shared memory, so the bytes in flight per SM (two 64 KB stages) no longer
+// depend on registers.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+constexpr int AV3_ROWS = 64, AV3_BC = 256, AV3_ST = 3, AV3_WARPS = 16;
+constexpr size_t AV3_STAGE_A = (size_t)AV3_ROWS * AV3_BC * sizeof(float);  // 64 KB
+constexpr size_t AV3_STAGE_V = (size_t)K8 * AV3_BC * sizeof(float);        // 8 KB
+constexpr size_t AV3_SMEM = AV3_ST * (AV3_STAGE_A + AV3_STAGE_V);
+
+__global__ void __launch_bounds__(AV3_WARPS * 32, 1) k_av3(const __grid_constant__ CUtensorMap tmA, int64_t lda, int m,
+                                                           const float* __restrict__ Vt, const LsqrScalars* sc,
+                                                           double* __restrict__ Y, float* __restrict__ Ys,
+                                                           double* __restrict__ part, int* errflag) {
+  extern __shared__ __align__(1024) unsigned char av3_smem[];
+  float* sA = reinterpret_cast<float*>(av3_smem);
+  float* sV = reinterpret_cast<float*>(av3_smem + AV3_ST * AV3_STAGE_A);
+  __shared__ __align__(8) uint64_t full[AV3_ST], empty[AV3_ST];
+  __shared__ double sPart[AV3_WARPS][K8];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row_base = blockIdx.x * AV3_ROWS;
+  const int nst = (int)((lda + AV3_BC - 1) / AV3_BC);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < AV3_ST; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], AV3_WARPS);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int k) {
+    const int s = k % AV3_ST;
+    if (k >= AV3_ST) mbar_wait_bounded(&empty[s], (uint32_t)(((k / AV3_ST) - 1) & 1), errflag);
+    const int64_t j0 = (int64_t)k * AV3_BC;
+    const int cw = (int)((lda - j0) < (int64_t)AV3_BC ? (lda - j0) : (int64_t)AV3_BC);
+    mbar_expect_tx(&full[s], (uint32_t)(AV3_STAGE_A + K8 * cw * sizeof(float)));
+    tma_load_2d(sA + (size_t)s * AV3_ROWS * AV3_BC, &tmA, (int)j0, row_base, &full[s]);
+#pragma unroll
+    for (int c = 0; c < K8; ++c)
+      bulk_g2s(sV + (size_t)s * K8 * AV3_BC + c * AV3_BC, Vt + (int64_t)c * lda + j0, (uint32_t)(cw * sizeof(float)),
+               &full[s]);
+  };
+  if (threadIdx.x == 0)
+    for (int k = 0; k < AV3_ST && k < nst; ++k) issue(k);
+  float acc[4][K8];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < K8; ++c) acc[r][c] = 0.f;
+  double dacc = 0.0;
+  for (int k = 0; k < nst; ++k) {
+    const int s = k % AV3_ST;
+    mbar_wait_bounded(&full[s], (uint32_t)((k / AV3_ST) & 1), errflag);
+    const float* tA = sA + (size_t)s * AV3_ROWS * AV3_BC + (warp * 4) * AV3_BC;
+    const float* tV = sV + (size_t)s * K8 * AV3_BC;
+    const int64_t j0 = (int64_t)k * AV3_BC;
+    const int cw = (int)((lda - j0) < (int64_t)AV3_BC ? (lda - j0) : (int64_t)AV3_BC);
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int col = half * 128 + lane * 4;
+      if (col < cw) {
+        float a[4][4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const float4 v = *reinterpret_cast<const float4*>(tA + r * AV3_BC + col);
+          a[r][0] = v.x; a[r][1] = v.y; a[r][2] = v.z; a[r][3] = v.w;
+        }
+#pragma unroll
+        for (int c = 0; c < K8; ++c) {
+          const float4 vv = *reinterpret_cast<const float4*>(tV + c * AV3_BC + col);
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            acc[r][c] = fmaf(a[r][0], vv.x, acc[r][c]);
+            acc[r][c] = fmaf(a[r][1], vv.y, acc[r][c]);
+            acc[r][c] = fmaf(a[r][2], vv.z, acc[r][c]);
+            acc[r][c] = fmaf(a[r][3], vv.w, acc[r][c]);
+          }
+        }
+      }
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+    if (threadIdx.x == 0 && k + AV3_ST < nst) issue(k + AV3_ST);
+    if ((k & 3) == 3 || k == nst - 1) {
+      // reduce-scatter the 32 FP32 partials of 1024 columns into one FP64 sum per lane
+      float v[32];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < K8; ++c) { v[r * K8 + c] = acc[r][c]; acc[r][c] = 0.f; }
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) {
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < o; ++i) {
+          const float send = upper ? v[i] : v[i + o];
+          const float keep = upper ? v[i + o] : v[i];
+          v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+      }
+      dacc += (double)v[0];
+    }
+  }
+  double ssq = 0.0;
+  {
+    const int r = lane >> 3, c = lane & 7, row = row_base + warp * 4 + r;
+    if (row < m) {
+      const double y = dacc + sc[c].gamma * Y[(int64_t)row * K8 + c];
+      Y[(int64_t)row * K8 + c] = y;
+      Ys[(int64_t)row * K8 + c] = (float)y;
+      ssq = y * y;
+    }
+    ssq += __shfl_xor_sync(0xffffffffu, ssq, 8);
+    ssq += __shfl_xor_sync(0xffffffffu, ssq, 16);
+  }
+  if (lane < K8) sPart[warp][lane] = ssq;
+  __syncthreads();
+  if (threadIdx.x < K8) {
+    double a = 0.0;
+    for (int w = 0; w < AV3_WARPS; ++w) a += sPart[w][threadIdx.x];
+    part[(int64_t)blockIdx.x * K8 + threadIdx.x] = a;
+  }
+}
+
+// A^T Y: a CTA owns 512 columns (two 256-column tiles) and a row group; 32-row
+// stages of A plus the matching 32 rows of Y (1 KB) arrive by TMA; a thread owns
+// two columns; FP32 partials over 256 rows are added into FP64 registers.
+constexpr int ATU3_COLS = 512, ATU3_RS = 32, ATU3_ST = 3, ATU3_THREADS = 256;
+constexpr size_t ATU3_STAGE_A = (size_t)ATU3_RS * ATU3_COLS * sizeof(float);  // 64 KB
+constexpr size_t ATU3_STAGE_U = (size_t)ATU3_RS * K8 * sizeof(float);         // 1 KB
+constexpr size_t ATU3_SMEM = ATU3_ST * (ATU3_STAGE_A + ATU3_STAGE_U);
+
+__global__ void __launch_bounds__(ATU3_THREADS, 1) k_atu3(const __grid_constant__ CUtensorMap tmA, int64_t lda, int m,
+                                                          const float* __restrict__ Us, int rows_per_group,
+                                                          double* __restrict__ Zp, int* errflag) {
+  extern __shared__ __align__(1024) unsigned char atu3_smem[];
+  float* sA = reinterpret_cast<float*>(atu3_smem);
+  float* sU = reinterpret_cast<float*>(atu3_smem + ATU3_ST * ATU3_STAGE_A);
+  __shared__ __align__(8) uint64_t full[ATU3_ST], empty[ATU3_ST];
+  const int c0 = blockIdx.x * ATU3_COLS;
+  const int g = blockIdx.y;
+  const int r0 = g * rows_per_group, r1 = min(m, r0 + rows_per_group);
+  const int nst = (r1 > r0) ? (r1 - r0 + ATU3_RS - 1) / ATU3_RS : 0;
+  const int warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < ATU3_ST; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], ATU3_THREADS / 32);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int k) {
+    const int s = k % ATU3_ST;
+    if (k >= ATU3_ST) mbar_wait_bounded(&empty[s], (uint32_t)(((k / ATU3_ST) - 1) & 1), errflag);
+    const int rb = r0 + k * ATU3_RS;
+    const int nr = min(ATU3_RS, r1 - rb);
+    mbar_expect_tx(&full[s], (uint32_t)(ATU3_STAGE_A + (size_t)nr * K8 * sizeof(float)));
+    float* dA = sA + (size_t)s * ATU3_RS * ATU3_COLS;
+    tma_load_2d(dA, &tmA, c0, rb, &full[s]);
+    tma_load_2d(dA + ATU3_RS * 256, &tmA, c0 + 256, rb, &full[s]);
+    bulk_g2s(sU + (size_t)s * ATU3_RS * K8, Us + (int64_t)rb * K8, (uint32_t)(nr * K8 * sizeof(float)), &full[s]);
+  };
+  if (threadIdx.x == 0)
+    for (int k = 0; k < ATU3_ST && k < nst; ++k) issue(k);
+  const int tc = threadIdx.x * 2;          // the thread's two columns within the CTA block
+  const int box = tc >> 8, off = tc & 255;  // tile and column within the tile
+  float acc[2][K8];
+  double dacc[2][K8];
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+#pragma unroll
+    for (int c = 0; c < K8; ++c) { acc[q][c] = 0.f; dacc[q][c] = 0.0; }
+  for (int k = 0; k < nst; ++k) {
+    const int s = k % ATU3_ST;
+    mbar_wait_bounded(&full[s], (uint32_t)((k / ATU3_ST) & 1), errflag);
+    const int rb = r0 + k * ATU3_RS;
+    const int nr = min(ATU3_RS, r1 - rb);
+    const float* tA = sA + (size_t)s * ATU3_RS * ATU3_COLS + box * ATU3_RS * 256 + off;
+    const float* tU = sU + (size_t)s * ATU3_RS * K8;
+#pragma unroll 4
+    for (int r = 0; r < nr; ++r) {
+      const float2 a = *reinterpret_cast<const float2*>(tA + r * 256);
+      const float4 u0 = *reinterpret_cast<const float4*>(tU + r * K8);
+      const float4 u1 = *reinterpret_cast<const float4*>(tU + r * K8 + 4);
+      const float uu[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+#pragma unroll
+      for (int c = 0; c < K8; ++c) {
+        acc[0][c] += a.x * uu[c];
+        acc[1][c] += a.y * uu[c];
+      }
+    }
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) mbar_arrive(&empty[s]);
+    if (threadIdx.x == 0 && k + ATU3_ST < nst) issue(k + ATU3_ST);
+    if ((k & 7) == 7 || k == nst - 1) {
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+#pragma unroll
+        for (int c = 0; c < K8; ++c) { dacc[q][c] += (double)acc[q][c]; acc[q][c] = 0.f; }
+    }
+  }
+  (void)warp;
+  const int64_t col = (int64_t)c0 + tc;
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+    if (col + q < lda)
+#pragma unroll
+      for (int c = 0; c < K8; ++c) Zp[((int64_t)g * lda + col + q) * K8 + c] = dacc[q][c];
+}
+
 // V <- Z/beta - beta V (Z = sum of group partials, in order); partial ||V||^2.
 // On the initial call (init=1) the old V is taken as zero.
 __global__ void k_atu_reduce(const double* __restrict__ Zp, int groups, int64_t lda, int n, const LsqrScalars* sc,
@@ -799,6 +1024,34 @@ __global__ void k_setup_tol(LsqrScalars* sc, int k, const double* part_b, int nb
 // ---------------------------------------------------------------------------
 static inline unsigned cdiv(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
 
+// Build a 2-D tensor map of the row-major FP32 matrix (dims {lda, m}) with the
+// given box, through the driver entry point (no link against libcuda).
+static bool make_tmap(CUtensorMap* tm, const void* A, int64_t lda, int m, int box_cols, int box_rows, std::string& err) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    cudaDriverEntryPointQueryResult q;
+    void* fn = nullptr;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &fn, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+      err = "cuTensorMapEncodeTiled not available";
+      return false;
+    }
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  const cuuint64_t dims[2] = {(cuuint64_t)lda, (cuuint64_t)m};
+  const cuuint64_t strides[1] = {(cuuint64_t)lda * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(A), dims, strides, box, estr,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    err = "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")";
+    return false;
+  }
+  return true;
+}
+
 template <typename T>
 static void launch_resid(const DenseLsqr& L, const double* Xs, const double* Bp) {
   const unsigned nb = cdiv(L.m, AV_ROWS);
@@ -809,6 +1062,11 @@ template <typename T>
 static unsigned av2_blocks(const DenseLsqr& L) { return cdiv(L.m, AV2<T>::WARPS * AV2<T>::RR); }
 template <typename T>
 static void launch_av2(const DenseLsqr& L) {
+  if (sizeof(T) == 4 && L.use_tma) {
+    k_av3<<<cdiv(L.m, AV3_ROWS), AV3_WARPS * 32, AV3_SMEM, L.stream>>>(L.tm_av, L.lda, L.m, (const float*)L.Vs, L.sc,
+                                                                       L.Y, (float*)L.Ys, L.part, L.errflag);
+    return;
+  }
   const size_t smem = 2 * K8 * AV2<T>::CH * sizeof(T);
   k_av2<T><<<av2_blocks<T>(L), AV2<T>::WARPS * 32, smem, L.stream>>>((const T*)L.A, L.lda, L.m, (const T*)L.Vs, L.sc,
                                                                      L.Y, (T*)L.Ys, L.part, L.errflag);
@@ -819,6 +1077,12 @@ static size_t atu2_smem() {
 }
 template <typename T>
 static void launch_atu(const DenseLsqr& L) {
+  if (sizeof(T) == 4 && L.use_tma) {
+    dim3 g(cdiv(L.lda, ATU3_COLS), L.zgroups);
+    const int rpg = (int)((cdiv(L.m, L.zgroups) + 31) / 32 * 32);
+    k_atu3<<<g, ATU3_THREADS, ATU3_SMEM, L.stream>>>(L.tm_atu, L.lda, L.m, (const float*)L.Ys, rpg, L.Zp, L.errflag);
+    return;
+  }
   constexpr int vn = Vec<T>::N;
   dim3 g(cdiv(L.lda, ATU_THREADS * vn), L.zgroups);
   const int rpg = (int)((cdiv(L.m, L.zgroups) + 255) / 256 * 256);
@@ -828,6 +1092,8 @@ template <typename T>
 static cudaError_t set_sweep_attrs() {
   cudaError_t e = cudaFuncSetAttribute(k_av2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)(2 * K8 * AV2<T>::CH * sizeof(T)));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_av3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AV3_SMEM);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_atu3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ATU3_SMEM);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_atu2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)atu2_smem<T>());
   return e;
@@ -861,8 +1127,13 @@ bool DenseLsqr::setup(const void* A_dev, bool is_fp32, int m_, int n_, int64_t l
   CK(cudaMalloc(&Z, std::max<int64_t>(lda, mpad) * K8 * sizeof(double)));  // b / x0 staging
   CK(cudaMalloc(&Vs, lda * K8 * sizeof(double)));                            // T copy, or FP64 for residual
   // row groups for sweep 2: aim for >= 4 CTAs per SM
+  use_tma = fp32 && getenv("AGB_NO_TMA") == nullptr;
+  if (use_tma) {
+    if (!make_tmap(&tm_av, A_dev, lda, m, AV3_BC, AV3_ROWS, err)) return false;
+    if (!make_tmap(&tm_atu, A_dev, lda, m, 256, ATU3_RS, err)) return false;
+  }
   const int vn = fp32 ? 4 : 2;
-  const int colblocks = (int)cdiv(lda, ATU_THREADS * vn);
+  const int colblocks = use_tma ? (int)cdiv(lda, ATU3_COLS) : (int)cdiv(lda, ATU_THREADS * vn);
   // row groups of sweep 2: fill whole waves of resident CTAs
   CK(fp32 ? set_sweep_attrs<float>() : set_sweep_attrs<double>());
   int per_sm = 1, nsm = 152;
@@ -870,12 +1141,13 @@ bool DenseLsqr::setup(const void* A_dev, bool is_fp32, int m_, int n_, int64_t l
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (fp32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_atu2<float>, ATU_THREADS, atu2_smem<float>());
+    if (use_tma) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_atu3, ATU3_THREADS, ATU3_SMEM);
+    else if (fp32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_atu2<float>, ATU_THREADS, atu2_smem<float>());
     else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_atu2<double>, ATU_THREADS, atu2_smem<double>());
     per_sm = std::max(per_sm, 1);
   }
   const int slots = nsm * per_sm;
-  const int gmax = std::max(1, std::min((int)cdiv(m, 256), 64));
+  const int gmax = std::max(1, std::min((int)cdiv(m, use_tma ? 64 : 256), 64));
   int groups = 1;
   double best = -1.0;
   for (int G = 1; G <= gmax; ++G) {
@@ -936,7 +1208,7 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
   if (maxit == 0) maxit = 10 * (m + n + 50);
   const int64_t mpad = ((int64_t)m + 255) / 256 * 256;
   const unsigned nb_av = cdiv(m, AV_ROWS);  // residual sweep
-  const unsigned nb_av2 = fp32 ? av2_blocks<float>(*this) : av2_blocks<double>(*this);
+  const unsigned nb_av2 = fp32 ? (use_tma ? cdiv(m, AV3_ROWS) : av2_blocks<float>(*this)) : av2_blocks<double>(*this);
   CK(fp32 ? set_sweep_attrs<float>() : set_sweep_attrs<double>());
   const unsigned nb_red = cdiv((int64_t)n * K8, kThreads);
   const unsigned nb_upd = cdiv(lda * K8, kThreads);

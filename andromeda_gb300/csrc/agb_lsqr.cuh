@@ -1,6 +1,7 @@
 // Block LSQR on a dense row-major matrix resident in HBM (host-side driver).
 #pragma once
 #include "agb_common.cuh"
+#include <cuda.h>
 #include <vector>
 #include <string>
 
@@ -41,6 +42,11 @@ struct DenseLsqr {
   // iteration graph on the solver stream)
   cudaEvent_t pev[4 * 32] = {};
   bool pev_ready = false;
+  // TMA descriptors of A for the FP32 sweeps (2-D tiles: 256 columns x 64
+  // rows for A*V, 256 columns x 32 rows for A^T*U)
+  alignas(64) CUtensorMap tm_av{};
+  alignas(64) CUtensorMap tm_atu{};
+  bool use_tma = false;
   double t_av = 0.0, t_atu = 0.0;
   long n_av = 0, n_atu = 0;
   long launches = 0;           // kernels launched by precon/solve
