@@ -161,6 +161,51 @@ class Context:
         self._ck(self._L.agb_force_torque(self.h, nrhs, x.reshape(-1), int(wall), ft.reshape(-1)))
         return ft
 
+    def layout_sizes(self):
+        """(nsp, nn, nq, rows, unknowns, knowns) of the subdomain numbering."""
+        out = np.zeros(6, np.int32)
+        self._ck(self._L.agb_layout_sizes(self.h, out))
+        return tuple(int(v) for v in out)
+
+    def integral_matrices(self):
+        """All-row integral matrices (the CoR_Integrals drop-in), FP64.
+
+        Returns (T, G, errs): arrays of shape (ncomp, nsp, ncol) -- Laplace H/G
+        (ncomp 1), Stokes T/prT and G/prG (ncomp 9) -- and the fSP/qSP errors.
+        """
+        nsp, nn, nq = self.layout_sizes()[:3]
+        nc = 9 if self.kind == STOKES else 1
+        T = np.zeros(nc * nsp * nn)
+        G = np.zeros(nc * nsp * nq)
+        e = np.zeros(2)
+        self._ck(self._L.agb_integral_matrices(self.h, T.ctypes.data_as(C.c_void_p), G.ctypes.data_as(C.c_void_p),
+                                               e.ctypes.data_as(C.c_void_p)))
+        # column-major per component -> (ncomp, nsp, ncol)
+        T = T.reshape(nc, nn, nsp).transpose(0, 2, 1)
+        G = G.reshape(nc, nq, nsp).transpose(0, 2, 1)
+        return T, G, e
+
+    def solve_fields(self, u, q=None, maxit=0, eps=1e-8, refine=0):
+        """Any-BC solve: known u (nodes) / q (elements) in, full fields out.
+
+        ``u``: (nrhs, neq, nnodes), ``q``: (nrhs, neq, nelem) or None; both
+        give the known values and the warm start of the unknowns.  Returns
+        (u_out, q_out, nit, istop) with u_out/q_out in the same shapes.
+        """
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1, self.neq, self.nnodes)
+        nrhs = u.shape[0]
+        uo = np.zeros_like(u)
+        qo = np.zeros((nrhs, self.neq, self.nelem))
+        qp = None
+        if q is not None:
+            q = np.ascontiguousarray(q, dtype=np.float64).reshape(nrhs, self.neq, self.nelem)
+            qp = q.ctypes.data_as(C.c_void_p)
+        nit = np.zeros(nrhs, np.int32)
+        istop = np.zeros(nrhs, np.int32)
+        self._ck(self._L.agb_solve_fields(self.h, nrhs, u.ravel(), qp, uo.reshape(-1), qo.reshape(-1), int(maxit),
+                                          float(eps), int(refine), nit, istop))
+        return uo, qo, nit, istop
+
     def kernel_times(self, reset=False):
         """Cumulative live kernel times (ms) and launch counts since the last reset."""
         out = np.zeros(10)

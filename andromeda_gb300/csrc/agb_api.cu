@@ -3,6 +3,7 @@
 #include "../../include/andromeda_gb300.h"
 #include "agb_assembly.cuh"
 #include "agb_lsqr.cuh"
+#include "agb_general.cuh"
 #include "quad_tables.h"
 
 #include <chrono>
@@ -45,6 +46,13 @@ struct agb_context {
   double* d_normMul = nullptr;
   ElemGeom* d_geom = nullptr;
   RuleDev rule;
+  // general path (all source rows, any BC mix)
+  GeneralLayout gl;
+  GeneralDev gd;
+  double* d_rhsM = nullptr;   // dense rhs matrix of the general system (nrow x nb)
+  bool general = false;       // the assembled system came from the general path
+  double* d_b = nullptr;
+  size_t cap_b = 0;
   // assembled system
   int prec = -1;
   void* d_A = nullptr;
@@ -148,6 +156,8 @@ cudaError_t ensure(T*& p, size_t& cap, size_t count) {
 }
 
 void free_system(agb_context* c) {
+  dfree(c->d_rhsM);
+  c->general = false;
   dfree(c->d_A);
   dfree(c->d_q);
   dfree(c->d_pts);
@@ -167,7 +177,112 @@ void free_problem(agb_context* c) {
   dfree(c->d_geom);
   dfree(c->rule.l);
   dfree(c->rule.w);
+  c->gd.release();
   c->has_problem = false;
+}
+
+// Numbering of the subdomain (SetUpSubdomains lib_sdBem.f90:319, sdSetUpXandB
+// lib_sdBem.f90:4, StokesBigSystemXB lib_Stokes.f90:1180) and the BC routing
+// maps of sdSetUpSysMrhsM_CRS (lib_CRS.f90:148) / formUrow / formQrow
+// (lib_StokesFull.f90:4,94).
+void build_layout(agb_context* c) {
+  GeneralLayout& L = c->gl;
+  L = GeneralLayout();
+  L.kind = c->kind;
+  L.neq = c->neq;
+  const int nw = (int)c->walls.size();
+  // nodes of the subdomain, wall of the last element (in subdomain order) touching them
+  std::vector<int> wallOf(c->nnodes, -1);
+  for (int p = 0; p < c->ne; ++p) {
+    const int e = c->elemList[p];
+    const int nno = c->etype[e] == AGB_TRI ? 3 : 4;
+    for (int k = 0; k < nno; ++k) wallOf[c->con[4 * e + k]] = c->wallIdx[p];
+  }
+  L.posOfNode.assign(c->nnodes, -1);
+  for (int i = 0; i < c->nnodes; ++i)
+    if (wallOf[i] >= 0) {
+      L.posOfNode[i] = (int)L.nodeList.size();
+      L.nodeList.push_back(i);
+      L.nodeWall.push_back(wallOf[i]);
+    }
+  L.nn = (int)L.nodeList.size();
+  L.nq = c->ne;
+  L.nsp = L.nn + L.nq;
+  // node -> (element position, local index), ascending element position
+  std::vector<std::vector<std::pair<int, int>>> adj(L.nn);
+  for (int p = 0; p < c->ne; ++p) {
+    const int e = c->elemList[p];
+    const int nno = c->etype[e] == AGB_TRI ? 3 : 4;
+    for (int k = 0; k < nno; ++k) adj[L.posOfNode[c->con[4 * e + k]]].push_back({p, k});
+  }
+  L.adj_ptr.assign(L.nn + 1, 0);
+  for (int j = 0; j < L.nn; ++j) {
+    L.adj_ptr[j + 1] = L.adj_ptr[j] + (int)adj[j].size();
+    for (auto& pk : adj[j]) { L.adj_p.push_back(pk.first); L.adj_k.push_back(pk.second); }
+  }
+  auto bcOf = [&](int en, int widx) { return c->known[en * nw + widx]; };
+  // per-equation numbering (1-based as the reference, -999 = not set)
+  const int NS = -999;
+  std::vector<std::vector<int>> col(L.neq, std::vector<int>(L.nn, NS)), qcol(L.neq, std::vector<int>(L.nq, NS));
+  std::vector<int> nx(L.neq, 0), nb(L.neq, 0), neqn(L.neq, 0);
+  for (int en = 0; en < L.neq; ++en) {
+    for (int i = 0; i < L.nn; ++i) {
+      const int bc = bcOf(en, L.nodeWall[i]);
+      if (bc == AGB_BC_FUNCTION_) { nb[en]++; col[en][i] = nb[en]; }
+      else if (bc == AGB_BC_FLUX_) { nx[en]++; col[en][i] = nx[en]; neqn[en]++; }
+      else if (bc == AGB_BC_CONTACT_) { neqn[en]++; if (col[en][i] == NS) { nx[en]++; col[en][i] = nx[en]; } }
+    }
+    for (int p = 0; p < L.nq; ++p) {
+      const int bc = bcOf(en, c->wallIdx[p]);
+      if (bc == AGB_BC_FUNCTION_) { nx[en]++; qcol[en][p] = nx[en]; neqn[en]++; }
+      else if (bc == AGB_BC_FLUX_) { nb[en]++; qcol[en][p] = nb[en]; }
+      else if (bc == AGB_BC_CONTACT_) { neqn[en]++; if (qcol[en][p] == NS) { nx[en]++; qcol[en][p] = nx[en]; } }
+    }
+  }
+  // offsets of the big system (equation blocks one after another)
+  std::vector<int> offx(L.neq, 0), offb(L.neq, 0);
+  for (int en = 1; en < L.neq; ++en) { offx[en] = offx[en - 1] + nx[en - 1]; offb[en] = offb[en - 1] + nb[en - 1]; }
+  L.nx = L.nb = L.nrow = 0;
+  for (int en = 0; en < L.neq; ++en) { L.nx += nx[en]; L.nb += nb[en]; L.nrow += neqn[en]; }
+  // rows: u-source points first, then q-source points; equation-minor
+  for (int i = 0; i < L.nn; ++i)
+    for (int een = 0; een < L.neq; ++een) {
+      const int bc = bcOf(een, L.nodeWall[i]);
+      if (bc == AGB_BC_FLUX_ || bc == AGB_BC_CONTACT_) { L.row_src.push_back(i); L.row_een.push_back(een); }
+    }
+  for (int p = 0; p < L.nq; ++p)
+    for (int een = 0; een < L.neq; ++een) {
+      const int bc = bcOf(een, c->wallIdx[p]);
+      if (bc == AGB_BC_FUNCTION_ || bc == AGB_BC_CONTACT_) { L.row_src.push_back(L.nn + p); L.row_een.push_back(een); }
+    }
+  const bool stk = (c->kind == AGB_STOKES);
+  L.tmap_tgt.assign(L.neq * L.nn, 0); L.tmap_col.assign(L.neq * L.nn, 0); L.tmap_val.assign(L.neq * L.nn, 0.0);
+  L.gmap_tgt.assign(L.neq * L.nq, 0); L.gmap_col.assign(L.neq * L.nq, 0); L.gmap_val.assign(L.neq * L.nq, 0.0);
+  L.node_known.assign(L.neq * L.nn, 0); L.node_xcol.assign(L.neq * L.nn, -1); L.node_bcol.assign(L.neq * L.nn, -1);
+  L.elem_known.assign(L.neq * L.nq, 0); L.elem_xcol.assign(L.neq * L.nq, -1); L.elem_bcol.assign(L.neq * L.nq, -1);
+  for (int en = 0; en < L.neq; ++en) {
+    for (int j = 0; j < L.nn; ++j) {
+      const int bc = bcOf(en, L.nodeWall[j]), t = en * L.nn + j;
+      if (bc == AGB_BC_FUNCTION_) {
+        L.tmap_tgt[t] = 2; L.tmap_col[t] = col[en][j] - 1 + offb[en]; L.tmap_val[t] = 1.0;
+        L.node_known[t] = 1; L.node_bcol[t] = L.tmap_col[t];
+      } else if (bc == AGB_BC_FLUX_ || bc == AGB_BC_CONTACT_) {
+        L.tmap_tgt[t] = 1; L.tmap_col[t] = col[en][j] - 1 + offx[en]; L.tmap_val[t] = stk ? -1.0 : 1.0;
+        L.node_xcol[t] = L.tmap_col[t];
+      }
+    }
+    for (int p = 0; p < L.nq; ++p) {
+      const int bc = bcOf(en, c->wallIdx[p]), t = en * L.nq + p;
+      const double sc = c->normMul[c->wallIdx[p]] / c->diff;
+      if (bc == AGB_BC_FUNCTION_ || bc == AGB_BC_CONTACT_) {
+        L.gmap_tgt[t] = 1; L.gmap_col[t] = qcol[en][p] - 1 + offx[en]; L.gmap_val[t] = stk ? -sc : sc;
+        L.elem_xcol[t] = L.gmap_col[t];
+      } else if (bc == AGB_BC_FLUX_) {
+        L.gmap_tgt[t] = 2; L.gmap_col[t] = qcol[en][p] - 1 + offb[en]; L.gmap_val[t] = sc;
+        L.elem_known[t] = 1; L.elem_bcol[t] = L.gmap_col[t];
+      }
+    }
+  }
 }
 
 int check_ctx(agb_context* c, bool need_problem) {
@@ -235,6 +350,7 @@ int device_rhs(agb_context* c, int nrhs, int na) {
   return AGB_OK;
 }
 
+int assemble_general(agb_context* c, int precision);
 int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int refine, int* nit, int* istop,
              bool x0_zero) {
   if (!c->lsqr.A || c->lsqr.k != nrhs) {
@@ -252,6 +368,92 @@ int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int r
   }
   return AGB_OK;
 }
+// All source rows on the GPU in FP64 (general_integrals), BC routing into a
+// dense system (general_form), optional FP32 copy for the mixed solve, then the
+// column scaling of lsqr_precon.
+int assemble_general(agb_context* c, int precision) {
+  const GeneralLayout& L = c->gl;
+  if (L.nrow == 0 || L.nx == 0) return fail(c, AGB_ERR_ARG, "the boundary conditions leave no unknown");
+  const int ncomp = (c->kind == AGB_STOKES) ? 9 : 1;
+  double *T = nullptr, *G = nullptr, *err = nullptr, *sys = nullptr;
+  CUDA_OR_FAIL(c, cudaMalloc(&T, (size_t)ncomp * L.nsp * L.nn * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMalloc(&G, (size_t)ncomp * L.nsp * L.nq * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMalloc(&err, (size_t)L.nsp * sizeof(double)));
+  cudaError_t e = general_integrals(L, c->gd, c->d_geom, c->d_xyz, c->rule, c->iqud, T, G, err, c->stream);
+  c->nlaunch += 2 * (int)((L.nsp + 65534) / 65535 + 1);
+  if (e != cudaSuccess) { cudaFree(T); cudaFree(G); cudaFree(err); return fail(c, AGB_ERR_CUDA, std::string("general integrals: ") + cudaGetErrorString(e)); }
+  c->lda = ((int64_t)L.nx + 31) / 32 * 32;
+  c->m = L.nrow;
+  c->n = L.nx;
+  CUDA_OR_FAIL(c, cudaMalloc(&sys, (size_t)L.nrow * c->lda * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMemsetAsync(sys, 0, (size_t)L.nrow * c->lda * sizeof(double), c->stream));
+  CUDA_OR_FAIL(c, cudaMalloc(&c->d_rhsM, (size_t)L.nrow * std::max(L.nb, 1) * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMemsetAsync(c->d_rhsM, 0, (size_t)L.nrow * std::max(L.nb, 1) * sizeof(double), c->stream));
+  CUDA_OR_FAIL(c, general_form(L, c->gd, T, G, sys, c->lda, c->d_rhsM, c->stream));
+  c->nlaunch += 1;
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  cudaFree(T);
+  cudaFree(G);
+  cudaFree(err);
+  c->prec = precision;
+  if (precision == AGB_MIXED) {
+    float* a32 = nullptr;
+    CUDA_OR_FAIL(c, cudaMalloc(&a32, (size_t)L.nrow * c->lda * sizeof(float)));
+    CUDA_OR_FAIL(c, to_fp32(sys, a32, (int64_t)L.nrow * c->lda, c->stream));
+    c->nlaunch += 1;
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    cudaFree(sys);
+    c->d_A = a32;
+  } else {
+    c->d_A = sys;
+  }
+  CUDA_OR_FAIL(c, cudaMalloc(&c->d_q, c->lda * sizeof(double)));
+  if (!c->lsqr.setup(c->d_A, precision == AGB_MIXED, c->m, c->n, c->lda, 1, c->stream)) return fail(c, AGB_ERR_CUDA, c->lsqr.err);
+  if (!c->lsqr.precon(c->d_A, c->d_q)) return fail(c, AGB_ERR_CUDA, c->lsqr.err);
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  c->general = true;
+  c->assembled = true;
+  return AGB_OK;
+}
+
+// Known vector b[r][nb] and warm start x[r][nx] from nodal u [r][neq][nnodes]
+// and element q [r][neq][nelem] (global numbering); q may be NULL (zero).
+void gather_fields(const agb_context* c, int nrhs, const double* u, const double* q, std::vector<double>& b,
+                   std::vector<double>* x) {
+  const GeneralLayout& L = c->gl;
+  b.assign((size_t)nrhs * std::max(L.nb, 1), 0.0);
+  if (x) x->assign((size_t)nrhs * L.nx, 0.0);
+  for (int r = 0; r < nrhs; ++r)
+    for (int en = 0; en < L.neq; ++en) {
+      for (int j = 0; j < L.nn; ++j) {
+        const int t = en * L.nn + j;
+        const double v = u ? u[((size_t)r * L.neq + en) * c->nnodes + L.nodeList[j]] : 0.0;
+        if (L.node_known[t]) b[(size_t)r * L.nb + L.node_bcol[t]] = v;
+        else if (x && L.node_xcol[t] >= 0) (*x)[(size_t)r * L.nx + L.node_xcol[t]] = v;
+      }
+      for (int p = 0; p < L.nq; ++p) {
+        const int t = en * L.nq + p;
+        const double v = q ? q[((size_t)r * L.neq + en) * c->nelem + c->elemList[p]] : 0.0;
+        if (L.elem_known[t]) b[(size_t)r * L.nb + L.elem_bcol[t]] = v;
+        else if (x && L.elem_xcol[t] >= 0) (*x)[(size_t)r * L.nx + L.elem_xcol[t]] = v;
+      }
+    }
+}
+
+// rhs (device d_rhs, [r][m]) for the general system: rhsM * b (Stokes) or
+// rhsM * (-b) (Laplace)
+int general_rhs(agb_context* c, int nrhs, const std::vector<double>& b) {
+  const GeneralLayout& L = c->gl;
+  CUDA_OR_FAIL(c, ensure(c->d_rhs, c->cap_rhs, (size_t)nrhs * c->m));
+  CUDA_OR_FAIL(c, ensure(c->d_b, c->cap_b, b.size()));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_b, b.data(), b.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CUDA_OR_FAIL(c, dense_rhs(L.nrow, std::max(L.nb, 1), c->d_rhsM, nrhs, c->d_b, c->kind == AGB_LAPLACE ? -1.0 : 1.0,
+                            c->d_rhs, c->stream));
+  c->nlaunch += 1;
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  return AGB_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -276,6 +478,7 @@ int agb_create(agb_context** out, int device) {
   e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = upload_gauss_tables();
+  if (e == cudaSuccess) e = upload_general_tables();
   for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->tev[i]);
   if (e != cudaSuccess) {
     g_free_err = std::string("agb_create: ") + cudaGetErrorString(e);
@@ -399,7 +602,10 @@ int agb_set_problem(agb_context* c, int kind, int nwalls, const int* walls, cons
   CUDA_OR_FAIL(c, cudaMemcpyAsync(c->rule.l, l.data(), l.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   CUDA_OR_FAIL(c, cudaMemcpyAsync(c->rule.w, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
-  c->m = c->n = c->neq * c->ne;
+  build_layout(c);
+  CUDA_OR_FAIL(c, c->gd.upload(c->gl));
+  c->m = c->gl.nrow;
+  c->n = c->gl.nx;
   c->has_problem = true;
   return AGB_OK;
 }
@@ -436,14 +642,11 @@ int agb_assemble(agb_context* c, int precision) {
   int rc = check_ctx(c, true);
   if (rc) return rc;
   if (precision != AGB_FP64 && precision != AGB_MIXED) return fail(c, AGB_ERR_ARG, "precision must be AGB_FP64 or AGB_MIXED");
-  if (!c->all_dirichlet)
-    return fail(c, AGB_ERR_UNSUPPORTED, "agb_assemble: only walls with known function values are supported");
-  if (c->kind == AGB_LAPLACE && precision != AGB_FP64)
-    return fail(c, AGB_ERR_UNSUPPORTED, "Laplace systems are assembled in FP64 only");
-  if (c->kind == AGB_STOKES && !c->all_tri)
-    return fail(c, AGB_ERR_UNSUPPORTED, "Stokes fused assembly needs a triangle mesh");
+  const bool fast = c->all_dirichlet && ((c->kind == AGB_LAPLACE && precision == AGB_FP64) ||
+                                         (c->kind == AGB_STOKES && c->all_tri));
   cudaSetDevice(c->device);
   free_system(c);
+  if (!fast) return assemble_general(c, precision);
   c->prec = precision;
   const bool f32 = (precision == AGB_MIXED);
   const size_t tsz = f32 ? sizeof(float) : sizeof(double);
@@ -533,9 +736,15 @@ int agb_rhs(agb_context* c, int nrhs, const double* u, double* rhs) {
   if (!c->assembled) return fail(c, AGB_ERR_STATE, "system not assembled");
   if (nrhs < 1 || nrhs > AGB_MAX_RHS || !u) return fail(c, AGB_ERR_ARG, "nrhs must be 1..8");
   cudaSetDevice(c->device);
-  int na = 0;
-  if ((rc = stage_u(c, nrhs, u, &na))) return rc;
-  if ((rc = device_rhs(c, nrhs, na))) return rc;
+  if (c->general) {
+    std::vector<double> b;
+    gather_fields(c, nrhs, u, nullptr, b, nullptr);
+    if ((rc = general_rhs(c, nrhs, b))) return rc;
+  } else {
+    int na = 0;
+    if ((rc = stage_u(c, nrhs, u, &na))) return rc;
+    if ((rc = device_rhs(c, nrhs, na))) return rc;
+  }
   if (rhs)
     CUDA_OR_FAIL(c, cudaMemcpyAsync(rhs, c->d_rhs, (size_t)nrhs * c->m * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
@@ -550,9 +759,15 @@ int agb_solve(agb_context* c, int nrhs, const double* u, double* x, int maxit, d
   if (nrhs < 1 || nrhs > AGB_MAX_RHS || !u || !x) return fail(c, AGB_ERR_ARG, "nrhs must be 1..8");
   if (maxit < 0 || !(eps >= 0.0) || refine < 0) return fail(c, AGB_ERR_ARG, "bad solver parameters");
   cudaSetDevice(c->device);
-  int na = 0;
-  if ((rc = stage_u(c, nrhs, u, &na))) return rc;
-  if ((rc = device_rhs(c, nrhs, na))) return rc;
+  if (c->general) {
+    std::vector<double> b;
+    gather_fields(c, nrhs, u, nullptr, b, nullptr);
+    if ((rc = general_rhs(c, nrhs, b))) return rc;
+  } else {
+    int na = 0;
+    if ((rc = stage_u(c, nrhs, u, &na))) return rc;
+    if ((rc = device_rhs(c, nrhs, na))) return rc;
+  }
   CUDA_OR_FAIL(c, ensure(c->d_x, c->cap_x, (size_t)nrhs * c->n));
   CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_x, x, (size_t)nrhs * c->n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   bool zero = true;
@@ -707,6 +922,103 @@ int agb_kernel_times(agb_context* c, int reset, double* out) {
     c->lsqr.launches = 0;
     c->lsqr_prev_launches = 0;
   }
+  return AGB_OK;
+}
+
+int agb_integral_matrices(agb_context* c, double* T, double* G, double* errs) {
+  int rc = check_ctx(c, true);
+  if (rc) return rc;
+  cudaSetDevice(c->device);
+  const GeneralLayout& L = c->gl;
+  const int ncomp = (c->kind == AGB_STOKES) ? 9 : 1;
+  double *dT = nullptr, *dG = nullptr, *derr = nullptr;
+  CUDA_OR_FAIL(c, cudaMalloc(&dT, (size_t)ncomp * L.nsp * L.nn * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMalloc(&dG, (size_t)ncomp * L.nsp * L.nq * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMalloc(&derr, (size_t)L.nsp * sizeof(double)));
+  cudaError_t e = general_integrals(L, c->gd, c->d_geom, c->d_xyz, c->rule, c->iqud, dT, dG, derr, c->stream);
+  std::vector<double> hT((size_t)ncomp * L.nsp * L.nn), hG((size_t)ncomp * L.nsp * L.nq), herr(L.nsp);
+  if (e == cudaSuccess) e = cudaMemcpy(hT.data(), dT, hT.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(hG.data(), dG, hG.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(herr.data(), derr, herr.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(dT);
+  cudaFree(dG);
+  cudaFree(derr);
+  if (e != cudaSuccess) return fail(c, AGB_ERR_CUDA, std::string("agb_integral_matrices: ") + cudaGetErrorString(e));
+  // column-major per component, as Hmat(nsp, nnodes) of the reference
+  for (int cp = 0; cp < ncomp; ++cp)
+    for (int r = 0; r < L.nsp; ++r) {
+      if (T)
+        for (int j = 0; j < L.nn; ++j)
+          T[(size_t)cp * L.nsp * L.nn + (size_t)j * L.nsp + r] = hT[((size_t)cp * L.nsp + r) * L.nn + j];
+      if (G)
+        for (int p = 0; p < L.nq; ++p)
+          G[(size_t)cp * L.nsp * L.nq + (size_t)p * L.nsp + r] = hG[((size_t)cp * L.nsp + r) * L.nq + p];
+    }
+  if (errs) {
+    double eu = -1e300, eq = -1e300;
+    for (int r = 0; r < L.nsp; ++r) {
+      if (r < L.nn) eu = std::max(eu, herr[r]);
+      else eq = std::max(eq, herr[r]);
+    }
+    errs[0] = eu;
+    errs[1] = eq;
+  }
+  return AGB_OK;
+}
+
+int agb_layout_sizes(agb_context* c, int* sizes) {
+  int rc = check_ctx(c, true);
+  if (rc) return rc;
+  if (sizes) {
+    sizes[0] = c->gl.nsp; sizes[1] = c->gl.nn; sizes[2] = c->gl.nq;
+    sizes[3] = c->gl.nrow; sizes[4] = c->gl.nx; sizes[5] = c->gl.nb;
+  }
+  return AGB_OK;
+}
+
+int agb_solve_fields(agb_context* c, int nrhs, const double* u_in, const double* q_in, double* u_out, double* q_out,
+                     int maxit, double eps, int refine, int* nit, int* istop) {
+  int rc = check_ctx(c, true);
+  if (rc) return rc;
+  if (!c->assembled) return fail(c, AGB_ERR_STATE, "system not assembled");
+  if (nrhs < 1 || nrhs > AGB_MAX_RHS || !u_in || !u_out || !q_out) return fail(c, AGB_ERR_ARG, "nrhs must be 1..8");
+  if (maxit < 0 || !(eps >= 0.0) || refine < 0) return fail(c, AGB_ERR_ARG, "bad solver parameters");
+  cudaSetDevice(c->device);
+  std::vector<double> b, x;
+  gather_fields(c, nrhs, u_in, q_in, b, &x);
+  if (c->general) {
+    if ((rc = general_rhs(c, nrhs, b))) return rc;
+  } else {
+    int na = 0;
+    if ((rc = stage_u(c, nrhs, u_in, &na))) return rc;
+    if ((rc = device_rhs(c, nrhs, na))) return rc;
+  }
+  CUDA_OR_FAIL(c, ensure(c->d_x, c->cap_x, (size_t)nrhs * c->n));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_x, x.data(), x.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  bool zero = true;
+  for (double v : x) zero = zero && (v == 0.0);
+  if ((rc = do_solve(c, nrhs, c->d_x, maxit, eps, refine, nit, istop, zero))) return rc;
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(x.data(), c->d_x, x.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  // StokesDistributeUnknowns / the distribution loop of sdSolveCRS
+  const GeneralLayout& L = c->gl;
+  const size_t nu = (size_t)nrhs * L.neq * c->nnodes, nqv = (size_t)nrhs * L.neq * c->nelem;
+  std::copy(u_in, u_in + nu, u_out);
+  if (q_in) std::copy(q_in, q_in + nqv, q_out);
+  else std::fill(q_out, q_out + nqv, 0.0);
+  for (int r = 0; r < nrhs; ++r)
+    for (int en = 0; en < L.neq; ++en) {
+      for (int j = 0; j < L.nn; ++j) {
+        const int t = en * L.nn + j;
+        if (!L.node_known[t] && L.node_xcol[t] >= 0)
+          u_out[((size_t)r * L.neq + en) * c->nnodes + L.nodeList[j]] = x[(size_t)r * L.nx + L.node_xcol[t]];
+      }
+      for (int p = 0; p < L.nq; ++p) {
+        const int t = en * L.nq + p;
+        if (!L.elem_known[t] && L.elem_xcol[t] >= 0)
+          q_out[((size_t)r * L.neq + en) * c->nelem + c->elemList[p]] = x[(size_t)r * L.nx + L.elem_xcol[t]];
+      }
+    }
   return AGB_OK;
 }
 

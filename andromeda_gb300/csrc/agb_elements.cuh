@@ -1,0 +1,193 @@
+// Element integrals of one (source point, element) pair, FP64, device side.
+// Shared by the general (all-rows, all-BC) assembly of agb_general.cu.
+//
+// Reference behaviour (src/ file:line):
+//   triangle Laplace   Triangle_BEMIntAnal lib_sdBem.f90:741 -> Triangle_3DLapInt :859
+//                      (BemKernel :911) or si_tri_lap mod_singInt.f90:127
+//   quad Laplace       Quad_BEMIntNumAna lib_intAna.f90:156 -> Quad_BEMIntNum :219 or
+//                      si_qua_lap mod_singInt.f90:172
+//   triangle Stokes    Triangle_StokesIntAna lib_intAna.f90:96 -> Triangle_3DStokesInt
+//                      lib_Stokes.f90:2341 (StokesKernel :2450) or si_tri_stk
+//   quad Stokes        Quad_StokesIntNumAna lib_intAna.f90:5 -> Quad_StokesIntNum
+//                      lib_Stokes.f90:3754 (fixed 3x3 subcells) or si_qua_stk
+#pragma once
+#include "agb_common.cuh"
+#include "agb_singular.cuh"
+
+namespace agb {
+
+// The Gauss-Legendre tables gtGi/gtOme/gtNg1/gtNg2 are __constant__ arrays
+// defined by the including translation unit (without relocatable device code
+// every module holds, and uploads, its own copy).
+
+// Laplace: g, h[4] (nodal, linear shape functions)
+struct LapElem {
+  double g, h[4];
+};
+// Stokes: G {xx,xy,xz,yy,yz,zz}, prG[3], T[6][4] (component x local node), prT[3][4]
+struct StkElem {
+  double G[6], prG[3], T[6][4], prT[3][4];
+};
+
+__device__ __forceinline__ void quad_map(const double (*P)[3], double gii, double gij, double* X, double* N, double* f4) {
+  const double e1m = 1.0 - gii, e1p = 1.0 + gii, e2m = 1.0 - gij, e2p = 1.0 + gij;
+  f4[0] = 0.25 * e1m * e2m; f4[1] = 0.25 * e1p * e2m; f4[2] = 0.25 * e1p * e2p; f4[3] = 0.25 * e1m * e2p;
+  double KS[3], ET[3];
+  for (int k = 0; k < 3; ++k) {
+    X[k] = f4[0] * P[0][k] + f4[1] * P[1][k] + f4[2] * P[2][k] + f4[3] * P[3][k];
+    KS[k] = 0.25 * (-e2m * P[0][k] + e2m * P[1][k] + e2p * P[2][k] - e2p * P[3][k]);
+    ET[k] = 0.25 * (-e1m * P[0][k] - e1p * P[1][k] + e1p * P[2][k] + e1m * P[3][k]);
+  }
+  N[0] = KS[1] * ET[2] - ET[1] * KS[2];
+  N[1] = ET[0] * KS[2] - KS[0] * ET[2];
+  N[2] = KS[0] * ET[1] - ET[0] * KS[1];
+}
+
+// ---- Laplace ---------------------------------------------------------------
+__device__ inline LapElem lap_element(const ElemGeom& E, const double* s, int isrc, const double* rl, const double* rw,
+                                      int Q, int iqud) {
+  LapElem o;
+  o.g = 0.0;
+  o.h[0] = o.h[1] = o.h[2] = o.h[3] = 0.0;
+  const double fpi = 0.25 / AGB_PI;
+  if (E.type == AGB_TRI) {
+    if (isrc) {
+      o.g = agb_sing::tri_laplace(E.v[0], E.v[1], E.v[2], E.area, isrc);
+      return o;
+    }
+    const double n[3] = {E.multi * E.n[0], E.multi * E.n[1], E.multi * E.n[2]};
+    for (int q = 0; q < Q; ++q) {
+      const double l1 = rl[q], l2 = rl[Q + q], l3 = rl[2 * Q + q];
+      const double x = l1 * E.v[0][0] + l2 * E.v[1][0] + l3 * E.v[2][0];
+      const double y = l1 * E.v[0][1] + l2 * E.v[1][1] + l3 * E.v[2][1];
+      const double z = l1 * E.v[0][2] + l2 * E.v[1][2] + l3 * E.v[2][2];
+      const double RX = s[0] - x, RY = s[1] - y, RZ = s[2] - z;
+      const double RA = sqrt(RX * RX + RY * RY + RZ * RZ);
+      const double FG = fpi / RA;
+      const double FH = (RX * n[0] + RY * n[1] + RZ * n[2]) * (1.0 / (RA * RA)) * FG;
+      o.g += rw[q] * FG * E.area;
+      o.h[0] += rw[q] * FH * E.area * l1;
+      o.h[1] += rw[q] * FH * E.area * l2;
+      o.h[2] += rw[q] * FH * E.area * l3;
+    }
+    return o;
+  }
+  if (isrc) {
+    o.g = agb_sing::quad_laplace(E.v, isrc);
+    return o;
+  }
+  const int ng1 = gtNg1[iqud - 1], ng2 = gtNg2[iqud - 1];
+  auto dist = [&](int p, int q) {
+    const double dx = E.v[p][0] - E.v[q][0], dy = E.v[p][1] - E.v[q][1], dz = E.v[p][2] - E.v[q][2];
+    return sqrt(dx * dx + dy * dy + dz * dz);
+  };
+  const double d13 = fmax(dist(0, 1), dist(2, 3)), d24 = fmax(dist(1, 2), dist(3, 0));
+  const int ndx = max(2, (int)(d13 / 1.0 + 0.5)), nde = max(2, (int)(d24 / 1.0 + 0.5));
+  for (int ix = 1; ix <= ndx; ++ix)
+    for (int ie = 1; ie <= nde; ++ie) {
+      const double a = -1.0 + (ix - 1) * 2.0 / ndx, b = -1.0 + ix * 2.0 / ndx;
+      const double c = -1.0 + (ie - 1) * 2.0 / nde, d = -1.0 + ie * 2.0 / nde;
+      const double dex = 0.25 * (b - a) * (d - c);
+      for (int i = ng1; i <= ng2; ++i)
+        for (int j = ng1; j <= ng2; ++j) {
+          const double gii = a + 0.5 * (gtGi[i - 1] + 1.0) * (b - a);
+          const double gij = c + 0.5 * (gtGi[j - 1] + 1.0) * (d - c);
+          double X[3], N[3], f4[4];
+          quad_map(E.v, gii, gij, X, N, f4);
+          double aj = 1.0 / sqrt(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
+          const double n1 = E.multi * N[0] * aj, n2 = E.multi * N[1] * aj, n3 = E.multi * N[2] * aj;
+          aj = dex * gtOme[i - 1] * gtOme[j - 1] / aj;
+          const double RX = s[0] - X[0], RY = s[1] - X[1], RZ = s[2] - X[2];
+          const double RA = sqrt(RX * RX + RY * RY + RZ * RZ);
+          const double FG = fpi / RA;
+          const double FH = (RX * n1 + RY * n2 + RZ * n3) * (1.0 / (RA * RA)) * FG;
+          for (int k = 0; k < 4; ++k) o.h[k] += FH * aj * f4[k];
+          o.g += FG * aj;
+        }
+    }
+  return o;
+}
+
+// ---- Stokes ----------------------------------------------------------------
+__device__ __forceinline__ void stk_kernel(const double* s, const double* f, const double* n, double G[6], double T[6],
+                                           double prG[3], double prT[3]) {
+  const double rx = f[0] - s[0], ry = f[1] - s[1], rz = f[2] - s[2];
+  const double rxx = rx * rx, rxy = rx * ry, rxz = rx * rz, ryy = ry * ry, ryz = ry * rz, rzz = rz * rz;
+  const double ir2 = 1.0 / (rxx + ryy + rzz);
+  const double ir = sqrt(ir2);
+  const double ir3 = ir2 * ir;
+  G[0] = ir * (1.0 + rxx * ir2); G[1] = rxy * ir3; G[2] = rxz * ir3;
+  G[3] = ir * (1.0 + ryy * ir2); G[4] = ryz * ir3; G[5] = ir * (1.0 + rzz * ir2);
+  double c = -6.0 * ir2 * ir3 * (rx * n[0] + ry * n[1] + rz * n[2]);
+  T[0] = c * rxx; T[1] = c * rxy; T[2] = c * rxz; T[3] = c * ryy; T[4] = c * ryz; T[5] = c * rzz;
+  c = 2.0 * ir3;
+  prG[0] = c * rx; prG[1] = c * ry; prG[2] = c * rz;
+  c = 4.0 * ir3;
+  prT[0] = c * ((-1.0 + 3.0 * rxx * ir2) * n[0] + 3.0 * rxy * ir2 * n[1] + 3.0 * rxz * ir2 * n[2]);
+  prT[1] = c * (3.0 * rxy * ir2 * n[0] + (-1.0 + 3.0 * ryy * ir2) * n[1] + 3.0 * ryz * ir2 * n[2]);
+  prT[2] = c * (3.0 * rxz * ir2 * n[0] + 3.0 * ryz * ir2 * n[1] + (-1.0 + 3.0 * rzz * ir2) * n[2]);
+}
+
+__device__ inline void stk_element(const ElemGeom& E, const double* s, int isrc, const double* rl, const double* rw,
+                                   int Q, int iqud, StkElem& o) {
+  for (int k = 0; k < 6; ++k) {
+    o.G[k] = 0.0;
+    for (int j = 0; j < 4; ++j) o.T[k][j] = 0.0;
+  }
+  for (int k = 0; k < 3; ++k) {
+    o.prG[k] = 0.0;
+    for (int j = 0; j < 4; ++j) o.prT[k][j] = 0.0;
+  }
+  if (isrc) {
+    if (E.type == AGB_TRI) agb_sing::tri_stokes(E.v[0], E.v[1], E.v[2], E.area, isrc, o.G);
+    else agb_sing::quad_stokes(E.v, isrc, o.G);
+    return;
+  }
+  double G[6], T[6], prG[3], prT[3];
+  if (E.type == AGB_TRI) {
+    const double n[3] = {E.multi * E.n[0], E.multi * E.n[1], E.multi * E.n[2]};
+    for (int q = 0; q < Q; ++q) {
+      const double l[3] = {rl[q], rl[Q + q], rl[2 * Q + q]};
+      const double f[3] = {l[0] * E.v[0][0] + l[1] * E.v[1][0] + l[2] * E.v[2][0],
+                           l[0] * E.v[0][1] + l[1] * E.v[1][1] + l[2] * E.v[2][1],
+                           l[0] * E.v[0][2] + l[1] * E.v[1][2] + l[2] * E.v[2][2]};
+      stk_kernel(s, f, n, G, T, prG, prT);
+      const double w = rw[q] * E.area;
+      for (int k = 0; k < 6; ++k) o.G[k] += w * G[k];
+      for (int k = 0; k < 3; ++k) o.prG[k] += w * prG[k];
+      for (int j = 0; j < 3; ++j) {
+        const double wl = w * l[j];
+        for (int k = 0; k < 6; ++k) o.T[k][j] += wl * T[k];
+        for (int k = 0; k < 3; ++k) o.prT[k][j] += wl * prT[k];
+      }
+    }
+    return;
+  }
+  const int ng1 = gtNg1[iqud - 1], ng2 = gtNg2[iqud - 1];
+  for (int ix = 1; ix <= 3; ++ix)
+    for (int ie = 1; ie <= 3; ++ie) {
+      const double a = -1.0 + (ix - 1) * 2.0 / 3, b = -1.0 + ix * 2.0 / 3;
+      const double c = -1.0 + (ie - 1) * 2.0 / 3, d = -1.0 + ie * 2.0 / 3;
+      const double dex = 0.25 * (b - a) * (d - c);
+      for (int i = ng1; i <= ng2; ++i)
+        for (int j = ng1; j <= ng2; ++j) {
+          const double gii = a + 0.5 * (gtGi[i - 1] + 1.0) * (b - a);
+          const double gij = c + 0.5 * (gtGi[j - 1] + 1.0) * (d - c);
+          double X[3], N[3], f4[4];
+          quad_map(E.v, gii, gij, X, N, f4);
+          double aj = 1.0 / sqrt(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
+          const double nn[3] = {E.multi * N[0] * aj, E.multi * N[1] * aj, E.multi * N[2] * aj};
+          aj = dex * gtOme[i - 1] * gtOme[j - 1] / aj;
+          stk_kernel(s, X, nn, G, T, prG, prT);
+          for (int k = 0; k < 6; ++k) o.G[k] += aj * G[k];
+          for (int k = 0; k < 3; ++k) o.prG[k] += aj * prG[k];
+          for (int sp = 0; sp < 4; ++sp) {
+            const double w = aj * f4[sp];
+            for (int k = 0; k < 6; ++k) o.T[k][sp] += w * T[k];
+            for (int k = 0; k < 3; ++k) o.prT[k][sp] += w * prT[k];
+          }
+        }
+    }
+}
+
+}  // namespace agb

@@ -156,8 +156,14 @@ def particle_in_sphere(particle, outer_level: int = 2, outer_radius: float = 200
     return merge(p, outer)
 
 
-def quad_box(nx: int, ny: int, nz: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), inward: bool = False, wall: int = 1):
-    """Axis-aligned box of 4-node quads (outward normals unless ``inward``)."""
+def quad_box(nx: int, ny: int, nz: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), inward: bool = False, wall: int = 1,
+             face_walls: bool = False, triangles: bool = False):
+    """Axis-aligned box of 4-node quads (outward normals unless ``inward``).
+
+    ``face_walls``: wall ids 1..6 for the faces x-, x+, y-, y+, z-, z+
+    (otherwise every element gets ``wall``).  ``triangles``: split every quad
+    into two 3-node triangles.
+    """
     lo = np.asarray(lo, float)
     hi = np.asarray(hi, float)
     nodes = {}
@@ -171,6 +177,7 @@ def quad_box(nx: int, ny: int, nz: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), 
         return nodes[key]
 
     quads = []
+    fw = []
     n = (nx, ny, nz)
     for ax in range(3):
         u, v = [a for a in range(3) if a != ax]
@@ -185,6 +192,7 @@ def quad_box(nx: int, ny: int, nz: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), 
                         p[v] = lo[v] + (hi[v] - lo[v]) * (j + dj) / n[v]
                         corners.append(node(p))
                     quads.append(corners)
+                    fw.append(1 + 2 * ax + side)
     xyz = np.array(xyz)
     quads = np.array(quads, dtype=np.int32)
     p = xyz[quads]
@@ -193,8 +201,13 @@ def quad_box(nx: int, ny: int, nz: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), 
     out = np.einsum("ij,ij->i", nrm, p.mean(axis=1) - ctr) > 0
     flip = out if inward else ~out
     quads[flip] = quads[flip][:, [0, 3, 2, 1]]
-    return {"xyz": xyz, "etype": np.full(len(quads), 3, np.int32), "con": quads,
-            "bcid": np.full(len(quads), wall, np.int32)}
+    bc = np.array(fw, np.int32) if face_walls else np.full(len(quads), wall, np.int32)
+    if triangles:
+        tris = np.concatenate([quads[:, [0, 1, 2]], quads[:, [0, 2, 3]]])
+        m = _tri_mesh(xyz, tris)
+        m["bcid"] = np.concatenate([bc, bc])
+        return m
+    return {"xyz": xyz, "etype": np.full(len(quads), 3, np.int32), "con": quads, "bcid": bc}
 
 
 def random_rotation(rng: np.random.Generator):

@@ -106,8 +106,11 @@ int agb_get_geometry(agb_context* ctx, double* normal, double* area, double* cen
 int agb_system_size(agb_context* ctx, int* m, int* n);
 
 /* Assemble the system matrix on the GPU in the given precision and apply the
- * reference's column scaling (lsqr_precon).  Current scope: every wall has
- * known function values (all-Dirichlet), triangles for AGB_MIXED. */
+ * reference's column scaling (lsqr_precon).  Walls with known function values
+ * only, triangles (Stokes) / FP64 (Laplace): fused single-layer assembly of the
+ * used rows.  Any other case (known fluxes, contact, Stokes quads, mixed
+ * Laplace): every source row in FP64 + BC routing (general path); AGB_MIXED
+ * then stores the routed system in FP32. */
 int agb_assemble(agb_context* ctx, int precision);
 
 /* Copy the assembled system to the host (m x n row-major), with (scaled=1) or
@@ -159,6 +162,30 @@ int agb_kernel_times(agb_context* ctx, int reset, double* out);
 int agb_lsqr_precon(int m, int n, int64_t nnz, double* q, const int64_t* ia, const int* ja, double* a);
 int agb_lsqr_solve(int m, int n, int64_t nnz, int* maxit, double eps, int* nit, int* ierr, const double* q,
                    const int64_t* ia, const int* ja, double* a, const double* b, double* x);
+
+/* Integral matrices of every source row -- the drop-in of CoR_Integrals
+ * (lib_int.f90:4, sdFormIntegralMatrices :225) and CoR_Integrals_Stokes
+ * (lib_Stokes.f90:2664, sdFormIntegralMatricesStokes :1391), FP64 on the GPU:
+ * rows = the nn u-source points (subdomain nodes, ascending) then the nq
+ * q-source points (element centroids, subdomain order); free terms included.
+ * Each component matrix is column-major nsp x ncol like Hmat(nsp,nnodes).
+ * Laplace: T = H (1 matrix, ncol = nn), G (1, ncol = nq).  Stokes: T = 9
+ * matrices Txx,Txy,Txz,Tyy,Tyz,Tzz,prTx,prTy,prTz; G = 9 matrices
+ * Gxx,Gxy,Gxz,Gyy,Gyz,Gzz,prGx,prGy,prGz.  errs[2] = the reference's fSP/qSP
+ * self-check residuals (max over u-rows, over q-rows). */
+int agb_integral_matrices(agb_context* ctx, double* T, double* G, double* errs);
+
+/* Sizes of the subdomain numbering: {nsp, nn, nq, rows, unknowns, knowns}. */
+int agb_layout_sizes(agb_context* ctx, int* sizes);
+
+/* Solve with any boundary-condition mix of the subdomain (sdSolveCRS
+ * lib_CRS.f90:4 / StokesBigSystemSOLVEcrs lib_Stokes.f90:417 +
+ * StokesDistributeUnknowns lib_StokesFull.f90:446): u_in[r][neq][nnodes] and
+ * q_in[r][neq][nelem] (may be NULL = 0) hold the known values and the warm
+ * start of the unknowns; u_out/q_out receive the fields with the unknowns
+ * filled in.  Works after agb_assemble on either assembly path. */
+int agb_solve_fields(agb_context* ctx, int nrhs, const double* u_in, const double* q_in, double* u_out,
+                     double* q_out, int maxit, double eps, int refine, int* nit, int* istop);
 
 /* Allocation-free column scaling for callers that cannot call cudaMalloc (a
  * host program that owns all device memory through its own pool or an
