@@ -121,6 +121,13 @@ class Context:
         self._ck(self._L.agb_system_size(self.h, C.byref(m), C.byref(n)))
         self.m, self.n = m.value, n.value
 
+    def set_integration(self, sing_mode=0, rec_depth=20, near_eta=0.0, near_depth=0):
+        """Triangle integration options: sing_mode 0 analytic / 1 recursive
+        subdivision (rec_depth levels); near_eta > 0 enables the adaptive
+        near-singular rule (near_depth levels).  Clears the assembled system."""
+        self._ck(self._L.agb_set_integration(self.h, int(sing_mode), int(rec_depth), float(near_eta),
+                                             int(near_depth)))
+
     def geometry(self):
         nrm = np.zeros(3 * self.nelem)
         area = np.zeros(self.nelem)

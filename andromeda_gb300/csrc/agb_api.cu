@@ -30,6 +30,7 @@ struct agb_context {
   bool has_mesh = false;
   // problem
   int kind = 0, neq = 0;
+  IntegOpt iopt;  // triangle integration options (agb_set_integration)
   std::vector<int> walls;
   std::vector<double> normMul;
   double diff = 1.0;
@@ -379,7 +380,7 @@ int assemble_general(agb_context* c, int precision) {
   CUDA_OR_FAIL(c, cudaMalloc(&T, (size_t)ncomp * L.nsp * L.nn * sizeof(double)));
   CUDA_OR_FAIL(c, cudaMalloc(&G, (size_t)ncomp * L.nsp * L.nq * sizeof(double)));
   CUDA_OR_FAIL(c, cudaMalloc(&err, (size_t)L.nsp * sizeof(double)));
-  cudaError_t e = general_integrals(L, c->gd, c->d_geom, c->d_xyz, c->rule, c->iqud, T, G, err, c->stream);
+  cudaError_t e = general_integrals(L, c->gd, c->d_geom, c->d_xyz, c->rule, c->iqud, c->iopt, T, G, err, c->stream);
   c->nlaunch += 2 * (int)((L.nsp + 65534) / 65535 + 1);
   if (e != cudaSuccess) { cudaFree(T); cudaFree(G); cudaFree(err); return fail(c, AGB_ERR_CUDA, std::string("general integrals: ") + cudaGetErrorString(e)); }
   c->lda = ((int64_t)L.nx + 31) / 32 * 32;
@@ -610,6 +611,21 @@ int agb_set_problem(agb_context* c, int kind, int nwalls, const int* walls, cons
   return AGB_OK;
 }
 
+int agb_set_integration(agb_context* c, int sing_mode, int rec_depth, double near_eta, int near_depth) {
+  int rc = check_ctx(c, true);
+  if (rc) return rc;
+  if (sing_mode != 0 && sing_mode != 1) return fail(c, AGB_ERR_ARG, "sing_mode must be 0 (analytic) or 1 (recursive)");
+  if (rec_depth < 0 || rec_depth > 30) return fail(c, AGB_ERR_ARG, "rec_depth must be 0..30");
+  if (!(near_eta >= 0.0) || !std::isfinite(near_eta)) return fail(c, AGB_ERR_ARG, "near_eta must be finite and >= 0");
+  if (near_depth < 0 || near_depth > 20) return fail(c, AGB_ERR_ARG, "near_depth must be 0..20");
+  c->iopt.sing = sing_mode;
+  c->iopt.rdepth = rec_depth;
+  c->iopt.near_eta = near_eta;
+  c->iopt.near_depth = near_depth;
+  c->assembled = false;
+  return AGB_OK;
+}
+
 int agb_get_geometry(agb_context* c, double* normal, double* area, double* centroid) {
   int rc = check_ctx(c, true);
   if (rc) return rc;
@@ -642,8 +658,8 @@ int agb_assemble(agb_context* c, int precision) {
   int rc = check_ctx(c, true);
   if (rc) return rc;
   if (precision != AGB_FP64 && precision != AGB_MIXED) return fail(c, AGB_ERR_ARG, "precision must be AGB_FP64 or AGB_MIXED");
-  const bool fast = c->all_dirichlet && ((c->kind == AGB_LAPLACE && precision == AGB_FP64) ||
-                                         (c->kind == AGB_STOKES && c->all_tri));
+  const bool fast = c->all_dirichlet && c->iopt.is_default() &&
+                    ((c->kind == AGB_LAPLACE && precision == AGB_FP64) || (c->kind == AGB_STOKES && c->all_tri));
   cudaSetDevice(c->device);
   free_system(c);
   if (!fast) return assemble_general(c, precision);
@@ -803,6 +819,7 @@ int agb_resistance_tensor(agb_context* c, int precision, int particle_wall, int 
   int rc = check_ctx(c, true);
   if (rc) return rc;
   if (c->kind != AGB_STOKES) return fail(c, AGB_ERR_UNSUPPORTED, "resistance tensor needs a Stokes problem");
+  if (!c->all_dirichlet) return fail(c, AGB_ERR_UNSUPPORTED, "resistance tensor needs velocity known on every wall");
   if (!R) return fail(c, AGB_ERR_ARG, "R is NULL");
   int pidx = -1, oidx = -1;
   for (size_t k = 0; k < c->walls.size(); ++k) {
@@ -838,9 +855,15 @@ int agb_resistance_tensor(agb_context* c, int precision, int particle_wall, int 
     for (int a = 0; a < 3; ++a)
       for (int b = 0; b < 3; ++b) u[((size_t)(3 + a) * 3 + b) * c->nnodes + i] = w[a][b];
   }
-  int na = 0;
-  if ((rc = stage_u(c, k, u.data(), &na))) return rc;
-  if ((rc = device_rhs(c, k, na))) return rc;
+  if (c->general) {
+    std::vector<double> b;
+    gather_fields(c, k, u.data(), nullptr, b, nullptr);
+    if ((rc = general_rhs(c, k, b))) return rc;
+  } else {
+    int na = 0;
+    if ((rc = stage_u(c, k, u.data(), &na))) return rc;
+    if ((rc = device_rhs(c, k, na))) return rc;
+  }
   CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
   auto t2 = clk::now();
   CUDA_OR_FAIL(c, ensure(c->d_x, c->cap_x, (size_t)k * c->n));
@@ -935,7 +958,7 @@ int agb_integral_matrices(agb_context* c, double* T, double* G, double* errs) {
   CUDA_OR_FAIL(c, cudaMalloc(&dT, (size_t)ncomp * L.nsp * L.nn * sizeof(double)));
   CUDA_OR_FAIL(c, cudaMalloc(&dG, (size_t)ncomp * L.nsp * L.nq * sizeof(double)));
   CUDA_OR_FAIL(c, cudaMalloc(&derr, (size_t)L.nsp * sizeof(double)));
-  cudaError_t e = general_integrals(L, c->gd, c->d_geom, c->d_xyz, c->rule, c->iqud, dT, dG, derr, c->stream);
+  cudaError_t e = general_integrals(L, c->gd, c->d_geom, c->d_xyz, c->rule, c->iqud, c->iopt, dT, dG, derr, c->stream);
   std::vector<double> hT((size_t)ncomp * L.nsp * L.nn), hG((size_t)ncomp * L.nsp * L.nq), herr(L.nsp);
   if (e == cudaSuccess) e = cudaMemcpy(hT.data(), dT, hT.size() * sizeof(double), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(hG.data(), dG, hG.size() * sizeof(double), cudaMemcpyDeviceToHost);

@@ -30,3 +30,21 @@ struct ElemGeom {
 };
 
 static inline const char* agb_cuda_str(cudaError_t e) { return cudaGetErrorString(e); }
+
+// Integration options of the triangle integrals:
+//   sing 0: analytic self-element integrals (the reference's assembly);
+//   sing 1: recursive midpoint subdivision toward the source, rdepth levels
+//           (Triangle_BEMInt lib_sdBem.f90:775-852 / Triangle_StokesInt
+//           lib_Stokes.f90:2251-2336 with IntRecDepth = parTriRecur); quads keep
+//           the analytic scheme;
+//   near_eta > 0: adaptive near-singular rule for non-singular triangles: a
+//           (sub-)triangle whose centroid is closer to the source than near_eta x
+//           its longest edge is split into its four children, up to near_depth
+//           levels (<= 20); leaves take the regular rule.
+struct IntegOpt {
+  int sing = 0;
+  int rdepth = 20;
+  double near_eta = 0.0;
+  int near_depth = 0;
+  bool is_default() const { return sing == 0 && !(near_eta > 0.0 && near_depth > 0); }
+};

@@ -29,6 +29,105 @@ struct StkElem {
   double G[6], prG[3], T[6][4], prT[3][4];
 };
 
+// A sub-triangle as the element barycentrics of its three vertices B[k][j].
+// Midpoint split with 4 = (1+2)/2, 5 = (2+3)/2, 6 = (1+3)/2: child 0 = (1,4,6),
+// 1 = (4,2,5), 2 = (6,5,3), 3 = (4,5,6); each child has a quarter of the area
+// and half the edges of its parent.
+struct Bary {
+  double b[3][3];
+};
+__device__ __forceinline__ Bary bary_identity() {
+  Bary B;
+  for (int k = 0; k < 3; ++k)
+    for (int j = 0; j < 3; ++j) B.b[k][j] = (k == j) ? 1.0 : 0.0;
+  return B;
+}
+__device__ __forceinline__ Bary sub_child(const Bary& P, int d) {
+  Bary C;
+  for (int j = 0; j < 3; ++j) {
+    const double m4 = 0.5 * (P.b[0][j] + P.b[1][j]);
+    const double m5 = 0.5 * (P.b[2][j] + P.b[1][j]);
+    const double m6 = 0.5 * (P.b[0][j] + P.b[2][j]);
+    if (d == 0) { C.b[0][j] = P.b[0][j]; C.b[1][j] = m4; C.b[2][j] = m6; }
+    else if (d == 1) { C.b[0][j] = m4; C.b[1][j] = P.b[1][j]; C.b[2][j] = m5; }
+    else if (d == 2) { C.b[0][j] = m6; C.b[1][j] = m5; C.b[2][j] = P.b[2][j]; }
+    else { C.b[0][j] = m4; C.b[1][j] = m5; C.b[2][j] = m6; }
+  }
+  return C;
+}
+
+// Visits the sub-triangles of triangle E for source s in the order of the
+// reference's recursion (children 0..3, depth first): rule(B, area_of_sub,
+// skip_centroid).  skip_centroid marks the last piece of a centroid-source
+// recursion, whose centroid is the source: a rule with a centroid point
+// (ITRI 1, 2, 4) would divide by r = 0 there, so that point is left out.
+template <class F>
+__device__ inline void tri_walk(const IntegOpt& o, const ElemGeom& E, const double* s, int isrc, F&& rule) {
+  if (isrc) {
+    // only the child holding the source recurses; the last piece takes the regular rule
+    const int ks = isrc - 1;
+    Bary B = bary_identity();
+    double a = E.area;
+    for (int lev = 0; lev < o.rdepth; ++lev) {
+      for (int d = 0; d < ks; ++d) rule(sub_child(B, d), 0.25 * a, false);
+      B = sub_child(B, ks);
+      a *= 0.25;
+    }
+    rule(B, a, isrc == 4);
+    for (int lev = o.rdepth - 1; lev >= 0; --lev) {
+      Bary Bl = bary_identity();
+      double al = E.area;
+      for (int t = 0; t < lev; ++t) {
+        Bl = sub_child(Bl, ks);
+        al *= 0.25;
+      }
+      for (int d = ks + 1; d < 4; ++d) rule(sub_child(Bl, d), 0.25 * al, false);
+    }
+    return;
+  }
+  if (o.near_eta > 0.0 && o.near_depth > 0) {
+    auto edge = [&](int p, int q) {
+      const double dx = E.v[p][0] - E.v[q][0], dy = E.v[p][1] - E.v[q][1], dz = E.v[p][2] - E.v[q][2];
+      return sqrt(dx * dx + dy * dy + dz * dz);
+    };
+    const double diam = fmax(edge(0, 1), fmax(edge(1, 2), edge(2, 0)));
+    // depth-first stack: 2 bits per level (child index), the level in bits 58..63;
+    // at most 3 * near_depth + 1 <= 61 entries
+    uint64_t stack[64];
+    int top = 0;
+    stack[top++] = 0;
+    while (top > 0) {
+      const uint64_t e = stack[--top];
+      const int lev = (int)(e >> 58);
+      Bary B = bary_identity();
+      double a = E.area, h = diam;
+      for (int t = 0; t < lev; ++t) {
+        B = sub_child(B, (int)((e >> (2 * t)) & 3u));
+        a *= 0.25;
+        h *= 0.5;
+      }
+      double c[3] = {0.0, 0.0, 0.0};
+      for (int j = 0; j < 3; ++j) {
+        const double Lc = (B.b[0][j] + B.b[1][j] + B.b[2][j]) / 3.0;
+        for (int i = 0; i < 3; ++i) c[i] += Lc * E.v[j][i];
+      }
+      const double d = sqrt((s[0] - c[0]) * (s[0] - c[0]) + (s[1] - c[1]) * (s[1] - c[1]) +
+                            (s[2] - c[2]) * (s[2] - c[2]));
+      if (lev < o.near_depth && d < o.near_eta * h && top <= 60) {
+        for (int ch = 3; ch >= 0; --ch)
+          stack[top++] = (e & ((1ull << 58) - 1)) | ((uint64_t)ch << (2 * lev)) | ((uint64_t)(lev + 1) << 58);
+      } else {
+        rule(B, a, false);
+      }
+    }
+    return;
+  }
+  rule(bary_identity(), E.area, false);
+}
+__device__ __forceinline__ bool is_centroid_point(double l1, double l2, double l3) {
+  return fabs(l1 - l2) < 1e-12 && fabs(l2 - l3) < 1e-12;
+}
+
 __device__ __forceinline__ void quad_map(const double (*P)[3], double gii, double gij, double* X, double* N, double* f4) {
   const double e1m = 1.0 - gii, e1p = 1.0 + gii, e2m = 1.0 - gij, e2p = 1.0 + gij;
   f4[0] = 0.25 * e1m * e2m; f4[1] = 0.25 * e1p * e2m; f4[2] = 0.25 * e1p * e2p; f4[3] = 0.25 * e1m * e2p;
@@ -45,31 +144,36 @@ __device__ __forceinline__ void quad_map(const double (*P)[3], double gii, doubl
 
 // ---- Laplace ---------------------------------------------------------------
 __device__ inline LapElem lap_element(const ElemGeom& E, const double* s, int isrc, const double* rl, const double* rw,
-                                      int Q, int iqud) {
+                                      int Q, int iqud, const IntegOpt& opt) {
   LapElem o;
   o.g = 0.0;
   o.h[0] = o.h[1] = o.h[2] = o.h[3] = 0.0;
   const double fpi = 0.25 / AGB_PI;
   if (E.type == AGB_TRI) {
-    if (isrc) {
+    if (isrc && opt.sing == 0) {
       o.g = agb_sing::tri_laplace(E.v[0], E.v[1], E.v[2], E.area, isrc);
       return o;
     }
     const double n[3] = {E.multi * E.n[0], E.multi * E.n[1], E.multi * E.n[2]};
-    for (int q = 0; q < Q; ++q) {
-      const double l1 = rl[q], l2 = rl[Q + q], l3 = rl[2 * Q + q];
-      const double x = l1 * E.v[0][0] + l2 * E.v[1][0] + l3 * E.v[2][0];
-      const double y = l1 * E.v[0][1] + l2 * E.v[1][1] + l3 * E.v[2][1];
-      const double z = l1 * E.v[0][2] + l2 * E.v[1][2] + l3 * E.v[2][2];
-      const double RX = s[0] - x, RY = s[1] - y, RZ = s[2] - z;
-      const double RA = sqrt(RX * RX + RY * RY + RZ * RZ);
-      const double FG = fpi / RA;
-      const double FH = (RX * n[0] + RY * n[1] + RZ * n[2]) * (1.0 / (RA * RA)) * FG;
-      o.g += rw[q] * FG * E.area;
-      o.h[0] += rw[q] * FH * E.area * l1;
-      o.h[1] += rw[q] * FH * E.area * l2;
-      o.h[2] += rw[q] * FH * E.area * l3;
-    }
+    tri_walk(opt, E, s, isrc, [&](const Bary& B, double area, bool skip_centroid) {
+      for (int q = 0; q < Q; ++q) {
+        const double l1 = rl[q], l2 = rl[Q + q], l3 = rl[2 * Q + q];
+        if (skip_centroid && is_centroid_point(l1, l2, l3)) continue;
+        double L[3];
+        for (int j = 0; j < 3; ++j) L[j] = l1 * B.b[0][j] + l2 * B.b[1][j] + l3 * B.b[2][j];
+        const double x = L[0] * E.v[0][0] + L[1] * E.v[1][0] + L[2] * E.v[2][0];
+        const double y = L[0] * E.v[0][1] + L[1] * E.v[1][1] + L[2] * E.v[2][1];
+        const double z = L[0] * E.v[0][2] + L[1] * E.v[1][2] + L[2] * E.v[2][2];
+        const double RX = s[0] - x, RY = s[1] - y, RZ = s[2] - z;
+        const double RA = sqrt(RX * RX + RY * RY + RZ * RZ);
+        const double FG = fpi / RA;
+        const double FH = (RX * n[0] + RY * n[1] + RZ * n[2]) * (1.0 / (RA * RA)) * FG;
+        o.g += rw[q] * FG * area;
+        o.h[0] += rw[q] * FH * area * L[0];
+        o.h[1] += rw[q] * FH * area * L[1];
+        o.h[2] += rw[q] * FH * area * L[2];
+      }
+    });
     return o;
   }
   if (isrc) {
@@ -129,7 +233,7 @@ __device__ __forceinline__ void stk_kernel(const double* s, const double* f, con
 }
 
 __device__ inline void stk_element(const ElemGeom& E, const double* s, int isrc, const double* rl, const double* rw,
-                                   int Q, int iqud, StkElem& o) {
+                                   int Q, int iqud, const IntegOpt& opt, StkElem& o) {
   for (int k = 0; k < 6; ++k) {
     o.G[k] = 0.0;
     for (int j = 0; j < 4; ++j) o.T[k][j] = 0.0;
@@ -138,7 +242,7 @@ __device__ inline void stk_element(const ElemGeom& E, const double* s, int isrc,
     o.prG[k] = 0.0;
     for (int j = 0; j < 4; ++j) o.prT[k][j] = 0.0;
   }
-  if (isrc) {
+  if (isrc && (E.type != AGB_TRI || opt.sing == 0)) {
     if (E.type == AGB_TRI) agb_sing::tri_stokes(E.v[0], E.v[1], E.v[2], E.area, isrc, o.G);
     else agb_sing::quad_stokes(E.v, isrc, o.G);
     return;
@@ -146,21 +250,26 @@ __device__ inline void stk_element(const ElemGeom& E, const double* s, int isrc,
   double G[6], T[6], prG[3], prT[3];
   if (E.type == AGB_TRI) {
     const double n[3] = {E.multi * E.n[0], E.multi * E.n[1], E.multi * E.n[2]};
-    for (int q = 0; q < Q; ++q) {
-      const double l[3] = {rl[q], rl[Q + q], rl[2 * Q + q]};
-      const double f[3] = {l[0] * E.v[0][0] + l[1] * E.v[1][0] + l[2] * E.v[2][0],
-                           l[0] * E.v[0][1] + l[1] * E.v[1][1] + l[2] * E.v[2][1],
-                           l[0] * E.v[0][2] + l[1] * E.v[1][2] + l[2] * E.v[2][2]};
-      stk_kernel(s, f, n, G, T, prG, prT);
-      const double w = rw[q] * E.area;
-      for (int k = 0; k < 6; ++k) o.G[k] += w * G[k];
-      for (int k = 0; k < 3; ++k) o.prG[k] += w * prG[k];
-      for (int j = 0; j < 3; ++j) {
-        const double wl = w * l[j];
-        for (int k = 0; k < 6; ++k) o.T[k][j] += wl * T[k];
-        for (int k = 0; k < 3; ++k) o.prT[k][j] += wl * prT[k];
+    tri_walk(opt, E, s, isrc, [&](const Bary& B, double area, bool skip_centroid) {
+      for (int q = 0; q < Q; ++q) {
+        const double l1 = rl[q], l2 = rl[Q + q], l3 = rl[2 * Q + q];
+        if (skip_centroid && is_centroid_point(l1, l2, l3)) continue;
+        double l[3];
+        for (int j = 0; j < 3; ++j) l[j] = l1 * B.b[0][j] + l2 * B.b[1][j] + l3 * B.b[2][j];
+        const double f[3] = {l[0] * E.v[0][0] + l[1] * E.v[1][0] + l[2] * E.v[2][0],
+                             l[0] * E.v[0][1] + l[1] * E.v[1][1] + l[2] * E.v[2][1],
+                             l[0] * E.v[0][2] + l[1] * E.v[1][2] + l[2] * E.v[2][2]};
+        stk_kernel(s, f, n, G, T, prG, prT);
+        const double w = rw[q] * area;
+        for (int k = 0; k < 6; ++k) o.G[k] += w * G[k];
+        for (int k = 0; k < 3; ++k) o.prG[k] += w * prG[k];
+        for (int j = 0; j < 3; ++j) {
+          const double wl = w * l[j];
+          for (int k = 0; k < 6; ++k) o.T[k][j] += wl * T[k];
+          for (int k = 0; k < 3; ++k) o.prT[k][j] += wl * prT[k];
+        }
       }
-    }
+    });
     return;
   }
   const int ng1 = gtNg1[iqud - 1], ng2 = gtNg2[iqud - 1];

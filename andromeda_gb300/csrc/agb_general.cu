@@ -53,6 +53,7 @@ struct GenArgs {
   const int* adj_ptr;
   const int* adj_p;
   const int* adj_k;
+  IntegOpt opt;
 };
 
 template <int STK>
@@ -79,7 +80,14 @@ __global__ void k_gen_elem(GenArgs a, int row0, int nrows, double* __restrict__ 
   double* out = E + ((int64_t)rl * a.nq + p) * NV;
   if constexpr (STK) {
     StkElem o;
-    stk_element(G, s, isrc, a.rl, a.rw, a.Q, a.iqud, o);
+    stk_element(G, s, isrc, a.rl, a.rw, a.Q, a.iqud, a.opt, o);
+    if (isrc && r >= a.nn) {
+      // sdIntRowQStokes adds no pressure terms of the self element (lib_Stokes.f90:1747-1760)
+      for (int k = 0; k < 3; ++k) {
+        o.prG[k] = 0.0;
+        for (int j = 0; j < 4; ++j) o.prT[k][j] = 0.0;
+      }
+    }
     int t = 0;
     for (int k = 0; k < 6; ++k) out[t++] = o.G[k];
     for (int k = 0; k < 3; ++k) out[t++] = o.prG[k];
@@ -88,7 +96,7 @@ __global__ void k_gen_elem(GenArgs a, int row0, int nrows, double* __restrict__ 
     for (int k = 0; k < 3; ++k)
       for (int j = 0; j < 4; ++j) out[t++] = o.prT[k][j];
   } else {
-    LapElem o = lap_element(G, s, isrc, a.rl, a.rw, a.Q, a.iqud);
+    LapElem o = lap_element(G, s, isrc, a.rl, a.rw, a.Q, a.iqud, a.opt);
     out[0] = o.g;
     for (int k = 0; k < 4; ++k) out[1 + k] = o.h[k];
   }
@@ -262,13 +270,15 @@ cudaError_t GeneralDev::upload(const GeneralLayout& L) {
 }
 
 cudaError_t general_integrals(const GeneralLayout& L, const GeneralDev& D, const ElemGeom* geom, const double* xyz,
-                              const RuleDev& rule, int iqud, double* T, double* G, double* err_row, cudaStream_t s) {
+                              const RuleDev& rule, int iqud, const IntegOpt& opt, double* T, double* G,
+                              double* err_row, cudaStream_t s) {
   const bool stk = (L.kind == 2);
   const int NV = stk ? NV_STK : NV_LAP;
   GenArgs a;
   a.kind = L.kind; a.nn = L.nn; a.nq = L.nq; a.nsp = L.nsp; a.Q = rule.Q; a.iqud = iqud;
   a.geom = geom; a.xyz = xyz; a.rl = rule.l; a.rw = rule.w; a.nodeList = D.nodeList; a.posOfNode = D.posOfNode;
   a.adj_ptr = D.adj_ptr; a.adj_p = D.adj_p; a.adj_k = D.adj_k;
+  a.opt = opt;
   const int64_t per_row = (int64_t)L.nq * NV * (int64_t)sizeof(double);
   int chunk = (int)std::max<int64_t>(1, std::min<int64_t>(L.nsp, (int64_t)(1u << 30) / std::max<int64_t>(per_row, 1)));
   chunk = std::min(chunk, 65535);

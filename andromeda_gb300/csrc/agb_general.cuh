@@ -54,7 +54,8 @@ struct GeneralDev {
 // (Txx,Txy,Txz,Tyy,Tyz,Tzz,prTx,prTy,prTz) and G[9][nsp][nq] (Gxx..Gzz,
 // prGx..prGz).  err_row[nsp] receives the reference's self-check residual.
 cudaError_t general_integrals(const GeneralLayout& L, const GeneralDev& D, const ElemGeom* geom, const double* xyz,
-                              const RuleDev& rule, int iqud, double* T, double* G, double* err_row, cudaStream_t s);
+                              const RuleDev& rule, int iqud, const IntegOpt& opt, double* T, double* G,
+                              double* err_row, cudaStream_t s);
 
 // Dense system (nrow x lda, row-major) and right-hand-side matrix (nrow x nb)
 // from the integral matrices (BC routing of sdSetUpSysMrhsM_CRS / formUrow /

@@ -31,7 +31,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Stokes resistance-tensor solves/s at <=1e-6 rel err: mixed/batched vs FP64 GPU"
 GOLDEN_TRUTH = os.path.join(ROOT, "tests", "golden", "c2_fp64_tensor.json")
-PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "k_av2_k_atu2_k_stokes_G_l4.md")
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "k_av3_k_atu3_l4.md")
 
 
 def parse():
@@ -301,7 +301,7 @@ def main():
     if os.path.exists(PROFILE_TRAFFIC) and args.level == 5:
         with open(PROFILE_TRAFFIC) as f:
             for line in f:
-                if line.startswith("traffic_bytes_per_launch_k_av2_c2:"):
+                if line.startswith("traffic_bytes_per_launch_k_av3_c2:"):
                     traffic = float(line.split(":")[1])
     roofline = {"bound": "hbm", "kernel": "k_av3 (LSQR A*V sweep, FP32 A streamed by TMA, 8 RHS)",
                 "achieved": a_bytes / (av_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",

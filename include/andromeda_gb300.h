@@ -95,6 +95,24 @@ int agb_set_mesh(agb_context* ctx, int nnodes, const double* xyz, int nelem, con
 int agb_set_problem(agb_context* ctx, int kind, int nwalls, const int* walls, const double* normMul, double diff,
                     const int* known, int itri, int iqud);
 
+/* Integration options of the triangle integrals (default: sing_mode 0,
+ * near_eta 0 -- the reference's assembly).  Replaces the commented-out
+ * alternative of sdIntRowU/Q and sdIntRowU/QStokes (lib_sdBem.f90:510,668;
+ * lib_Stokes.f90:1697,2030) and parTriRecur (mod_par.f90:232):
+ *   sing_mode 0: analytic self-element integrals (si_tri_lap / si_tri_stk);
+ *   sing_mode 1: recursive midpoint subdivision toward the source, rec_depth
+ *                levels (Triangle_BEMInt lib_sdBem.f90:775, Triangle_StokesInt
+ *                lib_Stokes.f90:2251; quads stay analytic); rec_depth 0..30;
+ *   near_eta > 0, near_depth 1..20: adaptive near-singular rule for the other
+ *                triangles (no reference counterpart): a (sub-)triangle whose
+ *                centroid is closer to the source than near_eta x its longest
+ *                edge is split into its four midpoint children, up to near_depth
+ *                levels, all in FP64.
+ * Non-default options send agb_assemble through the general FP64 assembly
+ * (for AGB_MIXED the routed system is then copied to FP32).  Call after
+ * agb_set_problem; it clears the assembled system. */
+int agb_set_integration(agb_context* ctx, int sing_mode, int rec_depth, double near_eta, int near_depth);
+
 /* Element geometry in global element order (normal 3*nelem, area nelem,
  * centroid 3*nelem); elements outside the subdomain are zero. */
 int agb_get_geometry(agb_context* ctx, double* normal, double* area, double* centroid);

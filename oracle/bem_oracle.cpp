@@ -372,20 +372,155 @@ static inline void bem_kernel(double sx, double sy, double sz, double fx, double
   G = 0.25 / (PI * RA);
   H = (RX * nx + RY * ny + RZ * nz) * IRA2 * G;
 }
-// Triangle_3DLapInt (lib_sdBem.f90:859-905); accumulates into out[0..3]
-static void tri_lap_regular(const TriRule& R, const double v[9], const double s[3], const double n[3],
-                            double area, double out[4]) {
+// -----------------------------------------------------------------------------
+// Sub-triangles.  A sub-triangle of an element is held as the barycentric
+// coordinates (in the element) of its three vertices, B[k][j].  A quadrature
+// point with sub-triangle barycentrics l maps to the element barycentrics
+// L_j = sum_k l_k B[k][j]; the position is sum_j L_j v_j and the linear shape
+// weights are L_j (the element's).  The midpoint split of
+// Triangle_BEMInt / Triangle_StokesInt (lib_sdBem.f90:775-852,
+// lib_Stokes.f90:2251-2336): with the edge midpoints 4 = (1+2)/2, 5 = (2+3)/2,
+// 6 = (1+3)/2, child 0 = (1,4,6), 1 = (4,2,5), 2 = (6,5,3), 3 = (4,5,6).
+// Children have a quarter of the parent's area and half its edges.
+// -----------------------------------------------------------------------------
+struct Bary { double b[3][3]; };
+static Bary bary_identity() {
+  Bary B;
+  for (int k = 0; k < 3; ++k)
+    for (int j = 0; j < 3; ++j) B.b[k][j] = (k == j) ? 1.0 : 0.0;
+  return B;
+}
+static Bary sub_child(const Bary& P, int d) {
+  double m4[3], m5[3], m6[3];
+  for (int j = 0; j < 3; ++j) {
+    m4[j] = 0.5 * (P.b[0][j] + P.b[1][j]);
+    m5[j] = 0.5 * (P.b[2][j] + P.b[1][j]);
+    m6[j] = 0.5 * (P.b[0][j] + P.b[2][j]);
+  }
+  Bary C;
+  for (int j = 0; j < 3; ++j) {
+    switch (d) {
+      case 0: C.b[0][j] = P.b[0][j]; C.b[1][j] = m4[j]; C.b[2][j] = m6[j]; break;
+      case 1: C.b[0][j] = m4[j]; C.b[1][j] = P.b[1][j]; C.b[2][j] = m5[j]; break;
+      case 2: C.b[0][j] = m6[j]; C.b[1][j] = m5[j]; C.b[2][j] = P.b[2][j]; break;
+      default: C.b[0][j] = m4[j]; C.b[1][j] = m5[j]; C.b[2][j] = m6[j]; break;
+    }
+  }
+  return C;
+}
+
+// Integration options of the triangle integrals.
+//   sing 0: analytic self-element integrals (the reference's assembly);
+//   sing 1: recursive midpoint subdivision toward the source, rdepth levels
+//           (Triangle_BEMInt / Triangle_StokesInt with IntRecDepth = parTriRecur,
+//           the alternative left commented out at lib_sdBem.f90:510,668 and
+//           lib_Stokes.f90:1697,2030; live in lib_domain.f90:286).  Quads keep
+//           the analytic scheme.
+//   near_eta > 0: adaptive near-singular rule for non-singular triangles (no
+//           reference counterpart): a (sub-)triangle whose centroid lies closer
+//           to the source than near_eta x its longest edge is split into its four
+//           children, up to near_depth levels; leaves take the regular rule.
+struct IntegOpt {
+  int sing = 0;
+  int rdepth = 20;
+  double near_eta = 0.0;
+  int near_depth = 0;
+};
+
+// Visits the sub-triangles of element v for source s in the order of the
+// reference's recursion (children 0..3, depth first) and calls
+// rule(B, area_of_sub, skip_centroid).  skip_centroid is set for the last piece
+// of a centroid-source recursion: the source is that piece's centroid, and a
+// rule with a centroid point (ITRI 1, 2, 4) would divide by r = 0 there (the
+// reference's Triangle_BEMInt does); that one point is left out.
+template <class F>
+static void tri_walk(const IntegOpt& o, const double v[9], const double s[3], double area, int isrc, F&& rule) {
+  if (isrc) {
+    // Triangle_BEMInt: only the child holding the source (vertex isrc, or the
+    // centre child for the centroid) recurses; the final piece is integrated
+    // with the regular rule.
+    const int ks = isrc - 1;
+    Bary B = bary_identity();
+    double a = area;
+    for (int lev = 0; lev < o.rdepth; ++lev) {
+      for (int d = 0; d < ks; ++d) rule(sub_child(B, d), 0.25 * a, false);
+      B = sub_child(B, ks);
+      a *= 0.25;
+    }
+    rule(B, a, isrc == 4);
+    for (int lev = o.rdepth - 1; lev >= 0; --lev) {
+      Bary Bl = bary_identity();
+      double al = area;
+      for (int t = 0; t < lev; ++t) { Bl = sub_child(Bl, ks); al *= 0.25; }
+      for (int d = ks + 1; d < 4; ++d) rule(sub_child(Bl, d), 0.25 * al, false);
+    }
+    return;
+  }
+  if (o.near_eta > 0.0 && o.near_depth > 0) {
+    auto edge = [&](int p, int q) {
+      const double dx = v[3 * p] - v[3 * q], dy = v[3 * p + 1] - v[3 * q + 1], dz = v[3 * p + 2] - v[3 * q + 2];
+      return std::sqrt(dx * dx + dy * dy + dz * dz);
+    };
+    const double diam = std::max(edge(0, 1), std::max(edge(1, 2), edge(2, 0)));
+    // depth-first stack of sub-triangles: 2 bits per level (child index) + the level in bits 58..63
+    uint64_t stack[64];
+    int top = 0;
+    stack[top++] = 0;
+    while (top > 0) {
+      const uint64_t e = stack[--top];
+      const int lev = (int)(e >> 58);
+      Bary B = bary_identity();
+      double a = area, h = diam;
+      for (int t = 0; t < lev; ++t) {
+        B = sub_child(B, (int)((e >> (2 * t)) & 3u));
+        a *= 0.25;
+        h *= 0.5;
+      }
+      double c[3] = {0.0, 0.0, 0.0};
+      for (int j = 0; j < 3; ++j) {
+        const double Lc = (B.b[0][j] + B.b[1][j] + B.b[2][j]) / 3.0;
+        for (int i = 0; i < 3; ++i) c[i] += Lc * v[3 * j + i];
+      }
+      const double d = std::sqrt((s[0] - c[0]) * (s[0] - c[0]) + (s[1] - c[1]) * (s[1] - c[1]) +
+                                 (s[2] - c[2]) * (s[2] - c[2]));
+      if (lev < o.near_depth && d < o.near_eta * h) {
+        for (int ch = 3; ch >= 0; --ch) stack[top++] = (e & ((1ull << 58) - 1)) | ((uint64_t)ch << (2 * lev)) |
+                                                       ((uint64_t)(lev + 1) << 58);
+      } else {
+        rule(B, a, false);
+      }
+    }
+    return;
+  }
+  rule(bary_identity(), area, false);
+}
+// the centroid point of a symmetric rule: l1 = l2 = l3
+static inline bool is_centroid_point(double l1, double l2, double l3) {
+  return std::fabs(l1 - l2) < 1e-12 && std::fabs(l2 - l3) < 1e-12;
+}
+
+// Triangle_3DLapInt (lib_sdBem.f90:859-905) over the sub-triangle B;
+// accumulates into out[0..3] (G, H at the three element nodes)
+static void tri_lap_sub(const TriRule& R, const double v[9], const Bary& B, const double s[3], const double n[3],
+                        double area, double out[4], bool skip_centroid = false) {
   for (int i = 0; i < R.n; ++i) {
-    double x = R.l1[i] * v[0] + R.l2[i] * v[3] + R.l3[i] * v[6];
-    double y = R.l1[i] * v[1] + R.l2[i] * v[4] + R.l3[i] * v[7];
-    double z = R.l1[i] * v[2] + R.l2[i] * v[5] + R.l3[i] * v[8];
+    if (skip_centroid && is_centroid_point(R.l1[i], R.l2[i], R.l3[i])) continue;
+    double L[3];
+    for (int j = 0; j < 3; ++j) L[j] = R.l1[i] * B.b[0][j] + R.l2[i] * B.b[1][j] + R.l3[i] * B.b[2][j];
+    double x = L[0] * v[0] + L[1] * v[3] + L[2] * v[6];
+    double y = L[0] * v[1] + L[1] * v[4] + L[2] * v[7];
+    double z = L[0] * v[2] + L[1] * v[5] + L[2] * v[8];
     double G, H;
     bem_kernel(s[0], s[1], s[2], x, y, z, n[0], n[1], n[2], G, H);
     out[0] += R.w[i] * G * area;
-    out[1] += R.w[i] * H * area * R.l1[i];
-    out[2] += R.w[i] * H * area * R.l2[i];
-    out[3] += R.w[i] * H * area * R.l3[i];
+    out[1] += R.w[i] * H * area * L[0];
+    out[2] += R.w[i] * H * area * L[1];
+    out[3] += R.w[i] * H * area * L[2];
   }
+}
+static void tri_lap_regular(const TriRule& R, const double v[9], const double s[3], const double n[3],
+                            double area, double out[4]) {
+  tri_lap_sub(R, v, bary_identity(), s, n, area, out);
 }
 // Quad_BEMIntNum (lib_intAna.f90:219-344); out[0]=G, out[1..4]=H at nodes
 static void quad_lap_regular(int iqud, const double q[12], const double s[3], double multi, double out[5]) {
@@ -464,17 +599,20 @@ struct StkElem {
 };
 static const int kSym[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
 
-// Triangle_3DStokesInt (lib_Stokes.f90:2341-2446)
-static void tri_stk_regular(const TriRule& R, const double v[9], const double s[3], const double n[3], double area,
-                            StkElem& E) {
+// Triangle_3DStokesInt (lib_Stokes.f90:2341-2446) over the sub-triangle B
+static void tri_stk_sub(const TriRule& R, const double v[9], const Bary& B, const double s[3], const double n[3],
+                        double area, StkElem& E, bool skip_centroid = false) {
   double G[3][3], T[3][3], prG[3], prT[3], f[3];
   for (int i = 0; i < R.n; ++i) {
-    f[0] = R.l1[i] * v[0] + R.l2[i] * v[3] + R.l3[i] * v[6];
-    f[1] = R.l1[i] * v[1] + R.l2[i] * v[4] + R.l3[i] * v[7];
-    f[2] = R.l1[i] * v[2] + R.l2[i] * v[5] + R.l3[i] * v[8];
+    if (skip_centroid && is_centroid_point(R.l1[i], R.l2[i], R.l3[i])) continue;
+    double l[3];
+    for (int j = 0; j < 3; ++j) l[j] = R.l1[i] * B.b[0][j] + R.l2[i] * B.b[1][j] + R.l3[i] * B.b[2][j];
+    f[0] = l[0] * v[0] + l[1] * v[3] + l[2] * v[6];
+    f[1] = l[0] * v[1] + l[1] * v[4] + l[2] * v[7];
+    f[2] = l[0] * v[2] + l[1] * v[5] + l[2] * v[8];
     stokes_kernel(s, f, n, G, T, prG, prT);
     double w = R.w[i] * area;
-    double wl[3] = {w * R.l1[i], w * R.l2[i], w * R.l3[i]};
+    double wl[3] = {w * l[0], w * l[1], w * l[2]};
     for (int k = 0; k < 6; ++k) E.G[k] += w * G[kSym[k][0]][kSym[k][1]];
     for (int k = 0; k < 3; ++k) E.prG[k] += w * prG[k];
     for (int k = 0; k < 6; ++k)
@@ -482,6 +620,10 @@ static void tri_stk_regular(const TriRule& R, const double v[9], const double s[
     for (int k = 0; k < 3; ++k)
       for (int j = 0; j < 3; ++j) E.prT[k][j] += wl[j] * prT[k];
   }
+}
+static void tri_stk_regular(const TriRule& R, const double v[9], const double s[3], const double n[3], double area,
+                            StkElem& E) {
+  tri_stk_sub(R, v, bary_identity(), s, n, area, E);
 }
 // Quad_StokesIntNum (lib_Stokes.f90:3754-3940): fixed 3x3 subcells
 static void quad_stk_regular(int iqud, const double q[12], const double s[3], double multi, StkElem& E) {
@@ -566,6 +708,7 @@ struct Problem {
   // quadrature
   TriRule tri;
   int iqud = 4;
+  IntegOpt opt;
   // integral matrices
   std::vector<double> H, G;   // Laplace: nsp x sd_nnodes / nsp x sd_nqnodes, column-major
   std::vector<double> M[18];  // Stokes: Txx..Tzz, prTx..prTz (nsp x nn), Gxx..Gzz, prGx..prGz (nsp x nq)
@@ -687,9 +830,10 @@ static void lap_row_u(const Problem& P, int irow, double* rowH, double* rowG, do
       element_vertices(P, ie, v);
       if (P.type[ie] == 2) {
         double n[3] = {mm * P.normal[3 * ie], mm * P.normal[3 * ie + 1], mm * P.normal[3 * ie + 2]};
-        if (isrc == 0) {
+        if (isrc == 0 || P.opt.sing == 1) {
           double out[4] = {0, 0, 0, 0};
-          tri_lap_regular(P.tri, v, s, n, P.area[ie], out);
+          tri_walk(P.opt, v, s, P.area[ie], isrc,
+                   [&](const Bary& B, double a, bool sk) { tri_lap_sub(P.tri, v, B, s, n, a, out, sk); });
           integ = out[0]; inteH[0] = out[1]; inteH[1] = out[2]; inteH[2] = out[3];
         } else {
           integ = si_tri_lap(v, P.area[ie], isrc);
@@ -734,9 +878,10 @@ static void lap_row_q(const Problem& P, int irow, double* rowH, double* rowG, do
       element_vertices(P, ie, v);
       if (P.type[ie] == 2) {
         double n[3] = {mm * P.normal[3 * ie], mm * P.normal[3 * ie + 1], mm * P.normal[3 * ie + 2]};
-        if (isrc == 0) {
+        if (isrc == 0 || P.opt.sing == 1) {
           double out[4] = {0, 0, 0, 0};
-          tri_lap_regular(P.tri, v, s, n, P.area[ie], out);
+          tri_walk(P.opt, v, s, P.area[ie], isrc,
+                   [&](const Bary& B, double a, bool sk) { tri_lap_sub(P.tri, v, B, s, n, a, out, sk); });
           integ = out[0]; inteH[0] = out[1]; inteH[1] = out[2]; inteH[2] = out[3];
         } else {
           integ = si_tri_lap(v, P.area[ie], isrc);
@@ -800,9 +945,9 @@ static void stk_element(const Problem& P, int ie, const double s[3], int isrc, d
   element_vertices(P, ie, v);
   E.zero();
   if (P.type[ie] == 2) {
-    if (isrc == 0) {
+    if (isrc == 0 || P.opt.sing == 1) {
       double n[3] = {mm * P.normal[3 * ie], mm * P.normal[3 * ie + 1], mm * P.normal[3 * ie + 2]};
-      tri_stk_regular(P.tri, v, s, n, P.area[ie], E);
+      tri_walk(P.opt, v, s, P.area[ie], isrc, [&](const Bary& B, double a, bool sk) { tri_stk_sub(P.tri, v, B, s, n, a, E, sk); });
     } else {
       si_tri_stk(v, P.area[ie], isrc, E.G);  // T, prT, prG stay zero (lib_intAna.f90:136-148)
     }
@@ -1361,6 +1506,32 @@ void orc_tri_stk_regular(int itri, const double v[9], const double s[3], const d
   for (int k = 0; k < 3; ++k) for (int j = 0; j < 3; ++j) out[p++] = E.prT[k][j];
 }
 
+// Triangle element integrals under the integration options (sing, rdepth,
+// near_eta, near_depth of IntegOpt): Laplace out = {G, H1, H2, H3}; Stokes out =
+// G[6], prG[3], T[6][3], prT[3][3].  isrc 0 (regular), 1..3 (vertex), 4 (centroid).
+void orc_tri_lap_opt(int itri, const double v[9], const double s[3], const double n[3], int isrc, int sing, int rdepth,
+                     double near_eta, int near_depth, double out[4]) {
+  TriRule R = wx_rule(itri);
+  IntegOpt o;
+  o.sing = sing; o.rdepth = rdepth; o.near_eta = near_eta; o.near_depth = near_depth;
+  for (int k = 0; k < 4; ++k) out[k] = 0.0;
+  tri_walk(o, v, s, orc_tri_area(v), isrc, [&](const Bary& B, double a, bool sk) { tri_lap_sub(R, v, B, s, n, a, out, sk); });
+}
+void orc_tri_stk_opt(int itri, const double v[9], const double s[3], const double n[3], int isrc, int sing, int rdepth,
+                     double near_eta, int near_depth, double out[36]) {
+  TriRule R = wx_rule(itri);
+  IntegOpt o;
+  o.sing = sing; o.rdepth = rdepth; o.near_eta = near_eta; o.near_depth = near_depth;
+  StkElem E;
+  E.zero();
+  tri_walk(o, v, s, orc_tri_area(v), isrc, [&](const Bary& B, double a, bool sk) { tri_stk_sub(R, v, B, s, n, a, E, sk); });
+  int p = 0;
+  for (int k = 0; k < 6; ++k) out[p++] = E.G[k];
+  for (int k = 0; k < 3; ++k) out[p++] = E.prG[k];
+  for (int k = 0; k < 6; ++k) for (int j = 0; j < 3; ++j) out[p++] = E.T[k][j];
+  for (int k = 0; k < 3; ++k) for (int j = 0; j < 3; ++j) out[p++] = E.prT[k][j];
+}
+
 // ---- problem object ----------------------------------------------------------
 // kind 1 = Laplace (1 equation), 2 = Stokes (3 equations).  known[en*nwalls+k]
 // is the BC type (1 function, 2 flux, 3 contact) of equation en on wall walls[k].
@@ -1391,6 +1562,13 @@ void* orc_problem_create(int kind, int nnodes, const double* xyz, int nelem, con
   return P;
 }
 void orc_problem_destroy(void* h) { delete (Problem*)h; }
+// Integration options (IntegOpt) for the next orc_form_integrals.
+void orc_problem_set_integration(void* h, int sing, int rdepth, double near_eta, int near_depth) {
+  Problem* P = (Problem*)h;
+  P->opt.sing = sing; P->opt.rdepth = rdepth; P->opt.near_eta = near_eta; P->opt.near_depth = near_depth;
+  P->H.clear(); P->G.clear();
+  for (auto& m : P->M) m.clear();
+}
 
 // sizes: [nsp, sd_nnodes, sd_nqnodes, neq_rows, nx, nb] of the (big) system
 void orc_problem_sizes(void* h, int out[6]) {

@@ -51,6 +51,9 @@ def lib():
                                          C.c_int, C.c_int]
         L.orc_problem_create.restype = C.c_void_p
         L.orc_problem_destroy.argtypes = [C.c_void_p]
+        L.orc_problem_set_integration.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int]
+        L.orc_tri_lap_opt.argtypes = [C.c_int, dp, dp, dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, dp]
+        L.orc_tri_stk_opt.argtypes = [C.c_int, dp, dp, dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, dp]
         L.orc_problem_sizes.argtypes = [C.c_void_p, ip]
         L.orc_geometry.argtypes = [C.c_void_p, dp, dp, dp]
         L.orc_lists.argtypes = [C.c_void_p, ip, ip]
@@ -125,6 +128,22 @@ def tri_stk_regular(itri, v, s, n):
     return out
 
 
+def tri_lap_opt(itri, v, s, n, isrc=0, sing=0, rdepth=20, near_eta=0.0, near_depth=0):
+    """Triangle Laplace integrals {G, H1, H2, H3} under the integration options."""
+    out = np.zeros(4)
+    lib().orc_tri_lap_opt(itri, np.ascontiguousarray(v, float).ravel(), np.ascontiguousarray(s, float),
+                          np.ascontiguousarray(n, float), isrc, sing, rdepth, near_eta, near_depth, out)
+    return out
+
+
+def tri_stk_opt(itri, v, s, n, isrc=0, sing=0, rdepth=20, near_eta=0.0, near_depth=0):
+    """Triangle Stokes integrals G[6], prG[3], T[6][3], prT[3][3] under the integration options."""
+    out = np.zeros(36)
+    lib().orc_tri_stk_opt(itri, np.ascontiguousarray(v, float).ravel(), np.ascontiguousarray(s, float),
+                          np.ascontiguousarray(n, float), isrc, sing, rdepth, near_eta, near_depth, out)
+    return out
+
+
 class Problem:
     """Mesh + one subdomain + BCs, mirroring the reference's module state."""
 
@@ -172,6 +191,10 @@ class Problem:
         ql = np.zeros(self.sd_nqnodes, np.int32)
         lib().orc_lists(self.h, nl, ql)
         return nl, ql
+
+    def set_integration(self, sing=0, rdepth=20, near_eta=0.0, near_depth=0):
+        """Integration options of the triangle integrals (IntegOpt of the oracle)."""
+        lib().orc_problem_set_integration(self.h, int(sing), int(rdepth), float(near_eta), int(near_depth))
 
     def form_integrals(self):
         e = np.zeros(2)

@@ -195,3 +195,71 @@ def test_golden_values_frozen(orc):
         assert np.allclose(orc.si_tri_stk(v, isrc), g["si_tri_stk"][isrc - 1], rtol=1e-13, atol=0)
     for itri in range(1, 6):
         assert np.allclose(orc.triangle_test(itri), g["triangle_test"][itri - 1], rtol=1e-13, atol=0)
+
+
+# ---- integration options: recursive self-element scheme, adaptive near-singular rule ----
+_TRI = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.3, 0.9, 0.0]])
+
+
+@pytest.mark.parametrize("isrc", [1, 2, 3, 4])
+def test_recursive_singular_converges_to_analytic(orc, isrc):
+    """Triangle_BEMInt's midpoint recursion toward the source (lib_sdBem.f90:775)
+    converges to the Ren-Chan closed form: the error, set by the last piece
+    taken with the regular rule, halves with every level."""
+    v = _TRI
+    s = v[isrc - 1] if isrc < 4 else v.mean(axis=0)
+    n = np.array([0.0, 0.0, 1.0])
+    ana = orc.si_tri_lap(v, isrc)
+    errs = [abs(orc.tri_lap_opt(5, v, s, n, isrc, 1, d)[0] - ana) / ana for d in (6, 10, 14)]
+    assert errs[2] < 5e-6
+    assert errs[0] > 10 * errs[1] > 100 * errs[2]
+    # Stokes: the six Stokeslet components against si_tri_stk
+    g_ana = orc.si_tri_stk(v, isrc)
+    g_rec = orc.tri_stk_opt(5, v, s, n, isrc, 1, 16)[:6]
+    assert np.max(np.abs(g_rec - g_ana)) / np.max(np.abs(g_ana)) < 5e-6
+    # rules with a centroid point (ITRI 1, 2, 4): the last piece of a centroid
+    # recursion leaves that point out instead of dividing by r = 0
+    for itri in (1, 2, 4):
+        g = orc.tri_lap_opt(itri, v, s, n, isrc, 1, 14)[0]
+        assert np.isfinite(g) and abs(g - ana) / ana < 5e-3
+
+
+def _dblquad_tri(f, v):
+    """High-order reference: adaptive Gauss-Kronrod over the triangle (scipy)."""
+    from scipy import integrate
+    e1, e2 = v[1] - v[0], v[2] - v[0]
+    jac = np.linalg.norm(np.cross(e1, e2))
+    val, _ = integrate.dblquad(lambda b, a: f(v[0] + a * e1 + b * e2, a, b), 0.0, 1.0, 0.0, lambda a: 1.0 - a,
+                               epsabs=1e-14, epsrel=1e-13)
+    return val * jac
+
+
+@pytest.mark.parametrize("height", [0.05, 0.01])
+def test_near_singular_rule_against_high_order_reference(orc, height):
+    """The adaptive near-singular rule (no reference counterpart) against an
+    independent adaptive Gauss-Kronrod integration of G and the nodal H."""
+    pytest.importorskip("scipy")
+    v = _TRI
+    n = np.array([0.0, 0.0, 1.0])
+    s = np.array([0.5, 0.03, height])
+
+    def G(x, a, b):
+        return 0.25 / np.pi / np.linalg.norm(s - x)
+
+    def H(k):
+        def f(x, a, b):
+            r = s - x
+            ra = np.linalg.norm(r)
+            lam = (1.0 - a - b, a, b)[k]
+            return (r @ n) / ra ** 2 * 0.25 / np.pi / ra * lam
+        return f
+
+    ref = np.array([_dblquad_tri(G, v)] + [_dblquad_tri(H(k), v) for k in range(3)])
+    plain = orc.tri_lap_opt(5, v, s, n)
+    near = orc.tri_lap_opt(5, v, s, n, 0, 0, 0, 1.5, 12)
+    scale = np.max(np.abs(ref))
+    assert np.max(np.abs(plain - ref)) / scale > 1e-4      # the regular rule is off
+    assert np.max(np.abs(near - ref)) / scale < 1e-9       # the adaptive rule is not
+    # far from the element the rule changes nothing
+    far = np.array([0.4, 0.3, 3.0])
+    assert np.array_equal(orc.tri_lap_opt(5, v, far, n), orc.tri_lap_opt(5, v, far, n, 0, 0, 0, 1.5, 12))
