@@ -45,6 +45,7 @@ SIGNATURES = {
     "agb_integral_matrices": ([vp, vp, vp, vp], I),
     "agb_layout_sizes": ([vp, ip], I),
     "agb_solve_fields": ([vp, I, dp, vp, dp, dp, I, D, I, ip, ip], I),
+    "agb_batch_resistance": ([vp, I, ip, dp, ip, ip, ip, ip, I, I, I, I, D, D, I, dp, ip, ip, dp], I),
 }
 
 _lib = None

@@ -234,6 +234,44 @@ class Context:
                         "device_ms": t[5], "istop": istop.tolist()}
 
 
+def batch_resistance(meshes, particle_wall=1, outer_wall=2, itri=5, maxit=0, eps=1e-7, mem_gb=0.0, autotune=True,
+                     device=0, ctx=None):
+    """Mixed-precision resistance tensors of many bodies in one batched call.
+
+    ``meshes``: list of particle-in-container triangle meshes (the dict layout
+    of :mod:`andromeda_gb300.mesh`).  Returns (R[nb,6,6], nit[nb,6],
+    istop[nb,6], stats) with R[i, r] = (F, T) on particle i for rigid motion r
+    of its container.  ``ctx``: a :class:`Context` to run on (its per-body
+    contexts are kept for later calls); a new one on ``device`` otherwise.
+    """
+    own = ctx is None
+    C_ = Context(device) if own else ctx
+    try:
+        nb = len(meshes)
+        node_off = np.zeros(nb + 1, np.int32)
+        elem_off = np.zeros(nb + 1, np.int32)
+        for i, m in enumerate(meshes):
+            node_off[i + 1] = node_off[i] + len(m["xyz"])
+            elem_off[i + 1] = elem_off[i] + len(m["etype"])
+        xyz = np.ascontiguousarray(np.concatenate([m["xyz"] for m in meshes]), dtype=np.float64).ravel()
+        et = np.ascontiguousarray(np.concatenate([m["etype"] for m in meshes]), dtype=np.int32)
+        con = np.ascontiguousarray(np.concatenate([m["con"] for m in meshes]), dtype=np.int32).ravel()
+        bc = np.ascontiguousarray(np.concatenate([m["bcid"] for m in meshes]), dtype=np.int32)
+        R = np.zeros((nb, 6, 6))
+        nit = np.zeros((nb, 6), np.int32)
+        istop = np.zeros((nb, 6), np.int32)
+        st = np.zeros(16)
+        C_._ck(C_._L.agb_batch_resistance(C_.h, nb, node_off, xyz, elem_off, et, con, bc, int(particle_wall),
+                                          int(outer_wall), int(itri), int(maxit), float(eps), float(mem_gb),
+                                          int(bool(autotune)), R.reshape(-1), nit.reshape(-1), istop.reshape(-1), st))
+        keys = ["assemble_ms", "solve_ms", "total_ms", "waves", "av_ms", "atu_ms", "av_launches", "atu_launches",
+                "av_bytes", "launches", "av_rows", "atu_rs", "atu_rows", "iterations", "device_ms", "ft_ms"]
+        return R, nit, istop, dict(zip(keys, st.tolist()))
+    finally:
+        if own:
+            C_.close()
+
+
 def dirichlet_known(kind, nwalls):
     neq = 3 if kind == STOKES else 1
     return np.full((neq, nwalls), BC_FUNCTION, dtype=np.int32)

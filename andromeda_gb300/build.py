@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libandromeda_gb300.so")
-SOURCES = ["agb_api.cu", "agb_assembly.cu", "agb_lsqr.cu", "agb_noalloc.cu", "agb_general.cu"]
+SOURCES = ["agb_api.cu", "agb_assembly.cu", "agb_lsqr.cu", "agb_noalloc.cu", "agb_general.cu", "agb_batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

@@ -4,6 +4,7 @@
 #include "agb_assembly.cuh"
 #include "agb_lsqr.cuh"
 #include "agb_general.cuh"
+#include "agb_batch.cuh"
 #include "quad_tables.h"
 
 #include <chrono>
@@ -31,6 +32,7 @@ struct agb_context {
   // problem
   int kind = 0, neq = 0;
   IntegOpt iopt;  // triangle integration options (agb_set_integration)
+  std::vector<agb_context*> pool;  // per-body contexts of agb_batch_resistance (reused)
   std::vector<int> walls;
   std::vector<double> normMul;
   double diff = 1.0;
@@ -176,6 +178,7 @@ void free_problem(agb_context* c) {
   dfree(c->d_wall);
   dfree(c->d_normMul);
   dfree(c->d_geom);
+  dfree(c->d_rowact);  // sized by the element count of the problem
   dfree(c->rule.l);
   dfree(c->rule.w);
   c->gd.release();
@@ -492,6 +495,8 @@ int agb_create(agb_context** out, int device) {
 
 int agb_destroy(agb_context* c) {
   if (!c) return AGB_OK;
+  for (agb_context* p : c->pool) agb_destroy(p);
+  c->pool.clear();
   cudaSetDevice(c->device);
   free_problem(c);
   dfree(c->d_xyz);
@@ -814,6 +819,42 @@ int agb_force_torque(agb_context* c, int nrhs, const double* x, int wall, double
   return AGB_OK;
 }
 
+// Right-hand sides of the six rigid motions of the container (e_x, e_y, e_z
+// translations, then e_a x r rotations), particle at rest: the outer-wall
+// velocities of StokesInlet3sidesForceCRS / ...TorqueOmegaCRS
+// (lib_particle.f90:341,176), into c->d_rhs [6][m].
+static int resistance_rhs(agb_context* c, int oidx) {
+  int rc;
+  const int k = 6;
+  std::vector<double> u((size_t)k * 3 * c->nnodes, 0.0);
+  std::vector<char> onOuter(c->nnodes, 0);
+  for (int p = 0; p < c->ne; ++p)
+    if (c->wallIdx[p] == oidx) {
+      const int e = c->elemList[p];
+      const int nno = (c->etype[e] == AGB_TRI) ? 3 : 4;
+      for (int kk = 0; kk < nno; ++kk) onOuter[c->con[4 * e + kk]] = 1;
+    }
+  for (int i = 0; i < c->nnodes; ++i) {
+    if (!onOuter[i]) continue;
+    const double* x = &c->xyz[3 * i];
+    for (int a = 0; a < 3; ++a) u[((size_t)a * 3 + a) * c->nnodes + i] = 1.0;
+    // e_a x r
+    const double w[3][3] = {{0, -x[2], x[1]}, {x[2], 0, -x[0]}, {-x[1], x[0], 0}};
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) u[((size_t)(3 + a) * 3 + b) * c->nnodes + i] = w[a][b];
+  }
+  if (c->general) {
+    std::vector<double> b;
+    gather_fields(c, k, u.data(), nullptr, b, nullptr);
+    if ((rc = general_rhs(c, k, b))) return rc;
+  } else {
+    int na = 0;
+    if ((rc = stage_u(c, k, u.data(), &na))) return rc;
+    if ((rc = device_rhs(c, k, na))) return rc;
+  }
+  return AGB_OK;
+}
+
 int agb_resistance_tensor(agb_context* c, int precision, int particle_wall, int outer_wall, int maxit, double eps,
                           int refine, double* R, int* nit, int* istop, double* times_ms) {
   int rc = check_ctx(c, true);
@@ -837,33 +878,8 @@ int agb_resistance_tensor(agb_context* c, int precision, int particle_wall, int 
   auto t0 = clk::now();
   if ((rc = agb_assemble(c, precision))) return rc;
   auto t1 = clk::now();
-  // six rigid motions of the container, particle at rest
   const int k = 6;
-  std::vector<double> u((size_t)k * 3 * c->nnodes, 0.0);
-  std::vector<char> onOuter(c->nnodes, 0);
-  for (int p = 0; p < c->ne; ++p)
-    if (c->wallIdx[p] == oidx) {
-      const int e = c->elemList[p];
-      for (int kk = 0; kk < 3; ++kk) onOuter[c->con[4 * e + kk]] = 1;
-    }
-  for (int i = 0; i < c->nnodes; ++i) {
-    if (!onOuter[i]) continue;
-    const double* x = &c->xyz[3 * i];
-    for (int a = 0; a < 3; ++a) u[((size_t)a * 3 + a) * c->nnodes + i] = 1.0;
-    // e_a x r
-    const double w[3][3] = {{0, -x[2], x[1]}, {x[2], 0, -x[0]}, {-x[1], x[0], 0}};
-    for (int a = 0; a < 3; ++a)
-      for (int b = 0; b < 3; ++b) u[((size_t)(3 + a) * 3 + b) * c->nnodes + i] = w[a][b];
-  }
-  if (c->general) {
-    std::vector<double> b;
-    gather_fields(c, k, u.data(), nullptr, b, nullptr);
-    if ((rc = general_rhs(c, k, b))) return rc;
-  } else {
-    int na = 0;
-    if ((rc = stage_u(c, k, u.data(), &na))) return rc;
-    if ((rc = device_rhs(c, k, na))) return rc;
-  }
+  if ((rc = resistance_rhs(c, oidx))) return rc;
   CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
   auto t2 = clk::now();
   CUDA_OR_FAIL(c, ensure(c->d_x, c->cap_x, (size_t)k * c->n));
@@ -1042,6 +1058,145 @@ int agb_solve_fields(agb_context* c, int nrhs, const double* u_in, const double*
           q_out[((size_t)r * L.neq + en) * c->nelem + c->elemList[p]] = x[(size_t)r * L.nx + L.elem_xcol[t]];
       }
     }
+  return AGB_OK;
+}
+
+
+int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const double* xyz, const int* elem_off,
+                         const int* etype, const int* con, const int* bcid, int particle_wall, int outer_wall,
+                         int itri, int maxit, double eps, double mem_gb, int autotune, double* R, int* nit,
+                         int* istop, double* stats) {
+  if (!c) return AGB_ERR_ARG;
+  if (nbodies < 1 || !node_off || !xyz || !elem_off || !etype || !con || !bcid || !R)
+    return fail(c, AGB_ERR_ARG, "agb_batch_resistance: missing arrays");
+  if (itri < 1 || itri > 5 || maxit < 0 || !(eps >= 0.0) || !(mem_gb >= 0.0))
+    return fail(c, AGB_ERR_ARG, "agb_batch_resistance: bad parameters");
+  for (int i = 0; i < nbodies; ++i)
+    if (node_off[i + 1] <= node_off[i] || elem_off[i + 1] <= elem_off[i])
+      return fail(c, AGB_ERR_ARG, "agb_batch_resistance: empty body " + std::to_string(i));
+  cudaSetDevice(c->device);
+  using clk = std::chrono::steady_clock;
+  auto ms = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
+  const auto t_start = clk::now();
+  cudaEvent_t d0 = nullptr, d1 = nullptr;
+  CUDA_OR_FAIL(c, cudaEventCreate(&d0));
+  CUDA_OR_FAIL(c, cudaEventCreate(&d1));
+  CUDA_OR_FAIL(c, cudaEventRecord(d0, c->stream));
+  // device bytes of one body: FP32 matrix + assembly/solver work buffers
+  auto body_bytes = [&](int i) {
+    const double ne = (double)(elem_off[i + 1] - elem_off[i]);
+    const double n = 3.0 * ne, lda = std::ceil(n / 32.0) * 32.0;
+    // A + solver vectors and up to 64 row-group partials of the per-body column
+    // scaling + quadrature points + allocation granularity
+    return n * lda * 4.0 + lda * 64.0 * 80.0 + ne * 126.0 * 16.0 * 1.1 + 8.0e6;
+  };
+  double budget = mem_gb * 1e9;
+  if (budget <= 0.0) {
+    size_t fr = 0, tot = 0;
+    CUDA_OR_FAIL(c, cudaMemGetInfo(&fr, &tot));
+    budget = 0.7 * (double)fr;
+  }
+  // waves: largest bodies first, packed greedily under the budget
+  std::vector<int> order(nbodies);
+  for (int i = 0; i < nbodies; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return body_bytes(a) > body_bytes(b); });
+  std::vector<std::vector<int>> waves;
+  double used = 0.0;
+  for (int i : order) {
+    const double bb = body_bytes(i);
+    if (waves.empty() || (used + bb > budget && !waves.back().empty())) {
+      waves.emplace_back();
+      used = 0.0;
+    }
+    waves.back().push_back(i);
+    used += bb;
+  }
+  size_t maxwave = 0;
+  for (auto& w : waves) maxwave = std::max(maxwave, w.size());
+  while (c->pool.size() < maxwave) {
+    agb_context* p = nullptr;
+    const int rc = agb_create(&p, c->device);
+    if (rc) return fail(c, rc, std::string("agb_batch_resistance: ") + agb_last_error(nullptr));
+    c->pool.push_back(p);
+  }
+  BatchTune tune;
+  BatchStats bst;
+  bool tuned = false;
+  double t_asm = 0.0, t_solve = 0.0, t_ft = 0.0;
+  const int walls[2] = {particle_wall, outer_wall};
+  const int known[6] = {AGB_BC_FUNCTION, AGB_BC_FUNCTION, AGB_BC_FUNCTION, AGB_BC_FUNCTION, AGB_BC_FUNCTION,
+                        AGB_BC_FUNCTION};
+  for (const auto& w : waves) {
+    const auto ta = clk::now();
+    std::vector<BatchBody> bodies(w.size());
+    for (size_t t = 0; t < w.size(); ++t) {
+      const int i = w[t];
+      agb_context* p = c->pool[t];
+      const int nn = node_off[i + 1] - node_off[i], ne = elem_off[i + 1] - elem_off[i];
+      int rc = agb_set_mesh(p, nn, xyz + 3 * (size_t)node_off[i], ne, etype + elem_off[i], con + 4 * (size_t)elem_off[i],
+                            bcid + elem_off[i]);
+      if (!rc) rc = agb_set_problem(p, AGB_STOKES, 2, walls, nullptr, 1.0, known, itri, 4);
+      if (!rc && (p->all_tri == false)) rc = fail(p, AGB_ERR_UNSUPPORTED, "batched bodies must be triangle meshes");
+      if (!rc) rc = agb_assemble(p, AGB_MIXED);
+      if (!rc) rc = resistance_rhs(p, 1);
+      if (!rc && ensure(p->d_x, p->cap_x, (size_t)6 * p->n) != cudaSuccess) rc = fail(p, AGB_ERR_CUDA, "x buffer");
+      if (rc) return fail(c, rc, "agb_batch_resistance: body " + std::to_string(i) + ": " + p->err);
+      bodies[t].A = (const float*)p->d_A;
+      bodies[t].lda = p->lda;
+      bodies[t].m = p->m;
+      bodies[t].n = p->n;
+      bodies[t].b = p->d_rhs;
+      bodies[t].q = p->d_q;
+      bodies[t].x = p->d_x;
+    }
+    const auto tb = clk::now();
+    if (autotune && !tuned) {
+      std::string rep, err;
+      if (!batch_autotune(bodies, c->stream, tune, rep, err)) return fail(c, AGB_ERR_CUDA, "batch autotune: " + err);
+      tuned = true;
+    }
+    std::vector<int> nv, iv;
+    std::string err;
+    if (!batch_lsqr_solve(bodies, 6, eps, maxit, tune, c->stream, nv, iv, &bst, err))
+      return fail(c, AGB_ERR_CUDA, "batch solve: " + err);
+    const auto tc = clk::now();
+    for (size_t t = 0; t < w.size(); ++t) {
+      const int i = w[t];
+      agb_context* p = c->pool[t];
+      if (!p->d_ft) CUDA_OR_FAIL(c, cudaMalloc(&p->d_ft, 6 * AGB_MAX_RHS * sizeof(double)));
+      CUDA_OR_FAIL(c, launch_force_torque(p->ne, 6, p->d_geom, p->d_x, 0, p->d_ft, c->stream));
+      CUDA_OR_FAIL(c, cudaMemcpyAsync(R + 36 * (size_t)i, p->d_ft, 36 * sizeof(double), cudaMemcpyDeviceToHost,
+                                      c->stream));
+      for (int r = 0; r < 6; ++r) {
+        if (nit) nit[6 * (size_t)i + r] = nv[6 * t + r];
+        if (istop) istop[6 * (size_t)i + r] = iv[6 * t + r];
+      }
+    }
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    bst.launches += (long)w.size();
+    const auto td = clk::now();
+    t_asm += ms(ta, tb);
+    t_solve += ms(tb, tc);
+    t_ft += ms(tc, td);
+  }
+  CUDA_OR_FAIL(c, cudaEventRecord(d1, c->stream));
+  CUDA_OR_FAIL(c, cudaEventSynchronize(d1));
+  float dev_ms = 0.f;
+  cudaEventElapsedTime(&dev_ms, d0, d1);
+  cudaEventDestroy(d0);
+  cudaEventDestroy(d1);
+  long asm_launches = 0;
+  for (agb_context* p : c->pool) {
+    asm_launches += p->nlaunch + p->lsqr.launches + p->lsqr_prev_launches;
+    p->nlaunch = 0; p->lsqr.launches = 0; p->lsqr_prev_launches = 0;
+  }
+  if (stats) {
+    stats[0] = t_asm; stats[1] = t_solve; stats[2] = ms(t_start, clk::now()); stats[3] = (double)waves.size();
+    stats[4] = bst.av_ms; stats[5] = bst.atu_ms; stats[6] = (double)bst.av_launches; stats[7] = (double)bst.atu_launches;
+    stats[8] = bst.bytes_av; stats[9] = (double)(bst.launches + asm_launches);
+    stats[10] = tune.av_rows; stats[11] = tune.atu_rs; stats[12] = tune.atu_rows; stats[13] = (double)bst.iterations;
+    stats[14] = dev_ms; stats[15] = t_ft;
+  }
   return AGB_OK;
 }
 

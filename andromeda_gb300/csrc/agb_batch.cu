@@ -1,0 +1,616 @@
+// Batched block LSQR over many dense FP32 systems of uneven size (the many-body
+// resistance workflow: one particle-in-container system per body, 6 rigid-body
+// right-hand sides each).
+//
+// The recurrence per system and right-hand side is the reference's LSQR
+// (lsqr_solve / lsqr_LSQR, src/lib_lsqr.f:33-127,470-1231) exactly as the
+// single-system solver runs it; what changes is the schedule:
+//   * one launch per sweep covers the tiles of ALL systems: a CTA finds its
+//     system by a binary search over a prefix table of tile counts, so a wave
+//     of hundreds of small bodies fills the GPU as one large body does;
+//   * systems whose right-hand sides have all stopped drop out (their tiles
+//     exit at once), so the wave's cost follows the systems still iterating;
+//   * the 7 launches of an iteration are captured once in a CUDA graph of
+//     `check_every` iterations and replayed until no system is active;
+//   * tile shapes (rows per A*V CTA, rows per A^T*U stage and per CTA) are
+//     picked by batch_autotune from timed candidates.
+// The sweep tiles are the TMA-fed bodies of agb_sweeps.cuh (tensor maps of
+// every system kept in a device table, 64-byte aligned).
+#include "agb_batch.cuh"
+#include "agb_sweeps.cuh"
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <cstdio>
+
+namespace agb {
+
+#define BCK(x)                                                                   \
+  do {                                                                           \
+    cudaError_t e_ = (x);                                                        \
+    if (e_ != cudaSuccess) {                                                     \
+      err = std::string(#x) + ": " + cudaGetErrorString(e_);                     \
+      return false;                                                              \
+    }                                                                            \
+  } while (0)
+
+static inline unsigned cdivu(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
+constexpr int BT = 256;  // threads of the element-wise kernels
+
+// Device descriptor of one system.
+struct GDesc {  // CUtensorMap members keep the 64-byte alignment TMA needs
+  CUtensorMap tm_av;   // box 256 x av_rows
+  CUtensorMap tm_atu;  // box 256 x atu_rs
+  const double* b;
+  const double* q;
+  double* x;
+  double *Y, *V, *W, *X, *Zp, *part;
+  float *Ys, *Vs;
+  LsqrScalars* sc;
+  int64_t lda, mpad;
+  int m, n, k, itnlim;
+  int cblocks, zgroups, rpg;
+  int nb_b, nb_av, nb_red, nb_upd;
+};
+
+struct GOffsets {
+  const int* b;    // init tiles (mpad * 8 / 256 per system)
+  const int* av;   // A*V tiles (m / av_rows)
+  const int* atu;  // A^T*U tiles (cblocks * zgroups)
+  const int* red;  // reduce tiles (n * 8 / 256)
+  const int* upd;  // update tiles (lda * 8 / 256)
+};
+
+__device__ __forceinline__ int find_body(const int* __restrict__ off, int nb, int blk) {
+  int lo = 0, hi = nb;  // off[lo] <= blk < off[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] <= blk) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// per-CTA sums of squares of 8 interleaved columns (lanes with equal c are 8 apart)
+__device__ __forceinline__ void block_sumsq8(double v, double* __restrict__ out) {
+  __shared__ double sP[BT / 32][K8];
+  double s = v * v;
+  s += __shfl_xor_sync(0xffffffffu, s, 8);
+  s += __shfl_xor_sync(0xffffffffu, s, 16);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane < K8) sP[warp][lane] = s;
+  __syncthreads();
+  if (threadIdx.x < K8) {
+    double a = 0.0;
+    for (int w = 0; w < BT / 32; ++w) a += sP[w][threadIdx.x];
+    out[threadIdx.x] = a;
+  }
+}
+
+// Y = Ys = b (r0 = b for the zero warm start), partial ||b||^2.
+__global__ void __launch_bounds__(BT) g_init_b(const GDesc* __restrict__ D, const int* __restrict__ off, int nb) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  const GDesc& d = D[bi];
+  const int blk = blockIdx.x - off[bi];
+  const int64_t t = (int64_t)blk * BT + threadIdx.x;
+  const int64_t r = t / K8;
+  const int c = (int)(t % K8);
+  double v = 0.0;
+  if (r < d.m && c < d.k) v = d.b[(int64_t)c * d.m + r];
+  if (r < d.mpad) {
+    d.Y[t] = v;
+    d.Ys[t] = (float)v;
+  }
+  block_sumsq8(v, d.part + (int64_t)blk * K8);
+}
+
+// Scalar phases, one CTA per system (same fixed-order reduction as the
+// single-system k_scalars).  Phase 0 also sets the lsqr_solve tolerances.
+__global__ void __launch_bounds__(256) g_scalars(const GDesc* __restrict__ D, int phase, int* __restrict__ bact,
+                                                 int* nactive, double eps) {
+  const int bi = blockIdx.x;
+  if (phase != 0 && !bact[bi]) return;
+  const GDesc& d = D[bi];
+  const int nbp = phase == 0 ? d.nb_b : phase == 2 ? d.nb_av : phase == 4 ? d.nb_upd : d.nb_red;
+  __shared__ double sred[256];
+  __shared__ double ssum[K8];
+  {
+    const int t = threadIdx.x, cc = t % K8;
+    double a = 0.0;
+    for (int b = t / K8; b < nbp; b += 256 / K8) a += d.part[(int64_t)b * K8 + cc];
+    sred[t] = a;
+    __syncthreads();
+    if (t < K8) {
+      double tot = 0.0;
+      for (int i = t; i < 256; i += K8) tot += sred[i];
+      ssum[t] = tot;
+    }
+    __syncthreads();
+  }
+  const int c = threadIdx.x;
+  if (c < K8) {
+    LsqrScalars& s = d.sc[c];
+    lsqr_phase(s, c, d.k, phase, ssum[c], nactive);
+    if (phase == 0 && c < d.k) {
+      // tolerances of lsqr_solve (r0 = b: ||b|| = beta0)
+      const double nrm_b = sqrt(ssum[c]);
+      s.atol = eps;
+      s.btol = (s.beta > 0.0) ? eps * nrm_b / s.beta : eps;
+      s.ctol = 1.0 / 1.0e8;
+      s.itnlim = d.itnlim;
+      s.active = (s.beta > 0.0) ? 1 : 0;
+      s.istop = 0;
+      s.itn = 0;
+      s.alpha = 0.0;
+    }
+  }
+  if (phase == 0 || phase == 4) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int any = 0;
+      for (int cc = 0; cc < K8; ++cc) any |= d.sc[cc].active;
+      bact[bi] = any;
+    }
+  }
+}
+
+template <int ROWS, int ST>
+__global__ void __launch_bounds__(ROWS / 4 * 32, 1) g_av(const GDesc* __restrict__ D, const int* __restrict__ off,
+                                                         int nb, const int* __restrict__ bact, int* errflag) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  if (!bact[bi]) return;
+  const GDesc& d = D[bi];
+  av3_tile<ROWS, ST>(&d.tm_av, d.lda, d.m, d.Vs, d.sc, d.Y, d.Ys, d.part, errflag, (int)(blockIdx.x - off[bi]));
+}
+
+template <int RS, int ST>
+__global__ void __launch_bounds__(ATU3_THREADS, 1) g_atu(const GDesc* __restrict__ D, const int* __restrict__ off,
+                                                         int nb, const int* __restrict__ bact, int* errflag) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  if (!bact[bi]) return;
+  const GDesc& d = D[bi];
+  const int local = blockIdx.x - off[bi];
+  atu3_tile<RS, ST>(&d.tm_atu, d.lda, d.m, d.Ys, d.rpg, d.Zp, errflag, local % d.cblocks, local / d.cblocks);
+}
+
+// V <- Z/beta - beta V over the row-group partials (in order); partial ||V||^2
+__global__ void __launch_bounds__(BT) g_reduce(const GDesc* __restrict__ D, const int* __restrict__ off, int nb,
+                                               const int* __restrict__ bact, int init) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  if (!bact[bi]) return;
+  const GDesc& d = D[bi];
+  const int blk = blockIdx.x - off[bi];
+  const int64_t t = (int64_t)blk * BT + threadIdx.x;
+  const int64_t j = t / K8;
+  const int c = (int)(t % K8);
+  double vn = 0.0;
+  if (j < d.n) {
+    double z = 0.0;
+    for (int g = 0; g < d.zgroups; ++g) z += d.Zp[((int64_t)g * d.lda + j) * K8 + c];
+    const double beta = d.sc[c].beta;
+    if (d.sc[c].active && beta > 0.0) {
+      vn = z / beta - (init ? 0.0 : beta * d.V[j * K8 + c]);
+      d.V[j * K8 + c] = vn;
+    } else {
+      vn = d.V[j * K8 + c];
+      if (!d.sc[c].active) vn = 0.0;
+    }
+  }
+  block_sumsq8(vn, d.part + (int64_t)blk * K8);
+}
+
+// V <- V/alpha; X += t1 W; W <- t2 W + V; partial (t3 W_old)^2; Vs (RHS-major) = V
+__global__ void __launch_bounds__(BT) g_update(const GDesc* __restrict__ D, const int* __restrict__ off, int nb,
+                                               const int* __restrict__ bact, int init) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  if (!bact[bi]) return;
+  const GDesc& d = D[bi];
+  const int blk = blockIdx.x - off[bi];
+  const int64_t t = (int64_t)blk * BT + threadIdx.x;
+  const int64_t j = t / K8;
+  const int c = (int)(t % K8);
+  double dk = 0.0;
+  if (j < d.lda) {
+    const int64_t id = j * K8 + c;
+    if (j >= d.n) {
+      d.V[id] = 0.0; d.W[id] = 0.0; d.X[id] = 0.0; d.Vs[(int64_t)c * d.lda + j] = 0.f;
+    } else {
+      const LsqrScalars& s = d.sc[c];
+      if (s.active) {
+        double v = d.V[id];
+        if (s.alpha > 0.0) v = v / s.alpha;
+        d.V[id] = v;
+        if (init) {
+          d.W[id] = v;
+          d.X[id] = 0.0;
+        } else {
+          const double w = d.W[id];
+          d.X[id] = s.t1 * w + d.X[id];
+          d.W[id] = s.t2 * w + v;
+          const double q = s.t3 * w;
+          dk = q;
+        }
+      } else if (init) {
+        d.W[id] = 0.0; d.X[id] = 0.0;
+      }
+      d.Vs[(int64_t)c * d.lda + j] = (float)d.V[id];
+    }
+  }
+  block_sumsq8(dk, d.part + (int64_t)blk * K8);
+}
+
+// x(:,c) = q .* X(:,c)   (zero warm start)
+__global__ void g_finish(const GDesc* __restrict__ D) {
+  const GDesc& d = D[blockIdx.y];
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)d.n * d.k;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(t / d.n);
+    const int64_t j = t % d.n;
+    d.x[(int64_t)c * d.n + j] = d.q[j] * d.X[j * K8 + c];
+  }
+}
+
+__global__ void g_fill(int* p, int n, int v) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) p[t] = v;
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+template <typename K>
+static cudaError_t set_smem(K kernel, size_t bytes) {
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+// Kernel table of the tunable tile shapes.
+struct AvVariant {
+  int rows;
+  void (*fn)(const GDesc*, const int*, int, const int*, int*);
+  size_t smem;
+  int threads;
+};
+struct AtuVariant {
+  int rs;
+  void (*fn)(const GDesc*, const int*, int, const int*, int*);
+  size_t smem;
+};
+static const AvVariant kAv[] = {
+    {64, g_av<64, 3>, SweepAV<64, 3>::SMEM, 64 / 4 * 32},
+    {32, g_av<32, 2>, SweepAV<32, 2>::SMEM, 32 / 4 * 32},
+};
+static const AtuVariant kAtu[] = {
+    {32, g_atu<32, 3>, SweepATU<32, 3>::SMEM},
+    {16, g_atu<16, 3>, SweepATU<16, 3>::SMEM},
+};
+static const AvVariant* av_variant(int rows) {
+  for (const auto& v : kAv)
+    if (v.rows == rows) return &v;
+  return nullptr;
+}
+static const AtuVariant* atu_variant(int rs) {
+  for (const auto& v : kAtu)
+    if (v.rs == rs) return &v;
+  return nullptr;
+}
+
+struct BatchSolver {
+  int nb = 0, k = 0;
+  BatchTune tune;
+  cudaStream_t s = 0;
+  std::vector<GDesc> hd;
+  std::vector<int> hoff_b, hoff_av, hoff_atu, hoff_red, hoff_upd;
+  GDesc* d_desc = nullptr;
+  int* d_off = nullptr;  // 5 tables of nb+1
+  GOffsets off{};
+  int* bact = nullptr;
+  int* nactive = nullptr;
+  int* h_nactive = nullptr;
+  int* errflag = nullptr;
+  void* pool = nullptr;
+  double bytes_A = 0.0;
+  std::string err;
+
+  ~BatchSolver() { release(); }
+  void release() {
+    cudaFree(d_desc); cudaFree(d_off); cudaFree(bact); cudaFree(nactive); cudaFree(errflag); cudaFree(pool);
+    if (h_nactive) cudaFreeHost(h_nactive);
+    d_desc = nullptr; d_off = nullptr; bact = nullptr; nactive = nullptr; errflag = nullptr; pool = nullptr;
+    h_nactive = nullptr;
+  }
+
+  bool setup(const std::vector<BatchBody>& bodies, int k_, int maxit, const BatchTune& t, cudaStream_t st) {
+    release();
+    nb = (int)bodies.size();
+    k = k_;
+    tune = t;
+    s = st;
+    if (nb == 0) { err = "empty batch"; return false; }
+    if (k < 1 || k > K8) { err = "number of right-hand sides must be 1..8"; return false; }
+    const AvVariant* av = av_variant(tune.av_rows);
+    const AtuVariant* at = atu_variant(tune.atu_rs);
+    if (!av || !at) { err = "unknown tile shape"; return false; }
+    BCK(set_smem(av->fn, av->smem));
+    BCK(set_smem(at->fn, at->smem));
+    hd.assign(nb, GDesc{});
+    hoff_b.assign(nb + 1, 0); hoff_av.assign(nb + 1, 0); hoff_atu.assign(nb + 1, 0);
+    hoff_red.assign(nb + 1, 0); hoff_upd.assign(nb + 1, 0);
+    // pool layout (bytes), every piece 256-byte aligned
+    size_t bytes = 0;
+    auto take = [&](size_t n) { const size_t o = bytes; bytes += (n + 255) / 256 * 256; return o; };
+    struct Offs { size_t Y, Ys, V, W, X, Vs, Zp, part, sc; };
+    std::vector<Offs> po(nb);
+    bytes_A = 0.0;
+    for (int i = 0; i < nb; ++i) {
+      const BatchBody& B = bodies[i];
+      if (B.lda % 32 != 0 || B.lda < B.n || B.m < 1 || B.n < 1 || !B.A || !B.b || !B.q || !B.x) {
+        err = "bad system " + std::to_string(i);
+        return false;
+      }
+      GDesc& d = hd[i];
+      d.lda = B.lda; d.m = B.m; d.n = B.n; d.k = k;
+      d.mpad = ((int64_t)B.m + 255) / 256 * 256;
+      d.itnlim = maxit > 0 ? maxit : 10 * (B.m + B.n + 50);
+      d.cblocks = (int)cdivu(B.lda, ATU3_COLS);
+      d.zgroups = std::max(1, (int)cdivu(B.m, std::max(tune.atu_rows, tune.atu_rs)));
+      d.rpg = (int)((cdivu(B.m, d.zgroups) + tune.atu_rs - 1) / tune.atu_rs * tune.atu_rs);
+      d.zgroups = (int)cdivu(B.m, d.rpg);
+      d.nb_b = (int)cdivu(d.mpad * K8, BT);
+      d.nb_av = (int)cdivu(B.m, tune.av_rows);
+      d.nb_red = (int)cdivu((int64_t)B.n * K8, BT);
+      d.nb_upd = (int)cdivu(B.lda * K8, BT);
+      const int nbmax = std::max(std::max(d.nb_b, d.nb_av), std::max(d.nb_red, d.nb_upd));
+      po[i].Y = take(d.mpad * K8 * sizeof(double));
+      po[i].Ys = take(d.mpad * K8 * sizeof(float));
+      po[i].V = take(B.lda * K8 * sizeof(double));
+      po[i].W = take(B.lda * K8 * sizeof(double));
+      po[i].X = take(B.lda * K8 * sizeof(double));
+      po[i].Vs = take(B.lda * K8 * sizeof(float));
+      po[i].Zp = take((size_t)d.zgroups * B.lda * K8 * sizeof(double));
+      po[i].part = take((size_t)nbmax * K8 * sizeof(double));
+      po[i].sc = take(K8 * sizeof(LsqrScalars));
+      hoff_b[i + 1] = hoff_b[i] + d.nb_b;
+      hoff_av[i + 1] = hoff_av[i] + d.nb_av;
+      hoff_atu[i + 1] = hoff_atu[i] + d.cblocks * d.zgroups;
+      hoff_red[i + 1] = hoff_red[i] + d.nb_red;
+      hoff_upd[i + 1] = hoff_upd[i] + d.nb_upd;
+      bytes_A += (double)B.m * (double)B.n * 4.0;
+      if (!make_tensor_map_2d(&d.tm_av, B.A, B.lda, B.m, SWEEP_BC, tune.av_rows, err)) return false;
+      if (!make_tensor_map_2d(&d.tm_atu, B.A, B.lda, B.m, SWEEP_BC, tune.atu_rs, err)) return false;
+      d.b = B.b; d.q = B.q; d.x = B.x;
+    }
+    BCK(cudaMalloc(&pool, bytes));
+    BCK(cudaMemsetAsync(pool, 0, bytes, s));
+    char* p = (char*)pool;
+    for (int i = 0; i < nb; ++i) {
+      GDesc& d = hd[i];
+      d.Y = (double*)(p + po[i].Y); d.Ys = (float*)(p + po[i].Ys);
+      d.V = (double*)(p + po[i].V); d.W = (double*)(p + po[i].W); d.X = (double*)(p + po[i].X);
+      d.Vs = (float*)(p + po[i].Vs); d.Zp = (double*)(p + po[i].Zp); d.part = (double*)(p + po[i].part);
+      d.sc = (LsqrScalars*)(p + po[i].sc);
+    }
+    BCK(cudaMalloc(&d_desc, nb * sizeof(GDesc)));
+    BCK(cudaMemcpyAsync(d_desc, hd.data(), nb * sizeof(GDesc), cudaMemcpyHostToDevice, s));
+    BCK(cudaMalloc(&d_off, 5 * (size_t)(nb + 1) * sizeof(int)));
+    const std::vector<int>* tabs[5] = {&hoff_b, &hoff_av, &hoff_atu, &hoff_red, &hoff_upd};
+    for (int t = 0; t < 5; ++t)
+      BCK(cudaMemcpyAsync(d_off + t * (nb + 1), tabs[t]->data(), (nb + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+    off.b = d_off; off.av = d_off + (nb + 1); off.atu = d_off + 2 * (nb + 1); off.red = d_off + 3 * (nb + 1);
+    off.upd = d_off + 4 * (nb + 1);
+    BCK(cudaMalloc(&bact, nb * sizeof(int)));
+    BCK(cudaMalloc(&nactive, sizeof(int)));
+    BCK(cudaMallocHost(&h_nactive, sizeof(int)));
+    BCK(cudaMalloc(&errflag, sizeof(int)));
+    BCK(cudaMemsetAsync(errflag, 0, sizeof(int), s));
+    g_fill<<<cdivu(nb, 256), 256, 0, s>>>(bact, nb, 1);
+    BCK(cudaStreamSynchronize(s));  // host tables above must outlive their copies
+    return true;
+  }
+
+  void launch_av() {
+    const AvVariant* av = av_variant(tune.av_rows);
+    av->fn<<<hoff_av[nb], av->threads, av->smem, s>>>(d_desc, off.av, nb, bact, errflag);
+  }
+  void launch_atu() {
+    const AtuVariant* at = atu_variant(tune.atu_rs);
+    at->fn<<<hoff_atu[nb], ATU3_THREADS, at->smem, s>>>(d_desc, off.atu, nb, bact, errflag);
+  }
+};
+
+bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, int maxit, const BatchTune& tune,
+                      cudaStream_t s, std::vector<int>& nit, std::vector<int>& istop, BatchStats* st,
+                      std::string& err) {
+  BatchSolver S;
+  if (!S.setup(bodies, k, maxit, tune, s)) { err = S.err; return false; }
+  const int nb = S.nb;
+  int itmax = 0;
+  for (const auto& d : S.hd) itmax = std::max(itmax, d.itnlim);
+  long launches = 0;
+  // initial vectors: r0 = b, beta0, tolerances; A^T r0, alpha0, W = V
+  g_init_b<<<S.hoff_b[nb], BT, 0, s>>>(S.d_desc, S.off.b, nb);
+  g_scalars<<<nb, 256, 0, s>>>(S.d_desc, 0, S.bact, S.nactive, eps);
+  S.launch_atu();
+  g_reduce<<<S.hoff_red[nb], BT, 0, s>>>(S.d_desc, S.off.red, nb, S.bact, 1);
+  g_scalars<<<nb, 256, 0, s>>>(S.d_desc, 1, S.bact, S.nactive, eps);
+  g_update<<<S.hoff_upd[nb], BT, 0, s>>>(S.d_desc, S.off.upd, nb, S.bact, 1);
+  launches += 6;
+  BCK(cudaGetLastError());
+  const int ce = std::max(1, std::min(tune.check_every, 32));
+  std::vector<cudaEvent_t> ev(4 * ce, nullptr);
+  for (auto& e : ev) BCK(cudaEventCreate(&e));
+  auto iteration = [&](int i) {
+    cudaEventRecordWithFlags(ev[4 * i], s, cudaEventRecordExternal);
+    S.launch_av();
+    cudaEventRecordWithFlags(ev[4 * i + 1], s, cudaEventRecordExternal);
+    g_scalars<<<nb, 256, 0, s>>>(S.d_desc, 2, S.bact, S.nactive, eps);
+    cudaEventRecordWithFlags(ev[4 * i + 2], s, cudaEventRecordExternal);
+    S.launch_atu();
+    cudaEventRecordWithFlags(ev[4 * i + 3], s, cudaEventRecordExternal);
+    g_reduce<<<S.hoff_red[nb], BT, 0, s>>>(S.d_desc, S.off.red, nb, S.bact, 0);
+    g_scalars<<<nb, 256, 0, s>>>(S.d_desc, 3, S.bact, S.nactive, eps);
+    g_update<<<S.hoff_upd[nb], BT, 0, s>>>(S.d_desc, S.off.upd, nb, S.bact, 0);
+    cudaMemsetAsync(S.nactive, 0, sizeof(int), s);
+    g_scalars<<<nb, 256, 0, s>>>(S.d_desc, 4, S.bact, S.nactive, eps);
+  };
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  bool ok = true;
+  auto cleanup = [&]() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    for (auto& e : ev) if (e) cudaEventDestroy(e);
+  };
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) ok = false;
+  if (ok) {
+    for (int i = 0; i < ce; ++i) iteration(i);
+    if (cudaStreamEndCapture(s, &graph) != cudaSuccess) ok = false;
+  }
+  if (ok && cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) ok = false;
+  if (!ok) {
+    err = std::string("batch graph capture: ") + cudaGetErrorString(cudaGetLastError());
+    cleanup();
+    return false;
+  }
+  // initial activity
+  cudaMemsetAsync(S.nactive, 0, sizeof(int), s);
+  std::vector<int> hb(nb);
+  if (cudaMemcpyAsync(hb.data(), S.bact, nb * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess) {
+    err = "batch: initial state";
+    cleanup();
+    return false;
+  }
+  int act = 0;
+  for (int v : hb) act += v;
+  long iters = 0;
+  double av_ms = 0.0, atu_ms = 0.0;
+  long nav = 0, natu = 0;
+  while (act > 0 && iters < (long)itmax + ce) {
+    if (cudaGraphLaunch(gexec, s) != cudaSuccess) { ok = false; break; }
+    launches += 7L * ce;
+    cudaMemcpyAsync(S.h_nactive, S.nactive, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) { ok = false; break; }
+    for (int i = 0; i < ce; ++i) {
+      float a = 0.f, b = 0.f;
+      if (cudaEventElapsedTime(&a, ev[4 * i], ev[4 * i + 1]) == cudaSuccess) { av_ms += a; ++nav; }
+      if (cudaEventElapsedTime(&b, ev[4 * i + 2], ev[4 * i + 3]) == cudaSuccess) { atu_ms += b; ++natu; }
+    }
+    (void)cudaGetLastError();
+    iters += ce;
+    act = *S.h_nactive;
+  }
+  cleanup();
+  if (!ok) {
+    err = std::string("batch iterations: ") + cudaGetErrorString(cudaGetLastError());
+    return false;
+  }
+  int nmax = 1;
+  for (const auto& d : S.hd) nmax = std::max(nmax, d.n * k);
+  g_finish<<<dim3(std::min<unsigned>(cdivu(nmax, 256), 1024), nb), 256, 0, s>>>(S.d_desc);
+  launches += 1;
+  std::vector<LsqrScalars> hs((size_t)nb * K8);
+  for (int i = 0; i < nb; ++i)
+    BCK(cudaMemcpyAsync(hs.data() + (size_t)i * K8, S.hd[i].sc, K8 * sizeof(LsqrScalars), cudaMemcpyDeviceToHost, s));
+  int hflag = 0;
+  BCK(cudaMemcpyAsync(&hflag, S.errflag, sizeof(int), cudaMemcpyDeviceToHost, s));
+  BCK(cudaStreamSynchronize(s));
+  BCK(cudaGetLastError());
+  if (hflag) { err = "a bounded barrier wait in a batched sweep gave up"; return false; }
+  nit.assign((size_t)nb * k, 0);
+  istop.assign((size_t)nb * k, 0);
+  for (int i = 0; i < nb; ++i)
+    for (int c = 0; c < k; ++c) {
+      nit[(size_t)i * k + c] = hs[(size_t)i * K8 + c].itn;
+      istop[(size_t)i * k + c] = hs[(size_t)i * K8 + c].istop;
+    }
+  if (st) {
+    st->av_ms += av_ms; st->atu_ms += atu_ms;
+    st->av_launches += nav; st->atu_launches += natu;
+    st->launches += launches;
+    st->iterations = std::max(st->iterations, iters);
+    for (int i = 0; i < nb; ++i) {
+      int mx = 0;
+      for (int c = 0; c < k; ++c) mx = std::max(mx, nit[(size_t)i * k + c]);
+      st->bytes_av += (double)mx * (double)S.hd[i].m * (double)S.hd[i].n * 4.0;
+    }
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner: times every candidate tile shape of the two sweeps on the given
+// systems (warm-up launch + 3 timed launches each, CUDA events), keeps the
+// fastest of each sweep.  The vectors are zero: the sweeps' cost does not
+// depend on the values.
+// ---------------------------------------------------------------------------
+static std::mutex g_tune_mu;
+static std::map<std::string, BatchTune> g_tune_cache;
+
+bool batch_autotune(const std::vector<BatchBody>& bodies, cudaStream_t s, BatchTune& best, std::string& report,
+                    std::string& err) {
+  double tot = 0.0;
+  for (const auto& b : bodies) tot += (double)b.m * (double)b.lda * 4.0;
+  int nbk = 0;
+  for (size_t v = bodies.size(); v > 1; v >>= 1) ++nbk;
+  int tbk = 0;
+  for (double v = tot / 1e6; v > 1.0; v /= 2.0) ++tbk;
+  const std::string key = std::to_string(nbk) + "/" + std::to_string(tbk);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      best = it->second;
+      report = "cached " + key;
+      return true;
+    }
+  }
+  cudaEvent_t e0, e1;
+  BCK(cudaEventCreate(&e0));
+  BCK(cudaEventCreate(&e1));
+  auto time_it = [&](BatchSolver& S, bool av) -> double {
+    if (av) S.launch_av(); else S.launch_atu();
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < 3; ++r) { if (av) S.launch_av(); else S.launch_atu(); }
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return ms / 3.0;
+  };
+  char line[160];
+  report.clear();
+  BatchTune t0 = best;
+  double best_av = 1e300, best_atu = 1e300;
+  for (const auto& av : kAv) {
+    BatchTune t = t0;
+    t.av_rows = av.rows;
+    BatchSolver S;
+    if (!S.setup(bodies, 1, 1, t, s)) { err = S.err; cudaEventDestroy(e0); cudaEventDestroy(e1); return false; }
+    const double ms = time_it(S, true);
+    snprintf(line, sizeof line, "av rows=%d: %.3f ms; ", av.rows, ms);
+    report += line;
+    if (ms < best_av) { best_av = ms; best.av_rows = av.rows; }
+  }
+  const int row_targets[] = {2048, 8192};
+  for (const auto& at : kAtu)
+    for (int rt : row_targets) {
+      BatchTune t = t0;
+      t.atu_rs = at.rs;
+      t.atu_rows = rt;
+      BatchSolver S;
+      if (!S.setup(bodies, 1, 1, t, s)) { err = S.err; cudaEventDestroy(e0); cudaEventDestroy(e1); return false; }
+      const double ms = time_it(S, false);
+      snprintf(line, sizeof line, "atu rs=%d rows=%d: %.3f ms; ", at.rs, rt, ms);
+      report += line;
+      if (ms < best_atu) { best_atu = ms; best.atu_rs = at.rs; best.atu_rows = rt; }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  BCK(cudaGetLastError());
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_cache[key] = best;
+  return true;
+}
+
+}  // namespace agb

@@ -1,0 +1,57 @@
+// Batched block LSQR: many dense FP32 systems of uneven size, each with up to
+// 8 right-hand sides, solved together -- every sweep of an iteration is ONE
+// launch over the tiles of all systems still iterating, and the iterations are
+// replayed from one captured CUDA graph.
+#pragma once
+#include "agb_lsqr.cuh"
+#include <string>
+#include <vector>
+
+namespace agb {
+
+// One system of the batch (device pointers, owned by the caller).
+struct BatchBody {
+  const float* A = nullptr;  // m x lda row-major, columns scaled by q (lsqr_precon)
+  int64_t lda = 0;           // multiple of 32, >= n
+  int m = 0, n = 0;
+  const double* b = nullptr;  // [k][m] right-hand sides
+  const double* q = nullptr;  // [n] column scales
+  double* x = nullptr;        // [k][n] solution (zero warm start)
+};
+
+// Tile shapes and schedule of the batched sweeps (picked by batch_autotune).
+struct BatchTune {
+  int av_rows = 64;        // rows per A*V CTA (64: 3 x 72 KB stages, 1 CTA/SM; 32: 2 x 40 KB, 2 CTAs/SM)
+  int atu_rs = 32;         // rows per A^T*U stage (32: 3 x 65 KB, 1 CTA/SM; 16: 3 x 32.5 KB, 2 CTAs/SM)
+  int atu_rows = 4096;     // rows per A^T*U CTA (row groups of a system)
+  int check_every = 8;     // iterations per graph replay
+};
+
+struct BatchStats {
+  double av_ms = 0.0, atu_ms = 0.0;  // summed device time of the two sweeps (CUDA events in the graph)
+  long av_launches = 0, atu_launches = 0;
+  long launches = 0;                 // all kernels launched
+  long iterations = 0;               // graph iterations run (max over systems)
+  double bytes_av = 0.0;             // algorithmic bytes of all A*V launches: sum over systems of
+                                     // (iterations while active) x m x n x 4
+};
+
+// Solves A_i x_i = b_i (least squares) for all systems with the reference's
+// lsqr_solve semantics (zero warm start, atol = btol = eps, conlim 1e8,
+// itnlim = maxit or 10(m+n+50)); nit/istop receive k entries per system.
+bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, int maxit, const BatchTune& tune,
+                      cudaStream_t s, std::vector<int>& nit, std::vector<int>& istop, BatchStats* st,
+                      std::string& err);
+
+// Times the candidate tile shapes of both sweeps on these systems (a few
+// launches each, CUDA events) and returns the fastest; `report` lists the
+// candidates and their times.  Results are cached per (systems, total size)
+// class for the process.
+bool batch_autotune(const std::vector<BatchBody>& bodies, cudaStream_t s, BatchTune& best, std::string& report,
+                    std::string& err);
+
+// 2-D tensor map of a row-major FP32 matrix (dims {lda, m}, box box_cols x box_rows).
+bool make_tensor_map_2d(CUtensorMap* tm, const void* A, int64_t lda, int m, int box_cols, int box_rows,
+                        std::string& err);
+
+}  // namespace agb

@@ -12,6 +12,9 @@
 //                                      reproducible)
 // Vector norms are reduced from per-CTA partials in index order in FP64.
 #include "agb_lsqr.cuh"
+#include "agb_async.cuh"
+#include "agb_sweeps.cuh"
+#include "agb_batch.cuh"
 #include <cudaTypedefs.h>
 #include <cstdio>
 #include <cstring>
@@ -28,7 +31,6 @@ namespace agb {
     }                                                                            \
   } while (0)
 
-constexpr int K8 = AGB_MAX_RHS;
 constexpr int kThreads = 256;
 
 template <typename T> struct Vec;
@@ -209,41 +211,6 @@ __global__ void __launch_bounds__(kThreads) k_atu(const T* __restrict__ A, int64
 // the warp (31 shuffles) so that lane l keeps the FP64 running sum of
 // (row l/8, rhs l%8) -- one FP64 register per lane instead of 32.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_u32(dst)),
-               "l"(src), "r"(bytes), "r"(smem_u32(bar))
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// bounded wait: after ~2^22 failed tries the barrier is reported through
-// errflag and the wait gives up (the copy is in bounds by construction, so
-// this only guards against a hang)
-__device__ __forceinline__ void mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* errflag) {
-  uint32_t tries = 0;
-  while (!mbar_try_wait(bar, parity)) {
-    if (++tries > (1u << 22)) {
-      if (errflag) atomicExch(errflag, 1);
-      break;
-    }
-  }
-}
-
 template <typename T> struct AV2;
 template <> struct AV2<float> { static constexpr int RR = 4, WARPS = 16, CH = 1024; };
 template <> struct AV2<double> { static constexpr int RR = 2, WARPS = 8, CH = 512; };
@@ -486,221 +453,23 @@ __global__ void __launch_bounds__(ATU_THREADS) k_atu2(const T* __restrict__ A, i
 // shared memory, so the bytes in flight per SM (two 64 KB stages) no longer
 // depend on registers.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
-constexpr int AV3_ROWS = 64, AV3_BC = 256, AV3_ST = 3, AV3_WARPS = 16;
-constexpr size_t AV3_STAGE_A = (size_t)AV3_ROWS * AV3_BC * sizeof(float);  // 64 KB
-constexpr size_t AV3_STAGE_V = (size_t)K8 * AV3_BC * sizeof(float);        // 8 KB
-constexpr size_t AV3_SMEM = AV3_ST * (AV3_STAGE_A + AV3_STAGE_V);
+constexpr int AV3_ROWS = 64, AV3_ST = 3, AV3_WARPS = AV3_ROWS / 4;
+constexpr size_t AV3_SMEM = SweepAV<AV3_ROWS, AV3_ST>::SMEM;
 
 __global__ void __launch_bounds__(AV3_WARPS * 32, 1) k_av3(const __grid_constant__ CUtensorMap tmA, int64_t lda, int m,
                                                            const float* __restrict__ Vt, const LsqrScalars* sc,
                                                            double* __restrict__ Y, float* __restrict__ Ys,
                                                            double* __restrict__ part, int* errflag) {
-  extern __shared__ __align__(1024) unsigned char av3_smem[];
-  float* sA = reinterpret_cast<float*>(av3_smem);
-  float* sV = reinterpret_cast<float*>(av3_smem + AV3_ST * AV3_STAGE_A);
-  __shared__ __align__(8) uint64_t full[AV3_ST], empty[AV3_ST];
-  __shared__ double sPart[AV3_WARPS][K8];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int row_base = blockIdx.x * AV3_ROWS;
-  const int nst = (int)((lda + AV3_BC - 1) / AV3_BC);
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < AV3_ST; ++s) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], AV3_WARPS);
-    }
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  __syncthreads();
-  auto issue = [&](int k) {
-    const int s = k % AV3_ST;
-    if (k >= AV3_ST) mbar_wait_bounded(&empty[s], (uint32_t)(((k / AV3_ST) - 1) & 1), errflag);
-    const int64_t j0 = (int64_t)k * AV3_BC;
-    const int cw = (int)((lda - j0) < (int64_t)AV3_BC ? (lda - j0) : (int64_t)AV3_BC);
-    mbar_expect_tx(&full[s], (uint32_t)(AV3_STAGE_A + K8 * cw * sizeof(float)));
-    tma_load_2d(sA + (size_t)s * AV3_ROWS * AV3_BC, &tmA, (int)j0, row_base, &full[s]);
-#pragma unroll
-    for (int c = 0; c < K8; ++c)
-      bulk_g2s(sV + (size_t)s * K8 * AV3_BC + c * AV3_BC, Vt + (int64_t)c * lda + j0, (uint32_t)(cw * sizeof(float)),
-               &full[s]);
-  };
-  if (threadIdx.x == 0)
-    for (int k = 0; k < AV3_ST && k < nst; ++k) issue(k);
-  float acc[4][K8];
-#pragma unroll
-  for (int r = 0; r < 4; ++r)
-#pragma unroll
-    for (int c = 0; c < K8; ++c) acc[r][c] = 0.f;
-  double dacc = 0.0;
-  for (int k = 0; k < nst; ++k) {
-    const int s = k % AV3_ST;
-    mbar_wait_bounded(&full[s], (uint32_t)((k / AV3_ST) & 1), errflag);
-    const float* tA = sA + (size_t)s * AV3_ROWS * AV3_BC + (warp * 4) * AV3_BC;
-    const float* tV = sV + (size_t)s * K8 * AV3_BC;
-    const int64_t j0 = (int64_t)k * AV3_BC;
-    const int cw = (int)((lda - j0) < (int64_t)AV3_BC ? (lda - j0) : (int64_t)AV3_BC);
-#pragma unroll
-    for (int half = 0; half < 2; ++half) {
-      const int col = half * 128 + lane * 4;
-      if (col < cw) {
-        float a[4][4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          const float4 v = *reinterpret_cast<const float4*>(tA + r * AV3_BC + col);
-          a[r][0] = v.x; a[r][1] = v.y; a[r][2] = v.z; a[r][3] = v.w;
-        }
-#pragma unroll
-        for (int c = 0; c < K8; ++c) {
-          const float4 vv = *reinterpret_cast<const float4*>(tV + c * AV3_BC + col);
-#pragma unroll
-          for (int r = 0; r < 4; ++r) {
-            acc[r][c] = fmaf(a[r][0], vv.x, acc[r][c]);
-            acc[r][c] = fmaf(a[r][1], vv.y, acc[r][c]);
-            acc[r][c] = fmaf(a[r][2], vv.z, acc[r][c]);
-            acc[r][c] = fmaf(a[r][3], vv.w, acc[r][c]);
-          }
-        }
-      }
-    }
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[s]);
-    if (threadIdx.x == 0 && k + AV3_ST < nst) issue(k + AV3_ST);
-    if ((k & 3) == 3 || k == nst - 1) {
-      // reduce-scatter the 32 FP32 partials of 1024 columns into one FP64 sum per lane
-      float v[32];
-#pragma unroll
-      for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = 0; c < K8; ++c) { v[r * K8 + c] = acc[r][c]; acc[r][c] = 0.f; }
-#pragma unroll
-      for (int o = 16; o >= 1; o >>= 1) {
-        const bool upper = (lane & o) != 0;
-#pragma unroll
-        for (int i = 0; i < o; ++i) {
-          const float send = upper ? v[i] : v[i + o];
-          const float keep = upper ? v[i + o] : v[i];
-          v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
-        }
-      }
-      dacc += (double)v[0];
-    }
-  }
-  double ssq = 0.0;
-  {
-    const int r = lane >> 3, c = lane & 7, row = row_base + warp * 4 + r;
-    if (row < m) {
-      const double y = dacc + sc[c].gamma * Y[(int64_t)row * K8 + c];
-      Y[(int64_t)row * K8 + c] = y;
-      Ys[(int64_t)row * K8 + c] = (float)y;
-      ssq = y * y;
-    }
-    ssq += __shfl_xor_sync(0xffffffffu, ssq, 8);
-    ssq += __shfl_xor_sync(0xffffffffu, ssq, 16);
-  }
-  if (lane < K8) sPart[warp][lane] = ssq;
-  __syncthreads();
-  if (threadIdx.x < K8) {
-    double a = 0.0;
-    for (int w = 0; w < AV3_WARPS; ++w) a += sPart[w][threadIdx.x];
-    part[(int64_t)blockIdx.x * K8 + threadIdx.x] = a;
-  }
+  av3_tile<AV3_ROWS, AV3_ST>(&tmA, lda, m, Vt, sc, Y, Ys, part, errflag, (int)blockIdx.x);
 }
 
-// A^T Y: a CTA owns 512 columns (two 256-column tiles) and a row group; 32-row
-// stages of A plus the matching 32 rows of Y (1 KB) arrive by TMA; a thread owns
-// two columns; FP32 partials over 256 rows are added into FP64 registers.
-constexpr int ATU3_COLS = 512, ATU3_RS = 32, ATU3_ST = 3, ATU3_THREADS = 256;
-constexpr size_t ATU3_STAGE_A = (size_t)ATU3_RS * ATU3_COLS * sizeof(float);  // 64 KB
-constexpr size_t ATU3_STAGE_U = (size_t)ATU3_RS * K8 * sizeof(float);         // 1 KB
-constexpr size_t ATU3_SMEM = ATU3_ST * (ATU3_STAGE_A + ATU3_STAGE_U);
+constexpr int ATU3_RS = 32, ATU3_ST = 3;
+constexpr size_t ATU3_SMEM = SweepATU<ATU3_RS, ATU3_ST>::SMEM;
 
 __global__ void __launch_bounds__(ATU3_THREADS, 1) k_atu3(const __grid_constant__ CUtensorMap tmA, int64_t lda, int m,
                                                           const float* __restrict__ Us, int rows_per_group,
                                                           double* __restrict__ Zp, int* errflag) {
-  extern __shared__ __align__(1024) unsigned char atu3_smem[];
-  float* sA = reinterpret_cast<float*>(atu3_smem);
-  float* sU = reinterpret_cast<float*>(atu3_smem + ATU3_ST * ATU3_STAGE_A);
-  __shared__ __align__(8) uint64_t full[ATU3_ST], empty[ATU3_ST];
-  const int c0 = blockIdx.x * ATU3_COLS;
-  const int g = blockIdx.y;
-  const int r0 = g * rows_per_group, r1 = min(m, r0 + rows_per_group);
-  const int nst = (r1 > r0) ? (r1 - r0 + ATU3_RS - 1) / ATU3_RS : 0;
-  const int warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < ATU3_ST; ++s) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], ATU3_THREADS / 32);
-    }
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  __syncthreads();
-  auto issue = [&](int k) {
-    const int s = k % ATU3_ST;
-    if (k >= ATU3_ST) mbar_wait_bounded(&empty[s], (uint32_t)(((k / ATU3_ST) - 1) & 1), errflag);
-    const int rb = r0 + k * ATU3_RS;
-    const int nr = min(ATU3_RS, r1 - rb);
-    mbar_expect_tx(&full[s], (uint32_t)(ATU3_STAGE_A + (size_t)nr * K8 * sizeof(float)));
-    float* dA = sA + (size_t)s * ATU3_RS * ATU3_COLS;
-    tma_load_2d(dA, &tmA, c0, rb, &full[s]);
-    tma_load_2d(dA + ATU3_RS * 256, &tmA, c0 + 256, rb, &full[s]);
-    bulk_g2s(sU + (size_t)s * ATU3_RS * K8, Us + (int64_t)rb * K8, (uint32_t)(nr * K8 * sizeof(float)), &full[s]);
-  };
-  if (threadIdx.x == 0)
-    for (int k = 0; k < ATU3_ST && k < nst; ++k) issue(k);
-  const int tc = threadIdx.x * 2;          // the thread's two columns within the CTA block
-  const int box = tc >> 8, off = tc & 255;  // tile and column within the tile
-  float acc[2][K8];
-  double dacc[2][K8];
-#pragma unroll
-  for (int q = 0; q < 2; ++q)
-#pragma unroll
-    for (int c = 0; c < K8; ++c) { acc[q][c] = 0.f; dacc[q][c] = 0.0; }
-  for (int k = 0; k < nst; ++k) {
-    const int s = k % ATU3_ST;
-    mbar_wait_bounded(&full[s], (uint32_t)((k / ATU3_ST) & 1), errflag);
-    const int rb = r0 + k * ATU3_RS;
-    const int nr = min(ATU3_RS, r1 - rb);
-    const float* tA = sA + (size_t)s * ATU3_RS * ATU3_COLS + box * ATU3_RS * 256 + off;
-    const float* tU = sU + (size_t)s * ATU3_RS * K8;
-#pragma unroll 4
-    for (int r = 0; r < nr; ++r) {
-      const float2 a = *reinterpret_cast<const float2*>(tA + r * 256);
-      const float4 u0 = *reinterpret_cast<const float4*>(tU + r * K8);
-      const float4 u1 = *reinterpret_cast<const float4*>(tU + r * K8 + 4);
-      const float uu[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
-#pragma unroll
-      for (int c = 0; c < K8; ++c) {
-        acc[0][c] += a.x * uu[c];
-        acc[1][c] += a.y * uu[c];
-      }
-    }
-    __syncwarp();
-    if ((threadIdx.x & 31) == 0) mbar_arrive(&empty[s]);
-    if (threadIdx.x == 0 && k + ATU3_ST < nst) issue(k + ATU3_ST);
-    if ((k & 7) == 7 || k == nst - 1) {
-#pragma unroll
-      for (int q = 0; q < 2; ++q)
-#pragma unroll
-        for (int c = 0; c < K8; ++c) { dacc[q][c] += (double)acc[q][c]; acc[q][c] = 0.f; }
-    }
-  }
-  (void)warp;
-  const int64_t col = (int64_t)c0 + tc;
-#pragma unroll
-  for (int q = 0; q < 2; ++q)
-    if (col + q < lda)
-#pragma unroll
-      for (int c = 0; c < K8; ++c) Zp[((int64_t)g * lda + col + q) * K8 + c] = dacc[q][c];
+  atu3_tile<ATU3_RS, ATU3_ST>(&tmA, lda, m, Us, rows_per_group, Zp, errflag, (int)blockIdx.x, (int)blockIdx.y);
 }
 
 // V <- Z/beta - beta V (Z = sum of group partials, in order); partial ||V||^2.
@@ -787,11 +556,6 @@ __global__ void k_update(int n, int64_t lda, const LsqrScalars* sc, int init, do
   }
 }
 
-__device__ double d2norm(double a, double b) {
-  double scale = fabs(a) + fabs(b);
-  if (scale == 0.0) return 0.0;
-  return scale * sqrt((a / scale) * (a / scale) + (b / scale) * (b / scale));
-}
 __device__ double sum_part(const double* part, int nb, int c) {
   double s = 0.0;
   for (int b = 0; b < nb; ++b) s += part[b * K8 + c];
@@ -827,102 +591,8 @@ __global__ void __launch_bounds__(SCAL_THREADS) k_scalars(LsqrScalars* sc, int k
   }
   const int c = threadIdx.x;
   if (c >= K8) return;
-  LsqrScalars& s = sc[c];
-  if (c >= k) { s.active = 0; return; }
-  if (phase == 0) {
-    s.beta = sqrt(ssum[c]);
-    return;
-  }
-  if (!s.active) return;
-  if (phase == 1) {
-    s.alpha = sqrt(ssum[c]);
-    if (s.beta <= 0.0) s.alpha = 0.0;
-    s.rhobar = s.alpha;
-    s.phibar = s.beta;
-    s.bnorm = s.beta;
-    s.rnorm = s.beta;
-    s.arnorm = s.alpha * s.beta;
-    s.anorm = s.acond = s.dnorm = s.dxmax = s.res2 = s.xnorm = s.xnorm1 = s.z = s.sn2 = 0.0;
-    s.cs2 = -1.0;
-    s.itn = 0;
-    s.istop = 0;
-    s.gamma = (s.beta > 0.0) ? -s.alpha / s.beta : 0.0;
-    if (s.arnorm == 0.0) s.active = 0;  // lsqr: GOTO 800 with istop = 0
-    return;
-  }
-  if (phase == 2) {
-    s.itn += 1;
-    s.beta = sqrt(ssum[c]);
-    double temp = d2norm(s.alpha, s.beta);
-    temp = d2norm(temp, 0.0);
-    s.anorm = d2norm(s.anorm, temp);
-    return;
-  }
-  if (phase == 3) {
-    if (s.beta > 0.0) {
-      s.alpha = sqrt(ssum[c]);
-    }
-    double rhbar1 = s.rhobar;
-    double rho = d2norm(rhbar1, s.beta);
-    double cs = rhbar1 / rho, sn = s.beta / rho;
-    double theta = sn * s.alpha;
-    s.rhobar = -cs * s.alpha;
-    double phi = cs * s.phibar;
-    s.phibar = sn * s.phibar;
-    double tau = sn * phi;
-    s.t1 = phi / rho;
-    s.t2 = -theta / rho;
-    s.t3 = 1.0 / rho;
-    // second rotation and norm estimates (depend only on scalars)
-    double delta = s.sn2 * rho, gambar = -s.cs2 * rho;
-    double rhs = phi - delta * s.z;
-    double zbar = rhs / gambar;
-    s.xnorm = d2norm(s.xnorm1, zbar);
-    double gamma = d2norm(gambar, theta);
-    s.cs2 = gambar / gamma;
-    s.sn2 = theta / gamma;
-    s.z = rhs / gamma;
-    s.xnorm1 = d2norm(s.xnorm1, s.z);
-    s.res2 = d2norm(s.res2, 0.0);
-    s.rnorm = d2norm(s.res2, s.phibar);
-    s.arnorm = s.alpha * fabs(tau);
-    // stash phi for the dxk monitor
-    s.dxmax = fmax(s.dxmax, 0.0);
-    s.acond = phi;  // temporary (phi), replaced in phase 4
-    return;
-  }
-  if (phase == 4) {
-    const double phi = s.acond;
-    double dknorm = sqrt(ssum[c]);
-    s.dnorm = d2norm(s.dnorm, dknorm);
-    double dxk = fabs(phi * dknorm);
-    if (s.dxmax < dxk) s.dxmax = dxk;
-    s.acond = s.anorm * s.dnorm;
-    const double one = 1.0, zero = 0.0;
-    double test1 = s.rnorm / s.bnorm;
-    double test2 = zero;
-    if (s.rnorm > zero) test2 = s.arnorm / (s.anorm * s.rnorm);
-    double test3 = one / s.acond;
-    double t1 = test1 / (one + s.anorm * s.xnorm / s.bnorm);
-    double rtol = s.btol + s.atol * s.anorm * s.xnorm / s.bnorm;
-    double t3 = one + test3, t2 = one + test2;
-    t1 = one + t1;
-    int istop = 0;
-    if (s.itn >= s.itnlim) istop = 5;
-    if (t3 <= one) istop = 4;
-    if (t2 <= one) istop = 2;
-    if (t1 <= one) istop = 1;
-    if (test3 <= s.ctol) istop = 4;
-    if (test2 <= s.atol) istop = 2;
-    if (test1 <= rtol) istop = 1;
-    s.istop = istop;
-    if (istop != 0) s.active = 0;
-    s.gamma = (s.beta > 0.0) ? -s.alpha / s.beta : 0.0;
-    if (s.beta <= 0.0) s.active = 0;
-    if (s.active) atomicAdd(nactive, 1);
-  }
+  lsqr_phase(sc[c], c, k, phase, ssum[c], nactive);
 }
-
 
 // ---------------------------------------------------------------------------
 // Column scaling (lsqr_precon): partial column sums of squares per row group,
@@ -1026,7 +696,8 @@ static inline unsigned cdiv(int64_t a, int64_t b) { return (unsigned)((a + b - 1
 
 // Build a 2-D tensor map of the row-major FP32 matrix (dims {lda, m}) with the
 // given box, through the driver entry point (no link against libcuda).
-static bool make_tmap(CUtensorMap* tm, const void* A, int64_t lda, int m, int box_cols, int box_rows, std::string& err) {
+bool make_tensor_map_2d(CUtensorMap* tm, const void* A, int64_t lda, int m, int box_cols, int box_rows,
+                        std::string& err) {
   static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   if (!encode) {
     cudaDriverEntryPointQueryResult q;
@@ -1129,8 +800,8 @@ bool DenseLsqr::setup(const void* A_dev, bool is_fp32, int m_, int n_, int64_t l
   // row groups for sweep 2: aim for >= 4 CTAs per SM
   use_tma = fp32 && getenv("AGB_NO_TMA") == nullptr;
   if (use_tma) {
-    if (!make_tmap(&tm_av, A_dev, lda, m, AV3_BC, AV3_ROWS, err)) return false;
-    if (!make_tmap(&tm_atu, A_dev, lda, m, 256, ATU3_RS, err)) return false;
+    if (!make_tensor_map_2d(&tm_av, A_dev, lda, m, SWEEP_BC, AV3_ROWS, err)) return false;
+    if (!make_tensor_map_2d(&tm_atu, A_dev, lda, m, 256, ATU3_RS, err)) return false;
   }
   const int vn = fp32 ? 4 : 2;
   const int colblocks = use_tma ? (int)cdiv(lda, ATU3_COLS) : (int)cdiv(lda, ATU_THREADS * vn);

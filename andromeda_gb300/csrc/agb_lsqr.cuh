@@ -44,8 +44,8 @@ struct DenseLsqr {
   bool pev_ready = false;
   // TMA descriptors of A for the FP32 sweeps (2-D tiles: 256 columns x 64
   // rows for A*V, 256 columns x 32 rows for A^T*U)
-  alignas(64) CUtensorMap tm_av{};
-  alignas(64) CUtensorMap tm_atu{};
+  CUtensorMap tm_av{};
+  CUtensorMap tm_atu{};
   bool use_tma = false;
   double t_av = 0.0, t_atu = 0.0;
   long n_av = 0, n_atu = 0;

@@ -1,0 +1,234 @@
+// TMA-fed FP32 LSQR sweeps over a row-major matrix, as tile bodies shared by
+// the single-system kernels (k_av3 / k_atu3) and the batched kernels that run
+// many systems in one launch.
+//
+// Sweep 1 (av3_tile): Y = A V + gamma Y for ROWS rows of A and 8 right-hand
+// sides.  A arrives in stages of ROWS x 256 columns by 2-D tensor-map copies,
+// the matching 8 x 256 slice of V (RHS-major) by 1-D bulk copies; ST stages
+// ring through shared memory with full/empty mbarriers (bounded waits).  A warp
+// owns 4 rows; lanes hold 4 x 8 FP32 accumulators, reduce-scattered every 1024
+// columns into one FP64 running sum per lane.
+//
+// Sweep 2 (atu3_tile): Zp[g] = A(rows of group g)^T Y for 512 columns; stages
+// of RS rows (two 256-column boxes) plus RS rows of Y; a thread owns 2 columns
+// x 8 right-hand sides, FP32 partials flushed into FP64 registers every 256
+// rows.
+#pragma once
+#include "agb_async.cuh"
+
+namespace agb {
+
+constexpr int SWEEP_BC = 256;       // columns per tensor-map box
+constexpr int ATU3_COLS = 512;      // columns per sweep-2 CTA
+constexpr int ATU3_THREADS = 256;
+
+template <int ROWS, int ST>
+struct SweepAV {
+  static constexpr int WARPS = ROWS / 4;
+  static constexpr size_t STAGE_A = (size_t)ROWS * SWEEP_BC * sizeof(float);
+  static constexpr size_t STAGE_V = (size_t)K8 * SWEEP_BC * sizeof(float);
+  static constexpr size_t SMEM = ST * (STAGE_A + STAGE_V);
+};
+template <int RS, int ST>
+struct SweepATU {
+  static constexpr size_t STAGE_A = (size_t)RS * ATU3_COLS * sizeof(float);
+  static constexpr size_t STAGE_U = (size_t)RS * K8 * sizeof(float);
+  static constexpr size_t SMEM = ST * (STAGE_A + STAGE_U);
+};
+
+template <int ROWS, int ST>
+__device__ __forceinline__ void av3_tile(const CUtensorMap* tmA, int64_t lda, int m, const float* __restrict__ Vt,
+                                         const LsqrScalars* sc, double* __restrict__ Y, float* __restrict__ Ys,
+                                         double* __restrict__ part, int* errflag, int blk) {
+  using P = SweepAV<ROWS, ST>;
+  constexpr int WARPS = P::WARPS;
+  extern __shared__ __align__(1024) unsigned char sweep_smem[];
+  float* sA = reinterpret_cast<float*>(sweep_smem);
+  float* sV = reinterpret_cast<float*>(sweep_smem + ST * P::STAGE_A);
+  __shared__ __align__(8) uint64_t full[ST], empty[ST];
+  __shared__ double sPart[WARPS][K8];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row_base = blk * ROWS;
+  const int nst = (int)((lda + SWEEP_BC - 1) / SWEEP_BC);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < ST; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], WARPS);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int k) {
+    const int s = k % ST;
+    if (k >= ST) mbar_wait_bounded(&empty[s], (uint32_t)(((k / ST) - 1) & 1), errflag);
+    const int64_t j0 = (int64_t)k * SWEEP_BC;
+    const int cw = (int)((lda - j0) < (int64_t)SWEEP_BC ? (lda - j0) : (int64_t)SWEEP_BC);
+    mbar_expect_tx(&full[s], (uint32_t)(P::STAGE_A + K8 * cw * sizeof(float)));
+    tma_load_2d(sA + (size_t)s * ROWS * SWEEP_BC, tmA, (int)j0, row_base, &full[s]);
+#pragma unroll
+    for (int c = 0; c < K8; ++c)
+      bulk_g2s(sV + (size_t)s * K8 * SWEEP_BC + c * SWEEP_BC, Vt + (int64_t)c * lda + j0,
+               (uint32_t)(cw * sizeof(float)), &full[s]);
+  };
+  if (threadIdx.x == 0)
+    for (int k = 0; k < ST && k < nst; ++k) issue(k);
+  float acc[4][K8];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < K8; ++c) acc[r][c] = 0.f;
+  double dacc = 0.0;
+  for (int k = 0; k < nst; ++k) {
+    const int s = k % ST;
+    mbar_wait_bounded(&full[s], (uint32_t)((k / ST) & 1), errflag);
+    const float* tA = sA + (size_t)s * ROWS * SWEEP_BC + (warp * 4) * SWEEP_BC;
+    const float* tV = sV + (size_t)s * K8 * SWEEP_BC;
+    const int64_t j0 = (int64_t)k * SWEEP_BC;
+    const int cw = (int)((lda - j0) < (int64_t)SWEEP_BC ? (lda - j0) : (int64_t)SWEEP_BC);
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int col = half * 128 + lane * 4;
+      if (col < cw) {
+        float a[4][4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const float4 v = *reinterpret_cast<const float4*>(tA + r * SWEEP_BC + col);
+          a[r][0] = v.x; a[r][1] = v.y; a[r][2] = v.z; a[r][3] = v.w;
+        }
+#pragma unroll
+        for (int c = 0; c < K8; ++c) {
+          const float4 vv = *reinterpret_cast<const float4*>(tV + c * SWEEP_BC + col);
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            acc[r][c] = fmaf(a[r][0], vv.x, acc[r][c]);
+            acc[r][c] = fmaf(a[r][1], vv.y, acc[r][c]);
+            acc[r][c] = fmaf(a[r][2], vv.z, acc[r][c]);
+            acc[r][c] = fmaf(a[r][3], vv.w, acc[r][c]);
+          }
+        }
+      }
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+    if (threadIdx.x == 0 && k + ST < nst) issue(k + ST);
+    if ((k & 3) == 3 || k == nst - 1) {
+      // reduce-scatter the 32 FP32 partials of 1024 columns into one FP64 sum per lane
+      float v[32];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < K8; ++c) { v[r * K8 + c] = acc[r][c]; acc[r][c] = 0.f; }
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) {
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < o; ++i) {
+          const float send = upper ? v[i] : v[i + o];
+          const float keep = upper ? v[i + o] : v[i];
+          v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+      }
+      dacc += (double)v[0];
+    }
+  }
+  double ssq = 0.0;
+  {
+    const int r = lane >> 3, c = lane & 7, row = row_base + warp * 4 + r;
+    if (row < m) {
+      const double y = dacc + sc[c].gamma * Y[(int64_t)row * K8 + c];
+      Y[(int64_t)row * K8 + c] = y;
+      Ys[(int64_t)row * K8 + c] = (float)y;
+      ssq = y * y;
+    }
+    ssq += __shfl_xor_sync(0xffffffffu, ssq, 8);
+    ssq += __shfl_xor_sync(0xffffffffu, ssq, 16);
+  }
+  if (lane < K8) sPart[warp][lane] = ssq;
+  __syncthreads();
+  if (threadIdx.x < K8) {
+    double a = 0.0;
+    for (int w = 0; w < WARPS; ++w) a += sPart[w][threadIdx.x];
+    part[(int64_t)blk * K8 + threadIdx.x] = a;
+  }
+}
+
+template <int RS, int ST>
+__device__ __forceinline__ void atu3_tile(const CUtensorMap* tmA, int64_t lda, int m, const float* __restrict__ Us,
+                                          int rows_per_group, double* __restrict__ Zp, int* errflag, int cblk,
+                                          int g) {
+  using P = SweepATU<RS, ST>;
+  constexpr int FLUSH = 256 / RS;  // stages per FP64 flush
+  extern __shared__ __align__(1024) unsigned char sweep_smem[];
+  float* sA = reinterpret_cast<float*>(sweep_smem);
+  float* sU = reinterpret_cast<float*>(sweep_smem + ST * P::STAGE_A);
+  __shared__ __align__(8) uint64_t full[ST], empty[ST];
+  const int c0 = cblk * ATU3_COLS;
+  const int r0 = g * rows_per_group, r1 = min(m, r0 + rows_per_group);
+  const int nst = (r1 > r0) ? (r1 - r0 + RS - 1) / RS : 0;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < ST; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], ATU3_THREADS / 32);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int k) {
+    const int s = k % ST;
+    if (k >= ST) mbar_wait_bounded(&empty[s], (uint32_t)(((k / ST) - 1) & 1), errflag);
+    const int rb = r0 + k * RS;
+    const int nr = min(RS, r1 - rb);
+    mbar_expect_tx(&full[s], (uint32_t)(P::STAGE_A + (size_t)nr * K8 * sizeof(float)));
+    float* dA = sA + (size_t)s * RS * ATU3_COLS;
+    tma_load_2d(dA, tmA, c0, rb, &full[s]);
+    tma_load_2d(dA + RS * SWEEP_BC, tmA, c0 + SWEEP_BC, rb, &full[s]);
+    bulk_g2s(sU + (size_t)s * RS * K8, Us + (int64_t)rb * K8, (uint32_t)(nr * K8 * sizeof(float)), &full[s]);
+  };
+  if (threadIdx.x == 0)
+    for (int k = 0; k < ST && k < nst; ++k) issue(k);
+  const int tc = threadIdx.x * 2;          // the thread's two columns within the CTA block
+  const int box = tc >> 8, off = tc & 255;  // tile and column within the tile
+  float acc[2][K8];
+  double dacc[2][K8];
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+#pragma unroll
+    for (int c = 0; c < K8; ++c) { acc[q][c] = 0.f; dacc[q][c] = 0.0; }
+  for (int k = 0; k < nst; ++k) {
+    const int s = k % ST;
+    mbar_wait_bounded(&full[s], (uint32_t)((k / ST) & 1), errflag);
+    const int rb = r0 + k * RS;
+    const int nr = min(RS, r1 - rb);
+    const float* tA = sA + (size_t)s * RS * ATU3_COLS + box * RS * SWEEP_BC + off;
+    const float* tU = sU + (size_t)s * RS * K8;
+#pragma unroll 4
+    for (int r = 0; r < nr; ++r) {
+      const float2 a = *reinterpret_cast<const float2*>(tA + r * SWEEP_BC);
+      const float4 u0 = *reinterpret_cast<const float4*>(tU + r * K8);
+      const float4 u1 = *reinterpret_cast<const float4*>(tU + r * K8 + 4);
+      const float uu[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+#pragma unroll
+      for (int c = 0; c < K8; ++c) {
+        acc[0][c] += a.x * uu[c];
+        acc[1][c] += a.y * uu[c];
+      }
+    }
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) mbar_arrive(&empty[s]);
+    if (threadIdx.x == 0 && k + ST < nst) issue(k + ST);
+    if ((k % FLUSH) == FLUSH - 1 || k == nst - 1) {
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+#pragma unroll
+        for (int c = 0; c < K8; ++c) { dacc[q][c] += (double)acc[q][c]; acc[q][c] = 0.f; }
+    }
+  }
+  const int64_t col = (int64_t)c0 + tc;
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+    if (col + q < lda)
+#pragma unroll
+      for (int c = 0; c < K8; ++c) Zp[((int64_t)g * lda + col + q) * K8 + c] = dacc[q][c];
+}
+
+}  // namespace agb

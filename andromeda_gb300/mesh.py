@@ -210,6 +210,32 @@ def quad_box(nx: int, ny: int, nz: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), 
     return {"xyz": xyz, "etype": np.full(len(quads), 3, np.int32), "con": quads, "bcid": bc}
 
 
+def superellipsoid_tri(a, b, c, e1, e2, n_target, rotation=None, inward=False, wall=1):
+    """Superellipsoid with about ``n_target`` triangles: n_sectors = round(sqrt(n))
+    longitudes, n_rings = round(n / (2 n_sectors)) latitude rings."""
+    ns = max(4, int(round(np.sqrt(n_target))))
+    nr = max(2, int(round(n_target / (2.0 * ns))))
+    return superellipsoid(a, b, c, e1, e2, nr, ns, rotation=rotation, inward=inward, wall=wall)
+
+
+def batch_bodies(n_bodies=512, seed=20260101, n_min=500, n_max=8000, outer_level=2, outer_radius=200.0):
+    """The many-body workload: superellipsoids a = 1, b, c ~ U(0.2, 1), e1, e2 ~
+    U(0.3, 1.8), uniform random orientation, element counts log-uniform in
+    [n_min, n_max], each inside its own container sphere (normals into the
+    particle).  Returns (meshes, params) with params rows (b, c, e1, e2, n_elem)."""
+    rng = np.random.default_rng(seed)
+    meshes, params = [], []
+    for _ in range(n_bodies):
+        b, c = rng.uniform(0.2, 1.0, 2)
+        e1, e2 = rng.uniform(0.3, 1.8, 2)
+        rot = random_rotation(rng)
+        n = float(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        body = superellipsoid_tri(1.0, b, c, e1, e2, n, rotation=rot, inward=True)
+        meshes.append(particle_in_sphere(body, outer_level=outer_level, outer_radius=outer_radius))
+        params.append((b, c, e1, e2, len(body["etype"])))
+    return meshes, np.array(params)
+
+
 def random_rotation(rng: np.random.Generator):
     """Uniform random rotation matrix from a unit quaternion."""
     q = rng.normal(size=4)

@@ -223,6 +223,30 @@ int agb_solve_fields(agb_context* ctx, int nrhs, const double* u_in, const doubl
 #define AGB_NOALLOC_MAX_COLUMNS AGB_NOALLOC_SCRATCH_DOUBLES
 int agb_lsqr_precon_dense_noalloc(int m, int n, int64_t lda, double* A, double* q);
 
+/* Batched resistance tensors (many bodies of uneven size, one container each).
+ * Body i is nodes node_off[i]..node_off[i+1]-1 of xyz (3 doubles per node)
+ * and elements elem_off[i]..elem_off[i+1]-1 of etype/con/bcid (con: 4 ints per
+ * element, 0-based node ids LOCAL to the body; triangles only), with the wall
+ * ids particle_wall and outer_wall.  For every body the reference's 6-RHS
+ * resistance workflow (StokesInlet3sidesForceCRS / ...TorqueOmegaCRS,
+ * lib_particle.f90:341,176; CoR_Integrals_Stokes lib_Stokes.f90:2664;
+ * lsqr_solve lib_lsqr.f:33) is run in mixed precision: R[36*i + 6*r + j] is
+ * component j (Fx,Fy,Fz,Tx,Ty,Tz) on the particle for rigid motion r of the
+ * container; nit/istop: 6 per body.  Bodies are assembled per body and solved
+ * together in waves that fit mem_gb of device memory (0: 70 % of the free
+ * memory): every LSQR sweep of a wave is one launch over the tiles of all of its
+ * bodies, replayed from a CUDA graph; autotune != 0 times the candidate tile
+ * shapes on the first wave.  stats (16 doubles, may be NULL): host ms of
+ * assembly+rhs, solve, total; waves; device ms and launches of the A*V and
+ * A^T*U sweeps; algorithmic bytes of all A*V launches; kernel launches; chosen
+ * A*V rows, A^T*U stage rows, A^T*U rows per CTA; graph iterations; device ms
+ * of the whole call; host ms of the force/torque step.  ctx only carries the
+ * device and the error text (its own mesh/problem are untouched). */
+int agb_batch_resistance(agb_context* ctx, int nbodies, const int* node_off, const double* xyz, const int* elem_off,
+                         const int* etype, const int* con, const int* bcid, int particle_wall, int outer_wall,
+                         int itri, int maxit, double eps, double mem_gb, int autotune, double* R, int* nit,
+                         int* istop, double* stats);
+
 #ifdef __cplusplus
 }
 #endif
