@@ -4,4 +4,5 @@ assembly and LSQR solve as hand-written sm_103a CUDA kernels behind a C ABI
 from . import mesh  # noqa: F401
 from ._lib import AgbError, LIB_PATH, load  # noqa: F401
 from .api import (BC_CONTACT, BC_FLUX, BC_FUNCTION, FP64, LAPLACE, MIXED, STOKES, Context,  # noqa: F401
-                  batch_resistance, dirichlet_known, lsqr_precon, lsqr_solve, version)
+                  batch_resistance, dirichlet_known, form_pre_fm, lsqr_precon, lsqr_solve, solv_eqn_fm,
+                  version)

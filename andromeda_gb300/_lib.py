@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(HERE, "libandromeda_gb300.so")
 dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 lp = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 vp = C.c_void_p
 I = C.c_int
 D = C.c_double
@@ -45,6 +46,19 @@ SIGNATURES = {
     "agb_integral_matrices": ([vp, vp, vp, vp], I),
     "agb_layout_sizes": ([vp, ip], I),
     "agb_solve_fields": ([vp, I, dp, vp, dp, dp, I, D, I, ip, ip], I),
+    "agb_form_pre_fm": ([I, I, dp, dp, C.POINTER(C.c_float), PI], I),
+    "agb_solv_eqn_fm": ([I, I, I, I, I, D, I, dp, dp, dp, dp, PI, C.POINTER(C.c_double), PI], I),
+    "agb_solve_lu": ([vp, I, dp, dp, PI], I),
+    "agb_mlp_create": ([C.POINTER(vp), I, I, I, I, C.c_ulonglong], I),
+    "agb_mlp_destroy": ([vp], I),
+    "agb_mlp_num_params": ([vp, C.POINTER(C.c_longlong)], I),
+    "agb_mlp_get_params": ([vp, fp], I),
+    "agb_mlp_set_params": ([vp, fp], I),
+    "agb_mlp_set_normalization": ([vp, fp, fp, fp, fp], I),
+    "agb_mlp_gradient": ([vp, I, fp, fp, I, fp, C.POINTER(C.c_double)], I),
+    "agb_mlp_train": ([vp, I, fp, fp, I, I, C.c_float, C.c_ulonglong, dp, dp], I),
+    "agb_mlp_predict": ([vp, I, fp, fp, I, C.POINTER(C.c_double)], I),
+    "agb_mlp_launches": ([vp], C.c_longlong),
     "agb_batch_resistance": ([vp, I, ip, dp, ip, ip, ip, ip, I, I, I, I, D, D, I, dp, ip, ip, dp], I),
 }
 

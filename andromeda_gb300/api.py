@@ -161,6 +161,16 @@ class Context:
         self._ck(self._L.agb_solve(self.h, nrhs, u.ravel(), x.reshape(-1), int(maxit), float(eps), int(refine), nit, istop))
         return x, nit, istop
 
+    def solve_lu(self, u):
+        """Direct FP64 LU solve of the assembled square system (the FULL path):
+        returns (x, info) with x in solve()'s layout."""
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        nrhs = u.shape[0]
+        x = np.zeros((nrhs, self.n))
+        info = C.c_int(0)
+        self._ck(self._L.agb_solve_lu(self.h, nrhs, u.ravel(), x.reshape(-1), C.byref(info)))
+        return x, info.value
+
     def force_torque(self, x, wall):
         x = np.ascontiguousarray(x, dtype=np.float64)
         nrhs = x.shape[0]
@@ -232,6 +242,35 @@ class Context:
                                                float(eps), int(refine), R.reshape(-1), nit, istop, t))
         return R, nit, {"assemble_ms": t[0], "rhs_ms": t[1], "solve_ms": t[2], "reduce_ms": t[3], "total_ms": t[4],
                         "device_ms": t[5], "istop": istop.tolist()}
+
+
+def form_pre_fm(a, pret=2):
+    """FormPREfm drop-in: returns (factors, q, ierr) for the square matrix a
+    (pret 2: LU on the GPU; q = 1-based pivots; pret 1: q = 1/diag)."""
+    L = load()
+    a = np.asarray(a, dtype=np.float64)
+    n = a.shape[0]
+    f = np.array(a.ravel(order="F"))
+    q = np.zeros(n)
+    cpu = C.c_float(0.0)
+    ierr = C.c_int(0)
+    _check(L.agb_form_pre_fm(int(pret), n, q, f, C.byref(cpu), C.byref(ierr)))
+    return f.reshape((n, n), order="F"), q, ierr.value
+
+
+def solv_eqn_fm(f, q, b, pret=2, prep=2):
+    """SolvEQNfm drop-in (slvt 0): x = A^-1 b from form_pre_fm's output."""
+    L = load()
+    n = f.shape[0]
+    fa = np.array(np.asarray(f, dtype=np.float64).ravel(order="F"))
+    qq = np.array(q, dtype=np.float64)
+    x = np.zeros(n)
+    nit = C.c_int(-1)
+    cpu = C.c_double(0.0)
+    ierr = C.c_int(0)
+    _check(L.agb_solv_eqn_fm(0, int(pret), int(prep), 0, 0, 0.0, n, qq, fa, np.ascontiguousarray(b, dtype=np.float64),
+                             x, C.byref(nit), C.byref(cpu), C.byref(ierr)))
+    return x, ierr.value
 
 
 def batch_resistance(meshes, particle_wall=1, outer_wall=2, itri=5, maxit=0, eps=1e-7, mem_gb=0.0, autotune=True,

@@ -5,6 +5,9 @@
 #include "agb_lsqr.cuh"
 #include "agb_general.cuh"
 #include "agb_batch.cuh"
+#include "agb_lu.cuh"
+#include "agb_mlp.cuh"
+#include <random>
 #include "quad_tables.h"
 
 #include <chrono>
@@ -32,7 +35,10 @@ struct agb_context {
   // problem
   int kind = 0, neq = 0;
   IntegOpt iopt;  // triangle integration options (agb_set_integration)
-  std::vector<agb_context*> pool;  // per-body contexts of agb_batch_resistance (reused)
+  double* d_lu = nullptr;      // column-major LU factors of the unscaled FP64 system (agb_solve_lu)
+  std::vector<int> lu_ipiv;    // its pivots (1-based)
+  bool lu_ready = false;
+  int lu_info = 0;
   std::vector<int> walls;
   std::vector<double> normMul;
   double diff = 1.0;
@@ -159,6 +165,8 @@ cudaError_t ensure(T*& p, size_t& cap, size_t count) {
 }
 
 void free_system(agb_context* c) {
+  dfree(c->d_lu);
+  c->lu_ready = false;
   dfree(c->d_rhsM);
   c->general = false;
   dfree(c->d_A);
@@ -330,7 +338,8 @@ int device_rhs(agb_context* c, int nrhs, int na) {
   CUDA_OR_FAIL(c, ensure(c->d_rhs, c->cap_rhs, (size_t)nrhs * c->m));
   if (c->kind == AGB_STOKES) {
     StokesRhsArgs a;
-    a.ne = c->ne; a.Q = c->rule.Q; a.ldp = 0; a.k = nrhs; a.nnodes = c->nnodes;
+    a.ne = c->ne; a.Q = c->rule.Q; a.ldp = (c->ne + 31) / 32 * 32; a.k = nrhs; a.nnodes = c->nnodes;
+    a.pts = c->d_pts;
     a.geom = c->d_geom; a.rule_l = c->rule.l; a.rule_w = c->rule.w; a.u = c->d_u;
     a.active = c->d_active; a.na = na; a.row_active = c->d_rowact; a.rhs = c->d_rhs;
     cudaEventRecord(c->tev[2], c->stream);
@@ -495,8 +504,6 @@ int agb_create(agb_context** out, int device) {
 
 int agb_destroy(agb_context* c) {
   if (!c) return AGB_OK;
-  for (agb_context* p : c->pool) agb_destroy(p);
-  c->pool.clear();
   cudaSetDevice(c->device);
   free_problem(c);
   dfree(c->d_xyz);
@@ -1062,6 +1069,15 @@ int agb_solve_fields(agb_context* c, int nrhs, const double* u_in, const double*
 }
 
 
+// One body of a batch on the device: pieces of the wave's arena.
+struct BatchSlot {
+  int body = 0, nn = 0, ne = 0, ldp = 0, m = 0, n = 0, groups = 1, na = 0;
+  int64_t lda = 0;
+  size_t o_xyz, o_et, o_con, o_wall, o_geom, o_pts, o_src, o_nrm, o_cs, o_A, o_q, o_u, o_act, o_ract, o_rhs, o_x,
+      o_ft, o_P;  // device offsets
+  size_t h_xyz, h_et, h_con, h_wall, h_cs, h_u, h_act, h_ract;  // offsets in the upload image
+};
+
 int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const double* xyz, const int* elem_off,
                          const int* etype, const int* con, const int* bcid, int particle_wall, int outer_wall,
                          int itri, int maxit, double eps, double mem_gb, int autotune, double* R, int* nit,
@@ -1071,39 +1087,92 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
     return fail(c, AGB_ERR_ARG, "agb_batch_resistance: missing arrays");
   if (itri < 1 || itri > 5 || maxit < 0 || !(eps >= 0.0) || !(mem_gb >= 0.0))
     return fail(c, AGB_ERR_ARG, "agb_batch_resistance: bad parameters");
-  for (int i = 0; i < nbodies; ++i)
+  for (int i = 0; i < nbodies; ++i) {
     if (node_off[i + 1] <= node_off[i] || elem_off[i + 1] <= elem_off[i])
       return fail(c, AGB_ERR_ARG, "agb_batch_resistance: empty body " + std::to_string(i));
+    const int nn = node_off[i + 1] - node_off[i];
+    bool pw = false, ow = false;
+    for (int e = elem_off[i]; e < elem_off[i + 1]; ++e) {
+      if (etype[e] != AGB_TRI) return fail(c, AGB_ERR_UNSUPPORTED, "batched bodies must be triangle meshes");
+      if (bcid[e] != particle_wall && bcid[e] != outer_wall)
+        return fail(c, AGB_ERR_ARG, "batched body " + std::to_string(i) + " has a third wall");
+      pw = pw || bcid[e] == particle_wall;
+      ow = ow || bcid[e] == outer_wall;
+      for (int k = 0; k < 3; ++k)
+        if (con[4 * (size_t)e + k] < 0 || con[4 * (size_t)e + k] >= nn)
+          return fail(c, AGB_ERR_ARG, "connectivity out of range in body " + std::to_string(i));
+    }
+    if (!pw || !ow) return fail(c, AGB_ERR_ARG, "batched body " + std::to_string(i) + " lacks a wall");
+  }
   cudaSetDevice(c->device);
   using clk = std::chrono::steady_clock;
   auto ms = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
   const auto t_start = clk::now();
+  cudaStream_t st = c->stream;
   cudaEvent_t d0 = nullptr, d1 = nullptr;
   CUDA_OR_FAIL(c, cudaEventCreate(&d0));
   CUDA_OR_FAIL(c, cudaEventCreate(&d1));
-  CUDA_OR_FAIL(c, cudaEventRecord(d0, c->stream));
-  // device bytes of one body: FP32 matrix + assembly/solver work buffers
-  auto body_bytes = [&](int i) {
-    const double ne = (double)(elem_off[i + 1] - elem_off[i]);
-    const double n = 3.0 * ne, lda = std::ceil(n / 32.0) * 32.0;
-    // A + solver vectors and up to 64 row-group partials of the per-body column
-    // scaling + quadrature points + allocation granularity
-    return n * lda * 4.0 + lda * 64.0 * 80.0 + ne * 126.0 * 16.0 * 1.1 + 8.0e6;
+  CUDA_OR_FAIL(c, cudaEventRecord(d0, st));
+  // quadrature rule (shared by all bodies)
+  std::vector<double> rl, rw;
+  expand_rule(itri, rl, rw);
+  const int Q = (int)rw.size();
+  RuleDev rule;
+  rule.Q = Q;
+  CUDA_OR_FAIL(c, cudaMallocAsync(&rule.l, rl.size() * sizeof(double), st));
+  CUDA_OR_FAIL(c, cudaMallocAsync(&rule.w, rw.size() * sizeof(double), st));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(rule.l, rl.data(), rl.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(rule.w, rw.data(), rw.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  // slot layout of every body
+  auto al = [](size_t v) { return (v + 255) / 256 * 256; };
+  std::vector<BatchSlot> slots(nbodies);
+  std::vector<size_t> dev_bytes(nbodies), up_bytes(nbodies);
+  for (int i = 0; i < nbodies; ++i) {
+    BatchSlot& b = slots[i];
+    b.body = i;
+    b.nn = node_off[i + 1] - node_off[i];
+    b.ne = elem_off[i + 1] - elem_off[i];
+    b.ldp = (b.ne + 31) / 32 * 32;
+    b.m = b.n = 3 * b.ne;
+    b.lda = ((int64_t)b.n + 31) / 32 * 32;
+    b.groups = std::max(1, std::min(32, b.m / 512));
+    size_t o = 0;
+    auto take = [&](size_t bytes) { const size_t r = o; o += al(bytes); return r; };
+    b.o_xyz = take(3 * (size_t)b.nn * 8); b.o_et = take((size_t)b.ne * 4); b.o_con = take(4 * (size_t)b.ne * 4);
+    b.o_wall = take((size_t)b.ne * 4); b.o_cs = take((size_t)b.ldp * 4); b.o_u = take(18 * (size_t)b.nn * 8);
+    b.o_act = take((size_t)b.ne * 4); b.o_ract = take((size_t)b.ne);
+    const size_t upload = o;  // the pieces above are uploaded from one host image
+    b.h_xyz = b.o_xyz; b.h_et = b.o_et; b.h_con = b.o_con; b.h_wall = b.o_wall; b.h_cs = b.o_cs; b.h_u = b.o_u;
+    b.h_act = b.o_act; b.h_ract = b.o_ract;
+    b.o_geom = take((size_t)b.ne * sizeof(ElemGeom));
+    b.o_pts = take((size_t)Q * b.ldp * sizeof(QPt<float>));
+    b.o_src = take(3 * (size_t)b.ldp * 4); b.o_nrm = take(3 * (size_t)b.ldp * 4);
+    b.o_A = take((size_t)b.m * b.lda * 4); b.o_q = take((size_t)b.lda * 8);
+    b.o_rhs = take(6 * (size_t)b.m * 8); b.o_x = take(6 * (size_t)b.n * 8); b.o_ft = take(6 * AGB_MAX_RHS * 8);
+    b.o_P = take((size_t)b.groups * b.lda * 8);
+    dev_bytes[i] = o;
+    up_bytes[i] = upload;
+  }
+  // solver vectors of the batched LSQR (pool of batch_lsqr_solve) per body
+  auto solver_bytes = [&](int i) {
+    const BatchSlot& b = slots[i];
+    const double mpad = std::ceil(b.m / 256.0) * 256.0;
+    return mpad * 8 * 12.0 + (double)b.lda * 8 * (8 * 3 + 4 + 8 * 8) + 65536.0;
   };
   double budget = mem_gb * 1e9;
   if (budget <= 0.0) {
     size_t fr = 0, tot = 0;
     CUDA_OR_FAIL(c, cudaMemGetInfo(&fr, &tot));
-    budget = 0.7 * (double)fr;
+    budget = 0.8 * (double)fr;
   }
   // waves: largest bodies first, packed greedily under the budget
   std::vector<int> order(nbodies);
   for (int i = 0; i < nbodies; ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return body_bytes(a) > body_bytes(b); });
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return dev_bytes[a] > dev_bytes[b]; });
   std::vector<std::vector<int>> waves;
   double used = 0.0;
   for (int i : order) {
-    const double bb = body_bytes(i);
+    const double bb = (double)dev_bytes[i] + solver_bytes(i);
     if (waves.empty() || (used + bb > budget && !waves.back().empty())) {
       waves.emplace_back();
       used = 0.0;
@@ -1111,85 +1180,173 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
     waves.back().push_back(i);
     used += bb;
   }
-  size_t maxwave = 0;
-  for (auto& w : waves) maxwave = std::max(maxwave, w.size());
-  while (c->pool.size() < maxwave) {
-    agb_context* p = nullptr;
-    const int rc = agb_create(&p, c->device);
-    if (rc) return fail(c, rc, std::string("agb_batch_resistance: ") + agb_last_error(nullptr));
-    c->pool.push_back(p);
-  }
   BatchTune tune;
   BatchStats bst;
   bool tuned = false;
   double t_asm = 0.0, t_solve = 0.0, t_ft = 0.0;
-  const int walls[2] = {particle_wall, outer_wall};
-  const int known[6] = {AGB_BC_FUNCTION, AGB_BC_FUNCTION, AGB_BC_FUNCTION, AGB_BC_FUNCTION, AGB_BC_FUNCTION,
-                        AGB_BC_FUNCTION};
+  long asm_launches = 0;
+  char* arena = nullptr;
+  char* h_img = nullptr;
+  size_t arena_cap = 0, img_cap = 0;
+  auto release = [&]() {
+    if (arena) cudaFree(arena);
+    if (h_img) cudaFreeHost(h_img);
+    cudaFree(rule.l);
+    cudaFree(rule.w);
+    cudaEventDestroy(d0);
+    cudaEventDestroy(d1);
+  };
+  auto bail = [&](int code, const std::string& msg) {
+    cudaStreamSynchronize(st);
+    release();
+    return fail(c, code, "agb_batch_resistance: " + msg);
+  };
   for (const auto& w : waves) {
     const auto ta = clk::now();
+    // arena of the wave
+    std::vector<size_t> base(w.size()), hbase(w.size());
+    size_t total = 0, htotal = 0;
+    for (size_t t = 0; t < w.size(); ++t) {
+      base[t] = total; total += dev_bytes[w[t]];
+      hbase[t] = htotal; htotal += up_bytes[w[t]];
+    }
+    if (total > arena_cap) {
+      if (arena) { cudaStreamSynchronize(st); cudaFree(arena); arena = nullptr; }
+      if (cudaMalloc(&arena, total) != cudaSuccess) return bail(AGB_ERR_CUDA, "arena of " + std::to_string(total) + " bytes");
+      arena_cap = total;
+    }
+    if (htotal > img_cap) {
+      if (h_img) { cudaStreamSynchronize(st); cudaFreeHost(h_img); h_img = nullptr; }
+      if (cudaMallocHost(&h_img, htotal) != cudaSuccess) return bail(AGB_ERR_CUDA, "host staging");
+      img_cap = htotal;
+    }
+    // host image: nodes, elements (particle wall first, then the container), u of
+    // the six rigid motions of the container, active elements and rows
+    cudaStreamSynchronize(st);  // the previous wave's upload of the image has completed
+    for (size_t t = 0; t < w.size(); ++t) {
+      BatchSlot& b = slots[w[t]];
+      const int i = b.body;
+      char* h = h_img + hbase[t];
+      double* hx = (double*)(h + b.h_xyz);
+      std::memcpy(hx, xyz + 3 * (size_t)node_off[i], 3 * (size_t)b.nn * 8);
+      int* het = (int*)(h + b.h_et);
+      int* hcon = (int*)(h + b.h_con);
+      int* hwall = (int*)(h + b.h_wall);
+      float* hcs = (float*)(h + b.h_cs);
+      double* hu = (double*)(h + b.h_u);
+      int* hact = (int*)(h + b.h_act);
+      unsigned char* hract = (unsigned char*)(h + b.h_ract);
+      std::vector<char> onOuter(b.nn, 0);
+      int p = 0;
+      for (int k = 0; k < 2; ++k)
+        for (int e = elem_off[i]; e < elem_off[i + 1]; ++e) {
+          if (bcid[e] != (k == 0 ? particle_wall : outer_wall)) continue;
+          het[p] = AGB_TRI;
+          for (int kk = 0; kk < 4; ++kk) hcon[4 * p + kk] = (kk < 3) ? con[4 * (size_t)e + kk] : -1;
+          hwall[p] = k;
+          hract[p] = (unsigned char)k;
+          if (k == 1)
+            for (int kk = 0; kk < 3; ++kk) onOuter[hcon[4 * p + kk]] = 1;
+          ++p;
+        }
+      for (int q = 0; q < b.ldp; ++q) hcs[q] = (q < b.ne) ? -1.0f : 0.0f;  // -(normMul/mu), mu = 1
+      std::memset(hu, 0, 18 * (size_t)b.nn * 8);
+      for (int n = 0; n < b.nn; ++n) {
+        if (!onOuter[n]) continue;
+        const double* x = hx + 3 * (size_t)n;
+        for (int a = 0; a < 3; ++a) hu[((size_t)a * 3 + a) * b.nn + n] = 1.0;
+        const double wv[3][3] = {{0, -x[2], x[1]}, {x[2], 0, -x[0]}, {-x[1], x[0], 0}};
+        for (int a = 0; a < 3; ++a)
+          for (int bb = 0; bb < 3; ++bb) hu[((size_t)(3 + a) * 3 + bb) * b.nn + n] = wv[a][bb];
+      }
+      b.na = 0;
+      for (int q = 0; q < b.ne; ++q)
+        if (hract[q]) hact[b.na++] = q;
+    }
+    // one upload per body (its pieces are contiguous in both images)
+    for (size_t t = 0; t < w.size(); ++t)
+      if (cudaMemcpyAsync(arena + base[t], h_img + hbase[t], up_bytes[w[t]], cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return bail(AGB_ERR_CUDA, "upload");
+    static const double kNormMul[2] = {1.0, 1.0};
+    double* d_nm = nullptr;
+    if (cudaMallocAsync(&d_nm, 2 * sizeof(double), st) != cudaSuccess ||
+        cudaMemcpyAsync(d_nm, kNormMul, 2 * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return bail(AGB_ERR_CUDA, "normMul");
     std::vector<BatchBody> bodies(w.size());
     for (size_t t = 0; t < w.size(); ++t) {
-      const int i = w[t];
-      agb_context* p = c->pool[t];
-      const int nn = node_off[i + 1] - node_off[i], ne = elem_off[i + 1] - elem_off[i];
-      int rc = agb_set_mesh(p, nn, xyz + 3 * (size_t)node_off[i], ne, etype + elem_off[i], con + 4 * (size_t)elem_off[i],
-                            bcid + elem_off[i]);
-      if (!rc) rc = agb_set_problem(p, AGB_STOKES, 2, walls, nullptr, 1.0, known, itri, 4);
-      if (!rc && (p->all_tri == false)) rc = fail(p, AGB_ERR_UNSUPPORTED, "batched bodies must be triangle meshes");
-      if (!rc) rc = agb_assemble(p, AGB_MIXED);
-      if (!rc) rc = resistance_rhs(p, 1);
-      if (!rc && ensure(p->d_x, p->cap_x, (size_t)6 * p->n) != cudaSuccess) rc = fail(p, AGB_ERR_CUDA, "x buffer");
-      if (rc) return fail(c, rc, "agb_batch_resistance: body " + std::to_string(i) + ": " + p->err);
-      bodies[t].A = (const float*)p->d_A;
-      bodies[t].lda = p->lda;
-      bodies[t].m = p->m;
-      bodies[t].n = p->n;
-      bodies[t].b = p->d_rhs;
-      bodies[t].q = p->d_q;
-      bodies[t].x = p->d_x;
+      const BatchSlot& b = slots[w[t]];
+      char* d = arena + base[t];
+      ElemGeom* geom = (ElemGeom*)(d + b.o_geom);
+      float* A = (float*)(d + b.o_A);
+      cudaError_t e = launch_geometry(b.ne, (const double*)(d + b.o_xyz), (const int*)(d + b.o_et),
+                                      (const int*)(d + b.o_con), (const int*)(d + b.o_wall), d_nm, geom, st);
+      if (e == cudaSuccess)
+        e = launch_expand_points<float>(b.ne, b.ldp, geom, rule, (QPt<float>*)(d + b.o_pts), (float*)(d + b.o_src),
+                                        (float*)(d + b.o_nrm), st);
+      if (e == cudaSuccess && b.lda > b.n)
+        e = cudaMemset2DAsync((char*)A + b.n * 4, b.lda * 4, 0, (b.lda - b.n) * 4, b.m, st);
+      if (e == cudaSuccess)
+        e = launch_stokes_G<float>(b.ne, Q, b.ldp, (const QPt<float>*)(d + b.o_pts), (const float*)(d + b.o_src),
+                                   (const float*)(d + b.o_cs), A, b.lda, st);
+      if (e == cudaSuccess) e = launch_stokes_self<float>(b.ne, geom, 1.0, A, b.lda, st);
+      if (e == cudaSuccess)
+        e = dense_colscale_f32(A, b.lda, b.m, b.n, (double*)(d + b.o_q), (double*)(d + b.o_P), b.groups, st);
+      if (e == cudaSuccess) {
+        StokesRhsArgs a;
+        a.ne = b.ne; a.Q = Q; a.ldp = b.ldp; a.k = 6; a.nnodes = b.nn;
+        a.pts = d + b.o_pts;
+        a.geom = geom; a.rule_l = rule.l; a.rule_w = rule.w; a.u = (const double*)(d + b.o_u);
+        a.active = (const int*)(d + b.o_act); a.na = b.na; a.row_active = (const unsigned char*)(d + b.o_ract);
+        a.rhs = (double*)(d + b.o_rhs);
+        e = launch_stokes_rhs<float>(a, st);
+      }
+      if (e != cudaSuccess) return bail(AGB_ERR_CUDA, std::string("assembly: ") + cudaGetErrorString(e));
+      asm_launches += 9 + (b.na > 0 ? 2 : 0);
+      bodies[t].A = A;
+      bodies[t].lda = b.lda;
+      bodies[t].m = b.m;
+      bodies[t].n = b.n;
+      bodies[t].b = (const double*)(d + b.o_rhs);
+      bodies[t].q = (const double*)(d + b.o_q);
+      bodies[t].x = (double*)(d + b.o_x);
     }
+    cudaFreeAsync(d_nm, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return bail(AGB_ERR_CUDA, "assembly of the wave");
     const auto tb = clk::now();
     if (autotune && !tuned) {
       std::string rep, err;
-      if (!batch_autotune(bodies, c->stream, tune, rep, err)) return fail(c, AGB_ERR_CUDA, "batch autotune: " + err);
+      if (!batch_autotune(bodies, st, tune, rep, err)) return bail(AGB_ERR_CUDA, "autotune: " + err);
       tuned = true;
     }
     std::vector<int> nv, iv;
     std::string err;
-    if (!batch_lsqr_solve(bodies, 6, eps, maxit, tune, c->stream, nv, iv, &bst, err))
-      return fail(c, AGB_ERR_CUDA, "batch solve: " + err);
+    if (!batch_lsqr_solve(bodies, 6, eps, maxit, tune, st, nv, iv, &bst, err)) return bail(AGB_ERR_CUDA, "solve: " + err);
     const auto tc = clk::now();
     for (size_t t = 0; t < w.size(); ++t) {
-      const int i = w[t];
-      agb_context* p = c->pool[t];
-      if (!p->d_ft) CUDA_OR_FAIL(c, cudaMalloc(&p->d_ft, 6 * AGB_MAX_RHS * sizeof(double)));
-      CUDA_OR_FAIL(c, launch_force_torque(p->ne, 6, p->d_geom, p->d_x, 0, p->d_ft, c->stream));
-      CUDA_OR_FAIL(c, cudaMemcpyAsync(R + 36 * (size_t)i, p->d_ft, 36 * sizeof(double), cudaMemcpyDeviceToHost,
-                                      c->stream));
+      const BatchSlot& b = slots[w[t]];
+      char* d = arena + base[t];
+      if (launch_force_torque(b.ne, 6, (const ElemGeom*)(d + b.o_geom), (const double*)(d + b.o_x), 0,
+                              (double*)(d + b.o_ft), st) != cudaSuccess ||
+          cudaMemcpyAsync(R + 36 * (size_t)b.body, d + b.o_ft, 36 * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+              cudaSuccess)
+        return bail(AGB_ERR_CUDA, "force/torque");
       for (int r = 0; r < 6; ++r) {
-        if (nit) nit[6 * (size_t)i + r] = nv[6 * t + r];
-        if (istop) istop[6 * (size_t)i + r] = iv[6 * t + r];
+        if (nit) nit[6 * (size_t)b.body + r] = nv[6 * t + r];
+        if (istop) istop[6 * (size_t)b.body + r] = iv[6 * t + r];
       }
     }
-    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
-    bst.launches += (long)w.size();
+    if (cudaStreamSynchronize(st) != cudaSuccess) return bail(AGB_ERR_CUDA, "force/torque");
+    asm_launches += (long)w.size();
     const auto td = clk::now();
     t_asm += ms(ta, tb);
     t_solve += ms(tb, tc);
     t_ft += ms(tc, td);
   }
-  CUDA_OR_FAIL(c, cudaEventRecord(d1, c->stream));
+  CUDA_OR_FAIL(c, cudaEventRecord(d1, st));
   CUDA_OR_FAIL(c, cudaEventSynchronize(d1));
   float dev_ms = 0.f;
   cudaEventElapsedTime(&dev_ms, d0, d1);
-  cudaEventDestroy(d0);
-  cudaEventDestroy(d1);
-  long asm_launches = 0;
-  for (agb_context* p : c->pool) {
-    asm_launches += p->nlaunch + p->lsqr.launches + p->lsqr_prev_launches;
-    p->nlaunch = 0; p->lsqr.launches = 0; p->lsqr_prev_launches = 0;
-  }
+  release();
   if (stats) {
     stats[0] = t_asm; stats[1] = t_solve; stats[2] = ms(t_start, clk::now()); stats[3] = (double)waves.size();
     stats[4] = bst.av_ms; stats[5] = bst.atu_ms; stats[6] = (double)bst.av_launches; stats[7] = (double)bst.atu_launches;
@@ -1199,5 +1356,368 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
   }
   return AGB_OK;
 }
+
+
+// ---------------------------------------------------------------------------
+// Direct solver of the FULL path
+// ---------------------------------------------------------------------------
+__global__ void k_lu_from_system(const double* __restrict__ A, int64_t lda, int m, int n, const double* __restrict__ q,
+                                 double* __restrict__ out) {
+  // out (column-major, leading dimension m) = A_rowmajor ./ q (undo lsqr_precon's column scaling)
+  __shared__ double tile[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;  // bx: column j block, by: row i block
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int i = by + r, j = bx + threadIdx.x;
+    if (i < m && j < n) tile[r][threadIdx.x] = A[(int64_t)i * lda + j] / q[j];
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int j = bx + r, i = by + threadIdx.x;
+    if (i < m && j < n) out[(int64_t)j * m + i] = tile[threadIdx.x][r];
+  }
+}
+
+int agb_form_pre_fm(int pret, int neq, double* q, double* a, float* cpu, int* ierr) {
+  if (neq < 1 || !q || !a) return fail(nullptr, AGB_ERR_ARG, "agb_form_pre_fm: bad arguments");
+  auto t0 = std::chrono::steady_clock::now();
+  if (ierr) *ierr = 0;
+  if (pret == 1) {
+    for (int i = 0; i < neq; ++i) q[i] = 1.0 / a[(size_t)i * neq + i];  // frmdiafm(neq, 1, a, q)
+  } else if (pret == 2) {
+    cudaStream_t s = nullptr;
+    double* dA = nullptr;
+    int* dpiv = nullptr;
+    int info = 0;
+    std::string err;
+    const size_t bytes = (size_t)neq * neq * sizeof(double);
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+      return fail(nullptr, AGB_ERR_CUDA, "agb_form_pre_fm: stream");
+    bool ok = cudaMalloc(&dA, bytes) == cudaSuccess && cudaMalloc(&dpiv, neq * sizeof(int)) == cudaSuccess &&
+              cudaMemcpyAsync(dA, a, bytes, cudaMemcpyHostToDevice, s) == cudaSuccess;
+    if (ok) ok = lu_factor_dev(dA, neq, neq, dpiv, &info, s, nullptr, err);
+    std::vector<int> hp(neq);
+    if (ok) ok = cudaMemcpyAsync(a, dA, bytes, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+                 cudaMemcpyAsync(hp.data(), dpiv, neq * sizeof(int), cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+                 cudaStreamSynchronize(s) == cudaSuccess;
+    cudaFree(dA);
+    cudaFree(dpiv);
+    cudaStreamDestroy(s);
+    if (!ok) return fail(nullptr, AGB_ERR_CUDA, "agb_form_pre_fm: " + (err.empty() ? std::string("CUDA error") : err));
+    for (int i = 0; i < neq; ++i) q[i] = (double)hp[i];
+    if (ierr) *ierr = info;
+  } else if (pret != 0) {
+    return fail(nullptr, AGB_ERR_ARG, "agb_form_pre_fm: preconditioner type must be 0, 1 or 2");
+  }
+  if (cpu) *cpu += (float)std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return AGB_OK;
+}
+
+int agb_solv_eqn_fm(int slvt, int pret, int prep, int maxit, int stopt, double eps, int neq, double* q, double* a,
+                    const double* b, double* x, int* nit, double* cpu, int* ierr) {
+  (void)maxit; (void)stopt; (void)eps;  // direct solver: no iteration control
+  if (neq < 1 || !q || !a || !b || !x) return fail(nullptr, AGB_ERR_ARG, "agb_solv_eqn_fm: bad arguments");
+  if (slvt != 0) return fail(nullptr, AGB_ERR_UNSUPPORTED, "agb_solv_eqn_fm: solver type must be 0 (direct)");
+  auto t0 = std::chrono::steady_clock::now();
+  double nb = 0.0;
+  for (int i = 0; i < neq; ++i) nb += b[i] * b[i];
+  if (nb == 0.0) {  // b = 0: x = 0, nit = 0, ierr = 0
+    std::fill(x, x + neq, 0.0);
+    if (nit) *nit = 0;
+    if (ierr) *ierr = 0;
+    return AGB_OK;
+  }
+  if (pret != 0 && prep == 1) {
+    float c2 = 0.f;
+    int rc = agb_form_pre_fm(pret, neq, q, a, &c2, ierr);
+    if (rc) return rc;
+  }
+  if (pret != 2) return fail(nullptr, AGB_ERR_UNSUPPORTED, "agb_solv_eqn_fm: the direct solver needs the LU (pret 2)");
+  std::vector<int> piv(neq);
+  for (int i = 0; i < neq; ++i) {
+    piv[i] = (int)q[i];
+    if (piv[i] < 1 || piv[i] > neq) return fail(nullptr, AGB_ERR_ARG, "agb_solv_eqn_fm: q holds no LU pivots");
+  }
+  cudaStream_t s = nullptr;
+  double *dA = nullptr, *dB = nullptr;
+  std::string err;
+  const size_t bytes = (size_t)neq * neq * sizeof(double);
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(nullptr, AGB_ERR_CUDA, "agb_solv_eqn_fm: stream");
+  bool ok = cudaMalloc(&dA, bytes) == cudaSuccess && cudaMalloc(&dB, neq * sizeof(double)) == cudaSuccess &&
+            cudaMemcpyAsync(dA, a, bytes, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+            cudaMemcpyAsync(dB, b, neq * sizeof(double), cudaMemcpyHostToDevice, s) == cudaSuccess;
+  if (ok) ok = lu_solve_dev(dA, neq, neq, piv.data(), 1, dB, s, nullptr, err);
+  if (ok) ok = cudaMemcpyAsync(x, dB, neq * sizeof(double), cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+               cudaStreamSynchronize(s) == cudaSuccess;
+  cudaFree(dA);
+  cudaFree(dB);
+  cudaStreamDestroy(s);
+  if (!ok) return fail(nullptr, AGB_ERR_CUDA, "agb_solv_eqn_fm: " + (err.empty() ? std::string("CUDA error") : err));
+  if (ierr) *ierr = 0;
+  if (cpu) *cpu += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return AGB_OK;
+}
+
+int agb_solve_lu(agb_context* c, int nrhs, const double* u, double* x, int* info) {
+  int rc = check_ctx(c, true);
+  if (rc) return rc;
+  if (!c->assembled) return fail(c, AGB_ERR_STATE, "system not assembled");
+  if (c->prec != AGB_FP64) return fail(c, AGB_ERR_UNSUPPORTED, "the direct solver needs the FP64 system");
+  if (c->m != c->n) return fail(c, AGB_ERR_UNSUPPORTED, "the direct solver needs a square system");
+  if (nrhs < 1 || nrhs > AGB_MAX_RHS || !u || !x) return fail(c, AGB_ERR_ARG, "nrhs must be 1..8");
+  cudaSetDevice(c->device);
+  const int n = c->n;
+  if (!c->lu_ready) {
+    int* dpiv = nullptr;
+    CUDA_OR_FAIL(c, cudaMalloc(&c->d_lu, (size_t)n * n * sizeof(double)));
+    dim3 g((n + 31) / 32, (n + 31) / 32), b(32, 8);
+    k_lu_from_system<<<g, b, 0, c->stream>>>((const double*)c->d_A, c->lda, n, n, c->d_q, c->d_lu);
+    c->nlaunch += 1;
+    CUDA_OR_FAIL(c, cudaGetLastError());
+    CUDA_OR_FAIL(c, cudaMalloc(&dpiv, n * sizeof(int)));
+    int inf = 0;
+    std::string err;
+    const bool ok = lu_factor_dev(c->d_lu, n, n, dpiv, &inf, c->stream, &c->nlaunch, err);
+    c->lu_ipiv.resize(n);
+    const bool ok2 = ok && cudaMemcpy(c->lu_ipiv.data(), dpiv, n * sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess;
+    cudaFree(dpiv);
+    if (!ok2) return fail(c, AGB_ERR_CUDA, "lu: " + err);
+    c->lu_info = inf;
+    c->lu_ready = true;
+  }
+  if (info) *info = c->lu_info;
+  if (c->general) {
+    std::vector<double> b;
+    gather_fields(c, nrhs, u, nullptr, b, nullptr);
+    if ((rc = general_rhs(c, nrhs, b))) return rc;
+  } else {
+    int na = 0;
+    if ((rc = stage_u(c, nrhs, u, &na))) return rc;
+    if ((rc = device_rhs(c, nrhs, na))) return rc;
+  }
+  CUDA_OR_FAIL(c, ensure(c->d_x, c->cap_x, (size_t)nrhs * n));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_x, c->d_rhs, (size_t)nrhs * n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                  c->stream));
+  std::string err;
+  if (!lu_solve_dev(c->d_lu, n, n, c->lu_ipiv.data(), nrhs, c->d_x, c->stream, &c->nlaunch, err))
+    return fail(c, AGB_ERR_CUDA, "lu solve: " + err);
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(x, c->d_x, (size_t)nrhs * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  return AGB_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// MLP surrogate of the resistance tensor
+// ---------------------------------------------------------------------------
+struct agb_mlp {
+  agb::Mlp net;
+  std::string err;
+};
+
+static int mlp_fail(agb_mlp* m, int code, const std::string& msg) {
+  if (m) m->err = msg;
+  return fail(nullptr, code, msg);
+}
+
+int agb_mlp_create(agb_mlp** out, int device, int nin, int nhidden, int nout, unsigned long long seed) {
+  if (!out || nin < 1 || nhidden < 1 || nout < 1) return fail(nullptr, AGB_ERR_ARG, "agb_mlp_create: bad sizes");
+  *out = nullptr;
+  if (cudaSetDevice(device) != cudaSuccess) return fail(nullptr, AGB_ERR_CUDA, "agb_mlp_create: device");
+  agb_mlp* m = new agb_mlp();
+  m->net.nin = nin;
+  m->net.nh = nhidden;
+  m->net.nout = nout;
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess || !m->net.init(device, seed, s)) {
+    const std::string e = "agb_mlp_create: " + m->net.err;
+    if (s) cudaStreamDestroy(s);
+    delete m;
+    return fail(nullptr, AGB_ERR_CUDA, e);
+  }
+  *out = m;
+  return AGB_OK;
+}
+
+int agb_mlp_destroy(agb_mlp* m) {
+  if (!m) return AGB_OK;
+  cudaSetDevice(m->net.device);
+  cudaStream_t s = m->net.s;
+  m->net.release();
+  if (s) cudaStreamDestroy(s);
+  delete m;
+  return AGB_OK;
+}
+
+int agb_mlp_num_params(agb_mlp* m, long long* n) {
+  if (!m || !n) return AGB_ERR_ARG;
+  *n = (long long)m->net.nparams();
+  return AGB_OK;
+}
+
+int agb_mlp_get_params(agb_mlp* m, float* p) {
+  if (!m || !p) return AGB_ERR_ARG;
+  cudaSetDevice(m->net.device);
+  if (cudaMemcpy(p, m->net.params, m->net.nparams() * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return mlp_fail(m, AGB_ERR_CUDA, "agb_mlp_get_params");
+  return AGB_OK;
+}
+
+int agb_mlp_set_params(agb_mlp* m, const float* p) {
+  if (!m || !p) return AGB_ERR_ARG;
+  cudaSetDevice(m->net.device);
+  if (cudaMemcpy(m->net.params, p, m->net.nparams() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+    return mlp_fail(m, AGB_ERR_CUDA, "agb_mlp_set_params");
+  return AGB_OK;
+}
+
+int agb_mlp_set_normalization(agb_mlp* m, const float* x_mean, const float* x_std, const float* y_mean,
+                              const float* y_std) {
+  if (!m || !x_mean || !x_std || !y_mean || !y_std) return AGB_ERR_ARG;
+  const int nin = m->net.nin, nout = m->net.nout;
+  std::vector<float> h(2 * (nin + nout));
+  for (int i = 0; i < nin; ++i) {
+    if (!(x_std[i] > 0.f)) return mlp_fail(m, AGB_ERR_ARG, "x_std must be positive");
+    h[i] = x_mean[i]; h[nin + i] = x_std[i];
+  }
+  for (int i = 0; i < nout; ++i) {
+    if (!(y_std[i] > 0.f)) return mlp_fail(m, AGB_ERR_ARG, "y_std must be positive");
+    h[2 * nin + i] = y_mean[i]; h[2 * nin + nout + i] = y_std[i];
+  }
+  cudaSetDevice(m->net.device);
+  if (cudaMemcpy(m->net.norm, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+    return mlp_fail(m, AGB_ERR_CUDA, "agb_mlp_set_normalization");
+  return AGB_OK;
+}
+
+int agb_mlp_gradient(agb_mlp* m, int n, const float* X, const float* Y, int split, float* grad, double* loss) {
+  if (!m || n < 1 || !X || !Y || !grad) return AGB_ERR_ARG;
+  agb::Mlp& net = m->net;
+  cudaSetDevice(net.device);
+  float *dX = nullptr, *dY = nullptr;
+  bool ok = net.ensure_ws(n) && cudaMalloc(&dX, (size_t)n * net.nin * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&dY, (size_t)n * net.nout * sizeof(float)) == cudaSuccess &&
+            cudaMemcpyAsync(dX, X, (size_t)n * net.nin * sizeof(float), cudaMemcpyHostToDevice, net.s) == cudaSuccess &&
+            cudaMemcpyAsync(dY, Y, (size_t)n * net.nout * sizeof(float), cudaMemcpyHostToDevice, net.s) == cudaSuccess;
+  if (ok) {
+    net.load_inputs(n, dX);
+    net.forward(n, true, split != 0);
+    net.backward(n, dY, split != 0);
+    ok = cudaGetLastError() == cudaSuccess &&
+         cudaMemcpyAsync(grad, net.grads, net.nparams() * sizeof(float), cudaMemcpyDeviceToHost, net.s) == cudaSuccess;
+    if (ok && loss) *loss = net.loss_sum(n) / ((double)n * net.nout);
+    ok = ok && cudaStreamSynchronize(net.s) == cudaSuccess;
+  }
+  cudaFree(dX);
+  cudaFree(dY);
+  if (!ok) return mlp_fail(m, AGB_ERR_CUDA, "agb_mlp_gradient: " + net.err);
+  return AGB_OK;
+}
+
+__global__ void k_mlp_gather_rows(int rows, int width, const int* __restrict__ idx, const float* __restrict__ src,
+                                  float* __restrict__ dst) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)rows * width) return;
+  const int r = (int)(t / width), j = (int)(t % width);
+  dst[t] = src[(int64_t)idx[r] * width + j];
+}
+
+int agb_mlp_train(agb_mlp* m, int n, const float* X, const float* Y, int epochs, int batch, float lr,
+                  unsigned long long seed, double* loss_hist, double* stats) {
+  if (!m || n < 1 || !X || !Y || epochs < 1 || batch < 1 || !(lr > 0.f)) return AGB_ERR_ARG;
+  agb::Mlp& net = m->net;
+  cudaSetDevice(net.device);
+  batch = std::min(batch, n);
+  float *dX = nullptr, *dY = nullptr, *bX = nullptr, *bY = nullptr;
+  int* didx = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  bool ok = net.ensure_ws(batch) && cudaMalloc(&dX, (size_t)n * net.nin * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&dY, (size_t)n * net.nout * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&bX, (size_t)batch * net.nin * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&bY, (size_t)batch * net.nout * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&didx, (size_t)n * sizeof(int)) == cudaSuccess &&
+            cudaMemcpyAsync(dX, X, (size_t)n * net.nin * sizeof(float), cudaMemcpyHostToDevice, net.s) == cudaSuccess &&
+            cudaMemcpyAsync(dY, Y, (size_t)n * net.nout * sizeof(float), cudaMemcpyHostToDevice, net.s) == cudaSuccess;
+  std::vector<int> perm(n);
+  for (int i = 0; i < n; ++i) perm[i] = i;
+  std::mt19937_64 rng(seed);
+  const long l0 = net.launches;
+  cudaEventRecord(e0, net.s);
+  for (int ep = 0; ok && ep < epochs; ++ep) {
+    std::shuffle(perm.begin(), perm.end(), rng);
+    ok = cudaMemcpyAsync(didx, perm.data(), n * sizeof(int), cudaMemcpyHostToDevice, net.s) == cudaSuccess;
+    double se = 0.0;
+    for (int b0 = 0; ok && b0 + batch <= n; b0 += batch) {  // full batches only
+      k_mlp_gather_rows<<<(unsigned)(((int64_t)batch * net.nin + 255) / 256), 256, 0, net.s>>>(batch, net.nin,
+                                                                                                 didx + b0, dX, bX);
+      k_mlp_gather_rows<<<(unsigned)(((int64_t)batch * net.nout + 255) / 256), 256, 0, net.s>>>(batch, net.nout,
+                                                                                                  didx + b0, dY, bY);
+      net.launches += 2;
+      net.load_inputs(batch, bX);
+      net.forward(batch, true, false);
+      net.backward(batch, bY, false);
+      net.adam(lr);
+      se += net.loss_sum(batch);
+      ok = cudaGetLastError() == cudaSuccess;
+    }
+    if (loss_hist) loss_hist[ep] = se / ((double)(n / batch) * batch * net.nout);
+    cudaStreamSynchronize(net.s);  // the host permutation is rewritten next epoch
+  }
+  cudaEventRecord(e1, net.s);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaFree(dX); cudaFree(dY); cudaFree(bX); cudaFree(bY); cudaFree(didx);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (!ok) return mlp_fail(m, AGB_ERR_CUDA, "agb_mlp_train: " + net.err);
+  if (stats) {
+    stats[0] = ms;
+    stats[1] = (double)(net.launches - l0);
+    stats[2] = (double)net.step;
+  }
+  return AGB_OK;
+}
+
+int agb_mlp_predict(agb_mlp* m, int n, const float* X, float* Y, int split, double* device_ms) {
+  if (!m || n < 0 || (n > 0 && (!X || !Y))) return AGB_ERR_ARG;
+  if (n == 0) return AGB_OK;
+  agb::Mlp& net = m->net;
+  cudaSetDevice(net.device);
+  const int chunk = std::min(n, 1 << 17);
+  float *dX = nullptr, *dY = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  bool ok = net.ensure_ws(chunk) && cudaMalloc(&dX, (size_t)n * net.nin * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&dY, (size_t)n * net.nout * sizeof(float)) == cudaSuccess &&
+            cudaMemcpyAsync(dX, X, (size_t)n * net.nin * sizeof(float), cudaMemcpyHostToDevice, net.s) == cudaSuccess;
+  if (ok) {
+    cudaEventRecord(e0, net.s);
+    for (int r0 = 0; r0 < n; r0 += chunk) {
+      const int rows = std::min(chunk, n - r0);
+      net.load_inputs(rows, dX + (size_t)r0 * net.nin);
+      net.forward(rows, false, split != 0);
+      net.output(rows, dY + (size_t)r0 * net.nout);
+    }
+    cudaEventRecord(e1, net.s);
+    ok = cudaGetLastError() == cudaSuccess &&
+         cudaMemcpyAsync(Y, dY, (size_t)n * net.nout * sizeof(float), cudaMemcpyDeviceToHost, net.s) == cudaSuccess &&
+         cudaStreamSynchronize(net.s) == cudaSuccess;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (device_ms) *device_ms = ms;
+  }
+  cudaFree(dX);
+  cudaFree(dY);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (!ok) return mlp_fail(m, AGB_ERR_CUDA, "agb_mlp_predict: " + net.err);
+  return AGB_OK;
+}
+
+long long agb_mlp_launches(agb_mlp* m) { return m ? (long long)m->net.launches : 0; }
 
 }  // extern "C"

@@ -290,10 +290,16 @@ __device__ __forceinline__ double wsum(double v) {
 
 template <typename T>
 __global__ void k_stokes_rhs(StokesRhsArgs a) {
+  // barycentric coordinates of the rule in T (the points themselves come from
+  // the expanded table, computed there in FP64 and rounded once)
+  __shared__ T sL[3][AGB_MAX_Q];
+  for (int t = threadIdx.x; t < 3 * a.Q; t += blockDim.x) sL[t / a.Q][t % a.Q] = (T)a.rule_l[t];
+  __syncthreads();
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const int i = warp;
   if (i >= a.ne) return;
+  const QPt<T>* __restrict__ pts = static_cast<const QPt<T>*>(a.pts);
   const ElemGeom& Gi = a.geom[i];
   const T sx = (T)Gi.c[0], sy = (T)Gi.c[1], sz = (T)Gi.c[2];
   const int Q = a.Q;
@@ -317,17 +323,14 @@ __global__ void k_stokes_rhs(StokesRhsArgs a) {
 #pragma unroll
     for (int c = 0; c < AGB_MAX_RHS; ++c) pe[c][0] = pe[c][1] = pe[c][2] = T(0);
     for (int q = 0; q < Q; ++q) {
-      const double l1 = a.rule_l[q], l2 = a.rule_l[Q + q], l3 = a.rule_l[2 * Q + q];
-      const T px = (T)(l1 * G.v[0][0] + l2 * G.v[1][0] + l3 * G.v[2][0]);
-      const T py = (T)(l1 * G.v[0][1] + l2 * G.v[1][1] + l3 * G.v[2][1]);
-      const T pz = (T)(l1 * G.v[0][2] + l2 * G.v[1][2] + l3 * G.v[2][2]);
-      const T w = (T)(a.rule_w[q] * G.area);
-      const T rx = px - sx, ry = py - sy, rz = pz - sz;
+      const QPt<T> P = pts[(int64_t)q * a.ldp + e];
+      const T w = P.w;
+      const T rx = P.x - sx, ry = P.y - sy, rz = P.z - sz;
       const T r2 = rx * rx + ry * ry + rz * rz;
       const T ir = rsq<T>(r2);
       const T ir2 = ir * ir;
       const T cn = T(-6) * w * (rx * nx + ry * ny + rz * nz) * (ir2 * ir2 * ir);
-      const T L1 = (T)l1, L2 = (T)l2, L3 = (T)l3;
+      const T L1 = sL[0][q], L2 = sL[1][q], L3 = sL[2][q];
 #pragma unroll
       for (int c = 0; c < AGB_MAX_RHS; ++c) {
         if (c < a.k) {
@@ -368,6 +371,7 @@ __global__ void __launch_bounds__(256) k_stokes_freeterm(StokesRhsArgs a, double
   const int t = blockIdx.x;  // index into the active list
   const int i = a.active[t];
   const int e0 = blockIdx.y * FT_CHUNK;
+  const QPt<T>* __restrict__ pts = static_cast<const QPt<T>*>(a.pts);
   const ElemGeom& Gi = a.geom[i];
   const T sx = (T)Gi.c[0], sy = (T)Gi.c[1], sz = (T)Gi.c[2];
   const int Q = a.Q;
@@ -378,12 +382,9 @@ __global__ void __launch_bounds__(256) k_stokes_freeterm(StokesRhsArgs a, double
     const T nx = (T)(G.multi * G.n[0]), ny = (T)(G.multi * G.n[1]), nz = (T)(G.multi * G.n[2]);
     T s0 = T(0), s1 = T(0), s2 = T(0);
     for (int q = 0; q < Q; ++q) {
-      const double l1 = a.rule_l[q], l2 = a.rule_l[Q + q], l3 = a.rule_l[2 * Q + q];
-      const T px = (T)(l1 * G.v[0][0] + l2 * G.v[1][0] + l3 * G.v[2][0]);
-      const T py = (T)(l1 * G.v[0][1] + l2 * G.v[1][1] + l3 * G.v[2][1]);
-      const T pz = (T)(l1 * G.v[0][2] + l2 * G.v[1][2] + l3 * G.v[2][2]);
-      const T w = (T)(a.rule_w[q] * G.area);
-      const T rx = px - sx, ry = py - sy, rz = pz - sz;
+      const QPt<T> P = pts[(int64_t)q * a.ldp + e];
+      const T w = P.w;
+      const T rx = P.x - sx, ry = P.y - sy, rz = P.z - sz;
       const T r2 = rx * rx + ry * ry + rz * rz;
       const T ir = rsq<T>(r2);
       const T ir2 = ir * ir;

@@ -39,6 +39,7 @@ cudaError_t launch_stokes_self(int ne, const ElemGeom* geom, double diff, T* A, 
 // rigid-body free term) for k velocity fields given at nodes u[c][3][nnodes].
 struct StokesRhsArgs {
   int ne, Q, ldp, k, nnodes;
+  const void* pts;           // QPt<T>[Q][ldp] of launch_expand_points (same T as the launch)
   const ElemGeom* geom;
   const double* rule_l;      // [3][Q]
   const double* rule_w;      // [Q]

@@ -50,6 +50,11 @@ bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, i
 bool batch_autotune(const std::vector<BatchBody>& bodies, cudaStream_t s, BatchTune& best, std::string& report,
                     std::string& err);
 
+// lsqr_precon column scaling (q_j = 1/||A(:,j)||, A <- A diag(q)) of one FP32
+// matrix, partial sums of `groups` row groups in P (groups x lda doubles).
+cudaError_t dense_colscale_f32(float* A, int64_t lda, int m, int n, double* q, double* P, int groups,
+                               cudaStream_t s);
+
 // 2-D tensor map of a row-major FP32 matrix (dims {lda, m}, box box_cols x box_rows).
 bool make_tensor_map_2d(CUtensorMap* tm, const void* A, int64_t lda, int m, int box_cols, int box_rows,
                         std::string& err);

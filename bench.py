@@ -48,10 +48,18 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=1)
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "batch"],
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "batch", "surrogate"],
                     help="sphere: one level-5 sphere (default); batch: the many-body superellipsoid set")
     ap.add_argument("--bodies", type=int, default=512, help="batch workload: number of bodies")
     ap.add_argument("--fp64-sample", type=int, default=6, help="batch workload: bodies solved on the FP64 path")
+    ap.add_argument("--batch-eps", type=float, default=3e-8,
+                    help="batch workload: LSQR eps (3e-8 keeps every sampled body within 1e-6 of FP64)")
+    ap.add_argument("--no-autotune", action="store_true", help="batch workload: default tile shapes")
+    ap.add_argument("--train-bodies", type=int, default=20000, help="surrogate: BEM tensors to train on")
+    ap.add_argument("--sur-elements", type=int, default=300, help="surrogate: triangles per training body")
+    ap.add_argument("--queries", type=int, default=1000000, help="surrogate: inference batch")
+    ap.add_argument("--audit", type=float, default=0.01, help="surrogate: fraction of queries re-solved by the BEM")
+    ap.add_argument("--epochs", type=int, default=600, help="surrogate: training epochs")
     return ap.parse_args()
 
 
@@ -244,9 +252,11 @@ def run_batch(args, rank, world, local):
     meshes, params = M.batch_bodies(n_bodies=args.bodies)
     mine = [m for i, m in enumerate(meshes) if i % world == rank]
     ctx = A.Context(local if world > 1 else 0)
+    eps = args.batch_eps
+    tune = not args.no_autotune
     warm = mine[:32]
     for _ in range(args.warmup):
-        A.batch_resistance(warm, eps=args.eps, ctx=ctx)
+        A.batch_resistance(warm, eps=eps, ctx=ctx, autotune=tune)
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
@@ -254,7 +264,7 @@ def run_batch(args, rank, world, local):
         t0 = time.perf_counter()
         Rs, nits, istops, sts = [], [], [], []
         for _ in range(args.steps):
-            R, nit, istop, st = A.batch_resistance(mine, eps=args.eps, ctx=ctx)
+            R, nit, istop, st = A.batch_resistance(mine, eps=eps, ctx=ctx, autotune=tune)
             Rs.append(R); nits.append(nit); istops.append(istop); sts.append(st)
         t1 = time.perf_counter()
     dev_s = sum(st["device_ms"] for st in sts) / 1000.0
@@ -278,16 +288,16 @@ def run_batch(args, rank, world, local):
             C = A.Context(0)
             C.set_mesh(mine[i])
             C.set_problem(A.STOKES, [1, 2], A.dirichlet_known(A.STOKES, 2), itri=5)
-            _, _, info = C.resistance_tensor(A.FP64, 1, 2, eps=args.eps)
+            _, _, info = C.resistance_tensor(A.FP64, 1, 2, eps=eps)
             t64.append(info["device_ms"])
-            Rt, _, _ = C.resistance_tensor(A.FP64, 1, 2, eps=args.eps * 1e-3)
+            Rt, _, _ = C.resistance_tensor(A.FP64, 1, 2, eps=eps * 1e-3)
             errs.append(float(np.max(np.abs(R[i] - Rt)) / np.max(np.abs(Rt))))
             C.close()
         rate64 = len(pick) / (sum(t64) / 1000.0)
         fp64 = {"solves_per_s": rate64, "sample_bodies": pick,
                 "sample_elements": [int(params[i][4]) for i in pick], "ms_per_body": t64,
                 "ratio_mixed_batched_over_fp64": value / world / rate64,
-                "truth": f"FP64 assembly + FP64 LSQR to eps {args.eps * 1e-3:g}"}
+                "truth": f"FP64 assembly + FP64 LSQR to eps {eps * 1e-3:g}"}
         rel_err = max(errs)
     else:
         errs, rel_err = None, None
@@ -304,7 +314,7 @@ def run_batch(args, rank, world, local):
                 "config": {"workload": f"{args.bodies} superellipsoids a=1, b,c~U(0.2,1), e1,e2~U(0.3,1.8), "
                                        f"random orientation, {int(ne.min())}..{int(ne.max())} tri (mean "
                                        f"{ne.mean():.0f}), each in an L2 container r=200, 6 RHS, ITRI 5, "
-                                       f"LSQR eps {args.eps:g}",
+                                       f"LSQR eps {eps:g}",
                            "precision": "mixed", "parallelism": "bodies split over ranks" if world > 1 else
                            "single GPU", "l2": "inputs larger than L2 (waves of tens of GB), no flush",
                            "warmup": f"{args.warmup} x the first {len(warm)} bodies"},
@@ -329,12 +339,91 @@ def run_batch(args, rank, world, local):
     ctx.close()
 
 
+def run_surrogate(args):
+    """Learned part: BEM tensors of superellipsoids (batched mixed BEM) train the
+    MLP on the GPU; one batch of queries is answered by it (BEM outside the
+    training hull), and a random audit fraction is re-solved by the BEM."""
+    import numpy as np
+    from andromeda_gb300 import surrogate as S
+    bem = dict(n_elem=args.sur_elements, outer_level=1, outer_radius=20.0, eps=args.batch_eps)
+    t0 = time.perf_counter()
+    P = S.sample_params(args.train_bodies, seed=20260101)
+    R, st_bem = S.bem_tensors(P, **bem)
+    t1 = time.perf_counter()
+    sur = S.Surrogate(device=0, seed=7, bem_kwargs=bem)
+    ntr = int(0.95 * len(P))
+    hist, st_tr = sur.fit(P[:ntr], R[:ntr], epochs=args.epochs, batch=512, lr=2e-3, lr_final=2e-5)
+    t2 = time.perf_counter()
+    Rv, inv, _ = sur.predict(P[ntr:], bem=False)
+    val_err = S.rel_err(Rv[inv], R[ntr:][inv])
+    Q = S.sample_params(args.queries, seed=99)
+    Xq = S.features(Q)
+    for _ in range(max(args.warmup, 1)):
+        sur.net.predict(Xq[:65536])
+    with ClockSampler(0) as clk:
+        times = []
+        for _ in range(max(args.steps, 1)):
+            _, ms = sur.net.predict(Xq)
+            times.append(ms)
+    inside = sur.hull.contains(Xq)
+    t3 = time.perf_counter()
+    Rq, inq, info_q = sur.predict(Q)  # in-hull by the MLP, the rest by the BEM
+    t4 = time.perf_counter()
+    aud, idx, ain, st_aud = sur.audit(Q, frac=args.audit, seed=3)
+    t5 = time.perf_counter()
+    ms = statistics.median(times)
+    flops = 2.0 * (5 * 256 + 2 * 256 * 256 + 256 * 21) * args.queries * 3  # split-BF16: three products per GEMM
+    peak, peak_kind = measured_peaks()
+    bf16 = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            bf16 = json.load(f).get("bf16_tflops")
+    except Exception:
+        pass
+    bem_rate = len(P) / (st_bem["device_ms"] / 1000.0)
+    line = {"metric": "surrogate resistance-tensor inferences/s (MLP 5-256-256-256-21, BEM fallback out of hull)",
+            "value": args.queries / (ms / 1000.0), "unit": "inferences/s", "n_gpus": 1, "steps": max(args.steps, 1),
+            "warmup": max(args.warmup, 1), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 tensor cores (split hi+lo, fp32 accumulation)",
+            "data": "synthetic (shapes b,c~U(0.2,1), e1,e2~U(0.3,1.8), seeds 20260101 / 99)",
+            "config": {"workload": f"{args.queries} queries; trained on {ntr} BEM tensors ({args.sur_elements}-triangle "
+                                   f"superellipsoids in L1 containers r=20, LSQR eps {args.batch_eps:g})",
+                       "epochs": args.epochs, "batch": 512},
+            "bem_training_set": {"bodies": len(P), "bem_solves_per_s": bem_rate, "host_s": t1 - t0},
+            "training": {"device_ms": st_tr["device_ms"], "launches": st_tr["launches"],
+                         "adam_steps": st_tr["adam_steps"], "loss_first": float(hist[0]),
+                         "loss_last": float(hist[-1]), "host_s": t2 - t1},
+            "validation_rel_err": {"median": float(np.median(val_err)), "p95": float(np.percentile(val_err, 95)),
+                                   "max": float(np.max(val_err)), "n": int(len(val_err))},
+            "queries_in_hull": int(inside.sum()), "queries_bem_fallback": int(info_q["n_bem"]),
+            "predict_all_host_s": t4 - t3,
+            "audit": {"fraction": args.audit, "n": int(len(idx)), "in_hull": int(ain.sum()),
+                      "rel_err_median": float(np.median(aud)) if len(aud) else None,
+                      "rel_err_p95": float(np.percentile(aud, 95)) if len(aud) else None,
+                      "rel_err_max": float(np.max(aud)) if len(aud) else None,
+                      "within_1e-3": float(np.mean(aud <= 1e-3)) if len(aud) else None, "host_s": t5 - t4},
+            "speedup_over_bem": (args.queries / (ms / 1000.0)) / bem_rate,
+            "roofline": {"bound": "tensor", "achieved": flops / (ms * 1e-3) / 1e12, "peak": bf16, "unit": "TFLOP/s",
+                         "frac": (flops / (ms * 1e-3) / 1e12 / bf16) if bf16 else None, "traffic": None,
+                         "peak_source": "measured bf16 (cuBLAS burst)" if bf16 else None,
+                         "note": "mma.sync m16n8k16 bf16; split mode counts its three products"},
+            "cpu_baseline": None, "clocks": clk.summary(), "gpu_launches": int(sur.net._L.agb_mlp_launches(sur.net.h)),
+            "e2e": {"value": args.queries / (t4 - t3), "unit": "inferences/s (predict with hull check, host arrays)",
+                    "h2d_bytes_per_step": int(args.queries * 5 * 4), "d2h_bytes_per_step": int(args.queries * 21 * 4)}}
+    print(json.dumps(line), flush=True)
+    sur.net.close()
+
+
 # ---------------------------------------------------------------------------
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.workload == "surrogate":
+        if rank == 0:
+            run_surrogate(args)
         return
     if args.workload == "batch":
         if world > 1:

@@ -247,6 +247,57 @@ int agb_batch_resistance(agb_context* ctx, int nbodies, const int* node_off, con
                          int itri, int maxit, double eps, double mem_gb, int autotune, double* R, int* nit,
                          int* istop, double* stats);
 
+/* Direct solver of the FULL path (LINPACK LU, FP64, on the GPU).
+ * agb_form_pre_fm replaces FormPREfm(pret,neq,q,a,cpu,ierr) (lib_solveFM.f:102):
+ *   pret 0 none; 1 diagonal, q = 1/a(i,i) (frmdiafm); 2 LU with partial pivoting
+ *   (dgefa, lib_solveFM.f:198) of the column-major neq x neq matrix a in place,
+ *   q = 1-based pivot rows as doubles, ierr = index of the first zero pivot or 0.
+ *   The pivots are dgefa's (same elimination order and tie rule); the factors
+ *   are stored in LAPACK form (positive multipliers, later interchanges applied
+ *   to L) and are meant for agb_solv_eqn_fm only.  cpu += elapsed seconds.
+ * agb_solv_eqn_fm replaces SolvEQNfm(slvt,pret,prep,maxit,stopt,eps,neq,q,a,b,
+ *   x,nit,cpu,ierr) (lib_solveFM.f:3): slvt 0 (direct) only; b = 0 gives x = 0,
+ *   nit = 0; prep 1 factors inside (as FormPREfm), prep 2 uses a/q from
+ *   agb_form_pre_fm; x = A^-1 b (dgesl, lib_solveFM.f:318).  maxit, stopt and eps
+ *   are ignored by the direct solver, as in the reference.
+ * agb_solve_lu: the same direct solve for the context's assembled FP64 square
+ *   system (the FULL path after CoR_Integrals: lib_StokesFull.f90:566-570,
+ *   lib_particle.f90:549,614): factors the unscaled system once per assembly,
+ *   then solves nrhs fields given as in agb_solve; x has agb_solve's layout;
+ *   info = first zero pivot or 0. */
+int agb_form_pre_fm(int pret, int neq, double* q, double* a, float* cpu, int* ierr);
+int agb_solv_eqn_fm(int slvt, int pret, int prep, int maxit, int stopt, double eps, int neq, double* q, double* a,
+                    const double* b, double* x, int* nit, double* cpu, int* ierr);
+int agb_solve_lu(agb_context* ctx, int nrhs, const double* u, double* x, int* info);
+
+/* MLP surrogate of the resistance tensor (no reference counterpart; the
+ * learned part of the many-body workflow): nin -> nhidden -> nhidden -> nhidden
+ * -> nout with SiLU, FP32 master weights, BF16 tensor-core GEMMs with FP32
+ * accumulation (split-BF16 hi+lo products on request), Adam.  Inputs and
+ * outputs are row-major float arrays (n x nin, n x nout) in physical units; the
+ * network works on (x - x_mean)/x_std and predicts (y - y_mean)/y_std.
+ * Parameters (agb_mlp_get/set_params, agb_mlp_gradient): W1 [nh][nin], b1,
+ * W2 [nh][nh], b2, W3 [nh][nh], b3, W4 [nout][nh], b4, concatenated.
+ * agb_mlp_gradient: one forward + backward of the mean squared normalised
+ * error on n rows (split != 0: split-BF16 products); gradient and loss out.
+ * agb_mlp_train: epochs over n rows in shuffled mini-batches (full batches
+ * only), loss_hist[epoch] = mean squared normalised error; stats[3]: device ms,
+ * kernel launches, Adam steps so far.  agb_mlp_predict: device_ms = kernel
+ * time of the n inferences. */
+typedef struct agb_mlp agb_mlp;
+int agb_mlp_create(agb_mlp** out, int device, int nin, int nhidden, int nout, unsigned long long seed);
+int agb_mlp_destroy(agb_mlp* m);
+int agb_mlp_num_params(agb_mlp* m, long long* n);
+int agb_mlp_get_params(agb_mlp* m, float* p);
+int agb_mlp_set_params(agb_mlp* m, const float* p);
+int agb_mlp_set_normalization(agb_mlp* m, const float* x_mean, const float* x_std, const float* y_mean,
+                              const float* y_std);
+int agb_mlp_gradient(agb_mlp* m, int n, const float* X, const float* Y, int split, float* grad, double* loss);
+int agb_mlp_train(agb_mlp* m, int n, const float* X, const float* Y, int epochs, int batch, float lr,
+                  unsigned long long seed, double* loss_hist, double* stats);
+int agb_mlp_predict(agb_mlp* m, int n, const float* X, float* Y, int split, double* device_ms);
+long long agb_mlp_launches(agb_mlp* m);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1453,6 +1453,72 @@ using namespace orc;
 // =============================================================================
 // C API used by the tests (ctypes)
 // =============================================================================
+// -----------------------------------------------------------------------------
+// LINPACK direct solver of the FULL path (lib_solveFM.f): dgefa :198, dgesl
+// :318, with the reference-BLAS idamax (first index of the largest |x|), dscal
+// and daxpy.  a is column-major a(lda, n); ipvt holds 1-based pivot rows as
+// doubles (the reference declares it REAL(8)).
+// -----------------------------------------------------------------------------
+static int linpack_dgefa(double* a, int lda, int n, double* ipvt) {
+  auto A = [&](int i, int j) -> double& { return a[(size_t)(j - 1) * lda + (i - 1)]; };  // 1-based
+  int info = 0;
+  const int nm1 = n - 1;
+  for (int k = 1; k <= nm1; ++k) {
+    const int kp1 = k + 1;
+    // l = idamax(n-k+1, a(k,k), 1) + k - 1
+    int l = k;
+    double dmax = std::fabs(A(k, k));
+    for (int i = k + 1; i <= n; ++i)
+      if (std::fabs(A(i, k)) > dmax) { dmax = std::fabs(A(i, k)); l = i; }
+    ipvt[k - 1] = (double)l;
+    if (A(l, k) == 0.0) { info = k; continue; }
+    if (l != k) std::swap(A(l, k), A(k, k));
+    double t = -1.0 / A(k, k);
+    for (int i = k + 1; i <= n; ++i) A(i, k) *= t;  // dscal(n-k, t, a(k+1,k), 1)
+    for (int j = kp1; j <= n; ++j) {
+      t = A(l, j);
+      if (l != k) { A(l, j) = A(k, j); A(k, j) = t; }
+      for (int i = k + 1; i <= n; ++i) A(i, j) += t * A(i, k);  // daxpy(n-k, t, a(k+1,k), 1, a(k+1,j), 1)
+    }
+  }
+  ipvt[n - 1] = (double)n;
+  if (A(n, n) == 0.0) info = n;
+  return info;
+}
+static void linpack_dgesl(const double* a, int lda, int n, const double* ipvt, double* b, int job) {
+  auto A = [&](int i, int j) { return a[(size_t)(j - 1) * lda + (i - 1)]; };
+  auto B = [&](int i) -> double& { return b[i - 1]; };
+  const int nm1 = n - 1;
+  if (job == 0) {
+    for (int k = 1; k <= nm1; ++k) {
+      const int l = (int)ipvt[k - 1];
+      const double t = B(l);
+      if (l != k) { B(l) = B(k); B(k) = t; }
+      for (int i = k + 1; i <= n; ++i) B(i) += t * A(i, k);
+    }
+    for (int kb = 1; kb <= n; ++kb) {
+      const int k = n + 1 - kb;
+      B(k) = B(k) / A(k, k);
+      const double t = -B(k);
+      for (int i = 1; i <= k - 1; ++i) B(i) += t * A(i, k);
+    }
+  } else {
+    for (int k = 1; k <= n; ++k) {
+      double t = 0.0;
+      for (int i = 1; i <= k - 1; ++i) t += A(i, k) * B(i);
+      B(k) = (B(k) - t) / A(k, k);
+    }
+    for (int kb = 1; kb <= nm1; ++kb) {
+      const int k = n - kb;
+      double t = 0.0;
+      for (int i = k + 1; i <= n; ++i) t += A(i, k) * B(i);
+      B(k) += t;
+      const int l = (int)ipvt[k - 1];
+      if (l != k) std::swap(B(l), B(k));
+    }
+  }
+}
+
 extern "C" {
 
 int orc_wx_rule(int itri, double* l1, double* l2, double* l3, double* w) {
@@ -1816,4 +1882,10 @@ void orc_set_threads(int n) {
 #endif
 }
 
+
+// dgefa / dgesl (lib_solveFM.f:198,318) for the direct-solver checks.
+int orc_dgefa(double* a, int lda, int n, double* ipvt) { return linpack_dgefa(a, lda, n, ipvt); }
+void orc_dgesl(const double* a, int lda, int n, const double* ipvt, double* b, int job) {
+  linpack_dgesl(a, lda, n, ipvt, b, job);
+}
 }  // extern "C"

@@ -51,6 +51,9 @@ def lib():
                                          C.c_int, C.c_int]
         L.orc_problem_create.restype = C.c_void_p
         L.orc_problem_destroy.argtypes = [C.c_void_p]
+        L.orc_dgefa.argtypes = [dp, C.c_int, C.c_int, dp]
+        L.orc_dgefa.restype = C.c_int
+        L.orc_dgesl.argtypes = [dp, C.c_int, C.c_int, dp, dp, C.c_int]
         L.orc_problem_set_integration.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int]
         L.orc_tri_lap_opt.argtypes = [C.c_int, dp, dp, dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, dp]
         L.orc_tri_stk_opt.argtypes = [C.c_int, dp, dp, dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, dp]
@@ -142,6 +145,27 @@ def tri_stk_opt(itri, v, s, n, isrc=0, sing=0, rdepth=20, near_eta=0.0, near_dep
     lib().orc_tri_stk_opt(itri, np.ascontiguousarray(v, float).ravel(), np.ascontiguousarray(s, float),
                           np.ascontiguousarray(n, float), isrc, sing, rdepth, near_eta, near_depth, out)
     return out
+
+
+def dgefa(a):
+    """LINPACK LU (lib_solveFM.f:198) of a square matrix: returns (factors in
+    LINPACK storage, ipvt 1-based as float64, info)."""
+    a = np.array(a, dtype=np.float64, order="F", copy=True)
+    n = a.shape[0]
+    ipvt = np.zeros(n)
+    flat = a.ravel(order="F")
+    info = lib().orc_dgefa(flat, n, n, ipvt)
+    return flat.reshape((n, n), order="F"), ipvt, int(info)
+
+
+def dgesl(f, ipvt, b, job=0):
+    """LINPACK solve (lib_solveFM.f:318) with dgefa's output."""
+    f = np.asarray(f, dtype=np.float64)
+    n = f.shape[0]
+    flat = np.ascontiguousarray(f.ravel(order="F"))
+    x = np.array(b, dtype=np.float64, copy=True)
+    lib().orc_dgesl(flat, n, n, np.ascontiguousarray(ipvt, dtype=np.float64), x, int(job))
+    return x
 
 
 class Problem:

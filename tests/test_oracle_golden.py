@@ -263,3 +263,45 @@ def test_near_singular_rule_against_high_order_reference(orc, height):
     # far from the element the rule changes nothing
     far = np.array([0.4, 0.3, 3.0])
     assert np.array_equal(orc.tri_lap_opt(5, v, far, n), orc.tri_lap_opt(5, v, far, n, 0, 0, 0, 1.5, 12))
+
+
+def test_linpack_direct_solver(orc):
+    """dgefa/dgesl restatement (lib_solveFM.f:198,318): pivots and U agree with
+    an independent LU with partial pivoting (scipy/LAPACK getrf), the solves
+    of A x = b and A^T x = b are exact to round-off, and a zero column is
+    reported through info."""
+    sl = pytest.importorskip("scipy.linalg")
+    rng = np.random.default_rng(3)
+    n = 60
+    A = rng.normal(size=(n, n))
+    b = rng.normal(size=n)
+    f, ipvt, info = orc.dgefa(A)
+    lu, piv = sl.lu_factor(A)
+    assert info == 0
+    assert np.array_equal(ipvt.astype(int), piv + 1)
+    assert np.max(np.abs(np.triu(f) - np.triu(lu))) < 1e-12 * np.max(np.abs(lu))
+    assert np.max(np.abs(A @ orc.dgesl(f, ipvt, b) - b)) < 1e-12 * n
+    assert np.max(np.abs(A.T @ orc.dgesl(f, ipvt, b, job=1) - b)) < 1e-12 * n
+    A[:, 7] = 0.0
+    _, _, info = orc.dgefa(A)
+    assert info == 8
+
+
+def test_mlp_oracle_gradient_by_finite_differences():
+    """The FP64 MLP oracle's backward pass against central differences."""
+    import mlp_oracle as mo
+    rng = np.random.default_rng(0)
+    nin, nh, nout = 5, 7, 4
+    npar = nh * nin + nh + 2 * (nh * nh + nh) + nout * nh + nout
+    p = rng.normal(scale=0.4, size=npar)
+    X = rng.normal(size=(9, nin))
+    T = rng.normal(size=(9, nout))
+    args = (X, T, np.zeros(nin), np.ones(nin), np.zeros(nout), np.ones(nout), nin, nh, nout)
+    _, g = mo.loss_and_grad(p, *args)
+    h = 1e-6
+    fd = np.zeros(npar)
+    for i in range(npar):
+        e = np.zeros(npar)
+        e[i] = h
+        fd[i] = (mo.loss_and_grad(p + e, *args)[0] - mo.loss_and_grad(p - e, *args)[0]) / (2 * h)
+    assert np.max(np.abs(fd - g)) < 1e-8 * max(1.0, np.max(np.abs(g)))
