@@ -21,7 +21,7 @@ import numpy as np
 from ._lib import AgbError, load
 
 LAPLACE, STOKES = 1, 2
-FP64, MIXED = 0, 1
+FP64, MIXED, MATRIX_FREE = 0, 1, 2
 BC_FUNCTION, BC_FLUX, BC_CONTACT = 1, 2, 3
 
 

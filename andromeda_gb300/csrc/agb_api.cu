@@ -7,6 +7,7 @@
 #include "agb_batch.cuh"
 #include "agb_lu.cuh"
 #include "agb_mlp.cuh"
+#include "agb_mfree.cuh"
 #include <random>
 #include "quad_tables.h"
 
@@ -35,6 +36,8 @@ struct agb_context {
   // problem
   int kind = 0, neq = 0;
   IntegOpt iopt;  // triangle integration options (agb_set_integration)
+  MfOp mfop;                   // matrix-free operator (AGB_MATRIX_FREE)
+  float* d_self6 = nullptr;
   double* d_lu = nullptr;      // column-major LU factors of the unscaled FP64 system (agb_solve_lu)
   std::vector<int> lu_ipiv;    // its pivots (1-based)
   bool lu_ready = false;
@@ -165,6 +168,8 @@ cudaError_t ensure(T*& p, size_t& cap, size_t count) {
 }
 
 void free_system(agb_context* c) {
+  dfree(c->d_self6);
+  c->lsqr.mf = nullptr;
   dfree(c->d_lu);
   c->lu_ready = false;
   dfree(c->d_rhsM);
@@ -343,7 +348,7 @@ int device_rhs(agb_context* c, int nrhs, int na) {
     a.geom = c->d_geom; a.rule_l = c->rule.l; a.rule_w = c->rule.w; a.u = c->d_u;
     a.active = c->d_active; a.na = na; a.row_active = c->d_rowact; a.rhs = c->d_rhs;
     cudaEventRecord(c->tev[2], c->stream);
-    if (c->prec == AGB_MIXED) CUDA_OR_FAIL(c, launch_stokes_rhs<float>(a, c->stream));
+    if (c->prec != AGB_FP64) CUDA_OR_FAIL(c, launch_stokes_rhs<float>(a, c->stream));
     else CUDA_OR_FAIL(c, launch_stokes_rhs<double>(a, c->stream));
     cudaEventRecord(c->tev[3], c->stream);
     c->nlaunch += (na > 0) ? 3 : 1;
@@ -366,8 +371,8 @@ int device_rhs(agb_context* c, int nrhs, int na) {
 int assemble_general(agb_context* c, int precision);
 int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int refine, int* nit, int* istop,
              bool x0_zero) {
-  if (!c->lsqr.A || c->lsqr.k != nrhs) {
-    if (!c->lsqr.setup(c->d_A, c->prec == AGB_MIXED, c->m, c->n, c->lda, nrhs, c->stream))
+  if ((!c->lsqr.A && !c->lsqr.mf) || c->lsqr.k != nrhs) {
+    if (!c->lsqr.setup(c->d_A, c->prec != AGB_FP64, c->m, c->n, c->lda, nrhs, c->stream))
       return fail(c, AGB_ERR_CUDA, "lsqr setup: " + c->lsqr.err);
   }
   std::vector<int> nt(nrhs, 0), is(nrhs, 0);
@@ -669,11 +674,49 @@ int agb_system_size(agb_context* c, int* m, int* n) {
 int agb_assemble(agb_context* c, int precision) {
   int rc = check_ctx(c, true);
   if (rc) return rc;
-  if (precision != AGB_FP64 && precision != AGB_MIXED) return fail(c, AGB_ERR_ARG, "precision must be AGB_FP64 or AGB_MIXED");
+  if (precision != AGB_FP64 && precision != AGB_MIXED && precision != AGB_MATRIX_FREE)
+    return fail(c, AGB_ERR_ARG, "precision must be AGB_FP64, AGB_MIXED or AGB_MATRIX_FREE");
   const bool fast = c->all_dirichlet && c->iopt.is_default() &&
                     ((c->kind == AGB_LAPLACE && precision == AGB_FP64) || (c->kind == AGB_STOKES && c->all_tri));
   cudaSetDevice(c->device);
   free_system(c);
+  if (precision == AGB_MATRIX_FREE) {
+    if (!(fast && c->kind == AGB_STOKES))
+      return fail(c, AGB_ERR_UNSUPPORTED, "the matrix-free operator needs a Stokes problem with velocity known on "
+                                          "every wall, triangles and the default integration");
+    c->prec = precision;
+    c->lda = ((int64_t)c->n + 31) / 32 * 32;
+    const int ldp = (c->ne + 31) / 32 * 32;
+    const int Q = c->rule.Q;
+    CUDA_OR_FAIL(c, cudaMalloc(&c->d_q, c->lda * sizeof(double)));
+    CUDA_OR_FAIL(c, cudaMemsetAsync(c->d_q, 0, c->lda * sizeof(double), c->stream));
+    CUDA_OR_FAIL(c, cudaMalloc(&c->d_pts, (size_t)Q * ldp * sizeof(QPt<float>)));
+    CUDA_OR_FAIL(c, cudaMalloc(&c->d_src, 3 * (size_t)ldp * sizeof(float)));
+    CUDA_OR_FAIL(c, cudaMalloc(&c->d_nrm, 3 * (size_t)ldp * sizeof(float)));
+    CUDA_OR_FAIL(c, cudaMalloc(&c->d_colscale, (size_t)ldp * sizeof(float)));
+    CUDA_OR_FAIL(c, cudaMalloc(&c->d_self6, (size_t)c->ne * 6 * sizeof(float)));
+    std::vector<float> csf(ldp, 0.f);
+    for (int p = 0; p < c->ne; ++p) csf[p] = (float)(-c->normMul[c->wallIdx[p]] / c->diff);
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_colscale, csf.data(), ldp * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CUDA_OR_FAIL(c, launch_expand_points<float>(c->ne, ldp, c->d_geom, c->rule, (QPt<float>*)c->d_pts,
+                                                (float*)c->d_src, (float*)c->d_nrm, c->stream));
+    c->mfop.ne = c->ne; c->mfop.Q = Q; c->mfop.ldp = ldp;
+    c->mfop.pts = (const QPt<float>*)c->d_pts; c->mfop.src = (const float*)c->d_src;
+    c->mfop.colscale = (const float*)c->d_colscale; c->mfop.self6 = c->d_self6;
+    CUDA_OR_FAIL(c, mf_setup_self(c->mfop, c->d_geom, c->diff, c->stream));
+    c->nlaunch += 2;
+    c->lsqr.mf = &c->mfop;
+    if (!c->lsqr.setup(nullptr, true, c->m, c->n, c->lda, 1, c->stream)) return fail(c, AGB_ERR_CUDA, c->lsqr.err);
+    cudaEventRecord(c->tev[0], c->stream);
+    if (!c->lsqr.precon(nullptr, c->d_q)) return fail(c, AGB_ERR_CUDA, c->lsqr.err);
+    cudaEventRecord(c->tev[1], c->stream);
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->tev[0], c->tev[1]) == cudaSuccess) { c->t_asm += ms; ++c->n_asm; }
+    (void)cudaGetLastError();
+    c->assembled = true;
+    return AGB_OK;
+  }
   if (!fast) return assemble_general(c, precision);
   c->prec = precision;
   const bool f32 = (precision == AGB_MIXED);
@@ -739,6 +782,7 @@ int agb_get_system(agb_context* c, int scaled, double* A, double* q) {
   int rc = check_ctx(c, true);
   if (rc) return rc;
   if (!c->assembled) return fail(c, AGB_ERR_STATE, "system not assembled");
+  if (c->prec == AGB_MATRIX_FREE && A) return fail(c, AGB_ERR_UNSUPPORTED, "the matrix-free system is not stored");
   cudaSetDevice(c->device);
   std::vector<double> qh(c->lda);
   CUDA_OR_FAIL(c, cudaMemcpy(qh.data(), c->d_q, c->lda * sizeof(double), cudaMemcpyDeviceToHost));

@@ -15,6 +15,7 @@
 #include "agb_async.cuh"
 #include "agb_sweeps.cuh"
 #include "agb_batch.cuh"
+#include "agb_mfree.cuh"
 #include <cudaTypedefs.h>
 #include <cstdio>
 #include <cstring>
@@ -733,6 +734,11 @@ template <typename T>
 static unsigned av2_blocks(const DenseLsqr& L) { return cdiv(L.m, AV2<T>::WARPS * AV2<T>::RR); }
 template <typename T>
 static void launch_av2(const DenseLsqr& L) {
+  if (L.mf) {
+    mf_av(*L.mf, (const float*)L.Vs, L.mf_q, L.lda, L.Yp, L.stream);
+    mf_av_reduce(L.m, L.mf_cb, L.Yp, L.sc, L.Y, (float*)L.Ys, L.part, L.stream);
+    return;
+  }
   if (sizeof(T) == 4 && L.use_tma) {
     k_av3<<<cdiv(L.m, AV3_ROWS), AV3_WARPS * 32, AV3_SMEM, L.stream>>>(L.tm_av, L.lda, L.m, (const float*)L.Vs, L.sc,
                                                                        L.Y, (float*)L.Ys, L.part, L.errflag);
@@ -748,6 +754,10 @@ static size_t atu2_smem() {
 }
 template <typename T>
 static void launch_atu(const DenseLsqr& L) {
+  if (L.mf) {
+    mf_atu(*L.mf, (const float*)L.Ys, L.mf_q, L.lda, L.Zp, false, L.stream);
+    return;
+  }
   if (sizeof(T) == 4 && L.use_tma) {
     dim3 g(cdiv(L.lda, ATU3_COLS), L.zgroups);
     const int rpg = (int)((cdiv(L.m, L.zgroups) + 31) / 32 * 32);
@@ -775,7 +785,8 @@ void DenseLsqr::release() {
     for (int i = 0; i < 4 * 32; ++i) cudaEventDestroy(pev[i]);
   pev_ready = false;
   cudaFree(Y); cudaFree(V); cudaFree(W); cudaFree(X); cudaFree(Z); cudaFree(Ys); cudaFree(Vs);
-  cudaFree(part); cudaFree(Zp); cudaFree(sc); cudaFree(nactive); cudaFree(XsD); cudaFree(errflag);
+  cudaFree(part); cudaFree(Zp); cudaFree(sc); cudaFree(nactive); cudaFree(XsD); cudaFree(errflag); cudaFree(Yp);
+  Yp = nullptr;
   XsD = nullptr; errflag = nullptr;
   if (h_nactive) cudaFreeHost(h_nactive);
   Y = V = W = X = Z = nullptr; Ys = Vs = nullptr; part = Zp = nullptr; sc = nullptr; nactive = nullptr;
@@ -798,7 +809,8 @@ bool DenseLsqr::setup(const void* A_dev, bool is_fp32, int m_, int n_, int64_t l
   CK(cudaMalloc(&Z, std::max<int64_t>(lda, mpad) * K8 * sizeof(double)));  // b / x0 staging
   CK(cudaMalloc(&Vs, lda * K8 * sizeof(double)));                            // T copy, or FP64 for residual
   // row groups for sweep 2: aim for >= 4 CTAs per SM
-  use_tma = fp32 && getenv("AGB_NO_TMA") == nullptr;
+  use_tma = fp32 && getenv("AGB_NO_TMA") == nullptr && A_dev != nullptr;
+  if (!A_dev && !mf) { err = "no matrix and no matrix-free operator"; return false; }
   if (use_tma) {
     if (!make_tensor_map_2d(&tm_av, A_dev, lda, m, SWEEP_BC, AV3_ROWS, err)) return false;
     if (!make_tensor_map_2d(&tm_atu, A_dev, lda, m, 256, ATU3_RS, err)) return false;
@@ -829,10 +841,15 @@ bool DenseLsqr::setup(const void* A_dev, bool is_fp32, int m_, int n_, int64_t l
     if (best < 0 && G == gmax) groups = G;
   }
   zgroups = groups;
+  if (mf) {
+    zgroups = mf_row_groups(*mf);
+    mf_cb = mf_col_blocks(*mf);
+    CK(cudaMalloc(&Yp, (size_t)mf_cb * m * K8 * sizeof(float)));
+  }
   CK(cudaMalloc(&XsD, lda * K8 * sizeof(double)));
   CK(cudaMalloc(&errflag, sizeof(int)));
   CK(cudaMemsetAsync(errflag, 0, sizeof(int), stream));
-  CK(cudaMalloc(&Zp, (int64_t)groups * lda * K8 * sizeof(double)));
+  CK(cudaMalloc(&Zp, (int64_t)zgroups * lda * K8 * sizeof(double)));
   const int64_t nbmax = std::max<int64_t>({(int64_t)cdiv(m, 16), (int64_t)cdiv(m, AV_ROWS),
                                            (int64_t)cdiv(lda * K8, kThreads), (int64_t)cdiv(mpad * K8, kThreads)});
   part_cap = (size_t)nbmax * K8 * 2;
@@ -864,6 +881,13 @@ cudaError_t dense_colscale_f32(float* A, int64_t lda, int m, int n, double* q, d
 }
 
 bool DenseLsqr::precon(void* A_dev, double* q_dev) {
+  if (mf) {  // q from the recomputed column sums of squares; A itself is never stored or scaled
+    CK(mf_atu(*mf, nullptr, nullptr, lda, Zp, true, stream));
+    k_colsq_finish<<<cdiv(lda, 256), 256, 0, stream>>>(Zp, zgroups, lda, n, q_dev);
+    launches += 2;
+    CK(cudaGetLastError());
+    return true;
+  }
   const int vn = fp32 ? 4 : 2;
   dim3 g(cdiv(lda, kThreads * vn), zgroups);
   const int rpg = (int)cdiv(m, zgroups);
@@ -892,7 +916,10 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
   if (maxit == 0) maxit = 10 * (m + n + 50);
   const int64_t mpad = ((int64_t)m + 255) / 256 * 256;
   const unsigned nb_av = cdiv(m, AV_ROWS);  // residual sweep
-  const unsigned nb_av2 = fp32 ? (use_tma ? cdiv(m, AV3_ROWS) : av2_blocks<float>(*this)) : av2_blocks<double>(*this);
+  const unsigned nb_av2 = mf ? cdiv((int64_t)m * K8, 256)
+                            : fp32 ? (use_tma ? cdiv(m, AV3_ROWS) : av2_blocks<float>(*this)) : av2_blocks<double>(*this);
+  mf_q = q_dev;
+  if (mf && !x0_zero) { err = "the matrix-free operator needs a zero warm start"; return false; }
   CK(fp32 ? set_sweep_attrs<float>() : set_sweep_attrs<double>());
   const unsigned nb_red = cdiv((int64_t)n * K8, kThreads);
   const unsigned nb_upd = cdiv(lda * K8, kThreads);

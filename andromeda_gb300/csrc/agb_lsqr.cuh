@@ -47,6 +47,11 @@ struct DenseLsqr {
   CUtensorMap tm_av{};
   CUtensorMap tm_atu{};
   bool use_tma = false;
+  // matrix-free operator (A == nullptr): the sweeps recompute A's entries
+  const struct MfOp* mf = nullptr;
+  float* Yp = nullptr;          // [col blocks][m][8] partial products of A V
+  int mf_cb = 0;
+  const double* mf_q = nullptr; // column scales applied on the fly
   double t_av = 0.0, t_atu = 0.0;
   long n_av = 0, n_atu = 0;
   long launches = 0;           // kernels launched by precon/solve

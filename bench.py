@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=1)
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "batch", "surrogate"],
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "batch", "surrogate", "large"],
                     help="sphere: one level-5 sphere (default); batch: the many-body superellipsoid set")
     ap.add_argument("--bodies", type=int, default=512, help="batch workload: number of bodies")
     ap.add_argument("--fp64-sample", type=int, default=6, help="batch workload: bodies solved on the FP64 path")
@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--queries", type=int, default=1000000, help="surrogate: inference batch")
     ap.add_argument("--audit", type=float, default=0.01, help="surrogate: fraction of queries re-solved by the BEM")
     ap.add_argument("--epochs", type=int, default=600, help="surrogate: training epochs")
+    ap.add_argument("--mf-iters", type=int, default=6, help="large: LSQR iterations timed (matrix-free sweeps)")
+    ap.add_argument("--grid", default="160x320", help="large: superellipsoid rings x sectors")
     return ap.parse_args()
 
 
@@ -339,6 +341,55 @@ def run_batch(args, rank, world, local):
     ctx.close()
 
 
+def run_large(args):
+    """Single large body, matrix-free: superellipsoid a=1, b=0.5, c=0.25,
+    e1=0.6, e2=1.4 on a rings x sectors signed-power grid (160 x 320 = 102400
+    triangles) in a level-2 container of radius 200; the single-layer matrix
+    (307 200^2 in FP32 would be 377 GB) is recomputed in every LSQR sweep.
+    A bounded number of LSQR iterations is timed (live CUDA events)."""
+    import numpy as np
+    import andromeda_gb300 as A
+    from andromeda_gb300 import mesh as M
+    nr, ns = (int(v) for v in args.grid.split("x"))
+    body = M.superellipsoid(1.0, 0.5, 0.25, 0.6, 1.4, nr, ns, inward=True)
+    m = M.particle_in_sphere(body, outer_level=2, outer_radius=200.0)
+    C = A.Context(0)
+    C.set_mesh(m)
+    C.set_problem(A.STOKES, [1, 2], A.dirichlet_known(A.STOKES, 2), itri=5)
+    ne = len(m["etype"])
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        C.kernel_times(reset=True)
+        R, nit, info = C.resistance_tensor(A.MATRIX_FREE, 1, 2, maxit=args.mf_iters, eps=args.batch_eps)
+        t1 = time.perf_counter()
+    kt = C.kernel_times(reset=True)
+    av_ms = kt["av_ms"] / max(kt["av_launches"], 1)
+    atu_ms = kt["atu_ms"] / max(kt["atu_launches"], 1)
+    # FP32 work of one sweep: ne^2 pairs x Q points x 28 flops (the point kernel) + the 8-RHS contraction
+    Q = 126
+    flops = float(ne) * ne * Q * 28.0 + float(ne) * ne * 2 * 9 * 8
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+    line = {"metric": "matrix-free LSQR sweep rate (FP32 recomputed single layer)", "value": 1000.0 / (av_ms + atu_ms),
+            "unit": "iterations/s", "n_gpus": 1, "steps": args.mf_iters, "warmup": 0,
+            "ms_per_step": av_ms + atu_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32 (fp64 self blocks, reductions, recurrences)", "data": "synthetic",
+            "config": {"workload": f"superellipsoid a=1 b=0.5 c=0.25 e1=0.6 e2=1.4, {nr}x{ns} grid "
+                                   f"({len(body['etype'])} tri) in an L2 container r=200, 6 RHS, ITRI 5",
+                       "unknowns": C.n, "matrix_fp32_gb_if_stored": C.n * C.n * 4 / 1e9},
+            "assemble_ms": info["assemble_ms"], "rhs_ms": info["rhs_ms"], "nit": [int(v) for v in nit],
+            "sweep_ms": {"av": av_ms, "atu": atu_ms},
+            "roofline": {"bound": "fp32 pipe", "kernel": "k_mf_av / k_mf_atu",
+                         "achieved": flops / (av_ms * 1e-3) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": flops / (av_ms * 1e-3) / 1e12 / fp32_peak, "traffic": None,
+                         "peak_source": "nominal FP32 (152 SM x 128 FMA/clk x 2 x 2.07 GHz)",
+                         "other_sweep": {"achieved": flops / (atu_ms * 1e-3) / 1e12,
+                                         "frac": flops / (atu_ms * 1e-3) / 1e12 / fp32_peak}},
+            "clocks": clk.summary(), "gpu_launches": kt["launches"], "host_s": t1 - t0,
+            "note": "a bounded number of iterations (maxit) is timed; the solve itself is not run to convergence"}
+    print(json.dumps(line), flush=True)
+    C.close()
+
+
 def run_surrogate(args):
     """Learned part: BEM tensors of superellipsoids (batched mixed BEM) train the
     MLP on the GPU; one batch of queries is answered by it (BEM outside the
@@ -424,6 +475,10 @@ def main():
     if args.workload == "surrogate":
         if rank == 0:
             run_surrogate(args)
+        return
+    if args.workload == "large":
+        if rank == 0:
+            run_large(args)
         return
     if args.workload == "batch":
         if world > 1:

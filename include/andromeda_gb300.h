@@ -65,6 +65,9 @@ typedef struct agb_context agb_context;
 #define AGB_MIXED 1 /* FP32 regular quadrature + FP32 matrix; FP64 singular
                        integrals, free-term row sums, norms/recurrences and
                        the refinement residual */
+#define AGB_MATRIX_FREE 2 /* AGB_MIXED arithmetic without a stored matrix: every
+                       LSQR sweep recomputes the single-layer entries (Stokes,
+                       velocity known on every wall, triangles; zero warm start) */
 
 /* boundary-condition types (mod_mesh.f90:110) */
 #define AGB_BC_FUNCTION 1
