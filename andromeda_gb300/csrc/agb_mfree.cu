@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(MF_NW * 32, 2) k_mf_atu(MfOp op, const float* 
   extern __shared__ __align__(16) unsigned char mf_smem[];
   QPt<float>* sp = reinterpret_cast<QPt<float>*>(mf_smem);
   constexpr int NV = COLSQ ? 3 : 24;
-  float* red = reinterpret_cast<float*>(mf_smem + (size_t)op.Q * 32 * sizeof(QPt<float>));  // [MF_NW][NV][32]
+  float* red = reinterpret_cast<float*>(mf_smem);  // [MF_NW][NV][32], reuses the point table after the sweep
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int ne = op.ne;
   const int j0 = blockIdx.x * 32;
@@ -278,7 +278,7 @@ static size_t av_smem(const MfOp& op) { return (size_t)op.Q * 32 * sizeof(QPt<fl
 static size_t atu_smem(const MfOp& op, bool colsq) {
   const size_t pts = (size_t)op.Q * 32 * sizeof(QPt<float>);
   const size_t red = (size_t)MF_NW * (colsq ? 3 : 24) * 32 * sizeof(float);
-  return pts > red ? pts + 0 : red;  // the reduction reuses the point table's space
+  return pts > red ? pts : red;  // the warp reduction reuses the point table's space
 }
 
 int mf_row_groups(const MfOp& op) { return (int)mcdiv(op.ne, MF_ROWS); }
