@@ -168,6 +168,7 @@ cudaError_t ensure(T*& p, size_t& cap, size_t count) {
 }
 
 void free_system(agb_context* c) {
+  c->lsqr.packed = false;
   dfree(c->d_self6);
   c->lsqr.mf = nullptr;
   dfree(c->d_lu);
@@ -722,10 +723,13 @@ int agb_assemble(agb_context* c, int precision) {
   const bool f32 = (precision == AGB_MIXED);
   const size_t tsz = f32 ? sizeof(float) : sizeof(double);
   c->lda = ((int64_t)c->n + 31) / 32 * 32;
-  CUDA_OR_FAIL(c, cudaMalloc(&c->d_A, (size_t)c->m * c->lda * tsz));
-  if (c->lda > c->n)
-    CUDA_OR_FAIL(c, cudaMemset2DAsync((char*)c->d_A + c->n * tsz, c->lda * tsz, 0, (c->lda - c->n) * tsz, c->m,
-                                      c->stream));
+  const bool packedA = (c->kind == AGB_STOKES && f32);  // mixed Stokes: packed symmetric blocks (allocated below)
+  if (!packedA) {
+    CUDA_OR_FAIL(c, cudaMalloc(&c->d_A, (size_t)c->m * c->lda * tsz));
+    if (c->lda > c->n)
+      CUDA_OR_FAIL(c, cudaMemset2DAsync((char*)c->d_A + c->n * tsz, c->lda * tsz, 0, (c->lda - c->n) * tsz, c->m,
+                                        c->stream));
+  }
   CUDA_OR_FAIL(c, cudaMalloc(&c->d_q, c->lda * sizeof(double)));
   if (c->kind == AGB_STOKES) {
     const int ldp = (c->ne + 31) / 32 * 32;
@@ -737,15 +741,21 @@ int agb_assemble(agb_context* c, int precision) {
     std::vector<double> cs(ldp, 0.0);
     for (int p = 0; p < c->ne; ++p) cs[p] = -c->normMul[c->wallIdx[p]] / c->diff;
     if (f32) {
+      // packed symmetric blocks: Ap[i][6][ldp] (2/3 of the bytes of the m x lda matrix)
+      CUDA_OR_FAIL(c, cudaMalloc(&c->d_A, (size_t)c->ne * 6 * ldp * sizeof(float)));
+      CUDA_OR_FAIL(c, cudaMemsetAsync(c->d_A, 0, (size_t)c->ne * 6 * ldp * sizeof(float), c->stream));
       std::vector<float> csf(cs.begin(), cs.end());
       CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_colscale, csf.data(), ldp * sizeof(float), cudaMemcpyHostToDevice, c->stream));
       CUDA_OR_FAIL(c, launch_expand_points<float>(c->ne, ldp, c->d_geom, c->rule, (QPt<float>*)c->d_pts,
                                                   (float*)c->d_src, (float*)c->d_nrm, c->stream));
       cudaEventRecord(c->tev[0], c->stream);
-      CUDA_OR_FAIL(c, launch_stokes_G<float>(c->ne, Q, ldp, (const QPt<float>*)c->d_pts, (const float*)c->d_src,
-                                             (const float*)c->d_colscale, (float*)c->d_A, c->lda, c->stream));
+      CUDA_OR_FAIL(c, launch_stokes_G_packed(c->ne, Q, ldp, (const QPt<float>*)c->d_pts, (const float*)c->d_src,
+                                             (const float*)c->d_colscale, (float*)c->d_A, c->stream));
       cudaEventRecord(c->tev[1], c->stream);
-      CUDA_OR_FAIL(c, launch_stokes_self<float>(c->ne, c->d_geom, c->diff, (float*)c->d_A, c->lda, c->stream));
+      CUDA_OR_FAIL(c, launch_stokes_self_packed(c->ne, ldp, c->d_geom, c->diff, (float*)c->d_A, c->stream));
+      c->lsqr.packed = true;
+      c->lsqr.pk_ne = c->ne;
+      c->lsqr.pk_ldp = ldp;
       c->nlaunch += 3;  // expand, single layer, self blocks
     } else {
       CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_colscale, cs.data(), ldp * sizeof(double), cudaMemcpyHostToDevice, c->stream));
@@ -787,6 +797,23 @@ int agb_get_system(agb_context* c, int scaled, double* A, double* q) {
   std::vector<double> qh(c->lda);
   CUDA_OR_FAIL(c, cudaMemcpy(qh.data(), c->d_q, c->lda * sizeof(double), cudaMemcpyDeviceToHost));
   if (q) std::copy(qh.begin(), qh.begin() + c->n, q);
+  if (A && c->lsqr.packed) {  // expand the symmetric blocks: A[3i+a][b ne + j] = Ap[i][sym(a,b)][j]
+    const int ne = c->lsqr.pk_ne, ldp = c->lsqr.pk_ldp;
+    static const int sym[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+    std::vector<float> row((size_t)6 * ldp);
+    for (int i = 0; i < ne; ++i) {
+      CUDA_OR_FAIL(c, cudaMemcpy(row.data(), (float*)c->d_A + (size_t)i * 6 * ldp, row.size() * sizeof(float),
+                                 cudaMemcpyDeviceToHost));
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+          for (int j = 0; j < ne; ++j) {
+            const double v = (double)row[(size_t)sym[a][b] * ldp + j];
+            const size_t col = (size_t)b * ne + j;
+            A[(size_t)(3 * i + a) * c->n + col] = scaled ? v * qh[col] : v;
+          }
+    }
+    return AGB_OK;
+  }
   if (A) {
     const bool f32 = c->prec == AGB_MIXED;
     std::vector<char> buf((size_t)c->lda * (f32 ? 4 : 8));

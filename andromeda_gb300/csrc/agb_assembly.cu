@@ -164,7 +164,10 @@ template <typename T> struct StkTile;
 template <> struct StkTile<float> { static constexpr int RS = 8; static constexpr int NW = 8; };
 template <> struct StkTile<double> { static constexpr int RS = 4; static constexpr int NW = 8; };
 
-template <typename T>
+// PACKED: the 3x3 blocks are symmetric, so the matrix is stored as six
+// planes Ap[i][c][ldp] (c = xx, xy, xz, yy, yz, zz; lda = 6 ldp), 2/3 of the
+// bytes of the full row-major A[3i+a][b ne + j].
+template <typename T, bool PACKED = false>
 __global__ void __launch_bounds__(StkTile<T>::NW * 32) k_stokes_G(int ne, int Q, int ldp, const QPt<T>* __restrict__ pts,
                                                                  const T* __restrict__ src, const T* __restrict__ colscale,
                                                                  int src_per_cta, T* __restrict__ A, int64_t lda) {
@@ -222,12 +225,17 @@ __global__ void __launch_bounds__(StkTile<T>::NW * 32) k_stokes_G(int ne, int Q,
           const T gxx = scale * (acc[r][0] + acc[r][1]), gxy = scale * acc[r][2], gxz = scale * acc[r][3];
           const T gyy = scale * (acc[r][0] + acc[r][4]), gyz = scale * acc[r][5];
           const T gzz = scale * (acc[r][0] + acc[r][6]);
-          T* r0 = A + (int64_t)(3 * i) * lda + j;
-          T* r1 = r0 + lda;
-          T* r2p = r1 + lda;
-          r0[0] = gxx; r0[ne] = gxy; r0[2 * ne] = gxz;
-          r1[0] = gxy; r1[ne] = gyy; r1[2 * ne] = gyz;
-          r2p[0] = gxz; r2p[ne] = gyz; r2p[2 * ne] = gzz;
+          if (PACKED) {
+            T* pr = A + (int64_t)i * lda + j;
+            pr[0] = gxx; pr[ldp] = gxy; pr[2 * ldp] = gxz; pr[3 * ldp] = gyy; pr[4 * ldp] = gyz; pr[5 * ldp] = gzz;
+          } else {
+            T* r0 = A + (int64_t)(3 * i) * lda + j;
+            T* r1 = r0 + lda;
+            T* r2p = r1 + lda;
+            r0[0] = gxx; r0[ne] = gxy; r0[2 * ne] = gxz;
+            r1[0] = gxy; r1[ne] = gyy; r1[2 * ne] = gyz;
+            r2p[0] = gxz; r2p[ne] = gyz; r2p[2 * ne] = gzz;
+          }
         }
       }
     }
@@ -252,6 +260,38 @@ cudaError_t launch_stokes_G(int ne, int Q, int ldp, const QPt<T>* pts, const T* 
 }
 template cudaError_t launch_stokes_G<float>(int, int, int, const QPt<float>*, const float*, const float*, float*, int64_t,
                                             cudaStream_t);
+
+cudaError_t launch_stokes_G_packed(int ne, int Q, int ldp, const QPt<float>* pts, const float* src,
+                                   const float* colscale, float* Ap, cudaStream_t s) {
+  constexpr int NW = StkTile<float>::NW;
+  const size_t smem = (size_t)Q * 32 * sizeof(QPt<float>);
+  cudaError_t e = cudaFuncSetAttribute(k_stokes_G<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int tiles = (int)cdiv(ne, 32);
+  const int want = 152 * 6;
+  int ychunks = std::max(1, std::min((want + tiles - 1) / tiles, (ne + 63) / 64));
+  const int spc = (int)cdiv(ne, ychunks);
+  ychunks = (int)cdiv(ne, spc);
+  k_stokes_G<float, true><<<dim3(tiles, ychunks), NW * 32, smem, s>>>(ne, Q, ldp, pts, src, colscale, spc, Ap,
+                                                                       6 * (int64_t)ldp);
+  return cudaGetLastError();
+}
+
+__global__ void k_stokes_self_packed(int ne, int ldp, const ElemGeom* __restrict__ geom, double diff,
+                                     float* __restrict__ Ap) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= ne) return;
+  const ElemGeom& G = geom[p];
+  double g[6];
+  agb_sing::tri_stokes(G.v[0], G.v[1], G.v[2], G.area, 4, g);
+  const double sc = -G.multi / diff;
+  float* pr = Ap + (int64_t)p * 6 * ldp + p;
+  for (int c = 0; c < 6; ++c) pr[(int64_t)c * ldp] = (float)(sc * g[c]);
+}
+cudaError_t launch_stokes_self_packed(int ne, int ldp, const ElemGeom* geom, double diff, float* Ap, cudaStream_t s) {
+  k_stokes_self_packed<<<cdiv(ne, 64), 64, 0, s>>>(ne, ldp, geom, diff, Ap);
+  return cudaGetLastError();
+}
 template cudaError_t launch_stokes_G<double>(int, int, int, const QPt<double>*, const double*, const double*, double*,
                                              int64_t, cudaStream_t);
 

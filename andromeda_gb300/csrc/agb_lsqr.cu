@@ -473,10 +473,320 @@ __global__ void __launch_bounds__(ATU3_THREADS, 1) k_atu3(const __grid_constant_
   atu3_tile<ATU3_RS, ATU3_ST>(&tmA, lda, m, Us, rows_per_group, Zp, errflag, (int)blockIdx.x, (int)blockIdx.y);
 }
 
+// ---------------------------------------------------------------------------
+// Sweeps over the packed single layer (symmetric 3x3 blocks stored once):
+// Ap[i][c][ldp] (c = xx, xy, xz, yy, yz, zz), A[3i+a][b ne + j] = Ap[i][sym(a,b)][j].
+// The column scaling of lsqr_precon is applied on the fly: sweep 1 reads
+// W = q.V (written by k_update into Vp[b][k][ldp]), sweep 2's partials are
+// scaled by q in k_atu_reduce.
+// ---------------------------------------------------------------------------
+constexpr int AVP_R = 32, AVP_BC = 64, AVP_ST = 4, AVP_WARPS = AVP_R / 2;
+constexpr size_t AVP_STAGE_A = 6 * (size_t)AVP_R * AVP_BC * sizeof(float);   // 48 KB
+constexpr size_t AVP_STAGE_W = 3 * (size_t)K8 * AVP_BC * sizeof(float);      // 6 KB
+constexpr size_t AVP_SMEM = AVP_ST * (AVP_STAGE_A + AVP_STAGE_W);
+
+__device__ __forceinline__ int sym6(int a, int b) {
+  const int lo = a < b ? a : b, hi = a < b ? b : a;
+  return lo == 0 ? hi : (lo == 1 ? 2 + hi : 5);
+}
+
+// reduce-scatter of 32 per-lane FP32 slots: afterwards lane l holds the warp
+// sum of slot l in v[0]
+__device__ __forceinline__ void reduce_scatter32(float (&v)[32], int lane) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    const bool upper = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < o; ++i) {
+      const float send = upper ? v[i] : v[i + o];
+      const float keep = upper ? v[i + o] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+    }
+  }
+}
+
+// Y[3i+a][k] = sum_j sum_b Ap[i][sym(a,b)][j] W[b][k][j] + gamma_k Y; a warp owns two rows i,
+// a lane two columns per stage; every 1024 columns the 24 FP32 sums of a row are
+// reduce-scattered over the warp into one FP64 running sum per lane.
+__global__ void __launch_bounds__(AVP_WARPS * 32, 1) k_avp(const __grid_constant__ CUtensorMap tmA,
+                                                          const __grid_constant__ CUtensorMap tmW, int ne, int ldp,
+                                                          const LsqrScalars* sc, double* __restrict__ Y,
+                                                          float* __restrict__ Ys, double* __restrict__ part,
+                                                          int* errflag) {
+  extern __shared__ __align__(1024) unsigned char avp_smem[];
+  float* sA = reinterpret_cast<float*>(avp_smem);
+  float* sW = reinterpret_cast<float*>(avp_smem + AVP_ST * AVP_STAGE_A);
+  __shared__ __align__(8) uint64_t full[AVP_ST], empty[AVP_ST];
+  __shared__ double sPart[AVP_WARPS][K8];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row_base = blockIdx.x * AVP_R;
+  const int nst = (ldp + AVP_BC - 1) / AVP_BC;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < AVP_ST; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], AVP_WARPS);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int k) {
+    const int s = k % AVP_ST;
+    if (k >= AVP_ST) mbar_wait_bounded(&empty[s], (uint32_t)(((k / AVP_ST) - 1) & 1), errflag);
+    const int j0 = k * AVP_BC;
+    mbar_expect_tx(&full[s], (uint32_t)(AVP_STAGE_A + AVP_STAGE_W));
+    float* dA = sA + (size_t)s * 6 * AVP_R * AVP_BC;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) tma_load_2d(dA + (size_t)c * AVP_R * AVP_BC, &tmA, c * ldp + j0, row_base, &full[s]);
+    tma_load_2d(sW + (size_t)s * 3 * K8 * AVP_BC, &tmW, j0, 0, &full[s]);
+  };
+  if (threadIdx.x == 0)
+    for (int k = 0; k < AVP_ST && k < nst; ++k) issue(k);
+  float acc[2][3][K8];
+  double dacc[2] = {0.0, 0.0};
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int c = 0; c < K8; ++c) acc[r][a][c] = 0.f;
+  for (int k = 0; k < nst; ++k) {
+    const int s = k % AVP_ST;
+    mbar_wait_bounded(&full[s], (uint32_t)((k / AVP_ST) & 1), errflag);
+    const float* tA = sA + (size_t)s * 6 * AVP_R * AVP_BC + (2 * warp) * AVP_BC + lane * 2;
+    const float* tW = sW + (size_t)s * 3 * K8 * AVP_BC + lane * 2;
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      float2 w[K8];
+#pragma unroll
+      for (int c = 0; c < K8; ++c) w[c] = *reinterpret_cast<const float2*>(tW + (size_t)(b * K8 + c) * AVP_BC);
+#pragma unroll
+      for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const float2 g = *reinterpret_cast<const float2*>(tA + (size_t)sym6(a, b) * AVP_R * AVP_BC + r * AVP_BC);
+#pragma unroll
+          for (int c = 0; c < K8; ++c) acc[r][a][c] = fmaf(g.y, w[c].y, fmaf(g.x, w[c].x, acc[r][a][c]));
+        }
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+    if (threadIdx.x == 0 && k + AVP_ST < nst) issue(k + AVP_ST);
+    if ((k & 15) == 15 || k == nst - 1) {
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        float v[32];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int c = 0; c < K8; ++c) { v[a * K8 + c] = acc[r][a][c]; acc[r][a][c] = 0.f; }
+#pragma unroll
+        for (int t = 24; t < 32; ++t) v[t] = 0.f;
+        reduce_scatter32(v, lane);
+        dacc[r] += (double)v[0];
+      }
+    }
+  }
+  // lane a*8+c holds row 3i+a, right-hand side c of each of the warp's two rows
+  double ssq = 0.0;
+  if (lane < 3 * K8) {
+    const int a = lane / K8, c = lane % K8;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int i = row_base + 2 * warp + r;
+      if (i < ne) {
+        const int64_t id = (int64_t)(3 * i + a) * K8 + c;
+        const double y = dacc[r] + sc[c].gamma * Y[id];
+        Y[id] = y;
+        Ys[id] = (float)y;
+        ssq += y * y;
+      }
+    }
+  }
+  // per-c partial sums: lanes c, c+8, c+16
+  ssq += __shfl_down_sync(0xffffffffu, ssq, 8);
+  ssq += __shfl_down_sync(0xffffffffu, ssq, 16);
+  if (lane < K8) sPart[warp][lane] = ssq;
+  __syncthreads();
+  if (threadIdx.x < K8) {
+    double t = 0.0;
+    for (int w = 0; w < AVP_WARPS; ++w) t += sPart[w][threadIdx.x];
+    part[(int64_t)blockIdx.x * K8 + threadIdx.x] = t;
+  }
+}
+
+// Zp[g][b ne + j][k] = sum_{i in group g} sum_a Ap[i][sym(a,b)][j] U[3i+a][k]; one thread per column j.
+constexpr int ATUP_C = 256, ATUP_RS = 8, ATUP_ST = 4;
+constexpr size_t ATUP_STAGE_A = 6 * (size_t)ATUP_RS * ATUP_C * sizeof(float);  // 48 KB
+constexpr size_t ATUP_STAGE_U = 3 * (size_t)ATUP_RS * K8 * sizeof(float);      // 768 B
+constexpr size_t ATUP_SMEM = ATUP_ST * (ATUP_STAGE_A + ATUP_STAGE_U);
+
+__global__ void __launch_bounds__(ATUP_C, 1) k_atup(const __grid_constant__ CUtensorMap tmA, int ne, int ldp,
+                                                   int64_t lda, const float* __restrict__ Us, int rows_per_group,
+                                                   double* __restrict__ Zp, int* errflag) {
+  extern __shared__ __align__(1024) unsigned char atup_smem[];
+  float* sA = reinterpret_cast<float*>(atup_smem);
+  float* sU = reinterpret_cast<float*>(atup_smem + ATUP_ST * ATUP_STAGE_A);
+  __shared__ __align__(8) uint64_t full[ATUP_ST], empty[ATUP_ST];
+  const int j0 = blockIdx.x * ATUP_C;
+  const int g = blockIdx.y;
+  const int r0 = g * rows_per_group, r1 = min(ne, r0 + rows_per_group);
+  const int nst = (r1 > r0) ? (r1 - r0 + ATUP_RS - 1) / ATUP_RS : 0;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < ATUP_ST; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], ATUP_C / 32);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int k) {
+    const int s = k % ATUP_ST;
+    if (k >= ATUP_ST) mbar_wait_bounded(&empty[s], (uint32_t)(((k / ATUP_ST) - 1) & 1), errflag);
+    const int rb = r0 + k * ATUP_RS;
+    const int nr = min(ATUP_RS, r1 - rb);
+    mbar_expect_tx(&full[s], (uint32_t)(ATUP_STAGE_A + (size_t)3 * nr * K8 * sizeof(float)));
+    float* dA = sA + (size_t)s * 6 * ATUP_RS * ATUP_C;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) tma_load_2d(dA + (size_t)c * ATUP_RS * ATUP_C, &tmA, c * ldp + j0, rb, &full[s]);
+    bulk_g2s(sU + (size_t)s * 3 * ATUP_RS * K8, Us + (int64_t)3 * rb * K8, (uint32_t)(3 * nr * K8 * sizeof(float)),
+             &full[s]);
+  };
+  if (threadIdx.x == 0)
+    for (int k = 0; k < ATUP_ST && k < nst; ++k) issue(k);
+  float acc[3][K8];
+  double dacc[3][K8];
+#pragma unroll
+  for (int b = 0; b < 3; ++b)
+#pragma unroll
+    for (int c = 0; c < K8; ++c) { acc[b][c] = 0.f; dacc[b][c] = 0.0; }
+  for (int k = 0; k < nst; ++k) {
+    const int s = k % ATUP_ST;
+    mbar_wait_bounded(&full[s], (uint32_t)((k / ATUP_ST) & 1), errflag);
+    const int rb = r0 + k * ATUP_RS;
+    const int nr = min(ATUP_RS, r1 - rb);
+    const float* tA = sA + (size_t)s * 6 * ATUP_RS * ATUP_C + threadIdx.x;
+    const float* tU = sU + (size_t)s * 3 * ATUP_RS * K8;
+    for (int r = 0; r < nr; ++r) {
+      float g6[6];
+#pragma unroll
+      for (int c = 0; c < 6; ++c) g6[c] = tA[(size_t)c * ATUP_RS * ATUP_C + r * ATUP_C];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float4 u0 = *reinterpret_cast<const float4*>(tU + (3 * r + a) * K8);
+        const float4 u1 = *reinterpret_cast<const float4*>(tU + (3 * r + a) * K8 + 4);
+        const float uu[K8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+          const float gv = g6[sym6(a, b)];
+#pragma unroll
+          for (int c = 0; c < K8; ++c) acc[b][c] = fmaf(gv, uu[c], acc[b][c]);
+        }
+      }
+    }
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) mbar_arrive(&empty[s]);
+    if (threadIdx.x == 0 && k + ATUP_ST < nst) issue(k + ATUP_ST);
+    if ((k & 31) == 31 || k == nst - 1) {
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+#pragma unroll
+        for (int c = 0; c < K8; ++c) { dacc[b][c] += (double)acc[b][c]; acc[b][c] = 0.f; }
+    }
+  }
+  const int j = j0 + threadIdx.x;
+  if (j < ne)
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+#pragma unroll
+      for (int c = 0; c < K8; ++c) Zp[((int64_t)g * lda + (int64_t)b * ne + j) * K8 + c] = dacc[b][c];
+}
+
+// r = b - A (q.Xs) over the packed (unscaled) matrix, FP64 accumulation (warm start / refinement residual);
+// one warp per row i
+__global__ void __launch_bounds__(256) k_residp(const float* __restrict__ Ap, int ne, int ldp,
+                                                const double* __restrict__ Xs, const double* __restrict__ qs,
+                                                const double* __restrict__ Bp, double* __restrict__ Y,
+                                                float* __restrict__ Ys, double* __restrict__ part) {
+  __shared__ double sPart[8][K8];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 8 + warp;
+  double acc[3][K8];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < K8; ++c) acc[a][c] = 0.0;
+  if (i < ne) {
+    const float* row = Ap + (int64_t)i * 6 * ldp;
+    for (int j = lane; j < ne; j += 32) {
+      double g6[6];
+#pragma unroll
+      for (int c = 0; c < 6; ++c) g6[c] = (double)row[(int64_t)c * ldp + j];
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        const double* x = Xs + ((int64_t)b * ne + j) * K8;
+        const double qv = qs[(int64_t)b * ne + j];  // Xs = x / q and Ap is the unscaled matrix
+#pragma unroll
+        for (int c = 0; c < K8; ++c) {
+          const double xv = qv * x[c];
+#pragma unroll
+          for (int a = 0; a < 3; ++a) acc[a][c] += g6[sym6(a, b)] * xv;
+        }
+      }
+    }
+  }
+  double ssq = 0.0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < K8; ++c) {
+      const double v = warp_sum(acc[a][c]);
+      if (lane == a * K8 + c && i < ne) {
+        const int64_t id = (int64_t)(3 * i + a) * K8 + c;
+        const double y = Bp[id] - v;
+        Y[id] = y;
+        Ys[id] = (float)y;
+        ssq = y * y;
+      }
+    }
+  ssq += __shfl_down_sync(0xffffffffu, ssq, 8);
+  ssq += __shfl_down_sync(0xffffffffu, ssq, 16);
+  if (lane < K8) sPart[warp][lane] = ssq;
+  __syncthreads();
+  if (threadIdx.x < K8) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += sPart[w][threadIdx.x];
+    part[(int64_t)blockIdx.x * K8 + threadIdx.x] = t;
+  }
+}
+
+// column sums of squares of the packed matrix per row group:
+// P[g][b ne + j] = sum_{i in g} sum_a Ap[i][sym(a,b)][j]^2
+__global__ void k_colsqp(const float* __restrict__ Ap, int ne, int ldp, int rows_per_group, double* __restrict__ P,
+                         int64_t lda) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int g = blockIdx.y;
+  if (j >= ne) return;
+  const int r0 = g * rows_per_group, r1 = min(ne, r0 + rows_per_group);
+  double s[6] = {0, 0, 0, 0, 0, 0};
+  for (int i = r0; i < r1; ++i) {
+    const float* row = Ap + (int64_t)i * 6 * ldp + j;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      const double v = (double)row[(int64_t)c * ldp];
+      s[c] += v * v;
+    }
+  }
+  // b = 0: xx, xy, xz; b = 1: xy, yy, yz; b = 2: xz, yz, zz
+  P[(int64_t)g * lda + j] = s[0] + s[1] + s[2];
+  P[(int64_t)g * lda + ne + j] = s[1] + s[3] + s[4];
+  P[(int64_t)g * lda + 2 * ne + j] = s[2] + s[4] + s[5];
+}
+
 // V <- Z/beta - beta V (Z = sum of group partials, in order); partial ||V||^2.
 // On the initial call (init=1) the old V is taken as zero.
 __global__ void k_atu_reduce(const double* __restrict__ Zp, int groups, int64_t lda, int n, const LsqrScalars* sc,
-                             int init, double* __restrict__ V, double* __restrict__ part) {
+                             int init, double* __restrict__ V, double* __restrict__ part,
+                             const double* __restrict__ qs = nullptr) {
   __shared__ double sP[kThreads / 32][K8];
   const int64_t t = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   const int64_t j = t / K8;
@@ -485,6 +795,7 @@ __global__ void k_atu_reduce(const double* __restrict__ Zp, int groups, int64_t 
   if (j < n) {
     double z = 0.0;
     for (int g = 0; g < groups; ++g) z += Zp[((int64_t)g * lda + j) * K8 + c];
+    if (qs) z *= qs[j];  // column scaling applied on the fly (packed layout)
     const double beta = sc[c].beta;
     if (sc[c].active && beta > 0.0) {
       vn = z / beta - (init ? 0.0 : beta * V[j * K8 + c]);
@@ -513,7 +824,8 @@ __global__ void k_atu_reduce(const double* __restrict__ Zp, int groups, int64_t 
 template <typename T>
 __global__ void k_update(int n, int64_t lda, const LsqrScalars* sc, int init, double* __restrict__ V,
                          double* __restrict__ W, double* __restrict__ X, T* __restrict__ Vs, double* __restrict__ part,
-                         int vs_rhs_major) {
+                         int vs_rhs_major, float* __restrict__ Vp = nullptr, int pk_ne = 0, int pk_ldp = 0,
+                         const double* __restrict__ qs = nullptr) {
   __shared__ double sP[kThreads / 32][K8];
   const int64_t t = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   const int64_t j = t / K8;
@@ -541,7 +853,13 @@ __global__ void k_update(int n, int64_t lda, const LsqrScalars* sc, int init, do
       } else if (init) {
         W[id] = 0.0; X[id] = 0.0;
       }
-      Vs[vs_rhs_major ? (int64_t)c * lda + j : id] = (T)V[id];
+      if (Vp) {  // packed layout: W = q.V as [b][k][ldp]
+        const int b = (int)(j / pk_ne);
+        const int64_t jj = j - (int64_t)b * pk_ne;
+        Vp[((int64_t)b * K8 + c) * pk_ldp + jj] = (float)(qs[j] * V[id]);
+      } else {
+        Vs[vs_rhs_major ? (int64_t)c * lda + j : id] = (T)V[id];
+      }
     }
   }
   double s = dk;
@@ -726,6 +1044,11 @@ bool make_tensor_map_2d(CUtensorMap* tm, const void* A, int64_t lda, int m, int 
 
 template <typename T>
 static void launch_resid(const DenseLsqr& L, const double* Xs, const double* Bp) {
+  if (L.packed) {
+    k_residp<<<cdiv(L.pk_ne, 8), 256, 0, L.stream>>>((const float*)L.A, L.pk_ne, L.pk_ldp, Xs, L.mf_q, Bp, L.Y,
+                                                     (float*)L.Ys, L.part);
+    return;
+  }
   const unsigned nb = cdiv(L.m, AV_ROWS);
   k_av<T, double><<<nb, kThreads, 0, L.stream>>>((const T*)L.A, L.lda, L.m, L.n, Xs, -1.0, L.sc, 0, Bp, L.Y,
                                                  (T*)L.Ys, L.part);
@@ -734,6 +1057,11 @@ template <typename T>
 static unsigned av2_blocks(const DenseLsqr& L) { return cdiv(L.m, AV2<T>::WARPS * AV2<T>::RR); }
 template <typename T>
 static void launch_av2(const DenseLsqr& L) {
+  if (L.packed) {
+    k_avp<<<cdiv(L.pk_ne, AVP_R), AVP_WARPS * 32, AVP_SMEM, L.stream>>>(L.tm_av, L.tm_vp, L.pk_ne, L.pk_ldp, L.sc,
+                                                                        L.Y, (float*)L.Ys, L.part, L.errflag);
+    return;
+  }
   if (L.mf) {
     mf_av(*L.mf, (const float*)L.Vs, L.mf_q, L.lda, L.Yp, L.stream);
     mf_av_reduce(L.m, L.mf_cb, L.Yp, L.sc, L.Y, (float*)L.Ys, L.part, L.stream);
@@ -754,6 +1082,12 @@ static size_t atu2_smem() {
 }
 template <typename T>
 static void launch_atu(const DenseLsqr& L) {
+  if (L.packed) {
+    const int rpg = (int)((cdiv(L.pk_ne, L.zgroups) + ATUP_RS - 1) / ATUP_RS * ATUP_RS);
+    k_atup<<<dim3(cdiv(L.pk_ldp, ATUP_C), L.zgroups), ATUP_C, ATUP_SMEM, L.stream>>>(
+        L.tm_atu, L.pk_ne, L.pk_ldp, L.lda, (const float*)L.Ys, rpg, L.Zp, L.errflag);
+    return;
+  }
   if (L.mf) {
     mf_atu(*L.mf, (const float*)L.Ys, L.mf_q, L.lda, L.Zp, false, L.stream);
     return;
@@ -775,6 +1109,8 @@ static cudaError_t set_sweep_attrs() {
                                        (int)(2 * K8 * AV2<T>::CH * sizeof(T)));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_av3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AV3_SMEM);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_atu3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ATU3_SMEM);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_avp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AVP_SMEM);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_atup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ATUP_SMEM);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_atu2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)atu2_smem<T>());
   return e;
@@ -785,8 +1121,9 @@ void DenseLsqr::release() {
     for (int i = 0; i < 4 * 32; ++i) cudaEventDestroy(pev[i]);
   pev_ready = false;
   cudaFree(Y); cudaFree(V); cudaFree(W); cudaFree(X); cudaFree(Z); cudaFree(Ys); cudaFree(Vs);
-  cudaFree(part); cudaFree(Zp); cudaFree(sc); cudaFree(nactive); cudaFree(XsD); cudaFree(errflag); cudaFree(Yp);
+  cudaFree(part); cudaFree(Zp); cudaFree(sc); cudaFree(nactive); cudaFree(XsD); cudaFree(errflag); cudaFree(Yp); cudaFree(Vp);
   Yp = nullptr;
+  Vp = nullptr;
   XsD = nullptr; errflag = nullptr;
   if (h_nactive) cudaFreeHost(h_nactive);
   Y = V = W = X = Z = nullptr; Ys = Vs = nullptr; part = Zp = nullptr; sc = nullptr; nactive = nullptr;
@@ -809,8 +1146,19 @@ bool DenseLsqr::setup(const void* A_dev, bool is_fp32, int m_, int n_, int64_t l
   CK(cudaMalloc(&Z, std::max<int64_t>(lda, mpad) * K8 * sizeof(double)));  // b / x0 staging
   CK(cudaMalloc(&Vs, lda * K8 * sizeof(double)));                            // T copy, or FP64 for residual
   // row groups for sweep 2: aim for >= 4 CTAs per SM
-  use_tma = fp32 && getenv("AGB_NO_TMA") == nullptr && A_dev != nullptr;
+  use_tma = fp32 && getenv("AGB_NO_TMA") == nullptr && A_dev != nullptr && !packed;
   if (!A_dev && !mf) { err = "no matrix and no matrix-free operator"; return false; }
+  if (packed) {
+    if (!fp32 || 3 * pk_ne != m || m != n || pk_ldp % 32 != 0 || pk_ldp < pk_ne) {
+      err = "packed layout: bad sizes";
+      return false;
+    }
+    if (!make_tensor_map_2d(&tm_av, A_dev, 6 * (int64_t)pk_ldp, pk_ne, AVP_BC, AVP_R, err)) return false;
+    if (!make_tensor_map_2d(&tm_atu, A_dev, 6 * (int64_t)pk_ldp, pk_ne, ATUP_C, ATUP_RS, err)) return false;
+    CK(cudaMalloc(&Vp, (size_t)3 * K8 * pk_ldp * sizeof(float)));
+    CK(cudaMemsetAsync(Vp, 0, (size_t)3 * K8 * pk_ldp * sizeof(float), stream));
+    if (!make_tensor_map_2d(&tm_vp, Vp, pk_ldp, 3 * K8, AVP_BC, 3 * K8, err)) return false;
+  }
   if (use_tma) {
     if (!make_tensor_map_2d(&tm_av, A_dev, lda, m, SWEEP_BC, AV3_ROWS, err)) return false;
     if (!make_tensor_map_2d(&tm_atu, A_dev, lda, m, 256, ATU3_RS, err)) return false;
@@ -841,6 +1189,19 @@ bool DenseLsqr::setup(const void* A_dev, bool is_fp32, int m_, int n_, int64_t l
     if (best < 0 && G == gmax) groups = G;
   }
   zgroups = groups;
+  if (packed) {  // row groups of the packed A^T U tiles (one CTA per SM): fill whole waves
+    const int cb = (int)cdiv(pk_ldp, ATUP_C);
+    const int gmx = std::max(1, std::min(64, (int)cdiv(pk_ne, 64)));
+    double bestp = -1.0;
+    zgroups = 1;
+    for (int G = 1; G <= gmx; ++G) {
+      const int64_t items = (int64_t)cb * G;
+      const double eff = (double)items / (double)(cdiv(items, nsm) * (int64_t)nsm);
+      const double score = eff - 0.002 * G;
+      if (items >= nsm && score > bestp) { bestp = score; zgroups = G; }
+      if (bestp < 0 && G == gmx) zgroups = G;
+    }
+  }
   if (mf) {
     zgroups = mf_row_groups(*mf);
     mf_cb = mf_col_blocks(*mf);
@@ -881,6 +1242,14 @@ cudaError_t dense_colscale_f32(float* A, int64_t lda, int m, int n, double* q, d
 }
 
 bool DenseLsqr::precon(void* A_dev, double* q_dev) {
+  if (packed) {  // q from the packed columns; the matrix stays unscaled, q is applied in the sweeps
+    const int rpg = (int)cdiv(pk_ne, zgroups);
+    k_colsqp<<<dim3(cdiv(pk_ne, 256), zgroups), 256, 0, stream>>>((const float*)A_dev, pk_ne, pk_ldp, rpg, Zp, lda);
+    k_colsq_finish<<<cdiv(lda, 256), 256, 0, stream>>>(Zp, zgroups, lda, n, q_dev);
+    launches += 2;
+    CK(cudaGetLastError());
+    return true;
+  }
   if (mf) {  // q from the recomputed column sums of squares; A itself is never stored or scaled
     CK(mf_atu(*mf, nullptr, nullptr, lda, Zp, true, stream));
     k_colsq_finish<<<cdiv(lda, 256), 256, 0, stream>>>(Zp, zgroups, lda, n, q_dev);
@@ -915,8 +1284,8 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
                       int* istop_host, double* rnorm_host, int check_every, bool x0_zero) {
   if (maxit == 0) maxit = 10 * (m + n + 50);
   const int64_t mpad = ((int64_t)m + 255) / 256 * 256;
-  const unsigned nb_av = cdiv(m, AV_ROWS);  // residual sweep
-  const unsigned nb_av2 = mf ? cdiv((int64_t)m * K8, 256)
+  const unsigned nb_av = packed ? cdiv(pk_ne, 8) : cdiv(m, AV_ROWS);  // residual sweep
+  const unsigned nb_av2 = packed ? cdiv(pk_ne, AVP_R) : mf ? cdiv((int64_t)m * K8, 256)
                             : fp32 ? (use_tma ? cdiv(m, AV3_ROWS) : av2_blocks<float>(*this)) : av2_blocks<double>(*this);
   mf_q = q_dev;
   if (mf && !x0_zero) { err = "the matrix-free operator needs a zero warm start"; return false; }
@@ -951,9 +1320,11 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
   k_pack<<<cdiv(lda * K8, 256), 256, 0, stream>>>(x_dev, n, k, lda, nullptr, Bp);
   // A^T r, alpha0, w = v
   if (fp32) launch_atu<float>(*this); else launch_atu<double>(*this);
-  k_atu_reduce<<<nb_red, kThreads, 0, stream>>>(Zp, zgroups, lda, n, sc, 1, V, part);
+  const double* qs = packed ? q_dev : nullptr;
+  k_atu_reduce<<<nb_red, kThreads, 0, stream>>>(Zp, zgroups, lda, n, sc, 1, V, part, qs);
   k_scalars<<<1, SCAL_THREADS, 0, stream>>>(sc, k, 1, part, nb_red, nactive);
-  if (fp32) k_update<float><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 1, V, W, X, (float*)Vs, part, 1);
+  if (fp32) k_update<float><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 1, V, W, X, (float*)Vs, part, 1, Vp, pk_ne,
+                                                              pk_ldp, qs);
   else k_update<double><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 1, V, W, X, (double*)Vs, part, 1);
   launches += x0_zero ? 10 : 11;
   CK(cudaGetLastError());
@@ -974,9 +1345,10 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
     cudaEventRecordWithFlags(pev[e + 2], stream, cudaEventRecordExternal);
     if (fp32) launch_atu<float>(*this); else launch_atu<double>(*this);
     cudaEventRecordWithFlags(pev[e + 3], stream, cudaEventRecordExternal);
-    k_atu_reduce<<<nb_red, kThreads, 0, stream>>>(Zp, zgroups, lda, n, sc, 0, V, part);
+    k_atu_reduce<<<nb_red, kThreads, 0, stream>>>(Zp, zgroups, lda, n, sc, 0, V, part, qs);
     k_scalars<<<1, SCAL_THREADS, 0, stream>>>(sc, k, 3, part, nb_red, nactive);
-    if (fp32) k_update<float><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 0, V, W, X, (float*)Vs, part, 1);
+    if (fp32) k_update<float><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 0, V, W, X, (float*)Vs, part, 1, Vp, pk_ne,
+                                                                pk_ldp, qs);
     else k_update<double><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 0, V, W, X, (double*)Vs, part, 1);
     cudaMemsetAsync(nactive, 0, sizeof(int), stream);
     k_scalars<<<1, SCAL_THREADS, 0, stream>>>(sc, k, 4, part, nb_upd, nactive);
@@ -1029,6 +1401,7 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
 }
 
 bool DenseLsqr::residual(const double* b_dev, const double* x_dev, const double* q_dev, double* r_dev) {
+  mf_q = q_dev;
   const int64_t mpad = ((int64_t)m + 255) / 256 * 256;
   k_pack<<<cdiv(mpad * K8, 256), 256, 0, stream>>>(b_dev, m, k, mpad, nullptr, Z);
   k_pack<<<cdiv(lda * K8, 256), 256, 0, stream>>>(x_dev, n, k, lda, q_dev, XsD);

@@ -47,6 +47,12 @@ struct DenseLsqr {
   CUtensorMap tm_av{};
   CUtensorMap tm_atu{};
   bool use_tma = false;
+  // packed symmetric-block single layer (A = Ap[i][6][ldp], m = n = 3 ne): the
+  // sweeps read 6 of the 9 entries of every 3x3 block; q is applied on the fly
+  bool packed = false;
+  int pk_ne = 0, pk_ldp = 0;
+  float* Vp = nullptr;          // [3][8][ldp] = q.V, sweep-1 operand of the packed layout
+  CUtensorMap tm_vp{};
   // matrix-free operator (A == nullptr): the sweeps recompute A's entries
   const struct MfOp* mf = nullptr;
   float* Yp = nullptr;          // [col blocks][m][8] partial products of A V

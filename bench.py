@@ -10,7 +10,7 @@ known velocity, six right-hand sides = the container's unit translations and
 rotations.  One solve = assembly of the 62400 x 62400 single-layer system,
 its right-hand sides, block LSQR of the six fields to eps, force and torque
 on the sphere (the 6x6 resistance tensor).  Inputs: synthetic meshes built
-in-process (no dataset); the 15.6 GB system matrix is far larger than L2, so
+in-process (no dataset); the 10.4 GB packed system matrix is far larger than L2, so
 no L2 flush is needed between timed steps.
 
 --impl ours (default): the mixed-precision GPU path through the C ABI.
@@ -31,7 +31,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Stokes resistance-tensor solves/s at <=1e-6 rel err: mixed/batched vs FP64 GPU"
 GOLDEN_TRUTH = os.path.join(ROOT, "tests", "golden", "c2_fp64_tensor.json")
-PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "k_av3_k_atu3_l4.md")
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "k_avp_k_atup_l4.md")
 
 
 def parse():
@@ -552,20 +552,22 @@ def main():
     # roofline of the dominant kernel (A*V sweep of LSQR), live CUDA-event timing
     peak, peak_kind = measured_peaks()
     lda = (C.n + 31) // 32 * 32
-    a_bytes = C.m * lda * 4
+    # packed symmetric 3x3 blocks: 6 FP32 values per (collocation point, element) pair
+    ne_sys = C.m // 3
+    a_bytes = 6 * ne_sys * ne_sys * 4
     av_ms = kt["av_ms"] / max(kt["av_launches"], 1)
     atu_ms = kt["atu_ms"] / max(kt["atu_launches"], 1)
     traffic = None
     if os.path.exists(PROFILE_TRAFFIC) and args.level == 5:
         with open(PROFILE_TRAFFIC) as f:
             for line in f:
-                if line.startswith("traffic_bytes_per_launch_k_av3_c2:"):
+                if line.startswith("traffic_bytes_per_launch_k_avp_c2:"):
                     traffic = float(line.split(":")[1])
-    roofline = {"bound": "hbm", "kernel": "k_av3 (LSQR A*V sweep, FP32 A streamed by TMA, 8 RHS)",
+    roofline = {"bound": "hbm", "kernel": "k_avp (LSQR A*V sweep over the packed symmetric 3x3 blocks, FP32, TMA, 8 RHS)",
                 "achieved": a_bytes / (av_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                 "frac": a_bytes / (av_ms * 1e-3) / 1e9 / peak, "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": a_bytes,
-                "other_sweep": {"kernel": "k_atu3 (A^T*U, TMA)", "achieved": a_bytes / (atu_ms * 1e-3) / 1e9,
+                "other_sweep": {"kernel": "k_atup (A^T*U, packed, TMA)", "achieved": a_bytes / (atu_ms * 1e-3) / 1e9,
                                 "frac": a_bytes / (atu_ms * 1e-3) / 1e9 / peak}}
 
     # end to end through the C ABI with host buffers (mesh upload + solve + R back)
@@ -615,7 +617,7 @@ def main():
                 "data": "synthetic (meshes generated in-process)",
                 "config": {"workload": name, "precision": "mixed", "unknowns": C.n,
                            "parallelism": "replicas" if world > 1 else "single GPU",
-                           "l2": "inputs larger than L2 (15.6 GB matrix), no flush"},
+                           "l2": "inputs larger than L2 (10.4 GB packed matrix), no flush"},
                 "rel_err_vs_fp64": rel_err, "drag_over_analytic": drag_ratio, "torque_over_analytic": torque_ratio,
                 "nit": [int(v) for v in nit], "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
                 "clocks": clk.summary(), "gpu_launches": kt["launches"] * world,
