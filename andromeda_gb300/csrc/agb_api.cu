@@ -741,21 +741,23 @@ int agb_assemble(agb_context* c, int precision) {
     std::vector<double> cs(ldp, 0.0);
     for (int p = 0; p < c->ne; ++p) cs[p] = -c->normMul[c->wallIdx[p]] / c->diff;
     if (f32) {
-      // packed symmetric blocks: Ap[i][6][ldp] (2/3 of the bytes of the m x lda matrix)
-      CUDA_OR_FAIL(c, cudaMalloc(&c->d_A, (size_t)c->ne * 6 * ldp * sizeof(float)));
-      CUDA_OR_FAIL(c, cudaMemsetAsync(c->d_A, 0, (size_t)c->ne * 6 * ldp * sizeof(float), c->stream));
+      // packed symmetric blocks (pk_idx layout, 2/3 of the bytes of the m x lda matrix)
+      const int pldp = (c->ne + 63) / 64 * 64;
+      CUDA_OR_FAIL(c, cudaMalloc(&c->d_A, (size_t)c->ne * 6 * pldp * sizeof(float)));
+      CUDA_OR_FAIL(c, cudaMemsetAsync(c->d_A, 0, (size_t)c->ne * 6 * pldp * sizeof(float), c->stream));
       std::vector<float> csf(cs.begin(), cs.end());
       CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_colscale, csf.data(), ldp * sizeof(float), cudaMemcpyHostToDevice, c->stream));
       CUDA_OR_FAIL(c, launch_expand_points<float>(c->ne, ldp, c->d_geom, c->rule, (QPt<float>*)c->d_pts,
                                                   (float*)c->d_src, (float*)c->d_nrm, c->stream));
       cudaEventRecord(c->tev[0], c->stream);
-      CUDA_OR_FAIL(c, launch_stokes_G_packed(c->ne, Q, ldp, (const QPt<float>*)c->d_pts, (const float*)c->d_src,
-                                             (const float*)c->d_colscale, (float*)c->d_A, c->stream));
+      CUDA_OR_FAIL(c, launch_stokes_G_packed(c->ne, Q, ldp, pldp, (const QPt<float>*)c->d_pts,
+                                             (const float*)c->d_src, (const float*)c->d_colscale, (float*)c->d_A,
+                                             c->stream));
       cudaEventRecord(c->tev[1], c->stream);
-      CUDA_OR_FAIL(c, launch_stokes_self_packed(c->ne, ldp, c->d_geom, c->diff, (float*)c->d_A, c->stream));
+      CUDA_OR_FAIL(c, launch_stokes_self_packed(c->ne, pldp, c->d_geom, c->diff, (float*)c->d_A, c->stream));
       c->lsqr.packed = true;
       c->lsqr.pk_ne = c->ne;
-      c->lsqr.pk_ldp = ldp;
+      c->lsqr.pk_ldp = pldp;
       c->nlaunch += 3;  // expand, single layer, self blocks
     } else {
       CUDA_OR_FAIL(c, cudaMemcpyAsync(c->d_colscale, cs.data(), ldp * sizeof(double), cudaMemcpyHostToDevice, c->stream));
@@ -797,7 +799,7 @@ int agb_get_system(agb_context* c, int scaled, double* A, double* q) {
   std::vector<double> qh(c->lda);
   CUDA_OR_FAIL(c, cudaMemcpy(qh.data(), c->d_q, c->lda * sizeof(double), cudaMemcpyDeviceToHost));
   if (q) std::copy(qh.begin(), qh.begin() + c->n, q);
-  if (A && c->lsqr.packed) {  // expand the symmetric blocks: A[3i+a][b ne + j] = Ap[i][sym(a,b)][j]
+  if (A && c->lsqr.packed) {  // expand the symmetric blocks: A[3i+a][b ne + j] = Ap[pk_idx(i, sym(a,b), j)]
     const int ne = c->lsqr.pk_ne, ldp = c->lsqr.pk_ldp;
     static const int sym[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
     std::vector<float> row((size_t)6 * ldp);
@@ -807,7 +809,7 @@ int agb_get_system(agb_context* c, int scaled, double* A, double* q) {
       for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 3; ++b)
           for (int j = 0; j < ne; ++j) {
-            const double v = (double)row[(size_t)sym[a][b] * ldp + j];
+            const double v = (double)row[pk_idx(0, sym[a][b], j, ldp)];
             const size_t col = (size_t)b * ne + j;
             A[(size_t)(3 * i + a) * c->n + col] = scaled ? v * qh[col] : v;
           }

@@ -164,9 +164,9 @@ template <typename T> struct StkTile;
 template <> struct StkTile<float> { static constexpr int RS = 8; static constexpr int NW = 8; };
 template <> struct StkTile<double> { static constexpr int RS = 4; static constexpr int NW = 8; };
 
-// PACKED: the 3x3 blocks are symmetric, so the matrix is stored as six
-// planes Ap[i][c][ldp] (c = xx, xy, xz, yy, yz, zz; lda = 6 ldp), 2/3 of the
-// bytes of the full row-major A[3i+a][b ne + j].
+// PACKED: the 3x3 blocks are symmetric, so the matrix is stored with six
+// values per block in the layout of pk_idx (lda = 6 x the plane length), 2/3
+// of the bytes of the full row-major A[3i+a][b ne + j].
 template <typename T, bool PACKED = false>
 __global__ void __launch_bounds__(StkTile<T>::NW * 32) k_stokes_G(int ne, int Q, int ldp, const QPt<T>* __restrict__ pts,
                                                                  const T* __restrict__ src, const T* __restrict__ colscale,
@@ -226,8 +226,9 @@ __global__ void __launch_bounds__(StkTile<T>::NW * 32) k_stokes_G(int ne, int Q,
           const T gyy = scale * (acc[r][0] + acc[r][4]), gyz = scale * acc[r][5];
           const T gzz = scale * (acc[r][0] + acc[r][6]);
           if (PACKED) {
-            T* pr = A + (int64_t)i * lda + j;
-            pr[0] = gxx; pr[ldp] = gxy; pr[2 * ldp] = gxz; pr[3 * ldp] = gyy; pr[4 * ldp] = gyz; pr[5 * ldp] = gzz;
+            const int pl = (int)(lda / 6);  // plane length of the packed layout
+            T* pr = A + pk_idx(i, 0, j, pl);
+            pr[0] = gxx; pr[64] = gxy; pr[128] = gxz; pr[192] = gyy; pr[256] = gyz; pr[320] = gzz;
           } else {
             T* r0 = A + (int64_t)(3 * i) * lda + j;
             T* r1 = r0 + lda;
@@ -261,7 +262,7 @@ cudaError_t launch_stokes_G(int ne, int Q, int ldp, const QPt<T>* pts, const T* 
 template cudaError_t launch_stokes_G<float>(int, int, int, const QPt<float>*, const float*, const float*, float*, int64_t,
                                             cudaStream_t);
 
-cudaError_t launch_stokes_G_packed(int ne, int Q, int ldp, const QPt<float>* pts, const float* src,
+cudaError_t launch_stokes_G_packed(int ne, int Q, int ldp, int pldp, const QPt<float>* pts, const float* src,
                                    const float* colscale, float* Ap, cudaStream_t s) {
   constexpr int NW = StkTile<float>::NW;
   const size_t smem = (size_t)Q * 32 * sizeof(QPt<float>);
@@ -273,7 +274,7 @@ cudaError_t launch_stokes_G_packed(int ne, int Q, int ldp, const QPt<float>* pts
   const int spc = (int)cdiv(ne, ychunks);
   ychunks = (int)cdiv(ne, spc);
   k_stokes_G<float, true><<<dim3(tiles, ychunks), NW * 32, smem, s>>>(ne, Q, ldp, pts, src, colscale, spc, Ap,
-                                                                       6 * (int64_t)ldp);
+                                                                       6 * (int64_t)pldp);
   return cudaGetLastError();
 }
 
@@ -285,8 +286,8 @@ __global__ void k_stokes_self_packed(int ne, int ldp, const ElemGeom* __restrict
   double g[6];
   agb_sing::tri_stokes(G.v[0], G.v[1], G.v[2], G.area, 4, g);
   const double sc = -G.multi / diff;
-  float* pr = Ap + (int64_t)p * 6 * ldp + p;
-  for (int c = 0; c < 6; ++c) pr[(int64_t)c * ldp] = (float)(sc * g[c]);
+  float* pr = Ap + pk_idx(p, 0, p, ldp);
+  for (int c = 0; c < 6; ++c) pr[c * 64] = (float)(sc * g[c]);
 }
 cudaError_t launch_stokes_self_packed(int ne, int ldp, const ElemGeom* geom, double diff, float* Ap, cudaStream_t s) {
   k_stokes_self_packed<<<cdiv(ne, 64), 64, 0, s>>>(ne, ldp, geom, diff, Ap);

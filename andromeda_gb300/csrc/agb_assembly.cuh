@@ -31,12 +31,13 @@ cudaError_t launch_expand_points(int ne, int ldp, const ElemGeom* geom, const Ru
 template <typename T>
 cudaError_t launch_stokes_G(int ne, int Q, int ldp, const QPt<T>* pts, const T* src, const T* colscale, T* A,
                             int64_t lda, cudaStream_t s);
-// The same single layer in the packed layout of the symmetric 3x3 blocks:
-// Ap[i][c][ldp], c = xx, xy, xz, yy, yz, zz (row pitch 6 ldp floats), with the
-// analytic self blocks; 2/3 of the bytes of the full matrix.
-cudaError_t launch_stokes_G_packed(int ne, int Q, int ldp, const QPt<float>* pts, const float* src,
+// The same single layer in the packed layout of the symmetric 3x3 blocks
+// (pk_idx, plane length pldp = multiple of 64, row pitch 6 pldp floats), with
+// the analytic self blocks; 2/3 of the bytes of the full matrix.  ldp is the
+// pitch of the point table.
+cudaError_t launch_stokes_G_packed(int ne, int Q, int ldp, int pldp, const QPt<float>* pts, const float* src,
                                    const float* colscale, float* Ap, cudaStream_t s);
-cudaError_t launch_stokes_self_packed(int ne, int ldp, const ElemGeom* geom, double diff, float* Ap, cudaStream_t s);
+cudaError_t launch_stokes_self_packed(int ne, int pldp, const ElemGeom* geom, double diff, float* Ap, cudaStream_t s);
 // Self-element 3x3 blocks, analytic FP64 (Ren-Chan), written in T.
 template <typename T>
 cudaError_t launch_stokes_self(int ne, const ElemGeom* geom, double diff, T* A, int64_t lda, cudaStream_t s);

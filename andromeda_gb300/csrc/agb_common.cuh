@@ -48,3 +48,12 @@ struct IntegOpt {
   int near_depth = 0;
   bool is_default() const { return sing == 0 && !(near_eta > 0.0 && near_depth > 0); }
 };
+
+// Packed symmetric-block layout of the Stokes single layer (mixed path): the
+// six components c = xx, xy, xz, yy, yz, zz of block (i, j) are stored as
+// Ap[i][j / 64][c][j % 64] -- within a row, every 64 element columns carry all
+// six planes contiguously (1.5 KB runs); ldp (columns per plane) is a multiple of 64.
+__host__ __device__ __forceinline__ int64_t pk_idx(int i, int c, int j, int ldp) {
+  return (int64_t)i * 6 * ldp + (int64_t)(j >> 6) * 384 + c * 64 + (j & 63);
+}
+

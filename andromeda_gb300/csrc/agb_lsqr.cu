@@ -474,8 +474,8 @@ __global__ void __launch_bounds__(ATU3_THREADS, 1) k_atu3(const __grid_constant_
 }
 
 // ---------------------------------------------------------------------------
-// Sweeps over the packed single layer (symmetric 3x3 blocks stored once):
-// Ap[i][c][ldp] (c = xx, xy, xz, yy, yz, zz), A[3i+a][b ne + j] = Ap[i][sym(a,b)][j].
+// Sweeps over the packed single layer (symmetric 3x3 blocks stored once, in
+// the layout of pk_idx): A[3i+a][b ne + j] = Ap[pk_idx(i, sym(a,b), j)].
 // The column scaling of lsqr_precon is applied on the fly: sweep 1 reads
 // W = q.V (written by k_update into Vp[b][k][ldp]), sweep 2's partials are
 // scaled by q in k_atu_reduce.
@@ -534,9 +534,8 @@ __global__ void __launch_bounds__(AVP_WARPS * 32, 1) k_avp(const __grid_constant
     if (k >= AVP_ST) mbar_wait_bounded(&empty[s], (uint32_t)(((k / AVP_ST) - 1) & 1), errflag);
     const int j0 = k * AVP_BC;
     mbar_expect_tx(&full[s], (uint32_t)(AVP_STAGE_A + AVP_STAGE_W));
-    float* dA = sA + (size_t)s * 6 * AVP_R * AVP_BC;
-#pragma unroll
-    for (int c = 0; c < 6; ++c) tma_load_2d(dA + (size_t)c * AVP_R * AVP_BC, &tmA, c * ldp + j0, row_base, &full[s]);
+    // one 3-D box: 32 rows x (6 planes x 64 columns), 1.5 KB contiguous per row
+    tma_load_3d(sA + (size_t)s * 6 * AVP_R * AVP_BC, &tmA, 0, 6 * k, row_base, &full[s]);
     tma_load_2d(sW + (size_t)s * 3 * K8 * AVP_BC, &tmW, j0, 0, &full[s]);
   };
   if (threadIdx.x == 0)
@@ -552,7 +551,7 @@ __global__ void __launch_bounds__(AVP_WARPS * 32, 1) k_avp(const __grid_constant
   for (int k = 0; k < nst; ++k) {
     const int s = k % AVP_ST;
     mbar_wait_bounded(&full[s], (uint32_t)((k / AVP_ST) & 1), errflag);
-    const float* tA = sA + (size_t)s * 6 * AVP_R * AVP_BC + (2 * warp) * AVP_BC + lane * 2;
+    const float* tA = sA + (size_t)s * 6 * AVP_R * AVP_BC + (2 * warp) * 6 * AVP_BC + lane * 2;  // [row][c][64]
     const float* tW = sW + (size_t)s * 3 * K8 * AVP_BC + lane * 2;
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
@@ -563,7 +562,7 @@ __global__ void __launch_bounds__(AVP_WARPS * 32, 1) k_avp(const __grid_constant
       for (int r = 0; r < 2; ++r)
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-          const float2 g = *reinterpret_cast<const float2*>(tA + (size_t)sym6(a, b) * AVP_R * AVP_BC + r * AVP_BC);
+          const float2 g = *reinterpret_cast<const float2*>(tA + r * 6 * AVP_BC + sym6(a, b) * AVP_BC);
 #pragma unroll
           for (int c = 0; c < K8; ++c) acc[r][a][c] = fmaf(g.y, w[c].y, fmaf(g.x, w[c].x, acc[r][a][c]));
         }
@@ -645,9 +644,8 @@ __global__ void __launch_bounds__(ATUP_C, 1) k_atup(const __grid_constant__ CUte
     const int rb = r0 + k * ATUP_RS;
     const int nr = min(ATUP_RS, r1 - rb);
     mbar_expect_tx(&full[s], (uint32_t)(ATUP_STAGE_A + (size_t)3 * nr * K8 * sizeof(float)));
-    float* dA = sA + (size_t)s * 6 * ATUP_RS * ATUP_C;
-#pragma unroll
-    for (int c = 0; c < 6; ++c) tma_load_2d(dA + (size_t)c * ATUP_RS * ATUP_C, &tmA, c * ldp + j0, rb, &full[s]);
+    // one 3-D box: 8 rows x (4 column blocks x 6 planes x 64 columns), 6 KB contiguous per row
+    tma_load_3d(sA + (size_t)s * 6 * ATUP_RS * ATUP_C, &tmA, 0, 6 * (j0 / 64), rb, &full[s]);
     bulk_g2s(sU + (size_t)s * 3 * ATUP_RS * K8, Us + (int64_t)3 * rb * K8, (uint32_t)(3 * nr * K8 * sizeof(float)),
              &full[s]);
   };
@@ -664,12 +662,13 @@ __global__ void __launch_bounds__(ATUP_C, 1) k_atup(const __grid_constant__ CUte
     mbar_wait_bounded(&full[s], (uint32_t)((k / ATUP_ST) & 1), errflag);
     const int rb = r0 + k * ATUP_RS;
     const int nr = min(ATUP_RS, r1 - rb);
-    const float* tA = sA + (size_t)s * 6 * ATUP_RS * ATUP_C + threadIdx.x;
+    // [row][column block][c][64]: the thread's column is (t / 64, t % 64)
+    const float* tA = sA + (size_t)s * 6 * ATUP_RS * ATUP_C + (threadIdx.x >> 6) * 384 + (threadIdx.x & 63);
     const float* tU = sU + (size_t)s * 3 * ATUP_RS * K8;
     for (int r = 0; r < nr; ++r) {
       float g6[6];
 #pragma unroll
-      for (int c = 0; c < 6; ++c) g6[c] = tA[(size_t)c * ATUP_RS * ATUP_C + r * ATUP_C];
+      for (int c = 0; c < 6; ++c) g6[c] = tA[r * 6 * ATUP_C + c * 64];
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
         const float4 u0 = *reinterpret_cast<const float4*>(tU + (3 * r + a) * K8);
@@ -716,11 +715,11 @@ __global__ void __launch_bounds__(256) k_residp(const float* __restrict__ Ap, in
 #pragma unroll
     for (int c = 0; c < K8; ++c) acc[a][c] = 0.0;
   if (i < ne) {
-    const float* row = Ap + (int64_t)i * 6 * ldp;
     for (int j = lane; j < ne; j += 32) {
       double g6[6];
+      const float* pj = Ap + pk_idx(i, 0, j, ldp);
 #pragma unroll
-      for (int c = 0; c < 6; ++c) g6[c] = (double)row[(int64_t)c * ldp + j];
+      for (int c = 0; c < 6; ++c) g6[c] = (double)pj[c * 64];
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
         const double* x = Xs + ((int64_t)b * ne + j) * K8;
@@ -769,10 +768,10 @@ __global__ void k_colsqp(const float* __restrict__ Ap, int ne, int ldp, int rows
   const int r0 = g * rows_per_group, r1 = min(ne, r0 + rows_per_group);
   double s[6] = {0, 0, 0, 0, 0, 0};
   for (int i = r0; i < r1; ++i) {
-    const float* row = Ap + (int64_t)i * 6 * ldp + j;
+    const float* pj = Ap + pk_idx(i, 0, j, ldp);
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
-      const double v = (double)row[(int64_t)c * ldp];
+      const double v = (double)pj[c * 64];
       s[c] += v * v;
     }
   }
@@ -1042,6 +1041,35 @@ bool make_tensor_map_2d(CUtensorMap* tm, const void* A, int64_t lda, int m, int 
   return true;
 }
 
+// 3-D tensor map of the packed layout (pk_idx): dims {64 columns, 6 x pldp/64
+// (plane, column block), rows}, box {64, box_y, box_z}.
+static bool make_packed_map(CUtensorMap* tm, const void* Ap, int pldp, int ne, int box_y, int box_z,
+                            std::string& err) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    cudaDriverEntryPointQueryResult q;
+    void* fn = nullptr;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &fn, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+      err = "cuTensorMapEncodeTiled not available";
+      return false;
+    }
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  const cuuint64_t dims[3] = {64, (cuuint64_t)6 * (pldp / 64), (cuuint64_t)ne};
+  const cuuint64_t strides[2] = {64 * sizeof(float), (cuuint64_t)6 * pldp * sizeof(float)};
+  const cuuint32_t box[3] = {64, (cuuint32_t)box_y, (cuuint32_t)box_z};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = encode(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(Ap), dims, strides, box, estr,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    err = "cuTensorMapEncodeTiled (packed) failed (" + std::to_string((int)r) + ")";
+    return false;
+  }
+  return true;
+}
+
 template <typename T>
 static void launch_resid(const DenseLsqr& L, const double* Xs, const double* Bp) {
   if (L.packed) {
@@ -1149,12 +1177,12 @@ bool DenseLsqr::setup(const void* A_dev, bool is_fp32, int m_, int n_, int64_t l
   use_tma = fp32 && getenv("AGB_NO_TMA") == nullptr && A_dev != nullptr && !packed;
   if (!A_dev && !mf) { err = "no matrix and no matrix-free operator"; return false; }
   if (packed) {
-    if (!fp32 || 3 * pk_ne != m || m != n || pk_ldp % 32 != 0 || pk_ldp < pk_ne) {
+    if (!fp32 || 3 * pk_ne != m || m != n || pk_ldp % 64 != 0 || pk_ldp < pk_ne) {
       err = "packed layout: bad sizes";
       return false;
     }
-    if (!make_tensor_map_2d(&tm_av, A_dev, 6 * (int64_t)pk_ldp, pk_ne, AVP_BC, AVP_R, err)) return false;
-    if (!make_tensor_map_2d(&tm_atu, A_dev, 6 * (int64_t)pk_ldp, pk_ne, ATUP_C, ATUP_RS, err)) return false;
+    if (!make_packed_map(&tm_av, A_dev, pk_ldp, pk_ne, 6, AVP_R, err)) return false;
+    if (!make_packed_map(&tm_atu, A_dev, pk_ldp, pk_ne, 6 * (ATUP_C / 64), ATUP_RS, err)) return false;
     CK(cudaMalloc(&Vp, (size_t)3 * K8 * pk_ldp * sizeof(float)));
     CK(cudaMemsetAsync(Vp, 0, (size_t)3 * K8 * pk_ldp * sizeof(float), stream));
     if (!make_tensor_map_2d(&tm_vp, Vp, pk_ldp, 3 * K8, AVP_BC, 3 * K8, err)) return false;
