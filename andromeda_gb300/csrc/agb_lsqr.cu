@@ -614,12 +614,12 @@ __global__ void __launch_bounds__(AVP_WARPS * 32, 1) k_avp(const __grid_constant
 }
 
 // Zp[g][b ne + j][k] = sum_{i in group g} sum_a Ap[i][sym(a,b)][j] U[3i+a][k]; one thread per column j.
-constexpr int ATUP_C = 256, ATUP_RS = 8, ATUP_ST = 4;
+constexpr int ATUP_C = 256, ATUP_RS = 8, ATUP_ST = 2;  // 97.5 KB: two CTAs (16 warps) per SM
 constexpr size_t ATUP_STAGE_A = 6 * (size_t)ATUP_RS * ATUP_C * sizeof(float);  // 48 KB
 constexpr size_t ATUP_STAGE_U = 3 * (size_t)ATUP_RS * K8 * sizeof(float);      // 768 B
 constexpr size_t ATUP_SMEM = ATUP_ST * (ATUP_STAGE_A + ATUP_STAGE_U);
 
-__global__ void __launch_bounds__(ATUP_C, 1) k_atup(const __grid_constant__ CUtensorMap tmA, int ne, int ldp,
+__global__ void __launch_bounds__(ATUP_C, 2) k_atup(const __grid_constant__ CUtensorMap tmA, int ne, int ldp,
                                                    int64_t lda, const float* __restrict__ Us, int rows_per_group,
                                                    double* __restrict__ Zp, int* errflag) {
   extern __shared__ __align__(1024) unsigned char atup_smem[];
@@ -1217,16 +1217,19 @@ bool DenseLsqr::setup(const void* A_dev, bool is_fp32, int m_, int n_, int64_t l
     if (best < 0 && G == gmax) groups = G;
   }
   zgroups = groups;
-  if (packed) {  // row groups of the packed A^T U tiles (one CTA per SM): fill whole waves
+  if (packed) {  // row groups of the packed A^T U tiles: fill whole waves of resident CTAs
+    int occ = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_atup, ATUP_C, ATUP_SMEM);
+    const int pslots = nsm * std::max(occ, 1);
     const int cb = (int)cdiv(pk_ldp, ATUP_C);
     const int gmx = std::max(1, std::min(64, (int)cdiv(pk_ne, 64)));
     double bestp = -1.0;
     zgroups = 1;
     for (int G = 1; G <= gmx; ++G) {
       const int64_t items = (int64_t)cb * G;
-      const double eff = (double)items / (double)(cdiv(items, nsm) * (int64_t)nsm);
+      const double eff = (double)items / (double)(cdiv(items, pslots) * (int64_t)pslots);
       const double score = eff - 0.002 * G;
-      if (items >= nsm && score > bestp) { bestp = score; zgroups = G; }
+      if (items >= pslots && score > bestp) { bestp = score; zgroups = G; }
       if (bestp < 0 && G == gmx) zgroups = G;
     }
   }
