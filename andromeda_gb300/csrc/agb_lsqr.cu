@@ -480,8 +480,11 @@ __global__ void __launch_bounds__(ATU3_THREADS, 1) k_atu3(const __grid_constant_
 // W = q.V (written by k_update into Vp[b][k][ldp]), sweep 2's partials are
 // scaled by q in k_atu_reduce.
 // ---------------------------------------------------------------------------
+// rows per CTA: at most 30 (two per compute warp, plus one producer warp); the
+// launch picks an even count that fills whole waves (row blocks / resident
+// CTAs close to an integer)
 constexpr int AVP_R = 32, AVP_BC = 64, AVP_ST = 4, AVP_WARPS = AVP_R / 2;
-constexpr size_t AVP_STAGE_A = 6 * (size_t)AVP_R * AVP_BC * sizeof(float);   // 48 KB
+constexpr size_t AVP_STAGE_A = 6 * (size_t)AVP_R * AVP_BC * sizeof(float);   // 48 KB (space of 32 rows)
 constexpr size_t AVP_STAGE_W = 3 * (size_t)K8 * AVP_BC * sizeof(float);      // 6 KB
 constexpr size_t AVP_SMEM = AVP_ST * (AVP_STAGE_A + AVP_STAGE_W);
 
@@ -510,7 +513,7 @@ __device__ __forceinline__ void reduce_scatter32(float (&v)[32], int lane) {
 // reduce-scattered over the warp into one FP64 running sum per lane.
 __global__ void __launch_bounds__(AVP_WARPS * 32, 1) k_avp(const __grid_constant__ CUtensorMap tmA,
                                                           const __grid_constant__ CUtensorMap tmW, int ne, int ldp,
-                                                          const LsqrScalars* sc, double* __restrict__ Y,
+                                                          int rows, const LsqrScalars* sc, double* __restrict__ Y,
                                                           float* __restrict__ Ys, double* __restrict__ part,
                                                           int* errflag) {
   extern __shared__ __align__(1024) unsigned char avp_smem[];
@@ -519,12 +522,14 @@ __global__ void __launch_bounds__(AVP_WARPS * 32, 1) k_avp(const __grid_constant
   __shared__ __align__(8) uint64_t full[AVP_ST], empty[AVP_ST];
   __shared__ double sPart[AVP_WARPS][K8];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int row_base = blockIdx.x * AVP_R;
+  const int row_base = blockIdx.x * rows;
+  const int nwarps = rows / 2;
+  const uint32_t stage_bytes = (uint32_t)(rows * 6 * AVP_BC * sizeof(float) + AVP_STAGE_W);
   const int nst = (ldp + AVP_BC - 1) / AVP_BC;
   if (threadIdx.x == 0) {
     for (int s = 0; s < AVP_ST; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], AVP_WARPS);
+      mbar_init(&empty[s], nwarps);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -533,13 +538,19 @@ __global__ void __launch_bounds__(AVP_WARPS * 32, 1) k_avp(const __grid_constant
     const int s = k % AVP_ST;
     if (k >= AVP_ST) mbar_wait_bounded(&empty[s], (uint32_t)(((k / AVP_ST) - 1) & 1), errflag);
     const int j0 = k * AVP_BC;
-    mbar_expect_tx(&full[s], (uint32_t)(AVP_STAGE_A + AVP_STAGE_W));
+    mbar_expect_tx(&full[s], stage_bytes);
     // one 3-D box: 32 rows x (6 planes x 64 columns), 1.5 KB contiguous per row
     tma_load_3d(sA + (size_t)s * 6 * AVP_R * AVP_BC, &tmA, 0, 6 * k, row_base, &full[s]);
     tma_load_2d(sW + (size_t)s * 3 * K8 * AVP_BC, &tmW, j0, 0, &full[s]);
   };
-  if (threadIdx.x == 0)
-    for (int k = 0; k < AVP_ST && k < nst; ++k) issue(k);
+  // warp nwarps is the producer: it only issues the stages (waiting for their
+  // slots to be released), so no compute warp ever blocks on a refill
+  double ssq = 0.0;
+  if (warp == nwarps) {
+    if (lane == 0)
+      for (int k = 0; k < nst; ++k) issue(k);
+    __syncwarp();
+  } else {
   float acc[2][3][K8];
   double dacc[2] = {0.0, 0.0};
 #pragma unroll
@@ -569,7 +580,6 @@ __global__ void __launch_bounds__(AVP_WARPS * 32, 1) k_avp(const __grid_constant
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
-    if (threadIdx.x == 0 && k + AVP_ST < nst) issue(k + AVP_ST);
     if ((k & 15) == 15 || k == nst - 1) {
 #pragma unroll
       for (int r = 0; r < 2; ++r) {
@@ -586,7 +596,6 @@ __global__ void __launch_bounds__(AVP_WARPS * 32, 1) k_avp(const __grid_constant
     }
   }
   // lane a*8+c holds row 3i+a, right-hand side c of each of the warp's two rows
-  double ssq = 0.0;
   if (lane < 3 * K8) {
     const int a = lane / K8, c = lane % K8;
 #pragma unroll
@@ -605,10 +614,11 @@ __global__ void __launch_bounds__(AVP_WARPS * 32, 1) k_avp(const __grid_constant
   ssq += __shfl_down_sync(0xffffffffu, ssq, 8);
   ssq += __shfl_down_sync(0xffffffffu, ssq, 16);
   if (lane < K8) sPart[warp][lane] = ssq;
+  }
   __syncthreads();
   if (threadIdx.x < K8) {
     double t = 0.0;
-    for (int w = 0; w < AVP_WARPS; ++w) t += sPart[w][threadIdx.x];
+    for (int w = 0; w < nwarps; ++w) t += sPart[w][threadIdx.x];
     part[(int64_t)blockIdx.x * K8 + threadIdx.x] = t;
   }
 }
@@ -1086,8 +1096,9 @@ static unsigned av2_blocks(const DenseLsqr& L) { return cdiv(L.m, AV2<T>::WARPS 
 template <typename T>
 static void launch_av2(const DenseLsqr& L) {
   if (L.packed) {
-    k_avp<<<cdiv(L.pk_ne, AVP_R), AVP_WARPS * 32, AVP_SMEM, L.stream>>>(L.tm_av, L.tm_vp, L.pk_ne, L.pk_ldp, L.sc,
-                                                                        L.Y, (float*)L.Ys, L.part, L.errflag);
+    k_avp<<<cdiv(L.pk_ne, L.avp_rows), (L.avp_rows / 2 + 1) * 32, AVP_SMEM, L.stream>>>(L.tm_av, L.tm_vp, L.pk_ne, L.pk_ldp,
+                                                                              L.avp_rows, L.sc, L.Y, (float*)L.Ys,
+                                                                              L.part, L.errflag);
     return;
   }
   if (L.mf) {
@@ -1181,7 +1192,19 @@ bool DenseLsqr::setup(const void* A_dev, bool is_fp32, int m_, int n_, int64_t l
       err = "packed layout: bad sizes";
       return false;
     }
-    if (!make_packed_map(&tm_av, A_dev, pk_ldp, pk_ne, 6, AVP_R, err)) return false;
+    {  // rows per A*V CTA (one CTA per SM): the even count <= 30 whose row blocks fill waves best
+      int dev = 0, nsm_ = 152;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev);
+      double best_eff = -1.0;
+      avp_rows = AVP_R;
+      for (int R = AVP_R - 2; R >= 20; R -= 2) {  // + one producer warp: at most 16 warps
+        const int64_t nrb = cdiv(pk_ne, R);
+        const double eff = (double)nrb / (double)(cdiv(nrb, nsm_) * (int64_t)nsm_);
+        if (eff > best_eff + 1e-9) { best_eff = eff; avp_rows = R; }
+      }
+    }
+    if (!make_packed_map(&tm_av, A_dev, pk_ldp, pk_ne, 6, avp_rows, err)) return false;
     if (!make_packed_map(&tm_atu, A_dev, pk_ldp, pk_ne, 6 * (ATUP_C / 64), ATUP_RS, err)) return false;
     CK(cudaMalloc(&Vp, (size_t)3 * K8 * pk_ldp * sizeof(float)));
     CK(cudaMemsetAsync(Vp, 0, (size_t)3 * K8 * pk_ldp * sizeof(float), stream));
@@ -1316,7 +1339,7 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
   if (maxit == 0) maxit = 10 * (m + n + 50);
   const int64_t mpad = ((int64_t)m + 255) / 256 * 256;
   const unsigned nb_av = packed ? cdiv(pk_ne, 8) : cdiv(m, AV_ROWS);  // residual sweep
-  const unsigned nb_av2 = packed ? cdiv(pk_ne, AVP_R) : mf ? cdiv((int64_t)m * K8, 256)
+  const unsigned nb_av2 = packed ? cdiv(pk_ne, avp_rows) : mf ? cdiv((int64_t)m * K8, 256)
                             : fp32 ? (use_tma ? cdiv(m, AV3_ROWS) : av2_blocks<float>(*this)) : av2_blocks<double>(*this);
   mf_q = q_dev;
   if (mf && !x0_zero) { err = "the matrix-free operator needs a zero warm start"; return false; }
