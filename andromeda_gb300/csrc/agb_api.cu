@@ -1144,7 +1144,7 @@ int agb_solve_fields(agb_context* c, int nrhs, const double* u_in, const double*
 
 // One body of a batch on the device: pieces of the wave's arena.
 struct BatchSlot {
-  int body = 0, nn = 0, ne = 0, ldp = 0, m = 0, n = 0, groups = 1, na = 0;
+  int body = 0, nn = 0, ne = 0, ldp = 0, pldp = 0, m = 0, n = 0, groups = 1, na = 0;
   int64_t lda = 0;
   size_t o_xyz, o_et, o_con, o_wall, o_geom, o_pts, o_src, o_nrm, o_cs, o_A, o_q, o_u, o_act, o_ract, o_rhs, o_x,
       o_ft, o_P;  // device offsets
@@ -1206,6 +1206,7 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
     b.nn = node_off[i + 1] - node_off[i];
     b.ne = elem_off[i + 1] - elem_off[i];
     b.ldp = (b.ne + 31) / 32 * 32;
+    b.pldp = (b.ne + 63) / 64 * 64;
     b.m = b.n = 3 * b.ne;
     b.lda = ((int64_t)b.n + 31) / 32 * 32;
     b.groups = std::max(1, std::min(32, b.m / 512));
@@ -1220,7 +1221,8 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
     b.o_geom = take((size_t)b.ne * sizeof(ElemGeom));
     b.o_pts = take((size_t)Q * b.ldp * sizeof(QPt<float>));
     b.o_src = take(3 * (size_t)b.ldp * 4); b.o_nrm = take(3 * (size_t)b.ldp * 4);
-    b.o_A = take((size_t)b.m * b.lda * 4); b.o_q = take((size_t)b.lda * 8);
+    b.o_A = take((size_t)b.ne * 6 * b.pldp * 4);  // packed symmetric blocks (pk_idx layout)
+    b.o_q = take((size_t)b.lda * 8);
     b.o_rhs = take(6 * (size_t)b.m * 8); b.o_x = take(6 * (size_t)b.n * 8); b.o_ft = take(6 * AGB_MAX_RHS * 8);
     b.o_P = take((size_t)b.groups * b.lda * 8);
     dev_bytes[i] = o;
@@ -1356,14 +1358,13 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
       if (e == cudaSuccess)
         e = launch_expand_points<float>(b.ne, b.ldp, geom, rule, (QPt<float>*)(d + b.o_pts), (float*)(d + b.o_src),
                                         (float*)(d + b.o_nrm), st);
-      if (e == cudaSuccess && b.lda > b.n)
-        e = cudaMemset2DAsync((char*)A + b.n * 4, b.lda * 4, 0, (b.lda - b.n) * 4, b.m, st);
+      if (e == cudaSuccess) e = cudaMemsetAsync(A, 0, (size_t)b.ne * 6 * b.pldp * 4, st);  // zero pad columns
       if (e == cudaSuccess)
-        e = launch_stokes_G<float>(b.ne, Q, b.ldp, (const QPt<float>*)(d + b.o_pts), (const float*)(d + b.o_src),
-                                   (const float*)(d + b.o_cs), A, b.lda, st);
-      if (e == cudaSuccess) e = launch_stokes_self<float>(b.ne, geom, 1.0, A, b.lda, st);
+        e = launch_stokes_G_packed(b.ne, Q, b.ldp, b.pldp, (const QPt<float>*)(d + b.o_pts),
+                                   (const float*)(d + b.o_src), (const float*)(d + b.o_cs), A, st);
+      if (e == cudaSuccess) e = launch_stokes_self_packed(b.ne, b.pldp, geom, 1.0, A, st);
       if (e == cudaSuccess)
-        e = dense_colscale_f32(A, b.lda, b.m, b.n, (double*)(d + b.o_q), (double*)(d + b.o_P), b.groups, st);
+        e = packed_colnorms(A, b.ne, b.pldp, b.lda, (double*)(d + b.o_q), (double*)(d + b.o_P), b.groups, st);
       if (e == cudaSuccess) {
         StokesRhsArgs a;
         a.ne = b.ne; a.Q = Q; a.ldp = b.ldp; a.k = 6; a.nnodes = b.nn;
@@ -1374,11 +1375,13 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
         e = launch_stokes_rhs<float>(a, st);
       }
       if (e != cudaSuccess) return bail(AGB_ERR_CUDA, std::string("assembly: ") + cudaGetErrorString(e));
-      asm_launches += 9 + (b.na > 0 ? 2 : 0);
+      asm_launches += 7 + (b.na > 0 ? 2 : 0);
       bodies[t].A = A;
       bodies[t].lda = b.lda;
       bodies[t].m = b.m;
       bodies[t].n = b.n;
+      bodies[t].pk_ne = b.ne;
+      bodies[t].pk_ldp = b.pldp;
       bodies[t].b = (const double*)(d + b.o_rhs);
       bodies[t].q = (const double*)(d + b.o_q);
       bodies[t].x = (double*)(d + b.o_x);
@@ -1424,7 +1427,7 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
     stats[0] = t_asm; stats[1] = t_solve; stats[2] = ms(t_start, clk::now()); stats[3] = (double)waves.size();
     stats[4] = bst.av_ms; stats[5] = bst.atu_ms; stats[6] = (double)bst.av_launches; stats[7] = (double)bst.atu_launches;
     stats[8] = bst.bytes_av; stats[9] = (double)(bst.launches + asm_launches);
-    stats[10] = tune.av_rows; stats[11] = tune.atu_rs; stats[12] = tune.atu_rows; stats[13] = (double)bst.iterations;
+    stats[10] = bst.av_rows; stats[11] = bst.atu_rs; stats[12] = bst.atu_rows; stats[13] = (double)bst.iterations;
     stats[14] = dev_ms; stats[15] = t_ft;
   }
   return AGB_OK;

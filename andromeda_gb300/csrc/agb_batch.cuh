@@ -11,9 +11,11 @@ namespace agb {
 
 // One system of the batch (device pointers, owned by the caller).
 struct BatchBody {
-  const float* A = nullptr;  // m x lda row-major, columns scaled by q (lsqr_precon)
+  const float* A = nullptr;  // m x lda row-major, columns scaled by q (lsqr_precon); or, with pk_ne > 0,
+                             // the packed symmetric 3x3 blocks (pk_idx layout), unscaled
   int64_t lda = 0;           // multiple of 32, >= n
   int m = 0, n = 0;
+  int pk_ne = 0, pk_ldp = 0;  // packed layout: m = n = 3 pk_ne, pk_ldp a multiple of 64 >= pk_ne
   const double* b = nullptr;  // [k][m] right-hand sides
   const double* q = nullptr;  // [n] column scales
   double* x = nullptr;        // [k][n] solution (zero warm start)
@@ -25,6 +27,8 @@ struct BatchTune {
   int atu_rs = 32;         // rows per A^T*U stage (32: 3 x 65 KB, 1 CTA/SM; 16: 3 x 32.5 KB, 2 CTAs/SM)
   int atu_rows = 4096;     // rows per A^T*U CTA (row groups of a system)
   int check_every = 8;     // iterations per graph replay
+  int avp_rows = 0;        // packed layout: block rows per A*V CTA (even, 20..30; 0 = fill whole waves)
+  int atup_rows = 1024;    // packed layout: block rows per A^T*U row group
 };
 
 struct BatchStats {
@@ -33,7 +37,9 @@ struct BatchStats {
   long launches = 0;                 // all kernels launched
   long iterations = 0;               // graph iterations run (max over systems)
   double bytes_av = 0.0;             // algorithmic bytes of all A*V launches: sum over systems of
-                                     // (iterations while active) x m x n x 4
+                                     // (iterations while active) x (m x n x 4, packed: 6 pk_ne^2 x 4)
+  int av_rows = 0, atu_rs = 0, atu_rows = 0;  // tile shapes used (packed: block rows per A*V CTA,
+                                              // per A^T*U stage, per A^T*U row group)
 };
 
 // Solves A_i x_i = b_i (least squares) for all systems with the reference's
@@ -54,6 +60,16 @@ bool batch_autotune(const std::vector<BatchBody>& bodies, cudaStream_t s, BatchT
 // matrix, partial sums of `groups` row groups in P (groups x lda doubles).
 cudaError_t dense_colscale_f32(float* A, int64_t lda, int m, int n, double* q, double* P, int groups,
                                cudaStream_t s);
+
+// lsqr_precon column norms of a packed FP32 matrix (pk_idx layout, ne block
+// rows): q_j = 1/||A(:,j)|| for the 3 ne columns (q_j = 0 for ne..lda-1); the
+// matrix is not scaled -- the packed sweeps apply q on the fly.
+cudaError_t packed_colnorms(const float* Ap, int ne, int ldp, int64_t lda, double* q, double* P, int groups,
+                            cudaStream_t s);
+
+// 3-D tensor map of the packed layout: dims {64 columns, 6 x ldp/64 (plane,
+// column block), ne rows}, box {64, box_y, box_z}.
+bool make_packed_map(CUtensorMap* tm, const void* Ap, int ldp, int ne, int box_y, int box_z, std::string& err);
 
 // 2-D tensor map of a row-major FP32 matrix (dims {lda, m}, box box_cols x box_rows).
 bool make_tensor_map_2d(CUtensorMap* tm, const void* A, int64_t lda, int m, int box_cols, int box_rows,

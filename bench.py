@@ -327,11 +327,11 @@ def run_batch(args, rank, world, local):
                         "h2d_bytes_per_step": int(sum(m["xyz"].nbytes + m["etype"].nbytes + m["con"].nbytes +
                                                       m["bcid"].nbytes for m in meshes)),
                         "d2h_bytes_per_step": int(args.bodies * (36 * 8 + 12 * 4))},
-                "roofline": {"bound": "hbm", "kernel": "g_av (batched LSQR A*V sweep, FP32 A by TMA, all bodies "
-                                                       "in one launch)",
+                "roofline": {"bound": "hbm", "kernel": "g_avp (batched LSQR A*V sweep over the packed symmetric "
+                                                       "3x3 blocks, FP32 by TMA, all bodies in one launch)",
                              "achieved": av_gbs, "peak": peak, "unit": "GB/s",
                              "frac": av_gbs / peak if av_gbs else None, "traffic": None, "peak_source": peak_kind,
-                             "other_sweep": {"kernel": "g_atu (batched A^T*U)", "achieved": atu_gbs,
+                             "other_sweep": {"kernel": "g_atup (batched A^T*U, packed)", "achieved": atu_gbs,
                                              "frac": atu_gbs / peak if atu_gbs else None}},
                 "batch": {k: st[k] for k in ("assemble_ms", "solve_ms", "total_ms", "waves", "av_rows", "atu_rs",
                                               "atu_rows", "iterations", "device_ms", "ft_ms")},

@@ -235,15 +235,16 @@ int agb_lsqr_precon_dense_noalloc(int m, int n, int64_t lda, double* A, double* 
  * lib_particle.f90:341,176; CoR_Integrals_Stokes lib_Stokes.f90:2664;
  * lsqr_solve lib_lsqr.f:33) is run in mixed precision: R[36*i + 6*r + j] is
  * component j (Fx,Fy,Fz,Tx,Ty,Tz) on the particle for rigid motion r of the
- * container; nit/istop: 6 per body.  Bodies are assembled per body and solved
- * together in waves that fit mem_gb of device memory (0: 70 % of the free
- * memory): every LSQR sweep of a wave is one launch over the tiles of all of its
- * bodies, replayed from a CUDA graph; autotune != 0 times the candidate tile
- * shapes on the first wave.  stats (16 doubles, may be NULL): host ms of
- * assembly+rhs, solve, total; waves; device ms and launches of the A*V and
- * A^T*U sweeps; algorithmic bytes of all A*V launches; kernel launches; chosen
- * A*V rows, A^T*U stage rows, A^T*U rows per CTA; graph iterations; device ms
- * of the whole call; host ms of the force/torque step.  ctx only carries the
+ * container; nit/istop: 6 per body.  Bodies are assembled per body (the
+ * single layer as packed symmetric 3x3 blocks, FP32) and solved together in
+ * waves that fit mem_gb of device memory (0: 80 % of the free memory): every
+ * LSQR sweep of a wave is one launch over the tiles of all of its bodies,
+ * replayed from a CUDA graph; autotune != 0 times the candidate tile shapes on
+ * the first wave.  stats (16 doubles, may be NULL): host ms of assembly+rhs,
+ * solve, total; waves; device ms and launches of the A*V and A^T*U sweeps;
+ * algorithmic bytes of all A*V launches; kernel launches; chosen block rows
+ * per A*V CTA, per A^T*U stage and per A^T*U row group; graph iterations;
+ * device ms of the whole call; host ms of the force/torque step.  ctx only carries the
  * device and the error text (its own mesh/problem are untouched). */
 int agb_batch_resistance(agb_context* ctx, int nbodies, const int* node_off, const double* xyz, const int* elem_off,
                          const int* etype, const int* con, const int* bcid, int particle_wall, int outer_wall,

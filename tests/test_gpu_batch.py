@@ -48,7 +48,7 @@ def test_batch_matches_single_body(agb):
     # bodies do too
     assert np.all(np.isin(istop, (1, 2, 4)))
     assert st["waves"] == 1 and st["av_launches"] > 0 and st["launches"] > 0
-    assert st["av_rows"] in (32, 64) and st["atu_rs"] in (16, 32)
+    assert 20 <= st["av_rows"] <= 30 and st["av_rows"] % 2 == 0 and st["atu_rs"] == 8
     for i, m in enumerate(meshes):
         Rm, nm = _single(agb, m, agb.MIXED, 1e-9)
         R64, _ = _single(agb, m, agb.FP64, 1e-11)
