@@ -1,6 +1,7 @@
-// Batched block LSQR over many dense FP32 systems of uneven size (the many-body
-// resistance workflow: one particle-in-container system per body, 6 rigid-body
-// right-hand sides each).
+// Batched block LSQR over many Stokes single-layer systems of uneven size (the
+// many-body resistance workflow: one particle-in-container system per body, 6
+// rigid-body right-hand sides each), every matrix in the packed symmetric-block
+// FP32 layout (pk_idx).
 //
 // The recurrence per system and right-hand side is the reference's LSQR
 // (lsqr_solve / lsqr_LSQR, src/lib_lsqr.f:33-127,470-1231) exactly as the
@@ -14,12 +15,10 @@
 //     `check_every` iterations and replayed until no system is active;
 //   * tile shapes (rows per A*V CTA, rows per A^T*U stage and per CTA) are
 //     picked by batch_autotune from timed candidates.
-// The sweep tiles are the TMA-fed bodies of agb_sweeps.cuh (tensor maps of
-// every system kept in a device table, 64-byte aligned).  A system is either
-// a row-major matrix with its columns scaled by q (av3_tile / atu3_tile) or
-// the packed symmetric 3x3 blocks of a Stokes single layer (avp_tile /
-// atup_tile: 2/3 of the bytes; q applied on the fly, W = q.V written by
-// g_update into Vp, the A^T U partials scaled by q in g_reduce).
+// The sweep tiles are the TMA-fed bodies avp_tile / atup_tile of
+// agb_sweeps.cuh (tensor maps of every system kept in a device table, 64-byte
+// aligned); the lsqr_precon column scaling q is applied on the fly: W = q.V is
+// written by g_update into Vp, the A^T U partials are scaled by q in g_reduce.
 #include "agb_batch.cuh"
 #include "agb_sweeps.cuh"
 
@@ -44,15 +43,15 @@ constexpr int BT = 256;  // threads of the element-wise kernels
 
 // Device descriptor of one system.
 struct GDesc {  // CUtensorMap members keep the 64-byte alignment TMA needs
-  CUtensorMap tm_av;   // box 256 x av_rows; packed: box {64, 6, avp_rows}
-  CUtensorMap tm_atu;  // box 256 x atu_rs; packed: box {64, 24, ATUP_RS}
-  CUtensorMap tm_vp;   // packed: W = q.V as [3 x 8 rows][pk_ldp], box {64, 24}
+  CUtensorMap tm_av;   // packed matrix, box {64, 6, avp_rows}
+  CUtensorMap tm_atu;  // packed matrix, box {64, 24, ATUP_RS}
+  CUtensorMap tm_vp;   // W = q.V as [3 x 8 rows][pk_ldp], box {64, 24}
   const double* b;
   const double* q;
   double* x;
   double *Y, *V, *W, *X, *Zp, *part;
-  float *Ys, *Vs, *Vp;
-  int pk_ne, pk_ldp;  // packed layout (pk_ne = 0: row-major)
+  float *Ys, *Vp;
+  int pk_ne, pk_ldp;  // block rows/columns, columns per plane of the packed store
   LsqrScalars* sc;
   int64_t lda, mpad;
   int m, n, k, itnlim;
@@ -62,7 +61,7 @@ struct GDesc {  // CUtensorMap members keep the 64-byte alignment TMA needs
 
 struct GOffsets {
   const int* b;    // init tiles (mpad * 8 / 256 per system)
-  const int* av;   // A*V tiles (m / av_rows)
+  const int* av;   // A*V tiles (pk_ne / avp_rows)
   const int* atu;  // A^T*U tiles (cblocks * zgroups)
   const int* red;  // reduce tiles (n * 8 / 256)
   const int* upd;  // update tiles (lda * 8 / 256)
@@ -161,25 +160,6 @@ __global__ void __launch_bounds__(256) g_scalars(const GDesc* __restrict__ D, in
   }
 }
 
-template <int ROWS, int ST>
-__global__ void __launch_bounds__(ROWS / 4 * 32, 1) g_av(const GDesc* __restrict__ D, const int* __restrict__ off,
-                                                         int nb, const int* __restrict__ bact, int* errflag) {
-  const int bi = find_body(off, nb, blockIdx.x);
-  if (!bact[bi]) return;
-  const GDesc& d = D[bi];
-  av3_tile<ROWS, ST>(&d.tm_av, d.lda, d.m, d.Vs, d.sc, d.Y, d.Ys, d.part, errflag, (int)(blockIdx.x - off[bi]));
-}
-
-template <int RS, int ST>
-__global__ void __launch_bounds__(ATU3_THREADS, 1) g_atu(const GDesc* __restrict__ D, const int* __restrict__ off,
-                                                         int nb, const int* __restrict__ bact, int* errflag) {
-  const int bi = find_body(off, nb, blockIdx.x);
-  if (!bact[bi]) return;
-  const GDesc& d = D[bi];
-  const int local = blockIdx.x - off[bi];
-  atu3_tile<RS, ST>(&d.tm_atu, d.lda, d.m, d.Ys, d.rpg, d.Zp, errflag, local % d.cblocks, local / d.cblocks);
-}
-
 __global__ void __launch_bounds__(AVP_WARPS * 32, 1) g_avp(const GDesc* __restrict__ D, const int* __restrict__ off,
                                                           int nb, const int* __restrict__ bact, int rows,
                                                           int* errflag) {
@@ -199,8 +179,7 @@ __global__ void __launch_bounds__(ATUP_C, 2) g_atup(const GDesc* __restrict__ D,
   atup_tile(&d.tm_atu, d.pk_ne, d.lda, d.Ys, d.rpg, d.Zp, errflag, local % d.cblocks, local / d.cblocks);
 }
 
-// V <- Z/beta - beta V over the row-group partials (in order, scaled by q for
-// a packed system); partial ||V||^2
+// V <- q.(Z/beta) - beta V over the row-group partials (in order); partial ||V||^2
 __global__ void __launch_bounds__(BT) g_reduce(const GDesc* __restrict__ D, const int* __restrict__ off, int nb,
                                                const int* __restrict__ bact, int init) {
   const int bi = find_body(off, nb, blockIdx.x);
@@ -214,7 +193,7 @@ __global__ void __launch_bounds__(BT) g_reduce(const GDesc* __restrict__ D, cons
   if (j < d.n) {
     double z = 0.0;
     for (int g = 0; g < d.zgroups; ++g) z += d.Zp[((int64_t)g * d.lda + j) * K8 + c];
-    if (d.pk_ne) z *= d.q[j];
+    z *= d.q[j];
     const double beta = d.sc[c].beta;
     if (d.sc[c].active && beta > 0.0) {
       vn = z / beta - (init ? 0.0 : beta * d.V[j * K8 + c]);
@@ -227,8 +206,8 @@ __global__ void __launch_bounds__(BT) g_reduce(const GDesc* __restrict__ D, cons
   block_sumsq8(vn, d.part + (int64_t)blk * K8);
 }
 
-// V <- V/alpha; X += t1 W; W <- t2 W + V; partial (t3 W_old)^2; Vs (RHS-major) = V,
-// or for a packed system Vp[b][k][jj] = q.V of column b pk_ne + jj
+// V <- V/alpha; X += t1 W; W <- t2 W + V; partial (t3 W_old)^2;
+// Vp[b][k][jj] = q.V of column b pk_ne + jj
 __global__ void __launch_bounds__(BT) g_update(const GDesc* __restrict__ D, const int* __restrict__ off, int nb,
                                                const int* __restrict__ bact, int init) {
   const int bi = find_body(off, nb, blockIdx.x);
@@ -243,7 +222,6 @@ __global__ void __launch_bounds__(BT) g_update(const GDesc* __restrict__ D, cons
     const int64_t id = j * K8 + c;
     if (j >= d.n) {
       d.V[id] = 0.0; d.W[id] = 0.0; d.X[id] = 0.0;
-      if (!d.pk_ne) d.Vs[(int64_t)c * d.lda + j] = 0.f;
     } else {
       const LsqrScalars& s = d.sc[c];
       if (s.active) {
@@ -263,13 +241,9 @@ __global__ void __launch_bounds__(BT) g_update(const GDesc* __restrict__ D, cons
       } else if (init) {
         d.W[id] = 0.0; d.X[id] = 0.0;
       }
-      if (d.pk_ne) {
-        const int b = (int)(j / d.pk_ne);
-        const int64_t jj = j - (int64_t)b * d.pk_ne;
-        d.Vp[((int64_t)b * K8 + c) * d.pk_ldp + jj] = (float)(d.q[j] * d.V[id]);
-      } else {
-        d.Vs[(int64_t)c * d.lda + j] = (float)d.V[id];
-      }
+      const int b = (int)(j / d.pk_ne);
+      const int64_t jj = j - (int64_t)b * d.pk_ne;
+      d.Vp[((int64_t)b * K8 + c) * d.pk_ldp + jj] = (float)(d.q[j] * d.V[id]);
     }
   }
   block_sumsq8(dk, d.part + (int64_t)blk * K8);
@@ -299,41 +273,9 @@ static cudaError_t set_smem(K kernel, size_t bytes) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-// Kernel table of the tunable tile shapes.
-struct AvVariant {
-  int rows;
-  void (*fn)(const GDesc*, const int*, int, const int*, int*);
-  size_t smem;
-  int threads;
-};
-struct AtuVariant {
-  int rs;
-  void (*fn)(const GDesc*, const int*, int, const int*, int*);
-  size_t smem;
-};
-static const AvVariant kAv[] = {
-    {64, g_av<64, 3>, SweepAV<64, 3>::SMEM, 64 / 4 * 32},
-    {32, g_av<32, 2>, SweepAV<32, 2>::SMEM, 32 / 4 * 32},
-};
-static const AtuVariant kAtu[] = {
-    {32, g_atu<32, 3>, SweepATU<32, 3>::SMEM},
-    {16, g_atu<16, 3>, SweepATU<16, 3>::SMEM},
-};
-static const AvVariant* av_variant(int rows) {
-  for (const auto& v : kAv)
-    if (v.rows == rows) return &v;
-  return nullptr;
-}
-static const AtuVariant* atu_variant(int rs) {
-  for (const auto& v : kAtu)
-    if (v.rs == rs) return &v;
-  return nullptr;
-}
-
 struct BatchSolver {
   int nb = 0, k = 0;
-  bool packed = false;  // every system in the packed layout (else every one row-major)
-  int avp_rows = 0;
+  int avp_rows = 0;  // block rows per A*V CTA
   BatchTune tune;
   cudaStream_t s = 0;
   std::vector<GDesc> hd;
@@ -365,68 +307,50 @@ struct BatchSolver {
     s = st;
     if (nb == 0) { err = "empty batch"; return false; }
     if (k < 1 || k > K8) { err = "number of right-hand sides must be 1..8"; return false; }
-    packed = bodies[0].pk_ne > 0;
-    for (const auto& B : bodies)
-      if ((B.pk_ne > 0) != packed) { err = "a batch mixes packed and row-major systems"; return false; }
-    if (packed) {
-      BCK(set_smem(g_avp, AVP_SMEM));
-      BCK(set_smem(g_atup, ATUP_SMEM));
-      avp_rows = tune.avp_rows;
-      if (avp_rows == 0) {  // the even count in 20..30 whose row blocks fill whole waves best
-        int dev = 0, nsm = 152;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        double best_eff = -1.0;
-        for (int R = AVP_R - 2; R >= 20; R -= 2) {
-          int64_t nrb = 0;
-          for (const auto& B : bodies) nrb += cdivu(B.pk_ne, R);
-          const double eff = (double)nrb / (double)(cdivu(nrb, nsm) * (int64_t)nsm);
-          if (eff > best_eff + 1e-9) { best_eff = eff; avp_rows = R; }
-        }
+    BCK(set_smem(g_avp, AVP_SMEM));
+    BCK(set_smem(g_atup, ATUP_SMEM));
+    avp_rows = tune.avp_rows;
+    if (avp_rows == 0) {  // the even count in 20..30 whose row blocks fill whole waves best
+      int dev = 0, nsm = 152;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      double best_eff = -1.0;
+      for (int R = AVP_R - 2; R >= 20; R -= 2) {
+        int64_t nrb = 0;
+        for (const auto& B : bodies) nrb += cdivu(B.pk_ne, R);
+        const double eff = (double)nrb / (double)(cdivu(nrb, nsm) * (int64_t)nsm);
+        if (eff > best_eff + 1e-9) { best_eff = eff; avp_rows = R; }
       }
-      if (avp_rows < 2 || avp_rows > AVP_R - 2 || avp_rows % 2) { err = "bad packed A*V rows"; return false; }
-    } else {
-      const AvVariant* av = av_variant(tune.av_rows);
-      const AtuVariant* at = atu_variant(tune.atu_rs);
-      if (!av || !at) { err = "unknown tile shape"; return false; }
-      BCK(set_smem(av->fn, av->smem));
-      BCK(set_smem(at->fn, at->smem));
     }
+    if (avp_rows < 2 || avp_rows > AVP_R - 2 || avp_rows % 2) { err = "bad A*V rows per CTA"; return false; }
     hd.assign(nb, GDesc{});
     hoff_b.assign(nb + 1, 0); hoff_av.assign(nb + 1, 0); hoff_atu.assign(nb + 1, 0);
     hoff_red.assign(nb + 1, 0); hoff_upd.assign(nb + 1, 0);
     // pool layout (bytes), every piece 256-byte aligned
     size_t bytes = 0;
     auto take = [&](size_t n) { const size_t o = bytes; bytes += (n + 255) / 256 * 256; return o; };
-    struct Offs { size_t Y, Ys, V, W, X, Vs, Zp, part, sc; };  // Vs: the packed systems' Vp
+    struct Offs { size_t Y, Ys, V, W, X, Vp, Zp, part, sc; };
     std::vector<Offs> po(nb);
     bytes_A = 0.0;
     for (int i = 0; i < nb; ++i) {
       const BatchBody& B = bodies[i];
-      if (B.lda % 32 != 0 || B.lda < B.n || B.m < 1 || B.n < 1 || !B.A || !B.b || !B.q || !B.x ||
-          (packed && (B.m != 3 * B.pk_ne || B.n != B.m || B.pk_ldp % 64 != 0 || B.pk_ldp < B.pk_ne))) {
+      if (B.lda % 32 != 0 || B.lda < B.n || B.pk_ne < 1 || B.m != 3 * B.pk_ne || B.n != B.m ||
+          B.pk_ldp % 64 != 0 || B.pk_ldp < B.pk_ne || !B.A || !B.b || !B.q || !B.x) {
         err = "bad system " + std::to_string(i);
         return false;
       }
       GDesc& d = hd[i];
       d.lda = B.lda; d.m = B.m; d.n = B.n; d.k = k;
-      d.pk_ne = packed ? B.pk_ne : 0;
-      d.pk_ldp = packed ? B.pk_ldp : 0;
+      d.pk_ne = B.pk_ne;
+      d.pk_ldp = B.pk_ldp;
       d.mpad = ((int64_t)B.m + 255) / 256 * 256;
       d.itnlim = maxit > 0 ? maxit : 10 * (B.m + B.n + 50);
-      if (packed) {  // A^T U tiles: 256 element columns x a group of block rows
-        d.cblocks = (int)cdivu(B.pk_ldp, ATUP_C);
-        d.zgroups = std::max(1, (int)cdivu(B.pk_ne, std::max(tune.atup_rows, ATUP_RS)));
-        d.rpg = (int)((cdivu(B.pk_ne, d.zgroups) + ATUP_RS - 1) / ATUP_RS * ATUP_RS);
-        d.zgroups = (int)cdivu(B.pk_ne, d.rpg);
-        d.nb_av = (int)cdivu(B.pk_ne, avp_rows);
-      } else {
-        d.cblocks = (int)cdivu(B.lda, ATU3_COLS);
-        d.zgroups = std::max(1, (int)cdivu(B.m, std::max(tune.atu_rows, tune.atu_rs)));
-        d.rpg = (int)((cdivu(B.m, d.zgroups) + tune.atu_rs - 1) / tune.atu_rs * tune.atu_rs);
-        d.zgroups = (int)cdivu(B.m, d.rpg);
-        d.nb_av = (int)cdivu(B.m, tune.av_rows);
-      }
+      // A^T U tiles: 256 element columns x a group of block rows
+      d.cblocks = (int)cdivu(B.pk_ldp, ATUP_C);
+      d.zgroups = std::max(1, (int)cdivu(B.pk_ne, std::max(tune.atup_rows, ATUP_RS)));
+      d.rpg = (int)((cdivu(B.pk_ne, d.zgroups) + ATUP_RS - 1) / ATUP_RS * ATUP_RS);
+      d.zgroups = (int)cdivu(B.pk_ne, d.rpg);
+      d.nb_av = (int)cdivu(B.pk_ne, avp_rows);
       d.nb_b = (int)cdivu(d.mpad * K8, BT);
       d.nb_red = (int)cdivu((int64_t)B.n * K8, BT);
       d.nb_upd = (int)cdivu(B.lda * K8, BT);
@@ -436,7 +360,7 @@ struct BatchSolver {
       po[i].V = take(B.lda * K8 * sizeof(double));
       po[i].W = take(B.lda * K8 * sizeof(double));
       po[i].X = take(B.lda * K8 * sizeof(double));
-      po[i].Vs = take(packed ? (size_t)3 * K8 * B.pk_ldp * sizeof(float) : B.lda * K8 * sizeof(float));
+      po[i].Vp = take((size_t)3 * K8 * B.pk_ldp * sizeof(float));
       po[i].Zp = take((size_t)d.zgroups * B.lda * K8 * sizeof(double));
       po[i].part = take((size_t)nbmax * K8 * sizeof(double));
       po[i].sc = take(K8 * sizeof(LsqrScalars));
@@ -445,14 +369,9 @@ struct BatchSolver {
       hoff_atu[i + 1] = hoff_atu[i] + d.cblocks * d.zgroups;
       hoff_red[i + 1] = hoff_red[i] + d.nb_red;
       hoff_upd[i + 1] = hoff_upd[i] + d.nb_upd;
-      bytes_A += packed ? 24.0 * (double)B.pk_ne * (double)B.pk_ne : (double)B.m * (double)B.n * 4.0;
-      if (packed) {
-        if (!make_packed_map(&d.tm_av, B.A, B.pk_ldp, B.pk_ne, 6, avp_rows, err)) return false;
-        if (!make_packed_map(&d.tm_atu, B.A, B.pk_ldp, B.pk_ne, 6 * (ATUP_C / 64), ATUP_RS, err)) return false;
-      } else {
-        if (!make_tensor_map_2d(&d.tm_av, B.A, B.lda, B.m, SWEEP_BC, tune.av_rows, err)) return false;
-        if (!make_tensor_map_2d(&d.tm_atu, B.A, B.lda, B.m, SWEEP_BC, tune.atu_rs, err)) return false;
-      }
+      bytes_A += 24.0 * (double)B.pk_ne * (double)B.pk_ne;
+      if (!make_packed_map(&d.tm_av, B.A, B.pk_ldp, B.pk_ne, 6, avp_rows, err)) return false;
+      if (!make_packed_map(&d.tm_atu, B.A, B.pk_ldp, B.pk_ne, 6 * (ATUP_C / 64), ATUP_RS, err)) return false;
       d.b = B.b; d.q = B.q; d.x = B.x;
     }
     BCK(cudaMalloc(&pool, bytes));
@@ -462,14 +381,10 @@ struct BatchSolver {
       GDesc& d = hd[i];
       d.Y = (double*)(p + po[i].Y); d.Ys = (float*)(p + po[i].Ys);
       d.V = (double*)(p + po[i].V); d.W = (double*)(p + po[i].W); d.X = (double*)(p + po[i].X);
-      d.Vs = (float*)(p + po[i].Vs); d.Zp = (double*)(p + po[i].Zp); d.part = (double*)(p + po[i].part);
+      d.Vp = (float*)(p + po[i].Vp); d.Zp = (double*)(p + po[i].Zp); d.part = (double*)(p + po[i].part);
       d.sc = (LsqrScalars*)(p + po[i].sc);
-      d.Vp = nullptr;
-      if (packed) {  // the pool is zeroed: the pad columns pk_ne..pk_ldp-1 of Vp stay zero
-        d.Vp = d.Vs;
-        d.Vs = nullptr;
-        if (!make_tensor_map_2d(&d.tm_vp, d.Vp, d.pk_ldp, 3 * K8, AVP_BC, 3 * K8, err)) return false;
-      }
+      // the pool is zeroed: the pad columns pk_ne..pk_ldp-1 of Vp stay zero
+      if (!make_tensor_map_2d(&d.tm_vp, d.Vp, d.pk_ldp, 3 * K8, AVP_BC, 3 * K8, err)) return false;
     }
     BCK(cudaMalloc(&d_desc, nb * sizeof(GDesc)));
     BCK(cudaMemcpyAsync(d_desc, hd.data(), nb * sizeof(GDesc), cudaMemcpyHostToDevice, s));
@@ -490,21 +405,9 @@ struct BatchSolver {
   }
 
   void launch_av() {
-    if (packed) {
-      g_avp<<<hoff_av[nb], (avp_rows / 2 + 1) * 32, AVP_SMEM, s>>>(d_desc, off.av, nb, bact, avp_rows, errflag);
-      return;
-    }
-    const AvVariant* av = av_variant(tune.av_rows);
-    av->fn<<<hoff_av[nb], av->threads, av->smem, s>>>(d_desc, off.av, nb, bact, errflag);
+    g_avp<<<hoff_av[nb], (avp_rows / 2 + 1) * 32, AVP_SMEM, s>>>(d_desc, off.av, nb, bact, avp_rows, errflag);
   }
-  void launch_atu() {
-    if (packed) {
-      g_atup<<<hoff_atu[nb], ATUP_C, ATUP_SMEM, s>>>(d_desc, off.atu, nb, bact, errflag);
-      return;
-    }
-    const AtuVariant* at = atu_variant(tune.atu_rs);
-    at->fn<<<hoff_atu[nb], ATU3_THREADS, at->smem, s>>>(d_desc, off.atu, nb, bact, errflag);
-  }
+  void launch_atu() { g_atup<<<hoff_atu[nb], ATUP_C, ATUP_SMEM, s>>>(d_desc, off.atu, nb, bact, errflag); }
 };
 
 bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, int maxit, const BatchTune& tune,
@@ -618,14 +521,13 @@ bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, i
     st->av_launches += nav; st->atu_launches += natu;
     st->launches += launches;
     st->iterations = std::max(st->iterations, iters);
-    st->av_rows = S.packed ? S.avp_rows : tune.av_rows;
-    st->atu_rs = S.packed ? ATUP_RS : tune.atu_rs;
-    st->atu_rows = S.packed ? tune.atup_rows : tune.atu_rows;
+    st->av_rows = S.avp_rows;
+    st->atu_rs = ATUP_RS;
+    st->atu_rows = tune.atup_rows;
     for (int i = 0; i < nb; ++i) {
       int mx = 0;
       for (int c = 0; c < k; ++c) mx = std::max(mx, nit[(size_t)i * k + c]);
-      const GDesc& d = S.hd[i];
-      st->bytes_av += (double)mx * (d.pk_ne ? 24.0 * (double)d.pk_ne * (double)d.pk_ne : (double)d.m * (double)d.n * 4.0);
+      st->bytes_av += (double)mx * 24.0 * (double)S.hd[i].pk_ne * (double)S.hd[i].pk_ne;
     }
   }
   return true;
@@ -643,13 +545,12 @@ static std::map<std::string, BatchTune> g_tune_cache;
 bool batch_autotune(const std::vector<BatchBody>& bodies, cudaStream_t s, BatchTune& best, std::string& report,
                     std::string& err) {
   double tot = 0.0;
-  for (const auto& b : bodies) tot += b.pk_ne ? 24.0 * (double)b.pk_ne * (double)b.pk_ldp : (double)b.m * (double)b.lda * 4.0;
+  for (const auto& b : bodies) tot += 24.0 * (double)b.pk_ne * (double)b.pk_ldp;
   int nbk = 0;
   for (size_t v = bodies.size(); v > 1; v >>= 1) ++nbk;
   int tbk = 0;
   for (double v = tot / 1e6; v > 1.0; v /= 2.0) ++tbk;
-  const bool pk = !bodies.empty() && bodies[0].pk_ne > 0;
-  const std::string key = std::string(pk ? "p" : "r") + std::to_string(nbk) + "/" + std::to_string(tbk);
+  const std::string key = std::to_string(nbk) + "/" + std::to_string(tbk);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cache.find(key);
@@ -676,53 +577,28 @@ bool batch_autotune(const std::vector<BatchBody>& bodies, cudaStream_t s, BatchT
   report.clear();
   BatchTune t0 = best;
   double best_av = 1e300, best_atu = 1e300;
-  if (!bodies.empty() && bodies[0].pk_ne > 0) {  // packed systems: rows per A*V CTA, block rows per A^T*U group
-    const int av_rows[] = {0, 30, 24};
-    for (int r : av_rows) {
-      BatchTune t = t0;
-      t.avp_rows = r;
-      BatchSolver S;
-      if (!S.setup(bodies, 1, 1, t, s)) { err = S.err; cudaEventDestroy(e0); cudaEventDestroy(e1); return false; }
-      const double ms = time_it(S, true);
-      snprintf(line, sizeof line, "avp rows=%d: %.3f ms; ", S.avp_rows, ms);
-      report += line;
-      if (ms < best_av) { best_av = ms; best.avp_rows = S.avp_rows; }
-    }
-    const int grp_rows[] = {512, 1024, 4096};
-    for (int g : grp_rows) {
-      BatchTune t = t0;
-      t.atup_rows = g;
-      BatchSolver S;
-      if (!S.setup(bodies, 1, 1, t, s)) { err = S.err; cudaEventDestroy(e0); cudaEventDestroy(e1); return false; }
-      const double ms = time_it(S, false);
-      snprintf(line, sizeof line, "atup rows=%d: %.3f ms; ", g, ms);
-      report += line;
-      if (ms < best_atu) { best_atu = ms; best.atup_rows = g; }
-    }
-  } else {
-  for (const auto& av : kAv) {
+  // rows per A*V CTA, block rows per A^T*U row group
+  const int av_rows[] = {0, 30, 24};
+  for (int r : av_rows) {
     BatchTune t = t0;
-    t.av_rows = av.rows;
+    t.avp_rows = r;
     BatchSolver S;
     if (!S.setup(bodies, 1, 1, t, s)) { err = S.err; cudaEventDestroy(e0); cudaEventDestroy(e1); return false; }
     const double ms = time_it(S, true);
-    snprintf(line, sizeof line, "av rows=%d: %.3f ms; ", av.rows, ms);
+    snprintf(line, sizeof line, "avp rows=%d: %.3f ms; ", S.avp_rows, ms);
     report += line;
-    if (ms < best_av) { best_av = ms; best.av_rows = av.rows; }
+    if (ms < best_av) { best_av = ms; best.avp_rows = S.avp_rows; }
   }
-  const int row_targets[] = {2048, 8192};
-  for (const auto& at : kAtu)
-    for (int rt : row_targets) {
-      BatchTune t = t0;
-      t.atu_rs = at.rs;
-      t.atu_rows = rt;
-      BatchSolver S;
-      if (!S.setup(bodies, 1, 1, t, s)) { err = S.err; cudaEventDestroy(e0); cudaEventDestroy(e1); return false; }
-      const double ms = time_it(S, false);
-      snprintf(line, sizeof line, "atu rs=%d rows=%d: %.3f ms; ", at.rs, rt, ms);
-      report += line;
-      if (ms < best_atu) { best_atu = ms; best.atu_rs = at.rs; best.atu_rows = rt; }
-    }
+  const int grp_rows[] = {512, 1024, 4096};
+  for (int g : grp_rows) {
+    BatchTune t = t0;
+    t.atup_rows = g;
+    BatchSolver S;
+    if (!S.setup(bodies, 1, 1, t, s)) { err = S.err; cudaEventDestroy(e0); cudaEventDestroy(e1); return false; }
+    const double ms = time_it(S, false);
+    snprintf(line, sizeof line, "atup rows=%d: %.3f ms; ", g, ms);
+    report += line;
+    if (ms < best_atu) { best_atu = ms; best.atup_rows = g; }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

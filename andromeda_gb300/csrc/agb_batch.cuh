@@ -1,5 +1,5 @@
-// Batched block LSQR: many dense FP32 systems of uneven size, each with up to
-// 8 right-hand sides, solved together -- every sweep of an iteration is ONE
+// Batched block LSQR: many Stokes single-layer systems of uneven size (packed
+// symmetric-block FP32 layout), each with up to 8 right-hand sides, solved together -- every sweep of an iteration is ONE
 // launch over the tiles of all systems still iterating, and the iterations are
 // replayed from one captured CUDA graph.
 #pragma once
@@ -11,24 +11,20 @@ namespace agb {
 
 // One system of the batch (device pointers, owned by the caller).
 struct BatchBody {
-  const float* A = nullptr;  // m x lda row-major, columns scaled by q (lsqr_precon); or, with pk_ne > 0,
-                             // the packed symmetric 3x3 blocks (pk_idx layout), unscaled
-  int64_t lda = 0;           // multiple of 32, >= n
-  int m = 0, n = 0;
-  int pk_ne = 0, pk_ldp = 0;  // packed layout: m = n = 3 pk_ne, pk_ldp a multiple of 64 >= pk_ne
+  const float* A = nullptr;   // packed symmetric 3x3 blocks (pk_idx layout), unscaled
+  int pk_ne = 0, pk_ldp = 0;  // block rows = block columns; columns per plane (multiple of 64, >= pk_ne)
+  int m = 0, n = 0;           // 3 pk_ne each
+  int64_t lda = 0;            // length of the column vectors: multiple of 32, >= n
   const double* b = nullptr;  // [k][m] right-hand sides
-  const double* q = nullptr;  // [n] column scales
+  const double* q = nullptr;  // [n] lsqr_precon column scales (applied on the fly)
   double* x = nullptr;        // [k][n] solution (zero warm start)
 };
 
 // Tile shapes and schedule of the batched sweeps (picked by batch_autotune).
 struct BatchTune {
-  int av_rows = 64;        // rows per A*V CTA (64: 3 x 72 KB stages, 1 CTA/SM; 32: 2 x 40 KB, 2 CTAs/SM)
-  int atu_rs = 32;         // rows per A^T*U stage (32: 3 x 65 KB, 1 CTA/SM; 16: 3 x 32.5 KB, 2 CTAs/SM)
-  int atu_rows = 4096;     // rows per A^T*U CTA (row groups of a system)
+  int avp_rows = 0;        // block rows per A*V CTA (even, 20..30; 0 = the count that fills whole waves)
+  int atup_rows = 1024;    // block rows per A^T*U row group
   int check_every = 8;     // iterations per graph replay
-  int avp_rows = 0;        // packed layout: block rows per A*V CTA (even, 20..30; 0 = fill whole waves)
-  int atup_rows = 1024;    // packed layout: block rows per A^T*U row group
 };
 
 struct BatchStats {
@@ -37,9 +33,9 @@ struct BatchStats {
   long launches = 0;                 // all kernels launched
   long iterations = 0;               // graph iterations run (max over systems)
   double bytes_av = 0.0;             // algorithmic bytes of all A*V launches: sum over systems of
-                                     // (iterations while active) x (m x n x 4, packed: 6 pk_ne^2 x 4)
-  int av_rows = 0, atu_rs = 0, atu_rows = 0;  // tile shapes used (packed: block rows per A*V CTA,
-                                              // per A^T*U stage, per A^T*U row group)
+                                     // (iterations while active) x 6 pk_ne^2 x 4
+  int av_rows = 0, atu_rs = 0, atu_rows = 0;  // tile shapes used: block rows per A*V CTA, per A^T*U
+                                              // stage, per A^T*U row group
 };
 
 // Solves A_i x_i = b_i (least squares) for all systems with the reference's
@@ -55,11 +51,6 @@ bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, i
 // class for the process.
 bool batch_autotune(const std::vector<BatchBody>& bodies, cudaStream_t s, BatchTune& best, std::string& report,
                     std::string& err);
-
-// lsqr_precon column scaling (q_j = 1/||A(:,j)||, A <- A diag(q)) of one FP32
-// matrix, partial sums of `groups` row groups in P (groups x lda doubles).
-cudaError_t dense_colscale_f32(float* A, int64_t lda, int m, int n, double* q, double* P, int groups,
-                               cudaStream_t s);
 
 // lsqr_precon column norms of a packed FP32 matrix (pk_idx layout, ne block
 // rows): q_j = 1/||A(:,j)|| for the 3 ne columns (q_j = 0 for ne..lda-1); the

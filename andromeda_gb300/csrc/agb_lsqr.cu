@@ -1061,19 +1061,6 @@ bool DenseLsqr::setup(const void* A_dev, bool is_fp32, int m_, int n_, int64_t l
   return true;
 }
 
-// lsqr_precon column scaling of one FP32 matrix with `groups` row groups of
-// partial sums in P (groups x lda doubles); no allocation, no synchronisation.
-cudaError_t dense_colscale_f32(float* A, int64_t lda, int m, int n, double* q, double* P, int groups,
-                               cudaStream_t s) {
-  dim3 g(cdiv(lda, kThreads * 4), groups);
-  const int rpg = (int)cdiv(m, groups);
-  k_colsq<float><<<g, kThreads, 0, s>>>(A, lda, m, rpg, P);
-  k_colsq_finish<<<cdiv(lda, 256), 256, 0, s>>>(P, groups, lda, n, q);
-  const int64_t tot = (int64_t)m * lda;
-  k_scale_cols<float><<<(unsigned)std::min<int64_t>(cdiv(tot, 256), 152 * 64), 256, 0, s>>>(A, lda, m, q);
-  return cudaGetLastError();
-}
-
 cudaError_t packed_colnorms(const float* Ap, int ne, int ldp, int64_t lda, double* q, double* P, int groups,
                             cudaStream_t s) {
   const int rpg = (int)cdiv(ne, groups);

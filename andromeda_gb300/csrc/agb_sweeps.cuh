@@ -1,6 +1,8 @@
-// TMA-fed FP32 LSQR sweeps over a row-major matrix, as tile bodies shared by
-// the single-system kernels (k_av3 / k_atu3) and the batched kernels that run
-// many systems in one launch.
+// TMA-fed FP32 LSQR sweeps as tile bodies: over a row-major matrix (av3_tile /
+// atu3_tile, used by k_av3 / k_atu3) and over the packed symmetric 3x3 blocks
+// of a Stokes single layer (avp_tile / atup_tile, used by the single-system
+// kernels k_avp / k_atup and by the batched kernels g_avp / g_atup that run
+// many systems in one launch).
 //
 // Sweep 1 (av3_tile): Y = A V + gamma Y for ROWS rows of A and 8 right-hand
 // sides.  A arrives in stages of ROWS x 256 columns by 2-D tensor-map copies,

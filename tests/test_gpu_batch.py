@@ -54,7 +54,10 @@ def test_batch_matches_single_body(agb):
         R64, _ = _single(agb, m, agb.FP64, 1e-11)
         assert _rel(R[i], Rm) < 1e-6, i
         assert _rel(R[i], R64) < 5e-6, i
-        assert np.all(np.abs(nit[i] - nm) <= np.maximum(3, nm // 20)), (nit[i], nm)
+        # at eps 1e-9 the last iterations run near the FP32 rounding floor of the
+        # matrix, where the summation order of the sweeps (rows per CTA, row
+        # groups: tuned per batch) moves the stopping iteration by a few percent
+        assert np.all(np.abs(nit[i] - nm) <= np.maximum(5, nm // 10)), (nit[i], nm)
 
 
 def test_batch_waves_give_the_same_tensors(agb):
