@@ -13,8 +13,8 @@
 //     exit at once), so the wave's cost follows the systems still iterating;
 //   * the 7 launches of an iteration are captured once in a CUDA graph of
 //     `check_every` iterations and replayed until no system is active;
-//   * tile shapes (rows per A*V CTA, rows per A^T*U stage and per CTA) are
-//     picked by batch_autotune from timed candidates.
+//   * the row groups of the A^T*U tiles are picked by batch_autotune from
+//     timed candidates (the A*V tile shape is fixed).
 // The sweep tiles are the TMA-fed bodies avp_tile / atup_tile of
 // agb_sweeps.cuh (tensor maps of every system kept in a device table, 64-byte
 // aligned); the lsqr_precon column scaling q is applied on the fly: W = q.V is
@@ -43,7 +43,7 @@ constexpr int BT = 256;  // threads of the element-wise kernels
 
 // Device descriptor of one system.
 struct GDesc {  // CUtensorMap members keep the 64-byte alignment TMA needs
-  CUtensorMap tm_av;   // packed matrix, box {64, 6, avp_rows}
+  CUtensorMap tm_av;   // packed matrix, box {64, 6 x AVP_NB, AVP_R}
   CUtensorMap tm_atu;  // packed matrix, box {64, 24, ATUP_RS}
   CUtensorMap tm_vp;   // W = q.V as [3 x 8 rows][pk_ldp], box {64, 24}
   const double* b;
@@ -61,7 +61,7 @@ struct GDesc {  // CUtensorMap members keep the 64-byte alignment TMA needs
 
 struct GOffsets {
   const int* b;    // init tiles (mpad * 8 / 256 per system)
-  const int* av;   // A*V tiles (pk_ne / avp_rows)
+  const int* av;   // A*V tiles (pk_ne / AVP_R)
   const int* atu;  // A^T*U tiles (cblocks * zgroups)
   const int* red;  // reduce tiles (n * 8 / 256)
   const int* upd;  // update tiles (lda * 8 / 256)
@@ -160,14 +160,12 @@ __global__ void __launch_bounds__(256) g_scalars(const GDesc* __restrict__ D, in
   }
 }
 
-__global__ void __launch_bounds__(AVP_WARPS * 32, 1) g_avp(const GDesc* __restrict__ D, const int* __restrict__ off,
-                                                          int nb, const int* __restrict__ bact, int rows,
-                                                          int* errflag) {
+__global__ void __launch_bounds__(AVP_THREADS, 1) g_avp(const GDesc* __restrict__ D, const int* __restrict__ off,
+                                                       int nb, const int* __restrict__ bact, int* errflag) {
   const int bi = find_body(off, nb, blockIdx.x);
   if (!bact[bi]) return;
   const GDesc& d = D[bi];
-  avp_tile(&d.tm_av, &d.tm_vp, d.pk_ne, d.pk_ldp, rows, d.sc, d.Y, d.Ys, d.part, errflag,
-           (int)(blockIdx.x - off[bi]));
+  avp_tile(&d.tm_av, &d.tm_vp, d.pk_ne, d.pk_ldp, d.sc, d.Y, d.Ys, d.part, errflag, (int)(blockIdx.x - off[bi]));
 }
 
 __global__ void __launch_bounds__(ATUP_C, 2) g_atup(const GDesc* __restrict__ D, const int* __restrict__ off, int nb,
@@ -275,7 +273,6 @@ static cudaError_t set_smem(K kernel, size_t bytes) {
 
 struct BatchSolver {
   int nb = 0, k = 0;
-  int avp_rows = 0;  // block rows per A*V CTA
   BatchTune tune;
   cudaStream_t s = 0;
   std::vector<GDesc> hd;
@@ -309,20 +306,6 @@ struct BatchSolver {
     if (k < 1 || k > K8) { err = "number of right-hand sides must be 1..8"; return false; }
     BCK(set_smem(g_avp, AVP_SMEM));
     BCK(set_smem(g_atup, ATUP_SMEM));
-    avp_rows = tune.avp_rows;
-    if (avp_rows == 0) {  // the even count in 20..30 whose row blocks fill whole waves best
-      int dev = 0, nsm = 152;
-      cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-      double best_eff = -1.0;
-      for (int R = AVP_R - 2; R >= 20; R -= 2) {
-        int64_t nrb = 0;
-        for (const auto& B : bodies) nrb += cdivu(B.pk_ne, R);
-        const double eff = (double)nrb / (double)(cdivu(nrb, nsm) * (int64_t)nsm);
-        if (eff > best_eff + 1e-9) { best_eff = eff; avp_rows = R; }
-      }
-    }
-    if (avp_rows < 2 || avp_rows > AVP_R - 2 || avp_rows % 2) { err = "bad A*V rows per CTA"; return false; }
     hd.assign(nb, GDesc{});
     hoff_b.assign(nb + 1, 0); hoff_av.assign(nb + 1, 0); hoff_atu.assign(nb + 1, 0);
     hoff_red.assign(nb + 1, 0); hoff_upd.assign(nb + 1, 0);
@@ -350,7 +333,7 @@ struct BatchSolver {
       d.zgroups = std::max(1, (int)cdivu(B.pk_ne, std::max(tune.atup_rows, ATUP_RS)));
       d.rpg = (int)((cdivu(B.pk_ne, d.zgroups) + ATUP_RS - 1) / ATUP_RS * ATUP_RS);
       d.zgroups = (int)cdivu(B.pk_ne, d.rpg);
-      d.nb_av = (int)cdivu(B.pk_ne, avp_rows);
+      d.nb_av = (int)cdivu(B.pk_ne, AVP_R);
       d.nb_b = (int)cdivu(d.mpad * K8, BT);
       d.nb_red = (int)cdivu((int64_t)B.n * K8, BT);
       d.nb_upd = (int)cdivu(B.lda * K8, BT);
@@ -370,7 +353,7 @@ struct BatchSolver {
       hoff_red[i + 1] = hoff_red[i] + d.nb_red;
       hoff_upd[i + 1] = hoff_upd[i] + d.nb_upd;
       bytes_A += 24.0 * (double)B.pk_ne * (double)B.pk_ne;
-      if (!make_packed_map(&d.tm_av, B.A, B.pk_ldp, B.pk_ne, 6, avp_rows, err)) return false;
+      if (!make_packed_map(&d.tm_av, B.A, B.pk_ldp, B.pk_ne, 6 * AVP_NB, AVP_R, err)) return false;
       if (!make_packed_map(&d.tm_atu, B.A, B.pk_ldp, B.pk_ne, 6 * (ATUP_C / 64), ATUP_RS, err)) return false;
       d.b = B.b; d.q = B.q; d.x = B.x;
     }
@@ -405,7 +388,7 @@ struct BatchSolver {
   }
 
   void launch_av() {
-    g_avp<<<hoff_av[nb], (avp_rows / 2 + 1) * 32, AVP_SMEM, s>>>(d_desc, off.av, nb, bact, avp_rows, errflag);
+    g_avp<<<hoff_av[nb], AVP_THREADS, AVP_SMEM, s>>>(d_desc, off.av, nb, bact, errflag);
   }
   void launch_atu() { g_atup<<<hoff_atu[nb], ATUP_C, ATUP_SMEM, s>>>(d_desc, off.atu, nb, bact, errflag); }
 };
@@ -521,7 +504,7 @@ bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, i
     st->av_launches += nav; st->atu_launches += natu;
     st->launches += launches;
     st->iterations = std::max(st->iterations, iters);
-    st->av_rows = S.avp_rows;
+    st->av_rows = AVP_R;
     st->atu_rs = ATUP_RS;
     st->atu_rows = tune.atup_rows;
     for (int i = 0; i < nb; ++i) {
@@ -534,9 +517,9 @@ bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, i
 }
 
 // ---------------------------------------------------------------------------
-// Autotuner: times every candidate tile shape of the two sweeps on the given
+// Autotuner: times the candidate row groups of the A^T*U sweep on the given
 // systems (warm-up launch + 3 timed launches each, CUDA events), keeps the
-// fastest of each sweep.  The vectors are zero: the sweeps' cost does not
+// fastest.  The vectors are zero: the sweeps' cost does not
 // depend on the values.
 // ---------------------------------------------------------------------------
 static std::mutex g_tune_mu;
@@ -576,19 +559,8 @@ bool batch_autotune(const std::vector<BatchBody>& bodies, cudaStream_t s, BatchT
   char line[160];
   report.clear();
   BatchTune t0 = best;
-  double best_av = 1e300, best_atu = 1e300;
-  // rows per A*V CTA, block rows per A^T*U row group
-  const int av_rows[] = {0, 30, 24};
-  for (int r : av_rows) {
-    BatchTune t = t0;
-    t.avp_rows = r;
-    BatchSolver S;
-    if (!S.setup(bodies, 1, 1, t, s)) { err = S.err; cudaEventDestroy(e0); cudaEventDestroy(e1); return false; }
-    const double ms = time_it(S, true);
-    snprintf(line, sizeof line, "avp rows=%d: %.3f ms; ", S.avp_rows, ms);
-    report += line;
-    if (ms < best_av) { best_av = ms; best.avp_rows = S.avp_rows; }
-  }
+  double best_atu = 1e300;
+  // block rows per A^T*U row group (the A*V tile shape is fixed)
   const int grp_rows[] = {512, 1024, 4096};
   for (int g : grp_rows) {
     BatchTune t = t0;

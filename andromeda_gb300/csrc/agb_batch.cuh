@@ -22,7 +22,6 @@ struct BatchBody {
 
 // Tile shapes and schedule of the batched sweeps (picked by batch_autotune).
 struct BatchTune {
-  int avp_rows = 0;        // block rows per A*V CTA (even, 20..30; 0 = the count that fills whole waves)
   int atup_rows = 1024;    // block rows per A^T*U row group
   int check_every = 8;     // iterations per graph replay
 };
@@ -45,7 +44,7 @@ bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, i
                       cudaStream_t s, std::vector<int>& nit, std::vector<int>& istop, BatchStats* st,
                       std::string& err);
 
-// Times the candidate tile shapes of both sweeps on these systems (a few
+// Times the candidate row groups of the A^T*U sweep on these systems (a few
 // launches each, CUDA events) and returns the fastest; `report` lists the
 // candidates and their times.  Results are cached per (systems, total size)
 // class for the process.

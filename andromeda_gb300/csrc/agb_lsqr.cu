@@ -476,12 +476,12 @@ __global__ void __launch_bounds__(ATU3_THREADS, 1) k_atu3(const __grid_constant_
 // ---------------------------------------------------------------------------
 // Sweeps over the packed single layer (tile bodies avp_tile / atup_tile).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(AVP_WARPS * 32, 1) k_avp(const __grid_constant__ CUtensorMap tmA,
-                                                          const __grid_constant__ CUtensorMap tmW, int ne, int ldp,
-                                                          int rows, const LsqrScalars* sc, double* __restrict__ Y,
-                                                          float* __restrict__ Ys, double* __restrict__ part,
-                                                          int* errflag) {
-  avp_tile(&tmA, &tmW, ne, ldp, rows, sc, Y, Ys, part, errflag, (int)blockIdx.x);
+__global__ void __launch_bounds__(AVP_THREADS, 1) k_avp(const __grid_constant__ CUtensorMap tmA,
+                                                       const __grid_constant__ CUtensorMap tmW, int ne, int ldp,
+                                                       const LsqrScalars* sc, double* __restrict__ Y,
+                                                       float* __restrict__ Ys, double* __restrict__ part,
+                                                       int* errflag) {
+  avp_tile(&tmA, &tmW, ne, ldp, sc, Y, Ys, part, errflag, (int)blockIdx.x);
 }
 
 __global__ void __launch_bounds__(ATUP_C, 2) k_atup(const __grid_constant__ CUtensorMap tmA, int ne, int ldp,
@@ -875,8 +875,8 @@ static unsigned av2_blocks(const DenseLsqr& L) { return cdiv(L.m, AV2<T>::WARPS 
 template <typename T>
 static void launch_av2(const DenseLsqr& L) {
   if (L.packed) {
-    k_avp<<<cdiv(L.pk_ne, L.avp_rows), (L.avp_rows / 2 + 1) * 32, AVP_SMEM, L.stream>>>(L.tm_av, L.tm_vp, L.pk_ne, L.pk_ldp,
-                                                                              L.avp_rows, L.sc, L.Y, (float*)L.Ys,
+    k_avp<<<cdiv(L.pk_ne, AVP_R), AVP_THREADS, AVP_SMEM, L.stream>>>(L.tm_av, L.tm_vp, L.pk_ne, L.pk_ldp,
+                                                                    L.sc, L.Y, (float*)L.Ys,
                                                                               L.part, L.errflag);
     return;
   }
@@ -971,19 +971,7 @@ bool DenseLsqr::setup(const void* A_dev, bool is_fp32, int m_, int n_, int64_t l
       err = "packed layout: bad sizes";
       return false;
     }
-    {  // rows per A*V CTA (one CTA per SM): the even count <= 30 whose row blocks fill waves best
-      int dev = 0, nsm_ = 152;
-      cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev);
-      double best_eff = -1.0;
-      avp_rows = AVP_R;
-      for (int R = AVP_R - 2; R >= 20; R -= 2) {  // + one producer warp: at most 16 warps
-        const int64_t nrb = cdiv(pk_ne, R);
-        const double eff = (double)nrb / (double)(cdiv(nrb, nsm_) * (int64_t)nsm_);
-        if (eff > best_eff + 1e-9) { best_eff = eff; avp_rows = R; }
-      }
-    }
-    if (!make_packed_map(&tm_av, A_dev, pk_ldp, pk_ne, 6, avp_rows, err)) return false;
+    if (!make_packed_map(&tm_av, A_dev, pk_ldp, pk_ne, 6 * AVP_NB, AVP_R, err)) return false;
     if (!make_packed_map(&tm_atu, A_dev, pk_ldp, pk_ne, 6 * (ATUP_C / 64), ATUP_RS, err)) return false;
     CK(cudaMalloc(&Vp, (size_t)3 * K8 * pk_ldp * sizeof(float)));
     CK(cudaMemsetAsync(Vp, 0, (size_t)3 * K8 * pk_ldp * sizeof(float), stream));
@@ -1113,7 +1101,7 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
   if (maxit == 0) maxit = 10 * (m + n + 50);
   const int64_t mpad = ((int64_t)m + 255) / 256 * 256;
   const unsigned nb_av = packed ? cdiv(pk_ne, 8) : cdiv(m, AV_ROWS);  // residual sweep
-  const unsigned nb_av2 = packed ? cdiv(pk_ne, avp_rows) : mf ? cdiv((int64_t)m * K8, 256)
+  const unsigned nb_av2 = packed ? cdiv(pk_ne, AVP_R) : mf ? cdiv((int64_t)m * K8, 256)
                             : fp32 ? (use_tma ? cdiv(m, AV3_ROWS) : av2_blocks<float>(*this)) : av2_blocks<double>(*this);
   mf_q = q_dev;
   if (mf && !x0_zero) { err = "the matrix-free operator needs a zero warm start"; return false; }

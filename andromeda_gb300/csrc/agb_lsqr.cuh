@@ -52,7 +52,6 @@ struct DenseLsqr {
   bool packed = false;
   int pk_ne = 0, pk_ldp = 0;
   float* Vp = nullptr;          // [3][8][ldp] = q.V, sweep-1 operand of the packed layout
-  int avp_rows = 32;            // rows per CTA of the packed sweep 1 (even, <= 32)
   CUtensorMap tm_vp{};
   // matrix-free operator (A == nullptr): the sweeps recompute A's entries
   const struct MfOp* mf = nullptr;

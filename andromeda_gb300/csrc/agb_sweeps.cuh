@@ -240,12 +240,16 @@ __device__ __forceinline__ void atu3_tile(const CUtensorMap* tmA, int64_t lda, i
 // W = q.V (written by the vector update into Vp[b][k][ldp]), sweep 2's
 // partials are scaled by q in the reduction of the row-group partials.
 // ---------------------------------------------------------------------------
-// rows per CTA: at most 30 (two per compute warp, plus one producer warp); the
-// launch picks an even count that fills whole waves (row blocks / resident
-// CTAs close to an integer)
-constexpr int AVP_R = 32, AVP_BC = 64, AVP_ST = 4, AVP_WARPS = AVP_R / 2;
-constexpr size_t AVP_STAGE_A = 6 * (size_t)AVP_R * AVP_BC * sizeof(float);   // 48 KB (space of 32 rows)
-constexpr size_t AVP_STAGE_W = 3 * (size_t)K8 * AVP_BC * sizeof(float);      // 6 KB
+// A CTA owns AVP_R = 16 rows (two per compute warp, plus one producer warp) and
+// streams them in stages of 3 column blocks (192 columns: 4.5 KB contiguous per
+// row), two stages in flight.  Timed on GB300 against 12..30 rows per CTA and
+// 64..256 columns per stage (random packed matrices of 5 440..20 800 rows):
+// this shape was the fastest or within 2 % of it at every size, 0.92 of the
+// copy bandwidth at 12 000..20 800 rows.
+constexpr int AVP_R = 16, AVP_NB = 3, AVP_BC = 64 * AVP_NB, AVP_ST = 2, AVP_WARPS = AVP_R / 2;
+constexpr int AVP_THREADS = (AVP_WARPS + 1) * 32;
+constexpr size_t AVP_STAGE_A = 6 * (size_t)AVP_R * AVP_BC * sizeof(float);   // 72 KB
+constexpr size_t AVP_STAGE_W = 3 * (size_t)K8 * AVP_BC * sizeof(float);      // 18 KB
 constexpr size_t AVP_SMEM = AVP_ST * (AVP_STAGE_A + AVP_STAGE_W);
 
 __device__ __forceinline__ int sym6(int a, int b) {
@@ -269,20 +273,21 @@ __device__ __forceinline__ void reduce_scatter32(float (&v)[32], int lane) {
 }
 
 // Y[3i+a][k] = sum_j sum_b Ap[i][sym(a,b)][j] W[b][k][j] + gamma_k Y; a warp owns two rows i,
-// a lane two columns per stage; every 1024 columns the 24 FP32 sums of a row are
-// reduce-scattered over the warp into one FP64 running sum per lane.
-__device__ __forceinline__ void avp_tile(const CUtensorMap* tmA, const CUtensorMap* tmW, int ne, int ldp, int rows,
+// a lane two columns of each 64-column block; every 960 columns the 24 FP32 sums of a
+// row are reduce-scattered over the warp into one FP64 running sum per lane.
+__device__ __forceinline__ void avp_tile(const CUtensorMap* tmA, const CUtensorMap* tmW, int ne, int ldp,
                                          const LsqrScalars* sc, double* __restrict__ Y, float* __restrict__ Ys,
                                          double* __restrict__ part, int* errflag, int blk) {
+  constexpr int FLUSH = 1024 / AVP_BC;  // stages per FP64 flush
   extern __shared__ __align__(1024) unsigned char avp_smem[];
   float* sA = reinterpret_cast<float*>(avp_smem);
   float* sW = reinterpret_cast<float*>(avp_smem + AVP_ST * AVP_STAGE_A);
   __shared__ __align__(8) uint64_t full[AVP_ST], empty[AVP_ST];
   __shared__ double sPart[AVP_WARPS][K8];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int row_base = blk * rows;
-  const int nwarps = rows / 2;
-  const uint32_t stage_bytes = (uint32_t)(rows * 6 * AVP_BC * sizeof(float) + AVP_STAGE_W);
+  const int row_base = blk * AVP_R;
+  constexpr int nwarps = AVP_WARPS;
+  constexpr uint32_t stage_bytes = (uint32_t)(AVP_STAGE_A + AVP_STAGE_W);
   const int nst = (ldp + AVP_BC - 1) / AVP_BC;
   if (threadIdx.x == 0) {
     for (int s = 0; s < AVP_ST; ++s) {
@@ -297,8 +302,8 @@ __device__ __forceinline__ void avp_tile(const CUtensorMap* tmA, const CUtensorM
     if (k >= AVP_ST) mbar_wait_bounded(&empty[s], (uint32_t)(((k / AVP_ST) - 1) & 1), errflag);
     const int j0 = k * AVP_BC;
     mbar_expect_tx(&full[s], stage_bytes);
-    // one 3-D box: 32 rows x (6 planes x 64 columns), 1.5 KB contiguous per row
-    tma_load_3d(sA + (size_t)s * 6 * AVP_R * AVP_BC, tmA, 0, 6 * k, row_base, &full[s]);
+    // one 3-D box: 16 rows x (3 column blocks x 6 planes x 64 columns), 4.5 KB contiguous per row
+    tma_load_3d(sA + (size_t)s * 6 * AVP_R * AVP_BC, tmA, 0, 6 * AVP_NB * k, row_base, &full[s]);
     tma_load_2d(sW + (size_t)s * 3 * K8 * AVP_BC, tmW, j0, 0, &full[s]);
   };
   // warp nwarps is the producer: it only issues the stages (waiting for their
@@ -320,25 +325,29 @@ __device__ __forceinline__ void avp_tile(const CUtensorMap* tmA, const CUtensorM
   for (int k = 0; k < nst; ++k) {
     const int s = k % AVP_ST;
     mbar_wait_bounded(&full[s], (uint32_t)((k / AVP_ST) & 1), errflag);
-    const float* tA = sA + (size_t)s * 6 * AVP_R * AVP_BC + (2 * warp) * 6 * AVP_BC + lane * 2;  // [row][c][64]
-    const float* tW = sW + (size_t)s * 3 * K8 * AVP_BC + lane * 2;
 #pragma unroll
-    for (int b = 0; b < 3; ++b) {
-      float2 w[K8];
+    for (int h = 0; h < AVP_NB; ++h) {
+      // [row][column block][c][64]
+      const float* tA = sA + (size_t)s * 6 * AVP_R * AVP_BC + (2 * warp) * 6 * AVP_BC + h * 384 + lane * 2;
+      const float* tW = sW + (size_t)s * 3 * K8 * AVP_BC + h * 64 + lane * 2;
 #pragma unroll
-      for (int c = 0; c < K8; ++c) w[c] = *reinterpret_cast<const float2*>(tW + (size_t)(b * K8 + c) * AVP_BC);
+      for (int b = 0; b < 3; ++b) {
+        float2 w[K8];
 #pragma unroll
-      for (int r = 0; r < 2; ++r)
+        for (int c = 0; c < K8; ++c) w[c] = *reinterpret_cast<const float2*>(tW + (size_t)(b * K8 + c) * AVP_BC);
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          const float2 g = *reinterpret_cast<const float2*>(tA + r * 6 * AVP_BC + sym6(a, b) * AVP_BC);
+        for (int r = 0; r < 2; ++r)
 #pragma unroll
-          for (int c = 0; c < K8; ++c) acc[r][a][c] = fmaf(g.y, w[c].y, fmaf(g.x, w[c].x, acc[r][a][c]));
-        }
+          for (int a = 0; a < 3; ++a) {
+            const float2 g = *reinterpret_cast<const float2*>(tA + r * 6 * AVP_BC + sym6(a, b) * 64);
+#pragma unroll
+            for (int c = 0; c < K8; ++c) acc[r][a][c] = fmaf(g.y, w[c].y, fmaf(g.x, w[c].x, acc[r][a][c]));
+          }
+      }
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
-    if ((k & 15) == 15 || k == nst - 1) {
+    if ((k % FLUSH) == FLUSH - 1 || k == nst - 1) {
 #pragma unroll
       for (int r = 0; r < 2; ++r) {
         float v[32];

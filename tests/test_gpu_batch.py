@@ -37,7 +37,7 @@ def _single(agb, m, precision, eps):
     C.set_problem(agb.STOKES, [1, 2], np.ones((3, 2), np.int32), itri=5)
     R, nit, info = C.resistance_tensor(precision, eps=eps)
     C.close()
-    return R, nit
+    return R, nit, np.asarray(info["istop"])
 
 
 def test_batch_matches_single_body(agb):
@@ -48,16 +48,22 @@ def test_batch_matches_single_body(agb):
     # bodies do too
     assert np.all(np.isin(istop, (1, 2, 4)))
     assert st["waves"] == 1 and st["av_launches"] > 0 and st["launches"] > 0
-    assert 20 <= st["av_rows"] <= 30 and st["av_rows"] % 2 == 0 and st["atu_rs"] == 8
+    assert st["av_rows"] == 16 and st["atu_rs"] == 8
     for i, m in enumerate(meshes):
-        Rm, nm = _single(agb, m, agb.MIXED, 1e-9)
-        R64, _ = _single(agb, m, agb.FP64, 1e-11)
+        Rm, nm, im = _single(agb, m, agb.MIXED, 1e-9)
+        R64, _, _ = _single(agb, m, agb.FP64, 1e-11)
         assert _rel(R[i], Rm) < 1e-6, i
         assert _rel(R[i], R64) < 5e-6, i
-        # at eps 1e-9 the last iterations run near the FP32 rounding floor of the
-        # matrix, where the summation order of the sweeps (rows per CTA, row
-        # groups: tuned per batch) moves the stopping iteration by a few percent
-        assert np.all(np.abs(nit[i] - nm) <= np.maximum(5, nm // 10)), (nit[i], nm)
+        # iteration counts of the right-hand sides that both runs stopped by the
+        # residual tests (istop 1/2): at eps 1e-9 the last iterations run near
+        # the FP32 rounding floor of the matrix, where the summation order of
+        # the sweeps (row groups tuned per batch) moves the stopping iteration
+        # by a few percent.  The condition-limit stop (istop 4) follows the
+        # growth of LSQR's condition estimate along the near-null direction of
+        # the first-kind system and is not compared.
+        both = np.isin(istop[i], (1, 2)) & np.isin(im, (1, 2))
+        d = np.abs(nit[i] - nm)[both]
+        assert np.all(d <= np.maximum(5, nm[both] // 10)), (nit[i], nm, istop[i], im)
 
 
 def test_batch_waves_give_the_same_tensors(agb):
