@@ -676,30 +676,31 @@ __device__ double sum_part(const double* part, int nb, int c) {
 // phase 3: alpha after sweep 2; plane rotations; t1,t2,t3; gamma for next sweep.
 // phase 4: after the x/w update: dnorm, xnorm, residual estimates, stopping tests.
 // The partial sums of the producing kernel are reduced by the whole block in
-// a fixed order (thread t sums blocks t/8, t/8+32, ... of column t%8, then the
-// 32 per-thread sums are added in index order): deterministic and O(nb/32)
-// dependent loads instead of O(nb).
-constexpr int SCAL_THREADS = 256;
+// a fixed order (thread t sums blocks t/8, t/8+128, ... of column t%8, then a
+// shared-memory tree whose strides are multiples of 8 adds the 128 per-thread
+// sums of each column): deterministic, and the serial part is O(nb/128)
+// independent loads per thread (the kernel sits on the critical path of every
+// LSQR iteration).
+constexpr int SCAL_THREADS = 1024;
 __global__ void __launch_bounds__(SCAL_THREADS) k_scalars(LsqrScalars* sc, int k, int phase, const double* part,
                                                           int nb, int* nactive) {
   __shared__ double sred[SCAL_THREADS];
-  __shared__ double ssum[K8];
   {
     const int t = threadIdx.x, cc = t % K8;
     double a = 0.0;
-      for (int b = t / K8; b < nb; b += SCAL_THREADS / K8) a += part[(int64_t)b * K8 + cc];
+#pragma unroll 4
+    for (int b = t / K8; b < nb; b += SCAL_THREADS / K8) a += part[(int64_t)b * K8 + cc];
     sred[t] = a;
     __syncthreads();
-    if (t < K8) {
-      double tot = 0.0;
-      for (int i = t; i < SCAL_THREADS; i += K8) tot += sred[i];
-      ssum[t] = tot;
+#pragma unroll
+    for (int st = SCAL_THREADS / 2; st >= K8; st >>= 1) {
+      if (t < st) sred[t] += sred[t + st];
+      __syncthreads();
     }
-    __syncthreads();
   }
   const int c = threadIdx.x;
   if (c >= K8) return;
-  lsqr_phase(sc[c], c, k, phase, ssum[c], nactive);
+  lsqr_phase(sc[c], c, k, phase, sred[c], nactive);
 }
 
 // ---------------------------------------------------------------------------
