@@ -152,10 +152,8 @@ def measured_peaks():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", str(rank)))
-    return rank, world, local
+    from andromeda_gb300.ranks import dist_env as env
+    return env()
 
 
 # ---------------------------------------------------------------------------
@@ -255,16 +253,15 @@ def run_batch(args, rank, world, local):
     import andromeda_gb300 as A
     from andromeda_gb300 import mesh as M
     meshes, params = M.batch_bodies(n_bodies=args.bodies)
-    mine = [m for i, m in enumerate(meshes) if i % world == rank]
+    from andromeda_gb300.ranks import shard, max_over_ranks, barrier
+    mine = [meshes[i] for i in shard(len(meshes), world, rank)]
     ctx = A.Context(local if world > 1 else 0)
     eps = args.batch_eps
     tune = not args.no_autotune
     warm = mine[:32]
     for _ in range(args.warmup):
         A.batch_resistance(warm, eps=eps, ctx=ctx, autotune=tune)
-    if world > 1:
-        import torch.distributed as dist
-        dist.barrier()
+    barrier()
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         Rs, nits, istops, sts = [], [], [], []
@@ -274,12 +271,7 @@ def run_batch(args, rank, world, local):
         t1 = time.perf_counter()
     dev_s = sum(st["device_ms"] for st in sts) / 1000.0
     wall_s = t1 - t0
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([dev_s, wall_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_s, wall_s = float(t[0].item()), float(t[1].item())
+    dev_s, wall_s = max_over_ranks([dev_s, wall_s], device="cuda" if world > 1 else "cpu")
     value = args.bodies * args.steps / dev_s
     R, nit, istop, st = Rs[-1], nits[-1], istops[-1], sts[-1]
     # FP64 GPU path on a seeded random sample of the bodies: its rate at the same
@@ -568,10 +560,8 @@ def main():
     kt = C.kernel_times(reset=True)
     elapsed = sum(dev_ms) / 1000.0
     if dist is not None:
-        import torch
-        t = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+        from andromeda_gb300.ranks import max_over_ranks
+        elapsed = max_over_ranks([elapsed], device="cuda")[0]
     value = world * args.steps / elapsed
     R = Rs[-1]
     nit = nits[-1]
