@@ -32,16 +32,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 // bounded wait: after ~2^22 failed tries the barrier is reported through
-// errflag and the wait gives up (the copy is in bounds by construction, so
-// this only guards against a hang)
-__device__ __forceinline__ void mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* errflag) {
+// errflag and the wait gives up (the copies are in bounds by construction, so
+// this only guards against a hang); once any wait has given up (errflag set),
+// later long waits give up after ~1024 tries, so a launch whose barrier broke
+// ends quickly.  Returns whether the barrier phase completed.
+__device__ __forceinline__ bool mbar_wait_ok(uint64_t* bar, uint32_t parity, int* errflag) {
   uint32_t tries = 0;
   while (!mbar_try_wait(bar, parity)) {
-    if (++tries > (1u << 22)) {
+    ++tries;
+    if ((tries & 1023u) == 0 && errflag && *(volatile int*)errflag) return false;
+    if (tries > (1u << 22)) {
       if (errflag) atomicExch(errflag, 1);
-      break;
+      return false;
     }
   }
+  return true;
+}
+__device__ __forceinline__ void mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* errflag) {
+  (void)mbar_wait_ok(bar, parity, errflag);
 }
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar) {

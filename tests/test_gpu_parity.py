@@ -206,3 +206,30 @@ def test_crs_dropin_matches_oracle(agb, orc):
     nit2, ierr2, _ = orc.lsqr_solve(mrow, ncol, ia, ja, a2, q2, b, x2, maxit=0, eps=1e-13)
     assert ierr1 == ierr2 == 4
     assert abs(nit1 - nit2) <= max(3, nit2 // 20)
+
+
+def test_c2_full_size_against_frozen_fp64(agb):
+    """The headline workload at full size (20 800 elements, 62 400 unknowns, the
+    10.4 GB packed single layer) through the mixed path, against the FP64 GPU
+    tensor frozen in tests/golden (FP64 assembly + FP64 LSQR to eps 1e-11).
+    Tolerances: 1e-6 relative to the largest entry (the benchmark's accuracy
+    bar), symmetry of the tensor within 1e-6 (the exact tensor is symmetric),
+    drag and torque of the concentric spheres within 1e-3 of the analytic
+    values (discretisation error of the level-5 sphere)."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(__file__), "golden", "c2_fp64_tensor.json")) as f:
+        ref = json.load(f)
+    R64 = np.asarray(ref["R"])
+    m = M.particle_in_sphere(M.icosphere(5, 1.0, inward=True), outer_level=2, outer_radius=200.0)
+    C = _ctx(agb, m, agb.STOKES, [1, 2])
+    R, nit, info = C.resistance_tensor(agb.MIXED, 1, 2, eps=1e-7)
+    C.close()
+    assert np.all(np.isin(info["istop"], (1, 2)))
+    assert _rel(R, R64) < 1e-6
+    assert np.max(np.abs(R - R.T)) / np.max(np.abs(R)) < 1e-6
+    lam = 1.0 / 200.0
+    drag = 6 * np.pi * (1 - lam ** 5) / (1 - 9 * lam / 4 + 5 * lam ** 3 / 2 - 9 * lam ** 5 / 4 + lam ** 6)
+    torque = 8 * np.pi / (1 - lam ** 3)
+    assert abs(abs(R[0, 0]) / drag - 1) < 1e-3
+    assert abs(abs(R[3, 3]) / torque - 1) < 1e-3
