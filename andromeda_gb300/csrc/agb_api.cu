@@ -1767,19 +1767,24 @@ int agb_mlp_predict(agb_mlp* m, int n, const float* X, float* Y, int split, doub
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  bool ok = net.ensure_ws(chunk) && cudaMalloc(&dX, (size_t)n * net.nin * sizeof(float)) == cudaSuccess &&
+  if (split < 0 || split > 2) return mlp_fail(m, AGB_ERR_ARG, "agb_mlp_predict: split must be 0, 1 or 2");
+  bool ok = (split == 1 || net.ensure_ws(chunk)) && cudaMalloc(&dX, (size_t)n * net.nin * sizeof(float)) == cudaSuccess &&
             cudaMalloc(&dY, (size_t)n * net.nout * sizeof(float)) == cudaSuccess &&
             cudaMemcpyAsync(dX, X, (size_t)n * net.nin * sizeof(float), cudaMemcpyHostToDevice, net.s) == cudaSuccess;
   if (ok) {
     cudaEventRecord(e0, net.s);
-    for (int r0 = 0; r0 < n; r0 += chunk) {
-      const int rows = std::min(chunk, n - r0);
-      net.load_inputs(rows, dX + (size_t)r0 * net.nin);
-      net.forward(rows, false, split != 0);
-      net.output(rows, dY + (size_t)r0 * net.nout);
+    if (split == 1) {  // fused split-BF16 inference: one kernel over all n queries
+      ok = net.infer(n, dX, dY);
+    } else {           // layer-by-layer GEMMs (split 2: split-BF16, 0: plain BF16 products)
+      for (int r0 = 0; r0 < n; r0 += chunk) {
+        const int rows = std::min(chunk, n - r0);
+        net.load_inputs(rows, dX + (size_t)r0 * net.nin);
+        net.forward(rows, false, split != 0);
+        net.output(rows, dY + (size_t)r0 * net.nout);
+      }
     }
     cudaEventRecord(e1, net.s);
-    ok = cudaGetLastError() == cudaSuccess &&
+    ok = ok && cudaGetLastError() == cudaSuccess &&
          cudaMemcpyAsync(Y, dY, (size_t)n * net.nout * sizeof(float), cudaMemcpyDeviceToHost, net.s) == cudaSuccess &&
          cudaStreamSynchronize(net.s) == cudaSuccess;
     float ms = 0.f;

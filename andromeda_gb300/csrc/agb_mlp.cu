@@ -39,6 +39,8 @@ __device__ __forceinline__ float dsilu_f(float z) {
   return s * (1.0f + z * (1.0f - s));
 }
 
+__device__ __forceinline__ uint32_t smem_u32_mlp(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
 __device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
   asm volatile(
       "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
@@ -223,6 +225,203 @@ static void gemm(bool split, int M, int N, int K, const float* A, int lda, const
 }
 
 // ---------------------------------------------------------------------------
+// Fused inference (split-BF16): one CTA runs 128 queries through all four
+// layers.  The activations stay in shared memory as BF16 hi/lo pairs
+// ([128][256+8] each); a warp owns 16 query rows and all output columns of a
+// layer (32 n-tiles x 4 FP32 accumulators per lane), so a layer's output can
+// overwrite the warp's own input rows without a block barrier.  The weights,
+// pre-split into BF16 hi/lo ([layer][hi/lo][N][K], k contiguous), stream
+// through two 40 KB shared-memory buffers in chunks of 32 k (cp.async, all
+// threads).  Input normalisation and output de-normalisation are fused.  The
+// accumulation order (k16 steps in order; hi*hi, hi*lo, lo*hi per step) and
+// the FP32 epilogues are those of k_mlp_gemm, so the outputs equal the
+// unfused forward's.
+// ---------------------------------------------------------------------------
+constexpr int FI_M = 128, FI_H = 256, FI_HP = FI_H + 8, FI_KC = 32, FI_WP = FI_KC + 8;
+constexpr int FI_NIN = 16, FI_NOUT = 32;  // padded K of layer 1, padded N of layer 4
+constexpr size_t FI_SMEM_H = 2ull * FI_M * FI_HP * sizeof(__nv_bfloat16);         // 132 KB
+constexpr size_t FI_SMEM_W = 2ull * 2 * FI_H * FI_WP * sizeof(__nv_bfloat16);     // 80 KB
+constexpr size_t FI_SMEM = FI_SMEM_H + FI_SMEM_W;
+// packed weight offsets (elements): L1 [2][256][16], L2 [2][256][256], L3 [2][256][256], L4 [2][32][256]
+constexpr int64_t FI_O1 = 0, FI_O2 = FI_O1 + 2 * FI_H * FI_NIN, FI_O3 = FI_O2 + 2 * FI_H * FI_H,
+                  FI_O4 = FI_O3 + 2 * FI_H * FI_H, FI_WTOT = FI_O4 + 2 * FI_NOUT * FI_H;
+constexpr int FI_CHUNKS = 1 + 3 * (FI_H / FI_KC);  // layer 1: one chunk of 16 k; layers 2-4: 8 each
+
+__global__ void k_mlp_pack_infer(const float* __restrict__ P, int nin, int nh, int nout, int64_t o0, int64_t o2,
+                                 int64_t o4, int64_t o6, __nv_bfloat16* __restrict__ wb) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= FI_WTOT) return;
+  int64_t r;
+  int K, N, k, n, hl;
+  const float* W;
+  int kin, nreal;
+  if (t < FI_O2) { r = t - FI_O1; K = FI_NIN; N = FI_H; W = P + o0; kin = nin; nreal = nh; }
+  else if (t < FI_O3) { r = t - FI_O2; K = FI_H; N = FI_H; W = P + o2; kin = nh; nreal = nh; }
+  else if (t < FI_O4) { r = t - FI_O3; K = FI_H; N = FI_H; W = P + o4; kin = nh; nreal = nh; }
+  else { r = t - FI_O4; K = FI_H; N = FI_NOUT; W = P + o6; kin = nh; nreal = nout; }
+  hl = (int)(r / ((int64_t)N * K));
+  const int64_t q = r % ((int64_t)N * K);
+  n = (int)(q / K);
+  k = (int)(q % K);
+  const float v = (n < nreal && k < kin) ? W[(int64_t)n * kin + k] : 0.f;
+  const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+  wb[t] = hl == 0 ? hi : __float2bfloat16_rn(v - __bfloat162float(hi));
+}
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32_mlp(dst)), "l"(src) : "memory");
+}
+
+// stage chunk c of the packed weights into buffer `buf` ([2 hl][256][FI_WP])
+__device__ __forceinline__ void fi_stage(const __nv_bfloat16* __restrict__ wb, __nv_bfloat16* Ws, int c) {
+  int64_t base;
+  int N, K, k0, kw;
+  if (c == 0) { base = FI_O1; N = FI_H; K = FI_NIN; k0 = 0; kw = FI_NIN; }
+  else {
+    const int l = (c - 1) / (FI_H / FI_KC);  // 0: layer 2, 1: layer 3, 2: layer 4
+    base = l == 0 ? FI_O2 : l == 1 ? FI_O3 : FI_O4;
+    N = l == 2 ? FI_NOUT : FI_H;
+    K = FI_H;
+    k0 = ((c - 1) % (FI_H / FI_KC)) * FI_KC;
+    kw = FI_KC;
+  }
+  const int per_row = kw / 8;  // 16-byte pieces per row
+  const int total = 2 * N * per_row;
+  for (int i = threadIdx.x; i < total; i += blockDim.x) {
+    const int hl = i / (N * per_row);
+    const int rem = i % (N * per_row);
+    const int n = rem / per_row, pc = rem % per_row;
+    cp_async16(Ws + ((size_t)hl * FI_H + n) * FI_WP + pc * 8, wb + base + ((int64_t)hl * N + n) * K + k0 + pc * 8);
+  }
+}
+
+// one chunk of KS k16 steps for NT n-tiles: A = this warp's 16 rows of H (cols kH..), B = the staged chunk
+template <int NT, int KS>
+__device__ __forceinline__ void fi_chunk(float (&acc)[32][4], const __nv_bfloat16* Hh, const __nv_bfloat16* Hl,
+                                         int kH, const __nv_bfloat16* Wh, const __nv_bfloat16* Wl, int gid, int tig) {
+#pragma unroll
+  for (int ks = 0; ks < KS; ++ks) {
+    uint32_t ah[4], al[4];
+    const int ka = kH + ks * 16 + tig * 2;
+    ah[0] = *reinterpret_cast<const uint32_t*>(Hh + gid * FI_HP + ka);
+    ah[1] = *reinterpret_cast<const uint32_t*>(Hh + (gid + 8) * FI_HP + ka);
+    ah[2] = *reinterpret_cast<const uint32_t*>(Hh + gid * FI_HP + ka + 8);
+    ah[3] = *reinterpret_cast<const uint32_t*>(Hh + (gid + 8) * FI_HP + ka + 8);
+    al[0] = *reinterpret_cast<const uint32_t*>(Hl + gid * FI_HP + ka);
+    al[1] = *reinterpret_cast<const uint32_t*>(Hl + (gid + 8) * FI_HP + ka);
+    al[2] = *reinterpret_cast<const uint32_t*>(Hl + gid * FI_HP + ka + 8);
+    al[3] = *reinterpret_cast<const uint32_t*>(Hl + (gid + 8) * FI_HP + ka + 8);
+    const int kb = ks * 16 + tig * 2;
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+      const int n = nt * 8 + gid;
+      uint32_t bh[2], bl[2];
+      bh[0] = *reinterpret_cast<const uint32_t*>(Wh + n * FI_WP + kb);
+      bh[1] = *reinterpret_cast<const uint32_t*>(Wh + n * FI_WP + kb + 8);
+      bl[0] = *reinterpret_cast<const uint32_t*>(Wl + n * FI_WP + kb);
+      bl[1] = *reinterpret_cast<const uint32_t*>(Wl + n * FI_WP + kb + 8);
+      mma_bf16(acc[nt], ah, bh);
+      mma_bf16(acc[nt], ah, bl);
+      mma_bf16(acc[nt], al, bh);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256, 1) k_mlp_infer(int n, int nin, int nout, const float* __restrict__ X,
+                                                      const float* __restrict__ P, int64_t ob1, int64_t ob2,
+                                                      int64_t ob3, int64_t ob4, const float* __restrict__ norm,
+                                                      const __nv_bfloat16* __restrict__ wb, float* __restrict__ Y) {
+  extern __shared__ __align__(16) unsigned char fi_smem[];
+  __nv_bfloat16* H = reinterpret_cast<__nv_bfloat16*>(fi_smem);                // [2 hl][128][FI_HP]
+  __nv_bfloat16* Wb = reinterpret_cast<__nv_bfloat16*>(fi_smem + FI_SMEM_H);   // [2 buf][2 hl][256][FI_WP]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gid = lane >> 2, tig = lane & 3;
+  const int row0 = blockIdx.x * FI_M + warp * 16;  // this warp's first query
+  __nv_bfloat16* Hh = H + (size_t)(warp * 16) * FI_HP;
+  __nv_bfloat16* Hl = H + (size_t)(FI_M + warp * 16) * FI_HP;
+  const float* xm = norm;
+  const float* xs = norm + nin;
+  const float* ym = norm + 2 * nin;
+  const float* ys = norm + 2 * nin + nout;
+  fi_stage(wb, Wb, 0);
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  // normalised inputs of the warp's 16 rows into H columns 0..15
+  for (int i = lane; i < 16 * FI_NIN; i += 32) {
+    const int r = i / FI_NIN, k = i % FI_NIN;
+    const int g = row0 + r;
+    float v = 0.f;
+    if (k < nin && g < n) v = (X[(int64_t)g * nin + k] - xm[k]) / xs[k];
+    const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+    Hh[r * FI_HP + k] = hi;
+    Hl[r * FI_HP + k] = __float2bfloat16_rn(v - __bfloat162float(hi));
+  }
+  __syncwarp();
+  float acc[32][4];
+#pragma unroll
+  for (int nt = 0; nt < 32; ++nt)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[nt][q] = 0.f;
+  for (int c = 0; c < FI_CHUNKS; ++c) {
+    if (c + 1 < FI_CHUNKS) {
+      fi_stage(wb, Wb + (size_t)((c + 1) & 1) * 2 * FI_H * FI_WP, c + 1);
+      asm volatile("cp.async.commit_group;" ::: "memory");
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    }
+    __syncthreads();
+    const __nv_bfloat16* Wh = Wb + (size_t)(c & 1) * 2 * FI_H * FI_WP;
+    const __nv_bfloat16* Wl = Wh + (size_t)FI_H * FI_WP;
+    const int layer = c == 0 ? 1 : 2 + (c - 1) / (FI_H / FI_KC);
+    const int kH = c == 0 ? 0 : ((c - 1) % (FI_H / FI_KC)) * FI_KC;
+    const bool last = c == 0 || ((c - 1) % (FI_H / FI_KC)) == FI_H / FI_KC - 1;
+    if (layer == 1) fi_chunk<32, 1>(acc, Hh, Hl, kH, Wh, Wl, gid, tig);
+    else if (layer < 4) fi_chunk<32, 2>(acc, Hh, Hl, kH, Wh, Wl, gid, tig);
+    else fi_chunk<FI_NOUT / 8, 2>(acc, Hh, Hl, kH, Wh, Wl, gid, tig);
+    if (last && layer < 4) {
+      // bias + SiLU, split into hi/lo over this warp's own rows (all of their reads are done)
+      const float* bias = P + (layer == 1 ? ob1 : layer == 2 ? ob2 : ob3);
+      __syncwarp();
+#pragma unroll
+      for (int nt = 0; nt < 32; ++nt) {
+        const int col = nt * 8 + tig * 2;
+        const float b0 = bias[col], b1 = bias[col + 1];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const float v0 = silu_f(acc[nt][2 * h] + b0), v1 = silu_f(acc[nt][2 * h + 1] + b1);
+          const __nv_bfloat16 h0 = __float2bfloat16_rn(v0), h1 = __float2bfloat16_rn(v1);
+          __nv_bfloat162 hh, ll;
+          hh.x = h0; hh.y = h1;
+          ll.x = __float2bfloat16_rn(v0 - __bfloat162float(h0));
+          ll.y = __float2bfloat16_rn(v1 - __bfloat162float(h1));
+          const int r = gid + 8 * h;
+          *reinterpret_cast<__nv_bfloat162*>(Hh + r * FI_HP + col) = hh;
+          *reinterpret_cast<__nv_bfloat162*>(Hl + r * FI_HP + col) = ll;
+          acc[nt][2 * h] = 0.f;
+          acc[nt][2 * h + 1] = 0.f;
+        }
+      }
+      __syncwarp();
+    } else if (last) {
+      // bias, de-normalisation, store
+      const float* bias = P + ob4;
+#pragma unroll
+      for (int nt = 0; nt < FI_NOUT / 8; ++nt)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int col = nt * 8 + tig * 2 + (q & 1);
+          const int g = row0 + gid + ((q >= 2) ? 8 : 0);
+          if (col < nout && g < n) {
+            const float v = acc[nt][q] + bias[col];
+            Y[(int64_t)g * nout + col] = v * ys[col] + ym[col];
+          }
+        }
+    }
+    __syncthreads();  // the buffer of chunk c is refilled by the stage of chunk c + 2
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Host object
 // ---------------------------------------------------------------------------
 Mlp::~Mlp() { release(); }
@@ -230,8 +429,10 @@ Mlp::~Mlp() { release(); }
 void Mlp::release() {
   cudaFree(params); cudaFree(grads); cudaFree(adam_m); cudaFree(adam_v); cudaFree(norm); cudaFree(ws);
   cudaFree(part);
+  cudaFree(wb);
   params = grads = adam_m = adam_v = norm = ws = nullptr;
   part = nullptr;
+  wb = nullptr;
   ws_rows = 0;
 }
 
@@ -383,6 +584,35 @@ void Mlp::output(int rows, float* Y_dev) {
   k_mlp_denorm_out<<<cdv((int64_t)rows * nout, 256), 256, 0, s>>>(rows, nout, Y, norm + 2 * nin,
                                                                    norm + 2 * nin + nout, Y_dev);
   launches += 1;
+}
+
+bool Mlp::infer(int rows, const float* X_dev, float* Y_dev) {
+  if (nh != FI_H || nin > FI_NIN || nout > FI_NOUT || nin < 1 || nout < 1) {
+    err = "fused inference needs nh = 256, nin <= 16, nout <= 32";
+    return false;
+  }
+  if (!wb && cudaMalloc(&wb, FI_WTOT * sizeof(__nv_bfloat16)) != cudaSuccess) {
+    wb = nullptr;
+    err = "mlp: inference weights";
+    return false;
+  }
+  if (cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FI_SMEM) != cudaSuccess) {
+    err = "mlp: fused inference shared memory";
+    return false;
+  }
+  int64_t o[8];
+  offsets(o);
+  __nv_bfloat16* w = static_cast<__nv_bfloat16*>(wb);
+  k_mlp_pack_infer<<<cdv(FI_WTOT, 256), 256, 0, s>>>(params, nin, nh, nout, o[0], o[2], o[4], o[6], w);
+  if (rows > 0)
+    k_mlp_infer<<<cdv(rows, FI_M), 256, FI_SMEM, s>>>(rows, nin, nout, X_dev, params, o[1], o[3], o[5], o[7], norm,
+                                                     w, Y_dev);
+  launches += rows > 0 ? 2 : 1;
+  if (cudaGetLastError() != cudaSuccess) {
+    err = "mlp: fused inference launch";
+    return false;
+  }
+  return true;
 }
 
 double Mlp::loss_sum(int rows) {

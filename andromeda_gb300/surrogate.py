@@ -148,11 +148,15 @@ class MLP:
                                        int(seed), hist, st))
         return hist, {"device_ms": st[0], "launches": int(st[1]), "adam_steps": int(st[2])}
 
-    def predict(self, X, split=True):
+    def predict(self, X, split=True, fused=True):
+        """Outputs for X (physical units) and the kernel time in ms.  split:
+        split-BF16 products (FP32-level accuracy); fused: one kernel for all
+        layers (split only), else the layer-by-layer GEMMs."""
         X = np.ascontiguousarray(X, dtype=np.float32)
         Y = np.zeros((len(X), self.nout), np.float32)
         ms = C.c_double()
-        self._ck(self._L.agb_mlp_predict(self.h, len(X), X, Y, int(bool(split)), C.byref(ms)))
+        mode = (1 if fused else 2) if split else 0
+        self._ck(self._L.agb_mlp_predict(self.h, len(X), X, Y, mode, C.byref(ms)))
         return Y, ms.value
 
 

@@ -286,8 +286,11 @@ int agb_solve_lu(agb_context* ctx, int nrhs, const double* u, double* x, int* in
  * error on n rows (split != 0: split-BF16 products); gradient and loss out.
  * agb_mlp_train: epochs over n rows in shuffled mini-batches (full batches
  * only), loss_hist[epoch] = mean squared normalised error; stats[3]: device ms,
- * kernel launches, Adam steps so far.  agb_mlp_predict: device_ms = kernel
- * time of the n inferences. */
+ * kernel launches, Adam steps so far.  agb_mlp_predict: split 1 = split-BF16
+ * products in one fused kernel (128 queries per CTA, activations kept on chip;
+ * needs nhidden = 256, nin <= 16, nout <= 32), split 2 = split-BF16 through
+ * the layer-by-layer GEMMs of the training forward (same results), split 0 =
+ * plain BF16 products; device_ms = kernel time of the n inferences. */
 typedef struct agb_mlp agb_mlp;
 int agb_mlp_create(agb_mlp** out, int device, int nin, int nhidden, int nout, unsigned long long seed);
 int agb_mlp_destroy(agb_mlp* m);

@@ -38,6 +38,35 @@ def test_mlp_gradient_matches_oracle(agb):
     net.close()
 
 
+def test_fused_inference_matches_layer_gemms_and_oracle(agb):
+    """The fused one-kernel split-BF16 inference against the layer-by-layer
+    split-BF16 GEMMs (same accumulation order and FP32 epilogues: equal up to
+    1 ulp of the outputs) and against the FP64 oracle forward (split-BF16
+    products carry ~16 mantissa bits: 1e-4 of the largest output), on a
+    query count that is not a multiple of the 128-query CTA tile."""
+    import mlp_oracle as mo
+    net = _net(agb)
+    rng = np.random.default_rng(5)
+    n = 1000
+    X = rng.uniform(0.2, 1.8, (n, 5)).astype(np.float32)
+    xm, xs = X.mean(0), X.std(0) + 1e-3
+    ym = rng.normal(size=21).astype(np.float32)
+    ys = rng.uniform(0.5, 2.0, 21).astype(np.float32)
+    net.set_normalization(xm, xs, ym, ys)
+    p = net.params()
+    p = p + rng.normal(scale=0.05, size=p.shape).astype(np.float32)  # non-zero biases
+    net.set_params(p)
+    Yf, _ = net.predict(X, split=True, fused=True)
+    Yg, _ = net.predict(X, split=True, fused=False)
+    assert np.all(np.isfinite(Yf))
+    assert np.max(np.abs(Yf - Yg)) <= 2.0 * np.max(np.spacing(np.abs(Yg)))
+    Xn = (X.astype(np.float64) - xm) / xs
+    Yo, _ = mo.forward(p.astype(np.float64), Xn)
+    Yo = Yo * ys + ym
+    assert np.max(np.abs(Yf - Yo)) < 1e-4 * np.max(np.abs(Yo))
+    net.close()
+
+
 def test_mlp_trains_on_the_gpu(agb):
     """A smooth 5 -> 21 map is learned: the loss falls by two orders of magnitude."""
     net = _net(agb)
