@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=1)
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "batch", "surrogate", "large"],
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "batch", "surrogate", "large", "laplace"],
                     help="sphere: one level-5 sphere (default); batch: the many-body superellipsoid set")
     ap.add_argument("--bodies", type=int, default=512, help="batch workload: number of bodies")
     ap.add_argument("--fp64-sample", type=int, default=6, help="batch workload: bodies solved on the FP64 path")
@@ -65,6 +65,8 @@ def parse():
                     help="large: packed FP32 matrix resident in HBM and solved to convergence, or matrix-free sweeps")
     ap.add_argument("--large-maxit", type=int, default=0, help="large/resident: LSQR iteration limit (0: reference default)")
     ap.add_argument("--grid", default="160x320", help="large: superellipsoid rings x sectors")
+    ap.add_argument("--itri", type=int, default=1, help="laplace: triangle rule (1 = 7 points)")
+    ap.add_argument("--laplace-eps", type=float, default=1e-12, help="laplace: LSQR eps")
     return ap.parse_args()
 
 
@@ -422,6 +424,69 @@ def run_large(args):
     C.close()
 
 
+def run_laplace(args):
+    """Laplace case of the reference (its own CPU-runnable configuration):
+    unit icosphere level 3 (642 nodes, 1 280 flat triangles), Dirichlet
+    u = x + 2y + 3z on the whole surface, unknown flux, FP64, ITRI --itri
+    (1 = 7-point rule), LSQR eps --laplace-eps.  A step is assembly + solve on
+    the GPU (FP64 path, host arrays in and out).  The oracle port of the
+    reference's CPU path (integration of all nsp rows, CRS system,
+    lsqr_precon + lsqr_solve) runs in full on the host cores beside it, and
+    its flux is the parity check of the step's."""
+    import numpy as np
+    import andromeda_gb300 as A
+    from andromeda_gb300 import mesh as M
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    m = M.icosphere(3)
+    u = m["xyz"] @ np.array([1.0, 2.0, 3.0])
+    C = A.Context(0)
+    C.set_mesh(m)
+    C.set_problem(A.LAPLACE, [1], A.dirichlet_known(A.LAPLACE, 1), itri=args.itri)
+
+    def step():
+        C.assemble(A.FP64)
+        return C.solve(u[None], eps=args.laplace_eps)
+
+    for _ in range(max(args.warmup, 1)):
+        step()
+    C.kernel_times(reset=True)
+    times = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            x, nit, istop = step()
+            times.append(time.perf_counter() - t0)
+    kt = C.kernel_times(reset=True)
+    n, _, _ = C.geometry()
+    qex = -(n @ np.array([1.0, 2.0, 3.0]))
+    C.close()
+    # the oracle (reference algorithm, FP64, host cores), timed in full
+    t0 = time.perf_counter()
+    P = oracle.Problem(1, m, walls=[1], known=[[1]], itri=args.itri)
+    P.form_integrals()
+    P.form_system()
+    _, q_ref, nit_ref, _ = P.laplace_solve(u, np.zeros(P.nelem), maxit=0, eps=args.laplace_eps)
+    t_cpu = time.perf_counter() - t0
+    P.close()
+    ms = 1000.0 * statistics.median(times)
+    line = {"metric": "Laplace BEM solves/s (assembly + LSQR, FP64)", "value": 1000.0 / ms, "unit": "solves/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 1), "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"unit icosphere L3 (1280 tri), Laplace, u = x+2y+3z, ITRI {args.itri}, "
+                                   f"LSQR eps {args.laplace_eps:g}"},
+            "nit": int(nit[0]), "istop": int(istop[0]), "nit_oracle": int(nit_ref),
+            "rel_err_vs_oracle": float(np.max(np.abs(x[0] - q_ref)) / np.max(np.abs(q_ref))),
+            "flux_rel_err_vs_analytic": float(np.linalg.norm(x[0] - qex) / np.linalg.norm(qex)),
+            "cpu_baseline": {"value": 1.0 / t_cpu, "unit": "solves/s", "cores": oracle.num_threads(), "kind": "port",
+                             "sample": "the whole solve (integration of all rows, CRS system, lsqr_precon + "
+                                       "lsqr_solve), not scaled"},
+            "e2e": {"value": 1000.0 / ms, "unit": "solves/s", "h2d_bytes_per_step": int(u.nbytes),
+                    "d2h_bytes_per_step": int(x.nbytes)},
+            "clocks": clk.summary(), "gpu_launches": kt["launches"] // max(args.steps, 1)}
+    print(json.dumps(line), flush=True)
+
+
 def run_surrogate(args):
     """Learned part: BEM tensors of superellipsoids (batched mixed BEM) train the
     MLP on the GPU; one batch of queries is answered by it (BEM outside the
@@ -513,6 +578,10 @@ def main():
     if args.workload == "large":
         if rank == 0:
             run_large(args)
+        return
+    if args.workload == "laplace":
+        if rank == 0:
+            run_laplace(args)
         return
     if args.workload == "batch":
         if world > 1:
