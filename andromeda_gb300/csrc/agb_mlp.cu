@@ -41,8 +41,11 @@ __device__ __forceinline__ float dsilu_f(float z) {
 
 __device__ __forceinline__ uint32_t smem_u32_mlp(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
+// not volatile: the only effect is the accumulator update, so the compiler may
+// interleave independent products (the three split products of one
+// accumulator stay in order through their data dependence)
 __device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-  asm volatile(
+  asm(
       "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
       "{%0,%1,%2,%3};"
       : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
@@ -227,10 +230,11 @@ static void gemm(bool split, int M, int N, int K, const float* A, int lda, const
 // ---------------------------------------------------------------------------
 // Fused inference (split-BF16): one CTA runs 128 queries through all four
 // layers.  The activations stay in shared memory as BF16 hi/lo pairs
-// ([128][256+8] each); a warp owns 16 query rows and all output columns of a
-// layer (32 n-tiles x 4 FP32 accumulators per lane), so a layer's output can
-// overwrite the warp's own input rows without a block barrier.  The weights,
-// pre-split into BF16 hi/lo ([layer][hi/lo][N][K], k contiguous), stream
+// ([128][256+8] each); 16 warps: two warps share 16 query rows, each owning
+// half of a layer's output columns (16 n-tiles x 4 FP32 accumulators per
+// lane); a block barrier separates the last reads of a layer's input rows from
+// the writes of its outputs into the same rows.  The weights, pre-split into
+// BF16 hi/lo ([layer][hi/lo][N][K], k contiguous), stream
 // through two 40 KB shared-memory buffers in chunks of 32 k (cp.async, all
 // threads).  Input normalisation and output de-normalisation are fused.  The
 // accumulation order (k16 steps in order; hi*hi, hi*lo, lo*hi per step) and
@@ -295,10 +299,13 @@ __device__ __forceinline__ void fi_stage(const __nv_bfloat16* __restrict__ wb, _
   }
 }
 
-// one chunk of KS k16 steps for NT n-tiles: A = this warp's 16 rows of H (cols kH..), B = the staged chunk
+// one chunk of KS k16 steps for NT n-tiles (B rows nbase*8 ...): A = the warp's 16 rows of H
+// (cols kH ...), B = the staged chunk; three passes (hi*hi, hi*lo, lo*hi) so
+// that consecutive products go to different accumulators
 template <int NT, int KS>
-__device__ __forceinline__ void fi_chunk(float (&acc)[32][4], const __nv_bfloat16* Hh, const __nv_bfloat16* Hl,
-                                         int kH, const __nv_bfloat16* Wh, const __nv_bfloat16* Wl, int gid, int tig) {
+__device__ __forceinline__ void fi_chunk(float (&acc)[16][4], const __nv_bfloat16* Hh, const __nv_bfloat16* Hl,
+                                         int kH, const __nv_bfloat16* Wh, const __nv_bfloat16* Wl, int nbase, int gid,
+                                         int tig) {
 #pragma unroll
   for (int ks = 0; ks < KS; ++ks) {
     uint32_t ah[4], al[4];
@@ -314,51 +321,68 @@ __device__ __forceinline__ void fi_chunk(float (&acc)[32][4], const __nv_bfloat1
     const int kb = ks * 16 + tig * 2;
 #pragma unroll
     for (int nt = 0; nt < NT; ++nt) {
-      const int n = nt * 8 + gid;
-      uint32_t bh[2], bl[2];
+      const int n = (nbase + nt) * 8 + gid;
+      uint32_t bh[2];
       bh[0] = *reinterpret_cast<const uint32_t*>(Wh + n * FI_WP + kb);
       bh[1] = *reinterpret_cast<const uint32_t*>(Wh + n * FI_WP + kb + 8);
+      mma_bf16(acc[nt], ah, bh);
+    }
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+      const int n = (nbase + nt) * 8 + gid;
+      uint32_t bl[2];
       bl[0] = *reinterpret_cast<const uint32_t*>(Wl + n * FI_WP + kb);
       bl[1] = *reinterpret_cast<const uint32_t*>(Wl + n * FI_WP + kb + 8);
-      mma_bf16(acc[nt], ah, bh);
       mma_bf16(acc[nt], ah, bl);
+    }
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+      const int n = (nbase + nt) * 8 + gid;
+      uint32_t bh[2];
+      bh[0] = *reinterpret_cast<const uint32_t*>(Wh + n * FI_WP + kb);
+      bh[1] = *reinterpret_cast<const uint32_t*>(Wh + n * FI_WP + kb + 8);
       mma_bf16(acc[nt], al, bh);
     }
   }
 }
 
-__global__ void __launch_bounds__(256, 1) k_mlp_infer(int n, int nin, int nout, const float* __restrict__ X,
-                                                      const float* __restrict__ P, int64_t ob1, int64_t ob2,
-                                                      int64_t ob3, int64_t ob4, const float* __restrict__ norm,
-                                                      const __nv_bfloat16* __restrict__ wb, float* __restrict__ Y) {
+// 16 warps: warp w owns query rows 16*(w/2) ... and output columns
+// 128*(w%2) ... of layers 1-3 (16 n-tiles), 16*(w%2) ... of layer 4 (2 n-tiles)
+constexpr int FI_THREADS = 512;
+__global__ void __launch_bounds__(FI_THREADS, 1) k_mlp_infer(int n, int nin, int nout, const float* __restrict__ X,
+                                                             const float* __restrict__ P, int64_t ob1, int64_t ob2,
+                                                             int64_t ob3, int64_t ob4, const float* __restrict__ norm,
+                                                             const __nv_bfloat16* __restrict__ wb,
+                                                             float* __restrict__ Y) {
   extern __shared__ __align__(16) unsigned char fi_smem[];
   __nv_bfloat16* H = reinterpret_cast<__nv_bfloat16*>(fi_smem);                // [2 hl][128][FI_HP]
   __nv_bfloat16* Wb = reinterpret_cast<__nv_bfloat16*>(fi_smem + FI_SMEM_H);   // [2 buf][2 hl][256][FI_WP]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int gid = lane >> 2, tig = lane & 3;
-  const int row0 = blockIdx.x * FI_M + warp * 16;  // this warp's first query
-  __nv_bfloat16* Hh = H + (size_t)(warp * 16) * FI_HP;
-  __nv_bfloat16* Hl = H + (size_t)(FI_M + warp * 16) * FI_HP;
+  const int rg = warp >> 1, ch = warp & 1;         // row group, column half
+  const int row0 = blockIdx.x * FI_M + rg * 16;    // the warp's first query
+  __nv_bfloat16* Hh = H + (size_t)(rg * 16) * FI_HP;
+  __nv_bfloat16* Hl = H + (size_t)(FI_M + rg * 16) * FI_HP;
   const float* xm = norm;
   const float* xs = norm + nin;
   const float* ym = norm + 2 * nin;
   const float* ys = norm + 2 * nin + nout;
   fi_stage(wb, Wb, 0);
   asm volatile("cp.async.commit_group;" ::: "memory");
-  // normalised inputs of the warp's 16 rows into H columns 0..15
-  for (int i = lane; i < 16 * FI_NIN; i += 32) {
-    const int r = i / FI_NIN, k = i % FI_NIN;
-    const int g = row0 + r;
-    float v = 0.f;
-    if (k < nin && g < n) v = (X[(int64_t)g * nin + k] - xm[k]) / xs[k];
-    const __nv_bfloat16 hi = __float2bfloat16_rn(v);
-    Hh[r * FI_HP + k] = hi;
-    Hl[r * FI_HP + k] = __float2bfloat16_rn(v - __bfloat162float(hi));
-  }
-  __syncwarp();
-  float acc[32][4];
+  // normalised inputs of the row group's 16 queries into H columns 0..15
+  if (ch == 0)
+    for (int i = lane; i < 16 * FI_NIN; i += 32) {
+      const int r = i / FI_NIN, k = i % FI_NIN;
+      const int g = row0 + r;
+      float v = 0.f;
+      if (k < nin && g < n) v = (X[(int64_t)g * nin + k] - xm[k]) / xs[k];
+      const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+      Hh[r * FI_HP + k] = hi;
+      Hl[r * FI_HP + k] = __float2bfloat16_rn(v - __bfloat162float(hi));
+    }
+  float acc[16][4];
 #pragma unroll
-  for (int nt = 0; nt < 32; ++nt)
+  for (int nt = 0; nt < 16; ++nt)
 #pragma unroll
     for (int q = 0; q < 4; ++q) acc[nt][q] = 0.f;
   for (int c = 0; c < FI_CHUNKS; ++c) {
@@ -369,22 +393,22 @@ __global__ void __launch_bounds__(256, 1) k_mlp_infer(int n, int nin, int nout, 
     } else {
       asm volatile("cp.async.wait_group 0;" ::: "memory");
     }
-    __syncthreads();
+    __syncthreads();  // chunk c staged; the previous layer's outputs (or the inputs) written
     const __nv_bfloat16* Wh = Wb + (size_t)(c & 1) * 2 * FI_H * FI_WP;
     const __nv_bfloat16* Wl = Wh + (size_t)FI_H * FI_WP;
     const int layer = c == 0 ? 1 : 2 + (c - 1) / (FI_H / FI_KC);
     const int kH = c == 0 ? 0 : ((c - 1) % (FI_H / FI_KC)) * FI_KC;
     const bool last = c == 0 || ((c - 1) % (FI_H / FI_KC)) == FI_H / FI_KC - 1;
-    if (layer == 1) fi_chunk<32, 1>(acc, Hh, Hl, kH, Wh, Wl, gid, tig);
-    else if (layer < 4) fi_chunk<32, 2>(acc, Hh, Hl, kH, Wh, Wl, gid, tig);
-    else fi_chunk<FI_NOUT / 8, 2>(acc, Hh, Hl, kH, Wh, Wl, gid, tig);
+    if (layer == 1) fi_chunk<16, 1>(acc, Hh, Hl, kH, Wh, Wl, 16 * ch, gid, tig);
+    else if (layer < 4) fi_chunk<16, 2>(acc, Hh, Hl, kH, Wh, Wl, 16 * ch, gid, tig);
+    else fi_chunk<FI_NOUT / 16, 2>(acc, Hh, Hl, kH, Wh, Wl, (FI_NOUT / 16) * ch, gid, tig);
     if (last && layer < 4) {
-      // bias + SiLU, split into hi/lo over this warp's own rows (all of their reads are done)
+      __syncthreads();  // both warps of a row group have read all of its input columns
+      // bias + SiLU, split into hi/lo
       const float* bias = P + (layer == 1 ? ob1 : layer == 2 ? ob2 : ob3);
-      __syncwarp();
 #pragma unroll
-      for (int nt = 0; nt < 32; ++nt) {
-        const int col = nt * 8 + tig * 2;
+      for (int nt = 0; nt < 16; ++nt) {
+        const int col = (16 * ch + nt) * 8 + tig * 2;
         const float b0 = bias[col], b1 = bias[col + 1];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
@@ -401,15 +425,14 @@ __global__ void __launch_bounds__(256, 1) k_mlp_infer(int n, int nin, int nout, 
           acc[nt][2 * h + 1] = 0.f;
         }
       }
-      __syncwarp();
     } else if (last) {
       // bias, de-normalisation, store
       const float* bias = P + ob4;
 #pragma unroll
-      for (int nt = 0; nt < FI_NOUT / 8; ++nt)
+      for (int nt = 0; nt < FI_NOUT / 16; ++nt)
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          const int col = nt * 8 + tig * 2 + (q & 1);
+          const int col = ((FI_NOUT / 16) * ch + nt) * 8 + tig * 2 + (q & 1);
           const int g = row0 + gid + ((q >= 2) ? 8 : 0);
           if (col < nout && g < n) {
             const float v = acc[nt][q] + bias[col];
@@ -605,8 +628,8 @@ bool Mlp::infer(int rows, const float* X_dev, float* Y_dev) {
   __nv_bfloat16* w = static_cast<__nv_bfloat16*>(wb);
   k_mlp_pack_infer<<<cdv(FI_WTOT, 256), 256, 0, s>>>(params, nin, nh, nout, o[0], o[2], o[4], o[6], w);
   if (rows > 0)
-    k_mlp_infer<<<cdv(rows, FI_M), 256, FI_SMEM, s>>>(rows, nin, nout, X_dev, params, o[1], o[3], o[5], o[7], norm,
-                                                     w, Y_dev);
+    k_mlp_infer<<<cdv(rows, FI_M), FI_THREADS, FI_SMEM, s>>>(rows, nin, nout, X_dev, params, o[1], o[3], o[5], o[7],
+                                                            norm, w, Y_dev);
   launches += rows > 0 ? 2 : 1;
   if (cudaGetLastError() != cudaSuccess) {
     err = "mlp: fused inference launch";
