@@ -33,9 +33,12 @@ struct GemmEpi {
 
 constexpr int GBM = 128, GBN = 64, GBK = 32, GPAD = 8;
 
-__device__ __forceinline__ float silu_f(float z) { return z / (1.0f + __expf(-z)); }
+// fast exponential and division (__expf, __fdividef: a few ulp; exp(-z) = inf
+// for z < -88 gives z * 0 = -0, the limit of SiLU) -- the activations are
+// BF16-split downstream, and the same functions serve training and inference
+__device__ __forceinline__ float silu_f(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
 __device__ __forceinline__ float dsilu_f(float z) {
-  const float s = 1.0f / (1.0f + __expf(-z));
+  const float s = __fdividef(1.0f, 1.0f + __expf(-z));
   return s * (1.0f + z * (1.0f - s));
 }
 
