@@ -275,6 +275,13 @@ __global__ void k_mlp_pack_infer(const float* __restrict__ P, int nin, int nh, i
   wb[t] = hl == 0 ? hi : __float2bfloat16_rn(v - __bfloat162float(hi));
 }
 
+// four 8x8 BF16 matrices from shared memory (lane l gives the address of row l%8 of matrix l/8)
+__device__ __forceinline__ void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(smem_u32_mlp(p)));
+}
+
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32_mlp(dst)), "l"(src) : "memory");
 }
@@ -304,11 +311,12 @@ __device__ __forceinline__ void fi_stage(const __nv_bfloat16* __restrict__ wb, _
 
 // one chunk of KS k16 steps for NT n-tiles (B rows nbase*8 ...): A = the warp's 16 rows of H
 // (cols kH ...), B = the staged chunk; three passes (hi*hi, hi*lo, lo*hi) so
-// that consecutive products go to different accumulators
+// that consecutive products go to different accumulators (NT even)
 template <int NT, int KS>
 __device__ __forceinline__ void fi_chunk(float (&acc)[16][4], const __nv_bfloat16* Hh, const __nv_bfloat16* Hl,
                                          int kH, const __nv_bfloat16* Wh, const __nv_bfloat16* Wl, int nbase, int gid,
                                          int tig) {
+  const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int ks = 0; ks < KS; ++ks) {
     uint32_t ah[4], al[4];
@@ -321,30 +329,31 @@ __device__ __forceinline__ void fi_chunk(float (&acc)[16][4], const __nv_bfloat1
     al[1] = *reinterpret_cast<const uint32_t*>(Hl + (gid + 8) * FI_HP + ka);
     al[2] = *reinterpret_cast<const uint32_t*>(Hl + gid * FI_HP + ka + 8);
     al[3] = *reinterpret_cast<const uint32_t*>(Hl + (gid + 8) * FI_HP + ka + 8);
-    const int kb = ks * 16 + tig * 2;
+    // B fragments of two n-tiles per ldmatrix.x4: matrices (nt, k 0-7), (nt, k 8-15),
+    // (nt+1, k 0-7), (nt+1, k 8-15); lane l addresses row l%8 of matrix l/8
+    const int lr = lane & 7, lm = lane >> 3;
+    const int koff = ks * 16 + (lm & 1) * 8;
+    const int nrow = (nbase + (lm >> 1)) * 8 + lr;
 #pragma unroll
-    for (int nt = 0; nt < NT; ++nt) {
-      const int n = (nbase + nt) * 8 + gid;
-      uint32_t bh[2];
-      bh[0] = *reinterpret_cast<const uint32_t*>(Wh + n * FI_WP + kb);
-      bh[1] = *reinterpret_cast<const uint32_t*>(Wh + n * FI_WP + kb + 8);
-      mma_bf16(acc[nt], ah, bh);
+    for (int nt = 0; nt < NT; nt += 2) {
+      uint32_t b0[2], b1[2];
+      ldsm_x4(b0[0], b0[1], b1[0], b1[1], Wh + (nrow + nt * 8) * FI_WP + koff);
+      mma_bf16(acc[nt], ah, b0);
+      mma_bf16(acc[nt + 1], ah, b1);
     }
 #pragma unroll
-    for (int nt = 0; nt < NT; ++nt) {
-      const int n = (nbase + nt) * 8 + gid;
-      uint32_t bl[2];
-      bl[0] = *reinterpret_cast<const uint32_t*>(Wl + n * FI_WP + kb);
-      bl[1] = *reinterpret_cast<const uint32_t*>(Wl + n * FI_WP + kb + 8);
-      mma_bf16(acc[nt], ah, bl);
+    for (int nt = 0; nt < NT; nt += 2) {
+      uint32_t b0[2], b1[2];
+      ldsm_x4(b0[0], b0[1], b1[0], b1[1], Wl + (nrow + nt * 8) * FI_WP + koff);
+      mma_bf16(acc[nt], ah, b0);
+      mma_bf16(acc[nt + 1], ah, b1);
     }
 #pragma unroll
-    for (int nt = 0; nt < NT; ++nt) {
-      const int n = (nbase + nt) * 8 + gid;
-      uint32_t bh[2];
-      bh[0] = *reinterpret_cast<const uint32_t*>(Wh + n * FI_WP + kb);
-      bh[1] = *reinterpret_cast<const uint32_t*>(Wh + n * FI_WP + kb + 8);
-      mma_bf16(acc[nt], al, bh);
+    for (int nt = 0; nt < NT; nt += 2) {
+      uint32_t b0[2], b1[2];
+      ldsm_x4(b0[0], b0[1], b1[0], b1[1], Wh + (nrow + nt * 8) * FI_WP + koff);
+      mma_bf16(acc[nt], al, b0);
+      mma_bf16(acc[nt + 1], al, b1);
     }
   }
 }
