@@ -319,16 +319,15 @@ __device__ __forceinline__ void fi_chunk(float (&acc)[16][4], const __nv_bfloat1
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int ks = 0; ks < KS; ++ks) {
+    // A fragments by ldmatrix.x4: matrices (rows 0-7, k 0-7), (rows 8-15, k 0-7),
+    // (rows 0-7, k 8-15), (rows 8-15, k 8-15) of the warp's 16 rows
     uint32_t ah[4], al[4];
-    const int ka = kH + ks * 16 + tig * 2;
-    ah[0] = *reinterpret_cast<const uint32_t*>(Hh + gid * FI_HP + ka);
-    ah[1] = *reinterpret_cast<const uint32_t*>(Hh + (gid + 8) * FI_HP + ka);
-    ah[2] = *reinterpret_cast<const uint32_t*>(Hh + gid * FI_HP + ka + 8);
-    ah[3] = *reinterpret_cast<const uint32_t*>(Hh + (gid + 8) * FI_HP + ka + 8);
-    al[0] = *reinterpret_cast<const uint32_t*>(Hl + gid * FI_HP + ka);
-    al[1] = *reinterpret_cast<const uint32_t*>(Hl + (gid + 8) * FI_HP + ka);
-    al[2] = *reinterpret_cast<const uint32_t*>(Hl + gid * FI_HP + ka + 8);
-    al[3] = *reinterpret_cast<const uint32_t*>(Hl + (gid + 8) * FI_HP + ka + 8);
+    {
+      const int arow = (lane & 7) + 8 * ((lane >> 3) & 1);
+      const int acol = kH + ks * 16 + 8 * (lane >> 4);
+      ldsm_x4(ah[0], ah[1], ah[2], ah[3], Hh + arow * FI_HP + acol);
+      ldsm_x4(al[0], al[1], al[2], al[3], Hl + arow * FI_HP + acol);
+    }
     // B fragments of two n-tiles per ldmatrix.x4: matrices (nt, k 0-7), (nt, k 8-15),
     // (nt+1, k 0-7), (nt+1, k 8-15); lane l addresses row l%8 of matrix l/8
     const int lr = lane & 7, lm = lane >> 3;
