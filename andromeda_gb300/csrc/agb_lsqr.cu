@@ -214,7 +214,8 @@ __global__ void __launch_bounds__(kThreads) k_atu(const T* __restrict__ A, int64
 // ---------------------------------------------------------------------------
 template <typename T> struct AV2;
 template <> struct AV2<float> { static constexpr int RR = 4, WARPS = 16, CH = 1024; };
-template <> struct AV2<double> { static constexpr int RR = 2, WARPS = 8, CH = 512; };
+template <> struct AV2<double> { static constexpr int RR = 1, WARPS = 8, CH = 512; };  // FP64-pipe bound: 8 rows per CTA
+                                                                                         // spread small systems over all SMs
 
 template <typename T>
 __global__ void __launch_bounds__(AV2<T>::WARPS * 32) k_av2(const T* __restrict__ A, int64_t lda, int m,
@@ -919,7 +920,7 @@ static void launch_atu(const DenseLsqr& L) {
   }
   constexpr int vn = Vec<T>::N;
   dim3 g(cdiv(L.lda, ATU_THREADS * vn), L.zgroups);
-  const int rpg = (int)((cdiv(L.m, L.zgroups) + 255) / 256 * 256);
+  const int rpg = (int)((cdiv(L.m, L.zgroups) + 31) / 32 * 32);
   k_atu2<T><<<g, ATU_THREADS, atu2_smem<T>(), L.stream>>>((const T*)L.A, L.lda, L.m, (const T*)L.Ys, rpg, L.Zp);
 }
 template <typename T>
@@ -997,7 +998,7 @@ bool DenseLsqr::setup(const void* A_dev, bool is_fp32, int m_, int n_, int64_t l
     per_sm = std::max(per_sm, 1);
   }
   const int slots = nsm * per_sm;
-  const int gmax = std::max(1, std::min((int)cdiv(m, use_tma ? 64 : 256), 64));
+  const int gmax = std::max(1, std::min((int)cdiv(m, use_tma ? 64 : 32), 64));
   int groups = 1;
   double best = -1.0;
   for (int G = 1; G <= gmax; ++G) {
