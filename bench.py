@@ -362,6 +362,19 @@ def run_large(args):
     workload = (f"superellipsoid a=1 b=0.5 c=0.25 e1=0.6 e2=1.4, {nr}x{ns} grid ({len(body['etype'])} tri) "
                 f"in an L2 container r=200, 6 RHS, ITRI 5")
     if args.large_mode == "resident":
+        # the packed FP32 single layer must fit in device memory (6 ne^2 x 4 B + ~2 %
+        # for the vectors); otherwise the matrix-free sweeps below
+        free_b = None
+        try:
+            import torch
+            free_b = torch.cuda.mem_get_info(0)[0]
+        except Exception:
+            pass
+        if free_b is not None and 24.0 * ne * ne * 1.02 > free_b:
+            print(f"# packed matrix ({24.0 * ne * ne / 1e9:.0f} GB) exceeds the free device memory "
+                  f"({free_b / 1e9:.0f} GB): matrix-free sweeps", file=sys.stderr)
+            args.large_mode = "mf"
+    if args.large_mode == "resident":
         with ClockSampler(0) as clk:
             t0 = time.perf_counter()
             C.kernel_times(reset=True)
