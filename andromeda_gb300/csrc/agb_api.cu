@@ -1773,7 +1773,7 @@ int agb_mlp_predict(agb_mlp* m, int n, const float* X, float* Y, int split, doub
             cudaMemcpyAsync(dX, X, (size_t)n * net.nin * sizeof(float), cudaMemcpyHostToDevice, net.s) == cudaSuccess;
   if (ok) {
     cudaEventRecord(e0, net.s);
-    if (split == 1) {  // fused split-BF16 inference: one kernel over all n queries
+    if (split == 1) {  // fused split-BF16 inference on tcgen05: one kernel over all n queries
       ok = net.infer(n, dX, dY);
     } else {           // layer-by-layer GEMMs (split 2: split-BF16, 0: plain BF16 products)
       for (int r0 = 0; r0 < n; r0 += chunk) {

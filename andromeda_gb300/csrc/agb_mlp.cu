@@ -1,6 +1,9 @@
 // MLP surrogate of the resistance tensor: 5 -> 256 -> 256 -> 256 -> 21 with
-// SiLU, FP32 master weights, BF16 tensor-core GEMMs (mma.sync m16n8k16, FP32
-// accumulation), hand-written forward, backward, Adam and inference.
+// SiLU, FP32 master weights, hand-written forward, backward, Adam and
+// inference.  Training runs on BF16 tensor-core GEMMs (mma.sync m16n8k16, FP32
+// accumulation; batches of 512 rows); inference of large query batches runs in
+// one fused kernel on the 5th-generation tensor cores (tcgen05, accumulators
+// in tensor memory; k_mlp_infer_tc below).
 //
 // Every layer product is one GEMM C[M][N] = sum_k A(m,k) B(n,k) whose operands
 // are read from FP32 global memory in either orientation (so the backward
@@ -9,8 +12,7 @@
 // by 8 warps (32 x 32 each).  The epilogue is fused: bias + SiLU (storing the
 // pre-activation for the backward pass), bias only, plain store, or the SiLU
 // derivative.  Optional split-BF16 mode (x = hi + lo, three products
-// hi*hi + hi*lo + lo*hi) gives FP32-level accuracy on the same tensor cores;
-// inference uses it.
+// hi*hi + hi*lo + lo*hi) gives FP32-level accuracy on the same tensor cores.
 #include "agb_mlp.cuh"
 
 #include <cuda_bf16.h>
@@ -231,227 +233,258 @@ static void gemm(bool split, int M, int N, int K, const float* A, int lda, const
 }
 
 // ---------------------------------------------------------------------------
-// Fused inference (split-BF16): one CTA runs 128 queries through all four
-// layers.  The activations stay in shared memory as BF16 hi/lo pairs
-// ([128][256+8] each); 16 warps: two warps share 16 query rows, each owning
-// half of a layer's output columns (16 n-tiles x 4 FP32 accumulators per
-// lane); a block barrier separates the last reads of a layer's input rows from
-// the writes of its outputs into the same rows.  The weights, pre-split into
-// BF16 hi/lo ([layer][hi/lo][N][K], k contiguous), stream
-// through two 40 KB shared-memory buffers in chunks of 32 k (cp.async, all
-// threads).  Input normalisation and output de-normalisation are fused.  The
-// accumulation order (k16 steps in order; hi*hi, hi*lo, lo*hi per step) and
-// the FP32 epilogues are those of k_mlp_gemm, so the outputs equal the
-// unfused forward's.
+// Fused inference on the 5th-generation tensor cores (tcgen05, split-BF16).
+// One CTA runs 128 queries (the tcgen05 M) through the four layers:
+//   * the activations live in shared memory as BF16 hi and lo halves in the
+//     no-swizzle K-major core-matrix layout (8 rows x 16 B per core matrix,
+//     [row/8][k/8][8][8]), 64 KB each;
+//   * the weights, pre-split and pre-packed in the same layout chunk by chunk
+//     (32 k per chunk; [layer chunk][hi/lo][n/8][k/8][8][8]), stream through a
+//     two-slot ring by one bulk copy per chunk (warp 8); a slot is released by
+//     tcgen05.commit of the products that read it;
+//   * one thread issues tcgen05.mma (M = 128, N = 256 or 32, K = 16; the three
+//     split products hi*hi, hi*lo, lo*hi per k step) into a 128 x 256 FP32
+//     accumulator in tensor memory;
+//   * 8 warps read the accumulator (tcgen05.ld, warp w: lanes 32 (w%4) ...,
+//     columns 128 (w/4) ...), add the bias, apply SiLU and write the next
+//     layer's hi/lo activations; layer 4 adds the bias, de-normalises, stores.
+// Every wait is bounded (error flag); the tensor memory is freed on every path.
 // ---------------------------------------------------------------------------
-constexpr int FI_M = 128, FI_H = 256, FI_HP = FI_H + 8, FI_KC = 32, FI_WP = FI_KC + 8;
-constexpr int FI_NIN = 16, FI_NOUT = 32;  // padded K of layer 1, padded N of layer 4
-constexpr size_t FI_SMEM_H = 2ull * FI_M * FI_HP * sizeof(__nv_bfloat16);         // 132 KB
-constexpr size_t FI_SMEM_W = 2ull * 2 * FI_H * FI_WP * sizeof(__nv_bfloat16);     // 80 KB
-constexpr size_t FI_SMEM = FI_SMEM_H + FI_SMEM_W;
-// packed weight offsets (elements): L1 [2][256][16], L2 [2][256][256], L3 [2][256][256], L4 [2][32][256]
-constexpr int64_t FI_O1 = 0, FI_O2 = FI_O1 + 2 * FI_H * FI_NIN, FI_O3 = FI_O2 + 2 * FI_H * FI_H,
-                  FI_O4 = FI_O3 + 2 * FI_H * FI_H, FI_WTOT = FI_O4 + 2 * FI_NOUT * FI_H;
-constexpr int FI_CHUNKS = 1 + 3 * (FI_H / FI_KC);  // layer 1: one chunk of 16 k; layers 2-4: 8 each
+constexpr int TC_M = 128, TC_H = 256, TC_NOUT = 32, TC_KC = 32;
+constexpr int TC_THREADS = 9 * 32;  // 8 epilogue warps (warp 0 lane 0 issues the products) + 1 copy warp
+constexpr size_t TC_H_BYTES = (size_t)TC_M * TC_H * 2;             // one half (hi or lo) of the activations
+constexpr size_t TC_SLOT = 2ull * TC_H * TC_KC * 2;                  // largest chunk: N 256 x K 32, hi + lo
+constexpr size_t TC_SMEM = 2 * TC_H_BYTES + 2 * TC_SLOT;             // 192 KB
+// packed weights (bytes): layer 1 one chunk (N 256, K 16), layers 2-3 eight chunks (N 256, K 32),
+// layer 4 eight chunks (N 32, K 32); hi then lo inside a chunk
+constexpr int64_t TC_C1 = 2ll * TC_H * 16 * 2, TC_C23 = 2ll * TC_H * TC_KC * 2, TC_C4 = 2ll * TC_NOUT * TC_KC * 2;
+constexpr int64_t TC_L2 = TC_C1, TC_L3 = TC_L2 + 8 * TC_C23, TC_L4 = TC_L3 + 8 * TC_C23, TC_WBYTES = TC_L4 + 8 * TC_C4;
+constexpr int TC_CHUNKS = 1 + 3 * 8;
 
-__global__ void k_mlp_pack_infer(const float* __restrict__ P, int nin, int nh, int nout, int64_t o0, int64_t o2,
-                                 int64_t o4, int64_t o6, __nv_bfloat16* __restrict__ wb) {
+__device__ __forceinline__ int64_t tc_chunk_off(int c) {
+  return c == 0 ? 0 : c <= 8 ? TC_L2 + (c - 1) * TC_C23 : c <= 16 ? TC_L3 + (c - 9) * TC_C23 : TC_L4 + (c - 17) * TC_C4;
+}
+__device__ __forceinline__ int64_t tc_chunk_bytes(int c) { return c == 0 ? TC_C1 : c <= 16 ? TC_C23 : TC_C4; }
+
+// one packed element per thread: (layer, hi/lo, n, k) -> chunk, core matrix, row, column
+__global__ void k_mlp_pack_tc(const float* __restrict__ P, int nin, int nh, int nout, int64_t o0, int64_t o2,
+                              int64_t o4, int64_t o6, __nv_bfloat16* __restrict__ wt) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= FI_WTOT) return;
-  int64_t r;
-  int K, N, k, n, hl;
-  const float* W;
-  int kin, nreal;
-  if (t < FI_O2) { r = t - FI_O1; K = FI_NIN; N = FI_H; W = P + o0; kin = nin; nreal = nh; }
-  else if (t < FI_O3) { r = t - FI_O2; K = FI_H; N = FI_H; W = P + o2; kin = nh; nreal = nh; }
-  else if (t < FI_O4) { r = t - FI_O3; K = FI_H; N = FI_H; W = P + o4; kin = nh; nreal = nh; }
-  else { r = t - FI_O4; K = FI_H; N = FI_NOUT; W = P + o6; kin = nh; nreal = nout; }
-  hl = (int)(r / ((int64_t)N * K));
-  const int64_t q = r % ((int64_t)N * K);
-  n = (int)(q / K);
-  k = (int)(q % K);
+  if (t >= TC_WBYTES / 2) return;
+  const int64_t b = 2 * t;  // byte offset of the element
+  int layer, c;
+  int64_t cb;
+  if (b < TC_L2) { layer = 1; c = 0; cb = b; }
+  else if (b < TC_L3) { layer = 2; c = (int)((b - TC_L2) / TC_C23); cb = (b - TC_L2) % TC_C23; }
+  else if (b < TC_L4) { layer = 3; c = (int)((b - TC_L3) / TC_C23); cb = (b - TC_L3) % TC_C23; }
+  else { layer = 4; c = (int)((b - TC_L4) / TC_C4); cb = (b - TC_L4) % TC_C4; }
+  const int N = layer == 4 ? TC_NOUT : TC_H, KC = layer == 1 ? 16 : TC_KC;
+  const int64_t half = (int64_t)N * KC * 2;
+  const int hl = (int)(cb / half);
+  const int64_t e = (cb % half) / 2;  // element within the half: [n/8][k/8][8][8]
+  const int core = (int)(e / 64), within = (int)(e % 64);
+  const int ng = core / (KC / 8), kc = core % (KC / 8);
+  const int n = ng * 8 + within / 8, k = c * KC + kc * 8 + within % 8;
+  const float* W = P + (layer == 1 ? o0 : layer == 2 ? o2 : layer == 3 ? o4 : o6);
+  const int kin = layer == 1 ? nin : nh, nreal = layer == 4 ? nout : nh;
   const float v = (n < nreal && k < kin) ? W[(int64_t)n * kin + k] : 0.f;
   const __nv_bfloat16 hi = __float2bfloat16_rn(v);
-  wb[t] = hl == 0 ? hi : __float2bfloat16_rn(v - __bfloat162float(hi));
+  wt[t] = hl == 0 ? hi : __float2bfloat16_rn(v - __bfloat162float(hi));
 }
 
-// four 8x8 BF16 matrices from shared memory (lane l gives the address of row l%8 of matrix l/8)
-__device__ __forceinline__ void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
-               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-               : "r"(smem_u32_mlp(p)));
+__device__ __forceinline__ uint64_t tc_sdesc(uint32_t addr, uint32_t sbo) {
+  // no-swizzle K-major: start >> 4, leading byte offset (next core matrix along K) 128 B,
+  // stride byte offset (next 8-row group) sbo, descriptor version 1 (bit 46)
+  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) |
+         ((uint64_t)1 << 46);
 }
-
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32_mlp(dst)), "l"(src) : "memory");
+__device__ __forceinline__ uint32_t tc_idesc(int n) {
+  // D F32 (bit 4), A and B BF16 (bits 7, 10), K-major, N >> 3 at bit 17, M >> 4 at bit 24
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
 }
-
-// stage chunk c of the packed weights into buffer `buf` ([2 hl][256][FI_WP])
-__device__ __forceinline__ void fi_stage(const __nv_bfloat16* __restrict__ wb, __nv_bfloat16* Ws, int c) {
-  int64_t base;
-  int N, K, k0, kw;
-  if (c == 0) { base = FI_O1; N = FI_H; K = FI_NIN; k0 = 0; kw = FI_NIN; }
-  else {
-    const int l = (c - 1) / (FI_H / FI_KC);  // 0: layer 2, 1: layer 3, 2: layer 4
-    base = l == 0 ? FI_O2 : l == 1 ? FI_O3 : FI_O4;
-    N = l == 2 ? FI_NOUT : FI_H;
-    K = FI_H;
-    k0 = ((c - 1) % (FI_H / FI_KC)) * FI_KC;
-    kw = FI_KC;
-  }
-  const int per_row = kw / 8;  // 16-byte pieces per row
-  const int total = 2 * N * per_row;
-  for (int i = threadIdx.x; i < total; i += blockDim.x) {
-    const int hl = i / (N * per_row);
-    const int rem = i % (N * per_row);
-    const int n = rem / per_row, pc = rem % per_row;
-    cp_async16(Ws + ((size_t)hl * FI_H + n) * FI_WP + pc * 8, wb + base + ((int64_t)hl * N + n) * K + k0 + pc * 8);
-  }
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+      "l"(da), "l"(db), "r"(idesc), "r"(acc)
+      : "memory");
 }
-
-// one chunk of KS k16 steps for NT n-tiles (B rows nbase*8 ...): A = the warp's 16 rows of H
-// (cols kH ...), B = the staged chunk; three passes (hi*hi, hi*lo, lo*hi) so
-// that consecutive products go to different accumulators (NT even)
-template <int NT, int KS>
-__device__ __forceinline__ void fi_chunk(float (&acc)[16][4], const __nv_bfloat16* Hh, const __nv_bfloat16* Hl,
-                                         int kH, const __nv_bfloat16* Wh, const __nv_bfloat16* Wl, int nbase, int gid,
-                                         int tig) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int ks = 0; ks < KS; ++ks) {
-    // A fragments by ldmatrix.x4: matrices (rows 0-7, k 0-7), (rows 8-15, k 0-7),
-    // (rows 0-7, k 8-15), (rows 8-15, k 8-15) of the warp's 16 rows
-    uint32_t ah[4], al[4];
-    {
-      const int arow = (lane & 7) + 8 * ((lane >> 3) & 1);
-      const int acol = kH + ks * 16 + 8 * (lane >> 4);
-      ldsm_x4(ah[0], ah[1], ah[2], ah[3], Hh + arow * FI_HP + acol);
-      ldsm_x4(al[0], al[1], al[2], al[3], Hl + arow * FI_HP + acol);
-    }
-    // B fragments of two n-tiles per ldmatrix.x4: matrices (nt, k 0-7), (nt, k 8-15),
-    // (nt+1, k 0-7), (nt+1, k 8-15); lane l addresses row l%8 of matrix l/8
-    const int lr = lane & 7, lm = lane >> 3;
-    const int koff = ks * 16 + (lm & 1) * 8;
-    const int nrow = (nbase + (lm >> 1)) * 8 + lr;
-#pragma unroll
-    for (int nt = 0; nt < NT; nt += 2) {
-      uint32_t b0[2], b1[2];
-      ldsm_x4(b0[0], b0[1], b1[0], b1[1], Wh + (nrow + nt * 8) * FI_WP + koff);
-      mma_bf16(acc[nt], ah, b0);
-      mma_bf16(acc[nt + 1], ah, b1);
-    }
-#pragma unroll
-    for (int nt = 0; nt < NT; nt += 2) {
-      uint32_t b0[2], b1[2];
-      ldsm_x4(b0[0], b0[1], b1[0], b1[1], Wl + (nrow + nt * 8) * FI_WP + koff);
-      mma_bf16(acc[nt], ah, b0);
-      mma_bf16(acc[nt + 1], ah, b1);
-    }
-#pragma unroll
-    for (int nt = 0; nt < NT; nt += 2) {
-      uint32_t b0[2], b1[2];
-      ldsm_x4(b0[0], b0[1], b1[0], b1[1], Wh + (nrow + nt * 8) * FI_WP + koff);
-      mma_bf16(acc[nt], al, b0);
-      mma_bf16(acc[nt + 1], al, b1);
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32_mlp(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, int* errflag) {
+  uint32_t ok = 0, tries = 0;
+  while (true) {
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(ok)
+                 : "r"(smem_u32_mlp(bar)), "r"(parity)
+                 : "memory");
+    if (ok) return true;
+    if ((++tries & 1023u) == 0 && *(volatile int*)errflag) return false;
+    if (tries > (1u << 22)) {
+      atomicExch(errflag, 1);
+      return false;
     }
   }
 }
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+// byte offset of (row, k) in a [row/8][k/8][8][8] BF16 half with 32 core matrices per 8-row group
+__device__ __forceinline__ uint32_t tc_hoff(int row, int k) {
+  return (uint32_t)(((row >> 3) * (TC_H / 8) + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
 
-// 16 warps: warp w owns query rows 16*(w/2) ... and output columns
-// 128*(w%2) ... of layers 1-3 (16 n-tiles), 16*(w%2) ... of layer 4 (2 n-tiles)
-constexpr int FI_THREADS = 512;
-__global__ void __launch_bounds__(FI_THREADS, 1) k_mlp_infer(int n, int nin, int nout, const float* __restrict__ X,
-                                                             const float* __restrict__ P, int64_t ob1, int64_t ob2,
-                                                             int64_t ob3, int64_t ob4, const float* __restrict__ norm,
-                                                             const __nv_bfloat16* __restrict__ wb,
-                                                             float* __restrict__ Y) {
-  extern __shared__ __align__(16) unsigned char fi_smem[];
-  __nv_bfloat16* H = reinterpret_cast<__nv_bfloat16*>(fi_smem);                // [2 hl][128][FI_HP]
-  __nv_bfloat16* Wb = reinterpret_cast<__nv_bfloat16*>(fi_smem + FI_SMEM_H);   // [2 buf][2 hl][256][FI_WP]
+__global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, int nout, const float* __restrict__ X,
+                                                                const float* __restrict__ P, int64_t ob1, int64_t ob2,
+                                                                int64_t ob3, int64_t ob4,
+                                                                const float* __restrict__ norm,
+                                                                const unsigned char* __restrict__ wt,
+                                                                float* __restrict__ Y, int* errflag) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  unsigned char* Hh = tc_smem;
+  unsigned char* Hl = tc_smem + TC_H_BYTES;
+  unsigned char* Wslot = tc_smem + 2 * TC_H_BYTES;
+  __shared__ __align__(8) uint64_t full[2], empty[2], accb;
+  __shared__ uint32_t tmem_base;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int gid = lane >> 2, tig = lane & 3;
-  const int rg = warp >> 1, ch = warp & 1;         // row group, column half
-  const int row0 = blockIdx.x * FI_M + rg * 16;    // the warp's first query
-  __nv_bfloat16* Hh = H + (size_t)(rg * 16) * FI_HP;
-  __nv_bfloat16* Hl = H + (size_t)(FI_M + rg * 16) * FI_HP;
+  const int q0 = blockIdx.x * TC_M;
   const float* xm = norm;
   const float* xs = norm + nin;
   const float* ym = norm + 2 * nin;
   const float* ys = norm + 2 * nin + nout;
-  fi_stage(wb, Wb, 0);
-  asm volatile("cp.async.commit_group;" ::: "memory");
-  // normalised inputs of the row group's 16 queries into H columns 0..15
-  if (ch == 0)
-    for (int i = lane; i < 16 * FI_NIN; i += 32) {
-      const int r = i / FI_NIN, k = i % FI_NIN;
-      const int g = row0 + r;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < 2; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32_mlp(&full[i])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32_mlp(&empty[i])) : "memory");
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32_mlp(&accb)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {  // 256 columns of tensor memory: the 128 x 256 FP32 accumulator
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32_mlp(&tmem_base))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (warp < 8) {  // normalised inputs into activation columns 0..15 (zeros beyond nin)
+    for (int i = threadIdx.x; i < TC_M * 16; i += 256) {
+      const int r = i >> 4, k = i & 15;
+      const int g = q0 + r;
       float v = 0.f;
       if (k < nin && g < n) v = (X[(int64_t)g * nin + k] - xm[k]) / xs[k];
       const __nv_bfloat16 hi = __float2bfloat16_rn(v);
-      Hh[r * FI_HP + k] = hi;
-      Hl[r * FI_HP + k] = __float2bfloat16_rn(v - __bfloat162float(hi));
+      *reinterpret_cast<__nv_bfloat16*>(Hh + tc_hoff(r, k)) = hi;
+      *reinterpret_cast<__nv_bfloat16*>(Hl + tc_hoff(r, k)) = __float2bfloat16_rn(v - __bfloat162float(hi));
     }
-  float acc[16][4];
-#pragma unroll
-  for (int nt = 0; nt < 16; ++nt)
-#pragma unroll
-    for (int q = 0; q < 4; ++q) acc[nt][q] = 0.f;
-  for (int c = 0; c < FI_CHUNKS; ++c) {
-    if (c + 1 < FI_CHUNKS) {
-      fi_stage(wb, Wb + (size_t)((c + 1) & 1) * 2 * FI_H * FI_WP, c + 1);
-      asm volatile("cp.async.commit_group;" ::: "memory");
-      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  if (warp == 8) {  // weight chunks: one bulk copy each into the two-slot ring
+    if (lane == 0) {
+      for (int c = 0; c < TC_CHUNKS; ++c) {
+        const int s = c & 1;
+        if (c >= 2 && !tc_wait(&empty[s], ((c >> 1) - 1) & 1, errflag)) break;
+        const uint32_t bytes = (uint32_t)tc_chunk_bytes(c);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32_mlp(&full[s])), "r"(bytes)
+                     : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32_mlp(Wslot + s * TC_SLOT)),
+                     "l"(wt + tc_chunk_off(c)), "r"(bytes), "r"(smem_u32_mlp(&full[s]))
+                     : "memory");
+      }
+    }
+    return;
+  }
+  // warps 0-7: products (warp 0, lane 0) and epilogues
+  bool ok = true;
+  const int lg = warp & 3, colh = warp >> 2;  // TMEM lane group, column half
+  const int row = lg * 32 + lane;
+  for (int layer = 1, c = 0; layer <= 4; ++layer) {
+    const int nchunks = layer == 1 ? 1 : 8;
+    const int N = layer == 4 ? TC_NOUT : TC_H;
+    if (warp == 0 && lane == 0) {
+      const uint32_t idesc = tc_idesc(N);
+      for (int j = 0; j < nchunks; ++j, ++c) {
+        const int s = c & 1;
+        if (!tc_wait(&full[s], (c >> 1) & 1, errflag)) { ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int KC = layer == 1 ? 16 : TC_KC;
+        const uint32_t bh = smem_u32_mlp(Wslot + s * TC_SLOT);
+        const uint32_t bl = bh + (uint32_t)N * KC * 2;
+        const uint32_t sbo_b = (uint32_t)(KC / 8) * 128;
+        for (int ks = 0; ks < KC / 16; ++ks) {
+          const int k0 = j * KC + ks * 16;  // activation column of this k step
+          const uint64_t ah = tc_sdesc(smem_u32_mlp(Hh) + (uint32_t)(k0 / 8) * 128, (TC_H / 8) * 128);
+          const uint64_t al = tc_sdesc(smem_u32_mlp(Hl) + (uint32_t)(k0 / 8) * 128, (TC_H / 8) * 128);
+          const uint64_t dbh = tc_sdesc(bh + ks * 256, sbo_b), dbl = tc_sdesc(bl + ks * 256, sbo_b);
+          tc_mma(tmem, ah, dbh, idesc, (j | ks) != 0);
+          tc_mma(tmem, ah, dbl, idesc, 1);
+          tc_mma(tmem, al, dbh, idesc, 1);
+        }
+        tc_commit(&empty[s]);  // the slot is free once these products are done
+      }
+      tc_commit(&accb);  // the layer's accumulator is complete
     } else {
-      asm volatile("cp.async.wait_group 0;" ::: "memory");
+      c += nchunks;
     }
-    __syncthreads();  // chunk c staged; the previous layer's outputs (or the inputs) written
-    const __nv_bfloat16* Wh = Wb + (size_t)(c & 1) * 2 * FI_H * FI_WP;
-    const __nv_bfloat16* Wl = Wh + (size_t)FI_H * FI_WP;
-    const int layer = c == 0 ? 1 : 2 + (c - 1) / (FI_H / FI_KC);
-    const int kH = c == 0 ? 0 : ((c - 1) % (FI_H / FI_KC)) * FI_KC;
-    const bool last = c == 0 || ((c - 1) % (FI_H / FI_KC)) == FI_H / FI_KC - 1;
-    if (layer == 1) fi_chunk<16, 1>(acc, Hh, Hl, kH, Wh, Wl, 16 * ch, gid, tig);
-    else if (layer < 4) fi_chunk<16, 2>(acc, Hh, Hl, kH, Wh, Wl, 16 * ch, gid, tig);
-    else fi_chunk<FI_NOUT / 16, 2>(acc, Hh, Hl, kH, Wh, Wl, (FI_NOUT / 16) * ch, gid, tig);
-    if (last && layer < 4) {
-      __syncthreads();  // both warps of a row group have read all of its input columns
-      // bias + SiLU, split into hi/lo
+    __syncwarp();
+    ok = tc_wait(&accb, (layer - 1) & 1, errflag) && ok;
+    __syncwarp();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tl = tmem + ((uint32_t)(lg * 32) << 16);
+    if (layer < 4) {
       const float* bias = P + (layer == 1 ? ob1 : layer == 2 ? ob2 : ob3);
-#pragma unroll
-      for (int nt = 0; nt < 16; ++nt) {
-        const int col = (16 * ch + nt) * 8 + tig * 2;
-        const float b0 = bias[col], b1 = bias[col + 1];
+      for (int c0 = colh * 128; c0 < colh * 128 + 128; c0 += 16) {
+        float v[16];
+        tc_ld16(tl + (uint32_t)c0, v);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-          const float v0 = silu_f(acc[nt][2 * h] + b0), v1 = silu_f(acc[nt][2 * h + 1] + b1);
-          const __nv_bfloat16 h0 = __float2bfloat16_rn(v0), h1 = __float2bfloat16_rn(v1);
-          __nv_bfloat162 hh, ll;
-          hh.x = h0; hh.y = h1;
-          ll.x = __float2bfloat16_rn(v0 - __bfloat162float(h0));
-          ll.y = __float2bfloat16_rn(v1 - __bfloat162float(h1));
-          const int r = gid + 8 * h;
-          *reinterpret_cast<__nv_bfloat162*>(Hh + r * FI_HP + col) = hh;
-          *reinterpret_cast<__nv_bfloat162*>(Hl + r * FI_HP + col) = ll;
-          acc[nt][2 * h] = 0.f;
-          acc[nt][2 * h + 1] = 0.f;
+          __align__(16) __nv_bfloat16 hv[8], lv[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const float z = silu_f(v[h * 8 + j] + bias[c0 + h * 8 + j]);
+            hv[j] = __float2bfloat16_rn(z);
+            lv[j] = __float2bfloat16_rn(z - __bfloat162float(hv[j]));
+          }
+          const uint32_t off = tc_hoff(row, c0 + h * 8);
+          *reinterpret_cast<uint4*>(Hh + off) = *reinterpret_cast<const uint4*>(hv);
+          *reinterpret_cast<uint4*>(Hl + off) = *reinterpret_cast<const uint4*>(lv);
         }
       }
-    } else if (last) {
-      // bias, de-normalisation, store
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // activations -> tensor-core reads
+    } else if (colh == 0) {
       const float* bias = P + ob4;
+      const int g = q0 + row;
+      for (int c0 = 0; c0 < TC_NOUT; c0 += 16) {
+        float v[16];
+        tc_ld16(tl + (uint32_t)c0, v);
 #pragma unroll
-      for (int nt = 0; nt < FI_NOUT / 16; ++nt)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int col = ((FI_NOUT / 16) * ch + nt) * 8 + tig * 2 + (q & 1);
-          const int g = row0 + gid + ((q >= 2) ? 8 : 0);
-          if (col < nout && g < n) {
-            const float v = acc[nt][q] + bias[col];
-            Y[(int64_t)g * nout + col] = v * ys[col] + ym[col];
-          }
+        for (int j = 0; j < 16; ++j) {
+          const int col = c0 + j;
+          if (col < nout && g < n) Y[(int64_t)g * nout + col] = (v[j] + bias[col]) * ys[col] + ym[col];
         }
+      }
     }
-    __syncthreads();  // the buffer of chunk c is refilled by the stage of chunk c + 2
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    asm volatile("bar.sync 1, 256;" ::: "memory");  // warps 0-7: the next layer reads all rows
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
+  (void)ok;
+  if (warp == 0) {
+    __syncwarp();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem) : "memory");
   }
 }
 
@@ -463,10 +496,12 @@ Mlp::~Mlp() { release(); }
 void Mlp::release() {
   cudaFree(params); cudaFree(grads); cudaFree(adam_m); cudaFree(adam_v); cudaFree(norm); cudaFree(ws);
   cudaFree(part);
-  cudaFree(wb);
+  cudaFree(wt);
+  cudaFree(tc_err);
   params = grads = adam_m = adam_v = norm = ws = nullptr;
   part = nullptr;
-  wb = nullptr;
+  wt = nullptr;
+  tc_err = nullptr;
   ws_rows = 0;
 }
 
@@ -621,29 +656,42 @@ void Mlp::output(int rows, float* Y_dev) {
 }
 
 bool Mlp::infer(int rows, const float* X_dev, float* Y_dev) {
-  if (nh != FI_H || nin > FI_NIN || nout > FI_NOUT || nin < 1 || nout < 1) {
-    err = "fused inference needs nh = 256, nin <= 16, nout <= 32";
+  if (nh != TC_H || nin > 16 || nout > TC_NOUT || nin < 1 || nout < 1) {
+    err = "tcgen05 inference needs nh = 256, nin <= 16, nout <= 32";
     return false;
   }
-  if (!wb && cudaMalloc(&wb, FI_WTOT * sizeof(__nv_bfloat16)) != cudaSuccess) {
-    wb = nullptr;
+  if (!wt && cudaMalloc(&wt, TC_WBYTES) != cudaSuccess) {
+    wt = nullptr;
     err = "mlp: inference weights";
     return false;
   }
-  if (cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FI_SMEM) != cudaSuccess) {
-    err = "mlp: fused inference shared memory";
+  if (!tc_err && cudaMalloc(&tc_err, sizeof(int)) != cudaSuccess) {
+    tc_err = nullptr;
+    err = "mlp: inference flag";
+    return false;
+  }
+  if (cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM) != cudaSuccess) {
+    err = "mlp: tcgen05 inference shared memory";
     return false;
   }
   int64_t o[8];
   offsets(o);
-  __nv_bfloat16* w = static_cast<__nv_bfloat16*>(wb);
-  k_mlp_pack_infer<<<cdv(FI_WTOT, 256), 256, 0, s>>>(params, nin, nh, nout, o[0], o[2], o[4], o[6], w);
+  cudaMemsetAsync(tc_err, 0, sizeof(int), s);
+  k_mlp_pack_tc<<<cdv(TC_WBYTES / 2, 256), 256, 0, s>>>(params, nin, nh, nout, o[0], o[2], o[4], o[6],
+                                                        static_cast<__nv_bfloat16*>(wt));
   if (rows > 0)
-    k_mlp_infer<<<cdv(rows, FI_M), FI_THREADS, FI_SMEM, s>>>(rows, nin, nout, X_dev, params, o[1], o[3], o[5], o[7],
-                                                            norm, w, Y_dev);
+    k_mlp_infer_tc<<<cdv(rows, TC_M), TC_THREADS, TC_SMEM, s>>>(rows, nin, nout, X_dev, params, o[1], o[3], o[5], o[7],
+                                                               norm, static_cast<const unsigned char*>(wt), Y_dev,
+                                                               tc_err);
   launches += rows > 0 ? 2 : 1;
-  if (cudaGetLastError() != cudaSuccess) {
-    err = "mlp: fused inference launch";
+  int h = 0;
+  if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(&h, tc_err, sizeof(int), cudaMemcpyDeviceToHost, s) !=
+                                               cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
+    err = "mlp: tcgen05 inference launch";
+    return false;
+  }
+  if (h) {
+    err = "mlp: a bounded barrier wait in the tcgen05 inference gave up";
     return false;
   }
   return true;

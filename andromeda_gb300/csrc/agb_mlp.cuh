@@ -16,7 +16,9 @@ struct Mlp {
   float* norm = nullptr;    // x_mean[nin], x_std[nin], y_mean[nout], y_std[nout]
   float* ws = nullptr;      // activations of ws_rows rows
   double* part = nullptr;   // loss partial sums
-  void* wb = nullptr;       // BF16 hi/lo weights of the fused inference kernel (nh = 256, nin <= 16, nout <= 32)
+  void* wt = nullptr;       // BF16 hi/lo weights packed for the tcgen05 inference kernel (nh = 256, nin <= 16,
+                            // nout <= 32)
+  int* tc_err = nullptr;    // bounded-wait flag of the tcgen05 inference kernel
   int ws_rows = 0;
   int step = 0;
   long launches = 0;
@@ -33,7 +35,7 @@ struct Mlp {
   void backward(int rows, const float* T_dev, bool split);  // gradients into grads, loss partials into part
   void adam(float lr);
   void output(int rows, float* Y_dev);              // de-normalised outputs of the last forward
-  bool infer(int rows, const float* X_dev, float* Y_dev);  // fused split-BF16 inference (one kernel)
+  bool infer(int rows, const float* X_dev, float* Y_dev);  // fused split-BF16 inference on tcgen05 (one kernel)
   double loss_sum(int rows);                        // sum of squared normalised errors of the last backward
 };
 

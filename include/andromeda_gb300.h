@@ -287,7 +287,8 @@ int agb_solve_lu(agb_context* ctx, int nrhs, const double* u, double* x, int* in
  * agb_mlp_train: epochs over n rows in shuffled mini-batches (full batches
  * only), loss_hist[epoch] = mean squared normalised error; stats[3]: device ms,
  * kernel launches, Adam steps so far.  agb_mlp_predict: split 1 = split-BF16
- * products in one fused kernel (128 queries per CTA, activations kept on chip;
+ * products in one fused kernel on the 5th-generation tensor cores (128
+ * queries per CTA, accumulators in tensor memory, activations kept on chip;
  * needs nhidden = 256, nin <= 16, nout <= 32), split 2 = split-BF16 through
  * the layer-by-layer GEMMs of the training forward (same results), split 0 =
  * plain BF16 products; device_ms = kernel time of the n inferences. */
