@@ -356,12 +356,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
   unsigned char* Wslot = tc_smem + 2 * TC_H_BYTES;
   __shared__ __align__(8) uint64_t full[2], empty[2], accb;
   __shared__ uint32_t tmem_base;
+  __shared__ float sbias[3][TC_H], sout[3][TC_NOUT];  // biases of layers 1-3; layer-4 bias, y_std, y_mean
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int q0 = blockIdx.x * TC_M;
   const float* xm = norm;
   const float* xs = norm + nin;
-  const float* ym = norm + 2 * nin;
-  const float* ys = norm + 2 * nin + nout;
   if (threadIdx.x == 0) {
     for (int i = 0; i < 2; ++i) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32_mlp(&full[i])) : "memory");
@@ -374,6 +373,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32_mlp(&tmem_base))
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (warp < 8) {  // biases and output scales into shared memory
+    for (int i = threadIdx.x; i < 3 * TC_H; i += 256)
+      sbias[i / TC_H][i % TC_H] = P[(i < TC_H ? ob1 : i < 2 * TC_H ? ob2 : ob3) + i % TC_H];
+    if (threadIdx.x < TC_NOUT) {
+      const int j = threadIdx.x;
+      sout[0][j] = j < nout ? P[ob4 + j] : 0.f;
+      sout[1][j] = j < nout ? norm[2 * nin + nout + j] : 0.f;
+      sout[2][j] = j < nout ? norm[2 * nin + j] : 0.f;
+    }
   }
   if (warp < 8) {  // normalised inputs into activation columns 0..15 (zeros beyond nin)
     for (int i = threadIdx.x; i < TC_M * 16; i += 256) {
@@ -445,7 +454,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tl = tmem + ((uint32_t)(lg * 32) << 16);
     if (layer < 4) {
-      const float* bias = P + (layer == 1 ? ob1 : layer == 2 ? ob2 : ob3);
+      const float* bias = sbias[layer - 1];
       for (int c0 = colh * 128; c0 < colh * 128 + 128; c0 += 16) {
         float v[16];
         tc_ld16(tl + (uint32_t)c0, v);
@@ -465,7 +474,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // activations -> tensor-core reads
     } else if (colh == 0) {
-      const float* bias = P + ob4;
+      const float* bias = sout[0];
       const int g = q0 + row;
       for (int c0 = 0; c0 < TC_NOUT; c0 += 16) {
         float v[16];
@@ -473,7 +482,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int col = c0 + j;
-          if (col < nout && g < n) Y[(int64_t)g * nout + col] = (v[j] + bias[col]) * ys[col] + ym[col];
+          if (col < nout && g < n) Y[(int64_t)g * nout + col] = (v[j] + bias[col]) * sout[1][col] + sout[2][col];
         }
       }
     }
