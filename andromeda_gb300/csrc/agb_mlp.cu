@@ -251,7 +251,7 @@ static void gemm(bool split, int M, int N, int K, const float* A, int lda, const
 // Every wait is bounded (error flag); the tensor memory is freed on every path.
 // ---------------------------------------------------------------------------
 constexpr int TC_M = 128, TC_H = 256, TC_NOUT = 32, TC_KC = 32;
-constexpr int TC_THREADS = 9 * 32;  // 8 epilogue warps (warp 0 lane 0 issues the products) + 1 copy warp
+constexpr int TC_THREADS = 10 * 32;  // 8 epilogue warps, 1 copy warp, 1 issuing warp
 constexpr size_t TC_H_BYTES = (size_t)TC_M * TC_H * 2;             // one half (hi or lo) of the activations
 constexpr size_t TC_SLOT = 2ull * TC_H * TC_KC * 2;                  // largest chunk: N 256 x K 32, hi + lo
 constexpr size_t TC_SMEM = 2 * TC_H_BYTES + 2 * TC_SLOT;             // 192 KB
@@ -354,7 +354,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
   unsigned char* Hh = tc_smem;
   unsigned char* Hl = tc_smem + TC_H_BYTES;
   unsigned char* Wslot = tc_smem + 2 * TC_H_BYTES;
-  __shared__ __align__(8) uint64_t full[2], empty[2], accb;
+  // full/empty: the weight ring; accb[b]: accumulator b complete; hready[j]: the 32
+  // activation columns of chunk j written by the epilogue (4 warps arrive)
+  __shared__ __align__(8) uint64_t full[2], empty[2], accb[2], hready[TC_H / TC_KC];
   __shared__ uint32_t tmem_base;
   __shared__ float sbias[3][TC_H], sout[3][TC_NOUT];  // biases of layers 1-3; layer-4 bias, y_std, y_mean
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -365,12 +367,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
     for (int i = 0; i < 2; ++i) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32_mlp(&full[i])) : "memory");
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32_mlp(&empty[i])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32_mlp(&accb[i])) : "memory");
     }
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32_mlp(&accb)) : "memory");
+    for (int i = 0; i < TC_H / TC_KC; ++i)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(smem_u32_mlp(&hready[i])) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) {  // 256 columns of tensor memory: the 128 x 256 FP32 accumulator
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32_mlp(&tmem_base))
+  if (warp == 0) {  // all 512 columns of tensor memory: two 128 x 256 FP32 accumulators
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32_mlp(&tmem_base))
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -383,8 +387,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
       sout[1][j] = j < nout ? norm[2 * nin + nout + j] : 0.f;
       sout[2][j] = j < nout ? norm[2 * nin + j] : 0.f;
     }
-  }
-  if (warp < 8) {  // normalised inputs into activation columns 0..15 (zeros beyond nin)
+    // normalised inputs into activation columns 0..15 (zeros beyond nin)
     for (int i = threadIdx.x; i < TC_M * 16; i += 256) {
       const int r = i >> 4, k = i & 15;
       const int g = q0 + r;
@@ -414,86 +417,92 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
                      : "memory");
       }
     }
-    return;
-  }
-  // warps 0-7: products (warp 0, lane 0) and epilogues
-  bool ok = true;
-  const int lg = warp & 3, colh = warp >> 2;  // TMEM lane group, column half
-  const int row = lg * 32 + lane;
-  for (int layer = 1, c = 0; layer <= 4; ++layer) {
-    const int nchunks = layer == 1 ? 1 : 8;
-    const int N = layer == 4 ? TC_NOUT : TC_H;
-    if (warp == 0 && lane == 0) {
-      const uint32_t idesc = tc_idesc(N);
-      for (int j = 0; j < nchunks; ++j, ++c) {
-        const int s = c & 1;
-        if (!tc_wait(&full[s], (c >> 1) & 1, errflag)) { ok = false; break; }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const int KC = layer == 1 ? 16 : TC_KC;
-        const uint32_t bh = smem_u32_mlp(Wslot + s * TC_SLOT);
-        const uint32_t bl = bh + (uint32_t)N * KC * 2;
-        const uint32_t sbo_b = (uint32_t)(KC / 8) * 128;
-        for (int ks = 0; ks < KC / 16; ++ks) {
-          const int k0 = j * KC + ks * 16;  // activation column of this k step
-          const uint64_t ah = tc_sdesc(smem_u32_mlp(Hh) + (uint32_t)(k0 / 8) * 128, (TC_H / 8) * 128);
-          const uint64_t al = tc_sdesc(smem_u32_mlp(Hl) + (uint32_t)(k0 / 8) * 128, (TC_H / 8) * 128);
-          const uint64_t dbh = tc_sdesc(bh + ks * 256, sbo_b), dbl = tc_sdesc(bl + ks * 256, sbo_b);
-          tc_mma(tmem, ah, dbh, idesc, (j | ks) != 0);
-          tc_mma(tmem, ah, dbl, idesc, 1);
-          tc_mma(tmem, al, dbh, idesc, 1);
-        }
-        tc_commit(&empty[s]);  // the slot is free once these products are done
-      }
-      tc_commit(&accb);  // the layer's accumulator is complete
-    } else {
-      c += nchunks;
-    }
-    __syncwarp();
-    ok = tc_wait(&accb, (layer - 1) & 1, errflag) && ok;
-    __syncwarp();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const uint32_t tl = tmem + ((uint32_t)(lg * 32) << 16);
-    if (layer < 4) {
-      const float* bias = sbias[layer - 1];
-      for (int c0 = colh * 128; c0 < colh * 128 + 128; c0 += 16) {
-        float v[16];
-        tc_ld16(tl + (uint32_t)c0, v);
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          __align__(16) __nv_bfloat16 hv[8], lv[8];
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const float z = silu_f(v[h * 8 + j] + bias[c0 + h * 8 + j]);
-            hv[j] = __float2bfloat16_rn(z);
-            lv[j] = __float2bfloat16_rn(z - __bfloat162float(hv[j]));
+  } else if (warp == 9) {  // products: layer l accumulates into buffer (l-1)&1; chunk j of a layer
+                           // waits for the activation columns of chunk j from the previous epilogue
+    if (lane == 0) {
+      bool ok = true;
+      for (int layer = 1, c = 0; layer <= 4 && ok; ++layer) {
+        const int nchunks = layer == 1 ? 1 : 8;
+        const int N = layer == 4 ? TC_NOUT : TC_H, KC = layer == 1 ? 16 : TC_KC;
+        const uint32_t idesc = tc_idesc(N);
+        const uint32_t tacc = tmem + (uint32_t)(((layer - 1) & 1) * TC_H);
+        for (int j = 0; j < nchunks; ++j, ++c) {
+          const int s = c & 1;
+          if (layer > 1 && !tc_wait(&hready[j], (layer - 2) & 1, errflag)) { ok = false; break; }
+          if (!tc_wait(&full[s], (c >> 1) & 1, errflag)) { ok = false; break; }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t bh = smem_u32_mlp(Wslot + s * TC_SLOT);
+          const uint32_t bl = bh + (uint32_t)N * KC * 2;
+          const uint32_t sbo_b = (uint32_t)(KC / 8) * 128;
+          for (int ks = 0; ks < KC / 16; ++ks) {
+            const int k0 = j * KC + ks * 16;  // activation column of this k step
+            const uint64_t ah = tc_sdesc(smem_u32_mlp(Hh) + (uint32_t)(k0 / 8) * 128, (TC_H / 8) * 128);
+            const uint64_t al = tc_sdesc(smem_u32_mlp(Hl) + (uint32_t)(k0 / 8) * 128, (TC_H / 8) * 128);
+            const uint64_t dbh = tc_sdesc(bh + ks * 256, sbo_b), dbl = tc_sdesc(bl + ks * 256, sbo_b);
+            tc_mma(tacc, ah, dbh, idesc, (j | ks) != 0);
+            tc_mma(tacc, ah, dbl, idesc, 1);
+            tc_mma(tacc, al, dbh, idesc, 1);
           }
-          const uint32_t off = tc_hoff(row, c0 + h * 8);
-          *reinterpret_cast<uint4*>(Hh + off) = *reinterpret_cast<const uint4*>(hv);
-          *reinterpret_cast<uint4*>(Hl + off) = *reinterpret_cast<const uint4*>(lv);
+          tc_commit(&empty[s]);  // the slot is free once these products are done
         }
+        tc_commit(&accb[(layer - 1) & 1]);  // also on a failed wait, so the epilogue warps never wait for nothing
       }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // activations -> tensor-core reads
-    } else if (colh == 0) {
-      const float* bias = sout[0];
-      const int g = q0 + row;
-      for (int c0 = 0; c0 < TC_NOUT; c0 += 16) {
-        float v[16];
-        tc_ld16(tl + (uint32_t)c0, v);
+    }
+  } else {  // warps 0-7: epilogues; warp w reads TMEM lanes 32 (w%4) ... and columns 128 (w/4) ...
+    const int lg = warp & 3, colh = warp >> 2;
+    const int row = lg * 32 + lane;
+    for (int layer = 1; layer <= 4; ++layer) {
+      const int b = (layer - 1) & 1;
+      if (!tc_wait(&accb[b], ((layer - 1) >> 1) & 1, errflag)) break;
+      __syncwarp();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t tl = tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)(b * TC_H);
+      if (layer < 4) {
+        const float* bias = sbias[layer - 1];
+        for (int jc = colh * 4; jc < colh * 4 + 4; ++jc) {  // activation chunks of 32 columns, in order
+          for (int c0 = jc * TC_KC; c0 < jc * TC_KC + TC_KC; c0 += 16) {
+            float v[16];
+            tc_ld16(tl + (uint32_t)c0, v);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int col = c0 + j;
-          if (col < nout && g < n) Y[(int64_t)g * nout + col] = (v[j] + bias[col]) * sout[1][col] + sout[2][col];
+            for (int h = 0; h < 2; ++h) {
+              __align__(16) __nv_bfloat16 hv[8], lv[8];
+#pragma unroll
+              for (int j = 0; j < 8; ++j) {
+                const float z = silu_f(v[h * 8 + j] + bias[c0 + h * 8 + j]);
+                hv[j] = __float2bfloat16_rn(z);
+                lv[j] = __float2bfloat16_rn(z - __bfloat162float(hv[j]));
+              }
+              const uint32_t off = tc_hoff(row, c0 + h * 8);
+              *reinterpret_cast<uint4*>(Hh + off) = *reinterpret_cast<const uint4*>(hv);
+              *reinterpret_cast<uint4*>(Hl + off) = *reinterpret_cast<const uint4*>(lv);
+            }
+          }
+          // chunk jc is written by this warp's 32 rows: publish it to the next layer's products
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncwarp();
+          if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32_mlp(&hready[jc])) : "memory");
+        }
+      } else if (colh == 0) {
+        const float* bias = sout[0];
+        const int g = q0 + row;
+        for (int c0 = 0; c0 < TC_NOUT; c0 += 16) {
+          float v[16];
+          tc_ld16(tl + (uint32_t)c0, v);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int col = c0 + j;
+            if (col < nout && g < n) Y[(int64_t)g * nout + col] = (v[j] + bias[col]) * sout[1][col] + sout[2][col];
+          }
         }
       }
     }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    asm volatile("bar.sync 1, 256;" ::: "memory");  // warps 0-7: the next layer reads all rows
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   }
-  (void)ok;
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();  // every product and every tensor-memory read is done
   if (warp == 0) {
-    __syncwarp();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem) : "memory");
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
   }
 }
 
