@@ -251,7 +251,8 @@ static void gemm(bool split, int M, int N, int K, const float* A, int lda, const
 // Every wait is bounded (error flag); the tensor memory is freed on every path.
 // ---------------------------------------------------------------------------
 constexpr int TC_M = 128, TC_H = 256, TC_NOUT = 32, TC_KC = 32;
-constexpr int TC_THREADS = 10 * 32;  // 8 epilogue warps, 1 copy warp, 1 issuing warp
+constexpr int TC_EPI = 16;                    // epilogue warps: 4 per TMEM lane group, 64 columns each
+constexpr int TC_THREADS = (TC_EPI + 2) * 32;  // + 1 copy warp + 1 issuing warp
 constexpr size_t TC_H_BYTES = (size_t)TC_M * TC_H * 2;             // one half (hi or lo) of the activations
 constexpr size_t TC_SLOT = 2ull * TC_H * TC_KC * 2;                  // largest chunk: N 256 x K 32, hi + lo
 constexpr size_t TC_SMEM = 2 * TC_H_BYTES + 2 * TC_SLOT;             // 192 KB
@@ -378,8 +379,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
-  if (warp < 8) {  // biases and output scales into shared memory
-    for (int i = threadIdx.x; i < 3 * TC_H; i += 256)
+  if (warp < TC_EPI) {  // biases and output scales into shared memory
+    for (int i = threadIdx.x; i < 3 * TC_H; i += TC_EPI * 32)
       sbias[i / TC_H][i % TC_H] = P[(i < TC_H ? ob1 : i < 2 * TC_H ? ob2 : ob3) + i % TC_H];
     if (threadIdx.x < TC_NOUT) {
       const int j = threadIdx.x;
@@ -388,7 +389,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
       sout[2][j] = j < nout ? norm[2 * nin + j] : 0.f;
     }
     // normalised inputs into activation columns 0..15 (zeros beyond nin)
-    for (int i = threadIdx.x; i < TC_M * 16; i += 256) {
+    for (int i = threadIdx.x; i < TC_M * 16; i += TC_EPI * 32) {
       const int r = i >> 4, k = i & 15;
       const int g = q0 + r;
       float v = 0.f;
@@ -403,7 +404,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
-  if (warp == 8) {  // weight chunks: one bulk copy each into the two-slot ring
+  if (warp == TC_EPI) {  // weight chunks: one bulk copy each into the two-slot ring
     if (lane == 0) {
       for (int c = 0; c < TC_CHUNKS; ++c) {
         const int s = c & 1;
@@ -417,7 +418,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
                      : "memory");
       }
     }
-  } else if (warp == 9) {  // products: layer l accumulates into buffer (l-1)&1; chunk j of a layer
+  } else if (warp == TC_EPI + 1) {  // products: layer l accumulates into buffer (l-1)&1; chunk j of a layer
                            // waits for the activation columns of chunk j from the previous epilogue
     if (lane == 0) {
       bool ok = true;
@@ -448,8 +449,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
         tc_commit(&accb[(layer - 1) & 1]);  // also on a failed wait, so the epilogue warps never wait for nothing
       }
     }
-  } else {  // warps 0-7: epilogues; warp w reads TMEM lanes 32 (w%4) ... and columns 128 (w/4) ...
-    const int lg = warp & 3, colh = warp >> 2;
+  } else {  // epilogue warps: warp w reads TMEM lanes 32 (w%4) ... and columns 64 (w/4) ...
+    const int lg = warp & 3, colq = warp >> 2;
     const int row = lg * 32 + lane;
     for (int layer = 1; layer <= 4; ++layer) {
       const int b = (layer - 1) & 1;
@@ -459,7 +460,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
       const uint32_t tl = tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)(b * TC_H);
       if (layer < 4) {
         const float* bias = sbias[layer - 1];
-        for (int jc = colh * 4; jc < colh * 4 + 4; ++jc) {  // activation chunks of 32 columns, in order
+        for (int jc = colq * 2; jc < colq * 2 + 2; ++jc) {  // activation chunks of 32 columns, in order
           for (int c0 = jc * TC_KC; c0 < jc * TC_KC + TC_KC; c0 += 16) {
             float v[16];
             tc_ld16(tl + (uint32_t)c0, v);
@@ -483,7 +484,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
           __syncwarp();
           if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32_mlp(&hready[jc])) : "memory");
         }
-      } else if (colh == 0) {
+      } else if (colq == 0) {
         const float* bias = sout[0];
         const int g = q0 + row;
         for (int c0 = 0; c0 < TC_NOUT; c0 += 16) {
