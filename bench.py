@@ -567,8 +567,8 @@ def run_surrogate(args):
             "roofline": {"bound": "tensor", "achieved": flops / (ms * 1e-3) / 1e12, "peak": bf16, "unit": "TFLOP/s",
                          "frac": (flops / (ms * 1e-3) / 1e12 / bf16) if bf16 else None, "traffic": None,
                          "peak_source": "measured bf16 (cuBLAS burst)" if bf16 else None,
-                         "kernel": "k_mlp_infer (all four layers in one kernel, 128 queries per CTA, "
-                                   "activations on chip; mma.sync m16n8k16 bf16)",
+                         "kernel": "k_mlp_infer_tc (all four layers in one kernel, 128 queries per CTA, "
+                                   "activations on chip; tcgen05.mma bf16, FP32 accumulators in TMEM)",
                          "note": "split-BF16: the three products per GEMM are counted"},
             "cpu_baseline": None, "clocks": clk.summary(), "gpu_launches": int(sur.net._L.agb_mlp_launches(sur.net.h)),
             "e2e": {"value": args.queries / (t4 - t3), "unit": "inferences/s (predict with hull check, host arrays)",
