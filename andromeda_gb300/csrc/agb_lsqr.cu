@@ -700,6 +700,7 @@ __global__ void __launch_bounds__(SCAL_THREADS) k_scalars(LsqrScalars* sc, int k
     }
   }
   const int c = threadIdx.x;
+  if (phase == 3 && c == 0) *nactive = 0;  // the active count of this iteration is rebuilt by phase 4
   if (c >= K8) return;
   lsqr_phase(sc[c], c, k, phase, sred[c], nactive);
 }
@@ -1153,23 +1154,24 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
     pev_ready = true;
   }
   int it_in_graph = 0;
+  // the two sweeps of the first iteration of every replay are timed live (event
+  // records in the graph); the other iterations carry no event nodes
   auto iteration = [&]() {
-    const int e = 4 * it_in_graph++;
-    cudaEventRecordWithFlags(pev[e], stream, cudaEventRecordExternal);
+    const bool timed = it_in_graph++ == 0;
+    if (timed) cudaEventRecordWithFlags(pev[0], stream, cudaEventRecordExternal);
     if (fp32) launch_av2<float>(*this);
     else launch_av2<double>(*this);
-    cudaEventRecordWithFlags(pev[e + 1], stream, cudaEventRecordExternal);
+    if (timed) cudaEventRecordWithFlags(pev[1], stream, cudaEventRecordExternal);
     k_scalars<<<1, SCAL_THREADS, 0, stream>>>(sc, k, 2, part, nb_av2, nactive);
-    cudaEventRecordWithFlags(pev[e + 2], stream, cudaEventRecordExternal);
+    if (timed) cudaEventRecordWithFlags(pev[2], stream, cudaEventRecordExternal);
     if (fp32) launch_atu<float>(*this); else launch_atu<double>(*this);
-    cudaEventRecordWithFlags(pev[e + 3], stream, cudaEventRecordExternal);
+    if (timed) cudaEventRecordWithFlags(pev[3], stream, cudaEventRecordExternal);
     k_atu_reduce<<<nb_red, kThreads, 0, stream>>>(Zp, zgroups, lda, n, sc, 0, V, part, qs);
     k_scalars<<<1, SCAL_THREADS, 0, stream>>>(sc, k, 3, part, nb_red, nactive);
     if (fp32) k_update<float><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 0, V, W, X, (float*)Vs, part, 1, Vp, pk_ne,
                                                                 pk_ldp, qs);
     else k_update<double><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 0, V, W, X, (double*)Vs, part, 1);
-    cudaMemsetAsync(nactive, 0, sizeof(int), stream);
-    k_scalars<<<1, SCAL_THREADS, 0, stream>>>(sc, k, 4, part, nb_upd, nactive);
+    k_scalars<<<1, SCAL_THREADS, 0, stream>>>(sc, k, 4, part, nb_upd, nactive);  // phase 3 zeroed nactive
   };
   // capture check_every iterations in one graph
   cudaGraph_t graph = nullptr;
@@ -1190,10 +1192,10 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
     launches += 7L * check_every;
     CK(cudaMemcpyAsync(h_nactive, nactive, sizeof(int), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
-    for (int i = 0; i < check_every; ++i) {
+    {
       float a = 0.f, b = 0.f;
-      if (cudaEventElapsedTime(&a, pev[4 * i], pev[4 * i + 1]) == cudaSuccess) { t_av += a; ++n_av; }
-      if (cudaEventElapsedTime(&b, pev[4 * i + 2], pev[4 * i + 3]) == cudaSuccess) { t_atu += b; ++n_atu; }
+      if (cudaEventElapsedTime(&a, pev[0], pev[1]) == cudaSuccess) { t_av += a; ++n_av; }
+      if (cudaEventElapsedTime(&b, pev[2], pev[3]) == cudaSuccess) { t_atu += b; ++n_atu; }
     }
     (void)cudaGetLastError();  // a timing query must not leak into the error checks
     iters += check_every;
