@@ -1,0 +1,106 @@
+"""Convert the reference's own test meshes into compact fixtures (run once, here).
+
+The reference ships gmsh meshes with its run cases; two of them are the inputs of
+the cases on this path:
+  * run/mesh/sphere-01.msh (gmsh 2.2): the Laplace case run/laplace/sphere
+    (wall "krogla", sphere of radius 0.5, 420 nodes, 836 triangles);
+  * run/mesh/sphere-in-sphere-1024-1843-3678-tri.msh (gmsh 4.1): the Stokes case
+    run/stokes/flow-over-sphere (walls "particle" and "outside").
+The node coordinates, the triangles (node order as in the file: the reference takes
+the element normal from nodes 1-3) and the physical wall ids are written to
+tests/golden/<name>.npz.  Run from the repository root:
+    python tests/golden/make_fixture_meshes.py /root/reference
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _sections(path):
+    out, name, body = {}, None, []
+    with open(path) as f:
+        for line in f:
+            line = line.strip()
+            if line.startswith("$End"):
+                out[name] = body
+                name, body = None, []
+            elif line.startswith("$"):
+                name, body = line[1:], []
+            elif name is not None:
+                body.append(line)
+    return out
+
+
+def read_msh(path):
+    """Triangles of a gmsh 2.2 or 4.1 ASCII mesh: (xyz, tris (0-based), physical id per triangle)."""
+    s = _sections(path)
+    version = s["MeshFormat"][0].split()[0]
+    if version.startswith("2"):
+        nodes = s["Nodes"]
+        n = int(nodes[0])
+        ids, xyz = [], []
+        for line in nodes[1:1 + n]:
+            p = line.split()
+            ids.append(int(p[0]))
+            xyz.append([float(v) for v in p[1:4]])
+        index = {t: i for i, t in enumerate(ids)}
+        tris, phys = [], []
+        els = s["Elements"]
+        for line in els[1:1 + int(els[0])]:
+            p = [int(v) for v in line.split()]
+            if p[1] != 2:
+                continue
+            ntags = p[2]
+            tris.append([index[t] for t in p[3 + ntags:6 + ntags]])
+            phys.append(p[3])
+        return np.array(xyz), np.array(tris, np.int32), np.array(phys, np.int32)
+    # gmsh 4.1: physical group of every surface entity from $Entities
+    ent = s["Entities"]
+    npts, ncur, nsur, _ = (int(v) for v in ent[0].split())
+    surf_phys = {}
+    for line in ent[1 + npts + ncur:1 + npts + ncur + nsur]:
+        p = line.split()
+        tag, nph = int(p[0]), int(p[7])
+        surf_phys[tag] = int(p[8]) if nph > 0 else 0
+    nodes = s["Nodes"]
+    nblocks = int(nodes[0].split()[0])
+    i = 1
+    ids, xyz = [], []
+    for _ in range(nblocks):
+        nb = int(nodes[i].split()[3])
+        tags = [int(v) for v in nodes[i + 1:i + 1 + nb]]
+        coords = [[float(v) for v in line.split()[:3]] for line in nodes[i + 1 + nb:i + 1 + 2 * nb]]
+        ids += tags
+        xyz += coords
+        i += 1 + 2 * nb
+    index = {t: k for k, t in enumerate(ids)}
+    els = s["Elements"]
+    nblocks = int(els[0].split()[0])
+    i = 1
+    tris, phys = [], []
+    for _ in range(nblocks):
+        dim, etag, etype, nb = (int(v) for v in els[i].split())
+        for line in els[i + 1:i + 1 + nb]:
+            if etype == 2 and dim == 2:
+                p = [int(v) for v in line.split()]
+                tris.append([index[t] for t in p[1:4]])
+                phys.append(surf_phys[etag])
+        i += 1 + nb
+    return np.array(xyz), np.array(tris, np.int32), np.array(phys, np.int32)
+
+
+def main(ref):
+    cases = {"sphere_01": "run/mesh/sphere-01.msh",
+             "sphere_in_sphere_3678": "run/mesh/sphere-in-sphere-1024-1843-3678-tri.msh"}
+    for name, rel in cases.items():
+        xyz, tris, phys = read_msh(os.path.join(ref, rel))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), xyz=xyz, tris=tris, phys=phys,
+                            source=np.array(rel))
+        print(name, xyz.shape, tris.shape, np.unique(phys, return_counts=True))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,96 @@
+"""Cases on the reference's own meshes (run/mesh/sphere-01.msh of run/laplace/sphere,
+run/mesh/sphere-in-sphere-1024-1843-3678-tri.msh of run/stokes/flow-over-sphere),
+converted once into tests/golden/*.npz with the node order of the files (the element
+normal comes from nodes 1-3, as in the reference).
+
+CPU (oracle): the Laplace case as the reference runs it (ITRI 5, u = 1 on the sphere:
+the flux vanishes) and u = x + 2y + 3z, whose flux n.(1,2,3) is exact on the
+polyhedral surface, so only quadrature and solver errors remain.
+GPU: the same cases through the C ABI against the oracle (1e-9), and the
+flow-over-sphere mesh through the resistance workflow: the mixed tensor within 1e-5
+of the FP64 one (this container is 1024 particle radii across: the FP32 matrix's
+rounding shows at a few 1e-6), symmetric, and the drag and torque within the
+discretisation error of the analytic concentric-sphere values (particle a = 0.5,
+container b = 512).
+"""
+import numpy as np
+import pytest
+
+from fixtures import reference_mesh
+
+
+def _laplace_oracle(orc, m, u):
+    P = orc.Problem(1, m, walls=[1], known=[[1]], itri=5)
+    errs = P.form_integrals()
+    n, _, _ = P.geometry()
+    _, q, nit, ierr = P.laplace_solve(u, np.zeros(P.nelem), maxit=0, eps=1e-12)
+    P.close()
+    return q, n, errs, ierr
+
+
+def test_fixture_meshes_shapes():
+    s = reference_mesh("sphere_01")
+    assert s["xyz"].shape == (420, 3) and len(s["etype"]) == 836 and set(s["bcid"]) == {1}
+    assert np.allclose(np.linalg.norm(s["xyz"], axis=1), 0.5)
+    f = reference_mesh("sphere_in_sphere_3678")
+    assert f["xyz"].shape == (1843, 3) and len(f["etype"]) == 3678
+    assert (f["bcid"] == 1).sum() == 3202 and (f["bcid"] == 2).sum() == 476
+
+
+def test_laplace_sphere01_reference_case(orc):
+    """run/laplace/sphere: u = 1 on the whole sphere -> q = 0."""
+    m = reference_mesh("sphere_01")
+    q, n, errs, ierr = _laplace_oracle(orc, m, np.ones(len(m["xyz"])))
+    assert ierr == 0 and errs[0] < 1e-12
+    assert np.max(np.abs(q)) < 1e-9
+
+
+def test_laplace_sphere01_linear_field(orc):
+    m = reference_mesh("sphere_01")
+    u = m["xyz"] @ np.array([1.0, 2.0, 3.0])
+    q, n, errs, ierr = _laplace_oracle(orc, m, u)
+    qex = -(n @ np.array([1.0, 2.0, 3.0]))
+    assert ierr == 0
+    assert np.linalg.norm(q - qex) / np.linalg.norm(qex) < 1e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("field", ["one", "linear"])
+def test_gpu_laplace_sphere01_vs_oracle(agb, orc, field):
+    m = reference_mesh("sphere_01")
+    u = np.ones(len(m["xyz"])) if field == "one" else m["xyz"] @ np.array([1.0, 2.0, 3.0])
+    q_ref, _, _, _ = _laplace_oracle(orc, m, u)
+    C = agb.Context(0)
+    C.set_mesh(m)
+    C.set_problem(agb.LAPLACE, [1], agb.dirichlet_known(agb.LAPLACE, 1), itri=5)
+    C.assemble(agb.FP64)
+    x, nit, istop = C.solve(u[None], eps=1e-12)
+    C.close()
+    scale = max(np.max(np.abs(q_ref)), 1.0)
+    assert istop[0] <= 3
+    assert np.max(np.abs(x[0] - q_ref)) < 1e-9 * scale
+
+
+@pytest.mark.gpu
+def test_gpu_flow_over_sphere_reference_mesh(agb):
+    m = reference_mesh("sphere_in_sphere_3678")
+    C = agb.Context(0)
+    C.set_mesh(m)
+    C.set_problem(agb.STOKES, [1, 2], agb.dirichlet_known(agb.STOKES, 2), itri=5)
+    R64, _, info64 = C.resistance_tensor(agb.FP64, 1, 2, eps=1e-11)
+    R32, _, info32 = C.resistance_tensor(agb.MIXED, 1, 2, eps=1e-8)
+    C.close()
+    # 1/2: converged; 4: the reference's condition limit (conlim 1e8), a legitimate stop of lsqr_solve
+    assert np.all(np.isin(info64["istop"], (1, 2, 4))) and np.all(np.isin(info32["istop"], (1, 2, 4)))
+    scale = np.max(np.abs(R64))
+    # the container is 1024 particle radii across (the benchmark's 200): the FP32
+    # matrix's rounding reaches the rotation couplings at a few 1e-6 here
+    print("mixed vs FP64", np.max(np.abs(R32 - R64)) / scale, "asymmetry", np.max(np.abs(R64 - R64.T)) / scale,
+          "drag", np.diag(R64)[:3] / (6 * np.pi * 0.5), "torque", np.diag(R64)[3:] / (np.pi))
+    assert np.max(np.abs(R32 - R64)) < 1e-5 * scale
+    assert np.max(np.abs(R64 - R64.T)) < 1e-4 * scale
+    lam = 0.5 / 512.0
+    drag = 6 * np.pi * 0.5 * (1 - lam ** 5) / (1 - 9 * lam / 4 + 5 * lam ** 3 / 2 - 9 * lam ** 5 / 4 + lam ** 6)
+    torque = 8 * np.pi * 0.5 ** 3 / (1 - lam ** 3)
+    assert np.allclose(np.diag(R64)[:3] / drag, 1.0, atol=5e-3)
+    assert np.allclose(np.diag(R64)[3:] / torque, 1.0, atol=1e-2)
