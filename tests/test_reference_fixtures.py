@@ -1,5 +1,6 @@
 """Cases on the reference's own meshes (run/mesh/sphere-01.msh of run/laplace/sphere,
-run/mesh/sphere-in-sphere-1024-1843-3678-tri.msh of run/stokes/flow-over-sphere),
+run/mesh/sphere-in-sphere-1024-1843-3678-tri.msh of run/stokes/flow-over-sphere,
+run/mesh/ellipsoid211-in-sphere-1024-1041-2117.msh of run/stokes/flow-over-ellipsoid),
 converted once into tests/golden/*.npz with the node order of the files (the element
 normal comes from nodes 1-3, as in the reference).
 
@@ -11,7 +12,11 @@ flow-over-sphere mesh through the resistance workflow: the mixed tensor within 1
 of the FP64 one (this container is 1024 particle radii across: the FP32 matrix's
 rounding shows at a few 1e-6), symmetric, and the drag and torque within the
 discretisation error of the analytic concentric-sphere values (particle a = 0.5,
-container b = 512).
+container b = 512); the flow-over-ellipsoid mesh: the drag along and across the
+spheroid's axis against the reference's own analytic resistances
+(CalResTensorPrime, lib_particle.f90:1906-1927, with the semi-minor axis of
+calForceOnEllipsoid, lib_particle.f90:1979-1996) within 1.5 % (discretisation and
+the container, 645 semi-minor axes away).
 """
 import numpy as np
 import pytest
@@ -94,3 +99,40 @@ def test_gpu_flow_over_sphere_reference_mesh(agb):
     torque = 8 * np.pi * 0.5 ** 3 / (1 - lam ** 3)
     assert np.allclose(np.diag(R64)[:3] / drag, 1.0, atol=5e-3)
     assert np.allclose(np.diag(R64)[3:] / torque, 1.0, atol=1e-2)
+
+
+def _spheroid_resistance(lam):
+    """Translational resistances of a prolate spheroid of aspect ratio lam, in units of
+    pi mu b U (b = semi-minor axis): (along the axis, across it) -- the closed forms
+    the reference evaluates in CalResTensorPrime (Oberbeck's solution)."""
+    l2 = lam * lam - 1.0
+    s = np.sqrt(l2)
+    lg = np.log(lam + s)
+    along = 8.0 * l2 ** 1.5 / ((2.0 * l2 + 1.0) * lg - lam * s)
+    across = 16.0 * l2 ** 1.5 / ((2.0 * l2 - 1.0) * lg + lam * s)
+    return along, across
+
+
+def test_spheroid_resistance_limits():
+    along, across = _spheroid_resistance(1.0 + 1e-6)
+    assert abs(along - 6.0) < 1e-4 and abs(across - 6.0) < 1e-4  # the sphere: 6 pi mu a U
+    along, across = _spheroid_resistance(2.0)
+    assert 6.0 < along < across
+
+
+@pytest.mark.gpu
+def test_gpu_flow_over_ellipsoid_reference_mesh(agb):
+    m = reference_mesh("ellipsoid211_in_sphere_2117")
+    C = agb.Context(0)
+    C.set_mesh(m)
+    C.set_problem(agb.STOKES, [1, 2], agb.dirichlet_known(agb.STOKES, 2), itri=5)
+    R64, _, info64 = C.resistance_tensor(agb.FP64, 1, 2, eps=1e-11)
+    R32, _, _ = C.resistance_tensor(agb.MIXED, 1, 2, eps=1e-8)
+    C.close()
+    scale = np.max(np.abs(R64))
+    assert np.max(np.abs(R32 - R64)) < 1e-5 * scale
+    b = (3.0 * (np.pi / 6.0) / (4.0 * np.pi * 2.0)) ** (1.0 / 3.0)  # volume of the sphere of radius 0.5
+    along, across = _spheroid_resistance(2.0)
+    ratio = np.diag(R64)[:3] / (np.array([along, across, across]) * b * np.pi)  # axis along x
+    print("spheroid drag / analytic", ratio)
+    assert np.allclose(ratio, 1.0, atol=1.5e-2)
