@@ -1,6 +1,6 @@
 """Convert the reference's own test meshes into compact fixtures (run once, here).
 
-The reference ships gmsh meshes with its run cases; three of them are the inputs of
+The reference ships gmsh meshes with its run cases; four of them are the inputs of
 the cases on this path:
   * run/mesh/sphere-01.msh (gmsh 2.2): the Laplace case run/laplace/sphere
     (wall "krogla", sphere of radius 0.5, 420 nodes, 836 triangles);
@@ -8,7 +8,10 @@ the cases on this path:
     run/stokes/flow-over-sphere (walls "particle" and "outside");
   * run/mesh/ellipsoid211-in-sphere-1024-1041-2117.msh (gmsh 4.1): the Stokes case
     run/stokes/flow-over-ellipsoid (a 2:1:1 spheroid of the volume of a sphere of
-    radius 0.5 in the same container).
+    radius 0.5 in the same container);
+  * run/mesh/kocka-000-111-314-624_tri.msh (gmsh 4.1): the unit cube of the Stokes
+    cases run/stokes/Couette and Poiseuille (walls top, bottom, back, front, left,
+    right).
 The node coordinates, the triangles (node order as in the file: the reference takes
 the element normal from nodes 1-3) and the physical wall ids are written to
 tests/golden/<name>.npz.  Run from the repository root:
@@ -98,7 +101,8 @@ def read_msh(path):
 def main(ref):
     cases = {"sphere_01": "run/mesh/sphere-01.msh",
              "sphere_in_sphere_3678": "run/mesh/sphere-in-sphere-1024-1843-3678-tri.msh",
-             "ellipsoid211_in_sphere_2117": "run/mesh/ellipsoid211-in-sphere-1024-1041-2117.msh"}
+             "ellipsoid211_in_sphere_2117": "run/mesh/ellipsoid211-in-sphere-1024-1041-2117.msh",
+             "cube_624": "run/mesh/kocka-000-111-314-624_tri.msh"}
     for name, rel in cases.items():
         xyz, tris, phys = read_msh(os.path.join(ref, rel))
         np.savez_compressed(os.path.join(HERE, name + ".npz"), xyz=xyz, tris=tris, phys=phys,

@@ -1,6 +1,7 @@
 """Cases on the reference's own meshes (run/mesh/sphere-01.msh of run/laplace/sphere,
 run/mesh/sphere-in-sphere-1024-1843-3678-tri.msh of run/stokes/flow-over-sphere,
-run/mesh/ellipsoid211-in-sphere-1024-1041-2117.msh of run/stokes/flow-over-ellipsoid),
+run/mesh/ellipsoid211-in-sphere-1024-1041-2117.msh of run/stokes/flow-over-ellipsoid,
+run/mesh/kocka-000-111-314-624_tri.msh of run/stokes/Couette),
 converted once into tests/golden/*.npz with the node order of the files (the element
 normal comes from nodes 1-3, as in the reference).
 
@@ -16,7 +17,8 @@ container b = 512); the flow-over-ellipsoid mesh: the drag along and across the
 spheroid's axis against the reference's own analytic resistances
 (CalResTensorPrime, lib_particle.f90:1906-1927, with the semi-minor axis of
 calForceOnEllipsoid, lib_particle.f90:1979-1996) within 1.5 % (discretisation and
-the container, 645 semi-minor axes away).
+the container, 645 semi-minor axes away); the Couette case on the cube (velocity on
+all six walls): the piecewise-constant traction of u = (z, 0, 0), oracle and GPU.
 """
 import numpy as np
 import pytest
@@ -136,3 +138,78 @@ def test_gpu_flow_over_ellipsoid_reference_mesh(agb):
     ratio = np.diag(R64)[:3] / (np.array([along, across, across]) * b * np.pi)  # axis along x
     print("spheroid drag / analytic", ratio)
     assert np.allclose(ratio, 1.0, atol=1.5e-2)
+
+
+def _couette_checks(q, m):
+    """Couette flow u = (z, 0, 0) in the reference's unit cube (mu = 1): traction
+    q = -(sigma . n) with n the mesh normal (out of the fluid): q_x = -1 on top, +1 on
+    bottom, q_z = +1 on left, -1 on right, the other tangential components 0, and the
+    normal component the same constant (the pressure level, free in an all-Dirichlet
+    problem) on every face.  Returns the largest deviation."""
+    x = m["xyz"]
+    t = m["con"][:, :3]
+    nrm = np.cross(x[t[:, 1]] - x[t[:, 0]], x[t[:, 2]] - x[t[:, 0]])
+    nrm /= np.linalg.norm(nrm, axis=1)[:, None]
+    want = {1: (0, -1.0), 2: (0, 1.0), 5: (2, 1.0), 6: (2, -1.0), 3: None, 4: None}  # wall: (component, value)
+    qn = np.sum(q.T * nrm, axis=1)
+    dev = np.max(np.abs(qn - np.mean(qn)))
+    for wall, w in want.items():
+        sel = m["bcid"] == wall
+        normal = int(np.argmax(np.abs(nrm[sel].mean(0))))
+        for comp in range(3):
+            if comp == normal:
+                continue
+            target = w[1] if (w is not None and comp == w[0]) else 0.0
+            dev = max(dev, np.max(np.abs(q[comp, sel] - target)))
+    return dev
+
+
+def _couette_fields(m):
+    U = np.zeros((1, 3, len(m["xyz"])))
+    U[0, 0] = m["xyz"][:, 2]
+    return U
+
+
+def test_couette_reference_cube(orc):
+    """run/stokes/Couette on run/mesh/kocka-000-111-314-624_tri.msh (velocity given on
+    all six walls)."""
+    m = reference_mesh("cube_624")
+    P = orc.Problem(2, m, walls=[1, 2, 3, 4, 5, 6], known=np.ones((3, 6)), itri=5)
+    P.form_integrals()
+    q, _, nits, ierr = P.stokes_solve_sequence(_couette_fields(m), maxit=0, eps=1e-13, fwall=1)
+    P.close()
+    assert _couette_checks(q[0], m) < 2e-3
+
+
+@pytest.mark.gpu
+def test_gpu_couette_reference_cube(agb, orc):
+    m = reference_mesh("cube_624")
+    U = _couette_fields(m)
+    P = orc.Problem(2, m, walls=[1, 2, 3, 4, 5, 6], known=np.ones((3, 6)), itri=5)
+    P.form_integrals()
+    q_ref, _, _, _ = P.stokes_solve_sequence(U, maxit=0, eps=1e-13, fwall=1)
+    P.close()
+    C = agb.Context(0)
+    C.set_mesh(m)
+    C.set_problem(agb.STOKES, [1, 2, 3, 4, 5, 6], agb.dirichlet_known(agb.STOKES, 6), itri=5)
+    C.assemble(agb.FP64)
+    x, nit, istop = C.solve(U, eps=1e-13)
+    C.close()
+    # the solution comes in the subdomain's element order: wall by wall in the order
+    # of the wall list (SetUpSubdomains), mesh order within a wall
+    order = np.concatenate([np.where(m["bcid"] == w)[0] for w in (1, 2, 3, 4, 5, 6)])
+    q = np.zeros((3, len(order)))
+    q[:, order] = x[0].reshape(3, -1)
+    assert _couette_checks(q, m) < 2e-3
+    # the pressure level (a constant normal traction) is the null direction of the
+    # all-Dirichlet system, where both LSQR runs stop on the condition limit at
+    # different levels: compare the solutions with it removed
+    x_ = m["xyz"]
+    t = m["con"][:, :3]
+    nrm = np.cross(x_[t[:, 1]] - x_[t[:, 0]], x_[t[:, 2]] - x_[t[:, 0]])
+    nrm /= np.linalg.norm(nrm, axis=1)[:, None]
+
+    def without_pressure(qq):
+        return qq - np.mean(np.sum(qq.T * nrm, axis=1)) * nrm.T
+
+    assert np.max(np.abs(without_pressure(q) - without_pressure(q_ref[0]))) < 1e-5
