@@ -213,3 +213,42 @@ def test_gpu_couette_reference_cube(agb, orc):
         return qq - np.mean(np.sum(qq.T * nrm, axis=1)) * nrm.T
 
     assert np.max(np.abs(without_pressure(q) - without_pressure(q_ref[0]))) < 1e-5
+
+
+@pytest.mark.gpu
+def test_gpu_couette_flux_bc_reference_cube(agb):
+    """run/stokes/Couette with stokesCouette-X-fluxBC.bic: the x traction given on the
+    four side walls (0 on front and back, -3 on left, +3 on right: pressure 3), the
+    velocity elsewhere.  Mixed boundary conditions through the general path: the side
+    walls' x velocity comes out as z, the tractions as in the Dirichlet case with the
+    normal component equal to the pressure."""
+    m = reference_mesh("cube_624")
+    walls = [1, 2, 3, 4, 5, 6]  # top, bottom, back, front, left, right
+    known = np.ones((3, 6), np.int32)
+    known[0, 2:] = 2  # x traction known on back, front, left, right
+    nn, ne = len(m["xyz"]), len(m["etype"])
+    U = _couette_fields(m)
+    Q = np.zeros((1, 3, ne))
+    Q[0, 0, m["bcid"] == 5] = -3.0
+    Q[0, 0, m["bcid"] == 6] = 3.0
+    C = agb.Context(0)
+    C.set_mesh(m)
+    C.set_problem(agb.STOKES, walls, known, itri=5)
+    C.assemble(agb.FP64)
+    uo, qo, nit, istop = C.solve_fields(U, Q, eps=1e-13)
+    C.close()
+    assert istop[0] <= 4
+    assert np.max(np.abs(uo[0, 0] - m["xyz"][:, 2])) < 2e-3 and np.max(np.abs(uo[0, 1:])) < 2e-3
+    x = m["xyz"]
+    t = m["con"][:, :3]
+    nrm = np.cross(x[t[:, 1]] - x[t[:, 0]], x[t[:, 2]] - x[t[:, 0]])
+    nrm /= np.linalg.norm(nrm, axis=1)[:, None]
+    q = qo[0]
+    assert np.max(np.abs(np.sum(q.T * nrm, axis=1) - 3.0)) < 5e-3  # normal traction = pressure
+    tang = q - np.sum(q.T * nrm, axis=1) * nrm.T
+    want = np.zeros_like(q)
+    want[0, m["bcid"] == 1] = -1.0
+    want[0, m["bcid"] == 2] = 1.0
+    want[2, m["bcid"] == 5] = 1.0
+    want[2, m["bcid"] == 6] = -1.0
+    assert np.max(np.abs(tang - want)) < 5e-3
