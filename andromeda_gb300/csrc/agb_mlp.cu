@@ -240,14 +240,17 @@ static void gemm(bool split, int M, int N, int K, const float* A, int lda, const
 //     [row/8][k/8][8][8]), 64 KB each;
 //   * the weights, pre-split and pre-packed in the same layout chunk by chunk
 //     (32 k per chunk; [layer chunk][hi/lo][n/8][k/8][8][8]), stream through a
-//     two-slot ring by one bulk copy per chunk (warp 8); a slot is released by
-//     tcgen05.commit of the products that read it;
-//   * one thread issues tcgen05.mma (M = 128, N = 256 or 32, K = 16; the three
-//     split products hi*hi, hi*lo, lo*hi per k step) into a 128 x 256 FP32
-//     accumulator in tensor memory;
-//   * 8 warps read the accumulator (tcgen05.ld, warp w: lanes 32 (w%4) ...,
-//     columns 128 (w/4) ...), add the bias, apply SiLU and write the next
-//     layer's hi/lo activations; layer 4 adds the bias, de-normalises, stores.
+//     two-slot ring by one bulk copy per chunk (the copy warp); a slot is
+//     released by tcgen05.commit of the products that read it;
+//   * one thread of the issuing warp issues tcgen05.mma (M = 128, N = 256 or 32,
+//     K = 16; the three split products hi*hi, hi*lo, lo*hi per k step) into one
+//     of two 128 x 256 FP32 accumulators in tensor memory (layer l into (l-1)&1);
+//     chunk j of a layer waits only for the 32 activation columns of chunk j, so
+//     a layer's products start while the previous epilogue writes later chunks;
+//   * 16 epilogue warps read the accumulator (tcgen05.ld, warp w: lanes
+//     32 (w%4) ..., columns 64 (w/4) ...), add the bias, apply SiLU and write the
+//     next layer's hi/lo activations chunk by chunk; layer 4 adds the bias,
+//     de-normalises and stores.
 // Every wait is bounded (error flag); the tensor memory is freed on every path.
 // ---------------------------------------------------------------------------
 constexpr int TC_M = 128, TC_H = 256, TC_NOUT = 32, TC_KC = 32;
@@ -255,7 +258,7 @@ constexpr int TC_EPI = 16;                    // epilogue warps: 4 per TMEM lane
 constexpr int TC_THREADS = (TC_EPI + 2) * 32;  // + 1 copy warp + 1 issuing warp
 constexpr size_t TC_H_BYTES = (size_t)TC_M * TC_H * 2;             // one half (hi or lo) of the activations
 constexpr size_t TC_SLOT = 2ull * TC_H * TC_KC * 2;                  // largest chunk: N 256 x K 32, hi + lo
-constexpr size_t TC_SMEM = 2 * TC_H_BYTES + 2 * TC_SLOT;             // 192 KB
+constexpr size_t TC_SMEM = 2 * TC_H_BYTES + 2 * TC_SLOT;             // 192 KB (+ 4 KB static)
 // packed weights (bytes): layer 1 one chunk (N 256, K 16), layers 2-3 eight chunks (N 256, K 32),
 // layer 4 eight chunks (N 32, K 32); hi then lo inside a chunk
 constexpr int64_t TC_C1 = 2ll * TC_H * 16 * 2, TC_C23 = 2ll * TC_H * TC_KC * 2, TC_C4 = 2ll * TC_NOUT * TC_KC * 2;
