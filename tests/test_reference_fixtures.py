@@ -1,7 +1,7 @@
 """Cases on the reference's own meshes (run/mesh/sphere-01.msh of run/laplace/sphere,
 run/mesh/sphere-in-sphere-1024-1843-3678-tri.msh of run/stokes/flow-over-sphere,
 run/mesh/ellipsoid211-in-sphere-1024-1041-2117.msh of run/stokes/flow-over-ellipsoid,
-run/mesh/kocka-000-111-314-624_tri.msh of run/stokes/Couette),
+run/mesh/kocka-000-111-314-624_tri.msh of run/stokes/Couette and Poiseuille),
 converted once into tests/golden/*.npz with the node order of the files (the element
 normal comes from nodes 1-3, as in the reference).
 
@@ -18,7 +18,8 @@ spheroid's axis against the reference's own analytic resistances
 (CalResTensorPrime, lib_particle.f90:1906-1927, with the semi-minor axis of
 calForceOnEllipsoid, lib_particle.f90:1979-1996) within 1.5 % (discretisation and
 the container, 645 semi-minor axes away); the Couette case on the cube (velocity on
-all six walls): the piecewise-constant traction of u = (z, 0, 0), oracle and GPU.
+all six walls): the piecewise-constant traction of u = (z, 0, 0), oracle and GPU;
+the Poiseuille case (mixed boundary conditions) on the oracle.
 """
 import numpy as np
 import pytest
@@ -252,3 +253,38 @@ def test_gpu_couette_flux_bc_reference_cube(agb):
     want[2, m["bcid"] == 5] = 1.0
     want[2, m["bcid"] == 6] = -1.0
     assert np.max(np.abs(tang - want)) < 5e-3
+
+
+def test_poiseuille_reference_cube(orc):
+    """run/stokes/Poiseuille (stokesPoiseuille-X.bic) on the reference's cube, on the
+    oracle: viscosity 1.5, inlet (left) u_x = (8/3) z (1 - z), x traction given on the
+    outlet (right; taken as 0 here, which only shifts the free pressure level) and on
+    front and back (0), no slip on top and bottom.  Plane Poiseuille flow: pressure
+    p = 8 (1 - x), wall shear mu du/dz = -+4.  With the traction convention
+    q = -(sigma . n): q_x = 4 on both plates, q_z = +-p on top/bottom, q_y = +-p on
+    back/front, q_x = -8 on the inlet.  The linear velocity elements carry the
+    quadratic profile only approximately (624 triangles): wall means within 5 %."""
+    m = reference_mesh("cube_624")
+    known = np.ones((3, 6), np.int32)
+    known[0, [2, 3, 5]] = 2  # x traction known on back, front, right
+    U = np.zeros((1, 3, len(m["xyz"])))
+    z = m["xyz"][:, 2]
+    U[0, 0] = (8.0 / 3.0) * (z - z * z)
+    P = orc.Problem(2, m, walls=[1, 2, 3, 4, 5, 6], known=known, diff=1.5, itri=5)
+    P.form_integrals()
+    q, _, nits, ierr = P.stokes_solve_sequence(U, maxit=0, eps=1e-13, fwall=1)
+    P.close()
+    assert ierr == 0
+    q = q[0]
+    cx = m["xyz"][m["con"][:, :3]].mean(axis=1)[:, 0]
+    top, bottom, back, front, left = (m["bcid"] == w for w in (1, 2, 3, 4, 5))
+    for sel in (top, bottom):
+        assert abs(np.mean(q[0, sel]) - 4.0) < 0.2
+    slope, icpt = np.polyfit(cx[top], q[2, top], 1)
+    assert abs(slope + 8.0) < 0.4 and abs(icpt - 8.0) < 0.4
+    slope, icpt = np.polyfit(cx[bottom], q[2, bottom], 1)
+    assert abs(slope - 8.0) < 0.4 and abs(icpt + 8.0) < 0.4
+    p_mean = 8.0 * (1.0 - np.mean(cx[back]))
+    assert abs(np.mean(q[1, back]) - p_mean) < 0.05 * p_mean
+    assert abs(np.mean(q[1, front]) + p_mean) < 0.05 * p_mean
+    assert abs(np.mean(q[0, left]) + 8.0) < 0.4
