@@ -522,8 +522,11 @@ static void tri_lap_regular(const TriRule& R, const double v[9], const double s[
                             double area, double out[4]) {
   tri_lap_sub(R, v, bary_identity(), s, n, area, out);
 }
-// Quad_BEMIntNum (lib_intAna.f90:219-344); out[0]=G, out[1..4]=H at nodes
-static void quad_lap_regular(int iqud, const double q[12], const double s[3], double multi, double out[5]) {
+// Quad_BEMIntNum (lib_intAna.f90:219-344); out[0]=G, out[1..4]=H at nodes.
+// ndiv > 0 replaces the edge-length subdivision by ndiv x ndiv cells: 1 is the
+// regular branch of Quad_BEMInt (lib_int.f90:329-601, ndivXi = ndivEt = 1).
+static void quad_lap_regular(int iqud, const double q[12], const double s[3], double multi, double out[5],
+                             int ndiv = 0) {
   const double *P1 = q, *P2 = q + 3, *P3 = q + 6, *P4 = q + 9;
   int ng1 = agb_tables::kGaussNg1[iqud - 1], ng2 = agb_tables::kGaussNg2[iqud - 1];
   for (int k = 0; k < 5; ++k) out[k] = 0.0;
@@ -535,6 +538,7 @@ static void quad_lap_regular(int iqud, const double q[12], const double s[3], do
   double d13 = std::max(d1, d3), d24 = std::max(d2, d4);
   int ndx = std::max(2, (int)(d13 / minedge + 0.5));
   int nde = std::max(2, (int)(d24 / minedge + 0.5));
+  if (ndiv > 0) ndx = nde = ndiv;
   for (int ix = 1; ix <= ndx; ++ix)
     for (int ie = 1; ie <= nde; ++ie) {
       double a = -1.0 + (ix - 1) * 2.0 / ndx, b = -1.0 + ix * 2.0 / ndx;
@@ -625,12 +629,14 @@ static void tri_stk_regular(const TriRule& R, const double v[9], const double s[
                             StkElem& E) {
   tri_stk_sub(R, v, bary_identity(), s, n, area, E);
 }
-// Quad_StokesIntNum (lib_Stokes.f90:3754-3940): fixed 3x3 subcells
-static void quad_stk_regular(int iqud, const double q[12], const double s[3], double multi, StkElem& E) {
+// Quad_StokesIntNum (lib_Stokes.f90:3754-3940): fixed 3x3 subcells; ndiv = 1 is
+// the regular branch of Quad_StokesInt (lib_Stokes.f90:3398-3752, one cell).
+static void quad_stk_regular(int iqud, const double q[12], const double s[3], double multi, StkElem& E,
+                             int ndiv = 3) {
   const double *P1 = q, *P2 = q + 3, *P3 = q + 6, *P4 = q + 9;
   int ng1 = agb_tables::kGaussNg1[iqud - 1], ng2 = agb_tables::kGaussNg2[iqud - 1];
   E.zero();
-  const int ndx = 3, nde = 3;
+  const int ndx = ndiv, nde = ndiv;
   double G[3][3], T[3][3], prG[3], prT[3];
   for (int ix = 1; ix <= ndx; ++ix)
     for (int ie = 1; ie <= nde; ++ie) {
@@ -1446,6 +1452,186 @@ static void force_torque(const Problem& P, const double* qx, const double* qy, c
   }
 }
 
+// -----------------------------------------------------------------------------
+// Post-processing of a solved Stokes / Laplace field: the surface pressure and
+// values at points inside the domain.  Not on the solve path; the integrals of
+// a domain point are the element integrals of the assembly with no singular
+// element (isrc = 0).
+// -----------------------------------------------------------------------------
+
+// pressureStokes (lib_Stokes.f90:4-94): pressure at the q-source points
+// (element centroids) from the pressure rows of the integral matrices, in the
+// differenced form of Ingber (1991) for the stresslet part, times 2 for a
+// point on a smooth wall.  u: 3 x nnodes, q: 3 x nelem (component-major).  The
+// centroid velocity is InterpolateToQMesh (lib_mesh.f90:635-684): 1/3 per
+// node on a triangle, the bilinear shape functions at the centre (1/4) on a
+// quad.  As in the reference, row r of the q-source rows takes the centroid
+// velocity of element r and writes p[r]; with the subdomain's elements in
+// mesh order (walls listed in the order the mesh holds them) row r is element
+// r.  The centroid velocity multiplies the row sum of prT, which the pressure
+// correction of sdIntRowQStokes (lib_Stokes.f90:1851-1863) sets to zero, so it
+// moves p by rounding only.  Needs the Stokes integral matrices
+// (orc_form_integrals).
+static void pressure_stokes(const Problem& P, const double* u, const double* q, double* p) {
+  const double osemPi = (double)std::atan(1.0f) * 4.0 * 8.0;  // single-precision ATAN(1.0)
+  const int nn = P.nnodes, ne = P.nelem;
+  std::vector<double> vq(3 * (size_t)ne, 0.0);
+  for (int e = 0; e < ne; ++e) {
+    const double f = (P.type[e] == 2) ? 1.0 / 3.0 : 0.25;
+    for (int c = 0; c < 3; ++c) {
+      double acc = 0.0;
+      for (int k = 0; k < P.nno[e]; ++k) acc += f * u[(size_t)c * nn + P.con[4 * e + k]];
+      vq[(size_t)c * ne + e] = acc;
+    }
+  }
+  const size_t nsp = (size_t)P.nsp;
+  const std::vector<double>&prTx = P.M[6], &prTy = P.M[7], &prTz = P.M[8];
+  const std::vector<double>&prGx = P.M[15], &prGy = P.M[16], &prGz = P.M[17];
+  for (int row = 0; row < P.sd_nqnodes; ++row) {
+    const size_t i = (size_t)P.sd_nnodes + row;
+    double acc = 0.0;
+    for (int j = 0; j < P.sd_nnodes; ++j) {
+      const int icol = P.nodeList[j];
+      const size_t k = (size_t)j * nsp + i;
+      acc = acc + P.diff * (prTx[k] * (u[icol] - vq[row]) + prTy[k] * (u[(size_t)nn + icol] - vq[(size_t)ne + row]) +
+                            prTz[k] * (u[2 * (size_t)nn + icol] - vq[2 * (size_t)ne + row]));
+    }
+    for (int j = 0; j < P.sd_nqnodes; ++j) {
+      const int icol = P.qnodeList[j];
+      const size_t k = (size_t)j * nsp + i;
+      acc = acc - (prGx[k] * q[icol] + prGy[k] * q[(size_t)ne + icol] + prGz[k] * q[2 * (size_t)ne + icol]);
+    }
+    p[row] = -acc / osemPi * 2.0;
+  }
+}
+
+// GetStokesDomainValue (lib_Stokes.f90:3043-3373): velocity (out[0..2]) and
+// pressure (out[3]) at a point s of the domain from the boundary velocity u
+// (3 x nnodes) and traction q (3 x nelem).  Triangles: Triangle_StokesInt with
+// isrc = 0 (the regular rule; the near-singular options of the problem apply);
+// quads: the regular branch of Quad_StokesInt (one cell).  err: the
+// reference's check of the point -- the stresslet diagonal sums to 8 pi and
+// sum G.n vanishes for a point inside; getStokesDV (lib_Stokes.f90:3020-3035)
+// flags err > 1e-2 as outside.
+static void stokes_domain_value(const Problem& P, const double s[3], const double* u, const double* q, double out[4],
+                                double& err) {
+  const double osemPi = (double)std::atan(1.0f) * 4.0 * 8.0;
+  const int nn = P.nnodes, ne = P.nelem;
+  StkRow R(nn, ne);
+  StkElem E;
+  for (size_t jj = 0; jj < P.loWalls.size(); ++jj) {
+    const int iWall = P.loWalls[jj];
+    const double mm = P.normMul[jj];
+    for (int ie = 0; ie < ne; ++ie) {
+      if (P.bcid[ie] != iWall) continue;
+      double v[12];
+      element_vertices(P, ie, v);
+      E.zero();
+      if (P.type[ie] == 2) {
+        const double n[3] = {mm * P.normal[3 * ie], mm * P.normal[3 * ie + 1], mm * P.normal[3 * ie + 2]};
+        tri_walk(P.opt, v, s, P.area[ie], 0, [&](const Bary& B, double a, bool sk) { tri_stk_sub(P.tri, v, B, s, n, a, E, sk); });
+      } else {
+        quad_stk_regular(P.iqud, v, s, mm, E, 1);
+      }
+      for (int j = 0; j < P.nno[ie]; ++j) {
+        const int nd = P.con[4 * ie + j];
+        for (int k = 0; k < 6; ++k) R.t(k, nd) += E.T[k][j];
+        for (int k = 0; k < 3; ++k) R.t(6 + k, nd) += E.prT[k][j];
+      }
+      for (int k = 0; k < 6; ++k) R.g(k, ie) = E.G[k];
+      for (int k = 0; k < 3; ++k) R.g(6 + k, ie) = E.prG[k];
+    }
+  }
+  err = -9.99;
+  double cx = 0, cy = 0, cz = 0;
+  for (int i = 0; i < nn; ++i) { cx -= R.t(0, i); cy -= R.t(3, i); cz -= R.t(5, i); }
+  err = std::max(err, std::fabs(cx / osemPi - 1.0));
+  err = std::max(err, std::fabs(cy / osemPi - 1.0));
+  err = std::max(err, std::fabs(cz / osemPi - 1.0));
+  cx = cy = cz = 0;
+  for (int i = 0; i < ne; ++i) {
+    const double m = P.multiOf(P.bcid[i]);
+    const double* n = &P.normal[3 * i];
+    cx = cx - R.g(0, i) * n[0] * m - R.g(1, i) * n[1] * m - R.g(2, i) * n[2] * m;
+    cy = cy - R.g(1, i) * n[0] * m - R.g(3, i) * n[1] * m - R.g(4, i) * n[2] * m;
+    cz = cz - R.g(2, i) * n[0] * m - R.g(4, i) * n[1] * m - R.g(5, i) * n[2] * m;
+  }
+  err = std::max(err, std::fabs(cx));
+  err = std::max(err, std::fabs(cy));
+  err = std::max(err, std::fabs(cz));
+  const double *ux = u, *uy = u + nn, *uz = u + 2 * (size_t)nn;
+  const double *qx = q, *qy = q + ne, *qz = q + 2 * (size_t)ne;
+  double rx = 0, ry = 0, rz = 0, pr = 0;
+  for (int i = 0; i < nn; ++i) {
+    rx = rx + R.t(0, i) * ux[i]; rx = rx + R.t(1, i) * uy[i]; rx = rx + R.t(2, i) * uz[i];
+    ry = ry + R.t(1, i) * ux[i]; ry = ry + R.t(3, i) * uy[i]; ry = ry + R.t(4, i) * uz[i];
+    rz = rz + R.t(2, i) * ux[i]; rz = rz + R.t(4, i) * uy[i]; rz = rz + R.t(5, i) * uz[i];
+    pr = pr + P.diff * (R.t(6, i) * ux[i] + R.t(7, i) * uy[i] + R.t(8, i) * uz[i]);
+  }
+  for (int i = 0; i < ne; ++i) {
+    rx = rx + R.g(0, i) * qx[i] / P.diff; rx = rx + R.g(1, i) * qy[i] / P.diff; rx = rx + R.g(2, i) * qz[i] / P.diff;
+    ry = ry + R.g(1, i) * qx[i] / P.diff; ry = ry + R.g(3, i) * qy[i] / P.diff; ry = ry + R.g(4, i) * qz[i] / P.diff;
+    rz = rz + R.g(2, i) * qx[i] / P.diff; rz = rz + R.g(4, i) * qy[i] / P.diff; rz = rz + R.g(5, i) * qz[i] / P.diff;
+    pr = pr - (R.g(6, i) * qx[i] + R.g(7, i) * qy[i] + R.g(8, i) * qz[i]);
+  }
+  out[0] = -rx / osemPi;
+  out[1] = -ry / osemPi;
+  out[2] = -rz / osemPi;
+  out[3] = -pr / osemPi;
+}
+
+// GetSubDomainValue (lib_domain.f90:210-344) with VerifyIntegrals
+// (lib_domain.f90:354-391): the Laplace field at a point s of the domain from
+// the boundary values u (nnodes) and fluxes q (nelem), divided by the point's
+// free-term coefficient c = -sum H (1 inside).  Triangles: Triangle_BEMInt with
+// isrc = 0; quads: the regular branch of Quad_BEMInt (one cell).  err: the
+// linear-field check (u = x_j, q = n_j) of VerifyIntegrals.
+static double laplace_domain_value(const Problem& P, const double s[3], const double* u, const double* q, double& err) {
+  const int nn = P.nnodes, ne = P.nelem;
+  std::vector<double> rowH(nn, 0.0), rowG(ne, 0.0);
+  for (size_t jj = 0; jj < P.loWalls.size(); ++jj) {
+    const int iWall = P.loWalls[jj];
+    const double mm = P.normMul[jj];
+    for (int ie = 0; ie < ne; ++ie) {
+      if (P.bcid[ie] != iWall) continue;
+      double v[12], integ = 0.0, inteH[4] = {0, 0, 0, 0};
+      element_vertices(P, ie, v);
+      if (P.type[ie] == 2) {
+        const double n[3] = {mm * P.normal[3 * ie], mm * P.normal[3 * ie + 1], mm * P.normal[3 * ie + 2]};
+        double o[4] = {0, 0, 0, 0};
+        tri_walk(P.opt, v, s, P.area[ie], 0, [&](const Bary& B, double a, bool sk) { tri_lap_sub(P.tri, v, B, s, n, a, o, sk); });
+        integ = o[0]; inteH[0] = o[1]; inteH[1] = o[2]; inteH[2] = o[3];
+      } else {
+        double o[5];
+        quad_lap_regular(P.iqud, v, s, mm, o, 1);
+        integ = o[0];
+        for (int k = 0; k < 4; ++k) inteH[k] = o[1 + k];
+      }
+      for (int j = 0; j < P.nno[ie]; ++j) rowH[P.con[4 * ie + j]] += inteH[j];
+      rowG[ie] = integ;
+    }
+  }
+  double c = 0.0;
+  for (int i = 0; i < nn; ++i) c = c - rowH[i];
+  err = 0.0;
+  for (int j = 0; j < 3; ++j) {
+    double cc = 0.0;
+    for (int i = 0; i < nn; ++i) cc = cc + rowH[i] * P.x[3 * i + j];
+    cc = cc + s[j] * c;
+    for (int i = 0; i < ne; ++i) cc = cc - rowG[i] * P.normal[3 * i + j] * P.multiOf(P.bcid[i]);
+    err = std::max(err, std::fabs(cc));
+  }
+  double res = 0.0;
+  for (int i = 0; i < nn; ++i) res = res - rowH[i] * u[i];
+  for (int i = 0; i < ne; ++i) {
+    double multi = 0.0;  // GetNormalMulti (lib_domain.f90:188-205): 0 for an element of no subdomain wall
+    for (size_t jj = 0; jj < P.loWalls.size(); ++jj)
+      if (P.bcid[i] == P.loWalls[jj]) multi = P.normMul[jj];
+    res = res - rowG[i] * q[i] * multi / P.diff;
+  }
+  return res / c;
+}
+
 }  // namespace orc
 
 using namespace orc;
@@ -1827,6 +2013,29 @@ int orc_stokes_solve_sequence(void* h, int nrhs, const double* u_in, double* q_o
 // Force and torque of a traction field on one wall (lib_particle.f90:1751-1904)
 void orc_force_torque(void* h, const double* qx, const double* qy, const double* qz, int wall, double ft[6]) {
   force_torque(*(Problem*)h, qx, qy, qz, wall, ft, ft + 3);
+}
+
+// Surface pressure at the q-source points (pressureStokes); u 3 x nnodes, q 3 x
+// nelem component-major, p sd_nqnodes.  Returns -1 without Stokes matrices.
+int orc_pressure_stokes(void* h, const double* u, const double* q, double* p) {
+  Problem* P = (Problem*)h;
+  if (P->kind != 2 || P->M[6].empty() || P->M[15].empty()) return -1;
+  pressure_stokes(*P, u, q, p);
+  return 0;
+}
+// Values at npts domain points pts[3*k]: Stokes out[4*k] = (ux, uy, uz, p) with
+// u 3 x nnodes, q 3 x nelem; Laplace out[k] with u nnodes, q nelem.  err[k] the
+// reference's integration check of the point.  OpenMP over the points.
+void orc_domain_values(void* h, int npts, const double* pts, const double* u, const double* q, double* out,
+                       double* err) {
+  Problem* P = (Problem*)h;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int k = 0; k < npts; ++k) {
+    double e = 0.0;
+    if (P->kind == 2) stokes_domain_value(*P, pts + 3 * (size_t)k, u, q, out + 4 * (size_t)k, e);
+    else out[k] = laplace_domain_value(*P, pts + 3 * (size_t)k, u, q, e);
+    err[k] = e;
+  }
 }
 
 // CPU baseline sample: integrate rows [r0, r1) of the reference's nsp rows

@@ -76,6 +76,9 @@ def lib():
         L.orc_stokes_solve_sequence.argtypes = [C.c_void_p, C.c_int, dp, dp, C.c_int, C.c_double, C.c_int, dp, ip]
         L.orc_stokes_solve_sequence.restype = C.c_int
         L.orc_force_torque.argtypes = [C.c_void_p, dp, dp, dp, C.c_int, dp]
+        L.orc_pressure_stokes.argtypes = [C.c_void_p, dp, dp, dp]
+        L.orc_pressure_stokes.restype = C.c_int
+        L.orc_domain_values.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp, dp]
         L.orc_time_rows.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
         L.orc_time_rows.restype = C.c_double
         L.orc_num_threads.restype = C.c_int
@@ -285,6 +288,29 @@ class Problem:
         q3 = np.ascontiguousarray(q3, dtype=np.float64)
         lib().orc_force_torque(self.h, q3[0].copy(), q3[1].copy(), q3[2].copy(), wall, ft)
         return ft
+
+    def pressure(self, u3, q3):
+        """Surface pressure at the q-source points (pressureStokes, lib_Stokes.f90:4-94)
+        of the velocity u3 (3, nnodes) and traction q3 (3, nelem); needs form_integrals."""
+        p = np.zeros(self.sd_nqnodes)
+        rc = lib().orc_pressure_stokes(self.h, np.ascontiguousarray(u3, dtype=np.float64).ravel(),
+                                       np.ascontiguousarray(q3, dtype=np.float64).ravel(), p)
+        if rc != 0:
+            raise RuntimeError("pressure needs the Stokes integral matrices (form_integrals)")
+        return p
+
+    def domain_values(self, points, u, q):
+        """Field at points inside the domain (GetStokesDomainValue lib_Stokes.f90:3043,
+        GetSubDomainValue lib_domain.f90:210).  Stokes: u (3, nnodes), q (3, nelem) ->
+        (npts, 4) = velocity and pressure; Laplace: u (nnodes,), q (nelem,) -> (npts,).
+        Also returns the reference's integration check of each point (small inside)."""
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        n = len(pts)
+        out = np.zeros(n * (4 if self.kind == 2 else 1))
+        err = np.zeros(n)
+        lib().orc_domain_values(self.h, n, pts.ravel(), np.ascontiguousarray(u, dtype=np.float64).ravel(),
+                                np.ascontiguousarray(q, dtype=np.float64).ravel(), out, err)
+        return (out.reshape(n, 4) if self.kind == 2 else out), err
 
 
 def lsqr_precon(m, n, ia, ja, a):
