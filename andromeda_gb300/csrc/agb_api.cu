@@ -101,6 +101,37 @@ int fail(agb_context* c, int code, const std::string& msg) {
   else g_free_err = msg;
   return code;
 }
+
+// Host checks of a mesh before anything reaches the device (they need no
+// context): every coordinate finite, connectivity inside [0, nnodes), and the
+// normal of every element -- the cross product of its nodes 1-3, as
+// CalElementNormal (lib_mesh.f90:716) takes it -- finite and of a length above
+// 1e-12 of the product of the two edge lengths (nodes 1-3 neither coincident
+// nor collinear to rounding), so that no element's normal divides by a zero
+// length.  Elements e0..e1-1 index the nodes of xyz.  Returns the first defect,
+// empty for a sound mesh.
+std::string mesh_defect(int nnodes, const double* xyz, int e0, int e1, const int* etype, const int* con) {
+  for (size_t i = 0; i < 3 * (size_t)nnodes; ++i)
+    if (!std::isfinite(xyz[i])) return "node " + std::to_string(i / 3) + " has a coordinate that is not finite";
+  for (int e = e0; e < e1; ++e) {
+    if (etype[e] != AGB_TRI && etype[e] != AGB_QUAD) return "element " + std::to_string(e) + ": type must be 2 or 3";
+    const int nno = etype[e] == AGB_TRI ? 3 : 4;
+    const int* ce = con + 4 * (size_t)e;
+    for (int k = 0; k < nno; ++k)
+      if (ce[k] < 0 || ce[k] >= nnodes) return "element " + std::to_string(e) + ": connectivity out of range";
+    const double* a = xyz + 3 * (size_t)ce[0];
+    const double* b = xyz + 3 * (size_t)ce[1];
+    const double* d = xyz + 3 * (size_t)ce[2];
+    const double u0 = b[0] - a[0], u1 = b[1] - a[1], u2 = b[2] - a[2];
+    const double v0 = d[0] - a[0], v1 = d[1] - a[1], v2 = d[2] - a[2];
+    const double n0 = u1 * v2 - u2 * v1, n1 = u2 * v0 - u0 * v2, n2 = u0 * v1 - u1 * v0;
+    const double len2 = n0 * n0 + n1 * n1 + n2 * n2;
+    const double edges2 = (u0 * u0 + u1 * u1 + u2 * u2) * (v0 * v0 + v1 * v1 + v2 * v2);
+    if (!(len2 > 1e-24 * edges2) || !std::isfinite(len2))
+      return "element " + std::to_string(e) + " is degenerate: its nodes 1-3 span no normal";
+  }
+  return std::string();
+}
 #define CUDA_OR_FAIL(ctx, expr)                                                               \
   do {                                                                                        \
     cudaError_t e_ = (expr);                                                                  \
@@ -530,14 +561,11 @@ const char* agb_last_error(const agb_context* c) { return c ? c->err.c_str() : g
 
 int agb_set_mesh(agb_context* c, int nnodes, const double* xyz, int nelem, const int* etype, const int* con,
                  const int* bcid) {
-  if (!c) return AGB_ERR_ARG;
+  // the mesh is checked before the context, so that these checks run without a GPU
   if (nnodes <= 0 || nelem <= 0 || !xyz || !etype || !con || !bcid) return fail(c, AGB_ERR_ARG, "empty mesh");
-  for (int e = 0; e < nelem; ++e) {
-    if (etype[e] != AGB_TRI && etype[e] != AGB_QUAD) return fail(c, AGB_ERR_ARG, "element type must be 2 or 3");
-    const int nno = etype[e] == AGB_TRI ? 3 : 4;
-    for (int k = 0; k < nno; ++k)
-      if (con[4 * e + k] < 0 || con[4 * e + k] >= nnodes) return fail(c, AGB_ERR_ARG, "connectivity out of range");
-  }
+  const std::string defect = mesh_defect(nnodes, xyz, 0, nelem, etype, con);
+  if (!defect.empty()) return fail(c, AGB_ERR_ARG, "agb_set_mesh: " + defect);
+  if (!c) return fail(c, AGB_ERR_ARG, "agb_set_mesh: no context");
   cudaSetDevice(c->device);
   free_problem(c);
   c->nnodes = nnodes;
@@ -1155,7 +1183,7 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
                          const int* etype, const int* con, const int* bcid, int particle_wall, int outer_wall,
                          int itri, int maxit, double eps, double mem_gb, int autotune, double* R, int* nit,
                          int* istop, double* stats) {
-  if (!c) return AGB_ERR_ARG;
+  // the bodies are checked before the context, so that these checks run without a GPU
   if (nbodies < 1 || !node_off || !xyz || !elem_off || !etype || !con || !bcid || !R)
     return fail(c, AGB_ERR_ARG, "agb_batch_resistance: missing arrays");
   if (itri < 1 || itri > 5 || maxit < 0 || !(eps >= 0.0) || !(mem_gb >= 0.0))
@@ -1176,7 +1204,10 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
           return fail(c, AGB_ERR_ARG, "connectivity out of range in body " + std::to_string(i));
     }
     if (!pw || !ow) return fail(c, AGB_ERR_ARG, "batched body " + std::to_string(i) + " lacks a wall");
+    const std::string defect = mesh_defect(nn, xyz + 3 * (size_t)node_off[i], elem_off[i], elem_off[i + 1], etype, con);
+    if (!defect.empty()) return fail(c, AGB_ERR_ARG, "batched body " + std::to_string(i) + ": " + defect);
   }
+  if (!c) return fail(c, AGB_ERR_ARG, "agb_batch_resistance: no context");
   cudaSetDevice(c->device);
   using clk = std::chrono::steady_clock;
   auto ms = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double, std::milli>(b - a).count(); };

@@ -86,7 +86,13 @@ const char* agb_last_error(const agb_context* ctx);
 
 /* Mesh.  xyz: 3*nnodes doubles (node-major: x,y,z of node 0, then node 1 ...).
  * etype: 2 = 3-node triangle, 3 = 4-node quad.  con: 4*nelem 0-based node ids
- * (4th entry ignored for triangles).  bcid: wall id of each element. */
+ * (4th entry ignored for triangles).  bcid: wall id of each element.
+ * Rejected with AGB_ERR_ARG before the context is used (so with ctx NULL the
+ * message is in agb_last_error(NULL)): a coordinate that is not finite,
+ * connectivity out of range, an unknown element type, and a degenerate element
+ * (nodes 1-3, which give the element normal as in CalElementNormal,
+ * lib_mesh.f90:716, coincident or collinear to rounding: the normal shorter
+ * than 1e-12 of the product of the two edges). */
 int agb_set_mesh(agb_context* ctx, int nnodes, const double* xyz, int nelem, const int* etype, const int* con,
                  const int* bcid);
 
@@ -245,7 +251,8 @@ int agb_lsqr_precon_dense_noalloc(int m, int n, int64_t lda, double* A, double* 
  * algorithmic bytes of all A*V launches; kernel launches; chosen block rows
  * per A*V CTA, per A^T*U stage and per A^T*U row group; graph iterations;
  * device ms of the whole call; host ms of the force/torque step.  ctx only carries the
- * device and the error text (its own mesh/problem are untouched). */
+ * device and the error text (its own mesh/problem are untouched).  Each body's
+ * mesh is checked like agb_set_mesh's before the context is used. */
 int agb_batch_resistance(agb_context* ctx, int nbodies, const int* node_off, const double* xyz, const int* elem_off,
                          const int* etype, const int* con, const int* bcid, int particle_wall, int outer_wall,
                          int itri, int maxit, double eps, double mem_gb, int autotune, double* R, int* nit,
