@@ -1453,6 +1453,135 @@ static void force_torque(const Problem& P, const double* qx, const double* qy, c
 }
 
 // -----------------------------------------------------------------------------
+// The LIS path of the Stokes system (SLET LIS): StokesBigSystemSOLVElis
+// (lib_StokesLis.f90:4-56) solves, with the LIS library, the square system whose
+// row of every equation is the number of its own unknown (DivideRows,
+// lib_StokesLis.f90:66-161: row = stk%col of the node component for a u-source
+// equation, stk%qcol of the element component for a q-source one), right-hand
+// side rhsM * known values (plis_rhs_matvec, mod_plis.f90:93-107), and the LIS
+// options of the and.inp key LISS, default "-i bicgstab -p jacobi -tol 1.0e-8
+// -maxiter 1000" (mod_par.f90:288).  LIS (2.1.6 in the reference's container
+// build, 2.1.10 in its install notes) is not part of the reference sources;
+// restated here is the published preconditioned BiCGSTAB of van der Vorst (1992)
+// in the form of Barrett et al., "Templates for the Solution of Linear Systems"
+// (SIAM 1994, Fig. 2.10), with the Jacobi preconditioner M = diag(A), a zero
+// initial guess (LIS's default) and the stop ||b - A x||_2 <= tol ||b||_2.
+// status: 0 converged, 1 iteration limit, 2 breakdown (rho, r~.v, t.t or omega
+// zero).
+// -----------------------------------------------------------------------------
+struct LisSystem {
+  int n = 0;
+  std::vector<int64_t> ia;  // 0-based CSR in the LIS row order
+  std::vector<int> ja;
+  std::vector<double> a, diag;
+  std::vector<int> row_of_crs;  // CRS-path row -> LIS row
+};
+
+// Builds the LIS-ordered system from the CRS-path system of stk_form_crs.
+// Returns false if the equations are not one per unknown (contact conditions).
+static bool lis_system(const Problem& P, LisSystem& L) {
+  const Eqn& S = P.stk;
+  const CRS& A = S.sys;
+  if (A.neq != S.nx) return false;
+  L.n = S.nx;
+  L.row_of_crs.assign(A.neq, -1);
+  int row = 0;
+  for (int i = 0; i < P.sd_nnodes; ++i)
+    for (int een = 0; een < 3; ++een) {
+      const int bc = P.knownOf(een, P.BCidList[i]);
+      if (bc == iFlux || bc == iContact) L.row_of_crs[row++] = S.col[P.nodeList[i] + een * P.nnodes] - 1;
+    }
+  for (int i = 0; i < P.sd_nqnodes; ++i)
+    for (int een = 0; een < 3; ++een) {
+      const int bc = P.knownOf(een, P.qbcidList[i]);
+      if (bc == iFunction || bc == iContact) L.row_of_crs[row++] = S.qcol[P.qnodeList[i] + een * P.nelem] - 1;
+    }
+  std::vector<int> crs_of_row(L.n, -1);
+  for (int r = 0; r < A.neq; ++r) {
+    const int lr = L.row_of_crs[r];
+    if (lr < 0 || lr >= L.n || crs_of_row[lr] >= 0) return false;
+    crs_of_row[lr] = r;
+  }
+  L.ia.assign(L.n + 1, 0);
+  L.ja.clear();
+  L.a.clear();
+  L.diag.assign(L.n, 0.0);
+  for (int lr = 0; lr < L.n; ++lr) {
+    const int r = crs_of_row[lr];
+    for (int64_t k = A.i[r] - 1; k < A.i[r + 1] - 1; ++k) {
+      L.ja.push_back(A.j[k] - 1);
+      L.a.push_back(A.v[k]);
+      if (A.j[k] - 1 == lr) L.diag[lr] = A.v[k];
+    }
+    L.ia[lr + 1] = (int64_t)L.a.size();
+  }
+  return true;
+}
+
+static void lis_matvec(const LisSystem& L, const double* x, double* y) {
+  for (int i = 0; i < L.n; ++i) {
+    double s = 0.0;
+    for (int64_t k = L.ia[i]; k < L.ia[i + 1]; ++k) s += L.a[k] * x[L.ja[k]];
+    y[i] = s;
+  }
+}
+
+static double dot(int n, const double* a, const double* b) {
+  double s = 0.0;
+  for (int i = 0; i < n; ++i) s += a[i] * b[i];
+  return s;
+}
+
+// Preconditioned BiCGSTAB (Templates Fig. 2.10) with M = diag(A), x0 = 0.
+static int bicgstab_jacobi(const LisSystem& L, const double* b, double* x, double tol, int maxiter, int& iters,
+                           double& relres) {
+  const int n = L.n;
+  std::vector<double> r(b, b + n), rt(b, b + n), p(n, 0.0), v(n, 0.0), ph(n), s(n), sh(n), t(n);
+  std::fill(x, x + n, 0.0);
+  const double bnrm = std::sqrt(dot(n, b, b));
+  iters = 0;
+  relres = 1.0;
+  if (bnrm == 0.0) { relres = 0.0; return 0; }
+  for (int i = 0; i < n; ++i)
+    if (L.diag[i] == 0.0) return 2;
+  double rho_old = 1.0, alpha = 1.0, omega = 1.0;
+  for (int it = 1; it <= maxiter; ++it) {
+    iters = it;
+    const double rho = dot(n, rt.data(), r.data());
+    if (rho == 0.0) return 2;
+    if (it == 1) p = r;
+    else {
+      const double beta = (rho / rho_old) * (alpha / omega);
+      for (int i = 0; i < n; ++i) p[i] = r[i] + beta * (p[i] - omega * v[i]);
+    }
+    for (int i = 0; i < n; ++i) ph[i] = p[i] / L.diag[i];
+    lis_matvec(L, ph.data(), v.data());
+    const double rtv = dot(n, rt.data(), v.data());
+    if (rtv == 0.0) return 2;
+    alpha = rho / rtv;
+    for (int i = 0; i < n; ++i) s[i] = r[i] - alpha * v[i];
+    const double snrm = std::sqrt(dot(n, s.data(), s.data())) / bnrm;
+    if (snrm <= tol) {
+      for (int i = 0; i < n; ++i) x[i] += alpha * ph[i];
+      relres = snrm;
+      return 0;
+    }
+    for (int i = 0; i < n; ++i) sh[i] = s[i] / L.diag[i];
+    lis_matvec(L, sh.data(), t.data());
+    const double tt = dot(n, t.data(), t.data());
+    if (tt == 0.0) return 2;
+    omega = dot(n, t.data(), s.data()) / tt;
+    for (int i = 0; i < n; ++i) x[i] += alpha * ph[i] + omega * sh[i];
+    for (int i = 0; i < n; ++i) r[i] = s[i] - omega * t[i];
+    relres = std::sqrt(dot(n, r.data(), r.data())) / bnrm;
+    if (relres <= tol) return 0;
+    if (omega == 0.0) return 2;
+    rho_old = rho;
+  }
+  return 1;
+}
+
+// -----------------------------------------------------------------------------
 // Post-processing of a solved Stokes / Laplace field: the surface pressure and
 // values at points inside the domain.  Not on the solve path; the integrals of
 // a domain point are the element integrals of the assembly with no singular
@@ -2008,6 +2137,67 @@ int orc_stokes_solve_sequence(void* h, int nrhs, const double* u_in, double* q_o
     if (ft) force_torque(*P, P->eqn[0].q.data(), P->eqn[1].q.data(), P->eqn[2].q.data(), fwall, ft + 6 * r, ft + 6 * r + 3);
   }
   return ierr_all;
+}
+
+// The LIS path (StokesBigSystemSOLVElis, lib_StokesLis.f90:4): for each of the
+// nrhs velocity fields u_in[r][3][nnodes] (known values; the unknown u are not
+// used), BiCGSTAB with Jacobi on the LIS-ordered system, then
+// StokesDistributeUnknowns into q_out[r][3][nelem] and, for wall fwall, force
+// and torque ft[r][6].  nits[r] / status[r] per field (status as
+// bicgstab_jacobi, 3: the system is not one equation per unknown).  Returns
+// the largest status.
+int orc_stokes_solve_lis(void* h, int nrhs, const double* u_in, double* q_out, double tol, int maxiter, int fwall,
+                         double* ft, int* nits, int* status, double* relres) {
+  Problem* P = (Problem*)h;
+  if (P->kind != 2) return -1;
+  if (P->M[0].empty()) { double e[2]; orc_form_integrals(h, e); }
+  stk_form_crs(*P);
+  Eqn& S = P->stk;
+  LisSystem L;
+  const bool ok = lis_system(*P, L);
+  int worst = 0;
+  for (int r = 0; r < nrhs; ++r) {
+    for (int en = 0; en < 3; ++en) {
+      P->eqn[en].u.assign(u_in + ((size_t)r * 3 + en) * P->nnodes, u_in + ((size_t)r * 3 + en + 1) * P->nnodes);
+      P->eqn[en].q.assign(P->nelem, 0.0);
+    }
+    if (!ok) { status[r] = 3; nits[r] = 0; worst = 3; continue; }
+    for (int i = 0; i < P->sd_nnodes; ++i) {
+      int isp = P->nodeList[i], wall = P->BCidList[i];
+      for (int en = 0; en < 3; ++en) {
+        int ispL = isp + en * P->nnodes;
+        if (P->knownOf(en, wall) == iFunction) S.b[S.col[ispL] - 1] = P->eqn[en].u[isp];
+      }
+    }
+    for (int i = 0; i < P->sd_nqnodes; ++i) {
+      int isp = P->qnodeList[i], wall = P->qbcidList[i];
+      for (int en = 0; en < 3; ++en) {
+        int ispL = isp + en * P->nelem;
+        if (P->knownOf(en, wall) == iFlux) S.b[S.qcol[ispL] - 1] = P->eqn[en].q[isp];
+      }
+    }
+    std::vector<double> bc(S.sys.neq), b(L.n);
+    crs_x_v(S.rhs, S.b.data(), bc.data());
+    for (int k = 0; k < S.sys.neq; ++k) b[L.row_of_crs[k]] = bc[k];
+    int it = 0;
+    double rr = 0.0;
+    const int st = bicgstab_jacobi(L, b.data(), S.x.data(), tol, maxiter, it, rr);
+    nits[r] = it;
+    status[r] = st;
+    if (relres) relres[r] = rr;
+    worst = std::max(worst, st);
+    for (int i = 0; i < P->sd_nqnodes; ++i) {
+      int isp = P->qnodeList[i], wall = P->qbcidList[i];
+      for (int en = 0; en < 3; ++en) {
+        int ispL = isp + en * P->nelem, bcq = P->knownOf(en, wall);
+        P->eqn[en].q[isp] = (bcq == iFlux) ? S.b[S.qcol[ispL] - 1] : S.x[S.qcol[ispL] - 1];
+      }
+    }
+    for (int en = 0; en < 3; ++en)
+      std::copy(P->eqn[en].q.begin(), P->eqn[en].q.end(), q_out + ((size_t)r * 3 + en) * P->nelem);
+    if (ft) force_torque(*P, P->eqn[0].q.data(), P->eqn[1].q.data(), P->eqn[2].q.data(), fwall, ft + 6 * r, ft + 6 * r + 3);
+  }
+  return worst;
 }
 
 // Force and torque of a traction field on one wall (lib_particle.f90:1751-1904)

@@ -76,6 +76,9 @@ def lib():
         L.orc_stokes_solve_sequence.argtypes = [C.c_void_p, C.c_int, dp, dp, C.c_int, C.c_double, C.c_int, dp, ip]
         L.orc_stokes_solve_sequence.restype = C.c_int
         L.orc_force_torque.argtypes = [C.c_void_p, dp, dp, dp, C.c_int, dp]
+        L.orc_stokes_solve_lis.argtypes = [C.c_void_p, C.c_int, dp, dp, C.c_double, C.c_int, C.c_int, dp, ip, ip,
+                                           dp]
+        L.orc_stokes_solve_lis.restype = C.c_int
         L.orc_pressure_stokes.argtypes = [C.c_void_p, dp, dp, dp]
         L.orc_pressure_stokes.restype = C.c_int
         L.orc_domain_values.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp, dp]
@@ -277,6 +280,23 @@ class Problem:
         ierr = lib().orc_stokes_solve_sequence(self.h, nrhs, u_fields.ravel(), q.reshape(-1), maxit, eps, fwall,
                                                ft.reshape(-1), nits)
         return q, ft, nits, ierr
+
+    def stokes_solve_lis(self, u_fields, tol=1e-8, maxiter=1000, fwall=1):
+        """The LIS path (StokesBigSystemSOLVElis, lib_StokesLis.f90:4) with the
+        reference's default LIS options: BiCGSTAB, Jacobi, tol 1e-8, 1000 iterations.
+        Returns (q [nrhs, 3, nelem], force/torque [nrhs, 6], iterations, status,
+        relative residual); status 0 converged, 1 iteration limit, 2 breakdown,
+        3 not one equation per unknown."""
+        u_fields = np.ascontiguousarray(u_fields, dtype=np.float64)
+        nrhs = u_fields.shape[0]
+        q = np.zeros((nrhs, 3, self.nelem))
+        ft = np.zeros((nrhs, 6))
+        nits = np.zeros(nrhs, np.int32)
+        status = np.zeros(nrhs, np.int32)
+        relres = np.zeros(nrhs)
+        lib().orc_stokes_solve_lis(self.h, nrhs, u_fields.ravel(), q.reshape(-1), float(tol), int(maxiter), fwall,
+                                   ft.reshape(-1), nits, status, relres)
+        return q, ft, nits, status, relres
 
     def time_rows(self, r0, r1, nthreads):
         cs = C.c_double(0.0)
