@@ -1,0 +1,61 @@
+"""Host logic of the learned surrogate on the CPU (no GPU): the feature map, the
+21-entry packing of the symmetric resistance tensor, the error measure, the
+parameter sampler of the many-body workload and the training hull that sends
+queries outside it to the BEM."""
+import numpy as np
+
+from andromeda_gb300 import surrogate as S
+
+
+def test_features_append_log_aspect():
+    P = np.array([[0.5, 0.25, 1.0, 1.2], [1.0, 1.0, 0.3, 1.8]])
+    X = S.features(P)
+    assert X.shape == (2, 5) and X.dtype == np.float32
+    assert np.allclose(X[:, :4], P)
+    assert np.allclose(X[:, 4], [np.log(4.0), 0.0])
+
+
+def test_targets_round_trip_symmetric_part():
+    rng = np.random.default_rng(0)
+    R = rng.normal(size=(5, 6, 6))
+    Y = S.tensor_to_targets(R)
+    assert Y.shape == (5, 21)
+    Rs = S.targets_to_tensor(Y)
+    assert np.allclose(Rs, np.swapaxes(Rs, 1, 2))
+    assert np.allclose(Rs, 0.5 * (R + np.swapaxes(R, 1, 2)), atol=1e-6)  # FP32 targets
+
+
+def test_rel_err_is_max_entry_relative():
+    Rt = np.zeros((2, 6, 6))
+    Rt[:, 0, 0] = [10.0, 2.0]
+    R = Rt.copy()
+    R[0, 1, 2] = 0.5
+    R[1, 3, 3] = -0.2
+    assert np.allclose(S.rel_err(R, Rt), [0.05, 0.1])
+
+
+def test_sample_params_ranges_and_seed():
+    P = S.sample_params(2000, seed=3)
+    assert P.shape == (2000, 4)
+    assert np.all((P[:, :2] >= 0.2) & (P[:, :2] <= 1.0))
+    assert np.all((P[:, 2:] >= 0.3) & (P[:, 2:] <= 1.8))
+    assert np.array_equal(P, S.sample_params(2000, seed=3))
+    assert not np.array_equal(P, S.sample_params(2000, seed=4))
+
+
+def test_hull_box_and_mahalanobis_guard():
+    X = S.features(S.sample_params(4000, seed=1))
+    H = S.Hull().fit(X)
+    assert np.all(H.contains(X))  # every training point is inside
+    # outside the axis box in one feature
+    out = X[:5].copy()
+    out[:, 2] = 2.5
+    assert not np.any(H.contains(out))
+    # inside the box feature by feature, but b = c = 0.95 with the largest log
+    # aspect of the set (the feature map would give log(1/0.95)): far from the
+    # training points in Mahalanobis distance
+    odd = X[:5].copy()
+    odd[:, 0] = 0.95
+    odd[:, 1] = 0.95
+    odd[:, 4] = X[:, 4].max()
+    assert not np.any(H.contains(odd))
