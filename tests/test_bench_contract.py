@@ -26,3 +26,39 @@ def test_reference_arm_json_line():
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
     assert "workload" in d["config"]
+
+
+def _bench_module():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_under_test", os.path.join(ROOT, "bench.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_clock_record_summary():
+    """The clocks object of the JSON line from nvidia-smi's CSV samples: median SM
+    clock under load, the maximum, and every throttle reason seen active."""
+    B = _bench_module()
+    cs = B.ClockSampler(0)
+    cs.out = ("2070, 2070, 900.5, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active\n"
+              "2055, 2070, 1350.2, 0x0000000000000004, Not Active, Not Active, Not Active, Active\n"
+              "1980, 2070, 1400.0, 0x0000000000000004, Not Active, Not Active, Not Active, Active\n"
+              "[N/A], 2070, 10, 0x0, Not Active, Not Active, Not Active, Not Active\n")
+    s = cs.summary()
+    assert s["sm_mhz"] == 2055.0 and s["sm_max_mhz"] == 2070.0
+    assert s["reasons"] == ["sw_power_cap"]
+    cs.out = "2070, 2070, 900, 0x0, Active, Not Active, Active, Not Active\n"
+    assert cs.summary()["reasons"] == ["hw_slowdown", "sw_thermal_slowdown"]
+    cs.out = None
+    assert cs.summary()["sm_mhz"] is None
+
+
+def test_measured_peaks_source():
+    B = _bench_module()
+    peak, kind = B.measured_peaks()
+    if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")):
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            assert peak == float(json.load(f)["hbm_gbs"]) and kind == "measured"
+    else:
+        assert (peak, kind) == (6800.0, "fallback")
