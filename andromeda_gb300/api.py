@@ -22,6 +22,7 @@ from ._lib import AgbError, load
 
 LAPLACE, STOKES = 1, 2
 FP64, MIXED, MATRIX_FREE = 0, 1, 2
+SOLVER_LSQR, SOLVER_BICGSTAB = 0, 1
 BC_FUNCTION, BC_FLUX, BC_CONTACT = 1, 2, 3
 
 
@@ -127,6 +128,11 @@ class Context:
         near-singular rule (near_depth levels).  Clears the assembled system."""
         self._ck(self._L.agb_set_integration(self.h, int(sing_mode), int(rec_depth), float(near_eta),
                                              int(near_depth)))
+
+    def set_solver(self, solver):
+        """SOLVER_LSQR (default, lsqr_solve) or SOLVER_BICGSTAB (the LIS path's
+        BiCGSTAB with the Jacobi preconditioner; packed mixed Stokes systems)."""
+        self._ck(self._L.agb_set_solver(self.h, int(solver)))
 
     def geometry(self):
         nrm = np.zeros(3 * self.nelem)

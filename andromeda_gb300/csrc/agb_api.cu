@@ -36,6 +36,7 @@ struct agb_context {
   // problem
   int kind = 0, neq = 0;
   IntegOpt iopt;  // triangle integration options (agb_set_integration)
+  int solver = AGB_SOLVER_LSQR;  // agb_set_solver
   MfOp mfop;                   // matrix-free operator (AGB_MATRIX_FREE)
   float* d_self6 = nullptr;
   double* d_lu = nullptr;      // column-major LU factors of the unscaled FP64 system (agb_solve_lu)
@@ -408,6 +409,18 @@ int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int r
       return fail(c, AGB_ERR_CUDA, "lsqr setup: " + c->lsqr.err);
   }
   std::vector<int> nt(nrhs, 0), is(nrhs, 0);
+  if (c->solver == AGB_SOLVER_BICGSTAB) {
+    if (!c->lsqr.packed)
+      return fail(c, AGB_ERR_UNSUPPORTED, "BiCGSTAB needs the packed mixed system (Stokes, velocity known on every "
+                                          "wall, triangles, default integration, AGB_MIXED)");
+    if (!c->lsqr.bicgstab(c->d_rhs, d_x, eps, maxit, nt.data(), is.data()))
+      return fail(c, AGB_ERR_CUDA, "bicgstab: " + c->lsqr.err);
+    for (int r = 0; r < nrhs; ++r) {
+      if (nit) nit[r] = nt[r];
+      if (istop) istop[r] = is[r];
+    }
+    return AGB_OK;
+  }
   for (int pass = 0; pass <= refine; ++pass) {
     if (!c->lsqr.solve(c->d_rhs, d_x, c->d_q, eps, maxit, nt.data(), is.data(), nullptr, 8, x0_zero && pass == 0))
       return fail(c, AGB_ERR_CUDA, "lsqr: " + c->lsqr.err);
@@ -669,6 +682,14 @@ int agb_set_integration(agb_context* c, int sing_mode, int rec_depth, double nea
   c->iopt.near_eta = near_eta;
   c->iopt.near_depth = near_depth;
   c->assembled = false;
+  return AGB_OK;
+}
+
+int agb_set_solver(agb_context* c, int solver) {
+  if (!c) return fail(c, AGB_ERR_ARG, "agb_set_solver: no context");
+  if (solver != AGB_SOLVER_LSQR && solver != AGB_SOLVER_BICGSTAB)
+    return fail(c, AGB_ERR_ARG, "solver must be AGB_SOLVER_LSQR or AGB_SOLVER_BICGSTAB");
+  c->solver = solver;
   return AGB_OK;
 }
 

@@ -897,6 +897,10 @@ static void launch_av2(const DenseLsqr& L) {
   k_av2<T><<<av2_blocks<T>(L), AV2<T>::WARPS * 32, smem, L.stream>>>((const T*)L.A, L.lda, L.m, (const T*)L.Vs, L.sc,
                                                                      L.Y, (T*)L.Ys, L.part, L.errflag);
 }
+void launch_avp(const DenseLsqr& L, const LsqrScalars* sc, double* Yout) {
+  k_avp<<<cdiv(L.pk_ne, AVP_R), AVP_THREADS, AVP_SMEM, L.stream>>>(L.tm_av, L.tm_vp, L.pk_ne, L.pk_ldp, sc, Yout,
+                                                                  (float*)L.Ys, L.part, L.errflag);
+}
 template <typename T>
 static size_t atu2_smem() {
   return 256 * K8 * sizeof(T) + (sizeof(T) == 4 ? (size_t)Vec<T>::N * K8 * ATU_THREADS * sizeof(double) : 0);
@@ -943,6 +947,11 @@ void DenseLsqr::release() {
   pev_ready = false;
   cudaFree(Y); cudaFree(V); cudaFree(W); cudaFree(X); cudaFree(Z); cudaFree(Ys); cudaFree(Vs);
   cudaFree(part); cudaFree(Zp); cudaFree(sc); cudaFree(nactive); cudaFree(XsD); cudaFree(errflag); cudaFree(Yp); cudaFree(Vp);
+  cudaFree(bg); cudaFree(bg_part); cudaFree(bsc); cudaFree(sc0);
+  bg = bg_part = nullptr;
+  bsc = nullptr;
+  sc0 = nullptr;
+  bg_diag = false;
   Yp = nullptr;
   Vp = nullptr;
   XsD = nullptr; errflag = nullptr;

@@ -69,6 +69,11 @@ typedef struct agb_context agb_context;
                        LSQR sweep recomputes the single-layer entries (Stokes,
                        velocity known on every wall, triangles; zero warm start) */
 
+/* solver of the assembled system (agb_set_solver; the SLET key of and.inp) */
+#define AGB_SOLVER_LSQR 0     /* lsqr_solve with lsqr_precon's column scaling (SLET CRS) */
+#define AGB_SOLVER_BICGSTAB 1 /* BiCGSTAB with the Jacobi preconditioner (SLET LIS with the
+                                 reference's default LIS options) */
+
 /* boundary-condition types (mod_mesh.f90:110) */
 #define AGB_BC_FUNCTION 1
 #define AGB_BC_FLUX 2
@@ -121,6 +126,19 @@ int agb_set_problem(agb_context* ctx, int kind, int nwalls, const int* walls, co
  * (for AGB_MIXED the routed system is then copied to FP32).  Call after
  * agb_set_problem; it clears the assembled system. */
 int agb_set_integration(agb_context* ctx, int sing_mode, int rec_depth, double near_eta, int near_depth);
+
+/* Solver of agb_solve / agb_resistance_tensor (the SLET key, mod_par.f90):
+ * AGB_SOLVER_LSQR (default; lsqr_solve, lib_lsqr.f:33) or AGB_SOLVER_BICGSTAB,
+ * the LIS path's solver (StokesBigSystemSOLVElis lib_StokesLis.f90:4 with the
+ * default options "-i bicgstab -p jacobi", mod_par.f90:288): every equation in
+ * the row of its own unknown, preconditioned BiCGSTAB (van der Vorst 1992) with
+ * M = diag(A), x0 = 0 (the warm start is not used), stop at
+ * ||b - A x|| <= eps ||b|| or maxit iterations (0: 1000, the LIS default).  With
+ * BiCGSTAB, istop[r] is 0 converged, 1 iteration limit, 2 breakdown.  BiCGSTAB
+ * needs the packed mixed system (Stokes, velocity known on every wall,
+ * triangles, default integration, AGB_MIXED); other systems return
+ * AGB_ERR_UNSUPPORTED from the solve. */
+int agb_set_solver(agb_context* ctx, int solver);
 
 /* Element geometry in global element order (normal 3*nelem, area nelem,
  * centroid 3*nelem); elements outside the subdomain are zero. */
