@@ -134,6 +134,26 @@ class Context:
         BiCGSTAB with the Jacobi preconditioner; packed mixed Stokes systems)."""
         self._ck(self._L.agb_set_solver(self.h, int(solver)))
 
+    def surface_pressure(self, u, q):
+        """Pressure at the element centroids (pressureStokes) of velocity u (3, nnodes)
+        and traction q (3, nelem); elements of no subdomain wall get 0."""
+        p = np.zeros(self.nelem)
+        self._ck(self._L.agb_surface_pressure(self.h, np.ascontiguousarray(u, dtype=np.float64).ravel(),
+                                              np.ascontiguousarray(q, dtype=np.float64).ravel(), p))
+        return p
+
+    def domain_values(self, points, u, q):
+        """Field at points inside the domain: Stokes (npts, 4) velocity and pressure,
+        Laplace (npts,); and the reference's check of each point."""
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        n = len(pts)
+        nv = 4 if self.kind == STOKES else 1
+        out = np.zeros(n * nv)
+        err = np.zeros(n)
+        self._ck(self._L.agb_domain_values(self.h, n, pts.ravel(), np.ascontiguousarray(u, dtype=np.float64).ravel(),
+                                           np.ascontiguousarray(q, dtype=np.float64).ravel(), out, err))
+        return (out.reshape(n, 4) if nv == 4 else out), err
+
     def geometry(self):
         nrm = np.zeros(3 * self.nelem)
         area = np.zeros(self.nelem)

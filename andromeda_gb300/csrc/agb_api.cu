@@ -1093,6 +1093,74 @@ int agb_kernel_times(agb_context* c, int reset, double* out) {
   return AGB_OK;
 }
 
+// Post-processing of a solved field: the surface pressure and the values at
+// points inside the domain (FP64, the element integrals of the general path).
+namespace {
+struct PostBufs {
+  double *u = nullptr, *q = nullptr, *pts = nullptr, *out = nullptr, *err = nullptr;
+  ~PostBufs() { cudaFree(u); cudaFree(q); cudaFree(pts); cudaFree(out); cudaFree(err); }
+};
+// q[comp][nelem] (mesh order) -> [comp][ne] (subdomain order), uploaded with u
+int post_upload(agb_context* c, PostBufs& B, const double* u, const double* q) {
+  const int nc = c->neq;
+  std::vector<double> qs((size_t)nc * c->ne);
+  for (int comp = 0; comp < nc; ++comp)
+    for (int pos = 0; pos < c->ne; ++pos) qs[(size_t)comp * c->ne + pos] = q[(size_t)comp * c->nelem + c->elemList[pos]];
+  CUDA_OR_FAIL(c, cudaMalloc(&B.u, (size_t)nc * c->nnodes * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMalloc(&B.q, qs.size() * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMemcpy(B.u, u, (size_t)nc * c->nnodes * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_OR_FAIL(c, cudaMemcpy(B.q, qs.data(), qs.size() * sizeof(double), cudaMemcpyHostToDevice));
+  return AGB_OK;
+}
+double osem_pi() { return (double)std::atan(1.0f) * 4.0 * 8.0; }  // the reference's ATAN(1.0) is single precision
+}  // namespace
+
+int agb_surface_pressure(agb_context* c, const double* u, const double* q, double* p) {
+  int rc = check_ctx(c, true);
+  if (rc) return rc;
+  if (!u || !q || !p) return fail(c, AGB_ERR_ARG, "agb_surface_pressure: missing arrays");
+  if (c->kind != AGB_STOKES) return fail(c, AGB_ERR_UNSUPPORTED, "agb_surface_pressure: Stokes problems only");
+  cudaSetDevice(c->device);
+  PostBufs B;
+  if ((rc = post_upload(c, B, u, q))) return rc;
+  CUDA_OR_FAIL(c, cudaMalloc(&B.out, (size_t)c->ne * sizeof(double)));
+  CUDA_OR_FAIL(c, surface_pressure(c->ne, c->d_geom, c->rule, c->iqud, c->iopt, B.u, c->nnodes, B.q, c->diff,
+                                   osem_pi(), B.out, c->stream));
+  c->nlaunch += 1;
+  std::vector<double> ps(c->ne);
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(ps.data(), B.out, ps.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  std::fill(p, p + c->nelem, 0.0);
+  for (int pos = 0; pos < c->ne; ++pos) p[c->elemList[pos]] = ps[pos];
+  return AGB_OK;
+}
+
+int agb_domain_values(agb_context* c, int npts, const double* pts, const double* u, const double* q, double* out,
+                      double* err) {
+  int rc = check_ctx(c, true);
+  if (rc) return rc;
+  if (npts < 0 || (npts > 0 && (!pts || !u || !q || !out || !err)))
+    return fail(c, AGB_ERR_ARG, "agb_domain_values: missing arrays");
+  if (npts == 0) return AGB_OK;
+  for (int64_t i = 0; i < 3 * (int64_t)npts; ++i)
+    if (!std::isfinite(pts[i])) return fail(c, AGB_ERR_ARG, "agb_domain_values: a point coordinate is not finite");
+  cudaSetDevice(c->device);
+  PostBufs B;
+  if ((rc = post_upload(c, B, u, q))) return rc;
+  const int nv = (c->kind == AGB_STOKES) ? 4 : 1;
+  CUDA_OR_FAIL(c, cudaMalloc(&B.pts, 3 * (size_t)npts * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMalloc(&B.out, (size_t)nv * npts * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMalloc(&B.err, (size_t)npts * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMemcpy(B.pts, pts, 3 * (size_t)npts * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_OR_FAIL(c, domain_values(c->kind == AGB_STOKES, c->ne, c->d_geom, c->rule, c->iqud, c->iopt, npts, B.pts, c->d_xyz, B.u,
+                                c->nnodes, B.q, c->diff, osem_pi(), B.out, B.err, c->stream));
+  c->nlaunch += 1;
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(out, B.out, (size_t)nv * npts * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(err, B.err, (size_t)npts * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  return AGB_OK;
+}
+
 int agb_integral_matrices(agb_context* c, double* T, double* G, double* errs) {
   int rc = check_ctx(c, true);
   if (rc) return rc;

@@ -220,6 +220,26 @@ int agb_lsqr_solve(int m, int n, int64_t nnz, int* maxit, double eps, int* nit, 
  * self-check residuals (max over u-rows, over q-rows). */
 int agb_integral_matrices(agb_context* ctx, double* T, double* G, double* errs);
 
+/* Surface pressure of a solved Stokes field (pressureStokes, lib_Stokes.f90:4-94):
+ * p at the centroid of every element of the subdomain (mesh order; 0 for an
+ * element of no subdomain wall) from the pressure rows of the q-source points
+ * (sdIntRowQStokes, lib_Stokes.f90:1562, self element left out as the
+ * reference's analytic branch does) contracted with the velocity u[3][nnodes]
+ * less the element's centre velocity and the traction q[3][nelem], times
+ * -2 / (8 pi).  FP64. */
+int agb_surface_pressure(agb_context* ctx, const double* u, const double* q, double* p);
+
+/* Values at npts points inside the domain (GetStokesDomainValue,
+ * lib_Stokes.f90:3043; GetSubDomainValue, lib_domain.f90:210) from the boundary
+ * values u[neq][nnodes] and fluxes/tractions q[neq][nelem]: Stokes
+ * out[4k..4k+3] = velocity, pressure; Laplace out[k].  err[k] is the
+ * reference's check of the point (Stokes: stresslet diagonal against 8 pi and
+ * sum G.n; getStokesDV treats err > 1e-2 as outside; Laplace: VerifyIntegrals).
+ * Triangles with the problem's integration options, quads as one Gauss cell
+ * (the regular branch of Quad_StokesInt / Quad_BEMInt).  FP64. */
+int agb_domain_values(agb_context* ctx, int npts, const double* pts, const double* u, const double* q, double* out,
+                      double* err);
+
 /* Sizes of the subdomain numbering: {nsp, nn, nq, rows, unknowns, knowns}. */
 int agb_layout_sizes(agb_context* ctx, int* sizes);
 
