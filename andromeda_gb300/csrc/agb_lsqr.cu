@@ -325,6 +325,7 @@ __global__ void __launch_bounds__(AV2<T>::WARPS * 32) k_av2(const T* __restrict_
     }
     __syncthreads();  // everyone is done with this buffer before it is refilled
   }
+  if (threadIdx.x == 0) mbar_drain(bar, 2, nch, errflag);
   double ssq = 0.0;
   if constexpr (sizeof(T) == 4) {
     const int r = lane >> 3, c = lane & 7, row = row0 + r;
