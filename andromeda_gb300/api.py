@@ -300,7 +300,7 @@ def solv_eqn_fm(f, q, b, pret=2, prep=2):
 
 
 def batch_resistance(meshes, particle_wall=1, outer_wall=2, itri=5, maxit=0, eps=1e-7, mem_gb=0.0, autotune=True,
-                     device=0, ctx=None):
+                     device=0, ctx=None, solver=None):
     """Mixed-precision resistance tensors of many bodies in one batched call.
 
     ``meshes``: list of particle-in-container triangle meshes (the dict layout
@@ -308,10 +308,14 @@ def batch_resistance(meshes, particle_wall=1, outer_wall=2, itri=5, maxit=0, eps
     istop[nb,6], stats) with R[i, r] = (F, T) on particle i for rigid motion r
     of its container.  ``ctx``: a :class:`Context` to run on (its per-body
     contexts are kept for later calls); a new one on ``device`` otherwise.
+    ``solver``: SOLVER_LSQR / SOLVER_BICGSTAB for this call and the context's
+    later ones (None: the context's setting, LSQR by default).
     """
     own = ctx is None
     C_ = Context(device) if own else ctx
     try:
+        if solver is not None:
+            C_.set_solver(solver)
         nb = len(meshes)
         node_off = np.zeros(nb + 1, np.int32)
         elem_off = np.zeros(nb + 1, np.int32)

@@ -1352,7 +1352,8 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
   auto solver_bytes = [&](int i) {
     const BatchSlot& b = slots[i];
     const double mpad = std::ceil(b.m / 256.0) * 256.0;
-    return mpad * 8 * 12.0 + (double)b.lda * 8 * (8 * 3 + 4 + 8 * 8) + 65536.0;
+    const double bicg = (c->solver == AGB_SOLVER_BICGSTAB) ? mpad * 8 * 8 * 7.0 + mpad * 8 : 0.0;
+    return mpad * 8 * 12.0 + (double)b.lda * 8 * (8 * 3 + 4 + 8 * 8) + 65536.0 + bicg;
   };
   double budget = mem_gb * 1e9;
   if (budget <= 0.0) {
@@ -1509,14 +1510,18 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
     cudaFreeAsync(d_nm, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return bail(AGB_ERR_CUDA, "assembly of the wave");
     const auto tb = clk::now();
-    if (autotune && !tuned) {
+    if (autotune && !tuned && c->solver == AGB_SOLVER_LSQR) {
       std::string rep, err;
       if (!batch_autotune(bodies, st, tune, rep, err)) return bail(AGB_ERR_CUDA, "autotune: " + err);
       tuned = true;
     }
     std::vector<int> nv, iv;
     std::string err;
-    if (!batch_lsqr_solve(bodies, 6, eps, maxit, tune, st, nv, iv, &bst, err)) return bail(AGB_ERR_CUDA, "solve: " + err);
+    if (c->solver == AGB_SOLVER_BICGSTAB) {
+      if (!batch_bicgstab_solve(bodies, 6, eps, maxit, st, nv, iv, &bst, err)) return bail(AGB_ERR_CUDA, "solve: " + err);
+    } else if (!batch_lsqr_solve(bodies, 6, eps, maxit, tune, st, nv, iv, &bst, err)) {
+      return bail(AGB_ERR_CUDA, "solve: " + err);
+    }
     const auto tc = clk::now();
     for (size_t t = 0; t < w.size(); ++t) {
       const BatchSlot& b = slots[w[t]];

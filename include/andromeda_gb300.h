@@ -137,7 +137,8 @@ int agb_set_integration(agb_context* ctx, int sing_mode, int rec_depth, double n
  * BiCGSTAB, istop[r] is 0 converged, 1 iteration limit, 2 breakdown.  BiCGSTAB
  * needs the packed mixed system (Stokes, velocity known on every wall,
  * triangles, default integration, AGB_MIXED); other systems return
- * AGB_ERR_UNSUPPORTED from the solve. */
+ * AGB_ERR_UNSUPPORTED from the solve.  agb_batch_resistance on this context
+ * solves its bodies with BiCGSTAB too (istop as above; no autotuning). */
 int agb_set_solver(agb_context* ctx, int solver);
 
 /* Element geometry in global element order (normal 3*nelem, area nelem,

@@ -80,3 +80,24 @@ def test_bicgstab_status_and_unsupported(agb):
     R64, _, info64 = C.resistance_tensor(agb.FP64, 1, 2, eps=1e-10)
     C.close()
     assert np.all(np.isin(info64["istop"], (1, 2, 4)))
+
+
+def test_batch_bicgstab_matches_fp64(agb):
+    """The batched BiCGSTAB (every sweep one launch over all bodies) on bodies of
+    uneven size: each tensor within 5e-6 of the body's FP64 LSQR tensor, as the
+    batched LSQR test asks, with far fewer iterations."""
+    rng = np.random.default_rng(7)
+    meshes = []
+    for n in (180, 320, 520, 760):
+        b, c = rng.uniform(0.3, 1.0, 2)
+        e1, e2 = rng.uniform(0.5, 1.5, 2)
+        body = M.superellipsoid_tri(1.0, b, c, e1, e2, n, rotation=M.random_rotation(rng), inward=True)
+        meshes.append(M.particle_in_sphere(body, outer_level=1, outer_radius=20.0))
+    R, nit, istop, st = agb.batch_resistance(meshes, eps=1e-9, solver=agb.SOLVER_BICGSTAB)
+    assert np.all(istop == 0) and st["av_launches"] > 0
+    for i, m in enumerate(meshes):
+        C = _ctx(agb, m)
+        R64, n64, _ = C.resistance_tensor(agb.FP64, 1, 2, eps=1e-11)
+        C.close()
+        assert np.max(np.abs(R[i] - R64)) < 5e-6 * np.max(np.abs(R64)), i
+        assert np.max(nit[i]) * 3 < np.max(n64), (i, nit[i], n64)
