@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--outer-radius", type=float, default=200.0)
     ap.add_argument("--eps", type=float, default=1e-7)
     ap.add_argument("--solver", default="lsqr", choices=["lsqr", "bicgstab"],
-                    help="sphere: LSQR (lsqr_solve, the default) or BiCGSTAB-Jacobi (the LIS path's solver)")
+                    help="sphere, batch, large: LSQR (lsqr_solve, the default) or BiCGSTAB-Jacobi (the LIS path's solver)")
     ap.add_argument("--fp64-iters", type=int, default=16, help="FP64 comparator LSQR sample (iterations)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -264,14 +264,15 @@ def run_batch(args, rank, world, local):
     eps = args.batch_eps
     tune = not args.no_autotune
     warm = mine[:32]
+    solver = A.SOLVER_BICGSTAB if args.solver == "bicgstab" else A.SOLVER_LSQR
     for _ in range(args.warmup):
-        A.batch_resistance(warm, eps=eps, ctx=ctx, autotune=tune)
+        A.batch_resistance(warm, eps=eps, ctx=ctx, autotune=tune, solver=solver)
     barrier()
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         Rs, nits, istops, sts = [], [], [], []
         for _ in range(args.steps):
-            R, nit, istop, st = A.batch_resistance(mine, eps=eps, ctx=ctx, autotune=tune)
+            R, nit, istop, st = A.batch_resistance(mine, eps=eps, ctx=ctx, autotune=tune, solver=solver)
             Rs.append(R); nits.append(nit); istops.append(istop); sts.append(st)
         t1 = time.perf_counter()
     dev_s = sum(st["device_ms"] for st in sts) / 1000.0
@@ -316,7 +317,8 @@ def run_batch(args, rank, world, local):
                 "config": {"workload": f"{args.bodies} superellipsoids a=1, b,c~U(0.2,1), e1,e2~U(0.3,1.8), "
                                        f"random orientation, {int(ne.min())}..{int(ne.max())} tri (mean "
                                        f"{ne.mean():.0f}), each in an L2 container r=200, 6 RHS, ITRI 5, "
-                                       f"LSQR eps {eps:g}",
+                                       + (f"BiCGSTAB-Jacobi tol {eps:g}" if args.solver == "bicgstab"
+                                          else f"LSQR eps {eps:g}"),
                            "precision": "mixed", "parallelism": "bodies split over ranks" if world > 1 else
                            "single GPU", "l2": "inputs larger than L2 (waves of tens of GB), no flush",
                            "warmup": f"{args.warmup} x the first {len(warm)} bodies"},
@@ -361,6 +363,7 @@ def run_large(args):
     C = A.Context(0)
     C.set_mesh(m)
     C.set_problem(A.STOKES, [1, 2], A.dirichlet_known(A.STOKES, 2), itri=5)
+    C.set_solver(A.SOLVER_BICGSTAB if args.solver == "bicgstab" else A.SOLVER_LSQR)
     ne = len(m["etype"])
     workload = (f"superellipsoid a=1 b=0.5 c=0.25 e1=0.6 e2=1.4, {nr}x{ns} grid ({len(body['etype'])} tri) "
                 f"in an L2 container r=200, 6 RHS, ITRI 5")
@@ -393,7 +396,8 @@ def run_large(args):
                 "value": 1000.0 / info["device_ms"], "unit": "solves/s", "n_gpus": 1, "steps": 1, "warmup": 0,
                 "ms_per_step": info["device_ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "fp32 (fp64 singular/free-term/reductions)", "data": "synthetic",
-                "config": {"workload": workload + f", LSQR eps {args.eps:g}", "unknowns": C.n,
+                "config": {"workload": workload + (f", BiCGSTAB-Jacobi tol {args.eps:g}" if args.solver == "bicgstab"
+                                                   else f", LSQR eps {args.eps:g}"), "unknowns": C.n,
                            "packed_matrix_gb": alg / 1e9, "l2": "inputs larger than L2, no flush"},
                 "assemble_ms": info["assemble_ms"], "rhs_ms": info["rhs_ms"], "solve_ms": info["solve_ms"],
                 "nit": [int(v) for v in nit], "istop": info["istop"],
@@ -403,8 +407,8 @@ def run_large(args):
                              "achieved": alg / (av_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                              "frac": alg / (av_ms * 1e-3) / 1e9 / peak, "traffic": None, "peak_source": peak_kind,
                              "algorithmic_bytes_per_launch": alg,
-                             "other_sweep": {"kernel": "k_atup", "achieved": alg / (atu_ms * 1e-3) / 1e9,
-                                             "frac": alg / (atu_ms * 1e-3) / 1e9 / peak}},
+                             "other_sweep": ({"kernel": "k_atup", "achieved": alg / (atu_ms * 1e-3) / 1e9,
+                                              "frac": alg / (atu_ms * 1e-3) / 1e9 / peak} if atu_ms > 0 else None)},
                 "clocks": clk.summary(), "gpu_launches": kt["launches"], "host_s": t1 - t0}
         print(json.dumps(line), flush=True)
         C.close()
