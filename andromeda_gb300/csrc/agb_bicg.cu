@@ -16,8 +16,9 @@
 // W[a][c][i] = fp32(p[3i+a][c] / d[3i+a]), so k_avp computes A D^-1 p from the
 // FP32 blocks; vectors, inner products and scalars are FP64, reduced in a fixed
 // order (bitwise reproducible).  Each iteration: two k_avp sweeps and six
-// vector kernels of a few MB.  Both sweeps of the first iteration of every 8
-// are timed with CUDA events into the A*V counters (agb_kernel_times).
+// vector kernels of a few MB, replayed eight at a time from a CUDA graph.  Both
+// sweeps of the first iteration of every replay are timed with CUDA events into
+// the A*V counters (agb_kernel_times).
 #include "agb_lsqr.cuh"
 #include "agb_sweeps.cuh"
 #include <algorithm>
@@ -346,41 +347,57 @@ bool DenseLsqr::bicgstab(const double* b_dev, double* x_dev, double tol, int max
     for (int i = 0; i < 4 * 32; ++i) BCK(cudaEventCreate(&pev[i]));
     pev_ready = true;
   }
-  // live timing of both sweeps of the first iteration of every 8 (events on the solver stream)
-  auto sweep = [&](double* Yout, bool timed, int e) {
-    if (timed) cudaEventRecord(pev[e], stream);
-    launch_avp(*this, sc0, Yout);
-    if (timed) cudaEventRecord(pev[e + 1], stream);
-    ++launches;
+  // eight iterations captured in one CUDA graph and replayed until no right-hand
+  // side is active; both sweeps of the first iteration of each replay are timed
+  // (events on the solver stream); sweeps after the last convergence read nothing
+  constexpr int CE = 8;
+  auto iteration = [&](bool timed) {
+    k_bg_p<<<BG_BLOCKS, BG_THREADS, 0, stream>>>(m, pk_ldp, R, P, V, dinv, bsc, Vp);
+    if (timed) cudaEventRecordWithFlags(pev[0], stream, cudaEventRecordExternal);
+    launch_avp(*this, sc0, V, nactive);                                 // v = A D^-1 p
+    if (timed) cudaEventRecordWithFlags(pev[1], stream, cudaEventRecordExternal);
+    k_bg_dots<<<BG_BLOCKS, BG_THREADS, 0, stream>>>(m, Rt, V, nullptr, nullptr, bg_part);
+    k_bg_alpha<<<1, 32, 0, stream>>>(bg_part, bsc);
+    k_bg_s<<<BG_BLOCKS, BG_THREADS, 0, stream>>>(m, pk_ldp, R, V, dinv, bsc, S, Vp, bg_part);
+    k_bg_scheck<<<1, 32, 0, stream>>>(bg_part, tol, bsc);
+    if (timed) cudaEventRecordWithFlags(pev[2], stream, cudaEventRecordExternal);
+    launch_avp(*this, sc0, T, nactive);                                 // t = A D^-1 s
+    if (timed) cudaEventRecordWithFlags(pev[3], stream, cudaEventRecordExternal);
+    k_bg_dots<<<BG_BLOCKS, BG_THREADS, 0, stream>>>(m, T, S, T, T, bg_part);
+    k_bg_omega<<<1, 32, 0, stream>>>(bg_part, bsc);
+    k_bg_xr<<<BG_BLOCKS, BG_THREADS, 0, stream>>>(m, P, S, T, dinv, Rt, bsc, X, R, bg_part);
+    k_bg_end<<<1, 32, 0, stream>>>(bg_part, tol, maxit, bsc, nactive);
   };
-  int it = 0;
-  while (it < maxit) {
-    const int chunk = std::min(8, maxit - it);
-    for (int j = 0; j < chunk; ++j) {
-      k_bg_p<<<BG_BLOCKS, BG_THREADS, 0, stream>>>(m, pk_ldp, R, P, V, dinv, bsc, Vp);
-      sweep(V, j == 0, 0);                                              // v = A D^-1 p
-      k_bg_dots<<<BG_BLOCKS, BG_THREADS, 0, stream>>>(m, Rt, V, nullptr, nullptr, bg_part);
-      k_bg_alpha<<<1, 32, 0, stream>>>(bg_part, bsc);
-      k_bg_s<<<BG_BLOCKS, BG_THREADS, 0, stream>>>(m, pk_ldp, R, V, dinv, bsc, S, Vp, bg_part);
-      k_bg_scheck<<<1, 32, 0, stream>>>(bg_part, tol, bsc);
-      sweep(T, j == 0, 2);                                              // t = A D^-1 s
-      k_bg_dots<<<BG_BLOCKS, BG_THREADS, 0, stream>>>(m, T, S, T, T, bg_part);
-      k_bg_omega<<<1, 32, 0, stream>>>(bg_part, bsc);
-      k_bg_xr<<<BG_BLOCKS, BG_THREADS, 0, stream>>>(m, P, S, T, dinv, Rt, bsc, X, R, bg_part);
-      k_bg_end<<<1, 32, 0, stream>>>(bg_part, tol, maxit, bsc, nactive);
-      launches += 9;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  BCK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+  for (int j = 0; j < CE; ++j) iteration(j == 0);
+  BCK(cudaStreamEndCapture(stream, &graph));
+  if (cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    err = "BiCGSTAB: graph instantiation failed";
+    return false;
+  }
+  bool ok = true;
+  for (int it = 0; it < maxit + CE; it += CE) {
+    if (cudaGraphLaunch(gexec, stream) != cudaSuccess) { ok = false; break; }
+    launches += 11L * CE;
+    if (cudaMemcpyAsync(h_nactive, nactive, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+        cudaStreamSynchronize(stream) != cudaSuccess) {
+      ok = false;
+      break;
     }
-    BCK(cudaGetLastError());
-    it += chunk;
-    BCK(cudaMemcpyAsync(h_nactive, nactive, sizeof(int), cudaMemcpyDeviceToHost, stream));
-    BCK(cudaStreamSynchronize(stream));
-    {
-      float a = 0.f, b = 0.f;
-      if (cudaEventElapsedTime(&a, pev[0], pev[1]) == cudaSuccess) { t_av += a; ++n_av; }
-      if (cudaEventElapsedTime(&b, pev[2], pev[3]) == cudaSuccess) { t_av += b; ++n_av; }
-    }
+    float a = 0.f, b = 0.f;
+    if (cudaEventElapsedTime(&a, pev[0], pev[1]) == cudaSuccess) { t_av += a; ++n_av; }
+    if (cudaEventElapsedTime(&b, pev[2], pev[3]) == cudaSuccess) { t_av += b; ++n_av; }
     (void)cudaGetLastError();  // a timing query must not leak into the error checks
     if (*h_nactive == 0) break;
+  }
+  cudaGraphExecDestroy(gexec);
+  cudaGraphDestroy(graph);
+  if (!ok) {
+    err = std::string("BiCGSTAB iterations: ") + cudaGetErrorString(cudaGetLastError());
+    return false;
   }
   k_bg_out<<<cdivu((long long)m * 8, 256), 256, 0, stream>>>(pk_ne, k, X, x_dev);
   ++launches;

@@ -100,8 +100,9 @@ struct DenseLsqr {
   void release();
 };
 
-// Y = A W over the packed layout (k_avp with the gammas of sc), W the solver's Vp.
-void launch_avp(const DenseLsqr& L, const LsqrScalars* sc, double* Y);
+// Y = A W over the packed layout (k_avp with the gammas of sc), W the solver's Vp;
+// nothing while *gate == 0 (device counter of active right-hand sides).
+void launch_avp(const DenseLsqr& L, const LsqrScalars* sc, double* Y, const int* gate);
 
 bool crs_lsqr_precon(int m, int n, int64_t nnz, double* q, const int64_t* ia, const int* ja, double* a, std::string& err);
 bool crs_lsqr_solve(int m, int n, int64_t nnz, int& maxit, double eps, int& nit, int& ierr, const double* q,
