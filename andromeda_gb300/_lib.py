@@ -32,6 +32,9 @@ SIGNATURES = {
     "agb_set_problem": ([vp, I, I, ip, dp, D, ip, I, I], I),
     "agb_get_geometry": ([vp, dp, dp, dp], I),
     "agb_set_integration": ([vp, I, I, D, I], I),
+    "agb_set_solver": ([vp, I], I),
+    "agb_surface_pressure": ([vp, dp, dp, dp], I),
+    "agb_domain_values": ([vp, I, dp, dp, dp, dp, dp], I),
     "agb_system_size": ([vp, PI, PI], I),
     "agb_assemble": ([vp, I], I),
     "agb_get_system": ([vp, I, vp, vp], I),

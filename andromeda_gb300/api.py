@@ -22,6 +22,7 @@ from ._lib import AgbError, load
 
 LAPLACE, STOKES = 1, 2
 FP64, MIXED, MATRIX_FREE = 0, 1, 2
+SOLVER_LSQR, SOLVER_BICGSTAB = 0, 1
 BC_FUNCTION, BC_FLUX, BC_CONTACT = 1, 2, 3
 
 
@@ -127,6 +128,31 @@ class Context:
         near-singular rule (near_depth levels).  Clears the assembled system."""
         self._ck(self._L.agb_set_integration(self.h, int(sing_mode), int(rec_depth), float(near_eta),
                                              int(near_depth)))
+
+    def set_solver(self, solver):
+        """SOLVER_LSQR (default, lsqr_solve) or SOLVER_BICGSTAB (the LIS path's
+        BiCGSTAB with the Jacobi preconditioner; packed mixed Stokes systems)."""
+        self._ck(self._L.agb_set_solver(self.h, int(solver)))
+
+    def surface_pressure(self, u, q):
+        """Pressure at the element centroids (pressureStokes) of velocity u (3, nnodes)
+        and traction q (3, nelem); elements of no subdomain wall get 0."""
+        p = np.zeros(self.nelem)
+        self._ck(self._L.agb_surface_pressure(self.h, np.ascontiguousarray(u, dtype=np.float64).ravel(),
+                                              np.ascontiguousarray(q, dtype=np.float64).ravel(), p))
+        return p
+
+    def domain_values(self, points, u, q):
+        """Field at points inside the domain: Stokes (npts, 4) velocity and pressure,
+        Laplace (npts,); and the reference's check of each point."""
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        n = len(pts)
+        nv = 4 if self.kind == STOKES else 1
+        out = np.zeros(n * nv)
+        err = np.zeros(n)
+        self._ck(self._L.agb_domain_values(self.h, n, pts.ravel(), np.ascontiguousarray(u, dtype=np.float64).ravel(),
+                                           np.ascontiguousarray(q, dtype=np.float64).ravel(), out, err))
+        return (out.reshape(n, 4) if nv == 4 else out), err
 
     def geometry(self):
         nrm = np.zeros(3 * self.nelem)
@@ -274,7 +300,7 @@ def solv_eqn_fm(f, q, b, pret=2, prep=2):
 
 
 def batch_resistance(meshes, particle_wall=1, outer_wall=2, itri=5, maxit=0, eps=1e-7, mem_gb=0.0, autotune=True,
-                     device=0, ctx=None):
+                     device=0, ctx=None, solver=None):
     """Mixed-precision resistance tensors of many bodies in one batched call.
 
     ``meshes``: list of particle-in-container triangle meshes (the dict layout
@@ -282,10 +308,14 @@ def batch_resistance(meshes, particle_wall=1, outer_wall=2, itri=5, maxit=0, eps
     istop[nb,6], stats) with R[i, r] = (F, T) on particle i for rigid motion r
     of its container.  ``ctx``: a :class:`Context` to run on (its per-body
     contexts are kept for later calls); a new one on ``device`` otherwise.
+    ``solver``: SOLVER_LSQR / SOLVER_BICGSTAB for this call and the context's
+    later ones (None: the context's setting, LSQR by default).
     """
     own = ctx is None
     C_ = Context(device) if own else ctx
     try:
+        if solver is not None:
+            C_.set_solver(solver)
         nb = len(meshes)
         node_off = np.zeros(nb + 1, np.int32)
         elem_off = np.zeros(nb + 1, np.int32)

@@ -36,6 +36,7 @@ struct agb_context {
   // problem
   int kind = 0, neq = 0;
   IntegOpt iopt;  // triangle integration options (agb_set_integration)
+  int solver = AGB_SOLVER_LSQR;  // agb_set_solver
   MfOp mfop;                   // matrix-free operator (AGB_MATRIX_FREE)
   float* d_self6 = nullptr;
   double* d_lu = nullptr;      // column-major LU factors of the unscaled FP64 system (agb_solve_lu)
@@ -408,6 +409,18 @@ int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int r
       return fail(c, AGB_ERR_CUDA, "lsqr setup: " + c->lsqr.err);
   }
   std::vector<int> nt(nrhs, 0), is(nrhs, 0);
+  if (c->solver == AGB_SOLVER_BICGSTAB) {
+    if (!c->lsqr.packed)
+      return fail(c, AGB_ERR_UNSUPPORTED, "BiCGSTAB needs the packed mixed system (Stokes, velocity known on every "
+                                          "wall, triangles, default integration, AGB_MIXED)");
+    if (!c->lsqr.bicgstab(c->d_rhs, d_x, eps, maxit, nt.data(), is.data()))
+      return fail(c, AGB_ERR_CUDA, "bicgstab: " + c->lsqr.err);
+    for (int r = 0; r < nrhs; ++r) {
+      if (nit) nit[r] = nt[r];
+      if (istop) istop[r] = is[r];
+    }
+    return AGB_OK;
+  }
   for (int pass = 0; pass <= refine; ++pass) {
     if (!c->lsqr.solve(c->d_rhs, d_x, c->d_q, eps, maxit, nt.data(), is.data(), nullptr, 8, x0_zero && pass == 0))
       return fail(c, AGB_ERR_CUDA, "lsqr: " + c->lsqr.err);
@@ -669,6 +682,14 @@ int agb_set_integration(agb_context* c, int sing_mode, int rec_depth, double nea
   c->iopt.near_eta = near_eta;
   c->iopt.near_depth = near_depth;
   c->assembled = false;
+  return AGB_OK;
+}
+
+int agb_set_solver(agb_context* c, int solver) {
+  if (!c) return fail(c, AGB_ERR_ARG, "agb_set_solver: no context");
+  if (solver != AGB_SOLVER_LSQR && solver != AGB_SOLVER_BICGSTAB)
+    return fail(c, AGB_ERR_ARG, "solver must be AGB_SOLVER_LSQR or AGB_SOLVER_BICGSTAB");
+  c->solver = solver;
   return AGB_OK;
 }
 
@@ -1072,6 +1093,74 @@ int agb_kernel_times(agb_context* c, int reset, double* out) {
   return AGB_OK;
 }
 
+// Post-processing of a solved field: the surface pressure and the values at
+// points inside the domain (FP64, the element integrals of the general path).
+namespace {
+struct PostBufs {
+  double *u = nullptr, *q = nullptr, *pts = nullptr, *out = nullptr, *err = nullptr;
+  ~PostBufs() { cudaFree(u); cudaFree(q); cudaFree(pts); cudaFree(out); cudaFree(err); }
+};
+// q[comp][nelem] (mesh order) -> [comp][ne] (subdomain order), uploaded with u
+int post_upload(agb_context* c, PostBufs& B, const double* u, const double* q) {
+  const int nc = c->neq;
+  std::vector<double> qs((size_t)nc * c->ne);
+  for (int comp = 0; comp < nc; ++comp)
+    for (int pos = 0; pos < c->ne; ++pos) qs[(size_t)comp * c->ne + pos] = q[(size_t)comp * c->nelem + c->elemList[pos]];
+  CUDA_OR_FAIL(c, cudaMalloc(&B.u, (size_t)nc * c->nnodes * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMalloc(&B.q, qs.size() * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMemcpy(B.u, u, (size_t)nc * c->nnodes * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_OR_FAIL(c, cudaMemcpy(B.q, qs.data(), qs.size() * sizeof(double), cudaMemcpyHostToDevice));
+  return AGB_OK;
+}
+double osem_pi() { return (double)std::atan(1.0f) * 4.0 * 8.0; }  // the reference's ATAN(1.0) is single precision
+}  // namespace
+
+int agb_surface_pressure(agb_context* c, const double* u, const double* q, double* p) {
+  int rc = check_ctx(c, true);
+  if (rc) return rc;
+  if (!u || !q || !p) return fail(c, AGB_ERR_ARG, "agb_surface_pressure: missing arrays");
+  if (c->kind != AGB_STOKES) return fail(c, AGB_ERR_UNSUPPORTED, "agb_surface_pressure: Stokes problems only");
+  cudaSetDevice(c->device);
+  PostBufs B;
+  if ((rc = post_upload(c, B, u, q))) return rc;
+  CUDA_OR_FAIL(c, cudaMalloc(&B.out, (size_t)c->ne * sizeof(double)));
+  CUDA_OR_FAIL(c, surface_pressure(c->ne, c->d_geom, c->rule, c->iqud, c->iopt, B.u, c->nnodes, B.q, c->diff,
+                                   osem_pi(), B.out, c->stream));
+  c->nlaunch += 1;
+  std::vector<double> ps(c->ne);
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(ps.data(), B.out, ps.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  std::fill(p, p + c->nelem, 0.0);
+  for (int pos = 0; pos < c->ne; ++pos) p[c->elemList[pos]] = ps[pos];
+  return AGB_OK;
+}
+
+int agb_domain_values(agb_context* c, int npts, const double* pts, const double* u, const double* q, double* out,
+                      double* err) {
+  int rc = check_ctx(c, true);
+  if (rc) return rc;
+  if (npts < 0 || (npts > 0 && (!pts || !u || !q || !out || !err)))
+    return fail(c, AGB_ERR_ARG, "agb_domain_values: missing arrays");
+  if (npts == 0) return AGB_OK;
+  for (int64_t i = 0; i < 3 * (int64_t)npts; ++i)
+    if (!std::isfinite(pts[i])) return fail(c, AGB_ERR_ARG, "agb_domain_values: a point coordinate is not finite");
+  cudaSetDevice(c->device);
+  PostBufs B;
+  if ((rc = post_upload(c, B, u, q))) return rc;
+  const int nv = (c->kind == AGB_STOKES) ? 4 : 1;
+  CUDA_OR_FAIL(c, cudaMalloc(&B.pts, 3 * (size_t)npts * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMalloc(&B.out, (size_t)nv * npts * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMalloc(&B.err, (size_t)npts * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMemcpy(B.pts, pts, 3 * (size_t)npts * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_OR_FAIL(c, domain_values(c->kind == AGB_STOKES, c->ne, c->d_geom, c->rule, c->iqud, c->iopt, npts, B.pts, c->d_xyz, B.u,
+                                c->nnodes, B.q, c->diff, osem_pi(), B.out, B.err, c->stream));
+  c->nlaunch += 1;
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(out, B.out, (size_t)nv * npts * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(err, B.err, (size_t)npts * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  return AGB_OK;
+}
+
 int agb_integral_matrices(agb_context* c, double* T, double* G, double* errs) {
   int rc = check_ctx(c, true);
   if (rc) return rc;
@@ -1263,7 +1352,8 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
   auto solver_bytes = [&](int i) {
     const BatchSlot& b = slots[i];
     const double mpad = std::ceil(b.m / 256.0) * 256.0;
-    return mpad * 8 * 12.0 + (double)b.lda * 8 * (8 * 3 + 4 + 8 * 8) + 65536.0;
+    const double bicg = (c->solver == AGB_SOLVER_BICGSTAB) ? mpad * 8 * 8 * 7.0 + mpad * 8 : 0.0;
+    return mpad * 8 * 12.0 + (double)b.lda * 8 * (8 * 3 + 4 + 8 * 8) + 65536.0 + bicg;
   };
   double budget = mem_gb * 1e9;
   if (budget <= 0.0) {
@@ -1420,14 +1510,18 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
     cudaFreeAsync(d_nm, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return bail(AGB_ERR_CUDA, "assembly of the wave");
     const auto tb = clk::now();
-    if (autotune && !tuned) {
+    if (autotune && !tuned && c->solver == AGB_SOLVER_LSQR) {
       std::string rep, err;
       if (!batch_autotune(bodies, st, tune, rep, err)) return bail(AGB_ERR_CUDA, "autotune: " + err);
       tuned = true;
     }
     std::vector<int> nv, iv;
     std::string err;
-    if (!batch_lsqr_solve(bodies, 6, eps, maxit, tune, st, nv, iv, &bst, err)) return bail(AGB_ERR_CUDA, "solve: " + err);
+    if (c->solver == AGB_SOLVER_BICGSTAB) {
+      if (!batch_bicgstab_solve(bodies, 6, eps, maxit, st, nv, iv, &bst, err)) return bail(AGB_ERR_CUDA, "solve: " + err);
+    } else if (!batch_lsqr_solve(bodies, 6, eps, maxit, tune, st, nv, iv, &bst, err)) {
+      return bail(AGB_ERR_CUDA, "solve: " + err);
+    }
     const auto tc = clk::now();
     for (size_t t = 0; t < w.size(); ++t) {
       const BatchSlot& b = slots[w[t]];

@@ -51,6 +51,23 @@ __device__ __forceinline__ bool mbar_wait_ok(uint64_t* bar, uint32_t parity, int
 __device__ __forceinline__ void mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* errflag) {
   (void)mbar_wait_ok(bar, parity, errflag);
 }
+// Before a CTA exits: wait, bounded but without the early exit on the error
+// flag, for the copies of the last stages of a ring of nslot slots (stage k
+// lands on full[k % nslot], phase parity (k / nslot) & 1).  On the normal path
+// the consumers already waited for every one of these phases, so each wait
+// returns at once; after a wait that gave up, it keeps the CTA alive until its
+// own copies have landed in its shared memory.
+__device__ __forceinline__ void mbar_drain(uint64_t* full, int nslot, int nst, int* errflag) {
+  for (int k = nst > nslot ? nst - nslot : 0; k < nst; ++k) {
+    uint32_t tries = 0;
+    while (!mbar_try_wait(&full[k % nslot], (uint32_t)((k / nslot) & 1))) {
+      if (++tries > (1u << 22)) {
+        if (errflag) atomicExch(errflag, 1);
+        break;
+      }
+    }
+  }
+}
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar) {
   asm volatile(

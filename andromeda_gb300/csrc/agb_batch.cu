@@ -57,6 +57,12 @@ struct GDesc {  // CUtensorMap members keep the 64-byte alignment TMA needs
   int m, n, k, itnlim;
   int cblocks, zgroups, rpg;
   int nb_b, nb_av, nb_red, nb_upd;
+  // BiCGSTAB (batch_bicgstab_solve): vectors [mpad][8] in the row numbering 3i+a,
+  // 1/diag(A), a second partial-sum array, the scalars; V is Y; sc0 zero gammas
+  const float* A;
+  double *Rb, *Rt, *Pb, *Sb, *Tb, *Xb, *dinv, *part2;
+  BicgScalars* bs;
+  const LsqrScalars* sc0;
 };
 
 struct GOffsets {
@@ -264,6 +270,255 @@ __global__ void g_fill(int* p, int n, int v) {
 }
 
 // ---------------------------------------------------------------------------
+// Batched BiCGSTAB with the Jacobi preconditioner (the solver of the
+// reference's LIS path; the recurrence of DenseLsqr::bicgstab, agb_bicg.cu),
+// every kernel one launch over the tiles of all systems.  Element-wise kernels
+// use the init tiles (mpad * 8 / 256 per system): t = 8 u + c, row u = 3i+a.
+// ---------------------------------------------------------------------------
+// per-CTA sums of 8 interleaved columns of v (lanes with equal c are 8 apart)
+__device__ __forceinline__ void block_sum8(double v, double* __restrict__ out) {
+  __shared__ double sQ[BT / 32][K8];
+  v += __shfl_xor_sync(0xffffffffu, v, 8);
+  v += __shfl_xor_sync(0xffffffffu, v, 16);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();  // sQ may still be read by a previous call in this kernel
+  if (lane < K8) sQ[warp][lane] = v;
+  __syncthreads();
+  if (threadIdx.x < K8) {
+    double a = 0.0;
+    for (int w = 0; w < BT / 32; ++w) a += sQ[w][threadIdx.x];
+    out[threadIdx.x] = a;
+  }
+}
+
+__global__ void __launch_bounds__(BT) gb_diag(const GDesc* __restrict__ D, const int* __restrict__ off, int nb,
+                                             int* __restrict__ bad) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  const GDesc& d = D[bi];
+  const int64_t u = (int64_t)(blockIdx.x - off[bi]) * BT + threadIdx.x;
+  if (u >= d.m) return;
+  const int i = (int)(u / 3), a = (int)(u % 3);
+  const double g = (double)d.A[pk_idx(i, sym6(a, a), i, d.pk_ldp)];
+  if (g == 0.0 || !isfinite(g)) {
+    atomicExch(bad, 1);
+    d.dinv[u] = 0.0;
+  } else {
+    d.dinv[u] = 1.0 / g;
+  }
+}
+
+// R = Rt = b, P = V = X = 0; partial ||b||^2
+__global__ void __launch_bounds__(BT) gb_init(const GDesc* __restrict__ D, const int* __restrict__ off, int nb) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  const GDesc& d = D[bi];
+  const int blk = blockIdx.x - off[bi];
+  const int64_t t = (int64_t)blk * BT + threadIdx.x;
+  const int64_t u = t / K8;
+  const int c = (int)(t % K8);
+  double v = 0.0;
+  if (u < d.m && c < d.k) v = d.b[(int64_t)c * d.m + u];
+  if (u < d.mpad) {
+    d.Rb[t] = v; d.Rt[t] = v; d.Pb[t] = 0.0; d.Y[t] = 0.0; d.Xb[t] = 0.0; d.Tb[t] = 0.0;
+  }
+  block_sum8(v * v, d.part + (int64_t)blk * K8);
+}
+
+// Scalar phases, one CTA per system: 0 start, 1 alpha, 2 the test on s, 3 omega,
+// 4 end of the iteration (stopping tests, rho, activity).  Partial sums over
+// the system's init tiles in a fixed order.
+__global__ void __launch_bounds__(256) gb_scal(const GDesc* __restrict__ D, int phase, int* __restrict__ bact,
+                                              int* nactive, double tol) {
+  const int bi = blockIdx.x;
+  if (phase != 0 && !bact[bi]) return;
+  const GDesc& d = D[bi];
+  __shared__ double sred[2][256];
+  __shared__ double ssum[2][K8];
+  const int two = (phase == 3 || phase == 4) ? 2 : 1;
+  {
+    const int t = threadIdx.x, cc = t % K8;
+    for (int h = 0; h < two; ++h) {
+      const double* P = h == 0 ? d.part : d.part2;
+      double a = 0.0;
+      for (int b = t / K8; b < d.nb_b; b += 256 / K8) a += P[(int64_t)b * K8 + cc];
+      sred[h][t] = a;
+    }
+    __syncthreads();
+    if (t < K8)
+      for (int h = 0; h < two; ++h) {
+        double tot = 0.0;
+        for (int i = t; i < 256; i += K8) tot += sred[h][i];
+        ssum[h][t] = tot;
+      }
+    __syncthreads();
+  }
+  const int c = threadIdx.x;
+  if (c < K8) {
+    BicgScalars& q = d.bs[c];
+    const double s0 = ssum[0][c], s1 = ssum[1][c];
+    if (phase == 0) {
+      q.bnorm = sqrt(s0);
+      q.rho = s0;
+      q.rho_old = q.alpha = q.omega = 1.0;
+      q.relres = (q.bnorm > 0.0) ? 1.0 : 0.0;
+      q.snorm = q.relres;
+      q.its = 0;
+      q.half = 0;
+      q.active = (c < d.k && q.bnorm > 0.0) ? 1 : 0;
+      q.status = q.active ? -1 : 0;
+    } else if (q.active) {
+      if (phase == 1) {
+        if (s0 == 0.0 || !isfinite(s0)) { q.status = 2; q.active = 0; q.alpha = 0.0; }
+        else q.alpha = q.rho / s0;
+      } else if (phase == 2) {
+        q.snorm = sqrt(s0) / q.bnorm;
+        q.half = (q.snorm <= tol) ? 1 : 0;
+      } else if (phase == 3) {
+        if (!q.half) {
+          if (s1 == 0.0 || !isfinite(s1)) { q.status = 2; q.active = 0; q.omega = 0.0; }
+          else q.omega = s0 / s1;
+        }
+      } else {
+        q.its += 1;
+        if (q.half) {
+          q.relres = q.snorm; q.status = 0; q.active = 0;
+        } else {
+          q.relres = sqrt(s0) / q.bnorm;
+          if (q.relres <= tol) { q.status = 0; q.active = 0; }
+          else if (q.its >= d.itnlim) { q.status = 1; q.active = 0; }
+          else if (s1 == 0.0 || q.omega == 0.0 || !isfinite(q.relres)) { q.status = 2; q.active = 0; }
+          else { q.rho_old = q.rho; q.rho = s1; }
+        }
+      }
+    }
+  }
+  if (phase == 0 || phase == 4) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int na = 0;
+      for (int cc = 0; cc < K8; ++cc) na += d.bs[cc].active;
+      bact[bi] = na > 0;
+      if (phase == 4 && na) atomicAdd(nactive, na);
+    }
+  }
+}
+
+// p = r (first iteration) or r + beta (p - omega v); Vp[a][c][i] = fp32(p / d)
+__global__ void __launch_bounds__(BT) gb_p(const GDesc* __restrict__ D, const int* __restrict__ off, int nb,
+                                          const int* __restrict__ bact) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  if (!bact[bi]) return;
+  const GDesc& d = D[bi];
+  const int64_t t = (int64_t)(blockIdx.x - off[bi]) * BT + threadIdx.x;
+  const int64_t u = t / K8;
+  const int c = (int)(t % K8);
+  if (u >= d.m) return;
+  const BicgScalars& q = d.bs[c];
+  float w = 0.f;
+  if (q.active) {
+    const double p = (q.its > 0) ? d.Rb[t] + (q.rho / q.rho_old) * (q.alpha / q.omega) * (d.Pb[t] - q.omega * d.Y[t])
+                                 : d.Rb[t];
+    d.Pb[t] = p;
+    w = (float)(p * d.dinv[u]);
+  }
+  d.Vp[((int64_t)(u % 3) * K8 + c) * d.pk_ldp + u / 3] = w;
+}
+
+// Y (which 0) or T (which 1) = A D^-1 (p or s), gamma 0
+__global__ void __launch_bounds__(AVP_THREADS, 1) gb_avp(const GDesc* __restrict__ D, const int* __restrict__ off,
+                                                        int nb, const int* __restrict__ bact, int* errflag,
+                                                        int which) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  if (!bact[bi]) return;
+  const GDesc& d = D[bi];
+  avp_tile(&d.tm_av, &d.tm_vp, d.pk_ne, d.pk_ldp, d.sc0, which ? d.Tb : d.Y, d.Ys, d.part, errflag,
+           (int)(blockIdx.x - off[bi]));
+}
+
+// mode 0: part = r~ . v; mode 1: part = t . s, part2 = t . t
+__global__ void __launch_bounds__(BT) gb_dots(const GDesc* __restrict__ D, const int* __restrict__ off, int nb,
+                                             const int* __restrict__ bact, int mode) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  if (!bact[bi]) return;
+  const GDesc& d = D[bi];
+  const int blk = blockIdx.x - off[bi];
+  const int64_t t = (int64_t)blk * BT + threadIdx.x;
+  const bool in = t / K8 < d.m;
+  if (mode == 0) {
+    block_sum8(in ? d.Rt[t] * d.Y[t] : 0.0, d.part + (int64_t)blk * K8);
+  } else {
+    block_sum8(in ? d.Tb[t] * d.Sb[t] : 0.0, d.part + (int64_t)blk * K8);
+    block_sum8(in ? d.Tb[t] * d.Tb[t] : 0.0, d.part2 + (int64_t)blk * K8);
+  }
+}
+
+// s = r - alpha v; Vp = fp32(s / d); partial ||s||^2
+__global__ void __launch_bounds__(BT) gb_s(const GDesc* __restrict__ D, const int* __restrict__ off, int nb,
+                                          const int* __restrict__ bact) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  if (!bact[bi]) return;
+  const GDesc& d = D[bi];
+  const int blk = blockIdx.x - off[bi];
+  const int64_t t = (int64_t)blk * BT + threadIdx.x;
+  const int64_t u = t / K8;
+  const int c = (int)(t % K8);
+  double ss = 0.0;
+  if (u < d.m) {
+    const BicgScalars& q = d.bs[c];
+    float w = 0.f;
+    if (q.active) {
+      const double sv = d.Rb[t] - q.alpha * d.Y[t];
+      d.Sb[t] = sv;
+      ss = sv * sv;
+      w = (float)(sv * d.dinv[u]);
+    }
+    d.Vp[((int64_t)(u % 3) * K8 + c) * d.pk_ldp + u / 3] = w;
+  }
+  block_sum8(ss, d.part + (int64_t)blk * K8);
+}
+
+// x += alpha p/d + omega s/d; r = s - omega t; partials ||r||^2, r~ . r
+__global__ void __launch_bounds__(BT) gb_xr(const GDesc* __restrict__ D, const int* __restrict__ off, int nb,
+                                           const int* __restrict__ bact) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  if (!bact[bi]) return;
+  const GDesc& d = D[bi];
+  const int blk = blockIdx.x - off[bi];
+  const int64_t t = (int64_t)blk * BT + threadIdx.x;
+  const int64_t u = t / K8;
+  const int c = (int)(t % K8);
+  double rr = 0.0, rtr = 0.0;
+  if (u < d.m) {
+    const BicgScalars& q = d.bs[c];
+    if (q.active) {
+      const double di = d.dinv[u];
+      if (q.half) {
+        d.Xb[t] += q.alpha * (d.Pb[t] * di);
+      } else {
+        d.Xb[t] += q.alpha * (d.Pb[t] * di) + q.omega * (d.Sb[t] * di);
+        const double r = d.Sb[t] - q.omega * d.Tb[t];
+        d.Rb[t] = r;
+        rr = r * r;
+        rtr = d.Rt[t] * r;
+      }
+    }
+  }
+  block_sum8(rr, d.part + (int64_t)blk * K8);
+  block_sum8(rtr, d.part2 + (int64_t)blk * K8);
+}
+
+// x(:,c) in the unknown numbering a ne + i
+__global__ void gb_finish(const GDesc* __restrict__ D) {
+  const GDesc& d = D[blockIdx.y];
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)d.m * K8;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(t % K8);
+    if (c >= d.k) continue;
+    const int64_t u = t / K8;
+    d.x[(int64_t)c * d.n + (u % 3) * d.pk_ne + u / 3] = d.Xb[t];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
 template <typename K>
@@ -296,7 +551,8 @@ struct BatchSolver {
     h_nactive = nullptr;
   }
 
-  bool setup(const std::vector<BatchBody>& bodies, int k_, int maxit, const BatchTune& t, cudaStream_t st) {
+  bool setup(const std::vector<BatchBody>& bodies, int k_, int maxit, const BatchTune& t, cudaStream_t st,
+             bool bicg = false) {
     release();
     nb = (int)bodies.size();
     k = k_;
@@ -312,8 +568,9 @@ struct BatchSolver {
     // pool layout (bytes), every piece 256-byte aligned
     size_t bytes = 0;
     auto take = [&](size_t n) { const size_t o = bytes; bytes += (n + 255) / 256 * 256; return o; };
-    struct Offs { size_t Y, Ys, V, W, X, Vp, Zp, part, sc; };
+    struct Offs { size_t Y, Ys, V, W, X, Vp, Zp, part, sc, bg, part2, bs; };
     std::vector<Offs> po(nb);
+    const size_t o_sc0 = take(K8 * sizeof(LsqrScalars));  // zero gammas of the BiCGSTAB sweeps
     bytes_A = 0.0;
     for (int i = 0; i < nb; ++i) {
       const BatchBody& B = bodies[i];
@@ -327,7 +584,7 @@ struct BatchSolver {
       d.pk_ne = B.pk_ne;
       d.pk_ldp = B.pk_ldp;
       d.mpad = ((int64_t)B.m + 255) / 256 * 256;
-      d.itnlim = maxit > 0 ? maxit : 10 * (B.m + B.n + 50);
+      d.itnlim = maxit > 0 ? maxit : (bicg ? 1000 : 10 * (B.m + B.n + 50));
       // A^T U tiles: 256 element columns x a group of block rows
       d.cblocks = (int)cdivu(B.pk_ldp, ATUP_C);
       d.zgroups = std::max(1, (int)cdivu(B.pk_ne, std::max(tune.atup_rows, ATUP_RS)));
@@ -347,6 +604,11 @@ struct BatchSolver {
       po[i].Zp = take((size_t)d.zgroups * B.lda * K8 * sizeof(double));
       po[i].part = take((size_t)nbmax * K8 * sizeof(double));
       po[i].sc = take(K8 * sizeof(LsqrScalars));
+      if (bicg) {
+        po[i].bg = take((size_t)(6 * d.mpad * K8 + d.mpad) * sizeof(double));  // R, Rt, P, S, T, X; 1/diag
+        po[i].part2 = take((size_t)nbmax * K8 * sizeof(double));
+        po[i].bs = take(K8 * sizeof(BicgScalars));
+      }
       hoff_b[i + 1] = hoff_b[i] + d.nb_b;
       hoff_av[i + 1] = hoff_av[i] + d.nb_av;
       hoff_atu[i + 1] = hoff_atu[i] + d.cblocks * d.zgroups;
@@ -356,6 +618,7 @@ struct BatchSolver {
       if (!make_packed_map(&d.tm_av, B.A, B.pk_ldp, B.pk_ne, 6 * AVP_NB, AVP_R, err)) return false;
       if (!make_packed_map(&d.tm_atu, B.A, B.pk_ldp, B.pk_ne, 6 * (ATUP_C / 64), ATUP_RS, err)) return false;
       d.b = B.b; d.q = B.q; d.x = B.x;
+      d.A = B.A;
     }
     BCK(cudaMalloc(&pool, bytes));
     BCK(cudaMemsetAsync(pool, 0, bytes, s));
@@ -366,6 +629,15 @@ struct BatchSolver {
       d.V = (double*)(p + po[i].V); d.W = (double*)(p + po[i].W); d.X = (double*)(p + po[i].X);
       d.Vp = (float*)(p + po[i].Vp); d.Zp = (double*)(p + po[i].Zp); d.part = (double*)(p + po[i].part);
       d.sc = (LsqrScalars*)(p + po[i].sc);
+      d.sc0 = (const LsqrScalars*)(p + o_sc0);
+      if (bicg) {
+        double* g = (double*)(p + po[i].bg);
+        const int64_t mv = d.mpad * K8;
+        d.Rb = g; d.Rt = g + mv; d.Pb = g + 2 * mv; d.Sb = g + 3 * mv; d.Tb = g + 4 * mv; d.Xb = g + 5 * mv;
+        d.dinv = g + 6 * mv;
+        d.part2 = (double*)(p + po[i].part2);
+        d.bs = (BicgScalars*)(p + po[i].bs);
+      }
       // the pool is zeroed: the pad columns pk_ne..pk_ldp-1 of Vp stay zero
       if (!make_tensor_map_2d(&d.tm_vp, d.Vp, d.pk_ldp, 3 * K8, AVP_BC, 3 * K8, err)) return false;
     }
@@ -511,6 +783,135 @@ bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, i
       int mx = 0;
       for (int c = 0; c < k; ++c) mx = std::max(mx, nit[(size_t)i * k + c]);
       st->bytes_av += (double)mx * 24.0 * (double)S.hd[i].pk_ne * (double)S.hd[i].pk_ne;
+    }
+  }
+  return true;
+}
+
+bool batch_bicgstab_solve(const std::vector<BatchBody>& bodies, int k, double tol, int maxit, cudaStream_t s,
+                          std::vector<int>& nit, std::vector<int>& status, BatchStats* st, std::string& err) {
+  BatchSolver S;
+  if (!S.setup(bodies, k, maxit, BatchTune(), s, true)) { err = S.err; return false; }
+  BCK(set_smem(gb_avp, AVP_SMEM));
+  const int nb = S.nb;
+  int itmax = 0;
+  for (const auto& d : S.hd) itmax = std::max(itmax, d.itnlim);
+  long launches = 0;
+  BCK(cudaMemsetAsync(S.nactive, 0, sizeof(int), s));
+  gb_diag<<<S.hoff_b[nb], BT, 0, s>>>(S.d_desc, S.off.b, nb, S.nactive);
+  int bad = 0;
+  BCK(cudaMemcpyAsync(&bad, S.nactive, sizeof(int), cudaMemcpyDeviceToHost, s));
+  BCK(cudaStreamSynchronize(s));
+  if (bad) {
+    err = "BiCGSTAB: a zero or non-finite diagonal entry (the Jacobi preconditioner needs every diagonal)";
+    return false;
+  }
+  gb_init<<<S.hoff_b[nb], BT, 0, s>>>(S.d_desc, S.off.b, nb);
+  gb_scal<<<nb, 256, 0, s>>>(S.d_desc, 0, S.bact, S.nactive, tol);
+  launches += 3;
+  BCK(cudaGetLastError());
+  const int ce = 8;
+  std::vector<cudaEvent_t> ev(4 * ce, nullptr);
+  for (auto& e : ev) BCK(cudaEventCreate(&e));
+  const unsigned nbv = S.hoff_b[nb], nav = S.hoff_av[nb];
+  auto iteration = [&](int i) {
+    gb_p<<<nbv, BT, 0, s>>>(S.d_desc, S.off.b, nb, S.bact);
+    cudaEventRecordWithFlags(ev[4 * i], s, cudaEventRecordExternal);
+    gb_avp<<<nav, AVP_THREADS, AVP_SMEM, s>>>(S.d_desc, S.off.av, nb, S.bact, S.errflag, 0);
+    cudaEventRecordWithFlags(ev[4 * i + 1], s, cudaEventRecordExternal);
+    gb_dots<<<nbv, BT, 0, s>>>(S.d_desc, S.off.b, nb, S.bact, 0);
+    gb_scal<<<nb, 256, 0, s>>>(S.d_desc, 1, S.bact, S.nactive, tol);
+    gb_s<<<nbv, BT, 0, s>>>(S.d_desc, S.off.b, nb, S.bact);
+    gb_scal<<<nb, 256, 0, s>>>(S.d_desc, 2, S.bact, S.nactive, tol);
+    cudaEventRecordWithFlags(ev[4 * i + 2], s, cudaEventRecordExternal);
+    gb_avp<<<nav, AVP_THREADS, AVP_SMEM, s>>>(S.d_desc, S.off.av, nb, S.bact, S.errflag, 1);
+    cudaEventRecordWithFlags(ev[4 * i + 3], s, cudaEventRecordExternal);
+    gb_dots<<<nbv, BT, 0, s>>>(S.d_desc, S.off.b, nb, S.bact, 1);
+    gb_scal<<<nb, 256, 0, s>>>(S.d_desc, 3, S.bact, S.nactive, tol);
+    gb_xr<<<nbv, BT, 0, s>>>(S.d_desc, S.off.b, nb, S.bact);
+    cudaMemsetAsync(S.nactive, 0, sizeof(int), s);
+    gb_scal<<<nb, 256, 0, s>>>(S.d_desc, 4, S.bact, S.nactive, tol);
+  };
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  bool ok = true;
+  auto cleanup = [&]() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    for (auto& e : ev) if (e) cudaEventDestroy(e);
+  };
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) ok = false;
+  if (ok) {
+    for (int i = 0; i < ce; ++i) iteration(i);
+    if (cudaStreamEndCapture(s, &graph) != cudaSuccess) ok = false;
+  }
+  if (ok && cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) ok = false;
+  if (!ok) {
+    err = std::string("batch BiCGSTAB graph capture: ") + cudaGetErrorString(cudaGetLastError());
+    cleanup();
+    return false;
+  }
+  std::vector<int> hb(nb);
+  if (cudaMemcpyAsync(hb.data(), S.bact, nb * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess) {
+    err = "batch BiCGSTAB: initial state";
+    cleanup();
+    return false;
+  }
+  int act = 0;
+  for (int v : hb) act += v;
+  long iters = 0;
+  double av_ms = 0.0;
+  long nav_t = 0;
+  while (act > 0 && iters < (long)itmax + ce) {
+    if (cudaGraphLaunch(gexec, s) != cudaSuccess) { ok = false; break; }
+    launches += 11L * ce;
+    cudaMemcpyAsync(S.h_nactive, S.nactive, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) { ok = false; break; }
+    for (int i = 0; i < ce; ++i) {
+      float a = 0.f, b = 0.f;
+      if (cudaEventElapsedTime(&a, ev[4 * i], ev[4 * i + 1]) == cudaSuccess) { av_ms += a; ++nav_t; }
+      if (cudaEventElapsedTime(&b, ev[4 * i + 2], ev[4 * i + 3]) == cudaSuccess) { av_ms += b; ++nav_t; }
+    }
+    (void)cudaGetLastError();
+    iters += ce;
+    act = *S.h_nactive;
+  }
+  cleanup();
+  if (!ok) {
+    err = std::string("batch BiCGSTAB iterations: ") + cudaGetErrorString(cudaGetLastError());
+    return false;
+  }
+  int mmax = 1;
+  for (const auto& d : S.hd) mmax = std::max(mmax, d.m * K8);
+  gb_finish<<<dim3(std::min<unsigned>(cdivu(mmax, 256), 1024), nb), 256, 0, s>>>(S.d_desc);
+  launches += 1;
+  std::vector<BicgScalars> hs((size_t)nb * K8);
+  for (int i = 0; i < nb; ++i)
+    BCK(cudaMemcpyAsync(hs.data() + (size_t)i * K8, S.hd[i].bs, K8 * sizeof(BicgScalars), cudaMemcpyDeviceToHost, s));
+  int hflag = 0;
+  BCK(cudaMemcpyAsync(&hflag, S.errflag, sizeof(int), cudaMemcpyDeviceToHost, s));
+  BCK(cudaStreamSynchronize(s));
+  BCK(cudaGetLastError());
+  if (hflag) { err = "a bounded barrier wait in a batched sweep gave up"; return false; }
+  nit.assign((size_t)nb * k, 0);
+  status.assign((size_t)nb * k, 0);
+  for (int i = 0; i < nb; ++i)
+    for (int c = 0; c < k; ++c) {
+      const BicgScalars& q = hs[(size_t)i * K8 + c];
+      nit[(size_t)i * k + c] = q.its;
+      status[(size_t)i * k + c] = q.status < 0 ? 1 : q.status;
+    }
+  if (st) {
+    st->av_ms += av_ms;
+    st->av_launches += nav_t;
+    st->launches += launches;
+    st->iterations = std::max(st->iterations, iters);
+    st->av_rows = AVP_R;
+    for (int i = 0; i < nb; ++i) {
+      int mx = 0;
+      for (int c = 0; c < k; ++c) mx = std::max(mx, nit[(size_t)i * k + c]);
+      st->bytes_av += 2.0 * (double)mx * 24.0 * (double)S.hd[i].pk_ne * (double)S.hd[i].pk_ne;
     }
   }
   return true;

@@ -44,6 +44,14 @@ bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, i
                       cudaStream_t s, std::vector<int>& nit, std::vector<int>& istop, BatchStats* st,
                       std::string& err);
 
+// BiCGSTAB with the Jacobi preconditioner (the solver of the reference's LIS path,
+// as DenseLsqr::bicgstab) on all systems together: x0 = 0, stop at
+// ||b - A x|| <= tol ||b|| or maxit iterations (0: 1000).  b: [k][m] in the row
+// numbering 3i+a; x: [k][n] in the unknown numbering a ne + i (as
+// batch_lsqr_solve).  status per column: 0 converged, 1 iteration limit, 2 breakdown.
+bool batch_bicgstab_solve(const std::vector<BatchBody>& bodies, int k, double tol, int maxit, cudaStream_t s,
+                          std::vector<int>& nit, std::vector<int>& status, BatchStats* st, std::string& err);
+
 // Times the candidate row groups of the A^T*U sweep on these systems (a few
 // launches each, CUDA events) and returns the fastest; `report` lists the
 // candidates and their times.  Results are cached per (systems, total size)

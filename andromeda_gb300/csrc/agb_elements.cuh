@@ -143,8 +143,10 @@ __device__ __forceinline__ void quad_map(const double (*P)[3], double gii, doubl
 }
 
 // ---- Laplace ---------------------------------------------------------------
+// qdiv > 0: a regular quad is integrated over qdiv x qdiv cells instead of the
+// edge-length subdivision (1: the regular branch of Quad_BEMInt, lib_int.f90:329).
 __device__ inline LapElem lap_element(const ElemGeom& E, const double* s, int isrc, const double* rl, const double* rw,
-                                      int Q, int iqud, const IntegOpt& opt) {
+                                      int Q, int iqud, const IntegOpt& opt, int qdiv = 0) {
   LapElem o;
   o.g = 0.0;
   o.h[0] = o.h[1] = o.h[2] = o.h[3] = 0.0;
@@ -186,7 +188,7 @@ __device__ inline LapElem lap_element(const ElemGeom& E, const double* s, int is
     return sqrt(dx * dx + dy * dy + dz * dz);
   };
   const double d13 = fmax(dist(0, 1), dist(2, 3)), d24 = fmax(dist(1, 2), dist(3, 0));
-  const int ndx = max(2, (int)(d13 / 1.0 + 0.5)), nde = max(2, (int)(d24 / 1.0 + 0.5));
+  const int ndx = qdiv > 0 ? qdiv : max(2, (int)(d13 / 1.0 + 0.5)), nde = qdiv > 0 ? qdiv : max(2, (int)(d24 / 1.0 + 0.5));
   for (int ix = 1; ix <= ndx; ++ix)
     for (int ie = 1; ie <= nde; ++ie) {
       const double a = -1.0 + (ix - 1) * 2.0 / ndx, b = -1.0 + ix * 2.0 / ndx;
@@ -232,8 +234,10 @@ __device__ __forceinline__ void stk_kernel(const double* s, const double* f, con
   prT[2] = c * (3.0 * rxz * ir2 * n[0] + 3.0 * ryz * ir2 * n[1] + (-1.0 + 3.0 * rzz * ir2) * n[2]);
 }
 
+// qdiv: cells per direction of a regular quad (3: Quad_StokesIntNum; 1: the regular
+// branch of Quad_StokesInt, lib_Stokes.f90:3398, used for points in the domain).
 __device__ inline void stk_element(const ElemGeom& E, const double* s, int isrc, const double* rl, const double* rw,
-                                   int Q, int iqud, const IntegOpt& opt, StkElem& o) {
+                                   int Q, int iqud, const IntegOpt& opt, StkElem& o, int qdiv = 3) {
   for (int k = 0; k < 6; ++k) {
     o.G[k] = 0.0;
     for (int j = 0; j < 4; ++j) o.T[k][j] = 0.0;
@@ -273,10 +277,10 @@ __device__ inline void stk_element(const ElemGeom& E, const double* s, int isrc,
     return;
   }
   const int ng1 = gtNg1[iqud - 1], ng2 = gtNg2[iqud - 1];
-  for (int ix = 1; ix <= 3; ++ix)
-    for (int ie = 1; ie <= 3; ++ie) {
-      const double a = -1.0 + (ix - 1) * 2.0 / 3, b = -1.0 + ix * 2.0 / 3;
-      const double c = -1.0 + (ie - 1) * 2.0 / 3, d = -1.0 + ie * 2.0 / 3;
+  for (int ix = 1; ix <= qdiv; ++ix)
+    for (int ie = 1; ie <= qdiv; ++ie) {
+      const double a = -1.0 + (ix - 1) * 2.0 / qdiv, b = -1.0 + ix * 2.0 / qdiv;
+      const double c = -1.0 + (ie - 1) * 2.0 / qdiv, d = -1.0 + ie * 2.0 / qdiv;
       const double dex = 0.25 * (b - a) * (d - c);
       for (int i = ng1; i <= ng2; ++i)
         for (int j = ng1; j <= ng2; ++j) {

@@ -369,4 +369,177 @@ cudaError_t to_fp32(const double* a, float* b, int64_t count, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Post-processing of a solved field (not on the solve path): one CTA per
+// evaluation point, its threads striding over the subdomain's elements with
+// the element integrals of the assembly (no singular element), the sums
+// reduced in a fixed order (warp shuffles, then warps in order).
+// ---------------------------------------------------------------------------
+constexpr int POST_THREADS = 256;
+
+template <int NV>
+__device__ __forceinline__ void post_reduce(double (&v)[NV], double (*sred)[POST_THREADS / 32]) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double x = v[k];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) sred[k][warp] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double t = 0.0;
+      for (int w = 0; w < POST_THREADS / 32; ++w) t += sred[k][w];
+      v[k] = t;
+    }
+}
+
+// pressureStokes (lib_Stokes.f90:4-94) at the centroid of element r: the
+// pressure rows of sdIntRowQStokes (self element left out, as its analytic
+// branch leaves prG/prT zero) contracted with u - (the element's centre
+// velocity) and q, times -2 / (8 pi).  With the pressure correction of the
+// q-rows (lib_Stokes.f90:1851-1863) the reference's sum over nodes equals this
+// differenced sum over elements.
+__global__ void __launch_bounds__(POST_THREADS) k_surface_pressure(int ne, const ElemGeom* __restrict__ geom,
+                                                                  const double* __restrict__ rl,
+                                                                  const double* __restrict__ rw, int Q, int iqud,
+                                                                  IntegOpt opt, const double* __restrict__ u,
+                                                                  int nnodes, const double* __restrict__ q,
+                                                                  double diff, double osemPi, double* __restrict__ p) {
+  __shared__ double sred[2][POST_THREADS / 32];
+  const int r = blockIdx.x;
+  const ElemGeom& Er = geom[r];
+  const double f = (Er.type == AGB_TRI) ? 1.0 / 3.0 : 0.25;
+  double ubar[3];
+  for (int c = 0; c < 3; ++c) {
+    double a = 0.0;
+    for (int k = 0; k < Er.nno; ++k) a += f * u[(int64_t)c * nnodes + Er.con[k]];
+    ubar[c] = a;
+  }
+  const double s[3] = {Er.c[0], Er.c[1], Er.c[2]};
+  double acc[2] = {0.0, 0.0};
+  for (int e = threadIdx.x; e < ne; e += POST_THREADS) {
+    if (e == r) continue;
+    const ElemGeom& E = geom[e];
+    StkElem o;
+    stk_element(E, s, 0, rl, rw, Q, iqud, opt, o);
+    for (int k = 0; k < E.nno; ++k)
+      for (int c = 0; c < 3; ++c) acc[0] += o.prT[c][k] * (u[(int64_t)c * nnodes + E.con[k]] - ubar[c]);
+    for (int c = 0; c < 3; ++c) acc[1] += o.prG[c] * q[(int64_t)c * ne + e];
+  }
+  post_reduce<2>(acc, sred);
+  if (threadIdx.x == 0) p[r] = -(diff * acc[0] - acc[1]) / osemPi * 2.0;
+}
+
+// GetStokesDomainValue (lib_Stokes.f90:3043-3373) at point k: velocity, pressure
+// and the reference's check of the point (stresslet diagonal sums 8 pi, sum G.n 0).
+__global__ void __launch_bounds__(POST_THREADS) k_domain_stokes(int ne, const ElemGeom* __restrict__ geom,
+                                                               const double* __restrict__ rl,
+                                                               const double* __restrict__ rw, int Q, int iqud,
+                                                               IntegOpt opt, const double* __restrict__ pts,
+                                                               const double* __restrict__ u, int nnodes,
+                                                               const double* __restrict__ q, double diff,
+                                                               double osemPi, double* __restrict__ out,
+                                                               double* __restrict__ err) {
+  __shared__ double sred[10][POST_THREADS / 32];
+  const int pk = blockIdx.x;
+  const double s[3] = {pts[3 * (int64_t)pk], pts[3 * (int64_t)pk + 1], pts[3 * (int64_t)pk + 2]};
+  // rx, ry, rz, p, sum Txx, sum Tyy, sum Tzz, sum G.n (x, y, z)
+  double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int e = threadIdx.x; e < ne; e += POST_THREADS) {
+    const ElemGeom& E = geom[e];
+    StkElem o;
+    stk_element(E, s, 0, rl, rw, Q, iqud, opt, o, 1);
+    for (int k = 0; k < E.nno; ++k) {
+      const int nd = E.con[k];
+      const double ux = u[nd], uy = u[(int64_t)nnodes + nd], uz = u[2 * (int64_t)nnodes + nd];
+      acc[0] += o.T[0][k] * ux + o.T[1][k] * uy + o.T[2][k] * uz;
+      acc[1] += o.T[1][k] * ux + o.T[3][k] * uy + o.T[4][k] * uz;
+      acc[2] += o.T[2][k] * ux + o.T[4][k] * uy + o.T[5][k] * uz;
+      acc[3] += diff * (o.prT[0][k] * ux + o.prT[1][k] * uy + o.prT[2][k] * uz);
+      acc[4] += o.T[0][k];
+      acc[5] += o.T[3][k];
+      acc[6] += o.T[5][k];
+    }
+    const double qx = q[e], qy = q[(int64_t)ne + e], qz = q[2 * (int64_t)ne + e];
+    acc[0] += (o.G[0] * qx + o.G[1] * qy + o.G[2] * qz) / diff;
+    acc[1] += (o.G[1] * qx + o.G[3] * qy + o.G[4] * qz) / diff;
+    acc[2] += (o.G[2] * qx + o.G[4] * qy + o.G[5] * qz) / diff;
+    acc[3] -= o.prG[0] * qx + o.prG[1] * qy + o.prG[2] * qz;
+    const double n0 = E.n[0] * E.multi, n1 = E.n[1] * E.multi, n2 = E.n[2] * E.multi;
+    acc[7] -= o.G[0] * n0 + o.G[1] * n1 + o.G[2] * n2;
+    acc[8] -= o.G[1] * n0 + o.G[3] * n1 + o.G[4] * n2;
+    acc[9] -= o.G[2] * n0 + o.G[4] * n1 + o.G[5] * n2;
+  }
+  post_reduce<10>(acc, sred);
+  if (threadIdx.x == 0) {
+    for (int c = 0; c < 4; ++c) out[4 * (int64_t)pk + c] = -acc[c] / osemPi;
+    double e = -9.99;
+    for (int c = 0; c < 3; ++c) e = fmax(e, fabs(-acc[4 + c] / osemPi - 1.0));
+    for (int c = 0; c < 3; ++c) e = fmax(e, fabs(acc[7 + c]));
+    err[pk] = e;
+  }
+}
+
+// GetSubDomainValue (lib_domain.f90:210-344) with VerifyIntegrals (:354-391) at point k.
+__global__ void __launch_bounds__(POST_THREADS) k_domain_laplace(int ne, const ElemGeom* __restrict__ geom,
+                                                                const double* __restrict__ rl,
+                                                                const double* __restrict__ rw, int Q, int iqud,
+                                                                IntegOpt opt, const double* __restrict__ pts,
+                                                                const double* __restrict__ xyz,
+                                                                const double* __restrict__ u,
+                                                                const double* __restrict__ q, double diff,
+                                                                double* __restrict__ out, double* __restrict__ err) {
+  __shared__ double sred[9][POST_THREADS / 32];
+  const int pk = blockIdx.x;
+  const double s[3] = {pts[3 * (int64_t)pk], pts[3 * (int64_t)pk + 1], pts[3 * (int64_t)pk + 2]};
+  // sum H u, sum G q multi / diff, c = -sum H, sum H x_j (3), sum G n_j multi (3)
+  double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int e = threadIdx.x; e < ne; e += POST_THREADS) {
+    const ElemGeom& E = geom[e];
+    const LapElem o = lap_element(E, s, 0, rl, rw, Q, iqud, opt, 1);
+    for (int k = 0; k < E.nno; ++k) {
+      const int nd = E.con[k];
+      acc[0] += o.h[k] * u[nd];
+      acc[2] -= o.h[k];
+      for (int j = 0; j < 3; ++j) acc[3 + j] += o.h[k] * xyz[3 * (int64_t)nd + j];
+    }
+    acc[1] += o.g * q[e] * E.multi / diff;
+    for (int j = 0; j < 3; ++j) acc[6 + j] += o.g * E.n[j] * E.multi;
+  }
+  post_reduce<9>(acc, sred);
+  if (threadIdx.x == 0) {
+    double e = 0.0;
+    for (int j = 0; j < 3; ++j) e = fmax(e, fabs(acc[3 + j] + s[j] * acc[2] - acc[6 + j]));
+    err[pk] = e;
+    out[pk] = (-acc[0] - acc[1]) / acc[2];
+  }
+}
+
+cudaError_t surface_pressure(int ne, const ElemGeom* geom, const RuleDev& rule, int iqud, const IntegOpt& opt,
+                             const double* u, int nnodes, const double* q, double diff, double osemPi, double* p,
+                             cudaStream_t s) {
+  cudaError_t e = upload_general_tables();
+  if (e != cudaSuccess || ne == 0) return e;
+  k_surface_pressure<<<ne, POST_THREADS, 0, s>>>(ne, geom, rule.l, rule.w, rule.Q, iqud, opt, u, nnodes, q, diff,
+                                                 osemPi, p);
+  return cudaGetLastError();
+}
+
+cudaError_t domain_values(bool stokes, int ne, const ElemGeom* geom, const RuleDev& rule, int iqud, const IntegOpt& opt,
+                          int npts, const double* pts, const double* xyz, const double* u, int nnodes,
+                          const double* q, double diff, double osemPi, double* out, double* err, cudaStream_t s) {
+  cudaError_t e = upload_general_tables();
+  if (e != cudaSuccess || npts == 0) return e;
+  if (stokes)
+    k_domain_stokes<<<npts, POST_THREADS, 0, s>>>(ne, geom, rule.l, rule.w, rule.Q, iqud, opt, pts, u, nnodes, q,
+                                                  diff, osemPi, out, err);
+  else
+    k_domain_laplace<<<npts, POST_THREADS, 0, s>>>(ne, geom, rule.l, rule.w, rule.Q, iqud, opt, pts, xyz, u, q, diff,
+                                                   out, err);
+  return cudaGetLastError();
+}
+
 }  // namespace agb

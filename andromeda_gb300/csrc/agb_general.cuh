@@ -73,4 +73,17 @@ cudaError_t upload_general_tables();
 // FP64 -> FP32 copy of the system (for the mixed solve of a general system)
 cudaError_t to_fp32(const double* a, float* b, int64_t count, cudaStream_t s);
 
+// Surface pressure at the centroids of the subdomain's elements (pressureStokes,
+// lib_Stokes.f90:4): u [3][nnodes], q [3][ne] in subdomain order, p [ne].
+cudaError_t surface_pressure(int ne, const ElemGeom* geom, const RuleDev& rule, int iqud, const IntegOpt& opt,
+                             const double* u, int nnodes, const double* q, double diff, double osemPi, double* p,
+                             cudaStream_t s);
+// Values at npts points of the domain (GetStokesDomainValue lib_Stokes.f90:3043 /
+// GetSubDomainValue lib_domain.f90:210): Stokes out[4k..4k+3] = velocity,
+// pressure (u [3][nnodes], q [3][ne]); Laplace out[k] (u [nnodes], q [ne]);
+// err[k] the reference's check of the point.
+cudaError_t domain_values(bool stokes, int ne, const ElemGeom* geom, const RuleDev& rule, int iqud, const IntegOpt& opt,
+                          int npts, const double* pts, const double* xyz, const double* u, int nnodes,
+                          const double* q, double diff, double osemPi, double* out, double* err, cudaStream_t s);
+
 }  // namespace agb

@@ -325,6 +325,7 @@ __global__ void __launch_bounds__(AV2<T>::WARPS * 32) k_av2(const T* __restrict_
     }
     __syncthreads();  // everyone is done with this buffer before it is refilled
   }
+  if (threadIdx.x == 0) mbar_drain(bar, 2, nch, errflag);
   double ssq = 0.0;
   if constexpr (sizeof(T) == 4) {
     const int r = lane >> 3, c = lane & 7, row = row0 + r;
@@ -897,6 +898,20 @@ static void launch_av2(const DenseLsqr& L) {
   k_av2<T><<<av2_blocks<T>(L), AV2<T>::WARPS * 32, smem, L.stream>>>((const T*)L.A, L.lda, L.m, (const T*)L.Vs, L.sc,
                                                                      L.Y, (T*)L.Ys, L.part, L.errflag);
 }
+// k_avp that does nothing once no right-hand side is active (*gate == 0): the
+// iterations replayed after the last one converged read no matrix
+__global__ void __launch_bounds__(AVP_THREADS, 1) k_avp_gated(const __grid_constant__ CUtensorMap tmA,
+                                                             const __grid_constant__ CUtensorMap tmW, int ne, int ldp,
+                                                             const LsqrScalars* sc, double* __restrict__ Y,
+                                                             float* __restrict__ Ys, double* __restrict__ part,
+                                                             int* errflag, const int* __restrict__ gate) {
+  if (*gate == 0) return;
+  avp_tile(&tmA, &tmW, ne, ldp, sc, Y, Ys, part, errflag, (int)blockIdx.x);
+}
+void launch_avp(const DenseLsqr& L, const LsqrScalars* sc, double* Yout, const int* gate) {
+  k_avp_gated<<<cdiv(L.pk_ne, AVP_R), AVP_THREADS, AVP_SMEM, L.stream>>>(L.tm_av, L.tm_vp, L.pk_ne, L.pk_ldp, sc, Yout,
+                                                                        (float*)L.Ys, L.part, L.errflag, gate);
+}
 template <typename T>
 static size_t atu2_smem() {
   return 256 * K8 * sizeof(T) + (sizeof(T) == 4 ? (size_t)Vec<T>::N * K8 * ATU_THREADS * sizeof(double) : 0);
@@ -931,6 +946,8 @@ static cudaError_t set_sweep_attrs() {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_av3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AV3_SMEM);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_atu3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ATU3_SMEM);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_avp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AVP_SMEM);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_avp_gated, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AVP_SMEM);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_atup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ATUP_SMEM);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_atu2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)atu2_smem<T>());
@@ -943,6 +960,11 @@ void DenseLsqr::release() {
   pev_ready = false;
   cudaFree(Y); cudaFree(V); cudaFree(W); cudaFree(X); cudaFree(Z); cudaFree(Ys); cudaFree(Vs);
   cudaFree(part); cudaFree(Zp); cudaFree(sc); cudaFree(nactive); cudaFree(XsD); cudaFree(errflag); cudaFree(Yp); cudaFree(Vp);
+  cudaFree(bg); cudaFree(bg_part); cudaFree(bsc); cudaFree(sc0);
+  bg = bg_part = nullptr;
+  bsc = nullptr;
+  sc0 = nullptr;
+  bg_diag = false;
   Yp = nullptr;
   Vp = nullptr;
   XsD = nullptr; errflag = nullptr;

@@ -17,6 +17,13 @@ struct LsqrScalars {
   int itn, istop, active, itnlim;
 };
 
+// Per right-hand-side BiCGSTAB state (DenseLsqr::bicgstab), FP64.  status: -1
+// running, 0 converged, 1 iteration limit, 2 breakdown.
+struct BicgScalars {
+  double rho, rho_old, alpha, omega, bnorm, relres, snorm;
+  int its, status, active, half;
+};
+
 // Dense block LSQR.  A is m x n row-major with leading dimension lda (lda is
 // a multiple of 32 and columns n..lda-1 are zero).  T = float (mixed path)
 // or double (FP64 path).  Up to AGB_MAX_RHS right-hand sides share every
@@ -58,6 +65,12 @@ struct DenseLsqr {
   float* Yp = nullptr;          // [col blocks][m][8] partial products of A V
   int mf_cb = 0;
   const double* mf_q = nullptr; // column scales applied on the fly
+  // BiCGSTAB work (bicgstab): R, Rt, P, S, T, X ([m][8] each) and 1/diag(A) [m]
+  double* bg = nullptr;
+  double* bg_part = nullptr;    // per-CTA partial sums
+  BicgScalars* bsc = nullptr;
+  LsqrScalars* sc0 = nullptr;   // zero gammas: the packed sweep writes Y = A W
+  bool bg_diag = false;         // 1/diag(A) computed for the current matrix
   double t_av = 0.0, t_atu = 0.0;
   long n_av = 0, n_atu = 0;
   long launches = 0;           // kernels launched by precon/solve
@@ -74,10 +87,22 @@ struct DenseLsqr {
   // FP64-accumulated residual sweep over A is skipped.
   bool solve(const double* b_dev, double* x_dev, const double* q_dev, double eps, int maxit, int* nit_host,
              int* istop_host, double* rnorm_host = nullptr, int check_every = 8, bool x0_zero = false);
+  // BiCGSTAB with the Jacobi preconditioner on the packed layout (the solver of
+  // the reference's LIS path): per column c, A x = b from x0 = 0 until
+  // ||b - A x|| <= tol ||b|| (recursive residual) or maxit iterations (0: 1000).
+  // b: column-major m x k in the row numbering 3i+a; x: column-major n x k in the
+  // unknown numbering a ne + i (that of solve).  status per column: 0 converged,
+  // 1 iteration limit, 2 breakdown.
+  bool bicgstab(const double* b_dev, double* x_dev, double tol, int maxit, int* nit_host, int* status_host,
+                double* relres_host = nullptr);
   // r = b - A (x ./ q) with FP64 accumulation (refinement residual).
   bool residual(const double* b_dev, const double* x_dev, const double* q_dev, double* r_dev);
   void release();
 };
+
+// Y = A W over the packed layout (k_avp with the gammas of sc), W the solver's Vp;
+// nothing while *gate == 0 (device counter of active right-hand sides).
+void launch_avp(const DenseLsqr& L, const LsqrScalars* sc, double* Y, const int* gate);
 
 bool crs_lsqr_precon(int m, int n, int64_t nnz, double* q, const int64_t* ia, const int* ja, double* a, std::string& err);
 bool crs_lsqr_solve(int m, int n, int64_t nnz, int& maxit, double eps, int& nit, int& ierr, const double* q,

@@ -317,6 +317,14 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32_mlp(bar))
                : "memory");
 }
+__device__ __forceinline__ bool tc_wait_once(uint64_t* bar, uint32_t parity) {
+  uint32_t ok = 0;
+  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+               : "=r"(ok)
+               : "r"(smem_u32_mlp(bar)), "r"(parity)
+               : "memory");
+  return ok != 0;
+}
 __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, int* errflag) {
   uint32_t ok = 0, tries = 0;
   while (true) {
@@ -409,9 +417,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
   const uint32_t tmem = tmem_base;
   if (warp == TC_EPI) {  // weight chunks: one bulk copy each into the two-slot ring
     if (lane == 0) {
+      int issued = 0;
       for (int c = 0; c < TC_CHUNKS; ++c) {
         const int s = c & 1;
         if (c >= 2 && !tc_wait(&empty[s], ((c >> 1) - 1) & 1, errflag)) break;
+        ++issued;
         const uint32_t bytes = (uint32_t)tc_chunk_bytes(c);
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32_mlp(&full[s])), "r"(bytes)
                      : "memory");
@@ -419,6 +429,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
                          smem_u32_mlp(Wslot + s * TC_SLOT)),
                      "l"(wt + tc_chunk_off(c)), "r"(bytes), "r"(smem_u32_mlp(&full[s]))
                      : "memory");
+      }
+      // the last copy into each slot has landed before the CTA may exit (on the normal
+      // path the MMA issuer already waited for both; after a wait that gave up this
+      // keeps the CTA alive until its own copies are done)
+      for (int c = issued > 2 ? issued - 2 : 0; c < issued; ++c) {
+        uint32_t tries = 0;
+        while (!tc_wait_once(&full[c & 1], (c >> 1) & 1))
+          if (++tries > (1u << 22)) {
+            atomicExch(errflag, 1);
+            break;
+          }
       }
     }
   } else if (warp == TC_EPI + 1) {  // products: layer l accumulates into buffer (l-1)&1; chunk j of a layer

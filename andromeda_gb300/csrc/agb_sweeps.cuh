@@ -133,6 +133,7 @@ __device__ __forceinline__ void av3_tile(const CUtensorMap* tmA, int64_t lda, in
       dacc += (double)v[0];
     }
   }
+  if (threadIdx.x == 0) mbar_drain(full, ST, nst, errflag);
   double ssq = 0.0;
   {
     const int r = lane >> 3, c = lane & 7, row = row_base + warp * 4 + r;
@@ -225,6 +226,7 @@ __device__ __forceinline__ void atu3_tile(const CUtensorMap* tmA, int64_t lda, i
         for (int c = 0; c < K8; ++c) { dacc[q][c] += (double)acc[q][c]; acc[q][c] = 0.f; }
     }
   }
+  if (threadIdx.x == 0) mbar_drain(full, ST, nst, errflag);
   const int64_t col = (int64_t)c0 + tc;
 #pragma unroll
   for (int q = 0; q < 2; ++q)
@@ -310,8 +312,10 @@ __device__ __forceinline__ void avp_tile(const CUtensorMap* tmA, const CUtensorM
   // slots to be released), so no compute warp ever blocks on a refill
   double ssq = 0.0;
   if (warp == nwarps) {
-    if (lane == 0)
+    if (lane == 0) {
       for (int k = 0; k < nst; ++k) issue(k);
+      mbar_drain(full, AVP_ST, nst, errflag);
+    }
     __syncwarp();
   } else {
   float acc[2][3][K8];
@@ -467,6 +471,7 @@ __device__ __forceinline__ void atup_tile(const CUtensorMap* tmA, int ne, int64_
         for (int c = 0; c < K8; ++c) { dacc[b][c] += (double)acc[b][c]; acc[b][c] = 0.f; }
     }
   }
+  if (threadIdx.x == 0) mbar_drain(full, ATUP_ST, nst, errflag);
   const int j = j0 + threadIdx.x;
   if (j < ne)
 #pragma unroll

@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--outer-level", type=int, default=2)
     ap.add_argument("--outer-radius", type=float, default=200.0)
     ap.add_argument("--eps", type=float, default=1e-7)
+    ap.add_argument("--solver", default="lsqr", choices=["lsqr", "bicgstab"],
+                    help="sphere, batch, large: LSQR (lsqr_solve, the default) or BiCGSTAB-Jacobi (the LIS path's solver)")
     ap.add_argument("--fp64-iters", type=int, default=16, help="FP64 comparator LSQR sample (iterations)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -74,9 +76,10 @@ def workload(args):
     from andromeda_gb300 import mesh as M
     p = M.icosphere(args.level, 1.0, inward=True)
     m = M.particle_in_sphere(p, outer_level=args.outer_level, outer_radius=args.outer_radius)
+    solver = "BiCGSTAB-Jacobi tol" if getattr(args, "solver", "lsqr") == "bicgstab" else "LSQR eps"
     name = (f"Stokes sphere a=1 icosphere L{args.level} ({len(p['etype'])} tri) in L{args.outer_level} container "
             f"r={args.outer_radius:g} ({len(m['etype']) - len(p['etype'])} tri), 6 RHS, ITRI 5, mu=1, "
-            f"LSQR eps {args.eps:g}")
+            f"{solver} {args.eps:g}")
     return m, name
 
 
@@ -261,14 +264,15 @@ def run_batch(args, rank, world, local):
     eps = args.batch_eps
     tune = not args.no_autotune
     warm = mine[:32]
+    solver = A.SOLVER_BICGSTAB if args.solver == "bicgstab" else A.SOLVER_LSQR
     for _ in range(args.warmup):
-        A.batch_resistance(warm, eps=eps, ctx=ctx, autotune=tune)
+        A.batch_resistance(warm, eps=eps, ctx=ctx, autotune=tune, solver=solver)
     barrier()
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         Rs, nits, istops, sts = [], [], [], []
         for _ in range(args.steps):
-            R, nit, istop, st = A.batch_resistance(mine, eps=eps, ctx=ctx, autotune=tune)
+            R, nit, istop, st = A.batch_resistance(mine, eps=eps, ctx=ctx, autotune=tune, solver=solver)
             Rs.append(R); nits.append(nit); istops.append(istop); sts.append(st)
         t1 = time.perf_counter()
     dev_s = sum(st["device_ms"] for st in sts) / 1000.0
@@ -313,7 +317,8 @@ def run_batch(args, rank, world, local):
                 "config": {"workload": f"{args.bodies} superellipsoids a=1, b,c~U(0.2,1), e1,e2~U(0.3,1.8), "
                                        f"random orientation, {int(ne.min())}..{int(ne.max())} tri (mean "
                                        f"{ne.mean():.0f}), each in an L2 container r=200, 6 RHS, ITRI 5, "
-                                       f"LSQR eps {eps:g}",
+                                       + (f"BiCGSTAB-Jacobi tol {eps:g}" if args.solver == "bicgstab"
+                                          else f"LSQR eps {eps:g}"),
                            "precision": "mixed", "parallelism": "bodies split over ranks" if world > 1 else
                            "single GPU", "l2": "inputs larger than L2 (waves of tens of GB), no flush",
                            "warmup": f"{args.warmup} x the first {len(warm)} bodies"},
@@ -358,6 +363,7 @@ def run_large(args):
     C = A.Context(0)
     C.set_mesh(m)
     C.set_problem(A.STOKES, [1, 2], A.dirichlet_known(A.STOKES, 2), itri=5)
+    C.set_solver(A.SOLVER_BICGSTAB if args.solver == "bicgstab" else A.SOLVER_LSQR)
     ne = len(m["etype"])
     workload = (f"superellipsoid a=1 b=0.5 c=0.25 e1=0.6 e2=1.4, {nr}x{ns} grid ({len(body['etype'])} tri) "
                 f"in an L2 container r=200, 6 RHS, ITRI 5")
@@ -390,7 +396,8 @@ def run_large(args):
                 "value": 1000.0 / info["device_ms"], "unit": "solves/s", "n_gpus": 1, "steps": 1, "warmup": 0,
                 "ms_per_step": info["device_ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "fp32 (fp64 singular/free-term/reductions)", "data": "synthetic",
-                "config": {"workload": workload + f", LSQR eps {args.eps:g}", "unknowns": C.n,
+                "config": {"workload": workload + (f", BiCGSTAB-Jacobi tol {args.eps:g}" if args.solver == "bicgstab"
+                                                   else f", LSQR eps {args.eps:g}"), "unknowns": C.n,
                            "packed_matrix_gb": alg / 1e9, "l2": "inputs larger than L2, no flush"},
                 "assemble_ms": info["assemble_ms"], "rhs_ms": info["rhs_ms"], "solve_ms": info["solve_ms"],
                 "nit": [int(v) for v in nit], "istop": info["istop"],
@@ -400,8 +407,8 @@ def run_large(args):
                              "achieved": alg / (av_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                              "frac": alg / (av_ms * 1e-3) / 1e9 / peak, "traffic": None, "peak_source": peak_kind,
                              "algorithmic_bytes_per_launch": alg,
-                             "other_sweep": {"kernel": "k_atup", "achieved": alg / (atu_ms * 1e-3) / 1e9,
-                                             "frac": alg / (atu_ms * 1e-3) / 1e9 / peak}},
+                             "other_sweep": ({"kernel": "k_atup", "achieved": alg / (atu_ms * 1e-3) / 1e9,
+                                              "frac": alg / (atu_ms * 1e-3) / 1e9 / peak} if atu_ms > 0 else None)},
                 "clocks": clk.summary(), "gpu_launches": kt["launches"], "host_s": t1 - t0}
         print(json.dumps(line), flush=True)
         C.close()
@@ -623,6 +630,8 @@ def main():
     C = A.Context(local if world > 1 else 0)
     C.set_mesh(m)
     C.set_problem(A.STOKES, [1, 2], A.dirichlet_known(A.STOKES, 2), itri=5)
+    solver = A.SOLVER_BICGSTAB if args.solver == "bicgstab" else A.SOLVER_LSQR
+    C.set_solver(solver)
 
     def step():
         return C.resistance_tensor(A.MIXED, 1, 2, eps=args.eps)
@@ -655,7 +664,7 @@ def main():
     if os.path.exists(GOLDEN_TRUTH):
         with open(GOLDEN_TRUTH) as f:
             g = json.load(f)
-        if g.get("workload") == name.split(", LSQR")[0]:
+        if g.get("workload") == name.split(", LSQR")[0].split(", BiCGSTAB")[0]:
             Rt = np.array(g["R"])
             rel_err = float(np.max(np.abs(R - Rt)) / np.max(np.abs(Rt)))
     lam = 1.0 / args.outer_radius
@@ -677,12 +686,13 @@ def main():
             for line in f:
                 if line.startswith("traffic_bytes_per_launch_k_avp_c2:"):
                     traffic = float(line.split(":")[1])
-    roofline = {"bound": "hbm", "kernel": "k_avp (LSQR A*V sweep over the packed symmetric 3x3 blocks, FP32, TMA, 8 RHS)",
+    which = "BiCGSTAB A D^-1 p / A D^-1 s sweeps" if args.solver == "bicgstab" else "LSQR A*V sweep"
+    roofline = {"bound": "hbm", "kernel": f"k_avp ({which} over the packed symmetric 3x3 blocks, FP32, TMA, 8 RHS)",
                 "achieved": a_bytes / (av_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                 "frac": a_bytes / (av_ms * 1e-3) / 1e9 / peak, "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": a_bytes,
-                "other_sweep": {"kernel": "k_atup (A^T*U, packed, TMA)", "achieved": a_bytes / (atu_ms * 1e-3) / 1e9,
-                                "frac": a_bytes / (atu_ms * 1e-3) / 1e9 / peak}}
+                "other_sweep": ({"kernel": "k_atup (A^T*U, packed, TMA)", "achieved": a_bytes / (atu_ms * 1e-3) / 1e9,
+                                 "frac": a_bytes / (atu_ms * 1e-3) / 1e9 / peak} if atu_ms > 0 else None)}
 
     # end to end through the C ABI with host buffers (mesh upload + solve + R back)
     e2e_vals = []
@@ -694,6 +704,7 @@ def main():
         C2 = A.Context(local if world > 1 else 0)
         C2.set_mesh(m)
         C2.set_problem(A.STOKES, [1, 2], A.dirichlet_known(A.STOKES, 2), itri=5)
+        C2.set_solver(solver)
         C2.resistance_tensor(A.MIXED, 1, 2, eps=args.eps)
         C2.close()
         e2e_vals.append(time.perf_counter() - t2)
@@ -704,6 +715,7 @@ def main():
     # iterations, scaled to the iteration count of the solve
     fp64 = None
     if args.fp64_iters > 0 and rank == 0:
+        C.set_solver(A.SOLVER_LSQR)  # the FP64 path solves with LSQR; a BiCGSTAB iteration costs two sweeps too
         C.kernel_times(reset=True)
         R64, nit64, info64 = C.resistance_tensor(A.FP64, 1, 2, maxit=args.fp64_iters, eps=args.eps)
         kt64 = C.kernel_times(reset=True)
@@ -729,7 +741,7 @@ def main():
                 "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (fp64 singular/free-term/reductions)",
                 "data": "synthetic (meshes generated in-process)",
-                "config": {"workload": name, "precision": "mixed", "unknowns": C.n,
+                "config": {"workload": name, "precision": "mixed", "solver": args.solver, "unknowns": C.n,
                            "parallelism": "replicas" if world > 1 else "single GPU",
                            "l2": "inputs larger than L2 (10.4 GB packed matrix), no flush"},
                 "rel_err_vs_fp64": rel_err, "drag_over_analytic": drag_ratio, "torque_over_analytic": torque_ratio,

@@ -69,6 +69,11 @@ typedef struct agb_context agb_context;
                        LSQR sweep recomputes the single-layer entries (Stokes,
                        velocity known on every wall, triangles; zero warm start) */
 
+/* solver of the assembled system (agb_set_solver; the SLET key of and.inp) */
+#define AGB_SOLVER_LSQR 0     /* lsqr_solve with lsqr_precon's column scaling (SLET CRS) */
+#define AGB_SOLVER_BICGSTAB 1 /* BiCGSTAB with the Jacobi preconditioner (SLET LIS with the
+                                 reference's default LIS options) */
+
 /* boundary-condition types (mod_mesh.f90:110) */
 #define AGB_BC_FUNCTION 1
 #define AGB_BC_FLUX 2
@@ -121,6 +126,20 @@ int agb_set_problem(agb_context* ctx, int kind, int nwalls, const int* walls, co
  * (for AGB_MIXED the routed system is then copied to FP32).  Call after
  * agb_set_problem; it clears the assembled system. */
 int agb_set_integration(agb_context* ctx, int sing_mode, int rec_depth, double near_eta, int near_depth);
+
+/* Solver of agb_solve / agb_resistance_tensor (the SLET key, mod_par.f90):
+ * AGB_SOLVER_LSQR (default; lsqr_solve, lib_lsqr.f:33) or AGB_SOLVER_BICGSTAB,
+ * the LIS path's solver (StokesBigSystemSOLVElis lib_StokesLis.f90:4 with the
+ * default options "-i bicgstab -p jacobi", mod_par.f90:288): every equation in
+ * the row of its own unknown, preconditioned BiCGSTAB (van der Vorst 1992) with
+ * M = diag(A), x0 = 0 (the warm start is not used), stop at
+ * ||b - A x|| <= eps ||b|| or maxit iterations (0: 1000, the LIS default).  With
+ * BiCGSTAB, istop[r] is 0 converged, 1 iteration limit, 2 breakdown.  BiCGSTAB
+ * needs the packed mixed system (Stokes, velocity known on every wall,
+ * triangles, default integration, AGB_MIXED); other systems return
+ * AGB_ERR_UNSUPPORTED from the solve.  agb_batch_resistance on this context
+ * solves its bodies with BiCGSTAB too (istop as above; no autotuning). */
+int agb_set_solver(agb_context* ctx, int solver);
 
 /* Element geometry in global element order (normal 3*nelem, area nelem,
  * centroid 3*nelem); elements outside the subdomain are zero. */
@@ -201,6 +220,26 @@ int agb_lsqr_solve(int m, int n, int64_t nnz, int* maxit, double eps, int* nit, 
  * Gxx,Gxy,Gxz,Gyy,Gyz,Gzz,prGx,prGy,prGz.  errs[2] = the reference's fSP/qSP
  * self-check residuals (max over u-rows, over q-rows). */
 int agb_integral_matrices(agb_context* ctx, double* T, double* G, double* errs);
+
+/* Surface pressure of a solved Stokes field (pressureStokes, lib_Stokes.f90:4-94):
+ * p at the centroid of every element of the subdomain (mesh order; 0 for an
+ * element of no subdomain wall) from the pressure rows of the q-source points
+ * (sdIntRowQStokes, lib_Stokes.f90:1562, self element left out as the
+ * reference's analytic branch does) contracted with the velocity u[3][nnodes]
+ * less the element's centre velocity and the traction q[3][nelem], times
+ * -2 / (8 pi).  FP64. */
+int agb_surface_pressure(agb_context* ctx, const double* u, const double* q, double* p);
+
+/* Values at npts points inside the domain (GetStokesDomainValue,
+ * lib_Stokes.f90:3043; GetSubDomainValue, lib_domain.f90:210) from the boundary
+ * values u[neq][nnodes] and fluxes/tractions q[neq][nelem]: Stokes
+ * out[4k..4k+3] = velocity, pressure; Laplace out[k].  err[k] is the
+ * reference's check of the point (Stokes: stresslet diagonal against 8 pi and
+ * sum G.n; getStokesDV treats err > 1e-2 as outside; Laplace: VerifyIntegrals).
+ * Triangles with the problem's integration options, quads as one Gauss cell
+ * (the regular branch of Quad_StokesInt / Quad_BEMInt).  FP64. */
+int agb_domain_values(agb_context* ctx, int npts, const double* pts, const double* u, const double* q, double* out,
+                      double* err);
 
 /* Sizes of the subdomain numbering: {nsp, nn, nq, rows, unknowns, knowns}. */
 int agb_layout_sizes(agb_context* ctx, int* sizes);

@@ -1,0 +1,103 @@
+"""GPU BiCGSTAB with the Jacobi preconditioner (AGB_SOLVER_BICGSTAB, the solver of
+the reference's LIS path) on the packed mixed Stokes system.
+
+* against the oracle's LIS path (FP64 BiCGSTAB-Jacobi on the same system): force and
+  torque within 2e-6 (the FP32 matrix), iteration counts within a few;
+* against the FP64 LSQR tensor on the level-3 sphere in the benchmark's container:
+  1e-6 relative, the benchmark's accuracy bar, with a fraction of LSQR's iterations;
+* its status codes and the systems it does not take.
+"""
+import numpy as np
+import pytest
+
+from andromeda_gb300 import mesh as M
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx(agb, m, walls=(1, 2)):
+    C = agb.Context(0)
+    C.set_mesh(m)
+    C.set_problem(agb.STOKES, list(walls), agb.dirichlet_known(agb.STOKES, len(walls)), itri=5)
+    return C
+
+
+def _rigid_motions(m, outer_wall=2):
+    nn = len(m["xyz"])
+    outer = np.unique(m["con"][m["bcid"] == outer_wall, :3])
+    U = np.zeros((6, 3, nn))
+    for i in range(3):
+        U[i, i, outer] = 1.0
+        w = np.zeros(3)
+        w[i] = 1.0
+        U[3 + i][:, outer] = np.cross(w, m["xyz"][outer]).T
+    return U
+
+
+def test_bicgstab_matches_oracle_lis_path(agb, orc):
+    m = M.particle_in_sphere(M.icosphere(2, 1.0, inward=True), outer_level=2, outer_radius=50.0)
+    P = orc.Problem(2, m, walls=[1, 2], known=np.ones((3, 2)), itri=5)
+    P.form_integrals()
+    _, ft_ref, n_ref, st_ref, _ = P.stokes_solve_lis(_rigid_motions(m), tol=1e-8)
+    P.close()
+    C = _ctx(agb, m)
+    C.set_solver(agb.SOLVER_BICGSTAB)
+    R, nit, info = C.resistance_tensor(agb.MIXED, 1, 2, eps=1e-8)
+    C.close()
+    assert np.all(np.asarray(info["istop"]) == 0) and np.all(st_ref == 0)
+    scale = np.max(np.abs(ft_ref))
+    assert np.max(np.abs(R - ft_ref)) < 2e-6 * scale
+    # the FP32 products slow the last digits of the recursive residual: a numpy
+    # emulation of this kernel sequence on the same system took 23-30 iterations
+    # where the FP64 oracle takes 18-24
+    assert np.all(nit <= 2 * n_ref + 10), (nit, n_ref)
+
+
+def test_bicgstab_tensor_against_fp64_lsqr(agb):
+    m = M.particle_in_sphere(M.icosphere(3, 1.0, inward=True), outer_level=2, outer_radius=200.0)
+    C = _ctx(agb, m)
+    R64, n64, _ = C.resistance_tensor(agb.FP64, 1, 2, eps=1e-11)
+    C.set_solver(agb.SOLVER_BICGSTAB)
+    R, nit, info = C.resistance_tensor(agb.MIXED, 1, 2, eps=1e-7)
+    C.close()
+    print("BiCGSTAB iterations", nit, "LSQR (FP64)", n64, "rel err", np.max(np.abs(R - R64)) / np.max(np.abs(R64)))
+    assert np.all(np.asarray(info["istop"]) == 0)
+    assert np.max(np.abs(R - R64)) < 1e-6 * np.max(np.abs(R64))
+    assert np.all(nit * 4 < n64)
+
+
+def test_bicgstab_status_and_unsupported(agb):
+    m = M.particle_in_sphere(M.icosphere(2, 1.0, inward=True), outer_level=1, outer_radius=20.0)
+    C = _ctx(agb, m)
+    C.set_solver(agb.SOLVER_BICGSTAB)
+    R, nit, info = C.resistance_tensor(agb.MIXED, 1, 2, maxit=2, eps=1e-12)
+    assert np.all(np.asarray(info["istop"]) == 1) and np.all(nit == 2)
+    with pytest.raises(agb.AgbError):
+        C.resistance_tensor(agb.FP64, 1, 2, eps=1e-8)  # BiCGSTAB takes the packed mixed system only
+    with pytest.raises(agb.AgbError):
+        C.set_solver(7)
+    C.set_solver(agb.SOLVER_LSQR)
+    R64, _, info64 = C.resistance_tensor(agb.FP64, 1, 2, eps=1e-10)
+    C.close()
+    assert np.all(np.isin(info64["istop"], (1, 2, 4)))
+
+
+def test_batch_bicgstab_matches_fp64(agb):
+    """The batched BiCGSTAB (every sweep one launch over all bodies) on bodies of
+    uneven size: each tensor within 5e-6 of the body's FP64 LSQR tensor, as the
+    batched LSQR test asks, with far fewer iterations."""
+    rng = np.random.default_rng(7)
+    meshes = []
+    for n in (180, 320, 520, 760):
+        b, c = rng.uniform(0.3, 1.0, 2)
+        e1, e2 = rng.uniform(0.5, 1.5, 2)
+        body = M.superellipsoid_tri(1.0, b, c, e1, e2, n, rotation=M.random_rotation(rng), inward=True)
+        meshes.append(M.particle_in_sphere(body, outer_level=1, outer_radius=20.0))
+    R, nit, istop, st = agb.batch_resistance(meshes, eps=1e-9, solver=agb.SOLVER_BICGSTAB)
+    assert np.all(istop == 0) and st["av_launches"] > 0
+    for i, m in enumerate(meshes):
+        C = _ctx(agb, m)
+        R64, n64, _ = C.resistance_tensor(agb.FP64, 1, 2, eps=1e-11)
+        C.close()
+        assert np.max(np.abs(R[i] - R64)) < 5e-6 * np.max(np.abs(R64)), i
+        assert np.max(nit[i]) * 3 < np.max(n64), (i, nit[i], n64)
