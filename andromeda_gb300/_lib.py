@@ -46,6 +46,7 @@ SIGNATURES = {
     "agb_lsqr_precon": ([I, I, C.c_int64, dp, lp, ip, dp], I),
     "agb_lsqr_solve": ([I, I, C.c_int64, PI, D, PI, PI, dp, lp, ip, dp, dp, dp], I),
     "agb_lsqr_precon_dense_noalloc": ([I, I, C.c_int64, vp, vp], I),
+    "agb_selftest_bounded_wait": ([I, C.c_uint, I, C.POINTER(C.c_int)], I),
     "agb_integral_matrices": ([vp, vp, vp, vp], I),
     "agb_layout_sizes": ([vp, ip], I),
     "agb_solve_fields": ([vp, I, dp, vp, dp, dp, I, D, I, ip, ip], I),

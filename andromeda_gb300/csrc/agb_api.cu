@@ -144,6 +144,21 @@ void dfree(P*& p) {
   if (p) cudaFree((void*)p);
   p = nullptr;
 }
+// device temporary owned by one scope: freed on every return unless released
+template <typename P>
+struct DevTemp {
+  P* p = nullptr;
+  DevTemp() = default;
+  DevTemp(const DevTemp&) = delete;
+  DevTemp& operator=(const DevTemp&) = delete;
+  ~DevTemp() { reset(); }
+  void reset() { dfree(p); }
+  P* release() {
+    P* q = p;
+    p = nullptr;
+    return q;
+  }
+};
 
 // Wandzura-Xiao orbit expansion into barycentric points on the reference
 // equilateral triangle (the construction of WandzuratXiaoBary,
@@ -409,12 +424,25 @@ int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int r
       return fail(c, AGB_ERR_CUDA, "lsqr setup: " + c->lsqr.err);
   }
   std::vector<int> nt(nrhs, 0), is(nrhs, 0);
-  if (c->solver == AGB_SOLVER_BICGSTAB) {
+  if (c->solver == AGB_SOLVER_BICGSTAB || c->solver == AGB_SOLVER_HYBRID) {
     if (!c->lsqr.packed)
       return fail(c, AGB_ERR_UNSUPPORTED, "BiCGSTAB needs the packed mixed system (Stokes, velocity known on every "
                                           "wall, triangles, default integration, AGB_MIXED)");
     if (!c->lsqr.bicgstab(c->d_rhs, d_x, eps, maxit, nt.data(), is.data()))
       return fail(c, AGB_ERR_CUDA, "bicgstab: " + c->lsqr.err);
+    bool all_converged = true;
+    for (int r = 0; r < nrhs; ++r) all_converged = all_converged && is[r] == 0;
+    if (c->solver == AGB_SOLVER_HYBRID && !all_converged) {
+      // LSQR (the reference's lsqr_solve, default iteration limit) from a zero
+      // start on every right-hand side
+      std::vector<int> nl(nrhs, 0), il(nrhs, 0);
+      if (!c->lsqr.solve(c->d_rhs, d_x, c->d_q, eps, 0, nl.data(), il.data(), nullptr, 8, true))
+        return fail(c, AGB_ERR_CUDA, "lsqr after bicgstab: " + c->lsqr.err);
+      for (int r = 0; r < nrhs; ++r) {
+        nt[r] += nl[r];
+        is[r] = 10 + il[r];
+      }
+    }
     for (int r = 0; r < nrhs; ++r) {
       if (nit) nit[r] = nt[r];
       if (istop) istop[r] = is[r];
@@ -438,37 +466,40 @@ int assemble_general(agb_context* c, int precision) {
   const GeneralLayout& L = c->gl;
   if (L.nrow == 0 || L.nx == 0) return fail(c, AGB_ERR_ARG, "the boundary conditions leave no unknown");
   const int ncomp = (c->kind == AGB_STOKES) ? 9 : 1;
-  double *T = nullptr, *G = nullptr, *err = nullptr, *sys = nullptr;
-  CUDA_OR_FAIL(c, cudaMalloc(&T, (size_t)ncomp * L.nsp * L.nn * sizeof(double)));
-  CUDA_OR_FAIL(c, cudaMalloc(&G, (size_t)ncomp * L.nsp * L.nq * sizeof(double)));
-  CUDA_OR_FAIL(c, cudaMalloc(&err, (size_t)L.nsp * sizeof(double)));
-  cudaError_t e = general_integrals(L, c->gd, c->d_geom, c->d_xyz, c->rule, c->iqud, c->iopt, T, G, err, c->stream);
+  // temporaries freed on every return (an allocation failure on a large body
+  // must not leave gigabytes of integrals or system behind)
+  DevTemp<double> T, G, err, sys;
+  DevTemp<float> a32;
+  CUDA_OR_FAIL(c, cudaMalloc(&T.p, (size_t)ncomp * L.nsp * L.nn * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMalloc(&G.p, (size_t)ncomp * L.nsp * L.nq * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMalloc(&err.p, (size_t)L.nsp * sizeof(double)));
+  cudaError_t e = general_integrals(L, c->gd, c->d_geom, c->d_xyz, c->rule, c->iqud, c->iopt, T.p, G.p, err.p,
+                                    c->stream);
   c->nlaunch += 2 * (int)((L.nsp + 65534) / 65535 + 1);
-  if (e != cudaSuccess) { cudaFree(T); cudaFree(G); cudaFree(err); return fail(c, AGB_ERR_CUDA, std::string("general integrals: ") + cudaGetErrorString(e)); }
+  if (e != cudaSuccess) return fail(c, AGB_ERR_CUDA, std::string("general integrals: ") + cudaGetErrorString(e));
   c->lda = ((int64_t)L.nx + 31) / 32 * 32;
   c->m = L.nrow;
   c->n = L.nx;
-  CUDA_OR_FAIL(c, cudaMalloc(&sys, (size_t)L.nrow * c->lda * sizeof(double)));
-  CUDA_OR_FAIL(c, cudaMemsetAsync(sys, 0, (size_t)L.nrow * c->lda * sizeof(double), c->stream));
+  CUDA_OR_FAIL(c, cudaMalloc(&sys.p, (size_t)L.nrow * c->lda * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMemsetAsync(sys.p, 0, (size_t)L.nrow * c->lda * sizeof(double), c->stream));
   CUDA_OR_FAIL(c, cudaMalloc(&c->d_rhsM, (size_t)L.nrow * std::max(L.nb, 1) * sizeof(double)));
   CUDA_OR_FAIL(c, cudaMemsetAsync(c->d_rhsM, 0, (size_t)L.nrow * std::max(L.nb, 1) * sizeof(double), c->stream));
-  CUDA_OR_FAIL(c, general_form(L, c->gd, T, G, sys, c->lda, c->d_rhsM, c->stream));
+  CUDA_OR_FAIL(c, general_form(L, c->gd, T.p, G.p, sys.p, c->lda, c->d_rhsM, c->stream));
   c->nlaunch += 1;
   CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
-  cudaFree(T);
-  cudaFree(G);
-  cudaFree(err);
+  T.reset();
+  G.reset();
+  err.reset();
   c->prec = precision;
   if (precision == AGB_MIXED) {
-    float* a32 = nullptr;
-    CUDA_OR_FAIL(c, cudaMalloc(&a32, (size_t)L.nrow * c->lda * sizeof(float)));
-    CUDA_OR_FAIL(c, to_fp32(sys, a32, (int64_t)L.nrow * c->lda, c->stream));
+    CUDA_OR_FAIL(c, cudaMalloc(&a32.p, (size_t)L.nrow * c->lda * sizeof(float)));
+    CUDA_OR_FAIL(c, to_fp32(sys.p, a32.p, (int64_t)L.nrow * c->lda, c->stream));
     c->nlaunch += 1;
     CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
-    cudaFree(sys);
-    c->d_A = a32;
+    sys.reset();
+    c->d_A = a32.release();
   } else {
-    c->d_A = sys;
+    c->d_A = sys.release();
   }
   CUDA_OR_FAIL(c, cudaMalloc(&c->d_q, c->lda * sizeof(double)));
   if (!c->lsqr.setup(c->d_A, precision == AGB_MIXED, c->m, c->n, c->lda, 1, c->stream)) return fail(c, AGB_ERR_CUDA, c->lsqr.err);
@@ -687,8 +718,8 @@ int agb_set_integration(agb_context* c, int sing_mode, int rec_depth, double nea
 
 int agb_set_solver(agb_context* c, int solver) {
   if (!c) return fail(c, AGB_ERR_ARG, "agb_set_solver: no context");
-  if (solver != AGB_SOLVER_LSQR && solver != AGB_SOLVER_BICGSTAB)
-    return fail(c, AGB_ERR_ARG, "solver must be AGB_SOLVER_LSQR or AGB_SOLVER_BICGSTAB");
+  if (solver != AGB_SOLVER_LSQR && solver != AGB_SOLVER_BICGSTAB && solver != AGB_SOLVER_HYBRID)
+    return fail(c, AGB_ERR_ARG, "solver must be AGB_SOLVER_LSQR, AGB_SOLVER_BICGSTAB or AGB_SOLVER_HYBRID");
   c->solver = solver;
   return AGB_OK;
 }
@@ -1352,7 +1383,7 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
   auto solver_bytes = [&](int i) {
     const BatchSlot& b = slots[i];
     const double mpad = std::ceil(b.m / 256.0) * 256.0;
-    const double bicg = (c->solver == AGB_SOLVER_BICGSTAB) ? mpad * 8 * 8 * 7.0 + mpad * 8 : 0.0;
+    const double bicg = (c->solver != AGB_SOLVER_LSQR) ? mpad * 8 * 8 * 7.0 + mpad * 8 : 0.0;
     return mpad * 8 * 12.0 + (double)b.lda * 8 * (8 * 3 + 4 + 8 * 8) + 65536.0 + bicg;
   };
   double budget = mem_gb * 1e9;
@@ -1517,8 +1548,32 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
     }
     std::vector<int> nv, iv;
     std::string err;
-    if (c->solver == AGB_SOLVER_BICGSTAB) {
+    if (c->solver != AGB_SOLVER_LSQR) {
       if (!batch_bicgstab_solve(bodies, 6, eps, maxit, st, nv, iv, &bst, err)) return bail(AGB_ERR_CUDA, "solve: " + err);
+      if (c->solver == AGB_SOLVER_HYBRID) {
+        // bodies with a right-hand side BiCGSTAB did not converge: batched LSQR
+        // (default tiles, the reference's iteration limit) from a zero start
+        std::vector<BatchBody> redo;
+        std::vector<size_t> where;
+        for (size_t t = 0; t < bodies.size(); ++t) {
+          bool ok = true;
+          for (int r = 0; r < 6; ++r) ok = ok && iv[6 * t + r] == 0;
+          if (!ok) {
+            redo.push_back(bodies[t]);
+            where.push_back(t);
+          }
+        }
+        if (!redo.empty()) {
+          std::vector<int> nl, il;
+          if (!batch_lsqr_solve(redo, 6, eps, 0, tune, st, nl, il, &bst, err))
+            return bail(AGB_ERR_CUDA, "solve (LSQR after BiCGSTAB): " + err);
+          for (size_t u = 0; u < where.size(); ++u)
+            for (int r = 0; r < 6; ++r) {
+              nv[6 * where[u] + r] += nl[6 * u + r];
+              iv[6 * where[u] + r] = 10 + il[6 * u + r];
+            }
+        }
+      }
     } else if (!batch_lsqr_solve(bodies, 6, eps, maxit, tune, st, nv, iv, &bst, err)) {
       return bail(AGB_ERR_CUDA, "solve: " + err);
     }

@@ -36,12 +36,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 // this only guards against a hang); once any wait has given up (errflag set),
 // later long waits give up after ~1024 tries, so a launch whose barrier broke
 // ends quickly.  Returns whether the barrier phase completed.
-__device__ __forceinline__ bool mbar_wait_ok(uint64_t* bar, uint32_t parity, int* errflag) {
+// (limit: the number of failed tries before giving up; the kernels use 2^22,
+// the self-test entry point agb_selftest_bounded_wait a caller-given one)
+__device__ __forceinline__ bool mbar_wait_ok(uint64_t* bar, uint32_t parity, int* errflag,
+                                             uint32_t limit = (1u << 22)) {
   uint32_t tries = 0;
   while (!mbar_try_wait(bar, parity)) {
     ++tries;
     if ((tries & 1023u) == 0 && errflag && *(volatile int*)errflag) return false;
-    if (tries > (1u << 22)) {
+    if (tries > limit) {
       if (errflag) atomicExch(errflag, 1);
       return false;
     }
@@ -192,6 +195,55 @@ __device__ __forceinline__ void lsqr_phase(LsqrScalars& s, int c, int k, int pha
     s.gamma = (s.beta > 0.0) ? -s.alpha / s.beta : 0.0;
     if (s.beta <= 0.0) s.active = 0;
     if (s.active) atomicAdd(nactive, 1);
+  }
+}
+
+// BiCGSTAB state of one right-hand side at the start (||b||^2 = bb) and at the
+// end of an iteration (rr = ||r||^2, rho = r~ . r); shared by the single-system
+// and the batched solvers.
+__device__ __forceinline__ void bicg_start(BicgScalars& q, double bb, bool used) {
+  q.bnorm = sqrt(bb);
+  q.rho = bb;  // r~ = r0 = b
+  q.rho_old = q.alpha = q.omega = 1.0;
+  q.relres = (q.bnorm > 0.0) ? 1.0 : 0.0;
+  q.snorm = q.relres;
+  q.best = q.relres;
+  q.its = 0;
+  q.half = 0;
+  q.since = 0;
+  q.active = (used && q.bnorm > 0.0) ? 1 : 0;
+  q.status = q.active ? -1 : 0;
+}
+__device__ __forceinline__ void bicg_end(BicgScalars& q, double rr, double rho, double tol, int maxit) {
+  q.its += 1;
+  if (q.half) {
+    q.relres = q.snorm;
+    q.status = 0;
+    q.active = 0;
+    return;
+  }
+  q.relres = sqrt(rr) / q.bnorm;
+  if (q.relres <= tol) {
+    q.status = 0;
+    q.active = 0;
+  } else if (q.its >= maxit) {
+    q.status = 1;
+    q.active = 0;
+  } else if (rho == 0.0 || q.omega == 0.0 || !isfinite(q.relres)) {
+    q.status = 2;
+    q.active = 0;
+  } else if (q.relres > BICG_DIVERGE * q.best || (q.relres >= 0.9 * q.best && q.since + 1 >= BICG_STALL)) {
+    q.status = 3;
+    q.active = 0;
+  } else {
+    if (q.relres < 0.9 * q.best) {
+      q.best = q.relres;
+      q.since = 0;
+    } else {
+      q.since += 1;
+    }
+    q.rho_old = q.rho;
+    q.rho = rho;
   }
 }
 

@@ -356,15 +356,7 @@ __global__ void __launch_bounds__(256) gb_scal(const GDesc* __restrict__ D, int 
     BicgScalars& q = d.bs[c];
     const double s0 = ssum[0][c], s1 = ssum[1][c];
     if (phase == 0) {
-      q.bnorm = sqrt(s0);
-      q.rho = s0;
-      q.rho_old = q.alpha = q.omega = 1.0;
-      q.relres = (q.bnorm > 0.0) ? 1.0 : 0.0;
-      q.snorm = q.relres;
-      q.its = 0;
-      q.half = 0;
-      q.active = (c < d.k && q.bnorm > 0.0) ? 1 : 0;
-      q.status = q.active ? -1 : 0;
+      bicg_start(q, s0, c < d.k);
     } else if (q.active) {
       if (phase == 1) {
         if (s0 == 0.0 || !isfinite(s0)) { q.status = 2; q.active = 0; q.alpha = 0.0; }
@@ -378,16 +370,7 @@ __global__ void __launch_bounds__(256) gb_scal(const GDesc* __restrict__ D, int 
           else q.omega = s0 / s1;
         }
       } else {
-        q.its += 1;
-        if (q.half) {
-          q.relres = q.snorm; q.status = 0; q.active = 0;
-        } else {
-          q.relres = sqrt(s0) / q.bnorm;
-          if (q.relres <= tol) { q.status = 0; q.active = 0; }
-          else if (q.its >= d.itnlim) { q.status = 1; q.active = 0; }
-          else if (s1 == 0.0 || q.omega == 0.0 || !isfinite(q.relres)) { q.status = 2; q.active = 0; }
-          else { q.rho_old = q.rho; q.rho = s1; }
-        }
+        bicg_end(q, s0, s1, tol, d.itnlim);
       }
     }
   }

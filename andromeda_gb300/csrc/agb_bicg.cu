@@ -107,16 +107,7 @@ __global__ void k_bg_start(const double* __restrict__ part, int k, BicgScalars* 
   int na = 0;
   for (int c = 0; c < 8; ++c) {
     BicgScalars& q = s[c];
-    const double bb = part_total(part, 0, c);
-    q.bnorm = sqrt(bb);
-    q.rho = bb;  // r~ = r0 = b
-    q.rho_old = q.alpha = q.omega = 1.0;
-    q.relres = (q.bnorm > 0.0) ? 1.0 : 0.0;
-    q.snorm = q.relres;
-    q.its = 0;
-    q.half = 0;
-    q.active = (c < k && q.bnorm > 0.0) ? 1 : 0;
-    q.status = q.active ? -1 : 0;
+    bicg_start(q, part_total(part, 0, c), c < k);
     na += q.active;
   }
   *nactive = na;
@@ -262,30 +253,7 @@ __global__ void k_bg_end(const double* __restrict__ part, double tol, int maxit,
   int na = 0;
   for (int c = 0; c < 8; ++c) {
     BicgScalars& q = s[c];
-    if (q.active) {
-      q.its += 1;
-      if (q.half) {
-        q.relres = q.snorm;
-        q.status = 0;
-        q.active = 0;
-      } else {
-        q.relres = sqrt(part_total(part, 0, c)) / q.bnorm;
-        const double rho = part_total(part, 1, c);
-        if (q.relres <= tol) {
-          q.status = 0;
-          q.active = 0;
-        } else if (q.its >= maxit) {
-          q.status = 1;
-          q.active = 0;
-        } else if (rho == 0.0 || q.omega == 0.0 || !isfinite(q.relres)) {
-          q.status = 2;
-          q.active = 0;
-        } else {
-          q.rho_old = q.rho;
-          q.rho = rho;
-        }
-      }
-    }
+    if (q.active) bicg_end(q, part_total(part, 0, c), part_total(part, 1, c), tol, maxit);
     na += q.active;
   }
   *nactive = na;

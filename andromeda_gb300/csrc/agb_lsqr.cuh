@@ -18,11 +18,17 @@ struct LsqrScalars {
 };
 
 // Per right-hand-side BiCGSTAB state (DenseLsqr::bicgstab), FP64.  status: -1
-// running, 0 converged, 1 iteration limit, 2 breakdown.
+// running, 0 converged, 1 iteration limit, 2 breakdown, 3 diverged or
+// stagnated (best: the smallest relative residual so far; since: iterations
+// since it last fell by 10 %).
 struct BicgScalars {
-  double rho, rho_old, alpha, omega, bnorm, relres, snorm;
-  int its, status, active, half;
+  double rho, rho_old, alpha, omega, bnorm, relres, snorm, best;
+  int its, status, active, half, since;
 };
+// BiCGSTAB stops a right-hand side whose residual grew BICG_DIVERGE times
+// above its best, or did not fall by 10 % within BICG_STALL iterations.
+constexpr double BICG_DIVERGE = 1.0e3;
+constexpr int BICG_STALL = 200;
 
 // Dense block LSQR.  A is m x n row-major with leading dimension lda (lda is
 // a multiple of 32 and columns n..lda-1 are zero).  T = float (mixed path)

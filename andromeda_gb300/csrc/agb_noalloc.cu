@@ -11,15 +11,20 @@
 // The scratch array (AGB_NOALLOC_SCRATCH_DOUBLES doubles = 8 MiB) lives in the
 // library's device image: every GPU that loads the library holds it until the
 // process exits.  Host code cannot use the array's name as a device address,
-// so the first call on each device looks the address up with
-// cudaGetSymbolAddress (with that device current) and caches it; make that
-// first call before any stream capture.  Every call on a device shares the one
+// so the first call in each CUDA context looks the address up with
+// cudaGetSymbolAddress (with that context's device current) and caches it under
+// the context's unique id; make that first call before any stream capture.  A
+// new context -- another device, a context that is not the primary one (as some
+// OpenACC or driver-API hosts make current), or the primary context re-created
+// after cudaDeviceReset -- has a new id, so its first call looks the address up
+// again instead of reusing an address of a module image that no longer exists.  Every call on a device shares the one
 // array and leaves its contents behind: calls whose kernels overlap on the GPU
 // (different streams or host threads) race on it and must be serialised by
 // the caller.  Nothing in the scratch needs to start at zero: each call writes
 // every entry it later reads.
 #include "../../include/andromeda_gb300.h"
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <mutex>
 #include <string>
@@ -32,9 +37,43 @@ static __device__ __align__(256) double g_noalloc_scratch[AGB_NOALLOC_SCRATCH_DO
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-double* g_scratch_ptr[kMaxDevices] = {};
+// scratch addresses by context id (cuCtxGetId: unique over the life of the
+// process, never reused); a full table starts over
+constexpr int kMaxContexts = 64;
+struct ScratchEntry {
+  unsigned long long ctx_id;
+  double* ptr;
+};
+ScratchEntry g_scratch[kMaxContexts];
+int g_nscratch = 0;
 std::mutex g_scratch_mu;
+
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+
+// unique id of the calling thread's current context (made current by the
+// runtime if there is none yet)
+cudaError_t current_context_id(unsigned long long* id) {
+  static PfnCtxGetCurrent get_current = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  if (!get_current || !get_id) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    void *f1 = nullptr, *f2 = nullptr;
+    cudaError_t e = cudaGetDriverEntryPoint("cuCtxGetCurrent", &f1, cudaEnableDefault, &q1);
+    if (e == cudaSuccess) e = cudaGetDriverEntryPoint("cuCtxGetId", &f2, cudaEnableDefault, &q2);
+    if (e != cudaSuccess) return e;
+    if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return cudaErrorNotSupported;
+    get_current = reinterpret_cast<PfnCtxGetCurrent>(f1);
+    get_id = reinterpret_cast<PfnCtxGetId>(f2);
+  }
+  cudaError_t e = cudaFree(nullptr);  // makes the device's primary context current if none is
+  if (e != cudaSuccess) return e;
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return cudaErrorDeviceUninitialized;
+  if (get_id(ctx, id) != CUDA_SUCCESS) return cudaErrorDeviceUninitialized;
+  return cudaSuccess;
+}
 
 // Per-row-group column sums of squares: P[g][j] = sum_{r in group g} A(r,j)^2
 // (one thread per column, rows of the group in order -> coalesced row reads).
@@ -87,20 +126,22 @@ extern "C" int agb_lsqr_precon_dense_noalloc(int m, int n, int64_t lda, double* 
   if (m <= 0 || n <= 0 || lda < n || !A || !q) return fail(AGB_ERR_ARG, "agb_lsqr_precon_dense_noalloc: bad sizes or NULL pointer");
   if ((int64_t)n > (int64_t)AGB_NOALLOC_SCRATCH_DOUBLES)
     return fail(AGB_ERR_ARG, "agb_lsqr_precon_dense_noalloc: n exceeds AGB_NOALLOC_MAX_COLUMNS (1048576)");
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return fail(AGB_ERR_CUDA, "cudaGetDevice", e);
-  if (dev < 0 || dev >= kMaxDevices) return fail(AGB_ERR_ARG, "device index beyond the supported range");
+  unsigned long long ctx_id = 0;
+  cudaError_t e = current_context_id(&ctx_id);
+  if (e != cudaSuccess) return fail(AGB_ERR_CUDA, "agb_lsqr_precon_dense_noalloc: current CUDA context", e);
   double* scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
+    for (int i = 0; i < g_nscratch; ++i)
+      if (g_scratch[i].ctx_id == ctx_id) scratch = g_scratch[i].ptr;
+    if (!scratch) {
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
       if (e != cudaSuccess) return fail(AGB_ERR_CUDA, "cudaGetSymbolAddress(g_noalloc_scratch)", e);
-      g_scratch_ptr[dev] = static_cast<double*>(p);
+      scratch = static_cast<double*>(p);
+      if (g_nscratch == kMaxContexts) g_nscratch = 0;
+      g_scratch[g_nscratch++] = {ctx_id, scratch};
     }
-    scratch = g_scratch_ptr[dev];
   }
   // row groups: as many as the scratch holds, at most 64
   int groups = (int)(AGB_NOALLOC_SCRATCH_DOUBLES / n);

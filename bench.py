@@ -44,12 +44,18 @@ def parse():
     ap.add_argument("--outer-level", type=int, default=2)
     ap.add_argument("--outer-radius", type=float, default=200.0)
     ap.add_argument("--eps", type=float, default=1e-7)
-    ap.add_argument("--solver", default="lsqr", choices=["lsqr", "bicgstab"],
-                    help="sphere, batch, large: LSQR (lsqr_solve, the default) or BiCGSTAB-Jacobi (the LIS path's solver)")
-    ap.add_argument("--fp64-iters", type=int, default=16, help="FP64 comparator LSQR sample (iterations)")
-    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--solver", default="lsqr", choices=["lsqr", "bicgstab", "hybrid"],
+                    help="sphere, batch, large: LSQR (lsqr_solve, the default), BiCGSTAB-Jacobi (the LIS path's "
+                         "solver), or hybrid (BiCGSTAB, LSQR for the systems where it does not converge)")
+    ap.add_argument("--fp64", default="full", choices=["full", "off"],
+                    help="sphere: the plain FP64 GPU comparator solved to convergence at the same eps (full)")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the full-size CPU estimate's sample")
+    ap.add_argument("--cpu-level", type=int, default=2,
+                    help="icosphere level of the body the CPU solves completely (the full-size body takes hours)")
+    ap.add_argument("--cpu-solves", type=int, default=3, help="sphere: complete CPU solves of the small body")
+    ap.add_argument("--c2-estimate", type=int, default=1, help="also estimate the full-size CPU solve (labelled)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--workload", default="sphere", choices=["sphere", "batch", "surrogate", "large", "laplace"],
                     help="sphere: one level-5 sphere (default); batch: the many-body superellipsoid set")
     ap.add_argument("--bodies", type=int, default=512, help="batch workload: number of bodies")
@@ -67,19 +73,29 @@ def parse():
                     help="large: packed FP32 matrix resident in HBM and solved to convergence, or matrix-free sweeps")
     ap.add_argument("--large-maxit", type=int, default=0, help="large/resident: LSQR iteration limit (0: reference default)")
     ap.add_argument("--grid", default="160x320", help="large: superellipsoid rings x sectors")
+    ap.add_argument("--large-fp64-eps", type=float, default=1e-10,
+                    help="large/resident: also solve the FP64 path to this eps where its matrix fits (0: off)")
     ap.add_argument("--itri", type=int, default=1, help="laplace: triangle rule (1 = 7 points)")
     ap.add_argument("--laplace-eps", type=float, default=1e-12, help="laplace: LSQR eps")
     return ap.parse_args()
+
+
+def solver_id(A, name):
+    return {"lsqr": A.SOLVER_LSQR, "bicgstab": A.SOLVER_BICGSTAB, "hybrid": A.SOLVER_HYBRID}[name]
+
+
+def solver_text(name, eps):
+    return {"lsqr": f"LSQR eps {eps:g}", "bicgstab": f"BiCGSTAB-Jacobi tol {eps:g}",
+            "hybrid": f"BiCGSTAB-Jacobi tol {eps:g}, LSQR eps {eps:g} where it does not converge"}[name]
 
 
 def workload(args):
     from andromeda_gb300 import mesh as M
     p = M.icosphere(args.level, 1.0, inward=True)
     m = M.particle_in_sphere(p, outer_level=args.outer_level, outer_radius=args.outer_radius)
-    solver = "BiCGSTAB-Jacobi tol" if getattr(args, "solver", "lsqr") == "bicgstab" else "LSQR eps"
     name = (f"Stokes sphere a=1 icosphere L{args.level} ({len(p['etype'])} tri) in L{args.outer_level} container "
             f"r={args.outer_radius:g} ({len(m['etype']) - len(p['etype'])} tri), 6 RHS, ITRI 5, mu=1, "
-            f"{solver} {args.eps:g}")
+            f"{solver_text(getattr(args, 'solver', 'lsqr'), args.eps)}")
     return m, name
 
 
@@ -156,6 +172,30 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+# FLOPs of k_stokes_G per (collocation point, element, quadrature point)
+STOKES_G_FLOPS_PER_POINT = 28
+
+
+def fp32_peak_tflops():
+    """Nominal FP32 peak of the GPU: SMs x 128 FP32 lanes x 2 (FMA) x the
+    maximum SM clock (measured clock from MEASURED_PEAKS.json when present).
+    No measured FP32 figure exists, so this is the nominal one."""
+    sms = 152
+    try:
+        import torch
+        if torch.cuda.is_available():
+            sms = torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        pass
+    mhz, src = 2070.0, "nominal (152 SMs x 128 lanes x 2 x 2070 MHz)"
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            mhz = float(json.load(f).get("sm_max_mhz", mhz))
+    src = f"nominal: {sms} SMs x 128 FP32 lanes x 2 (FMA) x {mhz:g} MHz"
+    return sms * 128 * 2 * mhz * 1e6 / 1e12, src
+
+
 def dist_env():
     from andromeda_gb300.ranks import dist_env as env
     return env()
@@ -164,37 +204,69 @@ def dist_env():
 # ---------------------------------------------------------------------------
 # CPU baseline: the FP64 restatement of the reference on the host cores
 # ---------------------------------------------------------------------------
-def cpu_baseline(m, nit_total, budget_s):
-    """Time a bounded sample of the reference algorithm and scale it to one
-    resistance-tensor solve of the same workload:
-      * integration: CoR_Integrals_Stokes computes all nsp = nnodes + nelem
-        rows (u- and q-source points, 18 component matrices); a slice of
-        rows is timed with all host threads and scaled by nsp;
-      * LSQR: the reference's serial CRS lsqr_solve; iterations on a smaller
-        system of the same kind are timed per nonzero and scaled to the
-        62400^2 system and to the iterations the solve needs (sum over the six
-        sequential right-hand sides)."""
-    import numpy as np
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
+    return oracle
+
+
+def small_body(level, outer_level, outer_radius):
     from andromeda_gb300 import mesh as M
+    p = M.icosphere(level, 1.0, inward=True)
+    m = M.particle_in_sphere(p, outer_level=outer_level, outer_radius=outer_radius)
+    name = (f"Stokes sphere a=1 icosphere L{level} ({len(p['etype'])} tri) in L{outer_level} container "
+            f"r={outer_radius:g} ({len(m['etype']) - len(p['etype'])} tri), 6 RHS, ITRI 5, mu=1")
+    return m, name
+
+
+def cpu_complete_solve(m, eps):
+    """One complete resistance-tensor solve by the reference algorithm (the
+    oracle's FP64 restatement), timed in full: CoR_Integrals_Stokes over all
+    nsp = nnodes + nelem source rows on every host thread (the reference
+    splits rows over MPI ranks), then per right-hand side the reference's
+    serial CRS system, lsqr_precon + lsqr_solve to eps and the force/torque
+    integrals (StokesInlet3sidesForceCRS / ...TorqueOmegaCRS, one field after
+    another).  Nothing is scaled."""
+    import numpy as np
+    oracle = _oracle()
+    U = rigid_fields(m)
+    t0 = time.perf_counter()
+    P = oracle.Problem(2, m, walls=[1, 2], known=np.ones((3, 2)), itri=5)
+    P.form_integrals()
+    t1 = time.perf_counter()
+    _, ft, nits, ierr = P.stokes_solve_sequence(U, maxit=0, eps=eps, fwall=1)
+    t2 = time.perf_counter()
+    P.close()
+    return {"seconds": t2 - t0, "integration_s": t1 - t0, "solve_s": t2 - t1, "nit": [int(v) for v in nits],
+            "ierr": int(ierr), "R": ft}
+
+
+def cpu_c2_estimate(m, nit_fp64, budget_s):
+    """Estimate (not a measurement) of one solve of the full-size workload by
+    the reference algorithm on these cores, which would take hours:
+      * integration: a slice of the source rows of this very mesh at ITRI 5 on
+        every host thread, scaled by nsp (every row integrates over all
+        elements, so the cost per row is uniform);
+      * LSQR: serial CRS iterations on the ITRI-5 system of a smaller body of
+        the same kind, per nonzero, scaled to the full system's nonzeros and to
+        the FP64 LSQR iteration counts of this workload (nit_fp64, summed over
+        the six right-hand sides the reference solves one after another)."""
+    import numpy as np
+    oracle = _oracle()
     threads = os.cpu_count() or 1
     P = oracle.Problem(2, m, walls=[1, 2], known=np.ones((3, 2)), itri=5)
     nsp = P.nsp
-    # rows: start from the q-source rows (the used ones) -- same cost per row
     t_row, rows = 0.0, 0
     r0 = P.sd_nnodes
-    chunk = threads
     t_start = time.perf_counter()
     while time.perf_counter() - t_start < 0.5 * budget_s and rows < 4 * threads * 8:
-        t, _ = P.time_rows(r0 + rows, r0 + rows + chunk, threads, )
+        t, _ = P.time_rows(r0 + rows, r0 + rows + threads, threads)
         t_row += t
-        rows += chunk
+        rows += threads
     P.close()
     t_integration = t_row / rows * nsp
-    # LSQR on a smaller problem of the same kind (level-3 sphere in container)
-    ms = M.particle_in_sphere(M.icosphere(3, 1.0, inward=True), outer_level=2, outer_radius=200.0)
-    Ps = oracle.Problem(2, ms, walls=[1, 2], known=np.ones((3, 2)), itri=1)
+    ms, _ = small_body(3, 2, 200.0)
+    Ps = oracle.Problem(2, ms, walls=[1, 2], known=np.ones((3, 2)), itri=5)
     Ps.form_integrals()
     Ps.form_system()
     ia, ja, a = Ps.crs(0)
@@ -210,39 +282,62 @@ def cpu_baseline(m, nit_total, budget_s):
             break
         it *= 2
     per_nnz_iter = dt / (it * len(a))
-    nnz_full = float(3 * len(m["etype"])) ** 2
-    t_lsqr = per_nnz_iter * nnz_full * nit_total
+    n_full = 3 * len(m["etype"])
+    nit_total = int(sum(nit_fp64))
+    t_lsqr = per_nnz_iter * float(n_full) ** 2 * nit_total
     total = t_integration + t_lsqr
-    sample = (f"{rows} of {nsp} integration rows on {threads} threads (scaled by nsp) + {it} serial CRS LSQR "
-              f"iterations on a {Ps.neq_rows}^2 system of the same kind (scaled by nnz to {3 * len(m['etype'])}^2 and "
-              f"to {nit_total} iterations = sum over the 6 sequential right-hand sides)")
-    return {"value": 1.0 / total, "unit": "solves/s", "cores": threads, "kind": "port", "sample": sample,
-            "seconds_per_solve": total, "integration_s": t_integration, "lsqr_s": t_lsqr,
-            "lsqr_threads": 1}
+    return {"kind": "extrapolated", "seconds_per_solve": total, "solves_per_s": 1.0 / total,
+            "integration_s": t_integration, "lsqr_s": t_lsqr, "cores": threads, "lsqr_threads": 1,
+            "sample": (f"{rows} of {nsp} integration rows (ITRI 5) on {threads} threads, scaled by nsp; {it} serial "
+                       f"CRS LSQR iterations on the ITRI-5 {Ps.neq_rows}^2 system of the L3 sphere, scaled by nnz "
+                       f"to {n_full}^2 and to {nit_total} iterations (FP64 LSQR counts {list(nit_fp64)} of this "
+                       f"workload, summed over the six sequential right-hand sides)")}
 
 
-# LSQR iterations of this workload at eps 1e-7, measured on the GPU path
-# (763 per translation, 250 per rotation); the reference solves the six
-# right-hand sides one after another, so its iteration total is their sum.
-C2_NIT_EPS1E7 = [763, 763, 763, 250, 251, 250]
+# FP64 LSQR iteration counts of the full-size workload at eps 1e-7 (the six
+# rigid motions), from the converged FP64 GPU solve, whose LSQR recurrence is
+# the reference's (iteration counts equal to the oracle's on every tested
+# system); used only by the estimate above when the reference arm runs alone.
+C2_NIT_FP64_EPS1E7 = None
 
 
 def run_reference(args, rank):
+    """Reference arm: complete solves by the reference algorithm (the FP64
+    oracle port) on the host cores, each step one full resistance-tensor solve
+    of a body small enough to finish in seconds (the L2 sphere in the same
+    container); the full-size workload's time is given as an estimate beside
+    it, labelled as such."""
     if rank != 0:
         return
-    m, name = workload(args)
-    nit_total = sum(C2_NIT_EPS1E7) if (args.level == 5 and abs(args.eps - 1e-7) < 1e-12) else 6 * 500
-    vals = []
-    info = None
+    import numpy as np
+    m, name = small_body(args.cpu_level, args.outer_level, args.outer_radius)
+    for _ in range(args.warmup):
+        cpu_complete_solve(m, args.eps)
+    secs, last = [], None
+    t0 = time.perf_counter()
     for _ in range(args.steps):
-        info = cpu_baseline(m, nit_total, args.cpu_seconds)
-        vals.append(info["value"])
-    v = statistics.median(vals)
+        last = cpu_complete_solve(m, args.eps)
+        secs.append(last["seconds"])
+    wall = time.perf_counter() - t0
+    v = args.steps / sum(secs)
+    threads = os.cpu_count() or 1
+    est = None
+    if args.c2_estimate:
+        mf, _ = workload(args)
+        nit64 = C2_NIT_FP64_EPS1E7 if (args.level == 5 and abs(args.eps - 1e-7) < 1e-12 and C2_NIT_FP64_EPS1E7) \
+            else None
+        if nit64:
+            est = cpu_c2_estimate(mf, nit64, args.cpu_seconds)
     line = {"metric": METRIC, "value": v, "unit": "solves/s", "impl": "reference", "n_gpus": 0, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": name, "iterations_assumed": nit_total},
-            "cpu_baseline": {k: info[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "warmup": args.warmup, "ms_per_step": 1000.0 * sum(secs) / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (meshes generated in-process)",
+            "config": {"workload": f"{name}, LSQR eps {args.eps:g} (complete solves; the full-size L{args.level} "
+                                   f"workload takes hours on the host cores, see c2_estimate)",
+                       "same_body_as_gpu_line": False, "nit": last["nit"]},
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} complete solves of the L{args.cpu_level} body, nothing scaled "
+                                       f"(integration on {threads} threads, serial CRS LSQR per right-hand side)"},
+            "host_s": wall, "c2_estimate": est,
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -264,7 +359,7 @@ def run_batch(args, rank, world, local):
     eps = args.batch_eps
     tune = not args.no_autotune
     warm = mine[:32]
-    solver = A.SOLVER_BICGSTAB if args.solver == "bicgstab" else A.SOLVER_LSQR
+    solver = solver_id(A, args.solver)
     for _ in range(args.warmup):
         A.batch_resistance(warm, eps=eps, ctx=ctx, autotune=tune, solver=solver)
     barrier()
@@ -317,8 +412,7 @@ def run_batch(args, rank, world, local):
                 "config": {"workload": f"{args.bodies} superellipsoids a=1, b,c~U(0.2,1), e1,e2~U(0.3,1.8), "
                                        f"random orientation, {int(ne.min())}..{int(ne.max())} tri (mean "
                                        f"{ne.mean():.0f}), each in an L2 container r=200, 6 RHS, ITRI 5, "
-                                       + (f"BiCGSTAB-Jacobi tol {eps:g}" if args.solver == "bicgstab"
-                                          else f"LSQR eps {eps:g}"),
+                                       + solver_text(args.solver, eps),
                            "precision": "mixed", "parallelism": "bodies split over ranks" if world > 1 else
                            "single GPU", "l2": "inputs larger than L2 (waves of tens of GB), no flush",
                            "warmup": f"{args.warmup} x the first {len(warm)} bodies"},
@@ -363,7 +457,7 @@ def run_large(args):
     C = A.Context(0)
     C.set_mesh(m)
     C.set_problem(A.STOKES, [1, 2], A.dirichlet_known(A.STOKES, 2), itri=5)
-    C.set_solver(A.SOLVER_BICGSTAB if args.solver == "bicgstab" else A.SOLVER_LSQR)
+    C.set_solver(solver_id(A, args.solver))
     ne = len(m["etype"])
     workload = (f"superellipsoid a=1 b=0.5 c=0.25 e1=0.6 e2=1.4, {nr}x{ns} grid ({len(body['etype'])} tri) "
                 f"in an L2 container r=200, 6 RHS, ITRI 5")
@@ -392,16 +486,37 @@ def run_large(args):
         peak, peak_kind = measured_peaks()
         alg = 24.0 * ne * ne
         sym = float(np.max(np.abs(R - R.T)) / np.max(np.abs(R)))
+        # error against the plain FP64 path on the same body, where its dense FP64
+        # matrix (3 ne x 3 ne x 8 B) fits the free device memory
+        fp64 = None
+        if args.large_fp64_eps > 0:
+            try:
+                import torch
+                free_b = torch.cuda.mem_get_info(0)[0]
+            except Exception:
+                free_b = None
+            need = 72.0 * ne * ((ne + 31) // 32 * 32) * 1.02
+            if free_b is None or need < 0.9 * free_b + 24.0 * ne * ne:
+                C.set_solver(A.SOLVER_LSQR)
+                R64, nit64, info64 = C.resistance_tensor(A.FP64, 1, 2, eps=args.large_fp64_eps)
+                fp64 = {"rel_err_vs_fp64": float(np.max(np.abs(R - R64)) / np.max(np.abs(R64))),
+                        "fp64_eps": args.large_fp64_eps, "fp64_nit": [int(v) for v in nit64],
+                        "fp64_istop": [int(v) for v in info64["istop"]], "fp64_device_ms": info64["device_ms"],
+                        "force_torque_rel_err": {
+                            "drag": float(np.max(np.abs(np.diag(R)[:3] - np.diag(R64)[:3]) / np.abs(np.diag(R64)[:3]))),
+                            "torque": float(np.max(np.abs(np.diag(R)[3:] - np.diag(R64)[3:]) /
+                                                   np.abs(np.diag(R64)[3:])))}}
+            else:
+                fp64 = {"skipped": f"the FP64 matrix ({need / 1e9:.0f} GB) does not fit"}
         line = {"metric": "Stokes resistance-tensor solves/s, single large body (mixed, packed matrix resident)",
                 "value": 1000.0 / info["device_ms"], "unit": "solves/s", "n_gpus": 1, "steps": 1, "warmup": 0,
                 "ms_per_step": info["device_ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "fp32 (fp64 singular/free-term/reductions)", "data": "synthetic",
-                "config": {"workload": workload + (f", BiCGSTAB-Jacobi tol {args.eps:g}" if args.solver == "bicgstab"
-                                                   else f", LSQR eps {args.eps:g}"), "unknowns": C.n,
+                "config": {"workload": workload + ", " + solver_text(args.solver, args.eps), "unknowns": C.n,
                            "packed_matrix_gb": alg / 1e9, "l2": "inputs larger than L2, no flush"},
                 "assemble_ms": info["assemble_ms"], "rhs_ms": info["rhs_ms"], "solve_ms": info["solve_ms"],
                 "nit": [int(v) for v in nit], "istop": info["istop"],
-                "tensor_asymmetry": sym, "R": R.tolist(),
+                "tensor_asymmetry": sym, "fp64_check": fp64, "R": R.tolist(),
                 "sweep_ms": {"av": av_ms, "atu": atu_ms},
                 "roofline": {"bound": "hbm", "kernel": "k_avp (packed A*V sweep, 253 GB per launch)",
                              "achieved": alg / (av_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
@@ -630,7 +745,7 @@ def main():
     C = A.Context(local if world > 1 else 0)
     C.set_mesh(m)
     C.set_problem(A.STOKES, [1, 2], A.dirichlet_known(A.STOKES, 2), itri=5)
-    solver = A.SOLVER_BICGSTAB if args.solver == "bicgstab" else A.SOLVER_LSQR
+    solver = solver_id(A, args.solver)
     C.set_solver(solver)
 
     def step():
@@ -664,7 +779,7 @@ def main():
     if os.path.exists(GOLDEN_TRUTH):
         with open(GOLDEN_TRUTH) as f:
             g = json.load(f)
-        if g.get("workload") == name.split(", LSQR")[0].split(", BiCGSTAB")[0]:
+        if g.get("workload") == name.split(", LSQR")[0].split(", BiCGSTAB")[0]:  # the mesh and BCs only
             Rt = np.array(g["R"])
             rel_err = float(np.max(np.abs(R - Rt)) / np.max(np.abs(Rt)))
     lam = 1.0 / args.outer_radius
@@ -686,7 +801,7 @@ def main():
             for line in f:
                 if line.startswith("traffic_bytes_per_launch_k_avp_c2:"):
                     traffic = float(line.split(":")[1])
-    which = "BiCGSTAB A D^-1 p / A D^-1 s sweeps" if args.solver == "bicgstab" else "LSQR A*V sweep"
+    which = "BiCGSTAB A D^-1 p / A D^-1 s sweeps" if args.solver != "lsqr" else "LSQR A*V sweep"
     roofline = {"bound": "hbm", "kernel": f"k_avp ({which} over the packed symmetric 3x3 blocks, FP32, TMA, 8 RHS)",
                 "achieved": a_bytes / (av_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                 "frac": a_bytes / (av_ms * 1e-3) / 1e9 / peak, "traffic": traffic, "peak_source": peak_kind,
@@ -711,27 +826,80 @@ def main():
     e2e = {"value": (world / statistics.median(e2e_vals)) if e2e_vals else None, "unit": "solves/s",
            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": len(e2e_vals)}
 
-    # plain FP64 GPU comparator: full FP64 assembly + a sample of FP64 LSQR
-    # iterations, scaled to the iteration count of the solve
+    # assembly roofline: k_stokes_G<float, packed>, the regular quadrature of
+    # every (collocation point, element) pair of the single layer; 28 flop per
+    # (pair, quadrature point), an FMA counted as 2 and the rsqrt as 1:
+    # r (3), r.r (5), rsqrt (1), w/r (1), 1/r^2 (1), w/r^3 (1), G accumulation
+    # (1), w r_a / r^3 (2), six symmetric r_a r_b sums (12: five FMAs and a
+    # multiply-add)
+    asm_ms = kt["assemble_ms"] / max(kt["assemble_launches"], 1)
+    q_pts = 126
+    asm_flops = float(ne_sys) ** 2 * q_pts * STOKES_G_FLOPS_PER_POINT
+    fp32_peak, fp32_kind = fp32_peak_tflops()
+    roofline_asm = {"bound": "fp32", "kernel": "k_stokes_G<float, packed> (single-layer regular quadrature, "
+                                               "ITRI 5: 126 points per pair)",
+                    "flops_per_launch": asm_flops, "ms": asm_ms,
+                    "achieved": asm_flops / (asm_ms * 1e-3) / 1e12 if asm_ms > 0 else None,
+                    "peak": fp32_peak, "unit": "TFLOP/s", "peak_source": fp32_kind,
+                    "frac": asm_flops / (asm_ms * 1e-3) / 1e12 / fp32_peak if asm_ms > 0 else None,
+                    "flops_per_pair_point": STOKES_G_FLOPS_PER_POINT}
+
+    # plain FP64 GPU comparator: FP64 assembly + FP64 LSQR to the same eps, to
+    # convergence, timed in full on the device
     fp64 = None
-    if args.fp64_iters > 0 and rank == 0:
-        C.set_solver(A.SOLVER_LSQR)  # the FP64 path solves with LSQR; a BiCGSTAB iteration costs two sweeps too
+    if args.fp64 == "full" and rank == 0:
+        C.set_solver(A.SOLVER_LSQR)  # the FP64 path solves with LSQR
         C.kernel_times(reset=True)
-        R64, nit64, info64 = C.resistance_tensor(A.FP64, 1, 2, maxit=args.fp64_iters, eps=args.eps)
+        R64, nit64, info64 = C.resistance_tensor(A.FP64, 1, 2, eps=args.eps)
         kt64 = C.kernel_times(reset=True)
+        err64 = None
+        if os.path.exists(GOLDEN_TRUTH) and rel_err is not None:
+            with open(GOLDEN_TRUTH) as f:
+                Rt = np.array(json.load(f)["R"])
+            err64 = float(np.max(np.abs(R64 - Rt)) / np.max(np.abs(Rt)))
         per_it = (kt64["av_ms"] + kt64["atu_ms"]) / max(kt64["av_launches"], 1)
-        nmax = int(max(nit))
-        est_ms = info64["assemble_ms"] + info64["rhs_ms"] + info64["reduce_ms"] + per_it * nmax
-        fp64 = {"solves_per_s_est": 1000.0 / est_ms, "assemble_ms": info64["assemble_ms"],
-                "ms_per_iteration_sweeps": per_it, "iterations_scaled_to": nmax,
-                "sample_iterations": int(max(nit64)),
-                "ratio_mixed_over_fp64": value / world / (1000.0 / est_ms)}
+        fp64 = {"solves_per_s": 1000.0 / info64["device_ms"], "device_ms": info64["device_ms"],
+                "assemble_ms": info64["assemble_ms"], "nit": [int(v) for v in nit64],
+                "istop": [int(v) for v in info64["istop"]], "ms_per_iteration_sweeps": per_it,
+                "rel_err_vs_fp64_truth": err64,
+                "ratio_mixed_over_fp64": value / world / (1000.0 / info64["device_ms"]),
+                "how": "FP64 assembly (k_stokes_G<double>) + FP64 block LSQR (k_av2/k_atu2) to the same eps, "
+                       "converged, CUDA events"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
-            cb = cpu_baseline(m, int(np.sum(nit)), args.cpu_seconds)
-            cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+            ms_small, name_small = small_body(args.cpu_level, args.outer_level, args.outer_radius)
+            runs = [cpu_complete_solve(ms_small, args.eps) for _ in range(max(1, args.cpu_solves))]
+            cpu_s = statistics.median(r["seconds"] for r in runs)
+            threads = os.cpu_count() or 1
+            # the GPU on the same small body: mixed path, complete solves, device time
+            Cs = A.Context(0)
+            Cs.set_mesh(ms_small)
+            Cs.set_problem(A.STOKES, [1, 2], A.dirichlet_known(A.STOKES, 2), itri=5)
+            Cs.resistance_tensor(A.MIXED, 1, 2, eps=args.eps)
+            gs, gR = [], None
+            for _ in range(5):
+                gR, _, gi = Cs.resistance_tensor(A.MIXED, 1, 2, eps=args.eps)
+                gs.append(gi["device_ms"])
+            R64s, _, g64 = Cs.resistance_tensor(A.FP64, 1, 2, eps=args.eps)
+            Cs.close()
+            Rc = runs[-1]["R"]
+            cpu = {"value": 1.0 / cpu_s, "unit": "solves/s", "cores": threads, "kind": "port",
+                   "sample": f"{len(runs)} complete solves (median) of {name_small}, LSQR eps {args.eps:g}, nothing "
+                             f"scaled: integration on {threads} threads, the reference's serial CRS LSQR per "
+                             f"right-hand side",
+                   "seconds": cpu_s, "integration_s": runs[-1]["integration_s"], "nit": runs[-1]["nit"],
+                   "same_body_gpu": {"mixed_solves_per_s": 1000.0 / statistics.median(gs),
+                                     "fp64_solves_per_s": 1000.0 / g64["device_ms"],
+                                     "ratio_mixed_gpu_over_cpu": cpu_s * 1000.0 / statistics.median(gs),
+                                     "ratio_fp64_gpu_over_cpu": cpu_s * 1000.0 / g64["device_ms"],
+                                     "rel_diff_fp64_gpu_vs_cpu": float(np.max(np.abs(R64s - Rc)) /
+                                                                       np.max(np.abs(Rc))),
+                                     "rel_diff_mixed_gpu_vs_cpu": float(np.max(np.abs(gR - Rc)) /
+                                                                        np.max(np.abs(Rc)))}}
+            if args.c2_estimate and fp64 is not None:
+                cpu["c2_estimate"] = cpu_c2_estimate(m, fp64["nit"], args.cpu_seconds)
         except Exception as ex:  # the baseline must not hide the GPU line
             cpu = {"value": None, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {ex}"}
@@ -745,7 +913,8 @@ def main():
                            "parallelism": "replicas" if world > 1 else "single GPU",
                            "l2": "inputs larger than L2 (10.4 GB packed matrix), no flush"},
                 "rel_err_vs_fp64": rel_err, "drag_over_analytic": drag_ratio, "torque_over_analytic": torque_ratio,
-                "nit": [int(v) for v in nit], "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+                "nit": [int(v) for v in nit], "e2e": e2e, "roofline": roofline, "roofline_assembly": roofline_asm,
+                "cpu_baseline": cpu,
                 "clocks": clk.summary(), "gpu_launches": kt["launches"] * world,
                 "kernel_ms": {"assemble_single_layer": kt["assemble_ms"] / max(kt["assemble_launches"], 1),
                               "rhs": kt["rhs_ms"] / max(kt["rhs_calls"], 1), "av_sweep": av_ms,

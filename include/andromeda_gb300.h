@@ -73,6 +73,10 @@ typedef struct agb_context agb_context;
 #define AGB_SOLVER_LSQR 0     /* lsqr_solve with lsqr_precon's column scaling (SLET CRS) */
 #define AGB_SOLVER_BICGSTAB 1 /* BiCGSTAB with the Jacobi preconditioner (SLET LIS with the
                                  reference's default LIS options) */
+#define AGB_SOLVER_HYBRID 2   /* BiCGSTAB-Jacobi first; LSQR (as AGB_SOLVER_LSQR, zero start,
+                                 the reference's default iteration limit) for every right-hand
+                                 side of a system whose BiCGSTAB did not converge on all of them
+                                 (no counterpart in the reference) */
 
 /* boundary-condition types (mod_mesh.f90:110) */
 #define AGB_BC_FUNCTION 1
@@ -134,7 +138,12 @@ int agb_set_integration(agb_context* ctx, int sing_mode, int rec_depth, double n
  * the row of its own unknown, preconditioned BiCGSTAB (van der Vorst 1992) with
  * M = diag(A), x0 = 0 (the warm start is not used), stop at
  * ||b - A x|| <= eps ||b|| or maxit iterations (0: 1000, the LIS default).  With
- * BiCGSTAB, istop[r] is 0 converged, 1 iteration limit, 2 breakdown.  BiCGSTAB
+ * BiCGSTAB, istop[r] is 0 converged, 1 iteration limit, 2 breakdown, 3 diverged
+ * or stagnated (the recursive residual rose 1e3 times above its best, or did
+ * not fall by 10 % in 200 iterations: the FP32 products of an ill-conditioned
+ * system).  AGB_SOLVER_HYBRID: as BiCGSTAB where every right-hand side of the
+ * system converges; otherwise all of them are solved again by LSQR and
+ * istop[r] = 10 + LSQR's istop, nit[r] the sum of both iteration counts.  BiCGSTAB
  * needs the packed mixed system (Stokes, velocity known on every wall,
  * triangles, default integration, AGB_MIXED); other systems return
  * AGB_ERR_UNSUPPORTED from the solve.  agb_batch_resistance on this context
@@ -202,6 +211,17 @@ int agb_resistance_tensor(agb_context* ctx, int precision, int particle_wall, in
  * reading. */
 int agb_kernel_times(agb_context* ctx, int reset, double* out);
 
+/* Self-test of the bounded barrier wait of the TMA-fed kernels (no counterpart
+ * in the reference; it tests this library's failure path).  One CTA of 32
+ * threads waits on the first phase of an mbarrier with the kernels' wait
+ * function and a limit of `polls` failed tries (1..2^22).  arrive = 0: nothing
+ * arrives and no copy is issued, the wait gives up, sets the launch's error
+ * word and returns; the call returns AGB_ERR_CUDA with "a bounded barrier wait
+ * gave up" in agb_last_error(NULL), as a solve whose wait gave up does, and the
+ * device stays usable.  arrive = 1: one thread arrives, every wait completes,
+ * AGB_OK.  *waits_completed: threads whose wait completed (0 or 32). */
+int agb_selftest_bounded_wait(int device, unsigned polls, int arrive, int* waits_completed);
+
 /* Drop-ins with the reference signatures (1-based CRS, int64 row pointers).
  * agb_lsqr_precon scales a in place like lsqr_precon; agb_lsqr_solve
  * warm-starts from x like lsqr_solve.  Both run on the current CUDA device. */
@@ -263,8 +283,10 @@ int agb_solve_fields(agb_context* ctx, int nrhs, const double* u_in, const doubl
  * allocates nothing: its scratch is a fixed 8 MiB array in the library's
  * device image (held by every GPU that loads the library until exit), so n is
  * limited to AGB_NOALLOC_MAX_COLUMNS and larger n is rejected with
- * AGB_ERR_ARG.  The first call on a device looks up the array's device address
- * (make it before any stream capture).  All calls on a device share the array:
+ * AGB_ERR_ARG.  The first call in each CUDA context (per device, and again
+ * in a context re-created after cudaDeviceReset or in a non-primary context
+ * made current by the host) looks up the array's device address (make it
+ * before any stream capture).  All calls on a device share the array:
  * calls that overlap on the GPU race on it.  Runs on the legacy default stream
  * and returns after the work is done; errors via agb_last_error(NULL). */
 #define AGB_NOALLOC_SCRATCH_DOUBLES (1 << 20)

@@ -1,6 +1,7 @@
 """The benchmark's reference arm on the host (no GPU): `bench.py --impl
-reference` times the reference algorithm (the oracle port) on a bounded sample
-and prints one JSON line with the fields the benchmark contract names."""
+reference` times complete solves by the reference algorithm (the oracle port)
+of a body small enough to finish in seconds, nothing scaled, and prints one
+JSON line with the fields the benchmark contract names."""
 import json
 import os
 import subprocess
@@ -25,7 +26,10 @@ def test_reference_arm_json_line():
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
-    assert "workload" in d["config"]
+    assert "workload" in d["config"] and "complete solves" in d["config"]["workload"]
+    assert "nothing scaled" in cb["sample"]
+    # the timed region is the run's own: steps x ms_per_step within the host time
+    assert d["steps"] * d["ms_per_step"] / 1000.0 <= d["host_s"] * 1.001
 
 
 def _bench_module():

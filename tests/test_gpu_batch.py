@@ -66,6 +66,25 @@ def test_batch_matches_single_body(agb):
         assert np.all(d <= np.maximum(5, nm[both] // 10)), (nit[i], nm, istop[i], im)
 
 
+def test_batch_many_body_set_within_1e6_of_fp64(agb):
+    """Six bodies of the 512-body benchmark set (seed 20260101, radius-200
+    level-2 containers): the smallest, the largest and four in between,
+    solved together by the batched mixed path at the benchmark's LSQR eps
+    3e-8; every tensor within 1e-6 of the body's FP64 tensor (FP64 assembly +
+    FP64 LSQR to eps 1e-10)."""
+    meshes, params = M.batch_bodies()
+    order = np.argsort(params[:, 4])
+    pick = [int(order[j]) for j in np.linspace(0, len(order) - 1, 6).round().astype(int)]
+    ne = params[pick, 4]
+    assert ne.min() < 600 and ne.max() > 7500
+    sel = [meshes[i] for i in pick]
+    R, nit, istop, st = agb.batch_resistance(sel, eps=3e-8)
+    assert st["waves"] == 1
+    for j, m in enumerate(sel):
+        R64, _, _ = _single(agb, m, agb.FP64, 1e-10)
+        assert _rel(R[j], R64) < 1e-6, (pick[j], int(ne[j]), _rel(R[j], R64), istop[j])
+
+
 def test_batch_waves_give_the_same_tensors(agb):
     """A memory budget of one body per wave runs four waves; the tensors agree
     with the one-wave run."""

@@ -4,7 +4,7 @@ quads, against the FP64 oracle.
 
 Tolerances: integral matrices and self-check errors 1e-12 relative to the
 largest entry (FP64 on both sides, only the summation order of the row sums
-differs); solutions of mixed-BC problems 1e-9 relative (both solved to eps 1e-13).
+differs); solutions of mixed-BC problems 1e-10 relative (both solved to eps 1e-13).
 """
 import numpy as np
 import pytest
@@ -82,8 +82,8 @@ def test_laplace_mixed_bc_solve(agb, orc, triangles):
     C.assemble(agb.FP64)
     uo, qo, nit, istop = C.solve_fields(u0[None, None], q0[None, None], eps=1e-13)
     assert istop[0] <= 3
-    assert _rel(uo[0, 0], u_ref) < 1e-9
-    assert _rel(qo[0, 0], q_ref) < 1e-9
+    assert _rel(uo[0, 0], u_ref) < 1e-10
+    assert _rel(qo[0, 0], q_ref) < 1e-10
     # the discrete solution reproduces the linear field on the flux walls
     flux_nodes = np.unique(m["con"][~np.isin(m["bcid"], [1, 2])][:, :3])
     assert np.max(np.abs(uo[0, 0, flux_nodes] - u[flux_nodes])) < 5e-3 * np.max(np.abs(u))
@@ -107,7 +107,7 @@ def test_stokes_mixed_bc_solve(agb, orc):
     C.assemble(agb.FP64)
     uo, qo, nit, istop = C.solve_fields(U, None, eps=1e-13)
     assert istop[0] <= 3
-    assert _rel(qo[0], q_ref[0]) < 1e-9
+    assert _rel(qo[0], q_ref[0]) < 1e-10
 
 
 def test_general_path_mixed_precision(agb):

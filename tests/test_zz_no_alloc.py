@@ -53,3 +53,27 @@ def test_noalloc_precon_rejects_oversized(agb):
     rc = L.agb_lsqr_precon_dense_noalloc(4, (1 << 20) + 1, (1 << 20) + 32, C.c_void_p(1), C.c_void_p(1))
     assert rc == 1
     assert b"AGB_NOALLOC_MAX_COLUMNS" in L.agb_last_error(None)
+
+
+def test_noalloc_precon_wide_matrices(agb):
+    """Widths where the scratch, not the cap of 64, sets the number of row
+    groups (n > 16384), up to the largest accepted width
+    AGB_NOALLOC_MAX_COLUMNS: q against 1/||A(:,j)|| computed in NumPy and the
+    scaled matrix against A diag(q)."""
+    torch = pytest.importorskip("torch")
+    L = agb.load()
+    rng = np.random.default_rng(5)
+    for m, n in [(3, 40000), (70, 20000), (2, 1 << 20)]:
+        lda = (n + 31) // 32 * 32
+        A = rng.normal(size=(m, n))
+        dA = torch.zeros((m, lda), dtype=torch.float64, device="cuda")
+        dA[:, :n] = torch.from_numpy(A).cuda()
+        dq = torch.zeros(n, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        rc = L.agb_lsqr_precon_dense_noalloc(m, n, lda, C.c_void_p(dA.data_ptr()), C.c_void_p(dq.data_ptr()))
+        assert rc == 0, L.agb_last_error(None)
+        q = dq.cpu().numpy()
+        q_np = 1.0 / np.sqrt(np.sum(A * A, axis=0))
+        assert np.max(np.abs(q - q_np) / q_np) < TOL
+        scaled = dA[:, :n].cpu().numpy()
+        assert np.max(np.abs(scaled - A * q_np[None, :])) <= TOL * np.max(np.abs(A * q_np[None, :]))
