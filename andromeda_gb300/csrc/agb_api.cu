@@ -80,9 +80,10 @@ struct agb_context {
   void* d_nrm = nullptr;
   void* d_colscale = nullptr;
   double *d_u = nullptr, *d_rhs = nullptr, *d_x = nullptr, *d_ft = nullptr;
+  double *d_res = nullptr, *d_dx = nullptr;  // refinement: FP64 residual and correction
   int *d_active = nullptr;
   unsigned char* d_rowact = nullptr;
-  size_t cap_u = 0, cap_rhs = 0, cap_x = 0, cap_act = 0;
+  size_t cap_u = 0, cap_rhs = 0, cap_x = 0, cap_act = 0, cap_res = 0, cap_dx = 0;
   // live kernel timing (CUDA events on the context stream)
   cudaEvent_t tev[4] = {};
   double t_asm = 0.0, t_rhs = 0.0;
@@ -417,6 +418,12 @@ int device_rhs(agb_context* c, int nrhs, int na) {
 }
 
 int assemble_general(agb_context* c, int precision);
+// relative LSQR tolerance of each refinement correction solve
+constexpr double kRefineEps = 1.0e-2;
+__global__ void k_axpy(int64_t n, const double* __restrict__ d, double* __restrict__ x) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) x[t] += d[t];
+}
 int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int refine, int* nit, int* istop,
              bool x0_zero) {
   if ((!c->lsqr.A && !c->lsqr.mf) || c->lsqr.k != nrhs) {
@@ -449,12 +456,26 @@ int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int r
     }
     return AGB_OK;
   }
-  for (int pass = 0; pass <= refine; ++pass) {
-    if (!c->lsqr.solve(c->d_rhs, d_x, c->d_q, eps, maxit, nt.data(), is.data(), nullptr, 8, x0_zero && pass == 0))
-      return fail(c, AGB_ERR_CUDA, "lsqr: " + c->lsqr.err);
+  if (!c->lsqr.solve(c->d_rhs, d_x, c->d_q, eps, maxit, nt.data(), is.data(), nullptr, 8, x0_zero))
+    return fail(c, AGB_ERR_CUDA, "lsqr: " + c->lsqr.err);
+  for (int r = 0; r < nrhs; ++r) {
+    if (nit) nit[r] = nt[r];
+    if (istop) istop[r] = is[r];
+  }
+  // iterative refinement: r = b - A x with FP64 accumulation over the stored
+  // matrix, the correction A d = r by LSQR from zero to the relative tolerance
+  // kRefineEps, x += d
+  for (int pass = 1; pass <= refine; ++pass) {
+    CUDA_OR_FAIL(c, ensure(c->d_res, c->cap_res, (size_t)nrhs * c->m));
+    CUDA_OR_FAIL(c, ensure(c->d_dx, c->cap_dx, (size_t)nrhs * c->n));
+    if (!c->lsqr.residual(c->d_rhs, d_x, c->d_q, c->d_res)) return fail(c, AGB_ERR_CUDA, "residual: " + c->lsqr.err);
+    if (!c->lsqr.solve(c->d_res, c->d_dx, c->d_q, kRefineEps, maxit, nt.data(), is.data(), nullptr, 8, true))
+      return fail(c, AGB_ERR_CUDA, "lsqr (refinement): " + c->lsqr.err);
+    k_axpy<<<(unsigned)(((int64_t)nrhs * c->n + 255) / 256), 256, 0, c->stream>>>((int64_t)nrhs * c->n, c->d_dx, d_x);
+    CUDA_OR_FAIL(c, cudaGetLastError());
+    c->nlaunch += 1;
     for (int r = 0; r < nrhs; ++r) {
-      if (nit) nit[r] = (pass == 0 ? 0 : nit[r]) + nt[r];
-      if (istop) istop[r] = is[r];
+      if (nit) nit[r] += nt[r];
     }
   }
   return AGB_OK;
@@ -591,6 +612,8 @@ int agb_destroy(agb_context* c) {
   dfree(c->d_u);
   dfree(c->d_rhs);
   dfree(c->d_x);
+  dfree(c->d_res);
+  dfree(c->d_dx);
   dfree(c->d_ft);
   dfree(c->d_active);
   dfree(c->d_rowact);

@@ -5,11 +5,14 @@
 //   triangle Laplace   Triangle_BEMIntAnal lib_sdBem.f90:741 -> Triangle_3DLapInt :859
 //                      (BemKernel :911) or si_tri_lap mod_singInt.f90:127
 //   quad Laplace       Quad_BEMIntNumAna lib_intAna.f90:156 -> Quad_BEMIntNum :219 or
-//                      si_qua_lap mod_singInt.f90:172
+//                      si_qua_lap mod_singInt.f90:172 (sing_mode 1: the polar
+//                      singular branch of Quad_BEMInt lib_int.f90:408)
 //   triangle Stokes    Triangle_StokesIntAna lib_intAna.f90:96 -> Triangle_3DStokesInt
 //                      lib_Stokes.f90:2341 (StokesKernel :2450) or si_tri_stk
 //   quad Stokes        Quad_StokesIntNumAna lib_intAna.f90:5 -> Quad_StokesIntNum
 //                      lib_Stokes.f90:3754 (fixed 3x3 subcells) or si_qua_stk
+//                      (sing_mode 1: the polar singular branch of Quad_StokesInt
+//                      lib_Stokes.f90:3494)
 #pragma once
 #include "agb_common.cuh"
 #include "agb_singular.cuh"
@@ -142,6 +145,62 @@ __device__ __forceinline__ void quad_map(const double (*P)[3], double gii, doubl
   N[2] = KS[0] * ET[1] - ET[0] * KS[1];
 }
 
+// Singular branch of Quad_BEMInt (lib_int.f90:408-524) / Quad_StokesInt
+// (lib_Stokes.f90:3494-3654), selected by sing_mode 1 for a quad's own node or
+// centre (isrc 1..5): the parameter square is split at the source into four
+// triangles, each integrated in polar coordinates about it (theta over
+// [th0, th1], rho over [0, roth(theta)], the quad rule's Gauss points on both);
+// the Jacobian rho cancels the 1/r singularity.  A triangle of zero width
+// (source on its edge) is skipped.  visit(X, nn (unit normal x multi), w, f4).
+template <class F>
+__device__ inline void quad_polar(const ElemGeom& E, int isrc, int iqud, F&& visit) {
+  const double ksi[5] = {0.0, 1.0, 1.0, 0.0, 0.5}, eta[5] = {0.0, 0.0, 1.0, 1.0, 0.5};
+  const double xx1 = ksi[isrc - 1], yy1 = eta[isrc - 1];
+  const int ng1 = gtNg1[iqud - 1], ng2 = gtNg2[iqud - 1];
+  for (int k = 1; k <= 4; ++k) {
+    double al, fii, th0, th1;
+    if (k == 1) {
+      if (1.0 - xx1 == 0.0) continue;
+      al = sqrt(yy1 * yy1 + (1.0 - xx1) * (1.0 - xx1));
+      fii = acos(yy1 / al);
+      th0 = 1.5 * AGB_PI + acos(yy1 / al);
+      th1 = 2.0 * AGB_PI + atan((1.0 - yy1) / (1.0 - xx1));
+    } else if (k == 2) {
+      if (1.0 - yy1 == 0.0) continue;
+      al = sqrt((1.0 - yy1) * (1.0 - yy1) + (1.0 - xx1) * (1.0 - xx1));
+      fii = acos((1.0 - xx1) / al);
+      th0 = asin((1.0 - yy1) / al);
+      th1 = 0.5 * AGB_PI + atan(xx1 / (1.0 - yy1));
+    } else if (k == 3) {
+      if (xx1 == 0.0) continue;
+      al = sqrt(xx1 * xx1 + (1.0 - yy1) * (1.0 - yy1));
+      fii = acos((1.0 - yy1) / al);
+      th0 = 0.5 * AGB_PI + acos((1.0 - yy1) / al);
+      th1 = AGB_PI + atan(yy1 / xx1);
+    } else {
+      if (yy1 == 0.0) continue;
+      al = sqrt(yy1 * yy1 + xx1 * xx1);
+      fii = acos(xx1 / al);
+      th0 = AGB_PI + acos(xx1 / al);
+      th1 = 1.5 * AGB_PI + atan((1.0 - xx1) / yy1);
+    }
+    for (int i = ng1; i <= ng2; ++i)
+      for (int j = ng1; j <= ng2; ++j) {
+        const double th = (th1 - th0) * gtGi[i - 1] / 2.0 + (th1 + th0) / 2.0;
+        const double roth = al * sin(fii) / sin(th - th0 + fii);
+        const double ro = roth * gtGi[j - 1] / 2.0 + roth / 2.0;
+        const double eti = 2.0 * (xx1 + ro * cos(th)) - 1.0;
+        const double etj = 2.0 * (yy1 + ro * sin(th)) - 1.0;
+        double X[3], N[3], f4[4];
+        quad_map(E.v, eti, etj, X, N, f4);
+        const double aj = 1.0 / sqrt(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
+        const double nn[3] = {E.multi * N[0] * aj, E.multi * N[1] * aj, E.multi * N[2] * aj};
+        const double w = (th1 - th0) * roth * ro * gtOme[i - 1] * gtOme[j - 1] / aj;
+        visit(X, nn, w, f4);
+      }
+  }
+}
+
 // ---- Laplace ---------------------------------------------------------------
 // qdiv > 0: a regular quad is integrated over qdiv x qdiv cells instead of the
 // edge-length subdivision (1: the regular branch of Quad_BEMInt, lib_int.f90:329).
@@ -178,8 +237,19 @@ __device__ inline LapElem lap_element(const ElemGeom& E, const double* s, int is
     });
     return o;
   }
-  if (isrc) {
+  if (isrc && opt.sing == 0) {
     o.g = agb_sing::quad_laplace(E.v, isrc);
+    return o;
+  }
+  if (isrc) {
+    quad_polar(E, isrc, iqud, [&](const double* X, const double* nn, double w, const double* f4) {
+      const double RX = s[0] - X[0], RY = s[1] - X[1], RZ = s[2] - X[2];
+      const double RA = sqrt(RX * RX + RY * RY + RZ * RZ);
+      const double FG = fpi / RA;
+      const double FH = (RX * nn[0] + RY * nn[1] + RZ * nn[2]) * (1.0 / (RA * RA)) * FG;
+      for (int k = 0; k < 4; ++k) o.h[k] += FH * w * f4[k];
+      o.g += FG * w;
+    });
     return o;
   }
   const int ng1 = gtNg1[iqud - 1], ng2 = gtNg2[iqud - 1];
@@ -246,12 +316,25 @@ __device__ inline void stk_element(const ElemGeom& E, const double* s, int isrc,
     o.prG[k] = 0.0;
     for (int j = 0; j < 4; ++j) o.prT[k][j] = 0.0;
   }
-  if (isrc && (E.type != AGB_TRI || opt.sing == 0)) {
+  if (isrc && opt.sing == 0) {
     if (E.type == AGB_TRI) agb_sing::tri_stokes(E.v[0], E.v[1], E.v[2], E.area, isrc, o.G);
     else agb_sing::quad_stokes(E.v, isrc, o.G);
     return;
   }
   double G[6], T[6], prG[3], prT[3];
+  if (isrc && E.type != AGB_TRI) {
+    // G and T by the polar rule; the pressure integrals of the own element
+    // (principal value / hypersingular) stay zero, as the analytic branch leaves them
+    quad_polar(E, isrc, iqud, [&](const double* X, const double* nn, double w, const double* f4) {
+      stk_kernel(s, X, nn, G, T, prG, prT);
+      for (int k = 0; k < 6; ++k) o.G[k] += w * G[k];
+      for (int sp = 0; sp < 4; ++sp) {
+        const double ww = w * f4[sp];
+        for (int k = 0; k < 6; ++k) o.T[k][sp] += ww * T[k];
+      }
+    });
+    return;
+  }
   if (E.type == AGB_TRI) {
     const double n[3] = {E.multi * E.n[0], E.multi * E.n[1], E.multi * E.n[2]};
     tri_walk(opt, E, s, isrc, [&](const Bary& B, double area, bool skip_centroid) {

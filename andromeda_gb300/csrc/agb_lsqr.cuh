@@ -28,7 +28,7 @@ struct BicgScalars {
 // BiCGSTAB stops a right-hand side whose residual grew BICG_DIVERGE times
 // above its best, or did not fall by 10 % within BICG_STALL iterations.
 constexpr double BICG_DIVERGE = 1.0e3;
-constexpr int BICG_STALL = 200;
+constexpr int BICG_STALL = 64;
 
 // Dense block LSQR.  A is m x n row-major with leading dimension lda (lda is
 // a multiple of 32 and columns n..lda-1 are zero).  T = float (mixed path)

@@ -7,15 +7,17 @@
 // one-CTA pivot search (first index of the largest |a|, as idamax) with the
 // row interchange inside the panel, then a multi-CTA scale + rank-1 update of
 // the panel's remaining columns; the interchanges are applied to the other
-// columns, then U12 = L11^-1 A12 (cuBLAS dtrsm) and A22 -= A21 U12 (cuBLAS
-// dgemm, the O(n^3) part).  Pivots are those of dgefa (same elimination order
-// and tie rule); the factors are kept in LAPACK form (positive multipliers,
-// every later interchange applied to L), which is what the solve consumes.
-// Solve: x = P b (gather), L y = x, U x = y (cuBLAS dtrsm), for many
-// right-hand sides at once.
+// columns, then U12 = L11^-1 A12 (k_lu_trsm_blk: a warp per column, the 64 x 64
+// triangle in shared memory) and A22 -= A21 U12 (k_lu_gemm_sub: 64 x 64 output
+// tiles, 4 x 4 FP64 accumulators per thread, the O(n^3) part; GB300's FP64 pipe
+// bounds it).  Pivots are those of dgefa (same elimination order and tie
+// rule); the factors are kept in LAPACK form (positive multipliers, every later
+// interchange applied to L), which is what the solve consumes.  Solve: x = P b
+// (gather), then L y = x and U x = y blockwise (the same two kernels: a block
+// triangle solve, then the update of the remaining rows), for many right-hand
+// sides at once.
 #include "agb_lu.cuh"
 
-#include <cublas_v2.h>
 #include <algorithm>
 #include <vector>
 
@@ -118,15 +120,107 @@ __global__ void k_lu_gather(const double* __restrict__ b, const int* __restrict_
   x[t] = b[(int64_t)c * n + perm[i]];
 }
 
-static const char* cublas_str(cublasStatus_t s) {
-  switch (s) {
-    case CUBLAS_STATUS_SUCCESS: return "success";
-    case CUBLAS_STATUS_NOT_INITIALIZED: return "not initialized";
-    case CUBLAS_STATUS_ALLOC_FAILED: return "alloc failed";
-    case CUBLAS_STATUS_INVALID_VALUE: return "invalid value";
-    case CUBLAS_STATUS_EXECUTION_FAILED: return "execution failed";
-    default: return "error";
+// B (jb x ncols, column-major, leading dimension ldb) <- T^-1 B for the jb x jb
+// (jb <= 64) triangle T (column-major, ldt): lower with unit diagonal (UPPER
+// false, forward substitution) or upper (UPPER true, backward).  One warp per
+// column; lane l holds rows l and l + 32; the triangle sits in shared memory.
+template <bool UPPER>
+__global__ void __launch_bounds__(256) k_lu_trsm_blk(int jb, const double* __restrict__ T, int64_t ldt,
+                                                   double* __restrict__ B, int64_t ldb, int ncols) {
+  __shared__ double sT[LU_NB][LU_NB + 1];
+  for (int t = threadIdx.x; t < jb * jb; t += blockDim.x) {
+    const int r = t % jb, c = t / jb;
+    sT[r][c] = T[r + (int64_t)c * ldt];
   }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int col = blockIdx.x * nw + warp; col < ncols; col += gridDim.x * nw) {
+    double* b = B + (int64_t)col * ldb;
+    const int r0 = lane, r1 = lane + 32;
+    double x0 = (r0 < jb) ? b[r0] : 0.0;
+    double x1 = (r1 < jb) ? b[r1] : 0.0;
+    if (!UPPER) {
+      for (int k = 0; k < jb; ++k) {
+        const double xk = __shfl_sync(0xffffffffu, k < 32 ? x0 : x1, k & 31);
+        if (r0 > k && r0 < jb) x0 -= sT[r0][k] * xk;
+        if (r1 > k && r1 < jb) x1 -= sT[r1][k] * xk;
+      }
+    } else {
+      for (int k = jb - 1; k >= 0; --k) {
+        if (k < 32) {
+          if (lane == k) x0 /= sT[k][k];
+        } else if (lane == k - 32) {
+          x1 /= sT[k][k];
+        }
+        const double xk = __shfl_sync(0xffffffffu, k < 32 ? x0 : x1, k & 31);
+        if (r0 < k) x0 -= sT[r0][k] * xk;
+        if (r1 < k) x1 -= sT[r1][k] * xk;
+      }
+    }
+    if (r0 < jb) b[r0] = x0;
+    if (r1 < jb) b[r1] = x1;
+  }
+}
+
+// C (m x n) -= A (m x k) B (k x n), all column-major, k <= 64: 64 x 64 output
+// tiles per CTA of 256 threads, 4 x 4 FP64 accumulators per thread, the
+// operands staged through shared memory in chunks of 32 of k.
+constexpr int LU_GT = 64, LU_GK = 32;
+__global__ void __launch_bounds__(256) k_lu_gemm_sub(int m, int n, int k, const double* __restrict__ A, int64_t lda,
+                                                   const double* __restrict__ B, int64_t ldb, double* __restrict__ C,
+                                                   int64_t ldc) {
+  __shared__ double sA[LU_GK][LU_GT + 1];  // [kk][row]
+  __shared__ double sB[LU_GT][LU_GK + 1];  // [col][kk]
+  const int r0 = blockIdx.x * LU_GT, c0 = blockIdx.y * LU_GT;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+  for (int k0 = 0; k0 < k; k0 += LU_GK) {
+    const int kc = min(LU_GK, k - k0);
+    for (int t = threadIdx.x; t < LU_GT * LU_GK; t += 256) {
+      const int rr = t % LU_GT, kk = t / LU_GT;
+      sA[kk][rr] = (r0 + rr < m && kk < kc) ? A[(r0 + rr) + (int64_t)(k0 + kk) * lda] : 0.0;
+      const int k2 = t % LU_GK, cc = t / LU_GK;
+      sB[cc][k2] = (k2 < kc && c0 + cc < n) ? B[(k0 + k2) + (int64_t)(c0 + cc) * ldb] : 0.0;
+    }
+    __syncthreads();
+    for (int kk = 0; kk < kc; ++kk) {
+      double a[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = sA[kk][tx + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bv[j] = sB[ty + 16 * j][kk];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], bv[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int r = r0 + tx + 16 * i, c = c0 + ty + 16 * j;
+      if (r < m && c < n) C[r + (int64_t)c * ldc] -= acc[i][j];
+    }
+}
+
+static void launch_trsm(bool upper, int jb, const double* T, int64_t ldt, double* B, int64_t ldb, int ncols,
+                        cudaStream_t s) {
+  const unsigned blocks = (unsigned)std::min<int64_t>(((int64_t)ncols + 7) / 8, 152 * 8);
+  if (upper)
+    k_lu_trsm_blk<true><<<blocks, 256, 0, s>>>(jb, T, ldt, B, ldb, ncols);
+  else
+    k_lu_trsm_blk<false><<<blocks, 256, 0, s>>>(jb, T, ldt, B, ldb, ncols);
+}
+static void launch_gemm_sub(int m, int n, int k, const double* A, int64_t lda, const double* B, int64_t ldb,
+                            double* C, int64_t ldc, cudaStream_t s) {
+  const dim3 grid((unsigned)((m + LU_GT - 1) / LU_GT), (unsigned)((n + LU_GT - 1) / LU_GT));
+  k_lu_gemm_sub<<<grid, 256, 0, s>>>(m, n, k, A, lda, B, ldb, C, ldc);
 }
 
 #define LCK(x)                                                                   \
@@ -137,25 +231,14 @@ static const char* cublas_str(cublasStatus_t s) {
       goto done;                                                                 \
     }                                                                            \
   } while (0)
-#define BLK(x)                                                                   \
-  do {                                                                           \
-    cublasStatus_t s_ = (x);                                                     \
-    if (s_ != CUBLAS_STATUS_SUCCESS) {                                           \
-      err = std::string(#x) + ": " + cublas_str(s_);                             \
-      goto done;                                                                 \
-    }                                                                            \
-  } while (0)
 
 bool lu_factor_dev(double* A, int64_t lda, int n, int* ipiv, int* info_host, cudaStream_t s, long* launches,
                    std::string& err) {
-  cublasHandle_t h = nullptr;
   double* recip = nullptr;
   int* info = nullptr;
   bool ok = false;
   long nl = 0;
   if (n < 1 || lda < n) { err = "lu: bad sizes"; return false; }
-  if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS) { err = "cublasCreate failed"; return false; }
-  BLK(cublasSetStream(h, s));
   LCK(cudaMallocAsync(&recip, sizeof(double), s));
   LCK(cudaMallocAsync(&info, sizeof(int), s));
   LCK(cudaMemsetAsync(info, 0, sizeof(int), s));
@@ -174,14 +257,14 @@ bool lu_factor_dev(double* A, int64_t lda, int n, int* ipiv, int* info_host, cud
     const int rest = n - j0 - jb;
     if (rest > 0) {
       k_lu_swap_cols<<<(unsigned)((rest + 255) / 256), 256, 0, s>>>(A, lda, ipiv, j0, jb, j0 + jb, n);
-      ++nl;
-      const double one = 1.0, mone = -1.0;
-      BLK(cublasDtrsm(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_UNIT, jb, rest, &one,
-                      A + j0 + (int64_t)j0 * lda, (int)lda, A + j0 + (int64_t)(j0 + jb) * lda, (int)lda));
-      BLK(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, rest, rest, jb, &mone, A + (j0 + jb) + (int64_t)j0 * lda, (int)lda,
-                      A + j0 + (int64_t)(j0 + jb) * lda, (int)lda, &one, A + (j0 + jb) + (int64_t)(j0 + jb) * lda,
-                      (int)lda));
-      nl += 2;
+      // U12 = L11^-1 A12, then A22 -= A21 U12
+      double* A11 = A + j0 + (int64_t)j0 * lda;
+      double* A12 = A + j0 + (int64_t)(j0 + jb) * lda;
+      double* A21 = A + (j0 + jb) + (int64_t)j0 * lda;
+      double* A22 = A + (j0 + jb) + (int64_t)(j0 + jb) * lda;
+      launch_trsm(false, jb, A11, lda, A12, lda, rest, s);
+      launch_gemm_sub(rest, rest, jb, A21, lda, A12, lda, A22, lda, s);
+      nl += 3;
     }
     LCK(cudaGetLastError());
   }
@@ -192,17 +275,16 @@ done:
   if (recip) cudaFreeAsync(recip, s);
   if (info) cudaFreeAsync(info, s);
   cudaStreamSynchronize(s);
-  cublasDestroy(h);
   if (launches) *launches += nl;
   return ok;
 }
 
 bool lu_solve_dev(const double* A, int64_t lda, int n, const int* ipiv_host, int nrhs, double* B, cudaStream_t s,
                   long* launches, std::string& err) {
-  cublasHandle_t h = nullptr;
   int* perm = nullptr;
   double* X = nullptr;
   bool ok = false;
+  long nl = 0;
   std::vector<int> p(n);
   for (int i = 0; i < n; ++i) p[i] = i;
   for (int k = 0; k < n; ++k) {
@@ -210,20 +292,33 @@ bool lu_solve_dev(const double* A, int64_t lda, int n, const int* ipiv_host, int
     if (l < 0 || l >= n) { err = "lu: pivot out of range"; return false; }
     std::swap(p[k], p[l]);
   }
-  if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS) { err = "cublasCreate failed"; return false; }
-  BLK(cublasSetStream(h, s));
   LCK(cudaMallocAsync(&perm, n * sizeof(int), s));
   LCK(cudaMallocAsync(&X, (size_t)n * nrhs * sizeof(double), s));
   LCK(cudaMemcpyAsync(perm, p.data(), n * sizeof(int), cudaMemcpyHostToDevice, s));
   k_lu_gather<<<(unsigned)(((int64_t)n * nrhs + 255) / 256), 256, 0, s>>>(B, perm, n, nrhs, X);
+  ++nl;
   LCK(cudaGetLastError());
-  {
-    const double one = 1.0;
-    BLK(cublasDtrsm(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_UNIT, n, nrhs, &one, A,
-                    (int)lda, X, n));
-    BLK(cublasDtrsm(h, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, nrhs, &one, A,
-                    (int)lda, X, n));
+  // L y = x: diagonal block, then the rows below
+  for (int k0 = 0; k0 < n; k0 += LU_NB) {
+    const int jb = std::min(LU_NB, n - k0);
+    launch_trsm(false, jb, A + k0 + (int64_t)k0 * lda, lda, X + k0, n, nrhs, s);
+    ++nl;
+    if (k0 + jb < n) {
+      launch_gemm_sub(n - k0 - jb, nrhs, jb, A + (k0 + jb) + (int64_t)k0 * lda, lda, X + k0, n, X + k0 + jb, n, s);
+      ++nl;
+    }
   }
+  // U x = y: from the last diagonal block up, then the rows above
+  for (int k0 = ((n - 1) / LU_NB) * LU_NB; k0 >= 0; k0 -= LU_NB) {
+    const int jb = std::min(LU_NB, n - k0);
+    launch_trsm(true, jb, A + k0 + (int64_t)k0 * lda, lda, X + k0, n, nrhs, s);
+    ++nl;
+    if (k0 > 0) {
+      launch_gemm_sub(k0, nrhs, jb, A + (int64_t)k0 * lda, lda, X + k0, n, X, n, s);
+      ++nl;
+    }
+  }
+  LCK(cudaGetLastError());
   LCK(cudaMemcpyAsync(B, X, (size_t)n * nrhs * sizeof(double), cudaMemcpyDeviceToDevice, s));
   LCK(cudaStreamSynchronize(s));
   ok = true;
@@ -231,8 +326,7 @@ done:
   if (perm) cudaFreeAsync(perm, s);
   if (X) cudaFreeAsync(X, s);
   cudaStreamSynchronize(s);
-  cublasDestroy(h);
-  if (launches) *launches += 1;
+  if (launches) *launches += nl;
   return ok;
 }
 

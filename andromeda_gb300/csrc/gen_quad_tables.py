@@ -15,7 +15,7 @@ The header keeps the reference's digits exactly (so quadrature sums agree with
 the reference to the last bit of the inputs).  Expansion of the orbits into
 barycentric points (WandzuratXiaoBary) is done by the consumers.
 
-Usage:  python gen_quad_tables.py /root/reference/src  > quad_tables.h
+Usage:  python gen_quad_tables.py <reference checkout>/src  > quad_tables.h
 """
 import re
 import sys
@@ -69,7 +69,9 @@ def parse_gauss(path):
 
 
 def main():
-    srcdir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python gen_quad_tables.py <reference checkout>/src > quad_tables.h")
+    srcdir = sys.argv[1]
     wx = parse_wx(srcdir + "/mod_trikotnik.f90")
     gi, ome, ng1, ng2 = parse_gauss(srcdir + "/mod_gauss.f90")
     assert [len(r) for r in wx] == [3, 7, 12, 19, 26], [len(r) for r in wx]

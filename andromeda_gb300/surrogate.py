@@ -5,10 +5,11 @@ training tensors; an MLP 5 -> 256 -> 256 -> 256 -> 21 (SiLU, BF16 tensor-core
 GEMMs with FP32 accumulation, trained on the GPU by the library's own forward,
 backward and Adam kernels) maps the shape parameters (b, c, e1, e2, log aspect)
 of a superellipsoid with a = 1 to the 21 upper-triangle entries of its
-symmetric 6x6 translation/rotation resistance tensor.  Queries outside the
-training hull (an axis box plus a Mahalanobis guard) are answered by the BEM
-itself, and a random audit subset is re-solved by the BEM to judge the
-surrogate's error.
+symmetric 6x6 translation/rotation resistance tensor.  An ensemble of such
+networks answers a query when it lies inside the training hull (an axis box
+plus a Mahalanobis guard) and the members agree within a threshold calibrated
+on held-out BEM tensors; every other query is answered by the BEM itself, and
+a random audit subset is re-solved by the BEM to judge the surrogate's error.
 """
 from __future__ import annotations
 
@@ -51,7 +52,7 @@ def rel_err(R, Rt):
     return np.max(np.abs(R - Rt), axis=(1, 2)) / np.max(np.abs(Rt), axis=(1, 2))
 
 
-def bem_tensors(params, n_elem=400, outer_level=1, outer_radius=20.0, eps=3e-8, ctx=None):
+def bem_tensors(params, n_elem=500, outer_level=2, outer_radius=200.0, eps=3e-8, ctx=None, solver=None):
     """Body-frame resistance tensors of superellipsoids (a = 1, b, c, e1, e2;
     no rotation) by the batched mixed-precision BEM, each body inside its own
     container sphere.  Returns (R [n, 6, 6], stats)."""
@@ -59,7 +60,8 @@ def bem_tensors(params, n_elem=400, outer_level=1, outer_radius=20.0, eps=3e-8, 
     for b, c, e1, e2 in np.asarray(params, dtype=np.float64)[:, :4]:
         body = M.superellipsoid_tri(1.0, b, c, e1, e2, n_elem, inward=True)
         meshes.append(M.particle_in_sphere(body, outer_level=outer_level, outer_radius=outer_radius))
-    R, nit, istop, st = batch_resistance(meshes, eps=eps, ctx=ctx)
+    kw = {} if solver is None else {"solver": solver}
+    R, nit, istop, st = batch_resistance(meshes, eps=eps, ctx=ctx, **kw)
     return R, st
 
 
@@ -161,16 +163,31 @@ class MLP:
 
 
 class Surrogate:
-    """MLP + training hull + BEM fallback."""
+    """An ensemble of MLPs + training hull + BEM fallback.
 
-    def __init__(self, device=0, seed=1, bem_kwargs=None):
-        self.net = MLP(device=device, seed=seed)
+    The members share the training data and differ in their initial weights
+    and batch order.  A query inside the training hull is answered by the
+    members' mean when their spread (max-entry distance of the members from the
+    mean, relative to the mean's largest entry) is at most ``tau``; ``tau`` is
+    calibrated on held-out BEM tensors (:meth:`calibrate`) so that every
+    accepted held-out answer is within the target error.  Every other query --
+    outside the hull or with a larger spread -- is answered by the BEM."""
+
+    def __init__(self, device=0, seed=1, bem_kwargs=None, members=4):
+        self.nets = [MLP(device=device, seed=seed + 7919 * k) for k in range(max(1, members))]
+        self.net = self.nets[0]
         self.hull = Hull()
         self.bem_kwargs = dict(bem_kwargs or {})
+        self.tau = np.inf
+
+    def close(self):
+        for n in self.nets:
+            n.close()
 
     def fit(self, params, R, epochs=400, batch=512, lr=1e-3, lr_final=1e-5, seed=0):
-        """Train on BEM tensors R of shapes `params`; the learning rate decays
-        geometrically from lr to lr_final over four stages of the epochs."""
+        """Train every member on BEM tensors R of shapes `params`; the learning
+        rate decays geometrically from lr to lr_final over four stages of the
+        epochs.  Returns (loss history of the first member, summed stats)."""
         X = features(params)
         Y = tensor_to_targets(R)
         self.hull.fit(X)
@@ -178,43 +195,86 @@ class Surrogate:
         ym = Y.mean(axis=0)
         ys = Y.std(axis=0)
         ys = np.maximum(ys, 1e-3 * np.max(ys))  # near-constant entries (symmetric shapes) keep a sane scale
-        self.net.set_normalization(xm, xs, ym, ys)
-        hist, total = [], {"device_ms": 0.0, "launches": 0, "adam_steps": 0}
+        hist0, total = None, {"device_ms": 0.0, "launches": 0, "adam_steps": 0}
         stages = 4
-        for k in range(stages):
-            e = epochs // stages + (1 if k < epochs % stages else 0)
-            lr_k = lr * (lr_final / lr) ** (k / max(stages - 1, 1))
-            h, st = self.net.train(X, Y, e, batch=batch, lr=lr_k, seed=seed + k)
-            hist.extend(h.tolist())
-            total["device_ms"] += st["device_ms"]
-            total["launches"] += st["launches"]
-            total["adam_steps"] = st["adam_steps"]
-        return np.array(hist), total
+        for mi, net in enumerate(self.nets):
+            net.set_normalization(xm, xs, ym, ys)
+            hist = []
+            for k in range(stages):
+                e = epochs // stages + (1 if k < epochs % stages else 0)
+                lr_k = lr * (lr_final / lr) ** (k / max(stages - 1, 1))
+                h, st = net.train(X, Y, e, batch=batch, lr=lr_k, seed=seed + 1009 * mi + k)
+                hist.extend(h.tolist())
+                total["device_ms"] += st["device_ms"]
+                total["launches"] += st["launches"]
+                total["adam_steps"] += st["adam_steps"]
+            if hist0 is None:
+                hist0 = np.array(hist)
+        return hist0, total
+
+    def ensemble(self, X):
+        """Members' mean targets [n, 21], their spread [n] and the summed kernel
+        time (ms) for features X."""
+        ys, ms = [], 0.0
+        for net in self.nets:
+            y, t = net.predict(X)
+            ys.append(y.astype(np.float64))
+            ms += t
+        Ys = np.stack(ys)
+        mean = Ys.mean(axis=0)
+        scale = np.max(np.abs(mean), axis=1)
+        spread = np.max(np.abs(Ys - mean[None]), axis=(0, 2)) / np.maximum(scale, 1e-300)
+        return mean, spread, ms
+
+    def calibrate(self, params, R, target=1e-3, margin=0.8):
+        """Largest spread threshold tau under which every held-out answer
+        (params, BEM tensors R) inside the hull is within margin * target of
+        the BEM.  Returns a summary of the held-out set."""
+        X = features(params)
+        inside = self.hull.contains(X)
+        mean, spread, _ = self.ensemble(X[inside])
+        err = rel_err(targets_to_tensor(mean), np.asarray(R)[inside])
+        order = np.argsort(spread)
+        ok = np.cumsum(err[order] > margin * target) == 0
+        nacc = int(np.sum(ok))  # a prefix of the spread-sorted held-out answers
+        self.tau = float(spread[order][nacc - 1]) if nacc > 0 else 0.0
+        return {"n": int(len(X)), "in_hull": int(inside.sum()), "accepted": nacc, "tau": self.tau,
+                "err_median": float(np.median(err)) if len(err) else None,
+                "err_max_accepted": float(np.max(err[order][:nacc])) if nacc else None}
 
     def predict(self, params, bem=True):
-        """Tensors for `params`: the MLP inside the hull, the BEM outside
-        (bem=False leaves NaN there).  Returns (R, inside mask, info)."""
+        """Tensors for `params`: the ensemble where the query is inside the hull
+        and the members agree within tau, the BEM elsewhere (bem=False leaves
+        NaN there).  Returns (R, accepted mask, info)."""
         X = features(params)
         inside = self.hull.contains(X)
         R = np.full((len(X), 6, 6), np.nan)
-        Y, ms = self.net.predict(X[inside])
-        R[inside] = targets_to_tensor(Y)
-        info = {"mlp_device_ms": ms, "n_mlp": int(inside.sum()), "n_bem": int((~inside).sum())}
-        if bem and (~inside).any():
-            Rb, st = bem_tensors(np.asarray(params)[~inside], **self.bem_kwargs)
-            R[~inside] = Rb
+        acc = np.zeros(len(X), bool)
+        ms = 0.0
+        if inside.any():
+            mean, spread, ms = self.ensemble(X[inside])
+            ok = spread <= self.tau
+            idx = np.where(inside)[0]
+            acc[idx[ok]] = True
+            R[idx[ok]] = targets_to_tensor(mean[ok])
+        info = {"mlp_device_ms": ms, "n_mlp": int(acc.sum()), "n_bem": int((~acc).sum()),
+                "n_outside_hull": int((~inside).sum()), "n_spread_rejected": int((inside & ~acc).sum())}
+        if bem and (~acc).any():
+            Rb, st = bem_tensors(np.asarray(params)[~acc], **self.bem_kwargs)
+            R[~acc] = Rb
             info["bem_ms"] = st["device_ms"]
-        return R, inside, info
+        return R, acc, info
 
     def audit(self, params, frac=0.01, seed=0):
         """BEM re-solve of a random fraction of the queries: max-entry relative
-        errors of the surrogate on them."""
+        errors of the accepted surrogate answers among them, and which were
+        accepted."""
         rng = np.random.default_rng(seed)
         n = len(params)
         k = max(1, int(round(frac * n)))
         idx = np.sort(rng.choice(n, size=k, replace=False))
         sub = np.asarray(params)[idx]
-        R, inside, _ = self.predict(sub, bem=False)
+        R, acc, _ = self.predict(sub, bem=False)
         Rb, st = bem_tensors(sub, **self.bem_kwargs)
-        err = rel_err(R[inside], Rb[inside]) if inside.any() else np.zeros(0)
-        return err, idx, inside, st
+        err = rel_err(R[acc], Rb[acc]) if acc.any() else np.zeros(0)
+        return err, idx, acc, st

@@ -120,7 +120,11 @@ int agb_set_problem(agb_context* ctx, int kind, int nwalls, const int* walls, co
  *   sing_mode 0: analytic self-element integrals (si_tri_lap / si_tri_stk);
  *   sing_mode 1: recursive midpoint subdivision toward the source, rec_depth
  *                levels (Triangle_BEMInt lib_sdBem.f90:775, Triangle_StokesInt
- *                lib_Stokes.f90:2251; quads stay analytic); rec_depth 0..30;
+ *                lib_Stokes.f90:2251); rec_depth 0..30; a quad's own node or
+ *                centre by the polar Gauss scheme of the singular branch of
+ *                Quad_BEMInt / Quad_StokesInt (lib_int.f90:408,
+ *                lib_Stokes.f90:3494) with the problem's quad rule iqud (the
+ *                reference's parQuadIntegSing, default 4 as parQuadIntegRegu);
  *   near_eta > 0, near_depth 1..20: adaptive near-singular rule for the other
  *                triangles (no reference counterpart): a (sub-)triangle whose
  *                centroid is closer to the source than near_eta x its longest
@@ -140,7 +144,7 @@ int agb_set_integration(agb_context* ctx, int sing_mode, int rec_depth, double n
  * ||b - A x|| <= eps ||b|| or maxit iterations (0: 1000, the LIS default).  With
  * BiCGSTAB, istop[r] is 0 converged, 1 iteration limit, 2 breakdown, 3 diverged
  * or stagnated (the recursive residual rose 1e3 times above its best, or did
- * not fall by 10 % in 200 iterations: the FP32 products of an ill-conditioned
+ * not fall by 10 % in 64 iterations: the FP32 products of an ill-conditioned
  * system).  AGB_SOLVER_HYBRID: as BiCGSTAB where every right-hand side of the
  * system converges; otherwise all of them are solved again by LSQR and
  * istop[r] = 10 + LSQR's istop, nit[r] the sum of both iteration counts.  BiCGSTAB
@@ -178,9 +182,12 @@ int agb_rhs(agb_context* ctx, int nrhs, const double* u, double* rhs);
 
 /* Solve for nrhs fields at once.  x[r][n] holds the warm start on entry (the
  * reference warm-starts from the previous solution) and the unknowns on exit.
- * maxit = 0 -> 10*(m+n+50); eps as the SOLVER line.  refine = number of extra
- * residual-correction passes (FP64 residual of the stored matrix).
- * nit[r], istop[r] per right-hand side. */
+ * maxit = 0 -> 10*(m+n+50); eps as the SOLVER line.  refine = number of
+ * iterative-refinement passes after the solve (no counterpart in the
+ * reference): each computes r = b - A x with FP64 accumulation over the stored
+ * matrix, solves A d = r by LSQR from zero to the relative tolerance 1e-2 and
+ * sets x += d (LSQR solves only).  nit[r] counts every LSQR iteration, istop[r]
+ * is that of the first solve; per right-hand side. */
 int agb_solve(agb_context* ctx, int nrhs, const double* u, double* x, int maxit, double eps, int refine, int* nit,
               int* istop);
 

@@ -676,6 +676,104 @@ static void quad_stk_regular(int iqud, const double q[12], const double s[3], do
     }
 }
 
+// Singular branch of Quad_BEMInt (lib_int.f90:408-524) and Quad_StokesInt
+// (lib_Stokes.f90:3494-3654): the source at local node isrc (1..4 corners,
+// 5 centre: ksi/eta data at lib_int.f90:362-363) splits the parameter square
+// into four triangles, each integrated in polar coordinates about the source
+// (theta over [TH0, TH1], rho over [0, ROTH(theta)], ng x ng Gauss points of
+// rule iqud); the Jacobian rho cancels the 1/r singularity.  A triangle of zero
+// width (source on its edge) is skipped, as the reference's GOTO 1000 does.
+// visit(X, nn (unit normal times multi), w, f4) receives every point.
+template <class F>
+static void quad_polar(int iqud, const double q[12], int isrc, double multi, F&& visit) {
+  static const double ksi[5] = {0.0, 1.0, 1.0, 0.0, 0.5}, eta[5] = {0.0, 0.0, 1.0, 1.0, 0.5};
+  const double PI = 3.14159265358979323846, PI2 = 2.0 * PI;
+  const double *P1 = q, *P2 = q + 3, *P3 = q + 6, *P4 = q + 9;
+  const int ng1 = agb_tables::kGaussNg1[iqud - 1], ng2 = agb_tables::kGaussNg2[iqud - 1];
+  const double xx1 = ksi[isrc - 1], yy1 = eta[isrc - 1];  // one cell: a = c = -1, b = d = 1
+  for (int k = 1; k <= 4; ++k) {
+    double al, fii, th0, th1;
+    if (k == 1) {
+      if (1.0 - xx1 == 0.0) continue;
+      al = std::sqrt(yy1 * yy1 + (1.0 - xx1) * (1.0 - xx1));
+      fii = std::acos(yy1 / al);
+      th0 = 1.5 * PI + std::acos(yy1 / al);
+      th1 = PI2 + std::atan((1.0 - yy1) / (1.0 - xx1));
+    } else if (k == 2) {
+      if (1.0 - yy1 == 0.0) continue;
+      al = std::sqrt((1.0 - yy1) * (1.0 - yy1) + (1.0 - xx1) * (1.0 - xx1));
+      fii = std::acos((1.0 - xx1) / al);
+      th0 = std::asin((1.0 - yy1) / al);
+      th1 = 0.5 * PI + std::atan(xx1 / (1.0 - yy1));
+    } else if (k == 3) {
+      if (xx1 == 0.0) continue;
+      al = std::sqrt(xx1 * xx1 + (1.0 - yy1) * (1.0 - yy1));
+      fii = std::acos((1.0 - yy1) / al);
+      th0 = 0.5 * PI + std::acos((1.0 - yy1) / al);
+      th1 = PI + std::atan(yy1 / xx1);
+    } else {
+      if (yy1 == 0.0) continue;
+      al = std::sqrt(yy1 * yy1 + xx1 * xx1);
+      fii = std::acos(xx1 / al);
+      th0 = PI + std::acos(xx1 / al);
+      th1 = 1.5 * PI + std::atan((1.0 - xx1) / yy1);
+    }
+    for (int i = ng1; i <= ng2; ++i)
+      for (int j = ng1; j <= ng2; ++j) {
+        const double th = (th1 - th0) * GI(i) / 2.0 + (th1 + th0) / 2.0;
+        const double roth = al * std::sin(fii) / std::sin(th - th0 + fii);
+        const double ro = roth * GI(j) / 2.0 + roth / 2.0;
+        const double eti = 2.0 * (xx1 + ro * std::cos(th)) - 1.0;
+        const double etj = 2.0 * (yy1 + ro * std::sin(th)) - 1.0;
+        const double e1m = 1.0 - eti, e1p = 1.0 + eti, e2m = 1.0 - etj, e2p = 1.0 + etj;
+        const double f4[4] = {0.25 * e1m * e2m, 0.25 * e1p * e2m, 0.25 * e1p * e2p, 0.25 * e1m * e2p};
+        double X[3], KS[3], ET[3];
+        for (int c = 0; c < 3; ++c) {
+          X[c] = f4[0] * P1[c] + f4[1] * P2[c] + f4[2] * P3[c] + f4[3] * P4[c];
+          KS[c] = 0.25 * (-e2m * P1[c] + e2m * P2[c] + e2p * P3[c] - e2p * P4[c]);
+          ET[c] = 0.25 * (-e1m * P1[c] - e1p * P2[c] + e1p * P3[c] + e1m * P4[c]);
+        }
+        const double anx = KS[1] * ET[2] - ET[1] * KS[2];
+        const double any = ET[0] * KS[2] - KS[0] * ET[2];
+        const double anz = KS[0] * ET[1] - ET[0] * KS[1];
+        const double ajac = 1.0 / std::sqrt(anx * anx + any * any + anz * anz);
+        const double nn[3] = {multi * anx * ajac, multi * any * ajac, multi * anz * ajac};
+        const double w = (th1 - th0) * roth * ro * OME(i) * OME(j) / ajac;
+        visit(X, nn, w, f4);
+      }
+  }
+}
+// Laplace: out[0] = G, out[1..4] = H at the nodes (BemKernel, lib_sdBem.f90:911)
+static void quad_lap_polar(int iqud, const double q[12], const double s[3], int isrc, double multi, double out[5]) {
+  for (int k = 0; k < 5; ++k) out[k] = 0.0;
+  const double fpi = 1.0 / (4.0 * 3.14159265358979323846);
+  quad_polar(iqud, q, isrc, multi, [&](const double* X, const double* nn, double w, const double* f4) {
+    const double rx = s[0] - X[0], ry = s[1] - X[1], rz = s[2] - X[2];
+    const double ra = std::sqrt(rx * rx + ry * ry + rz * rz);
+    const double fg = fpi / ra;
+    const double fh = (rx * nn[0] + ry * nn[1] + rz * nn[2]) / (ra * ra) * fg;
+    for (int k = 0; k < 4; ++k) out[1 + k] += fh * w * f4[k];
+    out[0] += fg * w;
+  });
+}
+// Stokes: G and T of the element; its pressure integrals prG (a Cauchy
+// principal value) and prT (hypersingular) are left zero, as the analytic
+// self-element branch leaves them (lib_intAna.f90:43-82) -- the polar rule
+// cannot integrate them, and the reference never calls this branch with its
+// source on the element (lib_Stokes.f90:3199 passes isrc = 0).
+static void quad_stk_polar(int iqud, const double q[12], const double s[3], int isrc, double multi, StkElem& E) {
+  E.zero();
+  double G[3][3], T[3][3], prG[3], prT[3];
+  quad_polar(iqud, q, isrc, multi, [&](const double* X, const double* nn, double w, const double* f4) {
+    stokes_kernel(s, X, nn, G, T, prG, prT);
+    for (int k = 0; k < 6; ++k) E.G[k] += w * G[kSym[k][0]][kSym[k][1]];
+    for (int isip = 0; isip < 4; ++isip) {
+      const double ww = w * f4[isip];
+      for (int k = 0; k < 6; ++k) E.T[k][isip] += ww * T[kSym[k][0]][kSym[k][1]];
+    }
+  });
+}
+
 // -----------------------------------------------------------------------------
 // Problem state: mesh + single subdomain + boundary conditions
 // -----------------------------------------------------------------------------
@@ -850,6 +948,11 @@ static void lap_row_u(const Problem& P, int irow, double* rowH, double* rowG, do
           quad_lap_regular(P.iqud, v, s, mm, out);
           integ = out[0];
           for (int k = 0; k < 4; ++k) inteH[k] = out[1 + k];
+        } else if (P.opt.sing == 1) {
+          double out[5];
+          quad_lap_polar(P.iqud, v, s, isrc, mm, out);
+          integ = out[0];
+          for (int k = 0; k < 4; ++k) inteH[k] = out[1 + k];
         } else {
           integ = si_qua_lap(v, isrc);
         }
@@ -896,6 +999,11 @@ static void lap_row_q(const Problem& P, int irow, double* rowH, double* rowG, do
         if (isrc == 0) {
           double out[5];
           quad_lap_regular(P.iqud, v, s, mm, out);
+          integ = out[0];
+          for (int k = 0; k < 4; ++k) inteH[k] = out[1 + k];
+        } else if (P.opt.sing == 1) {
+          double out[5];
+          quad_lap_polar(P.iqud, v, s, isrc, mm, out);
           integ = out[0];
           for (int k = 0; k < 4; ++k) inteH[k] = out[1 + k];
         } else {
@@ -959,6 +1067,7 @@ static void stk_element(const Problem& P, int ie, const double s[3], int isrc, d
     }
   } else {
     if (isrc == 0) quad_stk_regular(P.iqud, v, s, mm, E);
+    else if (P.opt.sing == 1) quad_stk_polar(P.iqud, v, s, isrc, mm, E);
     else si_qua_stk(v, isrc, E.G);  // Quad_StokesIntAna (lib_intAna.f90:43-82)
   }
 }
@@ -1865,6 +1974,15 @@ double orc_tri_area(const double v[9]) { return tri_area(v[0], v[1], v[2], v[3],
 double orc_si_tri_lap(const double v[9], int isrc) { return si_tri_lap(v, orc_tri_area(v), isrc); }
 void orc_si_tri_stk(const double v[9], int isrc, double G[6]) { si_tri_stk(v, orc_tri_area(v), isrc, G); }
 double orc_si_qua_lap(const double q[12], int isrc) { return si_qua_lap(q, isrc); }
+// the polar singular quad scheme: out[0] = G, out[1..4] = H (Laplace); G[6] (Stokes)
+void orc_quad_lap_polar(int iqud, const double q[12], const double s[3], int isrc, double multi, double out[5]) {
+  quad_lap_polar(iqud, q, s, isrc, multi, out);
+}
+void orc_quad_stk_polar(int iqud, const double q[12], const double s[3], int isrc, double multi, double G[6]) {
+  StkElem E;
+  quad_stk_polar(iqud, q, s, isrc, multi, E);
+  for (int k = 0; k < 6; ++k) G[k] = E.G[k];
+}
 void orc_si_qua_stk(const double q[12], int isrc, double G[6]) { si_qua_stk(q, isrc, G); }
 
 // Regular (non-singular) element integrals, for kernel-level checks.

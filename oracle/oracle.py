@@ -45,6 +45,8 @@ def lib():
         L.orc_si_qua_lap.argtypes = [dp, C.c_int]
         L.orc_si_qua_lap.restype = C.c_double
         L.orc_si_qua_stk.argtypes = [dp, C.c_int, dp]
+        L.orc_quad_lap_polar.argtypes = [C.c_int, dp, dp, C.c_int, C.c_double, dp]
+        L.orc_quad_stk_polar.argtypes = [C.c_int, dp, dp, C.c_int, C.c_double, dp]
         L.orc_tri_lap_regular.argtypes = [C.c_int, dp, dp, dp, dp]
         L.orc_tri_stk_regular.argtypes = [C.c_int, dp, dp, dp, dp]
         L.orc_problem_create.argtypes = [C.c_int, C.c_int, dp, C.c_int, ip, ip, ip, C.c_int, ip, dp, C.c_double, ip,
@@ -120,6 +122,23 @@ def si_qua_lap(q, isrc):
 def si_qua_stk(q, isrc):
     G = np.zeros(6)
     lib().orc_si_qua_stk(np.ascontiguousarray(q, dtype=np.float64).ravel(), isrc, G)
+    return G
+
+
+def quad_lap_polar(iqud, q, s, isrc, multi=1.0):
+    """Singular branch of Quad_BEMInt (polar Gauss about local node isrc):
+    (G, H[4])."""
+    out = np.zeros(5)
+    lib().orc_quad_lap_polar(int(iqud), np.ascontiguousarray(q, dtype=np.float64).ravel(),
+                             np.ascontiguousarray(s, dtype=np.float64).ravel(), int(isrc), float(multi), out)
+    return out[0], out[1:]
+
+
+def quad_stk_polar(iqud, q, s, isrc, multi=1.0):
+    """Singular branch of Quad_StokesInt: the six Stokeslet integrals."""
+    G = np.zeros(6)
+    lib().orc_quad_stk_polar(int(iqud), np.ascontiguousarray(q, dtype=np.float64).ravel(),
+                             np.ascontiguousarray(s, dtype=np.float64).ravel(), int(isrc), float(multi), G)
     return G
 
 

@@ -15,7 +15,7 @@ the cases on this path:
 The node coordinates, the triangles (node order as in the file: the reference takes
 the element normal from nodes 1-3) and the physical wall ids are written to
 tests/golden/<name>.npz.  Run from the repository root:
-    python tests/golden/make_fixture_meshes.py /root/reference
+    python tests/golden/make_fixture_meshes.py <reference checkout>
 """
 import os
 import sys
@@ -111,4 +111,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_fixture_meshes.py <reference checkout>")
+    main(sys.argv[1])

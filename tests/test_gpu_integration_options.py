@@ -1,7 +1,9 @@
 """GPU parity of the integration options (agb_set_integration) against the
 oracle run with the same options: the recursive self-element subdivision of
-Triangle_BEMInt / Triangle_StokesInt (lib_sdBem.f90:775, lib_Stokes.f90:2251)
-and the adaptive near-singular rule, through the general FP64 assembly.
+Triangle_BEMInt / Triangle_StokesInt (lib_sdBem.f90:775, lib_Stokes.f90:2251),
+the polar singular scheme of Quad_BEMInt / Quad_StokesInt (lib_int.f90:408,
+lib_Stokes.f90:3494) for a quad's own node or centre, and the adaptive
+near-singular rule, through the general FP64 assembly.
 
 Tolerance: 1e-12 relative to the largest entry of each integral matrix (FP64 on
 both sides; only FMA contraction and the row-sum order differ).
@@ -54,6 +56,39 @@ def test_stokes_options_parity(agb, orc, opt):
     C.set_integration(*opt)
     T, G, _ = C.integral_matrices()
     _check(T, G, P, 9)
+
+
+@pytest.mark.parametrize("kind", ["laplace", "stokes"])
+def test_quad_polar_singular_parity(agb, orc, kind):
+    """sing_mode 1 on a quad mesh: the own-node / centre integrals by the polar
+    scheme of the singular branch of Quad_BEMInt / Quad_StokesInt, GPU against
+    the oracle; a box with a warped face, so the polar H / T of the self element
+    do not vanish."""
+    m = M.quad_box(2, 2, 2, hi=(1.0, 0.7, 0.5), face_walls=True)
+    m = dict(m)
+    xyz = m["xyz"].copy()
+    top = np.isclose(xyz[:, 2], 0.5) & np.isclose(xyz[:, 0], 0.5) & np.isclose(xyz[:, 1], 0.35)
+    xyz[top, 2] += 0.08  # the middle node of the top face: its four quads become non-planar
+    m["xyz"] = xyz
+    walls = [1, 2, 3, 4, 5, 6]
+    if kind == "laplace":
+        known = [[1, 1, 2, 2, 2, 2]]
+        P = orc.Problem(1, m, walls=walls, known=known, itri=4, iqud=4)
+        k, ncomp = agb.LAPLACE, 1
+    else:
+        known = np.ones((3, 6), np.int32)
+        P = orc.Problem(2, m, walls=walls, known=known, itri=4, iqud=4)
+        k, ncomp = agb.STOKES, 9
+    P.set_integration(1, 6, 0.0, 0)
+    P.form_integrals()
+    C = agb.Context(0)
+    C.set_mesh(m)
+    C.set_problem(k, walls, known, itri=4, iqud=4)
+    C.set_integration(1, 6, 0.0, 0)
+    T, G, _ = C.integral_matrices()
+    C.close()
+    _check(T, G, P, ncomp)
+    assert np.count_nonzero(top) == 1
 
 
 def test_options_route_resistance_tensor_through_general_path(agb):

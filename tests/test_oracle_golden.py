@@ -101,6 +101,32 @@ def test_quad_singular_is_triangle_fan(orc):
     assert np.max(np.abs(g - eg)) < 1e-14
 
 
+@pytest.mark.parametrize("isrc", [1, 2, 3, 4, 5])
+def test_quad_polar_singular_scheme_against_closed_forms(orc, isrc):
+    """The singular branch of Quad_BEMInt / Quad_StokesInt (lib_int.f90:408-524,
+    lib_Stokes.f90:3494-3654: polar Gauss about the source in four triangles of
+    the parameter square) against the Ren-Chan closed forms of the split quad
+    (si_qua_lap / si_qua_stk): two independent methods, equal to 2e-14 at the
+    6- and 8-point rules on a flat quad (H vanishes there); at the reference's
+    default rule (IQUD 4) within 2e-7."""
+    q = np.array([[0, 0, 0], [1.3, 0.1, 0], [1.1, 0.9, 0], [-0.1, 1.0, 0]], dtype=float)
+    s = q[isrc - 1] if isrc < 5 else q.mean(0)
+    a, b = orc.si_qua_lap(q, isrc), orc.si_qua_stk(q, isrc)
+    for iqud, tol in ((4, 2e-7), (6, 2e-14), (8, 2e-14)):
+        g, h = orc.quad_lap_polar(iqud, q, s, isrc)
+        G = orc.quad_stk_polar(iqud, q, s, isrc)
+        assert abs(g - a) <= tol * abs(a)
+        assert np.max(np.abs(G - b)) <= tol * np.max(np.abs(b))
+        assert np.max(np.abs(h)) == 0.0
+    # a warped quad: the rule converges (6 vs 8 points) to 1e-12
+    w = q.copy()
+    w[2, 2] = 0.3
+    s = w[isrc - 1] if isrc < 5 else w.mean(0)
+    g6, h6 = orc.quad_lap_polar(6, w, s, isrc)
+    g8, h8 = orc.quad_lap_polar(8, w, s, isrc)
+    assert abs(g6 - g8) <= 1e-12 * abs(g8) and np.max(np.abs(h6 - h8)) <= 1e-12 * max(1e-3, np.max(np.abs(h8)))
+
+
 def test_mesh_generators_counts():
     m3 = M.icosphere(3)
     assert len(m3["xyz"]) == 642 and len(m3["etype"]) == 1280
