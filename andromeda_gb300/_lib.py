@@ -47,6 +47,10 @@ SIGNATURES = {
     "agb_lsqr_solve": ([I, I, C.c_int64, PI, D, PI, PI, dp, lp, ip, dp, dp, dp], I),
     "agb_lsqr_precon_dense_noalloc": ([I, I, C.c_int64, vp, vp], I),
     "agb_selftest_bounded_wait": ([I, C.c_uint, I, C.POINTER(C.c_int)], I),
+    "agb_mesh_read": ([C.c_char_p, ip, vp, vp, vp, vp, vp, C.c_char_p, I], I),
+    "agb_vtu_write": ([C.c_char_p, I, I, dp, I, ip, ip, ip, dp, I, C.POINTER(C.c_char_p), dp, dp, vp], I),
+    "agb_integrals_file_write": ([C.c_char_p, I, I, I, I, dp, dp, dp], I),
+    "agb_integrals_file_read": ([C.c_char_p, I, ip, dp, vp, vp], I),
     "agb_integral_matrices": ([vp, vp, vp, vp], I),
     "agb_layout_sizes": ([vp, ip], I),
     "agb_solve_fields": ([vp, I, dp, vp, dp, dp, I, D, I, ip, ip], I),

@@ -17,7 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libandromeda_gb300.so")
 SOURCES = ["agb_api.cu", "agb_assembly.cu", "agb_lsqr.cu", "agb_noalloc.cu", "agb_general.cu", "agb_batch.cu",
-           "agb_lu.cu", "agb_mlp.cu", "agb_mfree.cu", "agb_bicg.cu", "agb_selftest.cu"]
+           "agb_lu.cu", "agb_mlp.cu", "agb_mfree.cu", "agb_bicg.cu", "agb_selftest.cu",
+           "agb_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 
@@ -30,7 +31,7 @@ def nvcc() -> str:
 
 
 def _deps():
-    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h"))]
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h", ".cpp"))]
     deps.append(os.path.join(HERE, "..", "include", "andromeda_gb300.h"))
     return deps
 
@@ -49,7 +50,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     cc = nvcc()
 
     def compile_one(src):
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         cmd = [cc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)

@@ -420,6 +420,8 @@ int device_rhs(agb_context* c, int nrhs, int na) {
 int assemble_general(agb_context* c, int precision);
 // relative LSQR tolerance of each refinement correction solve
 constexpr double kRefineEps = 1.0e-2;
+// restarts of BiCGSTAB on its FP64 true residual
+constexpr int kBicgRestarts = 4;
 __global__ void k_axpy(int64_t n, const double* __restrict__ d, double* __restrict__ x) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) x[t] += d[t];
@@ -437,12 +439,66 @@ int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int r
                                           "wall, triangles, default integration, AGB_MIXED)");
     if (!c->lsqr.bicgstab(c->d_rhs, d_x, eps, maxit, nt.data(), is.data()))
       return fail(c, AGB_ERR_CUDA, "bicgstab: " + c->lsqr.err);
+    // The recursive residual of the FP32 products can drift from the true one:
+    // form r = b - A x with FP64 accumulation and, while a right-hand side's
+    // true residual is above eps ||b||, solve A d = r by BiCGSTAB (to eps
+    // ||b|| / ||r||) and set x += d -- FP64 refinement around the mixed solver.
+    {
+      const int64_t m = c->m, n = c->n;
+      std::vector<double> hb((size_t)nrhs * m), hr((size_t)nrhs * m);
+      std::vector<double> bn(nrhs, 0.0);
+      CUDA_OR_FAIL(c, cudaMemcpyAsync(hb.data(), c->d_rhs, hb.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                      c->stream));
+      CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+      for (int r = 0; r < nrhs; ++r) {
+        double ss = 0.0;
+        for (int64_t i = 0; i < m; ++i) ss += hb[(size_t)r * m + i] * hb[(size_t)r * m + i];
+        bn[r] = std::sqrt(ss);
+      }
+      CUDA_OR_FAIL(c, ensure(c->d_res, c->cap_res, (size_t)nrhs * m));
+      CUDA_OR_FAIL(c, ensure(c->d_dx, c->cap_dx, (size_t)nrhs * n));
+      for (int pass = 0; pass <= kBicgRestarts; ++pass) {
+        if (!c->lsqr.residual(c->d_rhs, d_x, c->d_q, c->d_res)) return fail(c, AGB_ERR_CUDA, "residual: " + c->lsqr.err);
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(hr.data(), c->d_res, hr.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                        c->stream));
+        CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+        double worst = 0.0;
+        bool again = false;
+        for (int r = 0; r < nrhs; ++r) {
+          double ss = 0.0;
+          for (int64_t i = 0; i < m; ++i) ss += hr[(size_t)r * m + i] * hr[(size_t)r * m + i];
+          const double rel = bn[r] > 0.0 ? std::sqrt(ss) / bn[r] : 0.0;
+          if (rel > eps && is[r] <= 1) {
+            again = true;
+            worst = std::max(worst, rel);
+            is[r] = 4;  // true residual above eps (until a restart brings it down)
+          } else {
+            if (is[r] == 4) is[r] = 0;
+            // a right-hand side that is done gets no further correction
+            CUDA_OR_FAIL(c, cudaMemsetAsync(c->d_res + (size_t)r * m, 0, (size_t)m * sizeof(double), c->stream));
+          }
+        }
+        if (!again || pass == kBicgRestarts) break;
+        std::vector<int> n2(nrhs, 0), i2(nrhs, 0);
+        CUDA_OR_FAIL(c, cudaMemsetAsync(c->d_dx, 0, (size_t)nrhs * n * sizeof(double), c->stream));
+        if (!c->lsqr.bicgstab(c->d_res, c->d_dx, eps / worst, maxit, n2.data(), i2.data()))
+          return fail(c, AGB_ERR_CUDA, "bicgstab (restart): " + c->lsqr.err);
+        k_axpy<<<(unsigned)(((int64_t)nrhs * n + 255) / 256), 256, 0, c->stream>>>((int64_t)nrhs * n, c->d_dx, d_x);
+        CUDA_OR_FAIL(c, cudaGetLastError());
+        c->nlaunch += 1;
+        for (int r = 0; r < nrhs; ++r) {
+          nt[r] += n2[r];
+          if (is[r] == 4 && i2[r] >= 2) is[r] = i2[r];  // the restart broke down or diverged
+        }
+      }
+    }
     bool all_converged = true;
     for (int r = 0; r < nrhs; ++r) all_converged = all_converged && is[r] == 0;
     if (c->solver == AGB_SOLVER_HYBRID && !all_converged) {
       // LSQR (the reference's lsqr_solve, default iteration limit) from a zero
       // start on every right-hand side
       std::vector<int> nl(nrhs, 0), il(nrhs, 0);
+      CUDA_OR_FAIL(c, cudaMemsetAsync(d_x, 0, (size_t)nrhs * c->n * sizeof(double), c->stream));
       if (!c->lsqr.solve(c->d_rhs, d_x, c->d_q, eps, 0, nl.data(), il.data(), nullptr, 8, true))
         return fail(c, AGB_ERR_CUDA, "lsqr after bicgstab: " + c->lsqr.err);
       for (int r = 0; r < nrhs; ++r) {
@@ -469,6 +525,8 @@ int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int r
     CUDA_OR_FAIL(c, ensure(c->d_res, c->cap_res, (size_t)nrhs * c->m));
     CUDA_OR_FAIL(c, ensure(c->d_dx, c->cap_dx, (size_t)nrhs * c->n));
     if (!c->lsqr.residual(c->d_rhs, d_x, c->d_q, c->d_res)) return fail(c, AGB_ERR_CUDA, "residual: " + c->lsqr.err);
+    // the solve from zero adds its start vector to the result: it must be zero
+    CUDA_OR_FAIL(c, cudaMemsetAsync(c->d_dx, 0, (size_t)nrhs * c->n * sizeof(double), c->stream));
     if (!c->lsqr.solve(c->d_res, c->d_dx, c->d_q, kRefineEps, maxit, nt.data(), is.data(), nullptr, 8, true))
       return fail(c, AGB_ERR_CUDA, "lsqr (refinement): " + c->lsqr.err);
     k_axpy<<<(unsigned)(((int64_t)nrhs * c->n + 255) / 256), 256, 0, c->stream>>>((int64_t)nrhs * c->n, c->d_dx, d_x);

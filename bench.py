@@ -76,6 +76,9 @@ def parse():
                     help="large: packed FP32 matrix resident in HBM and solved to convergence, or matrix-free sweeps")
     ap.add_argument("--large-maxit", type=int, default=0, help="large/resident: LSQR iteration limit (0: reference default)")
     ap.add_argument("--grid", default="160x320", help="large: superellipsoid rings x sectors")
+    ap.add_argument("--large-eps", type=float, default=3e-8,
+                    help="large: solver tolerance (LSQR at 1e-7 leaves 2.4e-6 on the 40x80 grid of this shape; "
+                         "3e-8 meets 1e-6)")
     ap.add_argument("--large-fp64-eps", type=float, default=1e-10,
                     help="large/resident: also solve the FP64 path to this eps where its matrix fits (0: off)")
     ap.add_argument("--itri", type=int, default=1, help="laplace: triangle rule (1 = 7 points)")
@@ -482,7 +485,7 @@ def run_large(args):
         with ClockSampler(0) as clk:
             t0 = time.perf_counter()
             C.kernel_times(reset=True)
-            R, nit, info = C.resistance_tensor(A.MIXED, 1, 2, maxit=args.large_maxit, eps=args.eps)
+            R, nit, info = C.resistance_tensor(A.MIXED, 1, 2, maxit=args.large_maxit, eps=args.large_eps)
             t1 = time.perf_counter()
         kt = C.kernel_times(reset=True)
         av_ms = kt["av_ms"] / max(kt["av_launches"], 1)
@@ -516,7 +519,7 @@ def run_large(args):
                 "value": 1000.0 / info["device_ms"], "unit": "solves/s", "n_gpus": 1, "steps": 1, "warmup": 0,
                 "ms_per_step": info["device_ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "fp32 (fp64 singular/free-term/reductions)", "data": "synthetic",
-                "config": {"workload": workload + ", " + solver_text(args.solver, args.eps), "unknowns": C.n,
+                "config": {"workload": workload + ", " + solver_text(args.solver, args.large_eps), "unknowns": C.n,
                            "packed_matrix_gb": alg / 1e9, "l2": "inputs larger than L2, no flush"},
                 "assemble_ms": info["assemble_ms"], "rhs_ms": info["rhs_ms"], "solve_ms": info["solve_ms"],
                 "nit": [int(v) for v in nit], "istop": info["istop"],

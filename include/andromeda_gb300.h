@@ -145,7 +145,11 @@ int agb_set_integration(agb_context* ctx, int sing_mode, int rec_depth, double n
  * BiCGSTAB, istop[r] is 0 converged, 1 iteration limit, 2 breakdown, 3 diverged
  * or stagnated (the recursive residual rose 1e3 times above its best, or did
  * not fall by 10 % in 64 iterations: the FP32 products of an ill-conditioned
- * system).  AGB_SOLVER_HYBRID: as BiCGSTAB where every right-hand side of the
+ * system), 4 the true residual stayed above eps.  The recursive residual of the
+ * FP32 products can drift from the true one, so after BiCGSTAB stops the true
+ * residual b - A x is formed with FP64 accumulation, and a right-hand side
+ * whose true residual is above eps ||b|| is solved again from x on that
+ * residual (FP64 refinement, at most 4 restarts).  AGB_SOLVER_HYBRID: as BiCGSTAB where every right-hand side of the
  * system converges; otherwise all of them are solved again by LSQR and
  * istop[r] = 10 + LSQR's istop, nit[r] the sum of both iteration counts.  BiCGSTAB
  * needs the packed mixed system (Stokes, velocity known on every wall,
@@ -267,6 +271,49 @@ int agb_surface_pressure(agb_context* ctx, const double* u, const double* q, dou
  * (the regular branch of Quad_StokesInt / Quad_BEMInt).  FP64. */
 int agb_domain_values(agb_context* ctx, int npts, const double* pts, const double* u, const double* q, double* out,
                       double* err);
+
+/* ---- file formats of the reference (host code, no GPU work; errors via
+ * agb_last_error(NULL)) ---------------------------------------------------- */
+
+/* Surface mesh as ReadMesh reads it (lib_meshRead.f90:80-160): gmsh 2.x ASCII
+ * (ReadGMSHv2 :244), gmsh 4.x ASCII (ReadGMSHv4Surface :385; element blocks of
+ * a dimension other than 2 are skipped, where the reference refuses a gmsh 4
+ * file whose entities include volumes) or the reference's "andromedaMesh" text
+ * (ReadAndromedaMesh :165).  Lines are read as rOneTL (lib_mesh.f90:1804)
+ * reads them: blank lines and lines holding '#' are skipped.  Node and element
+ * tags give the positions (node(j), element(j)).  Call with xyz == NULL to get
+ * sizes = {nnodes, nelem, nwalls}; then with arrays of those sizes: xyz
+ * 3*nnodes, etype/bcid nelem, con 4*nelem (0-based, -1 as the 4th node of a
+ * triangle: the layout of agb_set_mesh), wall_ids nwalls and wall_names
+ * nwalls x name_len bytes (NUL-padded; both may be NULL).  Element types other
+ * than 2/3 and node tags out of range are AGB_ERR_ARG (the reference stops). */
+int agb_mesh_read(const char* path, int* sizes, double* xyz, int* etype, int* con, int* bcid, int* wall_ids,
+                  char* wall_names, int name_len);
+
+/* ParaView result file (OutputMeshParaview, lib_mesh.f90:218-392): ASCII VTK
+ * UnstructuredGrid with point data u (3-vector for Stokes), node, u<name> per
+ * equation; cell data normale, pressure (Stokes), elemBCid, q<name>; points and
+ * cells (VTK types 5 triangle / 9 quad).  u [neq][nnodes], q [neq][nelem],
+ * normal [nelem][3], p [nelem] (Stokes; NULL for Laplace), names: neq equation
+ * names (x, y, z for Stokes). */
+int agb_vtu_write(const char* path, int kind, int nnodes, const double* xyz, int nelem, const int* etype,
+                  const int* con, const int* bcid, const double* normal, int neq, const char* const* names,
+                  const double* u, const double* q, const double* p);
+
+/* The integral-matrix cache and.integrals.bin (WriteIntegralsToDisk /
+ * ReadIntegralsFile lib_int.f90:136-221; WriteIntegralsToDiskStokes /
+ * ReadIntegralsFileStokes lib_Stokes.f90:2742-2876) in the record layout
+ * gfortran writes for FORM='UNFORMATTED' sequential files, one subdomain:
+ * [Stokes: parStokes = 1407], (nsp, nnodes, nqnodes), (FspCerr, QspCerr), then
+ * the matrices column by column in records of at most 8192 values (WrSMat,
+ * lib_util.f90:201) -- Laplace H, G; Stokes Txx,Tyy,Tzz,Txy,Txz,Tyz,
+ * Gxx,Gyy,Gzz,Gxy,Gxz,Gyz, prTx..z, prGx..z.  T and G are laid out as
+ * agb_integral_matrices returns them.  Reading: with T == NULL only sizes and
+ * errs are returned; otherwise sizes must equal the file's (the reference's
+ * check, lib_int.f90:152-157). */
+int agb_integrals_file_write(const char* path, int kind, int nsp, int nnodes, int nqnodes, const double* errs,
+                             const double* T, const double* G);
+int agb_integrals_file_read(const char* path, int kind, int* sizes, double* errs, double* T, double* G);
 
 /* Sizes of the subdomain numbering: {nsp, nn, nq, rows, unknowns, knowns}. */
 int agb_layout_sizes(agb_context* ctx, int* sizes);
