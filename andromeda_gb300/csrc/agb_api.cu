@@ -468,7 +468,7 @@ int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int r
           double ss = 0.0;
           for (int64_t i = 0; i < m; ++i) ss += hr[(size_t)r * m + i] * hr[(size_t)r * m + i];
           const double rel = bn[r] > 0.0 ? std::sqrt(ss) / bn[r] : 0.0;
-          if (rel > eps && is[r] <= 1) {
+          if (rel > eps && (is[r] == 0 || is[r] == 4)) {  // claimed converged, or restarted
             again = true;
             worst = std::max(worst, rel);
             is[r] = 4;  // true residual above eps (until a restart brings it down)
@@ -1631,6 +1631,68 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
     std::string err;
     if (c->solver != AGB_SOLVER_LSQR) {
       if (!batch_bicgstab_solve(bodies, 6, eps, maxit, st, nv, iv, &bst, err)) return bail(AGB_ERR_CUDA, "solve: " + err);
+      // FP64 refinement of the bodies whose recursive residual converged but whose
+      // true residual did not (istop 4): BiCGSTAB on r = b - A x from zero to
+      // eps ||b|| / ||r||, x += d, at most kBicgRestarts times
+      for (int pass = 0; pass < kBicgRestarts; ++pass) {
+        std::vector<BatchBody> redo;
+        std::vector<size_t> where;
+        for (size_t t = 0; t < bodies.size(); ++t) {
+          bool any4 = false, other = false;
+          for (int r = 0; r < 6; ++r) {
+            any4 = any4 || iv[6 * t + r] == 4;
+            other = other || (iv[6 * t + r] != 0 && iv[6 * t + r] != 4);
+          }
+          if (any4 && !other) {
+            redo.push_back(bodies[t]);
+            where.push_back(t);
+          }
+        }
+        if (redo.empty()) break;
+        std::vector<double*> rbuf(redo.size(), nullptr), dbuf(redo.size(), nullptr);
+        auto free_bufs = [&]() {
+          for (auto p : rbuf) if (p) cudaFreeAsync(p, st);
+          for (auto p : dbuf) if (p) cudaFreeAsync(p, st);
+        };
+        bool okb = true;
+        for (size_t u = 0; u < redo.size() && okb; ++u) {
+          okb = cudaMallocAsync(&rbuf[u], (size_t)6 * redo[u].m * sizeof(double), st) == cudaSuccess &&
+                cudaMallocAsync(&dbuf[u], (size_t)6 * redo[u].n * sizeof(double), st) == cudaSuccess &&
+                cudaMemsetAsync(dbuf[u], 0, (size_t)6 * redo[u].n * sizeof(double), st) == cudaSuccess;
+        }
+        std::vector<double> rel;
+        if (!okb || !batch_residual(redo, 6, st, rbuf, rel, err)) {
+          free_bufs();
+          return bail(AGB_ERR_CUDA, "restart residual: " + (okb ? err : std::string("allocation")));
+        }
+        double worst = 0.0;
+        for (size_t u = 0; u < redo.size(); ++u)
+          for (int r = 0; r < 6; ++r) {
+            const double v = rel[6 * u + r];
+            if (v > eps) worst = std::max(worst, v);
+            else if (cudaMemsetAsync(rbuf[u] + (size_t)r * redo[u].m, 0, (size_t)redo[u].m * sizeof(double), st) !=
+                     cudaSuccess) okb = false;  // done: no correction
+          }
+        std::vector<BatchBody> corr = redo;
+        for (size_t u = 0; u < redo.size(); ++u) {
+          corr[u].b = rbuf[u];
+          corr[u].x = dbuf[u];
+        }
+        std::vector<int> n2, i2;
+        if (!okb || worst <= 0.0 ||
+            !batch_bicgstab_solve(corr, 6, std::min(0.5, eps / worst), maxit, st, n2, i2, &bst, err) ||
+            !batch_axpy(redo, 6, dbuf, st, err) || !batch_residual(redo, 6, st, {}, rel, err)) {
+          free_bufs();
+          return bail(AGB_ERR_CUDA, "restart: " + err);
+        }
+        free_bufs();
+        for (size_t u = 0; u < redo.size(); ++u)
+          for (int r = 0; r < 6; ++r) {
+            const size_t t = 6 * where[u] + r;
+            nv[t] += n2[6 * u + r];
+            if (iv[t] == 4) iv[t] = rel[6 * u + r] <= eps ? 0 : (i2[6 * u + r] == 2 || i2[6 * u + r] == 3 ? i2[6 * u + r] : 4);
+          }
+      }
       if (c->solver == AGB_SOLVER_HYBRID) {
         // bodies with a right-hand side BiCGSTAB did not converge: batched LSQR
         // (default tiles, the reference's iteration limit) from a zero start

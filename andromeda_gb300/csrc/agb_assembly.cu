@@ -193,33 +193,36 @@ __global__ void __launch_bounds__(StkTile<T>::NW * 32) k_stokes_G(int ne, int Q,
       sx[r] = sxp[i]; sy[r] = syp[i]; sz[r] = szp[i];
     }
     T acc[RS][7];
-    if constexpr (sizeof(T) == 4) {
-      stokeslet_sums_f32<RS>(reinterpret_cast<const QPt<float>*>(sp), Q, lane, sx, sy, sz, acc);
-    } else {
 #pragma unroll
-      for (int r = 0; r < RS; ++r)
+    for (int r = 0; r < RS; ++r)
 #pragma unroll
-        for (int c = 0; c < 7; ++c) acc[r][c] = T(0);
+      for (int c = 0; c < 7; ++c) acc[r][c] = T(0);
 #pragma unroll 2
-      for (int q = 0; q < Q; ++q) {
-        const QPt<T> p = sp[q * 32 + lane];
+    for (int q = 0; q < Q; ++q) {
+      const QPt<T> p = sp[q * 32 + lane];
 #pragma unroll
-        for (int r = 0; r < RS; ++r) {
-          const T rx = p.x - sx[r], ry = p.y - sy[r], rz = p.z - sz[r];
-          const T r2 = rx * rx + ry * ry + rz * rz;
-          const T ir = rsq<T>(r2);
-          const T wi = p.w * ir;
-          const T wi3 = wi * (ir * ir);
-          acc[r][0] += wi;
-          const T ax = wi3 * rx, ay = wi3 * ry;
-          acc[r][1] += ax * rx;
-          acc[r][2] += ax * ry;
-          acc[r][3] += ax * rz;
-          acc[r][4] += ay * ry;
-          acc[r][5] += ay * rz;
-          acc[r][6] += (wi3 * rz) * rz;
-        }
+      for (int r = 0; r < RS; ++r) {
+        const T rx = p.x - sx[r], ry = p.y - sy[r], rz = p.z - sz[r];
+        const T r2 = rx * rx + ry * ry + rz * rz;
+        const T ir = rsq<T>(r2);
+        const T wi = p.w * ir;
+        const T wi3 = wi * (ir * ir);
+        acc[r][0] += wi;
+        const T ax = wi3 * rx, ay = wi3 * ry;
+        acc[r][1] += ax * rx;
+        acc[r][2] += ax * ry;
+        acc[r][3] += ax * rz;
+        acc[r][4] += ay * ry;
+        acc[r][5] += ay * rz;
+        // FP32: the zz sum follows from the trace, sum w rz^2/r^3 = sum w/r -
+        // (xx + yy), two instructions fewer per (source, point) in this
+        // issue-bound loop; the FP64 kernel sums it directly
+        if constexpr (sizeof(T) != 4) acc[r][6] += (wi3 * rz) * rz;
       }
+    }
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+      for (int r = 0; r < RS; ++r) acc[r][6] = acc[r][0] - acc[r][1] - acc[r][4];
     }
     if (j < ne) {
 #pragma unroll

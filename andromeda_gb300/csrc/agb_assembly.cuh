@@ -9,58 +9,6 @@ template <typename T> struct QPt;
 template <> struct __align__(16) QPt<float> { float x, y, z, w; };
 template <> struct __align__(32) QPt<double> { double x, y, z, w; };
 
-// Regular-quadrature sums of the Stokeslet over one element (the lane's
-// column: its Q points in sp[q * 32 + lane]) for RS source points, FP32:
-// acc[r] = {sum w/r, sum w rx rx/r^3, w rx ry/r^3, w rx rz/r^3, w ry ry/r^3,
-// w ry rz/r^3, w rz rz/r^3}.  Two sources per packed f32x2 instruction
-// (fma/add/mul.rn.f32x2 of sm_100+, each component rounded as the scalar
-// instruction), which halves the issued FP32 instructions of this issue-bound
-// loop; the rsqrt stays scalar.  28 flop per (source, point), an FMA counted as 2.
-template <int RS>
-__device__ __forceinline__ void stokeslet_sums_f32(const QPt<float>* __restrict__ sp, int Q, int lane,
-                                                   const float (&sx)[RS], const float (&sy)[RS], const float (&sz)[RS],
-                                                   float (&acc)[RS][7]) {
-  static_assert(RS % 2 == 0, "sources come in pairs");
-  float2 acc2[RS / 2][7], nsx[RS / 2], nsy[RS / 2], nsz[RS / 2];
-#pragma unroll
-  for (int h = 0; h < RS / 2; ++h) {
-    nsx[h] = make_float2(-sx[2 * h], -sx[2 * h + 1]);
-    nsy[h] = make_float2(-sy[2 * h], -sy[2 * h + 1]);
-    nsz[h] = make_float2(-sz[2 * h], -sz[2 * h + 1]);
-#pragma unroll
-    for (int c = 0; c < 7; ++c) acc2[h][c] = make_float2(0.f, 0.f);
-  }
-#pragma unroll 2
-  for (int q = 0; q < Q; ++q) {
-    const QPt<float> p = sp[q * 32 + lane];
-    const float2 px = make_float2(p.x, p.x), py = make_float2(p.y, p.y), pz = make_float2(p.z, p.z);
-    const float2 pw = make_float2(p.w, p.w);
-#pragma unroll
-    for (int h = 0; h < RS / 2; ++h) {
-      const float2 rx = __fadd2_rn(px, nsx[h]), ry = __fadd2_rn(py, nsy[h]), rz = __fadd2_rn(pz, nsz[h]);
-      const float2 r2 = __ffma2_rn(rx, rx, __ffma2_rn(ry, ry, __fmul2_rn(rz, rz)));
-      const float2 ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
-      const float2 wi = __fmul2_rn(pw, ir);
-      const float2 wi3 = __fmul2_rn(wi, __fmul2_rn(ir, ir));
-      acc2[h][0] = __fadd2_rn(acc2[h][0], wi);
-      const float2 ax = __fmul2_rn(wi3, rx), ay = __fmul2_rn(wi3, ry), az = __fmul2_rn(wi3, rz);
-      acc2[h][1] = __ffma2_rn(ax, rx, acc2[h][1]);
-      acc2[h][2] = __ffma2_rn(ax, ry, acc2[h][2]);
-      acc2[h][3] = __ffma2_rn(ax, rz, acc2[h][3]);
-      acc2[h][4] = __ffma2_rn(ay, ry, acc2[h][4]);
-      acc2[h][5] = __ffma2_rn(ay, rz, acc2[h][5]);
-      acc2[h][6] = __ffma2_rn(az, rz, acc2[h][6]);
-    }
-  }
-#pragma unroll
-  for (int h = 0; h < RS / 2; ++h)
-#pragma unroll
-    for (int c = 0; c < 7; ++c) {
-      acc[2 * h][c] = acc2[h][c].x;
-      acc[2 * h + 1][c] = acc2[h][c].y;
-    }
-}
-
 struct RuleDev {
   int Q = 0;
   double* l = nullptr;  // device [3][Q] barycentric coordinates

@@ -23,6 +23,7 @@
 #include "agb_sweeps.cuh"
 
 #include <algorithm>
+#include <cmath>
 #include <map>
 #include <mutex>
 #include <cstdio>
@@ -61,6 +62,7 @@ struct GDesc {  // CUtensorMap members keep the 64-byte alignment TMA needs
   // 1/diag(A), a second partial-sum array, the scalars; V is Y; sc0 zero gammas
   const float* A;
   double *Rb, *Rt, *Pb, *Sb, *Tb, *Xb, *dinv, *part2;
+  double* rr;  // ||b - A x||^2 per right-hand side (the FP64 check after the solve)
   BicgScalars* bs;
   const LsqrScalars* sc0;
 };
@@ -501,6 +503,50 @@ __global__ void gb_finish(const GDesc* __restrict__ D) {
   }
 }
 
+// ||b - A x||^2 per right-hand side with FP64 products and sums, A the body's
+// FP32 packed single layer, x from gb_finish: one warp per element row i (its
+// three equations), lanes over the element columns; a CTA per 8 rows of one
+// body (the A*V tiles of 16 rows, two CTAs each).  rr must start at zero.
+__global__ void __launch_bounds__(256) gb_resid(const GDesc* __restrict__ D, const int* __restrict__ off, int nb) {
+  const int tile = blockIdx.x >> 1;
+  const int bi = find_body(off, nb, tile);
+  const GDesc& d = D[bi];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = (tile - off[bi]) * AVP_R + (blockIdx.x & 1) * 8 + warp;
+  if (i >= d.pk_ne) return;  // a whole warp; the kernel has no block barrier
+  const int ne = d.pk_ne;
+  double acc[3][K8];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < K8; ++c) acc[a][c] = 0.0;
+  for (int j = lane; j < ne; j += 32) {
+    double g6[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) g6[c] = (double)d.A[pk_idx(i, c, j, d.pk_ldp)];
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+#pragma unroll
+      for (int c = 0; c < K8; ++c) {
+        if (c >= d.k) break;
+        const double xv = d.x[(int64_t)c * d.n + (int64_t)b * ne + j];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) acc[a][c] += g6[sym6(a, b)] * xv;
+      }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < K8; ++c) {
+      double v = acc[a][c];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0 && c < d.k) {
+        const double r = d.b[(int64_t)c * d.m + 3 * (int64_t)i + a] - v;
+        atomicAdd(&d.rr[c], r * r);
+      }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
@@ -551,7 +597,7 @@ struct BatchSolver {
     // pool layout (bytes), every piece 256-byte aligned
     size_t bytes = 0;
     auto take = [&](size_t n) { const size_t o = bytes; bytes += (n + 255) / 256 * 256; return o; };
-    struct Offs { size_t Y, Ys, V, W, X, Vp, Zp, part, sc, bg, part2, bs; };
+    struct Offs { size_t Y, Ys, V, W, X, Vp, Zp, part, sc, bg, part2, bs, rr; };
     std::vector<Offs> po(nb);
     const size_t o_sc0 = take(K8 * sizeof(LsqrScalars));  // zero gammas of the BiCGSTAB sweeps
     bytes_A = 0.0;
@@ -591,6 +637,7 @@ struct BatchSolver {
         po[i].bg = take((size_t)(6 * d.mpad * K8 + d.mpad) * sizeof(double));  // R, Rt, P, S, T, X; 1/diag
         po[i].part2 = take((size_t)nbmax * K8 * sizeof(double));
         po[i].bs = take(K8 * sizeof(BicgScalars));
+        po[i].rr = take(K8 * sizeof(double));
       }
       hoff_b[i + 1] = hoff_b[i] + d.nb_b;
       hoff_av[i + 1] = hoff_av[i] + d.nb_av;
@@ -620,6 +667,7 @@ struct BatchSolver {
         d.dinv = g + 6 * mv;
         d.part2 = (double*)(p + po[i].part2);
         d.bs = (BicgScalars*)(p + po[i].bs);
+        d.rr = (double*)(p + po[i].rr);
       }
       // the pool is zeroed: the pad columns pk_ne..pk_ldp-1 of Vp stay zero
       if (!make_tensor_map_2d(&d.tm_vp, d.Vp, d.pk_ldp, 3 * K8, AVP_BC, 3 * K8, err)) return false;
@@ -868,10 +916,17 @@ bool batch_bicgstab_solve(const std::vector<BatchBody>& bodies, int k, double to
   int mmax = 1;
   for (const auto& d : S.hd) mmax = std::max(mmax, d.m * K8);
   gb_finish<<<dim3(std::min<unsigned>(cdivu(mmax, 256), 1024), nb), 256, 0, s>>>(S.d_desc);
-  launches += 1;
+  // the true residual of every right-hand side, FP64 (the recursive residual
+  // of the FP32 products can drift from it)
+  for (int i = 0; i < nb; ++i) BCK(cudaMemsetAsync(S.hd[i].rr, 0, K8 * sizeof(double), s));
+  gb_resid<<<2 * S.hoff_av[nb], 256, 0, s>>>(S.d_desc, S.off.av, nb);
+  launches += 2;
   std::vector<BicgScalars> hs((size_t)nb * K8);
-  for (int i = 0; i < nb; ++i)
+  std::vector<double> hrr((size_t)nb * K8);
+  for (int i = 0; i < nb; ++i) {
     BCK(cudaMemcpyAsync(hs.data() + (size_t)i * K8, S.hd[i].bs, K8 * sizeof(BicgScalars), cudaMemcpyDeviceToHost, s));
+    BCK(cudaMemcpyAsync(hrr.data() + (size_t)i * K8, S.hd[i].rr, K8 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  }
   int hflag = 0;
   BCK(cudaMemcpyAsync(&hflag, S.errflag, sizeof(int), cudaMemcpyDeviceToHost, s));
   BCK(cudaStreamSynchronize(s));
@@ -883,7 +938,11 @@ bool batch_bicgstab_solve(const std::vector<BatchBody>& bodies, int k, double to
     for (int c = 0; c < k; ++c) {
       const BicgScalars& q = hs[(size_t)i * K8 + c];
       nit[(size_t)i * k + c] = q.its;
-      status[(size_t)i * k + c] = q.status < 0 ? 1 : q.status;
+      int stt = q.status < 0 ? 1 : q.status;
+      // converged by its recursive residual but not by the true one: 4
+      const double rel = q.bnorm > 0.0 ? std::sqrt(hrr[(size_t)i * K8 + c]) / q.bnorm : 0.0;
+      if (stt == 0 && !(rel <= tol)) stt = 4;
+      status[(size_t)i * k + c] = stt;
     }
   if (st) {
     st->av_ms += av_ms;
@@ -896,6 +955,131 @@ bool batch_bicgstab_solve(const std::vector<BatchBody>& bodies, int k, double to
       for (int c = 0; c < k; ++c) mx = std::max(mx, nit[(size_t)i * k + c]);
       st->bytes_av += 2.0 * (double)mx * 24.0 * (double)S.hd[i].pk_ne * (double)S.hd[i].pk_ne;
     }
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// True residual of many systems (FP64), for the BiCGSTAB restarts
+// ---------------------------------------------------------------------------
+struct RDesc {
+  const float* A;
+  int pk_ne, pk_ldp, m, n, k;
+  const double* b;
+  const double* x;
+  double* r;   // [k][m] or null
+  double* ss;  // [2][K8]: ||r||^2, ||b||^2 per right-hand side
+};
+
+// a warp per element row i (its three equations), lanes over the element
+// columns; CTAs of 8 rows, off[] = prefix of the CTAs per system
+__global__ void __launch_bounds__(256) gb_residual(const RDesc* __restrict__ D, const int* __restrict__ off, int nb) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  const RDesc& d = D[bi];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = (blockIdx.x - off[bi]) * 8 + warp;
+  if (i >= d.pk_ne) return;  // a whole warp; no block barrier in this kernel
+  const int ne = d.pk_ne;
+  double acc[3][K8];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < K8; ++c) acc[a][c] = 0.0;
+  for (int j = lane; j < ne; j += 32) {
+    double g6[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) g6[c] = (double)d.A[pk_idx(i, c, j, d.pk_ldp)];
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+#pragma unroll
+      for (int c = 0; c < K8; ++c) {
+        if (c >= d.k) break;
+        const double xv = d.x[(int64_t)c * d.n + (int64_t)b * ne + j];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) acc[a][c] += g6[sym6(a, b)] * xv;
+      }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < K8; ++c) {
+      double v = acc[a][c];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0 && c < d.k) {
+        const int64_t row = 3 * (int64_t)i + a;
+        const double bv = d.b[(int64_t)c * d.m + row];
+        const double r = bv - v;
+        if (d.r) d.r[(int64_t)c * d.m + row] = r;
+        atomicAdd(&d.ss[c], r * r);
+        atomicAdd(&d.ss[K8 + c], bv * bv);
+      }
+    }
+}
+
+bool batch_residual(const std::vector<BatchBody>& bodies, int k, cudaStream_t s, const std::vector<double*>& r_out,
+                    std::vector<double>& rel, std::string& err) {
+  const int nb = (int)bodies.size();
+  rel.assign((size_t)nb * k, 0.0);
+  if (nb == 0) return true;
+  std::vector<RDesc> hd(nb);
+  std::vector<int> off(nb + 1, 0);
+  RDesc* dd = nullptr;
+  int* doff = nullptr;
+  double* ss = nullptr;
+  bool ok = false;
+  std::vector<double> hss((size_t)nb * 2 * K8);
+  for (int i = 0; i < nb; ++i) {
+    const BatchBody& B = bodies[i];
+    hd[i] = RDesc{B.A, B.pk_ne, B.pk_ldp, B.m, B.n, k, B.b, B.x, r_out.empty() ? nullptr : r_out[i], nullptr};
+    off[i + 1] = off[i] + (int)cdivu(B.pk_ne, 8);
+  }
+#define RCK(x)                                                                   \
+  do {                                                                           \
+    cudaError_t e_ = (x);                                                        \
+    if (e_ != cudaSuccess) {                                                     \
+      err = std::string(#x) + ": " + cudaGetErrorString(e_);                     \
+      goto done;                                                                 \
+    }                                                                            \
+  } while (0)
+  RCK(cudaMallocAsync(&dd, nb * sizeof(RDesc), s));
+  RCK(cudaMallocAsync(&doff, (nb + 1) * sizeof(int), s));
+  RCK(cudaMallocAsync(&ss, (size_t)nb * 2 * K8 * sizeof(double), s));
+  RCK(cudaMemsetAsync(ss, 0, (size_t)nb * 2 * K8 * sizeof(double), s));
+  for (int i = 0; i < nb; ++i) hd[i].ss = ss + (size_t)i * 2 * K8;
+  RCK(cudaMemcpyAsync(dd, hd.data(), nb * sizeof(RDesc), cudaMemcpyHostToDevice, s));
+  RCK(cudaMemcpyAsync(doff, off.data(), (nb + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+  gb_residual<<<off[nb], 256, 0, s>>>(dd, doff, nb);
+  RCK(cudaGetLastError());
+  RCK(cudaMemcpyAsync(hss.data(), ss, hss.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  RCK(cudaStreamSynchronize(s));  // the host tables above must outlive their copies
+  for (int i = 0; i < nb; ++i)
+    for (int c = 0; c < k; ++c) {
+      const double rr = hss[(size_t)i * 2 * K8 + c], bb = hss[(size_t)i * 2 * K8 + K8 + c];
+      rel[(size_t)i * k + c] = bb > 0.0 ? std::sqrt(rr / bb) : 0.0;
+    }
+  ok = true;
+done:
+#undef RCK
+  if (dd) cudaFreeAsync(dd, s);
+  if (doff) cudaFreeAsync(doff, s);
+  if (ss) cudaFreeAsync(ss, s);
+  return ok;
+}
+
+__global__ void k_batch_axpy(int64_t n, const double* __restrict__ d, double* __restrict__ x) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    x[t] += d[t];
+}
+bool batch_axpy(const std::vector<BatchBody>& bodies, int k, const std::vector<double*>& d, cudaStream_t s,
+                std::string& err) {
+  for (size_t i = 0; i < bodies.size(); ++i) {
+    const int64_t n = (int64_t)k * bodies[i].n;
+    k_batch_axpy<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, s>>>(n, d[i], bodies[i].x);
+  }
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    err = std::string("batch axpy: ") + cudaGetErrorString(e);
+    return false;
   }
   return true;
 }

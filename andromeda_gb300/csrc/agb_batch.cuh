@@ -56,6 +56,15 @@ bool batch_bicgstab_solve(const std::vector<BatchBody>& bodies, int k, double to
 // launches each, CUDA events) and returns the fastest; `report` lists the
 // candidates and their times.  Results are cached per (systems, total size)
 // class for the process.
+// r = b - A x for every system (FP64 products and sums over the FP32 packed
+// blocks; A, b, x as in BatchBody), written to r_out[i] ([k][m], may be null),
+// and rel[i * k + c] = ||r|| / ||b|| per right-hand side (0 for b = 0).
+bool batch_residual(const std::vector<BatchBody>& bodies, int k, cudaStream_t s, const std::vector<double*>& r_out,
+                    std::vector<double>& rel, std::string& err);
+// x_i += d_i (k n values) for every system
+bool batch_axpy(const std::vector<BatchBody>& bodies, int k, const std::vector<double*>& d, cudaStream_t s,
+                std::string& err);
+
 bool batch_autotune(const std::vector<BatchBody>& bodies, cudaStream_t s, BatchTune& best, std::string& report,
                     std::string& err);
 

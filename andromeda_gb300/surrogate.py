@@ -31,18 +31,35 @@ def features(params):
     return np.column_stack([p, np.log(aspect)]).astype(np.float32)
 
 
-def tensor_to_targets(R):
-    """[n, 6, 6] tensors -> [n, 21] upper triangle of the symmetric part."""
+def shape_scale(params):
+    """[n, 6, 6] scale of the tensor entries: with the volume-equivalent radius
+    r = (a b c)^(1/3) (a = 1), force-velocity entries grow as r, couplings as
+    r^2, torque-rotation entries as r^3.  Dividing by it leaves O(1) targets of
+    similar size for every shape, so that the network's error is a similar
+    fraction of every body's tensor (the error measure is relative per body)."""
+    p = np.asarray(params, dtype=np.float64)
+    r = np.cbrt(p[:, 0] * p[:, 1])
+    k = np.array([0, 0, 0, 1, 1, 1])
+    return r[:, None, None] ** (1 + k[None, :, None] + k[None, None, :])
+
+
+def tensor_to_targets(R, params=None):
+    """[n, 6, 6] tensors -> [n, 21] upper triangle of the symmetric part (divided
+    by shape_scale when the shapes are given)."""
     R = np.asarray(R, dtype=np.float64)
     S = 0.5 * (R + np.swapaxes(R, 1, 2))
+    if params is not None:
+        S = S / shape_scale(params)
     return S[:, IU[0], IU[1]].astype(np.float32)
 
 
-def targets_to_tensor(y):
+def targets_to_tensor(y, params=None):
     y = np.asarray(y, dtype=np.float64)
     R = np.zeros((len(y), 6, 6))
     R[:, IU[0], IU[1]] = y
     R[:, IU[1], IU[0]] = y
+    if params is not None:
+        R = R * shape_scale(params)
     return R
 
 
@@ -165,8 +182,8 @@ class MLP:
 class Surrogate:
     """An ensemble of MLPs + training hull + BEM fallback.
 
-    The members share the training data and differ in their initial weights
-    and batch order.  A query inside the training hull is answered by the
+    The members differ in their initial weights, their batch order and the
+    random 85 % of the training tensors each one sees.  A query inside the training hull is answered by the
     members' mean when their spread (max-entry distance of the members from the
     mean, relative to the mean's largest entry) is at most ``tau``; ``tau`` is
     calibrated on held-out BEM tensors (:meth:`calibrate`) so that every
@@ -184,13 +201,17 @@ class Surrogate:
         for n in self.nets:
             n.close()
 
-    def fit(self, params, R, epochs=400, batch=512, lr=1e-3, lr_final=1e-5, seed=0):
-        """Train every member on BEM tensors R of shapes `params`; the learning
-        rate decays geometrically from lr to lr_final over four stages of the
-        epochs.  Returns (loss history of the first member, summed stats)."""
-        X = features(params)
-        Y = tensor_to_targets(R)
-        self.hull.fit(X)
+    def fit(self, params, R, epochs=400, batch=512, lr=1e-3, lr_final=1e-5, seed=0, subsample=0.85):
+        """Train every member on BEM tensors R of shapes `params` -- each on its
+        own random `subsample` of them (bagging: the members differ most where
+        the data are thin, which is where their spread should flag a query);
+        the learning rate decays geometrically from lr to lr_final over four
+        stages of the epochs.  Returns (loss history of the first member,
+        summed stats)."""
+        X_all = features(params)
+        Y_all = tensor_to_targets(R, params)
+        self.hull.fit(X_all)
+        X, Y = X_all, Y_all
         xm, xs = X.mean(axis=0), X.std(axis=0) + 1e-6
         ym = Y.mean(axis=0)
         ys = Y.std(axis=0)
@@ -199,6 +220,9 @@ class Surrogate:
         stages = 4
         for mi, net in enumerate(self.nets):
             net.set_normalization(xm, xs, ym, ys)
+            if subsample < 1.0 and len(self.nets) > 1:
+                pick = np.random.default_rng(seed + 7919 * mi).permutation(len(X_all))[:int(subsample * len(X_all))]
+                X, Y = X_all[np.sort(pick)], Y_all[np.sort(pick)]
             hist = []
             for k in range(stages):
                 e = epochs // stages + (1 if k < epochs % stages else 0)
@@ -233,7 +257,7 @@ class Surrogate:
         X = features(params)
         inside = self.hull.contains(X)
         mean, spread, _ = self.ensemble(X[inside])
-        err = rel_err(targets_to_tensor(mean), np.asarray(R)[inside])
+        err = rel_err(targets_to_tensor(mean, np.asarray(params)[inside]), np.asarray(R)[inside])
         order = np.argsort(spread)
         ok = np.cumsum(err[order] > margin * target) == 0
         nacc = int(np.sum(ok))  # a prefix of the spread-sorted held-out answers
@@ -256,7 +280,7 @@ class Surrogate:
             ok = spread <= self.tau
             idx = np.where(inside)[0]
             acc[idx[ok]] = True
-            R[idx[ok]] = targets_to_tensor(mean[ok])
+            R[idx[ok]] = targets_to_tensor(mean[ok], np.asarray(params)[idx[ok]])
         info = {"mlp_device_ms": ms, "n_mlp": int(acc.sum()), "n_bem": int((~acc).sum()),
                 "n_outside_hull": int((~inside).sum()), "n_spread_rejected": int((inside & ~acc).sum())}
         if bem and (~acc).any():

@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--cpu-solves", type=int, default=3, help="sphere: complete CPU solves of the small body")
     ap.add_argument("--c2-estimate", type=int, default=1, help="also estimate the full-size CPU solve (labelled)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lis-compare", type=int, default=3,
+                    help="sphere: timed solves of the LIS path's solver (BiCGSTAB-Jacobi, hybrid) beside the line")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--workload", default="sphere", choices=["sphere", "batch", "surrogate", "large", "laplace"],
                     help="sphere: one level-5 sphere (default); batch: the many-body superellipsoid set")
@@ -848,6 +850,30 @@ def main():
     e2e = {"value": (world / statistics.median(e2e_vals)) if e2e_vals else None, "unit": "solves/s",
            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": len(e2e_vals)}
 
+    # the LIS path's solver on the same system (SLET LIS: BiCGSTAB-Jacobi with
+    # FP64 true-residual restarts, LSQR for a system where it does not converge)
+    lis = None
+    if args.lis_compare and args.solver == "lsqr" and rank == 0:
+        C.set_solver(A.SOLVER_HYBRID)
+        ms_l, R_l, nit_l, ist_l = [], None, None, None
+        for _ in range(args.lis_compare + 1):
+            R_l, nit_l, info_l = C.resistance_tensor(A.MIXED, 1, 2, eps=args.eps)
+            ms_l.append(info_l["device_ms"])
+            ist_l = info_l["istop"]
+        C.set_solver(A.SOLVER_LSQR)
+        err_l = None
+        if os.path.exists(GOLDEN_TRUTH):
+            with open(GOLDEN_TRUTH) as f:
+                g = json.load(f)
+            if g.get("workload") == name.split(", LSQR")[0]:
+                Rt = np.array(g["R"])
+                err_l = float(np.max(np.abs(R_l - Rt)) / np.max(np.abs(Rt)))
+        ms_med = statistics.median(ms_l[1:])
+        lis = {"solver": "BiCGSTAB-Jacobi (LSQR where it does not converge), tol " + f"{args.eps:g}",
+               "solves_per_s": 1000.0 / ms_med, "ms_per_solve": ms_med, "rel_err_vs_fp64": err_l,
+               "nit": [int(v) for v in nit_l], "istop": [int(v) for v in ist_l],
+               "steps": len(ms_l) - 1, "speedup_over_lsqr": (1000.0 / ms_med) / (value / world)}
+
     # assembly roofline: k_stokes_G<float, packed>, the regular quadrature of
     # every (collocation point, element) pair of the single layer; 28 flop per
     # (pair, quadrature point), an FMA counted as 2 and the rsqrt as 1:
@@ -941,7 +967,7 @@ def main():
                 "kernel_ms": {"assemble_single_layer": kt["assemble_ms"] / max(kt["assemble_launches"], 1),
                               "rhs": kt["rhs_ms"] / max(kt["rhs_calls"], 1), "av_sweep": av_ms,
                               "atu_sweep": atu_ms},
-                "host_s": t1 - t0, "fp64_gpu": fp64}
+                "host_s": t1 - t0, "fp64_gpu": fp64, "lis_path": lis}
         print(json.dumps(line), flush=True)
     C.close()
     if dist is not None:

@@ -155,7 +155,10 @@ int agb_set_integration(agb_context* ctx, int sing_mode, int rec_depth, double n
  * needs the packed mixed system (Stokes, velocity known on every wall,
  * triangles, default integration, AGB_MIXED); other systems return
  * AGB_ERR_UNSUPPORTED from the solve.  agb_batch_resistance on this context
- * solves its bodies with BiCGSTAB too (istop as above; no autotuning). */
+ * solves its bodies with BiCGSTAB too (istop as above, with the same FP64
+ * true-residual check and restarts, batched over the bodies that need them;
+ * AGB_SOLVER_HYBRID re-solves by LSQR every body with a right-hand side that
+ * does not end at 0; no autotuning). */
 int agb_set_solver(agb_context* ctx, int solver);
 
 /* Element geometry in global element order (normal 3*nelem, area nelem,

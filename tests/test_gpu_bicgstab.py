@@ -108,12 +108,14 @@ def test_batch_bicgstab_matches_fp64(agb):
     uneven size.  Two of the four small bodies (262 and 586 elements) have
     systems so ill-conditioned that LSQR stops on its condition limit; on their
     FP32 products BiCGSTAB diverges or stagnates (status 3, stopped early) where
-    the FP64 oracle's BiCGSTAB converges.  The other two converge at tol 1e-8
-    within 1e-6 of the FP64 LSQR tensor in a fraction of LSQR's iterations, and
-    the batched tensors equal the single-system solver's."""
+    the FP64 oracle's BiCGSTAB converges.  The other two converge at tol 1e-8 --
+    their true residual checked in FP64 and the solve restarted on it where the
+    recursive residual drifted -- within 1e-6 of the FP64 LSQR tensor in a
+    fraction of LSQR's iterations, and the batched tensors equal the
+    single-system solver's."""
     meshes = _uneven_bodies()
     R, nit, istop, st = agb.batch_resistance(meshes, eps=1e-8, solver=agb.SOLVER_BICGSTAB)
-    assert st["av_launches"] > 0 and np.all(np.isin(istop, (0, 1, 2, 3)))
+    assert st["av_launches"] > 0 and np.all(np.isin(istop, (0, 1, 2, 3, 4)))
     ref = _fp64_tensors(agb, meshes)
     for i, m in enumerate(meshes):
         C = _ctx(agb, m)
