@@ -22,7 +22,7 @@ from ._lib import AgbError, load
 
 LAPLACE, STOKES = 1, 2
 FP64, MIXED, MATRIX_FREE = 0, 1, 2
-SOLVER_LSQR, SOLVER_BICGSTAB, SOLVER_HYBRID = 0, 1, 2
+SOLVER_LSQR, SOLVER_BICGSTAB, SOLVER_HYBRID, SOLVER_LSQR_BLOCK = 0, 1, 2, 3
 BC_FUNCTION, BC_FLUX, BC_CONTACT = 1, 2, 3
 # return codes of the C ABI (include/andromeda_gb300.h)
 OK, ERR_ARG, ERR_CUDA, ERR_STATE, ERR_UNSUPPORTED, ERR_NUMERIC = 0, 1, 2, 3, 4, 5

@@ -512,6 +512,14 @@ int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int r
     }
     return AGB_OK;
   }
+  c->lsqr.bj = false;
+  if (c->solver == AGB_SOLVER_LSQR_BLOCK) {
+    if (!c->lsqr.packed)
+      return fail(c, AGB_ERR_UNSUPPORTED, "the block preconditioner needs the packed mixed system (Stokes, velocity "
+                                          "known on every wall, triangles, default integration, AGB_MIXED)");
+    if (!c->lsqr.block_precon()) return fail(c, AGB_ERR_NUMERIC, "lsqr: " + c->lsqr.err);
+    c->lsqr.bj = true;
+  }
   if (!c->lsqr.solve(c->d_rhs, d_x, c->d_q, eps, maxit, nt.data(), is.data(), nullptr, 8, x0_zero))
     return fail(c, AGB_ERR_CUDA, "lsqr: " + c->lsqr.err);
   for (int r = 0; r < nrhs; ++r) {
@@ -799,8 +807,10 @@ int agb_set_integration(agb_context* c, int sing_mode, int rec_depth, double nea
 
 int agb_set_solver(agb_context* c, int solver) {
   if (!c) return fail(c, AGB_ERR_ARG, "agb_set_solver: no context");
-  if (solver != AGB_SOLVER_LSQR && solver != AGB_SOLVER_BICGSTAB && solver != AGB_SOLVER_HYBRID)
-    return fail(c, AGB_ERR_ARG, "solver must be AGB_SOLVER_LSQR, AGB_SOLVER_BICGSTAB or AGB_SOLVER_HYBRID");
+  if (solver != AGB_SOLVER_LSQR && solver != AGB_SOLVER_BICGSTAB && solver != AGB_SOLVER_HYBRID &&
+      solver != AGB_SOLVER_LSQR_BLOCK)
+    return fail(c, AGB_ERR_ARG,
+                "solver must be AGB_SOLVER_LSQR, AGB_SOLVER_BICGSTAB, AGB_SOLVER_HYBRID or AGB_SOLVER_LSQR_BLOCK");
   c->solver = solver;
   return AGB_OK;
 }
@@ -1622,7 +1632,7 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
     cudaFreeAsync(d_nm, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return bail(AGB_ERR_CUDA, "assembly of the wave");
     const auto tb = clk::now();
-    if (autotune && !tuned && c->solver == AGB_SOLVER_LSQR) {
+    if (autotune && !tuned && (c->solver == AGB_SOLVER_LSQR || c->solver == AGB_SOLVER_LSQR_BLOCK)) {
       std::string rep, err;
       if (!batch_autotune(bodies, st, tune, rep, err)) return bail(AGB_ERR_CUDA, "autotune: " + err);
       tuned = true;
@@ -1717,7 +1727,8 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
             }
         }
       }
-    } else if (!batch_lsqr_solve(bodies, 6, eps, maxit, tune, st, nv, iv, &bst, err)) {
+    } else if (!batch_lsqr_solve(bodies, 6, eps, maxit, tune, st, nv, iv, &bst, err,
+                                 c->solver == AGB_SOLVER_LSQR_BLOCK)) {
       return bail(AGB_ERR_CUDA, "solve: " + err);
     }
     const auto tc = clk::now();

@@ -247,4 +247,27 @@ __device__ __forceinline__ void bicg_end(BicgScalars& q, double rr, double rho, 
   }
 }
 
+// inverse of a 3x3 block B (FP64) into o[9], row-major, by cofactors; false
+// (and zeros) if it is singular or not finite
+__device__ __forceinline__ bool inv3(const double (&B)[3][3], double* o) {
+  const double c00 = B[1][1] * B[2][2] - B[1][2] * B[2][1], c01 = B[1][2] * B[2][0] - B[1][0] * B[2][2],
+               c02 = B[1][0] * B[2][1] - B[1][1] * B[2][0];
+  const double det = B[0][0] * c00 + B[0][1] * c01 + B[0][2] * c02;
+  if (!(det != 0.0) || !isfinite(det)) {
+    for (int k = 0; k < 9; ++k) o[k] = 0.0;
+    return false;
+  }
+  const double id = 1.0 / det;
+  o[0] = c00 * id;
+  o[1] = (B[0][2] * B[2][1] - B[0][1] * B[2][2]) * id;
+  o[2] = (B[0][1] * B[1][2] - B[0][2] * B[1][1]) * id;
+  o[3] = c01 * id;
+  o[4] = (B[0][0] * B[2][2] - B[0][2] * B[2][0]) * id;
+  o[5] = (B[0][2] * B[1][0] - B[0][0] * B[1][2]) * id;
+  o[6] = c02 * id;
+  o[7] = (B[0][1] * B[2][0] - B[0][0] * B[2][1]) * id;
+  o[8] = (B[0][0] * B[1][1] - B[0][1] * B[1][0]) * id;
+  return true;
+}
+
 }  // namespace agb

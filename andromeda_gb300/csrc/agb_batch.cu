@@ -63,6 +63,7 @@ struct GDesc {  // CUtensorMap members keep the 64-byte alignment TMA needs
   const float* A;
   double *Rb, *Rt, *Pb, *Sb, *Tb, *Xb, *dinv, *part2;
   double* rr;  // ||b - A x||^2 per right-hand side (the FP64 check after the solve)
+  double* pc9; // block-Jacobi right preconditioner of the LSQR ([ne][3][3] inverse self blocks), or null
   BicgScalars* bs;
   const LsqrScalars* sc0;
 };
@@ -198,8 +199,19 @@ __global__ void __launch_bounds__(BT) g_reduce(const GDesc* __restrict__ D, cons
   double vn = 0.0;
   if (j < d.n) {
     double z = 0.0;
-    for (int g = 0; g < d.zgroups; ++g) z += d.Zp[((int64_t)g * d.lda + j) * K8 + c];
-    z *= d.q[j];
+    if (d.pc9) {  // (A M^-1)^T u = M^-T (A^T u), the element's three components
+      const int b = (int)(j / d.pk_ne);
+      const int64_t i = j - (int64_t)b * d.pk_ne;
+      const double* mi = d.pc9 + 9 * i + 3 * b;
+      for (int bb = 0; bb < 3; ++bb) {
+        double zb = 0.0;
+        for (int g = 0; g < d.zgroups; ++g) zb += d.Zp[((int64_t)g * d.lda + (int64_t)bb * d.pk_ne + i) * K8 + c];
+        z += mi[bb] * zb;
+      }
+    } else {
+      for (int g = 0; g < d.zgroups; ++g) z += d.Zp[((int64_t)g * d.lda + j) * K8 + c];
+      z *= d.q[j];
+    }
     const double beta = d.sc[c].beta;
     if (d.sc[c].active && beta > 0.0) {
       vn = z / beta - (init ? 0.0 : beta * d.V[j * K8 + c]);
@@ -247,9 +259,11 @@ __global__ void __launch_bounds__(BT) g_update(const GDesc* __restrict__ D, cons
       } else if (init) {
         d.W[id] = 0.0; d.X[id] = 0.0;
       }
-      const int b = (int)(j / d.pk_ne);
-      const int64_t jj = j - (int64_t)b * d.pk_ne;
-      d.Vp[((int64_t)b * K8 + c) * d.pk_ldp + jj] = (float)(d.q[j] * d.V[id]);
+      if (!d.pc9) {  // with the block preconditioner g_pc_vp writes the operand
+        const int b = (int)(j / d.pk_ne);
+        const int64_t jj = j - (int64_t)b * d.pk_ne;
+        d.Vp[((int64_t)b * K8 + c) * d.pk_ldp + jj] = (float)(d.q[j] * d.V[id]);
+      }
     }
   }
   block_sumsq8(dk, d.part + (int64_t)blk * K8);
@@ -262,8 +276,50 @@ __global__ void g_finish(const GDesc* __restrict__ D) {
        t += (int64_t)gridDim.x * blockDim.x) {
     const int c = (int)(t / d.n);
     const int64_t j = t % d.n;
-    d.x[(int64_t)c * d.n + j] = d.q[j] * d.X[j * K8 + c];
+    double v;
+    if (d.pc9) {
+      const int b = (int)(j / d.pk_ne);
+      const int64_t i = j - (int64_t)b * d.pk_ne;
+      const double* mi = d.pc9 + 9 * i + 3 * b;
+      v = 0.0;
+      for (int bb = 0; bb < 3; ++bb) v += mi[bb] * d.X[((int64_t)bb * d.pk_ne + i) * K8 + c];
+    } else {
+      v = d.q[j] * d.X[j * K8 + c];
+    }
+    d.x[(int64_t)c * d.n + j] = v;
   }
+}
+
+// the sweep-1 operand of the block-preconditioned LSQR, W = M^-1 V as
+// [b][k][ldp] FP32, over the init tiles of the systems
+__global__ void __launch_bounds__(BT) g_pc_vp(const GDesc* __restrict__ D, const int* __restrict__ off, int nb,
+                                              const int* __restrict__ bact) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  if (!bact[bi]) return;
+  const GDesc& d = D[bi];
+  if (!d.pc9) return;
+  const int64_t t = (int64_t)(blockIdx.x - off[bi]) * BT + threadIdx.x;
+  const int64_t i = t / K8;
+  const int c = (int)(t % K8);
+  if (i >= d.pk_ne) return;
+  const double v0 = d.V[i * K8 + c], v1 = d.V[((int64_t)d.pk_ne + i) * K8 + c],
+               v2 = d.V[(2 * (int64_t)d.pk_ne + i) * K8 + c];
+  const double* mi = d.pc9 + 9 * i;
+#pragma unroll
+  for (int b = 0; b < 3; ++b)
+    d.Vp[((int64_t)b * K8 + c) * d.pk_ldp + i] = (float)(mi[3 * b] * v0 + mi[3 * b + 1] * v1 + mi[3 * b + 2] * v2);
+}
+
+// inverses of every system's 3x3 self blocks (FP64 from the FP32 packed
+// values); blockIdx.y = system
+__global__ void g_pc_blocks(const GDesc* __restrict__ D, int* __restrict__ bad) {
+  const GDesc& d = D[blockIdx.y];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!d.pc9 || i >= d.pk_ne) return;
+  double B[3][3];
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) B[a][b] = (double)d.A[pk_idx(i, sym6(a, b), i, d.pk_ldp)];
+  if (!inv3(B, d.pc9 + 9 * (int64_t)i)) atomicExch(bad, 1);
 }
 
 __global__ void g_fill(int* p, int n, int v) {
@@ -581,7 +637,7 @@ struct BatchSolver {
   }
 
   bool setup(const std::vector<BatchBody>& bodies, int k_, int maxit, const BatchTune& t, cudaStream_t st,
-             bool bicg = false) {
+             bool bicg = false, bool bj = false) {
     release();
     nb = (int)bodies.size();
     k = k_;
@@ -597,7 +653,7 @@ struct BatchSolver {
     // pool layout (bytes), every piece 256-byte aligned
     size_t bytes = 0;
     auto take = [&](size_t n) { const size_t o = bytes; bytes += (n + 255) / 256 * 256; return o; };
-    struct Offs { size_t Y, Ys, V, W, X, Vp, Zp, part, sc, bg, part2, bs, rr; };
+    struct Offs { size_t Y, Ys, V, W, X, Vp, Zp, part, sc, bg, part2, bs, rr, pc9; };
     std::vector<Offs> po(nb);
     const size_t o_sc0 = take(K8 * sizeof(LsqrScalars));  // zero gammas of the BiCGSTAB sweeps
     bytes_A = 0.0;
@@ -639,6 +695,7 @@ struct BatchSolver {
         po[i].bs = take(K8 * sizeof(BicgScalars));
         po[i].rr = take(K8 * sizeof(double));
       }
+      if (bj) po[i].pc9 = take((size_t)9 * B.pk_ne * sizeof(double));
       hoff_b[i + 1] = hoff_b[i] + d.nb_b;
       hoff_av[i + 1] = hoff_av[i] + d.nb_av;
       hoff_atu[i + 1] = hoff_atu[i] + d.cblocks * d.zgroups;
@@ -669,6 +726,7 @@ struct BatchSolver {
         d.bs = (BicgScalars*)(p + po[i].bs);
         d.rr = (double*)(p + po[i].rr);
       }
+      d.pc9 = bj ? (double*)(p + po[i].pc9) : nullptr;
       // the pool is zeroed: the pad columns pk_ne..pk_ldp-1 of Vp stay zero
       if (!make_tensor_map_2d(&d.tm_vp, d.Vp, d.pk_ldp, 3 * K8, AVP_BC, 3 * K8, err)) return false;
     }
@@ -698,13 +756,24 @@ struct BatchSolver {
 
 bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, int maxit, const BatchTune& tune,
                       cudaStream_t s, std::vector<int>& nit, std::vector<int>& istop, BatchStats* st,
-                      std::string& err) {
+                      std::string& err, bool bj) {
   BatchSolver S;
-  if (!S.setup(bodies, k, maxit, tune, s)) { err = S.err; return false; }
+  if (!S.setup(bodies, k, maxit, tune, s, false, bj)) { err = S.err; return false; }
   const int nb = S.nb;
   int itmax = 0;
   for (const auto& d : S.hd) itmax = std::max(itmax, d.itnlim);
   long launches = 0;
+  if (bj) {  // the inverse self blocks of every system
+    int nemax = 1;
+    for (const auto& d : S.hd) nemax = std::max(nemax, d.pk_ne);
+    BCK(cudaMemsetAsync(S.nactive, 0, sizeof(int), s));
+    g_pc_blocks<<<dim3(cdivu(nemax, 128), nb), 128, 0, s>>>(S.d_desc, S.nactive);
+    int bad = 0;
+    BCK(cudaMemcpyAsync(&bad, S.nactive, sizeof(int), cudaMemcpyDeviceToHost, s));
+    BCK(cudaStreamSynchronize(s));
+    ++launches;
+    if (bad) { err = "a singular 3x3 self block: the block preconditioner cannot be formed"; return false; }
+  }
   // initial vectors: r0 = b, beta0, tolerances; A^T r0, alpha0, W = V
   g_init_b<<<S.hoff_b[nb], BT, 0, s>>>(S.d_desc, S.off.b, nb);
   g_scalars<<<nb, 256, 0, s>>>(S.d_desc, 0, S.bact, S.nactive, eps);
@@ -712,7 +781,8 @@ bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, i
   g_reduce<<<S.hoff_red[nb], BT, 0, s>>>(S.d_desc, S.off.red, nb, S.bact, 1);
   g_scalars<<<nb, 256, 0, s>>>(S.d_desc, 1, S.bact, S.nactive, eps);
   g_update<<<S.hoff_upd[nb], BT, 0, s>>>(S.d_desc, S.off.upd, nb, S.bact, 1);
-  launches += 6;
+  if (bj) g_pc_vp<<<S.hoff_b[nb], BT, 0, s>>>(S.d_desc, S.off.b, nb, S.bact);
+  launches += bj ? 7 : 6;
   BCK(cudaGetLastError());
   const int ce = std::max(1, std::min(tune.check_every, 32));
   std::vector<cudaEvent_t> ev(4 * ce, nullptr);
@@ -728,6 +798,7 @@ bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, i
     g_reduce<<<S.hoff_red[nb], BT, 0, s>>>(S.d_desc, S.off.red, nb, S.bact, 0);
     g_scalars<<<nb, 256, 0, s>>>(S.d_desc, 3, S.bact, S.nactive, eps);
     g_update<<<S.hoff_upd[nb], BT, 0, s>>>(S.d_desc, S.off.upd, nb, S.bact, 0);
+    if (bj) g_pc_vp<<<S.hoff_b[nb], BT, 0, s>>>(S.d_desc, S.off.b, nb, S.bact);
     cudaMemsetAsync(S.nactive, 0, sizeof(int), s);
     g_scalars<<<nb, 256, 0, s>>>(S.d_desc, 4, S.bact, S.nactive, eps);
   };
@@ -766,7 +837,7 @@ bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, i
   long nav = 0, natu = 0;
   while (act > 0 && iters < (long)itmax + ce) {
     if (cudaGraphLaunch(gexec, s) != cudaSuccess) { ok = false; break; }
-    launches += 7L * ce;
+    launches += (bj ? 8L : 7L) * ce;
     cudaMemcpyAsync(S.h_nactive, S.nactive, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) { ok = false; break; }
     for (int i = 0; i < ce; ++i) {

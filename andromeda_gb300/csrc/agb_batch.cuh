@@ -42,7 +42,7 @@ struct BatchStats {
 // itnlim = maxit or 10(m+n+50)); nit/istop receive k entries per system.
 bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, int maxit, const BatchTune& tune,
                       cudaStream_t s, std::vector<int>& nit, std::vector<int>& istop, BatchStats* st,
-                      std::string& err);
+                      std::string& err, bool bj = false);
 
 // BiCGSTAB with the Jacobi preconditioner (the solver of the reference's LIS path,
 // as DenseLsqr::bicgstab) on all systems together: x0 = 0, stop at

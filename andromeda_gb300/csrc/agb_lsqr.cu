@@ -577,7 +577,8 @@ __global__ void k_colsqp(const float* __restrict__ Ap, int ne, int ldp, int rows
 // On the initial call (init=1) the old V is taken as zero.
 __global__ void k_atu_reduce(const double* __restrict__ Zp, int groups, int64_t lda, int n, const LsqrScalars* sc,
                              int init, double* __restrict__ V, double* __restrict__ part,
-                             const double* __restrict__ qs = nullptr) {
+                             const double* __restrict__ qs = nullptr, const double* __restrict__ pc9 = nullptr,
+                             int pk_ne = 0) {
   __shared__ double sP[kThreads / 32][K8];
   const int64_t t = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   const int64_t j = t / K8;
@@ -585,8 +586,21 @@ __global__ void k_atu_reduce(const double* __restrict__ Zp, int groups, int64_t 
   double vn = 0.0;
   if (j < n) {
     double z = 0.0;
-    for (int g = 0; g < groups; ++g) z += Zp[((int64_t)g * lda + j) * K8 + c];
-    if (qs) z *= qs[j];  // column scaling applied on the fly (packed layout)
+    if (pc9) {
+      // block-Jacobi right preconditioner: (A M^-1)^T u = M^-T (A^T u) with the
+      // element's symmetric 3x3 inverse self block, over its three components
+      const int b = (int)(j / pk_ne);
+      const int64_t i = j - (int64_t)b * pk_ne;
+      const double* mi = pc9 + 9 * i + 3 * b;
+      for (int bb = 0; bb < 3; ++bb) {
+        double zb = 0.0;
+        for (int g = 0; g < groups; ++g) zb += Zp[((int64_t)g * lda + (int64_t)bb * pk_ne + i) * K8 + c];
+        z += mi[bb] * zb;
+      }
+    } else {
+      for (int g = 0; g < groups; ++g) z += Zp[((int64_t)g * lda + j) * K8 + c];
+      if (qs) z *= qs[j];  // column scaling applied on the fly (packed layout)
+    }
     const double beta = sc[c].beta;
     if (sc[c].active && beta > 0.0) {
       vn = z / beta - (init ? 0.0 : beta * V[j * K8 + c]);
@@ -616,7 +630,7 @@ template <typename T>
 __global__ void k_update(int n, int64_t lda, const LsqrScalars* sc, int init, double* __restrict__ V,
                          double* __restrict__ W, double* __restrict__ X, T* __restrict__ Vs, double* __restrict__ part,
                          int vs_rhs_major, float* __restrict__ Vp = nullptr, int pk_ne = 0, int pk_ldp = 0,
-                         const double* __restrict__ qs = nullptr) {
+                         const double* __restrict__ qs = nullptr, int vp_later = 0) {
   __shared__ double sP[kThreads / 32][K8];
   const int64_t t = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   const int64_t j = t / K8;
@@ -644,7 +658,10 @@ __global__ void k_update(int n, int64_t lda, const LsqrScalars* sc, int init, do
       } else if (init) {
         W[id] = 0.0; X[id] = 0.0;
       }
-      if (Vp) {  // packed layout: W = q.V as [b][k][ldp]
+      if (vp_later) {
+        // the block-preconditioned operand is written by k_pc_vp (it mixes the
+        // three components of an element, which other threads update here)
+      } else if (Vp) {  // packed layout: W = q.V as [b][k][ldp]
         const int b = (int)(j / pk_ne);
         const int64_t jj = j - (int64_t)b * pk_ne;
         Vp[((int64_t)b * K8 + c) * pk_ldp + jj] = (float)(qs[j] * V[id]);
@@ -759,14 +776,50 @@ __global__ void k_pack(const double* __restrict__ src, int rows, int k, int64_t 
   }
   dst[t] = v;
 }
-// x_out(:,c) = q .* X(:,c) + x0(:,c)
+// x_out(:,c) = q .* X(:,c) + x0(:,c), or M^-1 X(:,c) + x0(:,c) with the block-Jacobi preconditioner
 __global__ void k_finish_x(const double* __restrict__ X, const double* __restrict__ q, const double* __restrict__ X0,
-                           int n, int k, const LsqrScalars* sc, double* __restrict__ xout) {
+                           int n, int k, const LsqrScalars* sc, double* __restrict__ xout,
+                           const double* __restrict__ pc9 = nullptr, int pk_ne = 0) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)n * k) return;
   const int c = (int)(t / n);
   const int64_t j = t % n;
-  xout[(int64_t)c * n + j] = q[j] * X[j * K8 + c] + X0[j * K8 + c];
+  double v;
+  if (pc9) {
+    const int b = (int)(j / pk_ne);
+    const int64_t i = j - (int64_t)b * pk_ne;
+    const double* mi = pc9 + 9 * i + 3 * b;
+    v = 0.0;
+    for (int bb = 0; bb < 3; ++bb) v += mi[bb] * X[((int64_t)bb * pk_ne + i) * K8 + c];
+  } else {
+    v = q[j] * X[j * K8 + c];
+  }
+  xout[(int64_t)c * n + j] = v + X0[j * K8 + c];
+}
+// the sweep-1 operand of the block-preconditioned packed LSQR: W = M^-1 V as
+// [b][k][ldp] FP32 (M = the elements' 3x3 self blocks)
+__global__ void k_pc_vp(int pk_ne, int pk_ldp, const double* __restrict__ V, const double* __restrict__ pc9,
+                        float* __restrict__ Vp) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)pk_ne * K8) return;
+  const int64_t i = t / K8;
+  const int c = (int)(t % K8);
+  const double v0 = V[i * K8 + c], v1 = V[((int64_t)pk_ne + i) * K8 + c], v2 = V[(2 * (int64_t)pk_ne + i) * K8 + c];
+  const double* mi = pc9 + 9 * i;
+#pragma unroll
+  for (int b = 0; b < 3; ++b)
+    Vp[((int64_t)b * K8 + c) * pk_ldp + i] = (float)(mi[3 * b] * v0 + mi[3 * b + 1] * v1 + mi[3 * b + 2] * v2);
+}
+// inverses of the elements' 3x3 self blocks of the packed matrix (FP64 from the
+// stored FP32 values); bad = 1 for a singular or non-finite block
+__global__ void k_pc_blocks(int pk_ne, int pk_ldp, const float* __restrict__ Ap, double* __restrict__ pc9,
+                            int* __restrict__ bad) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= pk_ne) return;
+  double B[3][3];
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) B[a][b] = (double)Ap[pk_idx(i, sym6(a, b), i, pk_ldp)];
+  if (!inv3(B, pc9 + 9 * (int64_t)i)) atomicExch(bad, 1);
 }
 __global__ void k_sumsq_rows(const double* __restrict__ B, int rows, double* __restrict__ part) {
   __shared__ double sP[kThreads / 32][K8];
@@ -960,7 +1013,10 @@ void DenseLsqr::release() {
   pev_ready = false;
   cudaFree(Y); cudaFree(V); cudaFree(W); cudaFree(X); cudaFree(Z); cudaFree(Ys); cudaFree(Vs);
   cudaFree(part); cudaFree(Zp); cudaFree(sc); cudaFree(nactive); cudaFree(XsD); cudaFree(errflag); cudaFree(Yp); cudaFree(Vp);
-  cudaFree(bg); cudaFree(bg_part); cudaFree(bsc); cudaFree(sc0);
+  cudaFree(bg); cudaFree(bg_part); cudaFree(bsc); cudaFree(sc0); cudaFree(pc9);
+  pc9 = nullptr;
+  pc9_ready = false;
+  bj = false;
   bg = bg_part = nullptr;
   bsc = nullptr;
   sc0 = nullptr;
@@ -1124,6 +1180,8 @@ __global__ void k_init_y(const double* __restrict__ Bp, int64_t count, double* _
 bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, double eps, int maxit, int* nit_host,
                       int* istop_host, double* rnorm_host, int check_every, bool x0_zero) {
   if (maxit == 0) maxit = 10 * (m + n + 50);
+  const bool use_bj = bj && packed && fp32 && pc9 && pc9_ready;
+  if (bj && !use_bj) { err = "the block preconditioner needs the packed mixed matrix"; return false; }
   const int64_t mpad = ((int64_t)m + 255) / 256 * 256;
   const unsigned nb_av = packed ? cdiv(pk_ne, 8) : cdiv(m, AV_ROWS);  // residual sweep
   const unsigned nb_av2 = packed ? cdiv(pk_ne, AVP_R) : mf ? cdiv((int64_t)m * K8, 256)
@@ -1162,12 +1220,14 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
   // A^T r, alpha0, w = v
   if (fp32) launch_atu<float>(*this); else launch_atu<double>(*this);
   const double* qs = packed ? q_dev : nullptr;
-  k_atu_reduce<<<nb_red, kThreads, 0, stream>>>(Zp, zgroups, lda, n, sc, 1, V, part, qs);
+  k_atu_reduce<<<nb_red, kThreads, 0, stream>>>(Zp, zgroups, lda, n, sc, 1, V, part, qs, use_bj ? pc9 : nullptr,
+                                               pk_ne);
   k_scalars<<<1, SCAL_THREADS, 0, stream>>>(sc, k, 1, part, nb_red, nactive);
   if (fp32) k_update<float><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 1, V, W, X, (float*)Vs, part, 1, Vp, pk_ne,
-                                                              pk_ldp, qs);
+                                                              pk_ldp, qs, use_bj ? 1 : 0);
   else k_update<double><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 1, V, W, X, (double*)Vs, part, 1);
-  launches += x0_zero ? 10 : 11;
+  if (use_bj) k_pc_vp<<<cdiv((int64_t)pk_ne * K8, 256), 256, 0, stream>>>(pk_ne, pk_ldp, V, pc9, Vp);
+  launches += (x0_zero ? 10 : 11) + (use_bj ? 1 : 0);
   CK(cudaGetLastError());
 
   if (check_every > 32) check_every = 32;
@@ -1188,11 +1248,13 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
     if (timed) cudaEventRecordWithFlags(pev[2], stream, cudaEventRecordExternal);
     if (fp32) launch_atu<float>(*this); else launch_atu<double>(*this);
     if (timed) cudaEventRecordWithFlags(pev[3], stream, cudaEventRecordExternal);
-    k_atu_reduce<<<nb_red, kThreads, 0, stream>>>(Zp, zgroups, lda, n, sc, 0, V, part, qs);
+    k_atu_reduce<<<nb_red, kThreads, 0, stream>>>(Zp, zgroups, lda, n, sc, 0, V, part, qs, use_bj ? pc9 : nullptr,
+                                                 pk_ne);
     k_scalars<<<1, SCAL_THREADS, 0, stream>>>(sc, k, 3, part, nb_red, nactive);
     if (fp32) k_update<float><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 0, V, W, X, (float*)Vs, part, 1, Vp, pk_ne,
-                                                                pk_ldp, qs);
+                                                                pk_ldp, qs, use_bj ? 1 : 0);
     else k_update<double><<<nb_upd, kThreads, 0, stream>>>(n, lda, sc, 0, V, W, X, (double*)Vs, part, 1);
+    if (use_bj) k_pc_vp<<<cdiv((int64_t)pk_ne * K8, 256), 256, 0, stream>>>(pk_ne, pk_ldp, V, pc9, Vp);
     k_scalars<<<1, SCAL_THREADS, 0, stream>>>(sc, k, 4, part, nb_upd, nactive);  // phase 3 zeroed nactive
   };
   // capture check_every iterations in one graph
@@ -1211,7 +1273,7 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
   int iters = 0;
   while (act > 0 && iters < maxit + check_every) {
     CK(cudaGraphLaunch(gexec, stream));
-    launches += 7L * check_every;
+    launches += (use_bj ? 8L : 7L) * check_every;
     CK(cudaMemcpyAsync(h_nactive, nactive, sizeof(int), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
     {
@@ -1226,7 +1288,8 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
   cudaGraphExecDestroy(gexec);
   cudaGraphDestroy(graph);
   // x = q .* dx + x0
-  k_finish_x<<<cdiv((int64_t)n * k, 256), 256, 0, stream>>>(X, q_dev, Bp, n, k, sc, x_dev);
+  k_finish_x<<<cdiv((int64_t)n * k, 256), 256, 0, stream>>>(X, q_dev, Bp, n, k, sc, x_dev, use_bj ? pc9 : nullptr,
+                                                             pk_ne);
   launches += 1;
   CK(cudaMemcpyAsync(hs, sc, sizeof(hs), cudaMemcpyDeviceToHost, stream));
   CK(cudaStreamSynchronize(stream));
@@ -1239,6 +1302,22 @@ bool DenseLsqr::solve(const double* b_dev, double* x_dev, const double* q_dev, d
     if (istop_host) istop_host[c] = hs[c].istop;
     if (rnorm_host) rnorm_host[c] = hs[c].rnorm;
   }
+  return true;
+}
+
+bool DenseLsqr::block_precon() {
+  if (!packed || !A) { err = "the block preconditioner needs the packed mixed matrix"; return false; }
+  if (pc9_ready) return true;
+  if (!pc9) CK(cudaMalloc(&pc9, (size_t)pk_ne * 9 * sizeof(double)));
+  CK(cudaMemsetAsync(nactive, 0, sizeof(int), stream));
+  k_pc_blocks<<<cdiv(pk_ne, 128), 128, 0, stream>>>(pk_ne, pk_ldp, (const float*)A, pc9, nactive);
+  CK(cudaGetLastError());
+  int bad = 0;
+  CK(cudaMemcpyAsync(&bad, nactive, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  CK(cudaStreamSynchronize(stream));
+  ++launches;
+  if (bad) { err = "a singular 3x3 self block: the block preconditioner cannot be formed"; return false; }
+  pc9_ready = true;
   return true;
 }
 

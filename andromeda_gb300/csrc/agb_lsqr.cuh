@@ -71,6 +71,11 @@ struct DenseLsqr {
   float* Yp = nullptr;          // [col blocks][m][8] partial products of A V
   int mf_cb = 0;
   const double* mf_q = nullptr; // column scales applied on the fly
+  // block-Jacobi right preconditioner of the packed LSQR (bj): the inverses of
+  // the elements' 3x3 self blocks [ne][3][3], in place of the column scales q
+  double* pc9 = nullptr;
+  bool bj = false;
+  bool pc9_ready = false;  // computed for the current matrix
   // BiCGSTAB work (bicgstab): R, Rt, P, S, T, X ([m][8] each) and 1/diag(A) [m]
   double* bg = nullptr;
   double* bg_part = nullptr;    // per-CTA partial sums
@@ -101,6 +106,8 @@ struct DenseLsqr {
   // 1 iteration limit, 2 breakdown.
   bool bicgstab(const double* b_dev, double* x_dev, double tol, int maxit, int* nit_host, int* status_host,
                 double* relres_host = nullptr);
+  // inverses of the packed matrix's 3x3 self blocks into pc9 (once per matrix)
+  bool block_precon();
   // r = b - A (x ./ q) with FP64 accumulation (refinement residual).
   bool residual(const double* b_dev, const double* x_dev, const double* q_dev, double* r_dev);
   void release();

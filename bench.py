@@ -44,9 +44,10 @@ def parse():
     ap.add_argument("--outer-level", type=int, default=2)
     ap.add_argument("--outer-radius", type=float, default=200.0)
     ap.add_argument("--eps", type=float, default=1e-7)
-    ap.add_argument("--solver", default="lsqr", choices=["lsqr", "bicgstab", "hybrid"],
+    ap.add_argument("--solver", default="lsqr", choices=["lsqr", "lsqr_block", "bicgstab", "hybrid"],
                     help="sphere, batch, large: LSQR (lsqr_solve, the default), BiCGSTAB-Jacobi (the LIS path's "
-                         "solver), or hybrid (BiCGSTAB, LSQR for the systems where it does not converge)")
+                         "solver), hybrid (BiCGSTAB, LSQR for the systems where it does not converge), or lsqr_block "
+                         "(LSQR with the 3x3 self-block right preconditioner)")
     ap.add_argument("--fp64", default="full", choices=["full", "off"],
                     help="sphere: the plain FP64 GPU comparator solved to convergence at the same eps (full)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the full-size CPU estimate's sample")
@@ -89,11 +90,13 @@ def parse():
 
 
 def solver_id(A, name):
-    return {"lsqr": A.SOLVER_LSQR, "bicgstab": A.SOLVER_BICGSTAB, "hybrid": A.SOLVER_HYBRID}[name]
+    return {"lsqr": A.SOLVER_LSQR, "bicgstab": A.SOLVER_BICGSTAB, "hybrid": A.SOLVER_HYBRID,
+            "lsqr_block": A.SOLVER_LSQR_BLOCK}[name]
 
 
 def solver_text(name, eps):
-    return {"lsqr": f"LSQR eps {eps:g}", "bicgstab": f"BiCGSTAB-Jacobi tol {eps:g}",
+    return {"lsqr": f"LSQR eps {eps:g}", "lsqr_block": f"LSQR (3x3 self-block preconditioner) eps {eps:g}",
+            "bicgstab": f"BiCGSTAB-Jacobi tol {eps:g}",
             "hybrid": f"BiCGSTAB-Jacobi tol {eps:g}, LSQR eps {eps:g} where it does not converge"}[name]
 
 

@@ -77,6 +77,11 @@ typedef struct agb_context agb_context;
                                  the reference's default iteration limit) for every right-hand
                                  side of a system whose BiCGSTAB did not converge on all of them
                                  (no counterpart in the reference) */
+#define AGB_SOLVER_LSQR_BLOCK 3 /* LSQR (lsqr_solve's recurrence and stopping tests) on A M^-1
+                                   with M the elements' 3x3 self blocks (block-Jacobi right
+                                   preconditioner) in place of lsqr_precon's column scaling;
+                                   packed mixed system only, also in agb_batch_resistance
+                                   (no counterpart in the reference) */
 
 /* boundary-condition types (mod_mesh.f90:110) */
 #define AGB_BC_FUNCTION 1
