@@ -1474,8 +1474,10 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
   auto solver_bytes = [&](int i) {
     const BatchSlot& b = slots[i];
     const double mpad = std::ceil(b.m / 256.0) * 256.0;
-    const double bicg = (c->solver != AGB_SOLVER_LSQR) ? mpad * 8 * 8 * 7.0 + mpad * 8 : 0.0;
-    return mpad * 8 * 12.0 + (double)b.lda * 8 * (8 * 3 + 4 + 8 * 8) + 65536.0 + bicg;
+    const bool bicg_used = c->solver == AGB_SOLVER_BICGSTAB || c->solver == AGB_SOLVER_HYBRID;
+    const double bicg = bicg_used ? mpad * 8 * 8 * 7.0 + mpad * 8 : 0.0;
+    const double pc9 = (c->solver == AGB_SOLVER_LSQR_BLOCK) ? 72.0 * b.ne : 0.0;
+    return mpad * 8 * 12.0 + (double)b.lda * 8 * (8 * 3 + 4 + 8 * 8) + 65536.0 + bicg + pc9;
   };
   double budget = mem_gb * 1e9;
   if (budget <= 0.0) {
@@ -1639,7 +1641,7 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
     }
     std::vector<int> nv, iv;
     std::string err;
-    if (c->solver != AGB_SOLVER_LSQR) {
+    if (c->solver == AGB_SOLVER_BICGSTAB || c->solver == AGB_SOLVER_HYBRID) {
       if (!batch_bicgstab_solve(bodies, 6, eps, maxit, st, nv, iv, &bst, err)) return bail(AGB_ERR_CUDA, "solve: " + err);
       // FP64 refinement of the bodies whose recursive residual converged but whose
       // true residual did not (istop 4): BiCGSTAB on r = b - A x from zero to
@@ -1648,12 +1650,9 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
         std::vector<BatchBody> redo;
         std::vector<size_t> where;
         for (size_t t = 0; t < bodies.size(); ++t) {
-          bool any4 = false, other = false;
-          for (int r = 0; r < 6; ++r) {
-            any4 = any4 || iv[6 * t + r] == 4;
-            other = other || (iv[6 * t + r] != 0 && iv[6 * t + r] != 4);
-          }
-          if (any4 && !other) {
+          bool any4 = false;
+          for (int r = 0; r < 6; ++r) any4 = any4 || iv[6 * t + r] == 4;
+          if (any4) {
             redo.push_back(bodies[t]);
             where.push_back(t);
           }
@@ -1675,22 +1674,35 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
           free_bufs();
           return bail(AGB_ERR_CUDA, "restart residual: " + (okb ? err : std::string("allocation")));
         }
+        // each correction to its own column's tolerance eps ||b|| / ||r||: one
+        // tolerance for all would push the columns nearly done below the FP32
+        // rounding of the products, where BiCGSTAB stagnates
         double worst = 0.0;
+        std::vector<double> tolc(6 * redo.size(), 0.5);
         for (size_t u = 0; u < redo.size(); ++u)
           for (int r = 0; r < 6; ++r) {
             const double v = rel[6 * u + r];
-            if (v > eps) worst = std::max(worst, v);
-            else if (cudaMemsetAsync(rbuf[u] + (size_t)r * redo[u].m, 0, (size_t)redo[u].m * sizeof(double), st) !=
-                     cudaSuccess) okb = false;  // done: no correction
+            if (v > eps && iv[6 * where[u] + r] == 4) {
+              worst = std::max(worst, v);
+              tolc[6 * u + r] = std::min(0.5, eps / v);
+            } else if (cudaMemsetAsync(rbuf[u] + (size_t)r * redo[u].m, 0, (size_t)redo[u].m * sizeof(double), st) !=
+                     cudaSuccess) okb = false;  // done, or failed otherwise: no correction
           }
         std::vector<BatchBody> corr = redo;
         for (size_t u = 0; u < redo.size(); ++u) {
           corr[u].b = rbuf[u];
           corr[u].x = dbuf[u];
         }
+        if (okb && worst <= 0.0) {  // the true residuals are within eps already
+          free_bufs();
+          for (size_t u = 0; u < redo.size(); ++u)
+            for (int r = 0; r < 6; ++r)
+              if (iv[6 * where[u] + r] == 4) iv[6 * where[u] + r] = 0;
+          break;
+        }
         std::vector<int> n2, i2;
-        if (!okb || worst <= 0.0 ||
-            !batch_bicgstab_solve(corr, 6, std::min(0.5, eps / worst), maxit, st, n2, i2, &bst, err) ||
+        if (!okb ||
+            !batch_bicgstab_solve(corr, 6, std::min(0.5, eps / worst), maxit, st, n2, i2, &bst, err, &tolc) ||
             !batch_axpy(redo, 6, dbuf, st, err) || !batch_residual(redo, 6, st, {}, rel, err)) {
           free_bufs();
           return bail(AGB_ERR_CUDA, "restart: " + err);

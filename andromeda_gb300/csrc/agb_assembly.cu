@@ -214,15 +214,8 @@ __global__ void __launch_bounds__(StkTile<T>::NW * 32) k_stokes_G(int ne, int Q,
         acc[r][3] += ax * rz;
         acc[r][4] += ay * ry;
         acc[r][5] += ay * rz;
-        // FP32: the zz sum follows from the trace, sum w rz^2/r^3 = sum w/r -
-        // (xx + yy), two instructions fewer per (source, point) in this
-        // issue-bound loop; the FP64 kernel sums it directly
-        if constexpr (sizeof(T) != 4) acc[r][6] += (wi3 * rz) * rz;
+        acc[r][6] += (wi3 * rz) * rz;
       }
-    }
-    if constexpr (sizeof(T) == 4) {
-#pragma unroll
-      for (int r = 0; r < RS; ++r) acc[r][6] = acc[r][0] - acc[r][1] - acc[r][4];
     }
     if (j < ne) {
 #pragma unroll

@@ -63,6 +63,7 @@ struct GDesc {  // CUtensorMap members keep the 64-byte alignment TMA needs
   const float* A;
   double *Rb, *Rt, *Pb, *Sb, *Tb, *Xb, *dinv, *part2;
   double* rr;  // ||b - A x||^2 per right-hand side (the FP64 check after the solve)
+  double* tolc;  // per right-hand side tolerances [K8] (BiCGSTAB restarts), or null: the launch's tol
   double* pc9; // block-Jacobi right preconditioner of the LSQR ([ne][3][3] inverse self blocks), or null
   BicgScalars* bs;
   const LsqrScalars* sc0;
@@ -413,6 +414,7 @@ __global__ void __launch_bounds__(256) gb_scal(const GDesc* __restrict__ D, int 
   if (c < K8) {
     BicgScalars& q = d.bs[c];
     const double s0 = ssum[0][c], s1 = ssum[1][c];
+    if (d.tolc) tol = d.tolc[c];
     if (phase == 0) {
       bicg_start(q, s0, c < d.k);
     } else if (q.active) {
@@ -616,6 +618,7 @@ struct BatchSolver {
   BatchTune tune;
   cudaStream_t s = 0;
   std::vector<GDesc> hd;
+  std::vector<double*> tolc_dev;  // per-column tolerance pieces of the pool (BiCGSTAB)
   std::vector<int> hoff_b, hoff_av, hoff_atu, hoff_red, hoff_upd;
   GDesc* d_desc = nullptr;
   int* d_off = nullptr;  // 5 tables of nb+1
@@ -648,12 +651,13 @@ struct BatchSolver {
     BCK(set_smem(g_avp, AVP_SMEM));
     BCK(set_smem(g_atup, ATUP_SMEM));
     hd.assign(nb, GDesc{});
+    tolc_dev.assign(nb, nullptr);
     hoff_b.assign(nb + 1, 0); hoff_av.assign(nb + 1, 0); hoff_atu.assign(nb + 1, 0);
     hoff_red.assign(nb + 1, 0); hoff_upd.assign(nb + 1, 0);
     // pool layout (bytes), every piece 256-byte aligned
     size_t bytes = 0;
     auto take = [&](size_t n) { const size_t o = bytes; bytes += (n + 255) / 256 * 256; return o; };
-    struct Offs { size_t Y, Ys, V, W, X, Vp, Zp, part, sc, bg, part2, bs, rr, pc9; };
+    struct Offs { size_t Y, Ys, V, W, X, Vp, Zp, part, sc, bg, part2, bs, rr, tolc, pc9; };
     std::vector<Offs> po(nb);
     const size_t o_sc0 = take(K8 * sizeof(LsqrScalars));  // zero gammas of the BiCGSTAB sweeps
     bytes_A = 0.0;
@@ -694,6 +698,7 @@ struct BatchSolver {
         po[i].part2 = take((size_t)nbmax * K8 * sizeof(double));
         po[i].bs = take(K8 * sizeof(BicgScalars));
         po[i].rr = take(K8 * sizeof(double));
+        po[i].tolc = take(K8 * sizeof(double));
       }
       if (bj) po[i].pc9 = take((size_t)9 * B.pk_ne * sizeof(double));
       hoff_b[i + 1] = hoff_b[i] + d.nb_b;
@@ -725,6 +730,8 @@ struct BatchSolver {
         d.part2 = (double*)(p + po[i].part2);
         d.bs = (BicgScalars*)(p + po[i].bs);
         d.rr = (double*)(p + po[i].rr);
+        d.tolc = nullptr;  // set by batch_bicgstab_solve when it is given per-column tolerances
+        tolc_dev[i] = (double*)(p + po[i].tolc);
       }
       d.pc9 = bj ? (double*)(p + po[i].pc9) : nullptr;
       // the pool is zeroed: the pad columns pk_ne..pk_ldp-1 of Vp stay zero
@@ -891,11 +898,24 @@ bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, i
 }
 
 bool batch_bicgstab_solve(const std::vector<BatchBody>& bodies, int k, double tol, int maxit, cudaStream_t s,
-                          std::vector<int>& nit, std::vector<int>& status, BatchStats* st, std::string& err) {
+                          std::vector<int>& nit, std::vector<int>& status, BatchStats* st, std::string& err,
+                          const std::vector<double>* tol_cols) {
   BatchSolver S;
   if (!S.setup(bodies, k, maxit, BatchTune(), s, true)) { err = S.err; return false; }
   BCK(set_smem(gb_avp, AVP_SMEM));
   const int nb = S.nb;
+  std::vector<double> htol;
+  if (tol_cols) {
+    if (tol_cols->size() != (size_t)nb * k) { err = "tol_cols must hold one tolerance per right-hand side"; return false; }
+    htol.assign((size_t)nb * K8, tol);
+    for (int i = 0; i < nb; ++i)
+      for (int c = 0; c < k; ++c) htol[(size_t)i * K8 + c] = (*tol_cols)[(size_t)i * k + c];
+    for (int i = 0; i < nb; ++i) {
+      BCK(cudaMemcpyAsync(S.tolc_dev[i], htol.data() + (size_t)i * K8, K8 * sizeof(double), cudaMemcpyHostToDevice, s));
+      S.hd[i].tolc = S.tolc_dev[i];
+    }
+    BCK(cudaMemcpyAsync(S.d_desc, S.hd.data(), nb * sizeof(GDesc), cudaMemcpyHostToDevice, s));
+  }
   int itmax = 0;
   for (const auto& d : S.hd) itmax = std::max(itmax, d.itnlim);
   long launches = 0;
@@ -1012,7 +1032,7 @@ bool batch_bicgstab_solve(const std::vector<BatchBody>& bodies, int k, double to
       int stt = q.status < 0 ? 1 : q.status;
       // converged by its recursive residual but not by the true one: 4
       const double rel = q.bnorm > 0.0 ? std::sqrt(hrr[(size_t)i * K8 + c]) / q.bnorm : 0.0;
-      if (stt == 0 && !(rel <= tol)) stt = 4;
+      if (stt == 0 && !(rel <= (tol_cols ? htol[(size_t)i * K8 + c] : tol))) stt = 4;
       status[(size_t)i * k + c] = stt;
     }
   if (st) {

@@ -48,9 +48,14 @@ bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, i
 // as DenseLsqr::bicgstab) on all systems together: x0 = 0, stop at
 // ||b - A x|| <= tol ||b|| or maxit iterations (0: 1000).  b: [k][m] in the row
 // numbering 3i+a; x: [k][n] in the unknown numbering a ne + i (as
-// batch_lsqr_solve).  status per column: 0 converged, 1 iteration limit, 2 breakdown.
+// batch_lsqr_solve).  status per column: 0 converged, 1 iteration limit, 2
+// breakdown, 3 diverged or stagnated, 4 converged by the recursive residual but
+// not by the FP64 true residual.  tol_cols (null, or [nb][k]): a tolerance per
+// right-hand side in place of tol (the restarts on the true residual solve each
+// correction to its own column's tolerance).
 bool batch_bicgstab_solve(const std::vector<BatchBody>& bodies, int k, double tol, int maxit, cudaStream_t s,
-                          std::vector<int>& nit, std::vector<int>& status, BatchStats* st, std::string& err);
+                          std::vector<int>& nit, std::vector<int>& status, BatchStats* st, std::string& err,
+                          const std::vector<double>* tol_cols = nullptr);
 
 // Times the candidate row groups of the A^T*U sweep on these systems (a few
 // launches each, CUDA events) and returns the fastest; `report` lists the

@@ -72,12 +72,9 @@ __device__ __forceinline__ void mf_blocks(const QPt<float>* __restrict__ sp, int
       acc[r][3] += ax * rz;
       acc[r][4] += ay * ry;
       acc[r][5] += ay * rz;
+      acc[r][6] += (wi3 * rz) * rz;
     }
   }
-  // the zz sum from the trace: sum w rz^2/r^3 = sum w/r - (xx + yy), as the
-  // FP32 assembly computes it
-#pragma unroll
-  for (int r = 0; r < MF_RS; ++r) acc[r][6] = acc[r][0] - acc[r][1] - acc[r][4];
 }
 
 __device__ __forceinline__ void mf_sym(const float (&a)[7], float scale, float (&g)[6]) {
