@@ -22,7 +22,7 @@ from ._lib import AgbError, load
 
 LAPLACE, STOKES = 1, 2
 FP64, MIXED, MATRIX_FREE = 0, 1, 2
-SOLVER_LSQR, SOLVER_BICGSTAB, SOLVER_HYBRID, SOLVER_LSQR_BLOCK = 0, 1, 2, 3
+SOLVER_LSQR, SOLVER_BICGSTAB, SOLVER_HYBRID, SOLVER_LSQR_BLOCK, SOLVER_GMRES = 0, 1, 2, 3, 4
 BC_FUNCTION, BC_FLUX, BC_CONTACT = 1, 2, 3
 # return codes of the C ABI (include/andromeda_gb300.h)
 OK, ERR_ARG, ERR_CUDA, ERR_STATE, ERR_UNSUPPORTED, ERR_NUMERIC = 0, 1, 2, 3, 4, 5
@@ -131,10 +131,16 @@ class Context:
         self._ck(self._L.agb_set_integration(self.h, int(sing_mode), int(rec_depth), float(near_eta),
                                              int(near_depth)))
 
-    def set_solver(self, solver):
-        """SOLVER_LSQR (default, lsqr_solve) or SOLVER_BICGSTAB (the LIS path's
-        BiCGSTAB with the Jacobi preconditioner; packed mixed Stokes systems)."""
+    def set_solver(self, solver, restart=None):
+        """SOLVER_LSQR (default, lsqr_solve), SOLVER_LSQR_BLOCK (LSQR with the
+        3x3 self-block preconditioner), SOLVER_BICGSTAB (the LIS path's BiCGSTAB
+        with the Jacobi preconditioner), SOLVER_HYBRID (BiCGSTAB, LSQR where it
+        does not converge) or SOLVER_GMRES (the LIS path with "-i gmres";
+        restart: its restart length, default 40).  All but SOLVER_LSQR take
+        packed mixed Stokes systems only."""
         self._ck(self._L.agb_set_solver(self.h, int(solver)))
+        if restart is not None:
+            self._ck(self._L.agb_set_gmres_restart(self.h, int(restart)))
 
     def surface_pressure(self, u, q):
         """Pressure at the element centroids (pressureStokes) of velocity u (3, nnodes)

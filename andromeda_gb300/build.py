@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libandromeda_gb300.so")
 SOURCES = ["agb_api.cu", "agb_assembly.cu", "agb_lsqr.cu", "agb_noalloc.cu", "agb_general.cu", "agb_batch.cu",
-           "agb_lu.cu", "agb_mlp.cu", "agb_mfree.cu", "agb_bicg.cu", "agb_selftest.cu",
+           "agb_lu.cu", "agb_mlp.cu", "agb_mfree.cu", "agb_bicg.cu", "agb_gmres.cu", "agb_selftest.cu",
            "agb_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]

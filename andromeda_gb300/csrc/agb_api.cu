@@ -37,6 +37,7 @@ struct agb_context {
   int kind = 0, neq = 0;
   IntegOpt iopt;  // triangle integration options (agb_set_integration)
   int solver = AGB_SOLVER_LSQR;  // agb_set_solver
+  int gmres_restart = 40;        // agb_set_gmres_restart (LIS's default restart length)
   MfOp mfop;                   // matrix-free operator (AGB_MATRIX_FREE)
   float* d_self6 = nullptr;
   double* d_lu = nullptr;      // column-major LU factors of the unscaled FP64 system (agb_solve_lu)
@@ -512,6 +513,18 @@ int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int r
     }
     return AGB_OK;
   }
+  if (c->solver == AGB_SOLVER_GMRES) {
+    if (!c->lsqr.packed)
+      return fail(c, AGB_ERR_UNSUPPORTED, "GMRES needs the packed mixed system (Stokes, velocity known on every "
+                                          "wall, triangles, default integration, AGB_MIXED)");
+    if (!c->lsqr.gmres(c->d_rhs, d_x, c->d_q, eps, maxit, c->gmres_restart, nt.data(), is.data()))
+      return fail(c, AGB_ERR_CUDA, "gmres: " + c->lsqr.err);
+    for (int r = 0; r < nrhs; ++r) {
+      if (nit) nit[r] = nt[r];
+      if (istop) istop[r] = is[r];
+    }
+    return AGB_OK;
+  }
   c->lsqr.bj = false;
   if (c->solver == AGB_SOLVER_LSQR_BLOCK) {
     if (!c->lsqr.packed)
@@ -808,10 +821,18 @@ int agb_set_integration(agb_context* c, int sing_mode, int rec_depth, double nea
 int agb_set_solver(agb_context* c, int solver) {
   if (!c) return fail(c, AGB_ERR_ARG, "agb_set_solver: no context");
   if (solver != AGB_SOLVER_LSQR && solver != AGB_SOLVER_BICGSTAB && solver != AGB_SOLVER_HYBRID &&
-      solver != AGB_SOLVER_LSQR_BLOCK)
+      solver != AGB_SOLVER_LSQR_BLOCK && solver != AGB_SOLVER_GMRES)
     return fail(c, AGB_ERR_ARG,
-                "solver must be AGB_SOLVER_LSQR, AGB_SOLVER_BICGSTAB, AGB_SOLVER_HYBRID or AGB_SOLVER_LSQR_BLOCK");
+                "solver must be AGB_SOLVER_LSQR, AGB_SOLVER_BICGSTAB, AGB_SOLVER_HYBRID, AGB_SOLVER_LSQR_BLOCK or "
+                "AGB_SOLVER_GMRES");
   c->solver = solver;
+  return AGB_OK;
+}
+
+int agb_set_gmres_restart(agb_context* c, int restart) {
+  if (!c) return fail(c, AGB_ERR_ARG, "agb_set_gmres_restart: no context");
+  if (restart < 1 || restart > 512) return fail(c, AGB_ERR_ARG, "agb_set_gmres_restart: restart must be 1..512");
+  c->gmres_restart = restart;
   return AGB_OK;
 }
 
@@ -1419,6 +1440,9 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
     if (!defect.empty()) return fail(c, AGB_ERR_ARG, "batched body " + std::to_string(i) + ": " + defect);
   }
   if (!c) return fail(c, AGB_ERR_ARG, "agb_batch_resistance: no context");
+  if (c->solver == AGB_SOLVER_GMRES)
+    return fail(c, AGB_ERR_UNSUPPORTED, "agb_batch_resistance: GMRES is a single-system solver here (use LSQR, "
+                                        "the block LSQR, BiCGSTAB or the hybrid)");
   cudaSetDevice(c->device);
   using clk = std::chrono::steady_clock;
   auto ms = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double, std::milli>(b - a).count(); };

@@ -1014,6 +1014,8 @@ void DenseLsqr::release() {
   cudaFree(Y); cudaFree(V); cudaFree(W); cudaFree(X); cudaFree(Z); cudaFree(Ys); cudaFree(Vs);
   cudaFree(part); cudaFree(Zp); cudaFree(sc); cudaFree(nactive); cudaFree(XsD); cudaFree(errflag); cudaFree(Yp); cudaFree(Vp);
   cudaFree(bg); cudaFree(bg_part); cudaFree(bsc); cudaFree(sc0); cudaFree(pc9);
+  cudaFree(gm); cudaFree(gm_part); cudaFree(gsc);
+  gm = nullptr; gm_part = nullptr; gsc = nullptr; gm_cap = 0; gm_mr = 0;
   pc9 = nullptr;
   pc9_ready = false;
   bj = false;

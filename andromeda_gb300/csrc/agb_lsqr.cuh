@@ -25,6 +25,15 @@ struct BicgScalars {
   double rho, rho_old, alpha, omega, bnorm, relres, snorm, best;
   int its, status, active, half, since;
 };
+// Per right-hand side GMRES state (DenseLsqr::gmres), FP64.  status: -1
+// running, 0 converged, 1 iteration limit, 3 a cycle without a 10 % gain of
+// the true residual.  jc: Arnoldi steps of the current cycle; hnext: the norm
+// that normalises the next basis vector; prev: the true relative residual at
+// the start of the cycle.
+struct GmresScalars {
+  double bnorm, beta, hnext, relres, prev;
+  int its, jc, active, status, cycles;
+};
 // BiCGSTAB stops a right-hand side whose residual grew BICG_DIVERGE times
 // above its best, or did not fall by 10 % within BICG_STALL iterations.
 constexpr double BICG_DIVERGE = 1.0e3;
@@ -82,6 +91,12 @@ struct DenseLsqr {
   BicgScalars* bsc = nullptr;
   LsqrScalars* sc0 = nullptr;   // zero gammas: the packed sweep writes Y = A W
   bool bg_diag = false;         // 1/diag(A) computed for the current matrix
+  // GMRES work (gmres): basis, w, X, r, Hessenberg and rotations; partial sums
+  double* gm = nullptr;
+  double* gm_part = nullptr;
+  size_t gm_cap = 0;
+  int gm_mr = 0;
+  GmresScalars* gsc = nullptr;
   double t_av = 0.0, t_atu = 0.0;
   long n_av = 0, n_atu = 0;
   long launches = 0;           // kernels launched by precon/solve
@@ -106,6 +121,14 @@ struct DenseLsqr {
   // 1 iteration limit, 2 breakdown.
   bool bicgstab(const double* b_dev, double* x_dev, double tol, int maxit, int* nit_host, int* status_host,
                 double* relres_host = nullptr);
+  // restarted GMRES(restart) with the 3x3 self-block right preconditioner on
+  // the packed layout: per column c, A x = b from x0 = 0 until the FP64 true
+  // residual ||b - A x|| <= tol ||b|| (checked at the end of every cycle) or
+  // maxit Arnoldi steps (0: 1000).  b, x as bicgstab; q: the column scales the
+  // residual sweep takes (those of solve).  status per column: 0 converged, 1
+  // iteration limit, 3 a cycle without a 10 % gain of the true residual.
+  bool gmres(const double* b_dev, double* x_dev, const double* q_dev, double tol, int maxit, int restart,
+             int* nit_host, int* status_host, double* relres_host = nullptr, int* cycles_host = nullptr);
   // inverses of the packed matrix's 3x3 self blocks into pc9 (once per matrix)
   bool block_precon();
   // r = b - A (x ./ q) with FP64 accumulation (refinement residual).

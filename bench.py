@@ -44,10 +44,13 @@ def parse():
     ap.add_argument("--outer-level", type=int, default=2)
     ap.add_argument("--outer-radius", type=float, default=200.0)
     ap.add_argument("--eps", type=float, default=1e-7)
-    ap.add_argument("--solver", default="lsqr", choices=["lsqr", "lsqr_block", "bicgstab", "hybrid"],
-                    help="sphere, batch, large: LSQR (lsqr_solve, the default), BiCGSTAB-Jacobi (the LIS path's "
-                         "solver), hybrid (BiCGSTAB, LSQR for the systems where it does not converge), or lsqr_block "
-                         "(LSQR with the 3x3 self-block right preconditioner)")
+    ap.add_argument("--solver", default="lsqr_block", choices=["lsqr", "lsqr_block", "bicgstab", "hybrid", "gmres"],
+                    help="sphere, batch, large: lsqr_block (LSQR with the 3x3 self-block right preconditioner, the "
+                         "default), lsqr (lsqr_solve with lsqr_precon's column scaling, the reference's), bicgstab "
+                         "(BiCGSTAB-Jacobi, the LIS path's solver), hybrid (BiCGSTAB, LSQR for the systems where it "
+                         "does not converge) or gmres (the LIS path with -i gmres, 3x3 self-block preconditioner; "
+                         "single bodies)")
+    ap.add_argument("--restart", type=int, default=40, help="gmres: restart length (40: the LIS default)")
     ap.add_argument("--fp64", default="full", choices=["full", "off"],
                     help="sphere: the plain FP64 GPU comparator solved to convergence at the same eps (full)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the full-size CPU estimate's sample")
@@ -91,13 +94,25 @@ def parse():
 
 def solver_id(A, name):
     return {"lsqr": A.SOLVER_LSQR, "bicgstab": A.SOLVER_BICGSTAB, "hybrid": A.SOLVER_HYBRID,
-            "lsqr_block": A.SOLVER_LSQR_BLOCK}[name]
+            "lsqr_block": A.SOLVER_LSQR_BLOCK, "gmres": A.SOLVER_GMRES}[name]
 
 
 def solver_text(name, eps):
     return {"lsqr": f"LSQR eps {eps:g}", "lsqr_block": f"LSQR (3x3 self-block preconditioner) eps {eps:g}",
             "bicgstab": f"BiCGSTAB-Jacobi tol {eps:g}",
-            "hybrid": f"BiCGSTAB-Jacobi tol {eps:g}, LSQR eps {eps:g} where it does not converge"}[name]
+            "hybrid": f"BiCGSTAB-Jacobi tol {eps:g}, LSQR eps {eps:g} where it does not converge",
+            "gmres": f"GMRES (3x3 self-block preconditioner) tol {eps:g}"}[name]
+
+
+def mesh_part(name):
+    """The mesh and boundary conditions of a workload name (without the solver)."""
+    for key in (", LSQR", ", BiCGSTAB", ", GMRES"):
+        name = name.split(key)[0]
+    return name
+
+
+def set_solver(A, C, name, args):
+    C.set_solver(solver_id(A, name), restart=args.restart if name == "gmres" else None)
 
 
 def workload(args):
@@ -469,7 +484,7 @@ def run_large(args):
     C = A.Context(0)
     C.set_mesh(m)
     C.set_problem(A.STOKES, [1, 2], A.dirichlet_known(A.STOKES, 2), itri=5)
-    C.set_solver(solver_id(A, args.solver))
+    set_solver(A, C, args.solver, args)
     ne = len(m["etype"])
     workload = (f"superellipsoid a=1 b=0.5 c=0.25 e1=0.6 e2=1.4, {nr}x{ns} grid ({len(body['etype'])} tri) "
                 f"in an L2 container r=200, 6 RHS, ITRI 5")
@@ -772,8 +787,7 @@ def main():
     C = A.Context(local if world > 1 else 0)
     C.set_mesh(m)
     C.set_problem(A.STOKES, [1, 2], A.dirichlet_known(A.STOKES, 2), itri=5)
-    solver = solver_id(A, args.solver)
-    C.set_solver(solver)
+    set_solver(A, C, args.solver, args)
 
     def step():
         return C.resistance_tensor(A.MIXED, 1, 2, eps=args.eps)
@@ -806,7 +820,7 @@ def main():
     if os.path.exists(GOLDEN_TRUTH):
         with open(GOLDEN_TRUTH) as f:
             g = json.load(f)
-        if g.get("workload") == name.split(", LSQR")[0].split(", BiCGSTAB")[0]:  # the mesh and BCs only
+        if g.get("workload") == mesh_part(name):  # the mesh and BCs only
             Rt = np.array(g["R"])
             rel_err = float(np.max(np.abs(R - Rt)) / np.max(np.abs(Rt)))
     lam = 1.0 / args.outer_radius
@@ -828,7 +842,8 @@ def main():
             for line in f:
                 if line.startswith("traffic_bytes_per_launch_k_avp_c2:"):
                     traffic = float(line.split(":")[1])
-    which = "LSQR A*V sweep" if args.solver in ("lsqr", "lsqr_block") else "BiCGSTAB A D^-1 p / A D^-1 s sweeps"
+    which = {"lsqr": "LSQR A*V sweep", "lsqr_block": "LSQR A*V sweep", "gmres": "GMRES A M^-1 v sweep"}.get(
+        args.solver, "BiCGSTAB A D^-1 p / A D^-1 s sweeps")
     roofline = {"bound": "hbm", "kernel": f"k_avp ({which} over the packed symmetric 3x3 blocks, FP32, TMA, 8 RHS)",
                 "achieved": a_bytes / (av_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                 "frac": a_bytes / (av_ms * 1e-3) / 1e9 / peak, "traffic": traffic, "peak_source": peak_kind,
@@ -846,7 +861,7 @@ def main():
         C2 = A.Context(local if world > 1 else 0)
         C2.set_mesh(m)
         C2.set_problem(A.STOKES, [1, 2], A.dirichlet_known(A.STOKES, 2), itri=5)
-        C2.set_solver(solver)
+        set_solver(A, C2, args.solver, args)
         C2.resistance_tensor(A.MIXED, 1, 2, eps=args.eps)
         C2.close()
         e2e_vals.append(time.perf_counter() - t2)
@@ -863,12 +878,12 @@ def main():
         if os.path.exists(GOLDEN_TRUTH):
             with open(GOLDEN_TRUTH) as f:
                 g = json.load(f)
-            if g.get("workload") == name.split(", LSQR")[0].split(", BiCGSTAB")[0]:
+            if g.get("workload") == mesh_part(name):
                 truth = np.array(g["R"])
-        for other in ("lsqr", "lsqr_block", "hybrid"):
+        for other in ("lsqr", "lsqr_block", "hybrid", "gmres"):
             if other == args.solver:
                 continue
-            C.set_solver(solver_id(A, other))
+            set_solver(A, C, other, args)
             ms_l, R_l, nit_l, ist_l = [], None, None, None
             for _ in range(args.lis_compare + 1):
                 R_l, nit_l, info_l = C.resistance_tensor(A.MIXED, 1, 2, eps=args.eps)
@@ -881,7 +896,7 @@ def main():
                                                  if truth is not None else None),
                              "nit": [int(v) for v in nit_l], "istop": [int(v) for v in ist_l],
                              "steps": len(ms_l) - 1, "ratio_to_headline": (1000.0 / ms_med) / (value / world)}
-        C.set_solver(solver_id(A, args.solver))
+        set_solver(A, C, args.solver, args)
 
     # assembly roofline: k_stokes_G<float, packed>, the regular quadrature of
     # every (collocation point, element) pair of the single layer; 28 flop per
@@ -934,7 +949,7 @@ def main():
             Cs = A.Context(0)
             Cs.set_mesh(ms_small)
             Cs.set_problem(A.STOKES, [1, 2], A.dirichlet_known(A.STOKES, 2), itri=5)
-            Cs.set_solver(solver_id(A, args.solver))
+            set_solver(A, Cs, args.solver, args)
             Cs.resistance_tensor(A.MIXED, 1, 2, eps=args.eps)
             gs, gR = [], None
             for _ in range(5):

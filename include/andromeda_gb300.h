@@ -82,6 +82,10 @@ typedef struct agb_context agb_context;
                                    preconditioner) in place of lsqr_precon's column scaling;
                                    packed mixed system only, also in agb_batch_resistance
                                    (no counterpart in the reference) */
+#define AGB_SOLVER_GMRES 4      /* restarted GMRES (SLET LIS with the LIS options "-i gmres
+                                   -restart m", the restart length set by agb_set_gmres_restart,
+                                   default 40 as LIS) with the 3x3 self-block right
+                                   preconditioner; packed mixed system only */
 
 /* boundary-condition types (mod_mesh.f90:110) */
 #define AGB_BC_FUNCTION 1
@@ -165,6 +169,17 @@ int agb_set_integration(agb_context* ctx, int sing_mode, int rec_depth, double n
  * AGB_SOLVER_HYBRID re-solves by LSQR every body with a right-hand side that
  * does not end at 0; no autotuning). */
 int agb_set_solver(agb_context* ctx, int solver);
+
+/* AGB_SOLVER_GMRES (the LIS path with "-i gmres", lis_solver_set_option at
+ * mod_plis.f90:235 taking the options of mod_par.f90:418): restarted GMRES(m)
+ * (Saad and Schultz 1986) on A M^-1, M the elements' 3x3 self blocks, x0 = 0,
+ * stop at ||b - A x|| <= eps ||b|| or maxit Arnoldi steps (0: 1000, the LIS
+ * default).  At the end of every cycle the true residual is formed with FP64
+ * accumulation over the stored matrix; the next cycle starts from it.  istop[r]:
+ * 0 converged (by the true residual), 1 iteration limit, 3 a cycle that did
+ * not lower the true residual by 10 %.  restart = m, 1..512 (default 40, the
+ * LIS default). */
+int agb_set_gmres_restart(agb_context* ctx, int restart);
 
 /* Element geometry in global element order (normal 3*nelem, area nelem,
  * centroid 3*nelem); elements outside the subdomain are zero. */

@@ -1690,6 +1690,141 @@ static int bicgstab_jacobi(const LisSystem& L, const double* b, double* x, doubl
   return 1;
 }
 
+// LIS with the options "-i gmres -restart m" (the LISS key of and.inp,
+// mod_par.f90:418): restarted GMRES(m) of Saad and Schultz (SIAM J. Sci. Stat.
+// Comput. 7, 1986; Saad, "Iterative Methods for Sparse Linear Systems", 2nd ed.,
+// Alg. 6.9: Arnoldi with Givens rotations), x0 = 0, right preconditioned so that
+// it minimises ||b - A x||_2 and stops at ||b - A x|| <= tol ||b||.  The
+// preconditioner M is block diagonal: the blocks of the unknowns that belong to
+// one node or one element (groups, LIS row numbers), inverted in FP64.  Gram-
+// Schmidt twice per step (CGS2).  At the end of every cycle the residual is
+// recomputed as b - A x; a cycle that does not lower it by 10 % stops with
+// status 3.  status: 0 converged, 1 iteration limit, 3 stagnated.
+static void block_inverses(const LisSystem& L, const std::vector<std::vector<int>>& groups,
+                           std::vector<std::vector<double>>& inv) {
+  inv.assign(groups.size(), {});
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    const std::vector<int>& g = groups[gi];
+    const int k = (int)g.size();
+    std::vector<double> B((size_t)k * k, 0.0), I((size_t)k * k, 0.0);
+    for (int a = 0; a < k; ++a) {
+      for (int64_t t = L.ia[g[a]]; t < L.ia[g[a] + 1]; ++t)
+        for (int b = 0; b < k; ++b)
+          if (L.ja[t] == g[b]) B[(size_t)a * k + b] = L.a[t];
+      I[(size_t)a * k + a] = 1.0;
+    }
+    // Gauss-Jordan with partial pivoting on the k x k block (k <= 3)
+    for (int col = 0; col < k; ++col) {
+      int piv = col;
+      for (int r = col + 1; r < k; ++r)
+        if (std::fabs(B[(size_t)r * k + col]) > std::fabs(B[(size_t)piv * k + col])) piv = r;
+      for (int c2 = 0; c2 < k; ++c2) {
+        std::swap(B[(size_t)col * k + c2], B[(size_t)piv * k + c2]);
+        std::swap(I[(size_t)col * k + c2], I[(size_t)piv * k + c2]);
+      }
+      const double d = B[(size_t)col * k + col];
+      for (int c2 = 0; c2 < k; ++c2) {
+        B[(size_t)col * k + c2] /= d;
+        I[(size_t)col * k + c2] /= d;
+      }
+      for (int r = 0; r < k; ++r) {
+        if (r == col) continue;
+        const double f = B[(size_t)r * k + col];
+        for (int c2 = 0; c2 < k; ++c2) {
+          B[(size_t)r * k + c2] -= f * B[(size_t)col * k + c2];
+          I[(size_t)r * k + c2] -= f * I[(size_t)col * k + c2];
+        }
+      }
+    }
+    inv[gi] = I;
+  }
+}
+
+static void block_apply(const std::vector<std::vector<int>>& groups, const std::vector<std::vector<double>>& inv,
+                        const double* v, double* z) {
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    const std::vector<int>& g = groups[gi];
+    const int k = (int)g.size();
+    for (int a = 0; a < k; ++a) {
+      double s = 0.0;
+      for (int b = 0; b < k; ++b) s += inv[gi][(size_t)a * k + b] * v[g[b]];
+      z[g[a]] = s;
+    }
+  }
+}
+
+static int gmres_block(const LisSystem& L, const std::vector<std::vector<int>>& groups, const double* b, double* x,
+                       double tol, int maxiter, int restart, int& iters, double& relres) {
+  const int n = L.n, mr = restart;
+  std::vector<std::vector<double>> inv;
+  block_inverses(L, groups, inv);
+  std::fill(x, x + n, 0.0);
+  iters = 0;
+  const double bnrm = std::sqrt(dot(n, b, b));
+  relres = bnrm > 0.0 ? 1.0 : 0.0;
+  if (bnrm == 0.0) return 0;
+  std::vector<double> r(b, b + n), w(n), z(n), Ax(n);
+  std::vector<std::vector<double>> V(mr, std::vector<double>(n));
+  std::vector<double> H((size_t)(mr + 1) * mr, 0.0), cs(mr), sn(mr), g(mr + 1), y(mr), h(mr + 1);
+  double prev = 1.0;
+  bool first = true;
+  for (;;) {
+    const double beta = std::sqrt(dot(n, r.data(), r.data()));
+    relres = beta / bnrm;
+    if (relres <= tol) return 0;
+    if (iters >= maxiter) return 1;
+    if (!first && relres > 0.9 * prev) return 3;
+    first = false;
+    prev = relres;
+    for (int i = 0; i < n; ++i) V[0][i] = r[i] / beta;
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int jc = 0;
+    for (int j = 0; j < mr; ++j) {
+      block_apply(groups, inv, V[j].data(), z.data());
+      lis_matvec(L, z.data(), w.data());
+      for (int i = 0; i <= j; ++i) H[(size_t)i * mr + j] = 0.0;
+      for (int pass = 0; pass < 2; ++pass) {
+        for (int i = 0; i <= j; ++i) h[i] = dot(n, V[i].data(), w.data());
+        for (int i = 0; i <= j; ++i) {
+          H[(size_t)i * mr + j] += h[i];
+          for (int t = 0; t < n; ++t) w[t] -= h[i] * V[i][t];
+        }
+      }
+      const double hn = std::sqrt(dot(n, w.data(), w.data()));
+      for (int l = 0; l < j; ++l) {
+        const double x0 = H[(size_t)l * mr + j], x1 = H[(size_t)(l + 1) * mr + j];
+        H[(size_t)l * mr + j] = cs[l] * x0 + sn[l] * x1;
+        H[(size_t)(l + 1) * mr + j] = -sn[l] * x0 + cs[l] * x1;
+      }
+      const double hd = H[(size_t)j * mr + j];
+      const double rr = std::hypot(hd, hn);
+      cs[j] = rr > 0.0 ? hd / rr : 1.0;
+      sn[j] = rr > 0.0 ? hn / rr : 0.0;
+      H[(size_t)j * mr + j] = rr;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = cs[j] * g[j];
+      ++iters;
+      jc = j + 1;
+      if (std::fabs(g[j + 1]) / bnrm <= tol || !(hn > 0.0) || iters >= maxiter || j + 1 == mr) break;
+      for (int t = 0; t < n; ++t) V[j + 1][t] = w[t] / hn;
+    }
+    for (int l = jc - 1; l >= 0; --l) {
+      double v = g[l];
+      for (int q = l + 1; q < jc; ++q) v -= H[(size_t)l * mr + q] * y[q];
+      const double d = H[(size_t)l * mr + l];
+      y[l] = d != 0.0 ? v / d : 0.0;
+    }
+    std::fill(w.begin(), w.end(), 0.0);
+    for (int l = 0; l < jc; ++l)
+      for (int t = 0; t < n; ++t) w[t] += y[l] * V[l][t];
+    block_apply(groups, inv, w.data(), z.data());
+    for (int t = 0; t < n; ++t) x[t] += z[t];
+    lis_matvec(L, x, Ax.data());
+    for (int t = 0; t < n; ++t) r[t] = b[t] - Ax[t];
+  }
+}
+
 // -----------------------------------------------------------------------------
 // Post-processing of a solved Stokes / Laplace field: the surface pressure and
 // values at points inside the domain.  Not on the solve path; the integrals of
@@ -2264,8 +2399,18 @@ int orc_stokes_solve_sequence(void* h, int nrhs, const double* u_in, double* q_o
 // and torque ft[r][6].  nits[r] / status[r] per field (status as
 // bicgstab_jacobi, 3: the system is not one equation per unknown).  Returns
 // the largest status.
+int orc_stokes_solve_lis_m(void* h, int nrhs, const double* u_in, double* q_out, double tol, int maxiter,
+                           int fwall, double* ft, int* nits, int* status, double* relres, int method, int restart);
 int orc_stokes_solve_lis(void* h, int nrhs, const double* u_in, double* q_out, double tol, int maxiter, int fwall,
                          double* ft, int* nits, int* status, double* relres) {
+  return orc_stokes_solve_lis_m(h, nrhs, u_in, q_out, tol, maxiter, fwall, ft, nits, status, relres, 0, 0);
+}
+
+// As orc_stokes_solve_lis with the LIS solver chosen: method 0 BiCGSTAB with
+// Jacobi (the default options), 1 GMRES(restart) with the node/element block
+// preconditioner (gmres_block).
+int orc_stokes_solve_lis_m(void* h, int nrhs, const double* u_in, double* q_out, double tol, int maxiter,
+                           int fwall, double* ft, int* nits, int* status, double* relres, int method, int restart) {
   Problem* P = (Problem*)h;
   if (P->kind != 2) return -1;
   if (P->M[0].empty()) { double e[2]; orc_form_integrals(h, e); }
@@ -2273,6 +2418,26 @@ int orc_stokes_solve_lis(void* h, int nrhs, const double* u_in, double* q_out, d
   Eqn& S = P->stk;
   LisSystem L;
   const bool ok = lis_system(*P, L);
+  // unknowns of one node or one element (LIS rows = unknown numbers): the blocks of gmres_block
+  std::vector<std::vector<int>> groups;
+  if (ok && method == 1) {
+    for (int i = 0; i < P->sd_nnodes; ++i) {
+      std::vector<int> g;
+      for (int een = 0; een < 3; ++een) {
+        const int bc = P->knownOf(een, P->BCidList[i]);
+        if (bc == iFlux || bc == iContact) g.push_back(S.col[P->nodeList[i] + een * P->nnodes] - 1);
+      }
+      if (!g.empty()) groups.push_back(g);
+    }
+    for (int i = 0; i < P->sd_nqnodes; ++i) {
+      std::vector<int> g;
+      for (int een = 0; een < 3; ++een) {
+        const int bc = P->knownOf(een, P->qbcidList[i]);
+        if (bc == iFunction || bc == iContact) g.push_back(S.qcol[P->qnodeList[i] + een * P->nelem] - 1);
+      }
+      if (!g.empty()) groups.push_back(g);
+    }
+  }
   int worst = 0;
   for (int r = 0; r < nrhs; ++r) {
     for (int en = 0; en < 3; ++en) {
@@ -2299,7 +2464,9 @@ int orc_stokes_solve_lis(void* h, int nrhs, const double* u_in, double* q_out, d
     for (int k = 0; k < S.sys.neq; ++k) b[L.row_of_crs[k]] = bc[k];
     int it = 0;
     double rr = 0.0;
-    const int st = bicgstab_jacobi(L, b.data(), S.x.data(), tol, maxiter, it, rr);
+    const int st = method == 1 ? gmres_block(L, groups, b.data(), S.x.data(), tol, maxiter, restart > 0 ? restart : 40,
+                                             it, rr)
+                               : bicgstab_jacobi(L, b.data(), S.x.data(), tol, maxiter, it, rr);
     nits[r] = it;
     status[r] = st;
     if (relres) relres[r] = rr;

@@ -81,6 +81,9 @@ def lib():
         L.orc_stokes_solve_lis.argtypes = [C.c_void_p, C.c_int, dp, dp, C.c_double, C.c_int, C.c_int, dp, ip, ip,
                                            dp]
         L.orc_stokes_solve_lis.restype = C.c_int
+        L.orc_stokes_solve_lis_m.argtypes = [C.c_void_p, C.c_int, dp, dp, C.c_double, C.c_int, C.c_int, dp, ip, ip,
+                                             dp, C.c_int, C.c_int]
+        L.orc_stokes_solve_lis_m.restype = C.c_int
         L.orc_pressure_stokes.argtypes = [C.c_void_p, dp, dp, dp]
         L.orc_pressure_stokes.restype = C.c_int
         L.orc_domain_values.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp, dp]
@@ -300,12 +303,13 @@ class Problem:
                                                ft.reshape(-1), nits)
         return q, ft, nits, ierr
 
-    def stokes_solve_lis(self, u_fields, tol=1e-8, maxiter=1000, fwall=1):
+    def stokes_solve_lis(self, u_fields, tol=1e-8, maxiter=1000, fwall=1, method="bicgstab", restart=40):
         """The LIS path (StokesBigSystemSOLVElis, lib_StokesLis.f90:4) with the
-        reference's default LIS options: BiCGSTAB, Jacobi, tol 1e-8, 1000 iterations.
+        reference's default LIS options: BiCGSTAB, Jacobi, tol 1e-8, 1000 iterations
+        (method "gmres": GMRES(restart) with the node/element block preconditioner).
         Returns (q [nrhs, 3, nelem], force/torque [nrhs, 6], iterations, status,
         relative residual); status 0 converged, 1 iteration limit, 2 breakdown,
-        3 not one equation per unknown."""
+        3 not one equation per unknown (GMRES: or stagnated)."""
         u_fields = np.ascontiguousarray(u_fields, dtype=np.float64)
         nrhs = u_fields.shape[0]
         q = np.zeros((nrhs, 3, self.nelem))
@@ -313,8 +317,9 @@ class Problem:
         nits = np.zeros(nrhs, np.int32)
         status = np.zeros(nrhs, np.int32)
         relres = np.zeros(nrhs)
-        lib().orc_stokes_solve_lis(self.h, nrhs, u_fields.ravel(), q.reshape(-1), float(tol), int(maxiter), fwall,
-                                   ft.reshape(-1), nits, status, relres)
+        lib().orc_stokes_solve_lis_m(self.h, nrhs, u_fields.ravel(), q.reshape(-1), float(tol), int(maxiter), fwall,
+                                     ft.reshape(-1), nits, status, relres, {"bicgstab": 0, "gmres": 1}[method],
+                                     int(restart))
         return q, ft, nits, status, relres
 
     def time_rows(self, r0, r1, nthreads):

@@ -1,0 +1,96 @@
+"""GPU restarted GMRES (AGB_SOLVER_GMRES: the LIS path with the options
+"-i gmres", right-preconditioned by the elements' 3x3 self blocks) on the packed
+mixed Stokes system.
+
+* against the oracle's LIS path with the same method (FP64 GMRES(40), the
+  node/element block preconditioner) on the same system: force and torque within
+  2e-6 (the FP32 matrix), Arnoldi steps within a few of the oracle's;
+* against the FP64 LSQR tensor on the level-4 sphere in the benchmark's
+  container: within 1e-6 (the benchmark's bar) in fewer products with the matrix
+  than the block LSQR needs, at restart lengths 40 and 10;
+* the systems and calls it does not take.
+"""
+import numpy as np
+import pytest
+
+from andromeda_gb300 import mesh as M
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx(agb, m, walls=(1, 2)):
+    C = agb.Context(0)
+    C.set_mesh(m)
+    C.set_problem(agb.STOKES, list(walls), agb.dirichlet_known(agb.STOKES, len(walls)), itri=5)
+    return C
+
+
+def _rigid_motions(m, outer_wall=2):
+    nn = len(m["xyz"])
+    outer = np.unique(m["con"][m["bcid"] == outer_wall, :3])
+    U = np.zeros((6, 3, nn))
+    for i in range(3):
+        U[i, i, outer] = 1.0
+        w = np.zeros(3)
+        w[i] = 1.0
+        U[3 + i][:, outer] = np.cross(w, m["xyz"][outer]).T
+    return U
+
+
+def _rel(a, b):
+    return np.max(np.abs(a - b)) / np.max(np.abs(b))
+
+
+def test_gmres_matches_oracle_lis_path(agb, orc):
+    m = M.particle_in_sphere(M.icosphere(2, 1.0, inward=True), outer_level=2, outer_radius=50.0)
+    P = orc.Problem(2, m, walls=[1, 2], known=np.ones((3, 2)), itri=5)
+    P.form_integrals()
+    _, ft_ref, n_ref, st_ref, _ = P.stokes_solve_lis(_rigid_motions(m), tol=1e-8, method="gmres")
+    P.close()
+    C = _ctx(agb, m)
+    C.set_solver(agb.SOLVER_GMRES)
+    R, nit, info = C.resistance_tensor(agb.MIXED, 1, 2, eps=1e-8)
+    C.close()
+    print("GMRES steps GPU", list(nit), "oracle", list(n_ref))
+    assert np.all(np.asarray(info["istop"]) == 0) and np.all(st_ref == 0)
+    assert np.max(np.abs(R - ft_ref)) < 2e-6 * np.max(np.abs(ft_ref))
+    # with FP32 products the residual estimate of the first cycle reaches tol in
+    # about the oracle's steps while the true residual is still above it (1e-8
+    # is below the FP32 rounding of A); one more cycle from the FP64 true
+    # residual ends it (17-18 steps in the oracle, 27-29 here)
+    assert np.all(nit <= 2 * n_ref + 5), (nit, n_ref)
+
+
+def test_gmres_tensor_against_fp64_lsqr(agb):
+    m = M.particle_in_sphere(M.icosphere(4, 1.0, inward=True), outer_level=2, outer_radius=200.0)
+    C = _ctx(agb, m)
+    R64, _, _ = C.resistance_tensor(agb.FP64, 1, 2, eps=1e-12)
+    C.set_solver(agb.SOLVER_LSQR_BLOCK)
+    Rb, nb, _ = C.resistance_tensor(agb.MIXED, 1, 2, eps=1e-7)
+    C.set_solver(agb.SOLVER_GMRES)
+    Rg, ng, info = C.resistance_tensor(agb.MIXED, 1, 2, eps=1e-7)
+    C.set_solver(agb.SOLVER_GMRES, restart=10)
+    R10, n10, info10 = C.resistance_tensor(agb.MIXED, 1, 2, eps=1e-7)
+    C.close()
+    print("GMRES steps", list(ng), "restart 10", list(n10), "block LSQR iterations", list(nb),
+          "errors", _rel(Rg, R64), _rel(R10, R64), _rel(Rb, R64))
+    assert np.all(np.asarray(info["istop"]) == 0) and np.all(np.asarray(info10["istop"]) == 0)
+    assert _rel(Rg, R64) < 1e-6 and _rel(R10, R64) < 1e-6
+    # one product with A per GMRES step, two per LSQR iteration
+    assert np.max(ng) < 2 * np.max(nb)
+
+
+def test_gmres_refusals(agb):
+    m = M.particle_in_sphere(M.icosphere(1, 1.0, inward=True), outer_level=1, outer_radius=10.0)
+    C = _ctx(agb, m)
+    C.set_solver(agb.SOLVER_GMRES)
+    with pytest.raises(agb.AgbError):
+        C.resistance_tensor(agb.FP64, 1, 2, eps=1e-8)  # the FP64 system is not packed
+    with pytest.raises(agb.AgbError):
+        C.set_solver(agb.SOLVER_GMRES, restart=0)
+    ctx = agb.Context(0)
+    ctx.set_solver(agb.SOLVER_GMRES)
+    with pytest.raises(agb.AgbError):
+        agb.batch_resistance([m], eps=1e-7, ctx=ctx)
+    ctx.close()
+    C.close()

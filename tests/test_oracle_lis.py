@@ -113,3 +113,47 @@ def test_lis_mixed_conditions_reference_cube(orc):
     P.close()
     assert status[0] == 0
     assert np.max(np.abs(q[0] - q_ls[0])) < 1e-6 * np.max(np.abs(q_ls[0]))
+
+
+def test_lis_gmres_matches_lsqr_and_bicgstab(sphere_case):
+    """The LIS options "-i gmres" (GMRES(40), the oracle's node/element block
+    preconditioner): the same force and torque as the LSQR path at tol 1e-12,
+    one product with the matrix per step, fewer products than BiCGSTAB."""
+    m, P, U, ft_ls, n_ls = sphere_case
+    q, ft, nits, status, relres = P.stokes_solve_lis(U, tol=1e-12, method="gmres")
+    assert np.all(status == 0) and np.all(relres <= 1e-12)
+    assert np.max(np.abs(ft - ft_ls)) < 1e-10 * np.max(np.abs(ft_ls))
+    _, _, nb, sb, _ = P.stokes_solve_lis(U, tol=1e-12)
+    assert np.all(sb == 0)
+    assert np.all(nits < 2 * nb), (nits, nb)  # GMRES step: one product; BiCGSTAB iteration: two
+
+
+def test_lis_gmres_restart_and_limit(sphere_case):
+    """A short restart length converges to the same answer over several cycles;
+    the iteration limit is reported as status 1."""
+    m, P, U, ft_ls, n_ls = sphere_case
+    _, ft40, n40, s40, _ = P.stokes_solve_lis(U[:2], tol=1e-10, method="gmres")
+    _, ft5, n5, s5, _ = P.stokes_solve_lis(U[:2], tol=1e-10, method="gmres", restart=5)
+    assert np.all(s40 == 0) and np.all(s5 == 0)
+    assert np.all(n5 >= n40)
+    assert np.max(np.abs(ft5 - ft40)) < 1e-8 * np.max(np.abs(ft40))
+    _, _, nl, sl, rl = P.stokes_solve_lis(U[:1], tol=1e-12, maxiter=3, method="gmres")
+    assert sl[0] == 1 and nl[0] == 3 and rl[0] > 1e-12
+
+
+def test_lis_gmres_mixed_conditions_reference_cube(orc):
+    """GMRES on the Poiseuille system, whose unknowns are velocities on some
+    walls and tractions on others (blocks of 1-3 unknowns per node or element)."""
+    m = reference_mesh("cube_624")
+    known = np.ones((3, 6), np.int32)
+    known[0, [2, 3, 5]] = 2
+    z = m["xyz"][:, 2]
+    U = np.zeros((1, 3, len(m["xyz"])))
+    U[0, 0] = (8.0 / 3.0) * (z - z * z)
+    P = orc.Problem(2, m, walls=[1, 2, 3, 4, 5, 6], known=known, diff=1.5, itri=5)
+    P.form_integrals()
+    q_ls, _, _, ierr = P.stokes_solve_sequence(U, maxit=0, eps=1e-13, fwall=1)
+    q, _, nits, status, _ = P.stokes_solve_lis(U, tol=1e-12, method="gmres", restart=60)
+    P.close()
+    assert status[0] == 0
+    assert np.max(np.abs(q[0] - q_ls[0])) < 1e-6 * np.max(np.abs(q_ls[0]))
