@@ -34,6 +34,7 @@ SIGNATURES = {
     "agb_set_integration": ([vp, I, I, D, I], I),
     "agb_set_solver": ([vp, I], I),
     "agb_set_gmres_restart": ([vp, I], I),
+    "agb_set_residual_mode": ([vp, I], I),
     "agb_surface_pressure": ([vp, dp, dp, dp], I),
     "agb_domain_values": ([vp, I, dp, dp, dp, dp, dp], I),
     "agb_system_size": ([vp, PI, PI], I),

@@ -142,6 +142,10 @@ class Context:
         if restart is not None:
             self._ck(self._L.agb_set_gmres_restart(self.h, int(restart)))
 
+    def set_residual_mode(self, mode):
+        """0: float-float true residuals on the FP32 pipe (default); 1: FP64."""
+        self._ck(self._L.agb_set_residual_mode(self.h, int(mode)))
+
     def surface_pressure(self, u, q):
         """Pressure at the element centroids (pressureStokes) of velocity u (3, nnodes)
         and traction q (3, nelem); elements of no subdomain wall get 0."""

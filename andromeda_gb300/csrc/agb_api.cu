@@ -38,6 +38,7 @@ struct agb_context {
   IntegOpt iopt;  // triangle integration options (agb_set_integration)
   int solver = AGB_SOLVER_LSQR;  // agb_set_solver
   int gmres_restart = 40;        // agb_set_gmres_restart (LIS's default restart length)
+  bool resid_fp64 = false;       // agb_set_residual_mode
   MfOp mfop;                   // matrix-free operator (AGB_MATRIX_FREE)
   float* d_self6 = nullptr;
   double* d_lu = nullptr;      // column-major LU factors of the unscaled FP64 system (agb_solve_lu)
@@ -433,6 +434,7 @@ int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int r
     if (!c->lsqr.setup(c->d_A, c->prec != AGB_FP64, c->m, c->n, c->lda, nrhs, c->stream))
       return fail(c, AGB_ERR_CUDA, "lsqr setup: " + c->lsqr.err);
   }
+  c->lsqr.resid_fp64 = c->resid_fp64;
   std::vector<int> nt(nrhs, 0), is(nrhs, 0);
   if (c->solver == AGB_SOLVER_BICGSTAB || c->solver == AGB_SOLVER_HYBRID) {
     if (!c->lsqr.packed)
@@ -826,6 +828,14 @@ int agb_set_solver(agb_context* c, int solver) {
                 "solver must be AGB_SOLVER_LSQR, AGB_SOLVER_BICGSTAB, AGB_SOLVER_HYBRID, AGB_SOLVER_LSQR_BLOCK or "
                 "AGB_SOLVER_GMRES");
   c->solver = solver;
+  return AGB_OK;
+}
+
+int agb_set_residual_mode(agb_context* c, int mode) {
+  if (!c) return fail(c, AGB_ERR_ARG, "agb_set_residual_mode: no context");
+  if (mode != 0 && mode != 1) return fail(c, AGB_ERR_ARG, "agb_set_residual_mode: mode must be 0 or 1");
+  c->resid_fp64 = mode == 1;
+  c->lsqr.resid_fp64 = c->resid_fp64;
   return AGB_OK;
 }
 

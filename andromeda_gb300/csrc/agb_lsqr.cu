@@ -550,6 +550,116 @@ __global__ void __launch_bounds__(256) k_residp(const float* __restrict__ Ap, in
   }
 }
 
+// q.Xs split into FP32 parts, x = xh + xl to about 2^-48 relative ([n][8])
+__global__ void k_split_x(int64_t n8, const double* __restrict__ Xs, const double* __restrict__ qs,
+                          float* __restrict__ Xh, float* __restrict__ Xl) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n8; t += (int64_t)gridDim.x * blockDim.x) {
+    const double x = qs[t >> 3] * Xs[t];
+    const float h = (float)x;
+    Xh[t] = h;
+    Xl[t] = (float)(x - (double)h);
+  }
+}
+
+// r = b - A x over the packed matrix as k_residp computes it, on the FP32 pipe:
+// with x = xh + xl, every product g xh is split exactly into p + pe (p the
+// rounded product, pe = fma(g, xh, -p)); the p are summed by TwoSum (Knuth;
+// s + e holds the running sum exactly up to the rounding of the error term),
+// the pe and the g xl terms into a third FP32 sum, and the three sums are
+// moved into FP64 accumulators every 64 terms of a lane.  The result is within
+// about 2^-40 (worst case; random rounding: 2^-46) of sum |a_ij x_j| of the
+// exact product, where FP64 accumulation gives 2^-53: far below any tolerance
+// the solvers test, on the FP32 pipe instead of the 1:64 FP64 pipe.  The adds
+// and the product use the _rn intrinsics so that nothing is contracted into an
+// FMA, which would break the exactness of TwoSum.  One warp per element row i.
+template <int KC>
+__global__ void __launch_bounds__(256) k_residp_ff(const float* __restrict__ Ap, int ne, int ldp,
+                                                   const float* __restrict__ Xh, const float* __restrict__ Xl,
+                                                   const double* __restrict__ Bp, double* __restrict__ Y,
+                                                   float* __restrict__ Ys, double* __restrict__ part) {
+  __shared__ double sPart[8][K8];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 8 + warp;
+  float sm[3][KC], er[3][KC], lo[3][KC];
+  double acc[3][KC];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < KC; ++c) {
+      sm[a][c] = er[a][c] = lo[a][c] = 0.f;
+      acc[a][c] = 0.0;
+    }
+  if (i < ne) {
+    for (int j0 = lane; j0 < ne; j0 += 32 * 64) {
+    const int j1 = min(ne, j0 + 32 * 64);
+    for (int j = j0; j < j1; j += 32) {
+      float g6[6];
+      const float* pj = Ap + pk_idx(i, 0, j, ldp);
+#pragma unroll
+      for (int c = 0; c < 6; ++c) g6[c] = pj[c * 64];
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        const float* xh = Xh + ((int64_t)b * ne + j) * K8;
+        const float* xl = Xl + ((int64_t)b * ne + j) * K8;
+        float hv[KC], lv[KC];
+#pragma unroll
+        for (int c = 0; c < KC; ++c) {
+          hv[c] = xh[c];
+          lv[c] = xl[c];
+        }
+#pragma unroll
+        for (int c = 0; c < KC; ++c)
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            const float g = g6[sym6(a, b)];
+            const float p = __fmul_rn(g, hv[c]);
+            const float pe = fmaf(g, hv[c], -p);
+            const float s0 = sm[a][c];
+            const float t = __fadd_rn(s0, p);
+            const float bp = __fsub_rn(t, s0);
+            const float e = __fadd_rn(__fsub_rn(s0, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+            sm[a][c] = t;
+            er[a][c] = __fadd_rn(er[a][c], e);
+            lo[a][c] = fmaf(g, lv[c], __fadd_rn(lo[a][c], pe));
+          }
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int c = 0; c < KC; ++c) {
+        acc[a][c] += (double)sm[a][c] + ((double)er[a][c] + (double)lo[a][c]);
+        sm[a][c] = er[a][c] = lo[a][c] = 0.f;
+      }
+    }
+  }
+  double ssq = 0.0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < K8; ++c) {
+      double v = 0.0;
+      if (c < KC) v = acc[a][c];
+      v = warp_sum(v);
+      if (lane == a * K8 + c && i < ne) {
+        const int64_t id = (int64_t)(3 * i + a) * K8 + c;
+        const double y = Bp[id] - v;
+        Y[id] = y;
+        Ys[id] = (float)y;
+        ssq = y * y;
+      }
+    }
+  ssq += __shfl_down_sync(0xffffffffu, ssq, 8);
+  ssq += __shfl_down_sync(0xffffffffu, ssq, 16);
+  if (lane < K8) sPart[warp][lane] = ssq;
+  __syncthreads();
+  if (threadIdx.x < K8) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += sPart[w][threadIdx.x];
+    part[(int64_t)blockIdx.x * K8 + threadIdx.x] = t;
+  }
+}
+
 // column sums of squares of the packed matrix per row group:
 // P[g][b ne + j] = sum_{i in g} sum_a Ap[i][sym(a,b)][j]^2
 __global__ void k_colsqp(const float* __restrict__ Ap, int ne, int ldp, int rows_per_group, double* __restrict__ P,
@@ -919,8 +1029,22 @@ bool make_packed_map(CUtensorMap* tm, const void* Ap, int pldp, int ne, int box_
 template <typename T>
 static void launch_resid(const DenseLsqr& L, const double* Xs, const double* Bp) {
   if (L.packed) {
-    k_residp<<<cdiv(L.pk_ne, 8), 256, 0, L.stream>>>((const float*)L.A, L.pk_ne, L.pk_ldp, Xs, L.mf_q, Bp, L.Y,
-                                                     (float*)L.Ys, L.part);
+    if (L.resid_fp64) {
+      k_residp<<<cdiv(L.pk_ne, 8), 256, 0, L.stream>>>((const float*)L.A, L.pk_ne, L.pk_ldp, Xs, L.mf_q, Bp, L.Y,
+                                                       (float*)L.Ys, L.part);
+      return;
+    }
+    // products and sums on the FP32 pipe in float-float form (k_residp_ff)
+    const int64_t n8 = (int64_t)3 * L.pk_ne * K8;
+    float* Xh = L.Xff;
+    float* Xl = L.Xff + L.lda * K8;
+    k_split_x<<<(unsigned)std::min<int64_t>(cdiv(n8, 256), 4096), 256, 0, L.stream>>>(n8, Xs, L.mf_q, Xh, Xl);
+    if (L.k <= 6)
+      k_residp_ff<6><<<cdiv(L.pk_ne, 8), 256, 0, L.stream>>>((const float*)L.A, L.pk_ne, L.pk_ldp, Xh, Xl, Bp, L.Y,
+                                                              (float*)L.Ys, L.part);
+    else
+      k_residp_ff<8><<<cdiv(L.pk_ne, 8), 256, 0, L.stream>>>((const float*)L.A, L.pk_ne, L.pk_ldp, Xh, Xl, Bp, L.Y,
+                                                              (float*)L.Ys, L.part);
     return;
   }
   const unsigned nb = cdiv(L.m, AV_ROWS);
@@ -1014,7 +1138,8 @@ void DenseLsqr::release() {
   cudaFree(Y); cudaFree(V); cudaFree(W); cudaFree(X); cudaFree(Z); cudaFree(Ys); cudaFree(Vs);
   cudaFree(part); cudaFree(Zp); cudaFree(sc); cudaFree(nactive); cudaFree(XsD); cudaFree(errflag); cudaFree(Yp); cudaFree(Vp);
   cudaFree(bg); cudaFree(bg_part); cudaFree(bsc); cudaFree(sc0); cudaFree(pc9);
-  cudaFree(gm); cudaFree(gm_part); cudaFree(gsc);
+  cudaFree(gm); cudaFree(gm_part); cudaFree(gsc); cudaFree(Xff);
+  Xff = nullptr;
   gm = nullptr; gm_part = nullptr; gsc = nullptr; gm_cap = 0; gm_mr = 0;
   pc9 = nullptr;
   pc9_ready = false;
@@ -1112,6 +1237,7 @@ bool DenseLsqr::setup(const void* A_dev, bool is_fp32, int m_, int n_, int64_t l
     CK(cudaMalloc(&Yp, (size_t)mf_cb * m * K8 * sizeof(float)));
   }
   CK(cudaMalloc(&XsD, lda * K8 * sizeof(double)));
+  CK(cudaMalloc(&Xff, 2 * lda * K8 * sizeof(float)));
   CK(cudaMalloc(&errflag, sizeof(int)));
   CK(cudaMemsetAsync(errflag, 0, sizeof(int), stream));
   CK(cudaMalloc(&Zp, (int64_t)zgroups * lda * K8 * sizeof(double)));

@@ -53,6 +53,8 @@ struct DenseLsqr {
   double *Y = nullptr, *V = nullptr, *W = nullptr, *X = nullptr, *Z = nullptr;
   void *Ys = nullptr, *Vs = nullptr;  // T copies used by the sweeps (Ys [m][8], Vs [8][lda])
   double* XsD = nullptr;       // x0./q packed [lda][8] for the FP64-accumulated residual
+  float* Xff = nullptr;        // q.XsD split into FP32 high and low parts [2][lda][8] (packed residual)
+  bool resid_fp64 = false;     // packed residual on the FP64 pipe (k_residp) instead of float-float
   int* errflag = nullptr;      // set by a kernel whose bounded wait gave up
   double* part = nullptr;      // per-CTA partial sums
   double* Zp = nullptr;        // per-row-group partial products of A^T Y

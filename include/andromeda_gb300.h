@@ -181,6 +181,13 @@ int agb_set_solver(agb_context* ctx, int solver);
  * LIS default). */
 int agb_set_gmres_restart(agb_context* ctx, int restart);
 
+/* Arithmetic of the true residual b - A x over the packed FP32 single layer
+ * (GMRES and BiCGSTAB restarts, refinement, LSQR warm starts): 0 (default)
+ * float-float products and sums on the FP32 pipe (TwoSum, flushed into FP64
+ * every 64 terms; within about 2^-40 of sum |a_ij x_j| of the exact residual),
+ * 1 FP64 products and sums (the FP64 pipe, ~10x slower on this part). */
+int agb_set_residual_mode(agb_context* ctx, int mode);
+
 /* Element geometry in global element order (normal 3*nelem, area nelem,
  * centroid 3*nelem); elements outside the subdomain are zero. */
 int agb_get_geometry(agb_context* ctx, double* normal, double* area, double* centroid);

@@ -94,3 +94,30 @@ def test_gmres_refusals(agb):
         agb.batch_resistance([m], eps=1e-7, ctx=ctx)
     ctx.close()
     C.close()
+
+
+def test_float_float_residual_matches_fp64(agb):
+    """The float-float true residual (default) against the FP64 one: GMRES and
+    BiCGSTAB, which restart from it, give the same tensors and step counts, and
+    one pass of FP64 refinement of the block LSQR lands on the same tensor."""
+    m = M.particle_in_sphere(M.icosphere(3, 1.0, inward=True), outer_level=2, outer_radius=200.0)
+    C = _ctx(agb, m)
+    out = {}
+    for mode in (0, 1):
+        C.set_residual_mode(mode)
+        for s in (agb.SOLVER_GMRES, agb.SOLVER_BICGSTAB):
+            C.set_solver(s)
+            out[mode, s] = C.resistance_tensor(agb.MIXED, 1, 2, eps=1e-8)
+        C.set_solver(agb.SOLVER_LSQR_BLOCK)
+        out[mode, "refine"] = C.resistance_tensor(agb.MIXED, 1, 2, eps=1e-7, refine=1)
+    C.close()
+    # the two residuals differ by ~2^-40 of sum |a_ij x_j|, ~1e-5 of a residual
+    # at 1e-7 of b; the refinement's correction solve (to 1e-2) carries that
+    # into its near-null component, which reaches the tensor at a few 1e-9
+    bar = {agb.SOLVER_GMRES: 1e-9, agb.SOLVER_BICGSTAB: 1e-9, "refine": 1e-8}
+    for key in (agb.SOLVER_GMRES, agb.SOLVER_BICGSTAB, "refine"):
+        R0, n0, _ = out[0, key]
+        R1, n1, _ = out[1, key]
+        print(key, list(n0), list(n1), _rel(R0, R1))
+        assert _rel(R0, R1) < bar[key], key
+        assert np.all(np.abs(np.asarray(n0) - np.asarray(n1)) <= 2), (key, n0, n1)
