@@ -44,12 +44,13 @@ def parse():
     ap.add_argument("--outer-level", type=int, default=2)
     ap.add_argument("--outer-radius", type=float, default=200.0)
     ap.add_argument("--eps", type=float, default=1e-7)
-    ap.add_argument("--solver", default="lsqr_block", choices=["lsqr", "lsqr_block", "bicgstab", "hybrid", "gmres"],
-                    help="sphere, batch, large: lsqr_block (LSQR with the 3x3 self-block right preconditioner, the "
-                         "default), lsqr (lsqr_solve with lsqr_precon's column scaling, the reference's), bicgstab "
-                         "(BiCGSTAB-Jacobi, the LIS path's solver), hybrid (BiCGSTAB, LSQR for the systems where it "
-                         "does not converge) or gmres (the LIS path with -i gmres, 3x3 self-block preconditioner; "
-                         "single bodies)")
+    ap.add_argument("--solver", default=None, choices=["lsqr", "lsqr_block", "bicgstab", "hybrid", "gmres"],
+                    help="sphere, batch, large: gmres (the default of sphere and large; the LIS path with -i gmres, "
+                         "3x3 self-block right preconditioner, FP64 true-residual restarts), lsqr_block (LSQR with "
+                         "the 3x3 self-block right preconditioner, the default of batch), lsqr (lsqr_solve with "
+                         "lsqr_precon's column scaling, the reference's), bicgstab "
+                         "(BiCGSTAB-Jacobi, the LIS path's default solver) or hybrid (BiCGSTAB, LSQR for the "
+                         "systems where it does not converge)")
     ap.add_argument("--restart", type=int, default=40, help="gmres: restart length (40: the LIS default)")
     ap.add_argument("--fp64", default="full", choices=["full", "off"],
                     help="sphere: the plain FP64 GPU comparator solved to convergence at the same eps (full)")
@@ -89,7 +90,10 @@ def parse():
                     help="large/resident: also solve the FP64 path to this eps where its matrix fits (0: off)")
     ap.add_argument("--itri", type=int, default=1, help="laplace: triangle rule (1 = 7 points)")
     ap.add_argument("--laplace-eps", type=float, default=1e-12, help="laplace: LSQR eps")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.solver is None:
+        args.solver = "lsqr_block" if args.workload == "batch" else "gmres"
+    return args
 
 
 def solver_id(A, name):
