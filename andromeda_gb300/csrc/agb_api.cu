@@ -1450,9 +1450,6 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
     if (!defect.empty()) return fail(c, AGB_ERR_ARG, "batched body " + std::to_string(i) + ": " + defect);
   }
   if (!c) return fail(c, AGB_ERR_ARG, "agb_batch_resistance: no context");
-  if (c->solver == AGB_SOLVER_GMRES)
-    return fail(c, AGB_ERR_UNSUPPORTED, "agb_batch_resistance: GMRES is a single-system solver here (use LSQR, "
-                                        "the block LSQR, BiCGSTAB or the hybrid)");
   cudaSetDevice(c->device);
   using clk = std::chrono::steady_clock;
   auto ms = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
@@ -1510,8 +1507,13 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
     const double mpad = std::ceil(b.m / 256.0) * 256.0;
     const bool bicg_used = c->solver == AGB_SOLVER_BICGSTAB || c->solver == AGB_SOLVER_HYBRID;
     const double bicg = bicg_used ? mpad * 8 * 8 * 7.0 + mpad * 8 : 0.0;
-    const double pc9 = (c->solver == AGB_SOLVER_LSQR_BLOCK) ? 72.0 * b.ne : 0.0;
-    return mpad * 8 * 12.0 + (double)b.lda * 8 * (8 * 3 + 4 + 8 * 8) + 65536.0 + bicg + pc9;
+    const double pc9 = (c->solver == AGB_SOLVER_LSQR_BLOCK || c->solver == AGB_SOLVER_GMRES) ? 72.0 * b.ne : 0.0;
+    const double mr = c->gmres_restart;
+    const double gm = (c->solver == AGB_SOLVER_GMRES)
+                          ? 64.0 * (mr * mpad + (mr + 1) * mr + 5 * (mr + 1) + mpad + mpad / 32 * (mr + 1)) +
+                                192.0 * b.ne
+                          : 0.0;
+    return mpad * 8 * 12.0 + (double)b.lda * 8 * (8 * 3 + 4 + 8 * 8) + 65536.0 + bicg + pc9 + gm;
   };
   double budget = mem_gb * 1e9;
   if (budget <= 0.0) {
@@ -1675,7 +1677,10 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
     }
     std::vector<int> nv, iv;
     std::string err;
-    if (c->solver == AGB_SOLVER_BICGSTAB || c->solver == AGB_SOLVER_HYBRID) {
+    if (c->solver == AGB_SOLVER_GMRES) {
+      if (!batch_gmres_solve(bodies, 6, eps, maxit, c->gmres_restart, st, nv, iv, &bst, err))
+        return bail(AGB_ERR_CUDA, "solve: " + err);
+    } else if (c->solver == AGB_SOLVER_BICGSTAB || c->solver == AGB_SOLVER_HYBRID) {
       if (!batch_bicgstab_solve(bodies, 6, eps, maxit, st, nv, iv, &bst, err)) return bail(AGB_ERR_CUDA, "solve: " + err);
       // FP64 refinement of the bodies whose recursive residual converged but whose
       // true residual did not (istop 4): BiCGSTAB on r = b - A x from zero to

@@ -65,6 +65,15 @@ struct GDesc {  // CUtensorMap members keep the 64-byte alignment TMA needs
   double* rr;  // ||b - A x||^2 per right-hand side (the FP64 check after the solve)
   double* tolc;  // per right-hand side tolerances [K8] (BiCGSTAB restarts), or null: the launch's tol
   double* pc9; // block-Jacobi right preconditioner of the LSQR ([ne][3][3] inverse self blocks), or null
+  // GMRES (batch_gmres_solve): basis [gmr][mpad][8], Hessenberg [gmr+1][gmr][8],
+  // rotations cs, sn, g, y and the Gram-Schmidt coefficients hc [gmr+1][8],
+  // the iterate X in the row numbering 3i+b of unknown b ne + i [mpad][8], x
+  // split for the float-float residual [n][8] each, partial sums
+  // [nb_b][gmr+1][8]; w = A M^-1 v is Y
+  double *gV, *gH, *gcs, *gsn, *gg, *gy, *ghc, *gX, *gpart;
+  float *gXh, *gXl;
+  GmresScalars* gs;
+  int gmr;
   BicgScalars* bs;
   const LsqrScalars* sc0;
 };
@@ -606,6 +615,368 @@ __global__ void __launch_bounds__(256) gb_resid(const GDesc* __restrict__ D, con
 }
 
 // ---------------------------------------------------------------------------
+// Batched restarted GMRES with the 3x3 self-block right preconditioner (the
+// recurrence of DenseLsqr::gmres, agb_gmres.cu), every kernel one launch over
+// the tiles of all systems.  Element-wise kernels use the init tiles
+// (mpad * 8 / 256 per system, t = 8 u + c); per-system reductions are one CTA
+// per system over its tiles' partial sums in a fixed order.  bact: systems
+// with a column still in the current cycle; bran: systems that ran the cycle
+// (their iterate is updated and their true residual formed after it).
+// ---------------------------------------------------------------------------
+// w = b (from_b) or the residual already in Y; partial 0: ||w||^2
+__global__ void __launch_bounds__(BT) gg_load(const GDesc* __restrict__ D, const int* __restrict__ off, int nb,
+                                             const int* __restrict__ bran, int from_b) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  if (!bran[bi]) return;
+  const GDesc& d = D[bi];
+  const int blk = blockIdx.x - off[bi];
+  const int64_t t = (int64_t)blk * BT + threadIdx.x;
+  const int64_t u = t / K8;
+  const int c = (int)(t % K8);
+  double v = 0.0;
+  if (from_b) {
+    if (u < d.m && c < d.k) v = d.b[(int64_t)c * d.m + u];
+    d.Y[t] = v;
+  } else {
+    v = d.Y[t];
+  }
+  block_sum8(v * v, d.gpart + (int64_t)blk * (d.gmr + 1) * K8);
+}
+
+// start of a cycle (DenseLsqr::gmres's k_gm_begin per system)
+__global__ void __launch_bounds__(256) gg_begin(const GDesc* __restrict__ D, int* __restrict__ bact,
+                                               int* __restrict__ bran, int* nactive, double tol, int first) {
+  const int bi = blockIdx.x;
+  if (!bran[bi]) return;
+  const GDesc& d = D[bi];
+  const int np = d.gmr + 1;
+  __shared__ double sred[256];
+  __shared__ double ssum[K8];
+  const int t = threadIdx.x, cc = t % K8;
+  double a = 0.0;
+  for (int b = t / K8; b < d.nb_b; b += 256 / K8) a += d.gpart[((int64_t)b * np) * K8 + cc];
+  sred[t] = a;
+  __syncthreads();
+  if (t < K8) {
+    double tot = 0.0;
+    for (int i = t; i < 256; i += K8) tot += sred[i];
+    ssum[t] = tot;
+  }
+  __syncthreads();
+  if (t < K8) {
+    GmresScalars& q = d.gs[t];
+    const double beta = sqrt(ssum[t]);
+    if (first) {
+      q.bnorm = beta;
+      q.its = 0;
+      q.cycles = 0;
+      q.status = (t < d.k && beta > 0.0) ? -1 : 0;
+      q.prev = 1.0;
+      q.relres = (beta > 0.0) ? 1.0 : 0.0;
+    }
+    q.jc = 0;
+    if (q.status == -1) {
+      const double rel = beta / q.bnorm;
+      q.relres = rel;
+      if (rel <= tol) q.status = 0;
+      else if (q.its >= d.itnlim) q.status = 1;
+      else if (!first && rel > 0.9 * q.prev) q.status = 3;
+      q.prev = rel;
+    }
+    q.active = (q.status == -1) ? 1 : 0;
+    if (q.active) q.cycles += 1;
+    q.beta = beta;
+    q.hnext = beta;
+    d.gg[t] = beta;
+  }
+  __syncthreads();
+  if (t == 0) {
+    int na = 0;
+    for (int c = 0; c < K8; ++c) na += d.gs[c].active;
+    bact[bi] = na > 0;
+    bran[bi] = na > 0;
+    if (na) atomicAdd(nactive, na);
+  }
+}
+
+// v_j = w / h; W = fp32(M^-1 v_j) as [b][8][ldp] (zero for an inactive column)
+__global__ void __launch_bounds__(BT) gg_pc(const GDesc* __restrict__ D, const int* __restrict__ off, int nb,
+                                           const int* __restrict__ bact, int j) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  if (!bact[bi]) return;
+  const GDesc& d = D[bi];
+  const int64_t t = (int64_t)(blockIdx.x - off[bi]) * BT + threadIdx.x;
+  const int i = (int)(t / K8), c = (int)(t % K8);
+  if (i >= d.pk_ne) return;
+  const GmresScalars& q = d.gs[c];
+  double* Vj = d.gV + (int64_t)j * d.mpad * K8;
+  float o[3] = {0.f, 0.f, 0.f};
+  if (q.active) {
+    const double inv = 1.0 / q.hnext;
+    double v[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const int64_t id = (int64_t)(3 * i + a) * K8 + c;
+      v[a] = d.Y[id] * inv;
+      Vj[id] = v[a];
+    }
+    const double* mi = d.pc9 + 9 * (int64_t)i;
+#pragma unroll
+    for (int b = 0; b < 3; ++b) o[b] = (float)(mi[3 * b] * v[0] + mi[3 * b + 1] * v[1] + mi[3 * b + 2] * v[2]);
+  } else {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) Vj[(int64_t)(3 * i + a) * K8 + c] = 0.0;
+  }
+#pragma unroll
+  for (int b = 0; b < 3; ++b) d.Vp[((int64_t)b * K8 + c) * d.pk_ldp + i] = o[b];
+}
+
+// partial l (l = 0..j): v_l . w
+__global__ void __launch_bounds__(BT) gg_dots(const GDesc* __restrict__ D, const int* __restrict__ off, int nb,
+                                             const int* __restrict__ bact, int j) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  if (!bact[bi]) return;
+  const GDesc& d = D[bi];
+  const int blk = blockIdx.x - off[bi];
+  const int64_t t = (int64_t)blk * BT + threadIdx.x;
+  const int64_t mv = d.mpad * K8;
+  const double w = d.Y[t];
+  for (int l = 0; l <= j; ++l)
+    block_sum8(d.gV[(int64_t)l * mv + t] * w, d.gpart + ((int64_t)blk * (d.gmr + 1) + l) * K8);
+}
+
+// hc[l] = v_l . w from the tile partials (in order); H[l][j] = hc (pass 0) or += hc
+__global__ void __launch_bounds__(256) gg_hred(const GDesc* __restrict__ D, const int* __restrict__ bact, int j,
+                                              int pass) {
+  const int bi = blockIdx.x;
+  if (!bact[bi]) return;
+  const GDesc& d = D[bi];
+  const int np = d.gmr + 1;
+  for (int p = threadIdx.x; p < (j + 1) * K8; p += blockDim.x) {
+    const int l = p / K8, c = p % K8;
+    double v = 0.0;
+    for (int b = 0; b < d.nb_b; ++b) v += d.gpart[((int64_t)b * np + l) * K8 + c];
+    d.ghc[p] = v;
+    double* h = d.gH + ((int64_t)l * d.gmr + j) * K8 + c;
+    *h = pass ? *h + v : v;
+  }
+}
+
+// w -= sum_l hc[l] v_l over the active columns; partial 0: ||w||^2
+__global__ void __launch_bounds__(BT) gg_orth(const GDesc* __restrict__ D, const int* __restrict__ off, int nb,
+                                             const int* __restrict__ bact, int j) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  if (!bact[bi]) return;
+  const GDesc& d = D[bi];
+  const int blk = blockIdx.x - off[bi];
+  const int64_t t = (int64_t)blk * BT + threadIdx.x;
+  const int c = (int)(t % K8);
+  const int64_t mv = d.mpad * K8;
+  double w = d.Y[t];
+  if (d.gs[c].active) {
+    for (int l = 0; l <= j; ++l) w -= d.ghc[l * K8 + c] * d.gV[(int64_t)l * mv + t];
+    d.Y[t] = w;
+  } else {
+    w = 0.0;
+  }
+  block_sum8(w * w, d.gpart + (int64_t)blk * (d.gmr + 1) * K8);
+}
+
+// end of step j (k_gm_givens per system)
+__global__ void __launch_bounds__(256) gg_givens(const GDesc* __restrict__ D, int* __restrict__ bact,
+                                                int* nactive, double tol, int j) {
+  const int bi = blockIdx.x;
+  if (!bact[bi]) return;
+  const GDesc& d = D[bi];
+  const int mr = d.gmr, np = mr + 1;
+  const int c = threadIdx.x;
+  if (c < K8) {
+    GmresScalars& q = d.gs[c];
+    if (q.active) {
+      double ss = 0.0;
+      for (int b = 0; b < d.nb_b; ++b) ss += d.gpart[((int64_t)b * np) * K8 + c];
+      const double hn = sqrt(ss);
+      double* H = d.gH;
+      for (int l = 0; l < j; ++l) {
+        double* a0 = H + ((int64_t)l * mr + j) * K8 + c;
+        double* a1 = H + ((int64_t)(l + 1) * mr + j) * K8 + c;
+        const double x0 = *a0, x1 = *a1, cs = d.gcs[l * K8 + c], sn = d.gsn[l * K8 + c];
+        *a0 = cs * x0 + sn * x1;
+        *a1 = -sn * x0 + cs * x1;
+      }
+      double* hjj = H + ((int64_t)j * mr + j) * K8 + c;
+      const double hd = *hjj;
+      const double r = hypot(hd, hn);
+      double cs = 1.0, sn = 0.0;
+      if (r > 0.0) {
+        cs = hd / r;
+        sn = hn / r;
+      }
+      *hjj = r;
+      d.gcs[j * K8 + c] = cs;
+      d.gsn[j * K8 + c] = sn;
+      const double gj = d.gg[j * K8 + c];
+      d.gg[(j + 1) * K8 + c] = -sn * gj;
+      d.gg[j * K8 + c] = cs * gj;
+      q.its += 1;
+      q.jc = j + 1;
+      q.hnext = hn;
+      q.relres = fabs(d.gg[(j + 1) * K8 + c]) / q.bnorm;
+      if (q.relres <= tol || !(hn > 0.0) || j + 1 == mr || q.its >= d.itnlim) q.active = 0;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int na = 0;
+    for (int cc = 0; cc < K8; ++cc) na += d.gs[cc].active;
+    bact[bi] = na > 0;
+    if (na) atomicAdd(nactive, na);
+  }
+}
+
+// y = R^-1 g per column over the jc steps of the cycle
+__global__ void gg_solve(const GDesc* __restrict__ D, const int* __restrict__ bran) {
+  const int bi = blockIdx.x;
+  if (!bran[bi]) return;
+  const GDesc& d = D[bi];
+  const int c = threadIdx.x;
+  if (c >= K8) return;
+  const int jc = d.gs[c].jc, mr = d.gmr;
+  for (int l = jc - 1; l >= 0; --l) {
+    double v = d.gg[l * K8 + c];
+    for (int p = l + 1; p < jc; ++p) v -= d.gH[((int64_t)l * mr + p) * K8 + c] * d.gy[p * K8 + c];
+    const double dd = d.gH[((int64_t)l * mr + l) * K8 + c];
+    d.gy[l * K8 + c] = (dd != 0.0) ? v / dd : 0.0;
+  }
+}
+
+// X += M^-1 (sum_l y_l v_l), a thread per (element, column)
+__global__ void __launch_bounds__(BT) gg_xupd(const GDesc* __restrict__ D, const int* __restrict__ off, int nb,
+                                             const int* __restrict__ bran) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  if (!bran[bi]) return;
+  const GDesc& d = D[bi];
+  const int64_t t = (int64_t)(blockIdx.x - off[bi]) * BT + threadIdx.x;
+  const int i = (int)(t / K8), c = (int)(t % K8);
+  if (i >= d.pk_ne) return;
+  const int jc = d.gs[c].jc;
+  if (jc == 0) return;
+  const int64_t mv = d.mpad * K8;
+  double z[3] = {0.0, 0.0, 0.0};
+  for (int l = 0; l < jc; ++l) {
+    const double yl = d.gy[l * K8 + c];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) z[a] += yl * d.gV[(int64_t)l * mv + (int64_t)(3 * i + a) * K8 + c];
+  }
+  const double* mi = d.pc9 + 9 * (int64_t)i;
+#pragma unroll
+  for (int b = 0; b < 3; ++b)
+    d.gX[(int64_t)(3 * i + b) * K8 + c] += mi[3 * b] * z[0] + mi[3 * b + 1] * z[1] + mi[3 * b + 2] * z[2];
+}
+
+// X (row numbering) -> FP32 high/low parts in the unknown numbering [b ne + i][8]
+__global__ void __launch_bounds__(BT) gg_split(const GDesc* __restrict__ D, const int* __restrict__ off, int nb,
+                                              const int* __restrict__ bran) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  if (!bran[bi]) return;
+  const GDesc& d = D[bi];
+  const int64_t t = (int64_t)(blockIdx.x - off[bi]) * BT + threadIdx.x;
+  const int64_t u = t / K8;
+  const int c = (int)(t % K8);
+  if (u >= d.m) return;
+  const int64_t i = u / 3, b = u % 3;
+  const double x = d.gX[t];
+  const float h = (float)x;
+  const int64_t id = (b * d.pk_ne + i) * K8 + c;
+  d.gXh[id] = h;
+  d.gXl[id] = (float)(x - (double)h);
+}
+
+// Y = b - A x per system in the float-float form of k_residp_ff (one warp per
+// element row; two CTAs of 8 rows per A*V tile of 16)
+template <int KC>
+__global__ void __launch_bounds__(256) gg_resid(const GDesc* __restrict__ D, const int* __restrict__ off, int nb,
+                                               const int* __restrict__ bran) {
+  const int tile = blockIdx.x >> 1;
+  const int bi = find_body(off, nb, tile);
+  if (!bran[bi]) return;
+  const GDesc& d = D[bi];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = (tile - off[bi]) * AVP_R + (blockIdx.x & 1) * 8 + warp;
+  if (i >= d.pk_ne) return;  // a whole warp; the kernel has no block barrier
+  const int ne = d.pk_ne;
+  float sm[3][KC], er[3][KC], lo[3][KC];
+  double acc[3][KC];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < KC; ++c) {
+      sm[a][c] = er[a][c] = lo[a][c] = 0.f;
+      acc[a][c] = 0.0;
+    }
+  for (int j0 = lane; j0 < ne; j0 += 32 * 64) {
+    const int j1 = min(ne, j0 + 32 * 64);
+    for (int j = j0; j < j1; j += 32) {
+      float g6[6];
+#pragma unroll
+      for (int cc = 0; cc < 6; ++cc) g6[cc] = d.A[pk_idx(i, cc, j, d.pk_ldp)];
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        const float* xh = d.gXh + ((int64_t)b * ne + j) * K8;
+        const float* xl = d.gXl + ((int64_t)b * ne + j) * K8;
+#pragma unroll
+        for (int c = 0; c < KC; ++c) {
+          const float hv = xh[c], lv = xl[c];
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            const float g = g6[sym6(a, b)];
+            const float p = __fmul_rn(g, hv);
+            const float pe = fmaf(g, hv, -p);
+            const float s0 = sm[a][c];
+            const float tt = __fadd_rn(s0, p);
+            const float bp = __fsub_rn(tt, s0);
+            const float e = __fadd_rn(__fsub_rn(s0, __fsub_rn(tt, bp)), __fsub_rn(p, bp));
+            sm[a][c] = tt;
+            er[a][c] = __fadd_rn(er[a][c], e);
+            lo[a][c] = fmaf(g, lv, __fadd_rn(lo[a][c], pe));
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int c = 0; c < KC; ++c) {
+        acc[a][c] += (double)sm[a][c] + ((double)er[a][c] + (double)lo[a][c]);
+        sm[a][c] = er[a][c] = lo[a][c] = 0.f;
+      }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < K8; ++c) {
+      double v = 0.0;
+      if (c < KC) v = acc[a][c];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) {
+        const int64_t row = 3 * (int64_t)i + a;
+        d.Y[row * K8 + c] = (c < d.k) ? d.b[(int64_t)c * d.m + row] - v : 0.0;
+      }
+    }
+}
+
+// x (column-major [k][n], unknown b ne + i) from X
+__global__ void __launch_bounds__(BT) gg_out(const GDesc* __restrict__ D, const int* __restrict__ off, int nb) {
+  const int bi = find_body(off, nb, blockIdx.x);
+  const GDesc& d = D[bi];
+  const int64_t t = (int64_t)(blockIdx.x - off[bi]) * BT + threadIdx.x;
+  const int64_t u = t / K8;
+  const int c = (int)(t % K8);
+  if (u >= d.m || c >= d.k) return;
+  d.x[(int64_t)c * d.n + (u % 3) * d.pk_ne + u / 3] = d.gX[t];
+}
+
+// ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
 template <typename K>
@@ -624,6 +995,7 @@ struct BatchSolver {
   int* d_off = nullptr;  // 5 tables of nb+1
   GOffsets off{};
   int* bact = nullptr;
+  int* bran = nullptr;  // GMRES: systems that run the current cycle
   int* nactive = nullptr;
   int* h_nactive = nullptr;
   int* errflag = nullptr;
@@ -633,14 +1005,16 @@ struct BatchSolver {
 
   ~BatchSolver() { release(); }
   void release() {
-    cudaFree(d_desc); cudaFree(d_off); cudaFree(bact); cudaFree(nactive); cudaFree(errflag); cudaFree(pool);
+    cudaFree(d_desc); cudaFree(d_off); cudaFree(bact); cudaFree(bran); cudaFree(nactive); cudaFree(errflag);
+    cudaFree(pool);
+    bran = nullptr;
     if (h_nactive) cudaFreeHost(h_nactive);
     d_desc = nullptr; d_off = nullptr; bact = nullptr; nactive = nullptr; errflag = nullptr; pool = nullptr;
     h_nactive = nullptr;
   }
 
   bool setup(const std::vector<BatchBody>& bodies, int k_, int maxit, const BatchTune& t, cudaStream_t st,
-             bool bicg = false, bool bj = false) {
+             bool bicg = false, bool bj = false, int gmr = 0) {
     release();
     nb = (int)bodies.size();
     k = k_;
@@ -657,7 +1031,7 @@ struct BatchSolver {
     // pool layout (bytes), every piece 256-byte aligned
     size_t bytes = 0;
     auto take = [&](size_t n) { const size_t o = bytes; bytes += (n + 255) / 256 * 256; return o; };
-    struct Offs { size_t Y, Ys, V, W, X, Vp, Zp, part, sc, bg, part2, bs, rr, tolc, pc9; };
+    struct Offs { size_t Y, Ys, V, W, X, Vp, Zp, part, sc, bg, part2, bs, rr, tolc, pc9, gm, gmf, gs; };
     std::vector<Offs> po(nb);
     const size_t o_sc0 = take(K8 * sizeof(LsqrScalars));  // zero gammas of the BiCGSTAB sweeps
     bytes_A = 0.0;
@@ -700,7 +1074,14 @@ struct BatchSolver {
         po[i].rr = take(K8 * sizeof(double));
         po[i].tolc = take(K8 * sizeof(double));
       }
-      if (bj) po[i].pc9 = take((size_t)9 * B.pk_ne * sizeof(double));
+      if (bj || gmr > 0) po[i].pc9 = take((size_t)9 * B.pk_ne * sizeof(double));
+      if (gmr > 0) {
+        const size_t mv = (size_t)d.mpad * K8;
+        po[i].gm = take(((size_t)gmr * mv + (size_t)(gmr + 1) * gmr * K8 + 5 * (size_t)(gmr + 1) * K8 + mv +
+                         (size_t)d.nb_b * (gmr + 1) * K8) * sizeof(double));
+        po[i].gmf = take(2 * (size_t)3 * B.pk_ne * K8 * sizeof(float));
+        po[i].gs = take(K8 * sizeof(GmresScalars));
+      }
       hoff_b[i + 1] = hoff_b[i] + d.nb_b;
       hoff_av[i + 1] = hoff_av[i] + d.nb_av;
       hoff_atu[i + 1] = hoff_atu[i] + d.cblocks * d.zgroups;
@@ -733,7 +1114,24 @@ struct BatchSolver {
         d.tolc = nullptr;  // set by batch_bicgstab_solve when it is given per-column tolerances
         tolc_dev[i] = (double*)(p + po[i].tolc);
       }
-      d.pc9 = bj ? (double*)(p + po[i].pc9) : nullptr;
+      d.pc9 = (bj || gmr > 0) ? (double*)(p + po[i].pc9) : nullptr;
+      d.gmr = gmr;
+      if (gmr > 0) {
+        const size_t mv = (size_t)d.mpad * K8;
+        double* g = (double*)(p + po[i].gm);
+        d.gV = g; g += (size_t)gmr * mv;
+        d.gH = g; g += (size_t)(gmr + 1) * gmr * K8;
+        d.gcs = g; g += (size_t)(gmr + 1) * K8;
+        d.gsn = g; g += (size_t)(gmr + 1) * K8;
+        d.gg = g; g += (size_t)(gmr + 1) * K8;
+        d.gy = g; g += (size_t)(gmr + 1) * K8;
+        d.ghc = g; g += (size_t)(gmr + 1) * K8;
+        d.gX = g; g += mv;
+        d.gpart = g;
+        d.gXh = (float*)(p + po[i].gmf);
+        d.gXl = d.gXh + (size_t)3 * d.pk_ne * K8;
+        d.gs = (GmresScalars*)(p + po[i].gs);
+      }
       // the pool is zeroed: the pad columns pk_ne..pk_ldp-1 of Vp stay zero
       if (!make_tensor_map_2d(&d.tm_vp, d.Vp, d.pk_ldp, 3 * K8, AVP_BC, 3 * K8, err)) return false;
     }
@@ -746,6 +1144,8 @@ struct BatchSolver {
     off.b = d_off; off.av = d_off + (nb + 1); off.atu = d_off + 2 * (nb + 1); off.red = d_off + 3 * (nb + 1);
     off.upd = d_off + 4 * (nb + 1);
     BCK(cudaMalloc(&bact, nb * sizeof(int)));
+    BCK(cudaMalloc(&bran, nb * sizeof(int)));
+    g_fill<<<cdivu(nb, 256), 256, 0, s>>>(bran, nb, 1);
     BCK(cudaMalloc(&nactive, sizeof(int)));
     BCK(cudaMallocHost(&h_nactive, sizeof(int)));
     BCK(cudaMalloc(&errflag, sizeof(int)));
@@ -1047,6 +1447,140 @@ bool batch_bicgstab_solve(const std::vector<BatchBody>& bodies, int k, double to
       st->bytes_av += 2.0 * (double)mx * 24.0 * (double)S.hd[i].pk_ne * (double)S.hd[i].pk_ne;
     }
   }
+  return true;
+}
+
+bool batch_gmres_solve(const std::vector<BatchBody>& bodies, int k, double tol, int maxit, int restart,
+                       cudaStream_t s, std::vector<int>& nit, std::vector<int>& status, BatchStats* st,
+                       std::string& err) {
+  if (restart < 1 || restart > 512) { err = "GMRES restart length must be 1..512"; return false; }
+  const int mr = restart;
+  BatchSolver S;
+  if (!S.setup(bodies, k, maxit > 0 ? maxit : 1000, BatchTune(), s, false, true, mr)) { err = S.err; return false; }
+  BCK(set_smem(gb_avp, AVP_SMEM));
+  const int nb = S.nb;
+  int itmax = 0;
+  for (const auto& d : S.hd) itmax = std::max(itmax, d.itnlim);
+  long launches = 0;
+  {  // the inverse self blocks of every system
+    int nemax = 1;
+    for (const auto& d : S.hd) nemax = std::max(nemax, d.pk_ne);
+    BCK(cudaMemsetAsync(S.nactive, 0, sizeof(int), s));
+    g_pc_blocks<<<dim3(cdivu(nemax, 128), nb), 128, 0, s>>>(S.d_desc, S.nactive);
+    int bad = 0;
+    BCK(cudaMemcpyAsync(&bad, S.nactive, sizeof(int), cudaMemcpyDeviceToHost, s));
+    BCK(cudaStreamSynchronize(s));
+    ++launches;
+    if (bad) { err = "a singular 3x3 self block: the block preconditioner cannot be formed"; return false; }
+  }
+  const unsigned nbv = S.hoff_b[nb], nav = S.hoff_av[nb];
+  gg_load<<<nbv, BT, 0, s>>>(S.d_desc, S.off.b, nb, S.bran, 1);
+  BCK(cudaMemsetAsync(S.nactive, 0, sizeof(int), s));
+  gg_begin<<<nb, 256, 0, s>>>(S.d_desc, S.bact, S.bran, S.nactive, tol, 1);
+  launches += 2;
+  BCK(cudaGetLastError());
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  for (auto& e : ev) BCK(cudaEventCreate(&e));
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  auto cleanup = [&]() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    for (auto& e : ev) if (e) cudaEventDestroy(e);
+  };
+  bool ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+  if (ok) {
+    for (int j = 0; j < mr; ++j) {
+      gg_pc<<<nbv, BT, 0, s>>>(S.d_desc, S.off.b, nb, S.bact, j);
+      if (j == 0) cudaEventRecordWithFlags(ev[0], s, cudaEventRecordExternal);
+      gb_avp<<<nav, AVP_THREADS, AVP_SMEM, s>>>(S.d_desc, S.off.av, nb, S.bact, S.errflag, 0);
+      if (j == 0) cudaEventRecordWithFlags(ev[1], s, cudaEventRecordExternal);
+      for (int pass = 0; pass < 2; ++pass) {
+        gg_dots<<<nbv, BT, 0, s>>>(S.d_desc, S.off.b, nb, S.bact, j);
+        gg_hred<<<nb, 256, 0, s>>>(S.d_desc, S.bact, j, pass);
+        gg_orth<<<nbv, BT, 0, s>>>(S.d_desc, S.off.b, nb, S.bact, j);
+      }
+      cudaMemsetAsync(S.nactive, 0, sizeof(int), s);
+      gg_givens<<<nb, 256, 0, s>>>(S.d_desc, S.bact, S.nactive, tol, j);
+    }
+    ok = cudaStreamEndCapture(s, &graph) == cudaSuccess;
+  }
+  if (ok) ok = cudaGraphInstantiate(&gexec, graph, 0) == cudaSuccess;
+  if (!ok) {
+    err = std::string("batch GMRES graph capture: ") + cudaGetErrorString(cudaGetLastError());
+    cleanup();
+    return false;
+  }
+  double av_ms = 0.0, timed_bytes = 0.0;
+  long nav_t = 0, cycles = 0;
+  std::vector<int> hbran(nb, 0);
+  for (int cyc = 0; cyc < itmax + 2; ++cyc) {
+    if (cudaMemcpyAsync(S.h_nactive, S.nactive, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(hbran.data(), S.bran, nb * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) { ok = false; break; }
+    if (*S.h_nactive == 0) break;
+    // algorithmic bytes of the cycle's first (timed) sweep: the systems in it
+    double cyc_bytes = 0.0;
+    for (int i = 0; i < nb; ++i)
+      if (hbran[i]) cyc_bytes += 24.0 * (double)S.hd[i].pk_ne * (double)S.hd[i].pk_ne;
+    if (cudaGraphLaunch(gexec, s) != cudaSuccess) { ok = false; break; }
+    launches += 9L * mr;
+    ++cycles;
+    // iterate update, float-float true residual and the start of the next cycle
+    gg_solve<<<nb, 32, 0, s>>>(S.d_desc, S.bran);
+    gg_xupd<<<nbv, BT, 0, s>>>(S.d_desc, S.off.b, nb, S.bran);
+    gg_split<<<nbv, BT, 0, s>>>(S.d_desc, S.off.b, nb, S.bran);
+    if (k <= 6) gg_resid<6><<<2 * nav, 256, 0, s>>>(S.d_desc, S.off.av, nb, S.bran);
+    else gg_resid<8><<<2 * nav, 256, 0, s>>>(S.d_desc, S.off.av, nb, S.bran);
+    gg_load<<<nbv, BT, 0, s>>>(S.d_desc, S.off.b, nb, S.bran, 0);
+    cudaMemsetAsync(S.nactive, 0, sizeof(int), s);
+    gg_begin<<<nb, 256, 0, s>>>(S.d_desc, S.bact, S.bran, S.nactive, tol, 0);
+    launches += 6;
+    float a = 0.f;
+    if (cudaEventSynchronize(ev[1]) == cudaSuccess && cudaEventElapsedTime(&a, ev[0], ev[1]) == cudaSuccess) {
+      av_ms += a;
+      ++nav_t;
+      timed_bytes += cyc_bytes;
+    }
+    (void)cudaGetLastError();
+  }
+  cleanup();
+  if (!ok) {
+    err = std::string("batch GMRES cycles: ") + cudaGetErrorString(cudaGetLastError());
+    return false;
+  }
+  gg_out<<<nbv, BT, 0, s>>>(S.d_desc, S.off.b, nb);
+  ++launches;
+  std::vector<GmresScalars> hs((size_t)nb * K8);
+  for (int i = 0; i < nb; ++i)
+    BCK(cudaMemcpyAsync(hs.data() + (size_t)i * K8, S.hd[i].gs, K8 * sizeof(GmresScalars), cudaMemcpyDeviceToHost,
+                        s));
+  int hflag = 0;
+  BCK(cudaMemcpyAsync(&hflag, S.errflag, sizeof(int), cudaMemcpyDeviceToHost, s));
+  BCK(cudaStreamSynchronize(s));
+  BCK(cudaGetLastError());
+  if (hflag) { err = "a bounded barrier wait in a batched sweep gave up"; return false; }
+  nit.assign((size_t)nb * k, 0);
+  status.assign((size_t)nb * k, 0);
+  long maxits = 0;
+  for (int i = 0; i < nb; ++i)
+    for (int c = 0; c < k; ++c) {
+      const GmresScalars& q = hs[(size_t)i * K8 + c];
+      nit[(size_t)i * k + c] = q.its;
+      status[(size_t)i * k + c] = q.status < 0 ? 1 : q.status;
+      maxits = std::max<long>(maxits, q.its);
+    }
+  if (st) {
+    // the first A*V sweep of every cycle is timed (live events), with the
+    // algorithmic bytes of the systems it covered
+    st->av_ms += av_ms;
+    st->av_launches += nav_t;
+    st->launches += launches;
+    st->iterations = std::max(st->iterations, maxits);
+    st->av_rows = AVP_R;
+    st->bytes_av += timed_bytes;
+  }
+  if (st) st->cycles += cycles;
   return true;
 }
 

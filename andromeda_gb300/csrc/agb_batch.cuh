@@ -31,10 +31,12 @@ struct BatchStats {
   long av_launches = 0, atu_launches = 0;
   long launches = 0;                 // all kernels launched
   long iterations = 0;               // graph iterations run (max over systems)
-  double bytes_av = 0.0;             // algorithmic bytes of all A*V launches: sum over systems of
-                                     // (iterations while active) x 6 pk_ne^2 x 4
+  double bytes_av = 0.0;             // algorithmic bytes of the timed A*V launches (LSQR, BiCGSTAB: all of
+                                     // them; GMRES: the first of every cycle): sum over the systems
+                                     // each covered of 6 pk_ne^2 x 4
   int av_rows = 0, atu_rs = 0, atu_rows = 0;  // tile shapes used: block rows per A*V CTA, per A^T*U
                                               // stage, per A^T*U row group
+  long cycles = 0;                   // GMRES restart cycles run
 };
 
 // Solves A_i x_i = b_i (least squares) for all systems with the reference's
@@ -56,6 +58,16 @@ bool batch_lsqr_solve(const std::vector<BatchBody>& bodies, int k, double eps, i
 bool batch_bicgstab_solve(const std::vector<BatchBody>& bodies, int k, double tol, int maxit, cudaStream_t s,
                           std::vector<int>& nit, std::vector<int>& status, BatchStats* st, std::string& err,
                           const std::vector<double>* tol_cols = nullptr);
+
+// Restarted GMRES(restart) with the 3x3 self-block right preconditioner on all
+// systems together (as DenseLsqr::gmres per system): x0 = 0, stop at the FP64-
+// accurate true residual ||b - A x|| <= tol ||b|| (formed in float-float form
+// at the end of every cycle) or maxit Arnoldi steps (0: 1000).  b, x as
+// batch_lsqr_solve.  status per column: 0 converged, 1 iteration limit, 3 a
+// cycle without a 10 % gain of the true residual.
+bool batch_gmres_solve(const std::vector<BatchBody>& bodies, int k, double tol, int maxit, int restart,
+                       cudaStream_t s, std::vector<int>& nit, std::vector<int>& status, BatchStats* st,
+                       std::string& err);
 
 // Times the candidate row groups of the A^T*U sweep on these systems (a few
 // launches each, CUDA events) and returns the fastest; `report` lists the

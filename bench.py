@@ -67,8 +67,9 @@ def parse():
                     help="sphere: one level-5 sphere (default); batch: the many-body superellipsoid set")
     ap.add_argument("--bodies", type=int, default=512, help="batch workload: number of bodies")
     ap.add_argument("--fp64-sample", type=int, default=6, help="batch workload: bodies solved on the FP64 path")
-    ap.add_argument("--batch-eps", type=float, default=3e-8,
-                    help="batch workload: LSQR eps (3e-8 keeps every sampled body within 1e-6 of FP64)")
+    ap.add_argument("--batch-eps", type=float, default=None,
+                    help="batch and surrogate: solver tolerance (default 1e-7 for GMRES, 3e-8 for LSQR, which "
+                         "keeps every sampled body within 1e-6 of FP64)")
     ap.add_argument("--no-autotune", action="store_true", help="batch workload: default tile shapes")
     ap.add_argument("--train-bodies", type=int, default=20000, help="surrogate: BEM tensors to train on")
     ap.add_argument("--sur-elements", type=int, default=500, help="surrogate: triangles per training body")
@@ -92,7 +93,11 @@ def parse():
     ap.add_argument("--laplace-eps", type=float, default=1e-12, help="laplace: LSQR eps")
     args = ap.parse_args()
     if args.solver is None:
-        args.solver = "lsqr_block" if args.workload == "batch" else "gmres"
+        args.solver = "gmres"
+    if args.batch_eps is None:
+        # GMRES stops on the true residual (1e-7 leaves 2-3e-7 on the sampled
+        # bodies); LSQR's stopping test needs 3e-8 for every body within 1e-6
+        args.batch_eps = 1e-7 if args.solver == "gmres" else 3e-8
     return args
 
 
@@ -454,8 +459,10 @@ def run_batch(args, rank, world, local):
                         "h2d_bytes_per_step": int(sum(m["xyz"].nbytes + m["etype"].nbytes + m["con"].nbytes +
                                                       m["bcid"].nbytes for m in meshes)),
                         "d2h_bytes_per_step": int(args.bodies * (36 * 8 + 12 * 4))},
-                "roofline": {"bound": "hbm", "kernel": "g_avp (batched LSQR A*V sweep over the packed symmetric "
-                                                       "3x3 blocks, FP32 by TMA, all bodies in one launch)",
+                "roofline": {"bound": "hbm", "kernel": ("gb_avp (batched GMRES A M^-1 v sweep" if args.solver == "gmres"
+                                                        else "g_avp (batched LSQR A*V sweep") +
+                                                       " over the packed symmetric 3x3 blocks, FP32 by TMA, all bodies "
+                                                       "in one launch)",
                              "achieved": av_gbs, "peak": peak, "unit": "GB/s",
                              "frac": av_gbs / peak if av_gbs else None, "traffic": None, "peak_source": peak_kind,
                              "other_sweep": {"kernel": "g_atup (batched A^T*U, packed)", "achieved": atu_gbs,
@@ -662,8 +669,10 @@ def run_surrogate(args):
     where the members disagree), and a random audit fraction is re-solved by
     the BEM."""
     import numpy as np
+    import andromeda_gb300 as A
     from andromeda_gb300 import surrogate as S
-    bem = dict(n_elem=args.sur_elements, outer_level=2, outer_radius=200.0, eps=args.batch_eps)
+    bem = dict(n_elem=args.sur_elements, outer_level=2, outer_radius=200.0, eps=args.batch_eps,
+               solver=solver_id(A, args.solver))
     t0 = time.perf_counter()
     P = S.sample_params(args.train_bodies, seed=20260101)
     R, st_bem = S.bem_tensors(P, **bem)
@@ -709,7 +718,8 @@ def run_surrogate(args):
             "data": "synthetic (shapes b,c~U(0.2,1), e1,e2~U(0.3,1.8), seeds 20260101 / 99)",
             "config": {"workload": f"{args.queries} queries; {nm} networks trained on {ntr} BEM tensors of the "
                                    f"many-body workload's shapes ({args.sur_elements}-triangle superellipsoids in L2 "
-                                   f"containers r=200, batched mixed BEM, LSQR eps {args.batch_eps:g}); {ncal} "
+                                   f"containers r=200, batched mixed BEM, {solver_text(args.solver, args.batch_eps)}); "
+                                   f"{ncal} "
                                    f"held-out tensors calibrate the agreement threshold",
                        "epochs": args.epochs, "batch": 512, "members": nm},
             "bem_training_set": {"bodies": len(P), "bem_solves_per_s": bem_rate, "host_s": t1 - t0},

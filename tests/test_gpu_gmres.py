@@ -121,3 +121,28 @@ def test_float_float_residual_matches_fp64(agb):
         print(key, list(n0), list(n1), _rel(R0, R1))
         assert _rel(R0, R1) < bar[key], key
         assert np.all(np.abs(np.asarray(n0) - np.asarray(n1)) <= 2), (key, n0, n1)
+
+
+def test_batch_gmres_config4_bodies(agb):
+    """The batched GMRES (every step one launch over all bodies) on six bodies
+    of the 512-body benchmark set (seed 20260101, r = 200 level-2 containers,
+    484-8010 triangles) at tol 1e-7: every tensor within 1e-6 of the body's
+    FP64 tensor (FP64 assembly + FP64 LSQR to 1e-10) and of the single-body
+    GMRES tensor to 1e-7 (the same recurrence; partial sums grouped by other
+    tiles)."""
+    meshes, params = M.batch_bodies()
+    order = np.argsort(params[:, 4])
+    pick = [int(order[j]) for j in np.linspace(0, len(order) - 1, 6).round().astype(int)]
+    sel = [meshes[i] for i in pick]
+    R, nit, istop, st = agb.batch_resistance(sel, eps=1e-7, solver=agb.SOLVER_GMRES)
+    print("batched GMRES steps", nit.tolist(), "status", istop.tolist())
+    assert np.all(istop == 0)
+    for j, m in enumerate(sel):
+        C = _ctx(agb, m)
+        R64, _, _ = C.resistance_tensor(agb.FP64, 1, 2, eps=1e-10)
+        C.set_solver(agb.SOLVER_GMRES)
+        Rs, ns, _ = C.resistance_tensor(agb.MIXED, 1, 2, eps=1e-7)
+        C.close()
+        print(j, int(params[pick[j], 4]), "vs FP64", _rel(R[j], R64), "vs single", _rel(R[j], Rs), list(ns))
+        assert _rel(R[j], R64) < 1e-6, j
+        assert _rel(R[j], Rs) < 1e-7, j
