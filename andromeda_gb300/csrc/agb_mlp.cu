@@ -239,36 +239,45 @@ static void gemm(bool split, int M, int N, int K, const float* A, int lda, const
 //     no-swizzle K-major core-matrix layout (8 rows x 16 B per core matrix,
 //     [row/8][k/8][8][8]), 64 KB each;
 //   * the weights, pre-split and pre-packed in the same layout chunk by chunk
-//     (32 k per chunk; [layer chunk][hi/lo][n/8][k/8][8][8]), stream through a
-//     two-slot ring by one bulk copy per chunk (the copy warp); a slot is
-//     released by tcgen05.commit of the products that read it;
+//     (16 k per chunk, one tcgen05 K step; [layer chunk][hi/lo][n/8][k/8][8][8]),
+//     stream from L2 through a five-slot ring of 16 KB slots, one bulk copy per
+//     chunk (the copy warp); a slot is released by tcgen05.commit of the
+//     products that read it.  Four chunks in flight hide the L2 latency behind
+//     the products of the chunk in use;
 //   * one thread of the issuing warp issues tcgen05.mma (M = 128, N = 256 or 32,
-//     K = 16; the three split products hi*hi, hi*lo, lo*hi per k step) into one
+//     K = 16; the three split products hi*hi, hi*lo, lo*hi per chunk) into one
 //     of two 128 x 256 FP32 accumulators in tensor memory (layer l into (l-1)&1);
-//     chunk j of a layer waits only for the 32 activation columns of chunk j, so
-//     a layer's products start while the previous epilogue writes later chunks;
-//   * 16 epilogue warps read the accumulator (tcgen05.ld, warp w: lanes
-//     32 (w%4) ..., columns 64 (w/4) ...), add the bias, apply SiLU and write the
-//     next layer's hi/lo activations chunk by chunk; layer 4 adds the bias,
-//     de-normalises and stores.
+//     the two chunks of a 32-column activation block wait only for that block,
+//     so a layer's products follow the previous layer's epilogue block by block;
+//   * 16 epilogue warps read the accumulator block by block, all of them on the
+//     same 32-column block at a time (warp w: tensor-memory lanes 32 (w%4) ...,
+//     columns 8 (w/4) ... of the block), the load of the next block in flight
+//     while the current one is processed: bias, SiLU and the hi/lo split of the
+//     next layer's activations; layer 4 adds the bias, de-normalises and stores.
 // Every wait is bounded (error flag); the tensor memory is freed on every path.
 // ---------------------------------------------------------------------------
-constexpr int TC_M = 128, TC_H = 256, TC_NOUT = 32, TC_KC = 32;
-constexpr int TC_EPI = 16;                    // epilogue warps: 4 per TMEM lane group, 64 columns each
+constexpr int TC_M = 128, TC_H = 256, TC_NOUT = 32, TC_KC = 16, TC_AB = 32;
+constexpr int TC_NSLOT = 5;                   // weight ring depth
+constexpr int TC_EPI = 16;                    // epilogue warps: 4 per TMEM lane group, 8 columns of a block each
 constexpr int TC_THREADS = (TC_EPI + 2) * 32;  // + 1 copy warp + 1 issuing warp
 constexpr size_t TC_H_BYTES = (size_t)TC_M * TC_H * 2;             // one half (hi or lo) of the activations
-constexpr size_t TC_SLOT = 2ull * TC_H * TC_KC * 2;                  // largest chunk: N 256 x K 32, hi + lo
-constexpr size_t TC_SMEM = 2 * TC_H_BYTES + 2 * TC_SLOT;             // 192 KB (+ 4 KB static)
-// packed weights (bytes): layer 1 one chunk (N 256, K 16), layers 2-3 eight chunks (N 256, K 32),
-// layer 4 eight chunks (N 32, K 32); hi then lo inside a chunk
-constexpr int64_t TC_C1 = 2ll * TC_H * 16 * 2, TC_C23 = 2ll * TC_H * TC_KC * 2, TC_C4 = 2ll * TC_NOUT * TC_KC * 2;
-constexpr int64_t TC_L2 = TC_C1, TC_L3 = TC_L2 + 8 * TC_C23, TC_L4 = TC_L3 + 8 * TC_C23, TC_WBYTES = TC_L4 + 8 * TC_C4;
-constexpr int TC_CHUNKS = 1 + 3 * 8;
+constexpr size_t TC_SLOT = 2ull * TC_H * TC_KC * 2;                  // largest chunk: N 256 x K 16, hi + lo
+constexpr size_t TC_SMEM = 2 * TC_H_BYTES + TC_NSLOT * TC_SLOT;      // 208 KB (+ 4 KB static)
+// packed weights (bytes): layer 1 one chunk (N 256, K 16), layers 2-3 sixteen chunks (N 256, K 16),
+// layer 4 sixteen chunks (N 32, K 16); hi then lo inside a chunk
+constexpr int TC_LCH = TC_H / TC_KC;  // chunks of layers 2-4
+constexpr int64_t TC_C1 = 2ll * TC_H * TC_KC * 2, TC_C23 = 2ll * TC_H * TC_KC * 2, TC_C4 = 2ll * TC_NOUT * TC_KC * 2;
+constexpr int64_t TC_L2 = TC_C1, TC_L3 = TC_L2 + TC_LCH * TC_C23, TC_L4 = TC_L3 + TC_LCH * TC_C23,
+                  TC_WBYTES = TC_L4 + TC_LCH * TC_C4;
+constexpr int TC_CHUNKS = 1 + 3 * TC_LCH;
 
 __device__ __forceinline__ int64_t tc_chunk_off(int c) {
-  return c == 0 ? 0 : c <= 8 ? TC_L2 + (c - 1) * TC_C23 : c <= 16 ? TC_L3 + (c - 9) * TC_C23 : TC_L4 + (c - 17) * TC_C4;
+  return c == 0 ? 0
+         : c <= TC_LCH     ? TC_L2 + (c - 1) * TC_C23
+         : c <= 2 * TC_LCH ? TC_L3 + (c - 1 - TC_LCH) * TC_C23
+                           : TC_L4 + (c - 1 - 2 * TC_LCH) * TC_C4;
 }
-__device__ __forceinline__ int64_t tc_chunk_bytes(int c) { return c == 0 ? TC_C1 : c <= 16 ? TC_C23 : TC_C4; }
+__device__ __forceinline__ int64_t tc_chunk_bytes(int c) { return c == 0 ? TC_C1 : c <= 2 * TC_LCH ? TC_C23 : TC_C4; }
 
 // one packed element per thread: (layer, hi/lo, n, k) -> chunk, core matrix, row, column
 __global__ void k_mlp_pack_tc(const float* __restrict__ P, int nin, int nh, int nout, int64_t o0, int64_t o2,
@@ -282,13 +291,13 @@ __global__ void k_mlp_pack_tc(const float* __restrict__ P, int nin, int nh, int 
   else if (b < TC_L3) { layer = 2; c = (int)((b - TC_L2) / TC_C23); cb = (b - TC_L2) % TC_C23; }
   else if (b < TC_L4) { layer = 3; c = (int)((b - TC_L3) / TC_C23); cb = (b - TC_L3) % TC_C23; }
   else { layer = 4; c = (int)((b - TC_L4) / TC_C4); cb = (b - TC_L4) % TC_C4; }
-  const int N = layer == 4 ? TC_NOUT : TC_H, KC = layer == 1 ? 16 : TC_KC;
-  const int64_t half = (int64_t)N * KC * 2;
+  const int N = layer == 4 ? TC_NOUT : TC_H;
+  const int64_t half = (int64_t)N * TC_KC * 2;
   const int hl = (int)(cb / half);
   const int64_t e = (cb % half) / 2;  // element within the half: [n/8][k/8][8][8]
   const int core = (int)(e / 64), within = (int)(e % 64);
-  const int ng = core / (KC / 8), kc = core % (KC / 8);
-  const int n = ng * 8 + within / 8, k = c * KC + kc * 8 + within % 8;
+  const int ng = core / (TC_KC / 8), kc = core % (TC_KC / 8);
+  const int n = ng * 8 + within / 8, k = c * TC_KC + kc * 8 + within % 8;
   const float* W = P + (layer == 1 ? o0 : layer == 2 ? o2 : layer == 3 ? o4 : o6);
   const int kin = layer == 1 ? nin : nh, nreal = layer == 4 ? nout : nh;
   const float v = (n < nreal && k < kin) ? W[(int64_t)n * kin + k] : 0.f;
@@ -340,20 +349,37 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, int* err
     }
   }
 }
-__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+// 8 accumulator columns of this warp's 32 lanes: issue the load; tc_ld8_wait makes
+// the registers valid (they are operands of the wait, so no use moves above it)
+__device__ __forceinline__ void tc_ld8_issue(uint32_t taddr, uint32_t (&r)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
+__device__ __forceinline__ void tc_ld8_wait(uint32_t (&r)[8]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7])
+               :
+               : "memory");
 }
 // byte offset of (row, k) in a [row/8][k/8][8][8] BF16 half with 32 core matrices per 8-row group
 __device__ __forceinline__ uint32_t tc_hoff(int row, int k) {
   return (uint32_t)(((row >> 3) * (TC_H / 8) + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+// bias + SiLU of 8 accumulator values, split into BF16 hi and lo, stored as one
+// 16-byte core-matrix row each
+__device__ __forceinline__ void tc_act8(const uint32_t (&r)[8], const float* bias, unsigned char* hh, unsigned char* hl) {
+  __align__(16) __nv_bfloat162 hv[4], lv[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const float z0 = silu_f(__uint_as_float(r[2 * j]) + bias[2 * j]);
+    const float z1 = silu_f(__uint_as_float(r[2 * j + 1]) + bias[2 * j + 1]);
+    hv[j] = __floats2bfloat162_rn(z0, z1);
+    const float2 h = __bfloat1622float2(hv[j]);
+    lv[j] = __floats2bfloat162_rn(z0 - h.x, z1 - h.y);
+  }
+  *reinterpret_cast<uint4*>(hh) = *reinterpret_cast<const uint4*>(hv);
+  *reinterpret_cast<uint4*>(hl) = *reinterpret_cast<const uint4*>(lv);
 }
 
 __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, int nout, const float* __restrict__ X,
@@ -367,8 +393,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
   unsigned char* Hl = tc_smem + TC_H_BYTES;
   unsigned char* Wslot = tc_smem + 2 * TC_H_BYTES;
   // full/empty: the weight ring; accb[b]: accumulator b complete; hready[j]: the 32
-  // activation columns of chunk j written by the epilogue (4 warps arrive)
-  __shared__ __align__(8) uint64_t full[2], empty[2], accb[2], hready[TC_H / TC_KC];
+  // activation columns of block j written by the epilogue (all 16 warps arrive)
+  __shared__ __align__(8) uint64_t full[TC_NSLOT], empty[TC_NSLOT], accb[2], hready[TC_H / TC_AB];
   __shared__ uint32_t tmem_base;
   __shared__ float sbias[3][TC_H], sout[3][TC_NOUT];  // biases of layers 1-3; layer-4 bias, y_std, y_mean
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -376,13 +402,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
   const float* xm = norm;
   const float* xs = norm + nin;
   if (threadIdx.x == 0) {
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < TC_NSLOT; ++i) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32_mlp(&full[i])) : "memory");
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32_mlp(&empty[i])) : "memory");
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32_mlp(&accb[i])) : "memory");
     }
-    for (int i = 0; i < TC_H / TC_KC; ++i)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(smem_u32_mlp(&hready[i])) : "memory");
+    for (int i = 0; i < 2; ++i)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32_mlp(&accb[i])) : "memory");
+    for (int i = 0; i < TC_H / TC_AB; ++i)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32_mlp(&hready[i])), "r"(TC_EPI) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {  // all 512 columns of tensor memory: two 128 x 256 FP32 accumulators
@@ -415,12 +442,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
-  if (warp == TC_EPI) {  // weight chunks: one bulk copy each into the two-slot ring
+  if (warp == TC_EPI) {  // weight chunks: one bulk copy each into the ring
     if (lane == 0) {
       int issued = 0;
       for (int c = 0; c < TC_CHUNKS; ++c) {
-        const int s = c & 1;
-        if (c >= 2 && !tc_wait(&empty[s], ((c >> 1) - 1) & 1, errflag)) break;
+        const int s = c % TC_NSLOT;
+        if (c >= TC_NSLOT && !tc_wait(&empty[s], ((c / TC_NSLOT) - 1) & 1, errflag)) break;
         ++issued;
         const uint32_t bytes = (uint32_t)tc_chunk_bytes(c);
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32_mlp(&full[s])), "r"(bytes)
@@ -431,11 +458,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
                      : "memory");
       }
       // the last copy into each slot has landed before the CTA may exit (on the normal
-      // path the MMA issuer already waited for both; after a wait that gave up this
-      // keeps the CTA alive until its own copies are done)
-      for (int c = issued > 2 ? issued - 2 : 0; c < issued; ++c) {
+      // path the MMA issuer already waited for all of them; after a wait that gave up
+      // this keeps the CTA alive until its own copies are done)
+      for (int c = issued > TC_NSLOT ? issued - TC_NSLOT : 0; c < issued; ++c) {
         uint32_t tries = 0;
-        while (!tc_wait_once(&full[c & 1], (c >> 1) & 1))
+        while (!tc_wait_once(&full[c % TC_NSLOT], (c / TC_NSLOT) & 1))
           if (++tries > (1u << 22)) {
             atomicExch(errflag, 1);
             break;
@@ -443,81 +470,78 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
       }
     }
   } else if (warp == TC_EPI + 1) {  // products: layer l accumulates into buffer (l-1)&1; chunk j of a layer
-                           // waits for the activation columns of chunk j from the previous epilogue
+                                    // waits for activation block j/2 from the previous epilogue
     if (lane == 0) {
       bool ok = true;
       for (int layer = 1, c = 0; layer <= 4 && ok; ++layer) {
-        const int nchunks = layer == 1 ? 1 : 8;
-        const int N = layer == 4 ? TC_NOUT : TC_H, KC = layer == 1 ? 16 : TC_KC;
+        const int nchunks = layer == 1 ? 1 : TC_LCH;
+        const int N = layer == 4 ? TC_NOUT : TC_H;
         const uint32_t idesc = tc_idesc(N);
         const uint32_t tacc = tmem + (uint32_t)(((layer - 1) & 1) * TC_H);
         for (int j = 0; j < nchunks; ++j, ++c) {
-          const int s = c & 1;
-          if (layer > 1 && !tc_wait(&hready[j], (layer - 2) & 1, errflag)) { ok = false; break; }
-          if (!tc_wait(&full[s], (c >> 1) & 1, errflag)) { ok = false; break; }
+          const int s = c % TC_NSLOT;
+          if (layer > 1 && (j & 1) == 0 && !tc_wait(&hready[j >> 1], (layer - 2) & 1, errflag)) { ok = false; break; }
+          if (!tc_wait(&full[s], (c / TC_NSLOT) & 1, errflag)) { ok = false; break; }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t bh = smem_u32_mlp(Wslot + s * TC_SLOT);
-          const uint32_t bl = bh + (uint32_t)N * KC * 2;
-          const uint32_t sbo_b = (uint32_t)(KC / 8) * 128;
-          for (int ks = 0; ks < KC / 16; ++ks) {
-            const int k0 = j * KC + ks * 16;  // activation column of this k step
-            const uint64_t ah = tc_sdesc(smem_u32_mlp(Hh) + (uint32_t)(k0 / 8) * 128, (TC_H / 8) * 128);
-            const uint64_t al = tc_sdesc(smem_u32_mlp(Hl) + (uint32_t)(k0 / 8) * 128, (TC_H / 8) * 128);
-            const uint64_t dbh = tc_sdesc(bh + ks * 256, sbo_b), dbl = tc_sdesc(bl + ks * 256, sbo_b);
-            tc_mma(tacc, ah, dbh, idesc, (j | ks) != 0);
-            tc_mma(tacc, ah, dbl, idesc, 1);
-            tc_mma(tacc, al, dbh, idesc, 1);
-          }
+          const uint32_t bl = bh + (uint32_t)N * TC_KC * 2;
+          const uint32_t sbo_b = (uint32_t)(TC_KC / 8) * 128;
+          const int k0 = j * TC_KC;  // activation column of this chunk
+          const uint64_t ah = tc_sdesc(smem_u32_mlp(Hh) + (uint32_t)(k0 / 8) * 128, (TC_H / 8) * 128);
+          const uint64_t al = tc_sdesc(smem_u32_mlp(Hl) + (uint32_t)(k0 / 8) * 128, (TC_H / 8) * 128);
+          const uint64_t dbh = tc_sdesc(bh, sbo_b), dbl = tc_sdesc(bl, sbo_b);
+          tc_mma(tacc, ah, dbh, idesc, j != 0);
+          tc_mma(tacc, ah, dbl, idesc, 1);
+          tc_mma(tacc, al, dbh, idesc, 1);
           tc_commit(&empty[s]);  // the slot is free once these products are done
         }
         tc_commit(&accb[(layer - 1) & 1]);  // also on a failed wait, so the epilogue warps never wait for nothing
       }
     }
-  } else {  // epilogue warps: warp w reads TMEM lanes 32 (w%4) ... and columns 64 (w/4) ...
-    const int lg = warp & 3, colq = warp >> 2;
+  } else {  // epilogue warps: warp w reads TMEM lanes 32 (w%4) ... and columns 8 (w/4) ... of each block
+    const int lg = warp & 3, sub = warp >> 2;
     const int row = lg * 32 + lane;
     for (int layer = 1; layer <= 4; ++layer) {
       const int b = (layer - 1) & 1;
       if (!tc_wait(&accb[b], ((layer - 1) >> 1) & 1, errflag)) break;
       __syncwarp();
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t tl = tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)(b * TC_H);
+      const uint32_t tl = tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)(b * TC_H) + (uint32_t)(sub * 8);
       if (layer < 4) {
-        const float* bias = sbias[layer - 1];
-        for (int jc = colq * 2; jc < colq * 2 + 2; ++jc) {  // activation chunks of 32 columns, in order
-          for (int c0 = jc * TC_KC; c0 < jc * TC_KC + TC_KC; c0 += 16) {
-            float v[16];
-            tc_ld16(tl + (uint32_t)c0, v);
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-              __align__(16) __nv_bfloat16 hv[8], lv[8];
-#pragma unroll
-              for (int j = 0; j < 8; ++j) {
-                const float z = silu_f(v[h * 8 + j] + bias[c0 + h * 8 + j]);
-                hv[j] = __float2bfloat16_rn(z);
-                lv[j] = __float2bfloat16_rn(z - __bfloat162float(hv[j]));
-              }
-              const uint32_t off = tc_hoff(row, c0 + h * 8);
-              *reinterpret_cast<uint4*>(Hh + off) = *reinterpret_cast<const uint4*>(hv);
-              *reinterpret_cast<uint4*>(Hl + off) = *reinterpret_cast<const uint4*>(lv);
-            }
-          }
-          // chunk jc is written by this warp's 32 rows: publish it to the next layer's products
+        const float* bias = sbias[layer - 1] + sub * 8;
+        uint32_t ra[8], rb[8];
+        tc_ld8_issue(tl, ra);
+        tc_ld8_wait(ra);
+#pragma unroll 1
+        for (int jb = 0; jb < TC_H / TC_AB; jb += 2) {  // two blocks per trip: ra holds block jb, rb block jb+1
+          tc_ld8_issue(tl + (uint32_t)((jb + 1) * TC_AB), rb);
+          tc_act8(ra, bias + jb * TC_AB, Hh + tc_hoff(row, jb * TC_AB + sub * 8), Hl + tc_hoff(row, jb * TC_AB + sub * 8));
+          // block jb is written by all 16 warps: publish it to the next layer's products
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
           __syncwarp();
-          if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32_mlp(&hready[jc])) : "memory");
+          if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32_mlp(&hready[jb])) : "memory");
+          tc_ld8_wait(rb);
+          if (jb + 2 < TC_H / TC_AB) tc_ld8_issue(tl + (uint32_t)((jb + 2) * TC_AB), ra);
+          tc_act8(rb, bias + (jb + 1) * TC_AB, Hh + tc_hoff(row, (jb + 1) * TC_AB + sub * 8),
+                  Hl + tc_hoff(row, (jb + 1) * TC_AB + sub * 8));
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncwarp();
+          if (lane == 0)
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32_mlp(&hready[jb + 1])) : "memory");
+          if (jb + 2 < TC_H / TC_AB) tc_ld8_wait(ra);
         }
-      } else if (colq == 0) {
-        const float* bias = sout[0];
+      } else {
+        uint32_t r[8];
+        tc_ld8_issue(tl, r);
+        tc_ld8_wait(r);
         const int g = q0 + row;
-        for (int c0 = 0; c0 < TC_NOUT; c0 += 16) {
-          float v[16];
-          tc_ld16(tl + (uint32_t)c0, v);
+        if (g < n) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int col = c0 + j;
-            if (col < nout && g < n) Y[(int64_t)g * nout + col] = (v[j] + bias[col]) * sout[1][col] + sout[2][col];
+          for (int j = 0; j < 8; ++j) {
+            const int col = sub * 8 + j;
+            if (col < nout) Y[(int64_t)g * nout + col] = (__uint_as_float(r[j]) + sout[0][col]) * sout[1][col] + sout[2][col];
           }
         }
       }

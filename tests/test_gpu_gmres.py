@@ -88,11 +88,6 @@ def test_gmres_refusals(agb):
         C.resistance_tensor(agb.FP64, 1, 2, eps=1e-8)  # the FP64 system is not packed
     with pytest.raises(agb.AgbError):
         C.set_solver(agb.SOLVER_GMRES, restart=0)
-    ctx = agb.Context(0)
-    ctx.set_solver(agb.SOLVER_GMRES)
-    with pytest.raises(agb.AgbError):
-        agb.batch_resistance([m], eps=1e-7, ctx=ctx)
-    ctx.close()
     C.close()
 
 
