@@ -74,6 +74,7 @@ struct agb_context {
   int64_t lda = 0;
   int m = 0, n = 0;
   double* d_q = nullptr;
+  bool q_ready = false;  // d_q holds lsqr_precon's column scaling of the assembled system
   bool assembled = false;
   DenseLsqr lsqr;
   // scratch
@@ -428,6 +429,16 @@ __global__ void k_axpy(int64_t n, const double* __restrict__ d, double* __restri
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) x[t] += d[t];
 }
+// lsqr_precon's column scaling q of the assembled system, formed on first use
+int ensure_q(agb_context* c) {
+  if (c->q_ready) return AGB_OK;
+  if (!c->lsqr.precon(c->d_A, c->d_q)) return fail(c, AGB_ERR_CUDA, c->lsqr.err);
+  c->nlaunch += 2;
+  // complete before any reader outside the context stream (agb_get_system copies on the default stream)
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  c->q_ready = true;
+  return AGB_OK;
+}
 int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int refine, int* nit, int* istop,
              bool x0_zero) {
   if ((!c->lsqr.A && !c->lsqr.mf) || c->lsqr.k != nrhs) {
@@ -461,7 +472,7 @@ int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int r
       CUDA_OR_FAIL(c, ensure(c->d_res, c->cap_res, (size_t)nrhs * m));
       CUDA_OR_FAIL(c, ensure(c->d_dx, c->cap_dx, (size_t)nrhs * n));
       for (int pass = 0; pass <= kBicgRestarts; ++pass) {
-        if (!c->lsqr.residual(c->d_rhs, d_x, c->d_q, c->d_res)) return fail(c, AGB_ERR_CUDA, "residual: " + c->lsqr.err);
+        if (!c->lsqr.residual(c->d_rhs, d_x, nullptr, c->d_res)) return fail(c, AGB_ERR_CUDA, "residual: " + c->lsqr.err);
         CUDA_OR_FAIL(c, cudaMemcpyAsync(hr.data(), c->d_res, hr.size() * sizeof(double), cudaMemcpyDeviceToHost,
                                         c->stream));
         CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
@@ -501,6 +512,7 @@ int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int r
       // LSQR (the reference's lsqr_solve, default iteration limit) from a zero
       // start on every right-hand side
       std::vector<int> nl(nrhs, 0), il(nrhs, 0);
+      if (int rc = ensure_q(c)) return rc;
       CUDA_OR_FAIL(c, cudaMemsetAsync(d_x, 0, (size_t)nrhs * c->n * sizeof(double), c->stream));
       if (!c->lsqr.solve(c->d_rhs, d_x, c->d_q, eps, 0, nl.data(), il.data(), nullptr, 8, true))
         return fail(c, AGB_ERR_CUDA, "lsqr after bicgstab: " + c->lsqr.err);
@@ -519,7 +531,7 @@ int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int r
     if (!c->lsqr.packed)
       return fail(c, AGB_ERR_UNSUPPORTED, "GMRES needs the packed mixed system (Stokes, velocity known on every "
                                           "wall, triangles, default integration, AGB_MIXED)");
-    if (!c->lsqr.gmres(c->d_rhs, d_x, c->d_q, eps, maxit, c->gmres_restart, nt.data(), is.data()))
+    if (!c->lsqr.gmres(c->d_rhs, d_x, nullptr, eps, maxit, c->gmres_restart, nt.data(), is.data()))
       return fail(c, AGB_ERR_CUDA, "gmres: " + c->lsqr.err);
     for (int r = 0; r < nrhs; ++r) {
       if (nit) nit[r] = nt[r];
@@ -535,6 +547,7 @@ int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int r
     if (!c->lsqr.block_precon()) return fail(c, AGB_ERR_NUMERIC, "lsqr: " + c->lsqr.err);
     c->lsqr.bj = true;
   }
+  if (int rc = ensure_q(c)) return rc;
   if (!c->lsqr.solve(c->d_rhs, d_x, c->d_q, eps, maxit, nt.data(), is.data(), nullptr, 8, x0_zero))
     return fail(c, AGB_ERR_CUDA, "lsqr: " + c->lsqr.err);
   for (int r = 0; r < nrhs; ++r) {
@@ -606,6 +619,7 @@ int assemble_general(agb_context* c, int precision) {
   CUDA_OR_FAIL(c, cudaMalloc(&c->d_q, c->lda * sizeof(double)));
   if (!c->lsqr.setup(c->d_A, precision == AGB_MIXED, c->m, c->n, c->lda, 1, c->stream)) return fail(c, AGB_ERR_CUDA, c->lsqr.err);
   if (!c->lsqr.precon(c->d_A, c->d_q)) return fail(c, AGB_ERR_CUDA, c->lsqr.err);
+  c->q_ready = true;
   CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
   c->general = true;
   c->assembled = true;
@@ -912,6 +926,7 @@ int agb_assemble(agb_context* c, int precision) {
     if (!c->lsqr.setup(nullptr, true, c->m, c->n, c->lda, 1, c->stream)) return fail(c, AGB_ERR_CUDA, c->lsqr.err);
     cudaEventRecord(c->tev[0], c->stream);
     if (!c->lsqr.precon(nullptr, c->d_q)) return fail(c, AGB_ERR_CUDA, c->lsqr.err);
+    c->q_ready = true;
     cudaEventRecord(c->tev[1], c->stream);
     CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
     float ms = 0.f;
@@ -984,9 +999,16 @@ int agb_assemble(agb_context* c, int precision) {
     CUDA_OR_FAIL(c, launch_laplace_system(a, c->stream));
     c->nlaunch += 1;
   }
-  // column scaling of lsqr_precon
+  // column scaling of lsqr_precon: the packed system keeps its matrix unscaled
+  // (the sweeps apply q), so q is formed when a solver first needs it (the
+  // LSQR paths; GMRES and BiCGSTAB never use it); any other system is scaled
+  // in place here
   if (!c->lsqr.setup(c->d_A, f32, c->m, c->n, c->lda, 1, c->stream)) return fail(c, AGB_ERR_CUDA, c->lsqr.err);
-  if (!c->lsqr.precon(c->d_A, c->d_q)) return fail(c, AGB_ERR_CUDA, c->lsqr.err);
+  c->q_ready = false;
+  if (!c->lsqr.packed) {
+    if (!c->lsqr.precon(c->d_A, c->d_q)) return fail(c, AGB_ERR_CUDA, c->lsqr.err);
+    c->q_ready = true;
+  }
   CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
   c->assembled = true;
   return AGB_OK;
@@ -999,6 +1021,7 @@ int agb_get_system(agb_context* c, int scaled, double* A, double* q) {
   if (c->prec == AGB_MATRIX_FREE && A) return fail(c, AGB_ERR_UNSUPPORTED, "the matrix-free system is not stored");
   cudaSetDevice(c->device);
   std::vector<double> qh(c->lda);
+  if (int rc = ensure_q(c)) return rc;
   CUDA_OR_FAIL(c, cudaMemcpy(qh.data(), c->d_q, c->lda * sizeof(double), cudaMemcpyDeviceToHost));
   if (q) std::copy(qh.begin(), qh.begin() + c->n, q);
   if (A && c->lsqr.packed) {  // expand the symmetric blocks: A[3i+a][b ne + j] = Ap[pk_idx(i, sym(a,b), j)]
@@ -1644,7 +1667,9 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
         e = launch_stokes_G_packed(b.ne, Q, b.ldp, b.pldp, (const QPt<float>*)(d + b.o_pts),
                                    (const float*)(d + b.o_src), (const float*)(d + b.o_cs), A, st);
       if (e == cudaSuccess) e = launch_stokes_self_packed(b.ne, b.pldp, geom, 1.0, A, st);
-      if (e == cudaSuccess)
+      // lsqr_precon's column scaling: only the LSQR solvers (and the hybrid's LSQR
+      // fallback) read it
+      if (e == cudaSuccess && c->solver != AGB_SOLVER_GMRES && c->solver != AGB_SOLVER_BICGSTAB)
         e = packed_colnorms(A, b.ne, b.pldp, b.lda, (double*)(d + b.o_q), (double*)(d + b.o_P), b.groups, st);
       if (e == cudaSuccess) {
         StokesRhsArgs a;
@@ -1656,7 +1681,8 @@ int agb_batch_resistance(agb_context* c, int nbodies, const int* node_off, const
         e = launch_stokes_rhs<float>(a, st);
       }
       if (e != cudaSuccess) return bail(AGB_ERR_CUDA, std::string("assembly: ") + cudaGetErrorString(e));
-      asm_launches += 7 + (b.na > 0 ? 2 : 0);
+      asm_launches += 5 + (c->solver != AGB_SOLVER_GMRES && c->solver != AGB_SOLVER_BICGSTAB ? 2 : 0) +
+                      (b.na > 0 ? 2 : 0);
       bodies[t].A = A;
       bodies[t].lda = b.lda;
       bodies[t].m = b.m;
@@ -1932,6 +1958,7 @@ int agb_solve_lu(agb_context* c, int nrhs, const double* u, double* x, int* info
     int* dpiv = nullptr;
     CUDA_OR_FAIL(c, cudaMalloc(&c->d_lu, (size_t)n * n * sizeof(double)));
     dim3 g((n + 31) / 32, (n + 31) / 32), b(32, 8);
+    if (int rc = ensure_q(c)) return rc;
     k_lu_from_system<<<g, b, 0, c->stream>>>((const double*)c->d_A, c->lda, n, n, c->d_q, c->d_lu);
     c->nlaunch += 1;
     CUDA_OR_FAIL(c, cudaGetLastError());

@@ -914,8 +914,8 @@ __global__ void __launch_bounds__(256) gg_resid(const GDesc* __restrict__ D, con
       sm[a][c] = er[a][c] = lo[a][c] = 0.f;
       acc[a][c] = 0.0;
     }
-  for (int j0 = lane; j0 < ne; j0 += 32 * 64) {
-    const int j1 = min(ne, j0 + 32 * 64);
+  for (int j0 = lane; j0 < ne; j0 += 32 * kFFTerms) {
+    const int j1 = min(ne, j0 + 32 * kFFTerms);
     for (int j = j0; j < j1; j += 32) {
       float g6[6];
 #pragma unroll

@@ -49,6 +49,11 @@ namespace {
 
 constexpr int GM_THREADS = 256;  // 32 rows x 8 right-hand sides per pass of a CTA
 constexpr int GM_BLOCKS = 304;   // 2 CTAs per SM on 152 SMs; fixed, so partial sums reduce in a fixed order
+// A cycle's Arnoldi steps run until the residual estimate |g_{j+1}| is below
+// kGmresInner * tol ||b||: with FP32 products the estimate runs ahead of the
+// true residual, and the margin lets the true residual formed at the end of
+// the cycle meet tol without a second cycle (and a second true residual).
+constexpr double kGmresInner = 0.5;
 
 inline unsigned gdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
@@ -67,10 +72,16 @@ __device__ __forceinline__ void gm_sum8(double v, double* sred, double* out) {
   __syncthreads();
 }
 
-// partial p of right-hand side c summed over the CTAs in order; np partials per CTA
+// partial p of right-hand side c summed over the CTAs by one warp in a fixed
+// order: lane k adds CTAs k, k+32, ..., then a butterfly over the lanes (every
+// lane ends with the same bits: each level adds the same two values).  All 32
+// lanes must call it.
 __device__ __forceinline__ double gm_total(const double* part, int np, int p, int c) {
+  const int lane = threadIdx.x & 31;
   double t = 0.0;
-  for (int b = 0; b < GM_BLOCKS; ++b) t += part[((size_t)b * np + p) * 8 + c];
+  for (int b = lane; b < GM_BLOCKS; b += 32) t += part[((size_t)b * np + p) * 8 + c];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
   return t;
 }
 
@@ -96,9 +107,14 @@ __global__ void __launch_bounds__(GM_THREADS) k_gm_load(int m, int k, const doub
 __global__ void k_gm_begin(const double* __restrict__ part, int np, int k, double tol, int maxit, int first,
                            GmresScalars* __restrict__ s, double* __restrict__ g, int* __restrict__ nactive) {
   const int c = threadIdx.x;
+  double tot = 0.0;
+  for (int cc = 0; cc < 8; ++cc) {
+    const double t = gm_total(part, np, 0, cc);
+    if (cc == c) tot = t;
+  }
   if (c < 8) {
     GmresScalars& q = s[c];
-    const double beta = sqrt(gm_total(part, np, 0, c));
+    const double beta = sqrt(tot);
     if (first) {
       q.bnorm = beta;
       q.its = 0;
@@ -180,17 +196,20 @@ __global__ void __launch_bounds__(GM_THREADS) k_gm_dots(int m, int j, const doub
   }
 }
 
-// hc[l] = v_l . w (l = 0..j) from the partials; H[l][j] = hc (pass 0) or += hc (pass 1)
-__global__ void k_gm_hred(int j, int mr, const double* __restrict__ part, int np, int pass,
-                          double* __restrict__ hc, double* __restrict__ H, const int* __restrict__ gate) {
+// hc[l] = v_l . w (l = 0..j) from the partials; H[l][j] = hc (pass 0) or += hc (pass 1).
+// CTA l, warp c (8 warps).
+__global__ void __launch_bounds__(256) k_gm_hred(int j, int mr, const double* __restrict__ part, int np, int pass,
+                                                 double* __restrict__ hc, double* __restrict__ H,
+                                                 const int* __restrict__ gate) {
   if (*gate == 0) return;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (j + 1) * 8) return;
-  const int l = t >> 3, c = t & 7;
+  const int l = blockIdx.x, c = threadIdx.x >> 5;
+  if (l > j) return;
   const double v = gm_total(part, np, l, c);
-  hc[t] = v;
-  double* h = H + ((size_t)l * mr + j) * 8 + c;
-  *h = pass ? *h + v : v;
+  if ((threadIdx.x & 31) == 0) {
+    hc[l * 8 + c] = v;
+    double* h = H + ((size_t)l * mr + j) * 8 + c;
+    *h = pass ? *h + v : v;
+  }
 }
 
 // w -= sum_l hc[l] v_l over the active columns; partial 0: ||w||^2
@@ -217,17 +236,22 @@ __global__ void __launch_bounds__(GM_THREADS) k_gm_orth(int m, int j, const doub
 
 // end of step j: h_{j+1,j} = ||w||, the previous rotations applied to column j
 // of H, a new rotation that zeroes h_{j+1,j}, g updated; the column leaves the
-// cycle when |g_{j+1}| <= tol ||b||, on a breakdown (h_{j+1,j} = 0: the Krylov
+// cycle when |g_{j+1}| <= tol ||b|| (tol: the in-cycle target kGmresInner x the solve's), on a breakdown (h_{j+1,j} = 0: the Krylov
 // space is invariant), at the end of the cycle or at the iteration limit
 __global__ void k_gm_givens(int j, int mr, const double* __restrict__ part, int np, double tol, int maxit,
                             double* __restrict__ H, double* __restrict__ cs, double* __restrict__ sn,
                             double* __restrict__ g, GmresScalars* __restrict__ s, int* __restrict__ nactive) {
   if (*nactive == 0) return;
   const int c = threadIdx.x;
+  double tot = 0.0;
+  for (int cc = 0; cc < 8; ++cc) {
+    const double t = gm_total(part, np, 0, cc);
+    if (cc == c) tot = t;
+  }
   if (c < 8) {
     GmresScalars& q = s[c];
     if (q.active) {
-      const double hn = sqrt(gm_total(part, np, 0, c));
+      const double hn = sqrt(tot);
       for (int l = 0; l < j; ++l) {
         double* a0 = H + ((size_t)l * mr + j) * 8 + c;
         double* a1 = H + ((size_t)(l + 1) * mr + j) * 8 + c;
@@ -376,10 +400,10 @@ bool DenseLsqr::gmres(const double* b_dev, double* x_dev, const double* q_dev, d
     if (j == 0) cudaEventRecordWithFlags(pev[1], stream, cudaEventRecordExternal);
     for (int pass = 0; pass < 2; ++pass) {
       k_gm_dots<<<GM_BLOCKS, GM_THREADS, 0, stream>>>(m, j, Vb, mv, w, gm_part, np, nactive);
-      k_gm_hred<<<gdiv((long long)(j + 1) * 8, 256), 256, 0, stream>>>(j, mr, gm_part, np, pass, hc, H, nactive);
+      k_gm_hred<<<j + 1, 256, 0, stream>>>(j, mr, gm_part, np, pass, hc, H, nactive);
       k_gm_orth<<<GM_BLOCKS, GM_THREADS, 0, stream>>>(m, j, Vb, mv, hc, gsc, w, gm_part, np, nactive);
     }
-    k_gm_givens<<<1, 32, 0, stream>>>(j, mr, gm_part, np, tol, maxit, H, cs, sn, g, gsc, nactive);
+    k_gm_givens<<<1, 32, 0, stream>>>(j, mr, gm_part, np, tol * kGmresInner, maxit, H, cs, sn, g, gsc, nactive);
   }
   GCK(cudaStreamEndCapture(stream, &graph));
   if (cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) {

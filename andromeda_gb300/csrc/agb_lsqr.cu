@@ -515,7 +515,7 @@ __global__ void __launch_bounds__(256) k_residp(const float* __restrict__ Ap, in
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
         const double* x = Xs + ((int64_t)b * ne + j) * K8;
-        const double qv = qs[(int64_t)b * ne + j];  // Xs = x / q and Ap is the unscaled matrix
+        const double qv = qs ? qs[(int64_t)b * ne + j] : 1.0;  // Xs = x / q and Ap is the unscaled matrix
 #pragma unroll
         for (int c = 0; c < K8; ++c) {
           const double xv = qv * x[c];
@@ -550,11 +550,11 @@ __global__ void __launch_bounds__(256) k_residp(const float* __restrict__ Ap, in
   }
 }
 
-// q.Xs split into FP32 parts, x = xh + xl to about 2^-48 relative ([n][8])
+// q.Xs (Xs itself when qs is null) split into FP32 parts, x = xh + xl to about 2^-48 relative ([n][8])
 __global__ void k_split_x(int64_t n8, const double* __restrict__ Xs, const double* __restrict__ qs,
                           float* __restrict__ Xh, float* __restrict__ Xl) {
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n8; t += (int64_t)gridDim.x * blockDim.x) {
-    const double x = qs[t >> 3] * Xs[t];
+    const double x = qs ? qs[t >> 3] * Xs[t] : Xs[t];
     const float h = (float)x;
     Xh[t] = h;
     Xl[t] = (float)(x - (double)h);
@@ -566,9 +566,10 @@ __global__ void k_split_x(int64_t n8, const double* __restrict__ Xs, const doubl
 // rounded product, pe = fma(g, xh, -p)); the p are summed by TwoSum (Knuth;
 // s + e holds the running sum exactly up to the rounding of the error term),
 // the pe and the g xl terms into a third FP32 sum, and the three sums are
-// moved into FP64 accumulators every 64 terms of a lane.  The result is within
-// about 2^-40 (worst case; random rounding: 2^-46) of sum |a_ij x_j| of the
-// exact product, where FP64 accumulation gives 2^-53: far below any tolerance
+// moved into FP64 accumulators every kFFTerms = 256 terms of a lane (the FP64
+// adds run at 1/64 of the FP32 rate: flushing every 64 terms cost ~15 % of the
+// kernel).  The result is within about 2^-38 (worst case; random rounding:
+// 2^-45) of sum |a_ij x_j| of the exact product, where FP64 accumulation gives 2^-53: far below any tolerance
 // the solvers test, on the FP32 pipe instead of the 1:64 FP64 pipe.  The adds
 // and the product use the _rn intrinsics so that nothing is contracted into an
 // FMA, which would break the exactness of TwoSum.  One warp per element row i.
@@ -590,8 +591,8 @@ __global__ void __launch_bounds__(256) k_residp_ff(const float* __restrict__ Ap,
       acc[a][c] = 0.0;
     }
   if (i < ne) {
-    for (int j0 = lane; j0 < ne; j0 += 32 * 64) {
-    const int j1 = min(ne, j0 + 32 * 64);
+    for (int j0 = lane; j0 < ne; j0 += 32 * kFFTerms) {
+    const int j1 = min(ne, j0 + 32 * kFFTerms);
     for (int j = j0; j < j1; j += 32) {
       float g6[6];
       const float* pj = Ap + pk_idx(i, 0, j, ldp);

@@ -30,6 +30,8 @@ struct BicgScalars {
 // the true residual.  jc: Arnoldi steps of the current cycle; hnext: the norm
 // that normalises the next basis vector; prev: the true relative residual at
 // the start of the cycle.
+// terms of a lane summed in float-float form before they move into FP64 (true residuals)
+constexpr int kFFTerms = 256;
 struct GmresScalars {
   double bnorm, beta, hnext, relres, prev;
   int its, jc, active, status, cycles;
@@ -133,7 +135,9 @@ struct DenseLsqr {
              int* nit_host, int* status_host, double* relres_host = nullptr, int* cycles_host = nullptr);
   // inverses of the packed matrix's 3x3 self blocks into pc9 (once per matrix)
   bool block_precon();
-  // r = b - A (x ./ q) with FP64 accumulation (refinement residual).
+  // r = b - A (x ./ q) with FP64 accumulation (refinement residual): the true
+  // residual of x for the matrix scaled by q; q_dev may be null on the packed
+  // system, whose matrix stays unscaled.
   bool residual(const double* b_dev, const double* x_dev, const double* q_dev, double* r_dev);
   void release();
 };

@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--lis-compare", type=int, default=3,
                     help="sphere: timed solves of each other solver (column-scaled LSQR, block LSQR, BiCGSTAB hybrid)")
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "batch", "surrogate", "large", "laplace"],
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "batch", "surrogate", "large", "laplace", "mlp"],
                     help="sphere: one level-5 sphere (default); batch: the many-body superellipsoid set")
     ap.add_argument("--bodies", type=int, default=512, help="batch workload: number of bodies")
     ap.add_argument("--fp64-sample", type=int, default=6, help="batch workload: bodies solved on the FP64 path")
@@ -198,13 +198,16 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def measured_peaks():
+def measured_peaks(key="hbm_gbs"):
+    """The measured peak (HBM copy GB/s, or "bf16_tflops") and its source."""
+    fallback = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}[key]
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         with open(p) as f:
             d = json.load(f)
-        return float(d["hbm_gbs"]), "measured"
-    return 6800.0, "fallback"
+        if key in d:
+            return float(d[key]), "measured"
+    return fallback, "fallback"
 
 
 # FLOPs of k_stokes_G per (collocation point, element, quadrature point)
@@ -755,6 +758,43 @@ def run_surrogate(args):
     sur.close()
 
 
+def run_mlp(args):
+    """The fused surrogate inference kernel alone: --queries queries through a
+    randomly initialised 5-256-256-256-21 network (weights and biases drawn
+    once, seed 3), split-BF16 products; the kernel's CUDA-event time per call.
+    The outputs are checked against the layer-by-layer split-BF16 GEMMs."""
+    import numpy as np
+    from andromeda_gb300.surrogate import MLP
+    net = MLP(device=0, seed=3)
+    rng = np.random.default_rng(0)
+    p = net.params()
+    net.set_params(p + rng.normal(scale=0.05, size=p.shape).astype(np.float32))
+    X = rng.uniform(0.2, 1.8, (args.queries, 5)).astype(np.float32)
+    net.set_normalization(X.mean(0), X.std(0) + 1e-3, np.zeros(21, np.float32), np.ones(21, np.float32))
+    for _ in range(max(args.warmup, 1)):
+        net.predict(X)
+    with ClockSampler(0) as clk:
+        ms = [net.predict(X)[1] for _ in range(max(args.steps, 1))]
+    Yf, _ = net.predict(X)
+    Yg, _ = net.predict(X, fused=False)
+    med = statistics.median(ms)
+    flops = 2.0 * (5 * 256 + 2 * 256 * 256 + 256 * 21) * args.queries * 3
+    peak, _ = measured_peaks("bf16_tflops")
+    line = {"metric": "surrogate inference kernel inferences/s (one MLP 5-256-256-256-21, split-BF16 tcgen05)",
+            "value": args.queries / (med / 1000.0), "unit": "inferences/s", "n_gpus": 1, "steps": len(ms),
+            "warmup": max(args.warmup, 1), "ms_per_step": med, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 tensor cores (split hi+lo, fp32 accumulation)",
+            "data": "synthetic (random weights, seed 3; inputs U(0.2, 1.8))",
+            "config": {"workload": f"{args.queries} queries, one network", "l2": "weights L2-resident by design"},
+            "roofline": {"bound": "tensor", "achieved": flops / (med * 1e-3) / 1e12, "peak": peak, "unit": "TFLOP/s",
+                         "frac": flops / (med * 1e-3) / 1e12 / peak if peak else None, "traffic": None,
+                         "kernel": "k_mlp_infer_tc", "note": "split-BF16: the three products per GEMM are counted"},
+            "max_abs_diff_vs_layer_gemms": float(np.max(np.abs(Yf - Yg))),
+            "clocks": clk.summary(), "cpu_baseline": None}
+    print(json.dumps(line), flush=True)
+    net.close()
+
+
 # ---------------------------------------------------------------------------
 def main():
     args = parse()
@@ -773,6 +813,10 @@ def main():
     if args.workload == "laplace":
         if rank == 0:
             run_laplace(args)
+        return
+    if args.workload == "mlp":
+        if rank == 0:
+            run_mlp(args)
         return
     if args.workload == "batch":
         if world > 1:
