@@ -329,6 +329,12 @@ __device__ __forceinline__ double wsum(double v) {
   return v;
 }
 
+// index of the symmetric pair (a, b) in {xx, xy, xz, yy, yz, zz}
+__device__ __forceinline__ int sym_ab(int a, int b) {
+  const int lo = a < b ? a : b, hi = a < b ? b : a;
+  return lo == 0 ? hi : (lo == 1 ? 2 + hi : 5);
+}
+
 template <typename T>
 __global__ void k_stokes_rhs(StokesRhsArgs a) {
   // barycentric coordinates of the rule in T (the points themselves come from
@@ -352,17 +358,16 @@ __global__ void k_stokes_rhs(StokesRhsArgs a) {
     if (e == i) continue;
     const ElemGeom& G = a.geom[e];
     const T nx = (T)(G.multi * G.n[0]), ny = (T)(G.multi * G.n[1]), nz = (T)(G.multi * G.n[2]);
-    T uv[AGB_MAX_RHS][3][3];  // [c][comp][local node]
+    // The stresslet applied to the linearly interpolated nodal velocities,
+    // int cn (r . u) r_a with u = sum_k L_k u_k, is linear in the u_k:
+    // accumulate the 18 moments m[k][ab] = int cn L_k r_a r_b over the element
+    // once and contract them with every right-hand side's nodal velocities
+    // afterwards (42 operations per point instead of ~110 for six fields).
+    T mom[3][6];
 #pragma unroll
-    for (int c = 0; c < AGB_MAX_RHS; ++c)
+    for (int kk = 0; kk < 3; ++kk)
 #pragma unroll
-      for (int b = 0; b < 3; ++b)
-#pragma unroll
-        for (int kk = 0; kk < 3; ++kk)
-          uv[c][b][kk] = (c < a.k) ? (T)a.u[((int64_t)c * 3 + b) * a.nnodes + G.con[kk]] : T(0);
-    T pe[AGB_MAX_RHS][3];
-#pragma unroll
-    for (int c = 0; c < AGB_MAX_RHS; ++c) pe[c][0] = pe[c][1] = pe[c][2] = T(0);
+      for (int s6 = 0; s6 < 6; ++s6) mom[kk][s6] = T(0);
     for (int q = 0; q < Q; ++q) {
       const QPt<T> P = pts[(int64_t)q * a.ldp + e];
       const T w = P.w;
@@ -371,24 +376,33 @@ __global__ void k_stokes_rhs(StokesRhsArgs a) {
       const T ir = rsq<T>(r2);
       const T ir2 = ir * ir;
       const T cn = T(-6) * w * (rx * nx + ry * ny + rz * nz) * (ir2 * ir2 * ir);
-      const T L1 = sL[0][q], L2 = sL[1][q], L3 = sL[2][q];
+      const T rr[6] = {rx * rx, rx * ry, rx * rz, ry * ry, ry * rz, rz * rz};
 #pragma unroll
-      for (int c = 0; c < AGB_MAX_RHS; ++c) {
-        if (c < a.k) {
-          const T ux = L1 * uv[c][0][0] + L2 * uv[c][0][1] + L3 * uv[c][0][2];
-          const T uy = L1 * uv[c][1][0] + L2 * uv[c][1][1] + L3 * uv[c][1][2];
-          const T uz = L1 * uv[c][2][0] + L2 * uv[c][2][1] + L3 * uv[c][2][2];
-          const T f = cn * (rx * ux + ry * uy + rz * uz);
-          pe[c][0] += f * rx;
-          pe[c][1] += f * ry;
-          pe[c][2] += f * rz;
-        }
+      for (int kk = 0; kk < 3; ++kk) {
+        const T ck = cn * sL[kk][q];
+#pragma unroll
+        for (int s6 = 0; s6 < 6; ++s6) mom[kk][s6] += ck * rr[s6];
       }
     }
 #pragma unroll
-    for (int c = 0; c < AGB_MAX_RHS; ++c)
+    for (int c = 0; c < AGB_MAX_RHS; ++c) {
+      if (c < a.k) {
+        T uv[3][3];  // [comp][local node] of right-hand side c
 #pragma unroll
-      for (int b = 0; b < 3; ++b) acc[c][b] += (double)pe[c][b];
+        for (int b = 0; b < 3; ++b)
+#pragma unroll
+          for (int kk = 0; kk < 3; ++kk) uv[b][kk] = (T)a.u[((int64_t)c * 3 + b) * a.nnodes + G.con[kk]];
+#pragma unroll
+        for (int ai = 0; ai < 3; ++ai) {
+          T pe = T(0);
+#pragma unroll
+          for (int kk = 0; kk < 3; ++kk)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) pe += mom[kk][sym_ab(ai, b)] * uv[b][kk];
+          acc[c][ai] += (double)pe;
+        }
+      }
+    }
   }
 #pragma unroll
   for (int c = 0; c < AGB_MAX_RHS; ++c)
