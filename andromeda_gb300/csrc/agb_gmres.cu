@@ -179,20 +179,46 @@ __global__ void __launch_bounds__(GM_THREADS) k_gm_pc(int ne, int ldp, int j, co
   for (int b = 0; b < 3; ++b) W[((size_t)b * 8 + c) * ldp + i] = o[b];
 }
 
-// partial l (l = 0..j): v_l . w
+// partial l (l = 0..j): v_l . w.  Eight basis vectors per pass over w (one
+// CTA reduction per eight); each partial sums its thread's terms in index
+// order, then over the warp and the CTA as gm_sum8 does.
 __global__ void __launch_bounds__(GM_THREADS) k_gm_dots(int m, int j, const double* __restrict__ Vb,
                                                        size_t vstride, const double* __restrict__ w,
                                                        double* __restrict__ part, int np,
                                                        const int* __restrict__ gate) {
   if (*gate == 0) return;
-  __shared__ double sred[GM_THREADS / 32 * 8];
-  for (int l = 0; l <= j; ++l) {
-    const double* v = Vb + (size_t)l * vstride;
-    double d = 0.0;
+  constexpr int LB = 8;
+  __shared__ double sred[GM_THREADS / 32][LB][8];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int l0 = 0; l0 <= j; l0 += LB) {
+    const int nl = min(LB, j + 1 - l0);
+    double d[LB];
+#pragma unroll
+    for (int u = 0; u < LB; ++u) d[u] = 0.0;
     for (long long t = (long long)blockIdx.x * GM_THREADS + threadIdx.x; t < (long long)m * 8;
-         t += (long long)GM_BLOCKS * GM_THREADS)
-      d += v[t] * w[t];
-    gm_sum8(d, sred, part + ((size_t)blockIdx.x * np + l) * 8);
+         t += (long long)GM_BLOCKS * GM_THREADS) {
+      const double wv = w[t];
+#pragma unroll
+      for (int u = 0; u < LB; ++u)
+        if (u < nl) d[u] += Vb[(size_t)(l0 + u) * vstride + t] * wv;
+    }
+#pragma unroll
+    for (int u = 0; u < LB; ++u) {
+      double v = d[u];
+      v += __shfl_down_sync(0xffffffffu, v, 16);
+      v += __shfl_down_sync(0xffffffffu, v, 8);
+      if (lane < 8) sred[warp][u][lane] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < LB * 8) {
+      const int u = threadIdx.x >> 3, c = threadIdx.x & 7;
+      if (u < nl) {
+        double tsum = 0.0;
+        for (int ww = 0; ww < GM_THREADS / 32; ++ww) tsum += sred[ww][u][c];
+        part[((size_t)blockIdx.x * np + l0 + u) * 8 + c] = tsum;
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -227,6 +253,7 @@ __global__ void __launch_bounds__(GM_THREADS) k_gm_orth(int m, int j, const doub
        t += (long long)GM_BLOCKS * GM_THREADS) {
     if (!act) continue;
     double v = w[t];
+#pragma unroll 8
     for (int l = 0; l <= j; ++l) v -= hc[l * 8 + c] * Vb[(size_t)l * vstride + t];
     w[t] = v;
     ss += v * v;
