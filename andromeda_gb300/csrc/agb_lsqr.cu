@@ -568,8 +568,10 @@ __global__ void k_split_x(int64_t n8, const double* __restrict__ Xs, const doubl
 // the pe and the g xl terms into a third FP32 sum, and the three sums are
 // moved into FP64 accumulators every kFFTerms = 256 terms of a lane (the FP64
 // adds run at 1/64 of the FP32 rate: flushing every 64 terms cost ~15 % of the
-// kernel).  The result is within about 2^-38 (worst case; random rounding:
-// 2^-45) of sum |a_ij x_j| of the exact product, where FP64 accumulation gives 2^-53: far below any tolerance
+// kernel).  The rounding left is that of the FP32 sum of the TwoSum errors and
+// of the third sum: at most about n^2 u^2 / 2 of sum |a_ij x_j| for n = 256
+// terms and u = 2^-24, i.e. 2^-33 in the worst case (random rounding: below
+// 2^-44), where FP64 accumulation gives 2^-53: far below any tolerance
 // the solvers test, on the FP32 pipe instead of the 1:64 FP64 pipe.  The adds
 // and the product use the _rn intrinsics so that nothing is contracted into an
 // FMA, which would break the exactness of TwoSum.  One warp per element row i.
