@@ -235,9 +235,8 @@ static void gemm(bool split, int M, int N, int K, const float* A, int lda, const
 // ---------------------------------------------------------------------------
 // Fused inference on the 5th-generation tensor cores (tcgen05, split-BF16).
 // One CTA runs 128 queries (the tcgen05 M) through the four layers:
-//   * the activations live in shared memory as BF16 hi and lo halves in the
-//     no-swizzle K-major core-matrix layout (8 rows x 16 B per core matrix,
-//     [row/8][k/8][8][8]), 64 KB each;
+//   * the activations live in shared memory as BF16 hi and lo halves, K-major
+//     with the 128-byte swizzle (tc_hoff), 64 KB each;
 //   * the weights, pre-split and pre-packed in the same layout chunk by chunk
 //     (16 k per chunk, one tcgen05 K step; [layer chunk][hi/lo][n/8][k/8][8][8]),
 //     stream from L2 through a five-slot ring of 16 KB slots, one bulk copy per
@@ -262,7 +261,9 @@ constexpr int TC_EPI = 16;                    // epilogue warps: 4 per TMEM lane
 constexpr int TC_THREADS = (TC_EPI + 2) * 32;  // + 1 copy warp + 1 issuing warp
 constexpr size_t TC_H_BYTES = (size_t)TC_M * TC_H * 2;             // one half (hi or lo) of the activations
 constexpr size_t TC_SLOT = 2ull * TC_H * TC_KC * 2;                  // largest chunk: N 256 x K 16, hi + lo
-constexpr size_t TC_SMEM = 2 * TC_H_BYTES + TC_NSLOT * TC_SLOT;      // 208 KB (+ 4 KB static)
+// + 1 KB so that the activations can start on a 1024-byte boundary (the 128-byte
+// swizzle repeats every 8 rows x 128 B)
+constexpr size_t TC_SMEM = 2 * TC_H_BYTES + TC_NSLOT * TC_SLOT + 1024;  // 209 KB (+ 4 KB static)
 // packed weights (bytes): layer 1 one chunk (N 256, K 16), layers 2-3 sixteen chunks (N 256, K 16),
 // layer 4 sixteen chunks (N 32, K 16); hi then lo inside a chunk
 constexpr int TC_LCH = TC_H / TC_KC;  // chunks of layers 2-4
@@ -362,9 +363,21 @@ __device__ __forceinline__ void tc_ld8_wait(uint32_t (&r)[8]) {
                :
                : "memory");
 }
-// byte offset of (row, k) in a [row/8][k/8][8][8] BF16 half with 32 core matrices per 8-row group
+// byte offset of (row, k) in one BF16 half of the activations, K-major with the
+// 128-byte swizzle: four column blocks of 64 k (16 KB each: 128 rows x 128 B),
+// 8-row groups of 1 KB, and within a row the 16-byte chunk k/8 stored at chunk
+// (k/8) xor (row % 8) -- the layout tcgen05 reads through a SWIZZLE_128B descriptor
 __device__ __forceinline__ uint32_t tc_hoff(int row, int k) {
-  return (uint32_t)(((row >> 3) * (TC_H / 8) + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2);
+  return (uint32_t)((k >> 6) * (TC_M * 128) + (row >> 3) * 1024 + (row & 7) * 128 +
+                    ((((k >> 3) & 7) ^ (row & 7)) << 4) + (k & 7) * 2);
+}
+// descriptor of the A operand at activation column k0 (a multiple of 16): the
+// column block's start advanced by k0 % 64 elements inside the swizzle atom,
+// stride 1 KB between 8-row groups, swizzle mode 2 (128 B) in bits 61-63
+__device__ __forceinline__ uint64_t tc_adesc(uint32_t half, int k0) {
+  const uint32_t addr = half + (uint32_t)((k0 >> 6) * (TC_M * 128) + (k0 & 63) * 2);
+  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
 }
 // bias + SiLU of 8 accumulator values, split into BF16 hi and lo, stored as one
 // 16-byte core-matrix row each
@@ -389,9 +402,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
                                                                 const unsigned char* __restrict__ wt,
                                                                 float* __restrict__ Y, int* errflag) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
-  unsigned char* Hh = tc_smem;
-  unsigned char* Hl = tc_smem + TC_H_BYTES;
-  unsigned char* Wslot = tc_smem + 2 * TC_H_BYTES;
+  // the activations on a 1024-byte boundary of the shared address space
+  unsigned char* Hh = tc_smem + ((1024u - (smem_u32_mlp(tc_smem) & 1023u)) & 1023u);
+  unsigned char* Hl = Hh + TC_H_BYTES;
+  unsigned char* Wslot = Hh + 2 * TC_H_BYTES;
   // full/empty: the weight ring; accb[b]: accumulator b complete; hready[j]: the 32
   // activation columns of block j written by the epilogue (all 16 warps arrive)
   __shared__ __align__(8) uint64_t full[TC_NSLOT], empty[TC_NSLOT], accb[2], hready[TC_H / TC_AB];
@@ -487,8 +501,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_infer_tc(int n, int nin, 
           const uint32_t bl = bh + (uint32_t)N * TC_KC * 2;
           const uint32_t sbo_b = (uint32_t)(TC_KC / 8) * 128;
           const int k0 = j * TC_KC;  // activation column of this chunk
-          const uint64_t ah = tc_sdesc(smem_u32_mlp(Hh) + (uint32_t)(k0 / 8) * 128, (TC_H / 8) * 128);
-          const uint64_t al = tc_sdesc(smem_u32_mlp(Hl) + (uint32_t)(k0 / 8) * 128, (TC_H / 8) * 128);
+          const uint64_t ah = tc_adesc(smem_u32_mlp(Hh), k0);
+          const uint64_t al = tc_adesc(smem_u32_mlp(Hl), k0);
           const uint64_t dbh = tc_sdesc(bh, sbo_b), dbl = tc_sdesc(bl, sbo_b);
           tc_mma(tacc, ah, dbh, idesc, j != 0);
           tc_mma(tacc, ah, dbl, idesc, 1);
