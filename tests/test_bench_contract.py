@@ -66,3 +66,25 @@ def test_measured_peaks_source():
             assert peak == float(json.load(f)["hbm_gbs"]) and kind == "measured"
     else:
         assert (peak, kind) == (6800.0, "fallback")
+
+
+def test_measured_bf16_peak_source():
+    B = _bench_module()
+    peak, kind = B.measured_peaks("bf16_tflops")
+    if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")):
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            assert peak == float(json.load(f)["bf16_tflops"]) and kind == "measured"
+    else:
+        assert (peak, kind) == (1900.0, "fallback")
+
+
+def test_profile_traffic_figures_present():
+    """The DRAM traffic that the headline and batch lines report comes from the
+    committed ncu summaries: both files carry their machine-readable line."""
+    B = _bench_module()
+    with open(B.PROFILE_TRAFFIC) as f:
+        t = [float(l.split(":")[1]) for l in f if l.startswith("traffic_bytes_per_launch_k_avp_c2:")]
+    assert len(t) == 1 and 1.0e10 < t[0] < 1.1e10  # 10.38 GB of packed matrix per launch, read once
+    with open(B.PROFILE_BATCH) as f:
+        r = [float(l.split(":")[1]) for l in f if l.startswith("traffic_ratio_gb_avp_b16:")]
+    assert len(r) == 1 and 1.0 <= r[0] < 1.1
