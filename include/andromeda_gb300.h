@@ -174,8 +174,11 @@ int agb_set_solver(agb_context* ctx, int solver);
  * mod_plis.f90:235 taking the options of mod_par.f90:418): restarted GMRES(m)
  * (Saad and Schultz 1986) on A M^-1, M the elements' 3x3 self blocks, x0 = 0,
  * stop at ||b - A x|| <= eps ||b|| or maxit Arnoldi steps (0: 1000, the LIS
- * default).  At the end of every cycle the true residual is formed with FP64
- * accumulation over the stored matrix; the next cycle starts from it.  istop[r]:
+ * default).  A cycle's steps run until the residual estimate is below
+ * eps/2 ||b|| (with FP32 products the estimate runs ahead of the true
+ * residual); at the end of every cycle the true residual is formed over the
+ * stored matrix (agb_set_residual_mode) and decides: within eps the
+ * right-hand side is done, otherwise the next cycle starts from it.  istop[r]:
  * 0 converged (by the true residual), 1 iteration limit, 3 a cycle that did
  * not lower the true residual by 10 %.  restart = m, 1..512 (default 40, the
  * LIS default). */
@@ -184,7 +187,8 @@ int agb_set_gmres_restart(agb_context* ctx, int restart);
 /* Arithmetic of the true residual b - A x over the packed FP32 single layer
  * (GMRES and BiCGSTAB restarts, refinement, LSQR warm starts): 0 (default)
  * float-float products and sums on the FP32 pipe (TwoSum, flushed into FP64
- * every 64 terms; within about 2^-40 of sum |a_ij x_j| of the exact residual),
+ * every 256 terms; within about 2^-33 of sum |a_ij x_j| of the exact residual
+ * in the worst case, below 2^-44 with random rounding),
  * 1 FP64 products and sums (the FP64 pipe, ~10x slower on this part). */
 int agb_set_residual_mode(agb_context* ctx, int mode);
 
