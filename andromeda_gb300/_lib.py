@@ -32,6 +32,7 @@ SIGNATURES = {
     "agb_set_problem": ([vp, I, I, ip, dp, D, ip, I, I], I),
     "agb_get_geometry": ([vp, dp, dp, dp], I),
     "agb_set_integration": ([vp, I, I, D, I], I),
+    "agb_set_node_walls": ([vp, I, vp], I),
     "agb_set_solver": ([vp, I], I),
     "agb_set_gmres_restart": ([vp, I], I),
     "agb_set_residual_mode": ([vp, I], I),

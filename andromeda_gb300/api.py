@@ -131,6 +131,20 @@ class Context:
         self._ck(self._L.agb_set_integration(self.h, int(sing_mode), int(rec_depth), float(near_eta),
                                              int(near_depth)))
 
+    def set_node_walls(self, node_wall=None):
+        """Walls of the subdomain's nodes (wall id per global node, < 0 keeps the
+        automatic assignment; None restores it for all): the reference's
+        subdomain%BCidList after the BiC file's EDGE / CORNER directives, e.g.
+        from :func:`andromeda_gb300.mesh.edge_corner_node_walls`.  Call after
+        set_problem; clears the assembled system."""
+        if node_wall is None:
+            self._ck(self._L.agb_set_node_walls(self.h, self.nnodes, None))
+            return
+        w = np.ascontiguousarray(node_wall, dtype=np.int32)
+        if w.shape != (self.nnodes,):
+            raise ValueError("node_wall needs one entry per mesh node")
+        self._ck(self._L.agb_set_node_walls(self.h, self.nnodes, w.ctypes.data_as(C.c_void_p)))
+
     def set_solver(self, solver, restart=None):
         """SOLVER_LSQR (default, lsqr_solve), SOLVER_LSQR_BLOCK (LSQR with the
         3x3 self-block preconditioner), SOLVER_BICGSTAB (the LIS path's BiCGSTAB

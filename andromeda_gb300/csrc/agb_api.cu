@@ -75,6 +75,7 @@ struct agb_context {
   int m = 0, n = 0;
   double* d_q = nullptr;
   bool q_ready = false;  // d_q holds lsqr_precon's column scaling of the assembled system
+  std::vector<int> node_wall_in;  // agb_set_node_walls: wall id per global node (< 0: the automatic rule)
   bool assembled = false;
   DenseLsqr lsqr;
   // scratch
@@ -228,6 +229,7 @@ void free_system(agb_context* c) {
   c->general = false;
   dfree(c->d_A);
   dfree(c->d_q);
+  c->q_ready = false;
   dfree(c->d_pts);
   dfree(c->d_src);
   dfree(c->d_nrm);
@@ -247,6 +249,7 @@ void free_problem(agb_context* c) {
   dfree(c->rule.l);
   dfree(c->rule.w);
   c->gd.release();
+  c->node_wall_in.clear();
   c->has_problem = false;
 }
 
@@ -267,6 +270,14 @@ void build_layout(agb_context* c) {
     const int nno = c->etype[e] == AGB_TRI ? 3 : 4;
     for (int k = 0; k < nno; ++k) wallOf[c->con[4 * e + k]] = c->wallIdx[p];
   }
+  // walls the driver placed the nodes on (subdomain%BCidList after the BiC file's
+  // EDGE / CORNER directives, agb_set_node_walls); ids checked against the walls there
+  if (!c->node_wall_in.empty())
+    for (int i = 0; i < c->nnodes; ++i) {
+      if (wallOf[i] < 0 || c->node_wall_in[i] < 0) continue;
+      for (int k = 0; k < nw; ++k)
+        if (c->walls[k] == c->node_wall_in[i]) wallOf[i] = k;
+    }
   L.posOfNode.assign(c->nnodes, -1);
   for (int i = 0; i < c->nnodes; ++i)
     if (wallOf[i] >= 0) {
@@ -816,6 +827,31 @@ int agb_set_problem(agb_context* c, int kind, int nwalls, const int* walls, cons
   c->m = c->gl.nrow;
   c->n = c->gl.nx;
   c->has_problem = true;
+  return AGB_OK;
+}
+
+int agb_set_node_walls(agb_context* c, int nnodes, const int* node_wall) {
+  int rc = check_ctx(c, true);
+  if (rc) return rc;
+  if (nnodes != c->nnodes) return fail(c, AGB_ERR_ARG, "agb_set_node_walls: nnodes differs from the mesh's");
+  if (node_wall)
+    for (int i = 0; i < nnodes; ++i) {
+      const int w = node_wall[i];
+      if (w < 0) continue;
+      bool ok = false;
+      for (int v : c->walls) ok = ok || v == w;
+      if (!ok)
+        return fail(c, AGB_ERR_ARG, "agb_set_node_walls: node " + std::to_string(i) + " placed on wall " +
+                                        std::to_string(w) + ", which is not a wall of the problem");
+    }
+  cudaSetDevice(c->device);
+  free_system(c);  // the numbering changes: any assembled system is stale
+  if (node_wall) c->node_wall_in.assign(node_wall, node_wall + nnodes);
+  else c->node_wall_in.clear();
+  build_layout(c);
+  CUDA_OR_FAIL(c, c->gd.upload(c->gl));
+  c->m = c->gl.nrow;
+  c->n = c->gl.nx;
   return AGB_OK;
 }
 

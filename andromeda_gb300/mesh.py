@@ -244,3 +244,45 @@ def random_rotation(rng: np.random.Generator):
     return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
                      [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
                      [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def edge_corner_node_walls(mesh, walls, rules=()):
+    """Walls of the nodes of a single subdomain after the BiC file's EDGE and
+    CORNER directives (HandleCornersEdges, src/lib_sdBem.f90:112-310).
+
+    The start is the reference's own assignment (SetUpSubdomains,
+    src/lib_sdBem.f90:388-394): every node takes the wall of the last element
+    touching it, elements taken wall by wall in the order of `walls`.  Then
+    each rule, in order: ("EDGE", w1, w2, target) puts on wall `target` every
+    node shared by an element of wall w1 and an element of wall w2;
+    ("CORNER", w1, w2, w3, target) every node shared by elements of the three
+    walls.  Returns the wall id of every mesh node (-1 where the node is not on
+    a wall of the subdomain): the argument of ``Context.set_node_walls`` (the
+    reference's subdomain%BCidList)."""
+    con = np.asarray(mesh["con"])
+    bcid = np.asarray(mesh["bcid"])
+    etype = np.asarray(mesh["etype"])
+    nn = len(mesh["xyz"])
+    nno = np.where(etype == 2, 3, 4)
+
+    def touched(w):
+        on = np.zeros(nn, bool)
+        if w in walls:
+            for e in np.where(bcid == w)[0]:
+                on[con[e, :nno[e]]] = True
+        return on
+
+    node_wall = np.full(nn, -1, np.int32)
+    for w in walls:
+        for e in np.where(bcid == w)[0]:
+            node_wall[con[e, :nno[e]]] = w
+    for rule in rules:
+        kind = str(rule[0]).upper()
+        if kind == "EDGE" and len(rule) == 4:
+            shared = touched(rule[1]) & touched(rule[2])
+        elif kind == "CORNER" and len(rule) == 5:
+            shared = touched(rule[1]) & touched(rule[2]) & touched(rule[3])
+        else:
+            raise ValueError(f"not an EDGE or CORNER rule: {rule!r}")
+        node_wall[shared & (node_wall >= 0)] = int(rule[-1])
+    return node_wall

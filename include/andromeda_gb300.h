@@ -122,6 +122,20 @@ int agb_set_mesh(agb_context* ctx, int nnodes, const double* xyz, int nelem, con
 int agb_set_problem(agb_context* ctx, int kind, int nwalls, const int* walls, const double* normMul, double diff,
                     const int* known, int itri, int iqud);
 
+/* Walls of the subdomain's nodes as the driver placed them: the reference's
+ * subdomain%BCidList after the BiC file's EDGE / CORNER directives
+ * (HandleCornersEdges, lib_sdBem.f90:112-310), which move a node shared by
+ * walls of different boundary conditions to a named wall.  Without this call a
+ * node takes the wall of the last element touching it in subdomain order, the
+ * reference's assignment before those directives (SetUpSubdomains,
+ * lib_sdBem.f90:388-394).  node_wall[i] = the wall id (bcid) of global node i,
+ * or < 0 to keep that assignment; NULL restores it for every node.  Every id
+ * must be a wall of the problem.  Call after agb_set_problem (agb_set_mesh and
+ * agb_set_problem reset it); an assembled system is released, as its numbering
+ * changes.  Only the general path (some wall with a known flux) sees the node
+ * walls: with every value known, all walls route alike. */
+int agb_set_node_walls(agb_context* ctx, int nnodes, const int* node_wall);
+
 /* Integration options of the triangle integrals (default: sing_mode 0,
  * near_eta 0 -- the reference's assembly).  Replaces the commented-out
  * alternative of sdIntRowU/Q and sdIntRowU/QStokes (lib_sdBem.f90:510,668;

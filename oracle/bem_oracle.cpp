@@ -2196,6 +2196,52 @@ void* orc_problem_create(int kind, int nnodes, const double* xyz, int nelem, con
   return P;
 }
 void orc_problem_destroy(void* h) { delete (Problem*)h; }
+
+// HandleCornersEdges (lib_sdBem.f90:112-310), the BiC file's EDGE and CORNER
+// directives of the (single) subdomain: every node shared by an element of wall
+// w1 and an element of wall w2 (EDGE; CORNER: and of wall w3) takes the wall
+// target in BCidList, i.e. the boundary condition of that wall.  The reference
+// runs its element loops over the subdomain's element list (the CORNER loop's
+// bounds use the global element count, which is the same list for a subdomain
+// holding every element); the set of nodes found is the intersection of the
+// walls' node sets, which is what is computed here.  The numbering of the
+// unknowns follows BCidList and is set up again.
+static void renumber(Problem& P) {
+  setup_xb(P);
+  if (P.kind == 2) stk_setup_xb(P);
+}
+static std::vector<char> wall_nodes(const Problem& P, int w) {
+  std::vector<char> on(P.nnodes, 0);
+  for (int e : P.elementList)
+    if (P.bcid[e] == w)
+      for (int j = 0; j < P.nno[e]; ++j) on[P.con[4 * e + j]] = 1;
+  return on;
+}
+void orc_problem_edge_corner(void* h, int w1, int w2, int w3, int target) {
+  Problem* P = (Problem*)h;
+  const std::vector<char> a = wall_nodes(*P, w1), b = wall_nodes(*P, w2);
+  std::vector<char> c(P->nnodes, 1);
+  if (w3 >= 0) c = wall_nodes(*P, w3);
+  for (int m = 0; m < P->sd_nnodes; ++m) {
+    const int i = P->nodeList[m];
+    if (a[i] && b[i] && c[i]) P->BCidList[m] = target;
+  }
+  renumber(*P);
+}
+// subdomain%BCidList from the driver: node_wall[global node] = wall id, < 0 keeps
+// the node's wall
+void orc_problem_set_node_walls(void* h, const int* node_wall) {
+  Problem* P = (Problem*)h;
+  for (int m = 0; m < P->sd_nnodes; ++m)
+    if (node_wall[P->nodeList[m]] >= 0) P->BCidList[m] = node_wall[P->nodeList[m]];
+  renumber(*P);
+}
+// BCidList per global node (-1: not a node of the subdomain)
+void orc_problem_node_walls(void* h, int* node_wall) {
+  Problem* P = (Problem*)h;
+  std::fill(node_wall, node_wall + P->nnodes, -1);
+  for (int m = 0; m < P->sd_nnodes; ++m) node_wall[P->nodeList[m]] = P->BCidList[m];
+}
 // Integration options (IntegOpt) for the next orc_form_integrals.
 void orc_problem_set_integration(void* h, int sing, int rdepth, double near_eta, int near_depth) {
   Problem* P = (Problem*)h;

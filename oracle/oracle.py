@@ -53,6 +53,9 @@ def lib():
                                          C.c_int, C.c_int]
         L.orc_problem_create.restype = C.c_void_p
         L.orc_problem_destroy.argtypes = [C.c_void_p]
+        L.orc_problem_edge_corner.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.orc_problem_set_node_walls.argtypes = [C.c_void_p, ip]
+        L.orc_problem_node_walls.argtypes = [C.c_void_p, ip]
         L.orc_dgefa.argtypes = [dp, C.c_int, C.c_int, dp]
         L.orc_dgefa.restype = C.c_int
         L.orc_dgesl.argtypes = [dp, C.c_int, C.c_int, dp, dp, C.c_int]
@@ -230,6 +233,32 @@ class Problem:
             self.close()
         except Exception:
             pass
+
+    def edge_rule(self, w1, w2, target):
+        """EDGE directive of the BiC file (HandleCornersEdges, lib_sdBem.f90:148-215)."""
+        lib().orc_problem_edge_corner(self.h, int(w1), int(w2), -1, int(target))
+        self._resize()
+
+    def corner_rule(self, w1, w2, w3, target):
+        """CORNER directive of the BiC file (HandleCornersEdges, lib_sdBem.f90:217-292)."""
+        lib().orc_problem_edge_corner(self.h, int(w1), int(w2), int(w3), int(target))
+        self._resize()
+
+    def set_node_walls(self, node_wall):
+        """subdomain%BCidList from the caller: wall id per global node, < 0 keeps it."""
+        lib().orc_problem_set_node_walls(self.h, np.ascontiguousarray(node_wall, dtype=np.int32))
+        self._resize()
+
+    def node_walls(self):
+        """BCidList as wall id per global node (-1: not a node of the subdomain)."""
+        out = np.zeros(self.nnodes, np.int32)
+        lib().orc_problem_node_walls(self.h, out)
+        return out
+
+    def _resize(self):
+        s = np.zeros(6, dtype=np.int32)
+        lib().orc_problem_sizes(self.h, s)
+        self.nsp, self.sd_nnodes, self.sd_nqnodes, self.neq_rows, self.nx, self.nb = map(int, s)
 
     def geometry(self):
         n = np.zeros(3 * self.nelem)

@@ -11,7 +11,11 @@ the cases on this path:
     radius 0.5 in the same container);
   * run/mesh/kocka-000-111-314-624_tri.msh (gmsh 4.1): the unit cube of the Stokes
     cases run/stokes/Couette and Poiseuille (walls top, bottom, back, front, left,
-    right).
+    right);
+  * run/mesh/surf_tri-kocka.msh (gmsh 2.2): the unit cube of the Laplace case
+    run/laplace/cube-triangles (walls spredaj, zadaj, zgoraj, spodaj, levo, desno;
+    50 nodes, 96 triangles), whose BiC file places its edge and corner nodes with
+    EDGE / CORNER directives.
 The node coordinates, the triangles (node order as in the file: the reference takes
 the element normal from nodes 1-3) and the physical wall ids are written to
 tests/golden/<name>.npz.  Run from the repository root:
@@ -102,7 +106,8 @@ def main(ref):
     cases = {"sphere_01": "run/mesh/sphere-01.msh",
              "sphere_in_sphere_3678": "run/mesh/sphere-in-sphere-1024-1843-3678-tri.msh",
              "ellipsoid211_in_sphere_2117": "run/mesh/ellipsoid211-in-sphere-1024-1041-2117.msh",
-             "cube_624": "run/mesh/kocka-000-111-314-624_tri.msh"}
+             "cube_624": "run/mesh/kocka-000-111-314-624_tri.msh",
+             "surf_tri_kocka": "run/mesh/surf_tri-kocka.msh"}
     for name, rel in cases.items():
         xyz, tris, phys = read_msh(os.path.join(ref, rel))
         np.savez_compressed(os.path.join(HERE, name + ".npz"), xyz=xyz, tris=tris, phys=phys,

@@ -19,7 +19,11 @@ spheroid's axis against the reference's own analytic resistances
 calForceOnEllipsoid, lib_particle.f90:1979-1996) within 1.5 % (discretisation and
 the container, 645 semi-minor axes away); the Couette case on the cube (velocity on
 all six walls): the piecewise-constant traction of u = (z, 0, 0), oracle and GPU;
-the Poiseuille case (mixed boundary conditions) on the oracle.
+the Poiseuille case (mixed boundary conditions) on the oracle; the Laplace case
+run/laplace/cube-triangles on run/mesh/surf_tri-kocka.msh with its BiC file's EDGE /
+CORNER directives (the walls of the nodes on the cube's edges and corners): the
+package's restatement of the directives against the oracle's, the oracle's fields
+against the exact linear fields, and the GPU (agb_set_node_walls) against the oracle.
 """
 import numpy as np
 import pytest
@@ -288,3 +292,101 @@ def test_poiseuille_reference_cube(orc):
     assert abs(np.mean(q[1, back]) - p_mean) < 0.05 * p_mean
     assert abs(np.mean(q[1, front]) + p_mean) < 0.05 * p_mean
     assert abs(np.mean(q[0, left]) + 8.0) < 0.4
+
+
+# run/laplace/cube-triangles: the unit cube of run/mesh/surf_tri-kocka.msh (walls 1
+# spredaj z=1, 2 zadaj z=0, 3 zgoraj y=1, 4 spodaj y=0, 5 levo x=0, 6 desno x=1), the
+# subdomain's walls in the order of its BiC file, and the file's EDGE / CORNER
+# directives (tri-kocka-prevod.bic) as wall ids
+CUBE_WALLS = [1, 2, 5, 6, 4, 3]
+CUBE_RULES = [("EDGE", 3, 2, 2), ("EDGE", 3, 1, 1), ("EDGE", 3, 6, 6), ("EDGE", 3, 5, 5),
+              ("EDGE", 4, 2, 2), ("EDGE", 4, 1, 1), ("EDGE", 4, 6, 6), ("EDGE", 4, 5, 5),
+              ("EDGE", 1, 5, 5), ("EDGE", 1, 6, 6), ("EDGE", 2, 5, 5), ("EDGE", 2, 6, 6),
+              ("CORNER", 3, 1, 5, 5), ("CORNER", 3, 1, 6, 6), ("CORNER", 3, 2, 5, 5), ("CORNER", 3, 2, 5, 5),
+              ("CORNER", 4, 1, 5, 5), ("CORNER", 4, 1, 6, 6), ("CORNER", 4, 2, 5, 5), ("CORNER", 4, 2, 5, 5)]
+# the two equations of the case: temperature u = -0.5 on levo, 0.5 on desno, no flux
+# elsewhere (u = x - 0.5); concentration u = 1 on spredaj, 3 on zadaj (u = 3 - 2z)
+CUBE_CASES = {"temperatura": ({5: -0.5, 6: 0.5}, lambda p: p[:, 0] - 0.5),
+              "koncentracija": ({1: 1.0, 2: 3.0}, lambda p: 3.0 - 2.0 * p[:, 2])}
+
+
+def _cube_oracle(orc, m, case, rules=True):
+    """Oracle solve of one equation of the cube case; returns (u, q, node walls, problem sizes)."""
+    dirichlet, exact = CUBE_CASES[case]
+    known = [[1 if w in dirichlet else 2 for w in CUBE_WALLS]]
+    P = orc.Problem(1, m, walls=CUBE_WALLS, known=known, itri=5)
+    if rules:
+        for r in CUBE_RULES:
+            if r[0] == "EDGE":
+                P.edge_rule(*r[1:])
+            else:
+                P.corner_rule(*r[1:])
+    P.form_integrals()
+    walls = P.node_walls()
+    # known values: u on the Dirichlet walls' nodes (by the node's wall), q = 0 elsewhere
+    u0 = np.array([dirichlet.get(int(w), 0.0) for w in walls])
+    u, q, nit, ierr = P.laplace_solve(u0, np.zeros(P.nelem), maxit=0, eps=1e-13)
+    sizes = (P.nx, P.nb)
+    P.close()
+    assert ierr == 0
+    return u, q, walls, sizes, u0
+
+
+def test_edge_corner_rules_match_the_oracle(orc):
+    """The package's restatement of HandleCornersEdges (mesh.edge_corner_node_walls)
+    against the oracle's on the reference's cube with its BiC file's directives:
+    the same wall for every node; every node on an edge or corner of a Dirichlet
+    face (levo, desno) ends on that face."""
+    from andromeda_gb300 import mesh as M
+    m = reference_mesh("surf_tri_kocka")
+    P = orc.Problem(1, m, walls=CUBE_WALLS, known=[[2, 2, 1, 1, 2, 2]], itri=5)
+    auto = P.node_walls()
+    assert np.array_equal(auto, M.edge_corner_node_walls(m, CUBE_WALLS))  # the automatic rule
+    for r in CUBE_RULES:
+        (P.edge_rule if r[0] == "EDGE" else P.corner_rule)(*r[1:])
+    walls = P.node_walls()
+    P.close()
+    assert np.array_equal(walls, M.edge_corner_node_walls(m, CUBE_WALLS, CUBE_RULES))
+    x = m["xyz"][:, 0]
+    assert np.all(walls[np.isclose(x, 0.0)] == 5) and np.all(walls[np.isclose(x, 1.0)] == 6)
+    assert np.sum(walls != auto) > 0
+    with pytest.raises(ValueError):
+        M.edge_corner_node_walls(m, CUBE_WALLS, [("EDGE", 1, 2)])
+
+
+@pytest.mark.parametrize("case", ["temperatura", "koncentracija"])
+def test_laplace_cube_edge_corner_case(orc, case):
+    """run/laplace/cube-triangles on the oracle with the BiC file's EDGE / CORNER
+    directives: the linear field of each equation at every node (the Dirichlet
+    ones exactly) and its flux on the elements."""
+    m = reference_mesh("surf_tri_kocka")
+    u, q, walls, sizes, u0 = _cube_oracle(orc, m, case)
+    dirichlet, exact = CUBE_CASES[case]
+    ue = exact(m["xyz"])
+    known = np.isin(walls, list(dirichlet))
+    assert np.max(np.abs(u[known] - ue[known])) < 1e-14
+    assert np.max(np.abs(u - ue)) < 1e-6  # 2.7e-8 / 6.7e-7 (3.3e-7 / 7.2e-7 without the directives)
+    u_auto, _, _, sizes_auto, _ = _cube_oracle(orc, m, case, rules=False)
+    assert sizes != sizes_auto  # the directives change which nodes are unknowns
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["temperatura", "koncentracija"])
+def test_gpu_laplace_cube_edge_corner_case(agb, orc, case):
+    """The same case through the C ABI, the node walls set by agb_set_node_walls from
+    the package's restatement of the directives: the oracle's fields to 1e-10."""
+    from andromeda_gb300 import mesh as M
+    m = reference_mesh("surf_tri_kocka")
+    u_ref, q_ref, walls, sizes, u0 = _cube_oracle(orc, m, case)
+    dirichlet, _ = CUBE_CASES[case]
+    known = [[1 if w in dirichlet else 2 for w in CUBE_WALLS]]
+    C = agb.Context(0)
+    C.set_mesh(m)
+    C.set_problem(agb.LAPLACE, CUBE_WALLS, known, itri=5)
+    C.set_node_walls(M.edge_corner_node_walls(m, CUBE_WALLS, CUBE_RULES))
+    C.assemble(agb.FP64)
+    uo, qo, nit, istop = C.solve_fields(u0[None, None], np.zeros((1, 1, len(m["etype"]))), eps=1e-13)
+    C.close()
+    assert istop[0] <= 3
+    assert np.max(np.abs(uo[0, 0] - u_ref)) < 1e-10 * np.max(np.abs(u_ref))
+    assert np.max(np.abs(qo[0, 0] - q_ref)) < 1e-10 * max(np.max(np.abs(q_ref)), 1.0)
