@@ -434,7 +434,7 @@ int device_rhs(agb_context* c, int nrhs, int na) {
 int assemble_general(agb_context* c, int precision);
 // relative LSQR tolerance of each refinement correction solve
 constexpr double kRefineEps = 1.0e-2;
-// restarts of BiCGSTAB on its FP64 true residual
+// restarts of BiCGSTAB on its true residual
 constexpr int kBicgRestarts = 4;
 __global__ void k_axpy(int64_t n, const double* __restrict__ d, double* __restrict__ x) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -465,9 +465,10 @@ int do_solve(agb_context* c, int nrhs, double* d_x, int maxit, double eps, int r
     if (!c->lsqr.bicgstab(c->d_rhs, d_x, eps, maxit, nt.data(), is.data()))
       return fail(c, AGB_ERR_CUDA, "bicgstab: " + c->lsqr.err);
     // The recursive residual of the FP32 products can drift from the true one:
-    // form r = b - A x with FP64 accumulation and, while a right-hand side's
-    // true residual is above eps ||b||, solve A d = r by BiCGSTAB (to eps
-    // ||b|| / ||r||) and set x += d -- FP64 refinement around the mixed solver.
+    // form r = b - A x over the stored matrix in float-float (or FP64)
+    // arithmetic and, while a right-hand side's true residual is above eps
+    // ||b||, solve A d = r by BiCGSTAB (to eps ||b|| / ||r||) and set x += d --
+    // iterative refinement in extended precision around the mixed solver.
     {
       const int64_t m = c->m, n = c->n;
       std::vector<double> hb((size_t)nrhs * m), hr((size_t)nrhs * m);

@@ -22,13 +22,14 @@
 // costs only launches.
 //
 // With FP32 products the Arnoldi relation holds to the FP32 rounding of A, so
-// the residual estimate |g_{j+1}| can fall below the true residual.  At the end
-// of every cycle the iterate is updated and its true residual b - A x is
-// formed with FP64 accumulation over the stored matrix (DenseLsqr::residual);
-// a column is converged when that residual is within tol, and the next cycle
-// starts from it otherwise (FP64 iterative refinement around the FP32 Krylov
-// solver).  A cycle that does not lower a column's true residual by 10 % stops
-// that column with status 3.
+// the residual estimate |g_{j+1}| can fall below the true residual: a cycle's
+// steps run until the estimate is below kGmresInner x tol.  At the end of
+// every cycle the iterate is updated and its true residual b - A x is formed
+// over the stored matrix in float-float (or FP64) arithmetic
+// (DenseLsqr::residual); a column is converged when that residual is within
+// tol, and the next cycle starts from it otherwise (iterative refinement in
+// extended precision around the FP32 Krylov solver).  A cycle that does not
+// lower a column's true residual by 10 % stops that column with status 3.
 #include "agb_lsqr.cuh"
 #include "agb_sweeps.cuh"
 #include <algorithm>
@@ -449,7 +450,7 @@ bool DenseLsqr::gmres(const double* b_dev, double* x_dev, const double* q_dev, d
     if (*h_nactive == 0) break;
     if (cudaGraphLaunch(gexec, stream) != cudaSuccess) { ok = false; break; }
     launches += 10L * mr;
-    // iterate update and the FP64 true residual of every column
+    // iterate update and the true residual of every column
     k_gm_solve<<<1, 32, 0, stream>>>(mr, H, g, gsc, y);
     k_gm_xupd<<<nb_el, GM_THREADS, 0, stream>>>(pk_ne, Vb, mv, y, pc9, gsc, X);
     k_gm_out<<<gdiv((long long)m * 8, 256), 256, 0, stream>>>(pk_ne, k, X, x_dev);
