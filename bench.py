@@ -260,26 +260,41 @@ def small_body(level, outer_level, outer_radius):
     return m, name
 
 
-def cpu_complete_solve(m, eps):
+def cpu_complete_solve(m, eps, threads=None):
     """One complete resistance-tensor solve by the reference algorithm (the
     oracle's FP64 restatement), timed in full: CoR_Integrals_Stokes over all
     nsp = nnodes + nelem source rows on every host thread (the reference
     splits rows over MPI ranks), then per right-hand side the reference's
     serial CRS system, lsqr_precon + lsqr_solve to eps and the force/torque
     integrals (StokesInlet3sidesForceCRS / ...TorqueOmegaCRS, one field after
-    another).  Nothing is scaled."""
+    another).  Nothing is scaled.  threads: the integration's host threads
+    (default: all of them; 1 is the reference's serial path)."""
     import numpy as np
     oracle = _oracle()
     U = rigid_fields(m)
-    t0 = time.perf_counter()
-    P = oracle.Problem(2, m, walls=[1, 2], known=np.ones((3, 2)), itri=5)
-    P.form_integrals()
-    t1 = time.perf_counter()
-    _, ft, nits, ierr = P.stokes_solve_sequence(U, maxit=0, eps=eps, fwall=1)
-    t2 = time.perf_counter()
-    P.close()
+    prev = oracle.num_threads()
+    if threads:
+        oracle.set_threads(threads)
+    try:
+        t0 = time.perf_counter()
+        P = oracle.Problem(2, m, walls=[1, 2], known=np.ones((3, 2)), itri=5)
+        P.form_integrals()
+        t1 = time.perf_counter()
+        _, ft, nits, ierr = P.stokes_solve_sequence(U, maxit=0, eps=eps, fwall=1)
+        t2 = time.perf_counter()
+        P.close()
+    finally:
+        oracle.set_threads(prev)
     return {"seconds": t2 - t0, "integration_s": t1 - t0, "solve_s": t2 - t1, "nit": [int(v) for v in nits],
             "ierr": int(ierr), "R": ft}
+
+
+def single_thread_leg(m, eps):
+    """The same complete solve with the integration on one host thread (the
+    reference's serial path: the whole solve on one core)."""
+    r = cpu_complete_solve(m, eps, threads=1)
+    return {"solves_per_s": 1.0 / r["seconds"], "seconds": r["seconds"], "integration_s": r["integration_s"],
+            "cores": 1}
 
 
 def cpu_c2_estimate(m, nit_fp64, budget_s):
@@ -363,6 +378,7 @@ def run_reference(args, rank):
     wall = time.perf_counter() - t0
     v = args.steps / sum(secs)
     threads = os.cpu_count() or 1
+    single = single_thread_leg(m, args.eps)
     est = None
     if args.c2_estimate:
         mf, _ = workload(args)
@@ -379,7 +395,7 @@ def run_reference(args, rank):
             "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
                              "sample": f"{args.steps} complete solves of the L{args.cpu_level} body, nothing scaled "
                                        f"(integration on {threads} threads, serial CRS LSQR per right-hand side)"},
-            "host_s": wall, "c2_estimate": est,
+            "host_s": wall, "c2_estimate": est, "single_thread": single,
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -1050,6 +1066,7 @@ def main():
                                                                        np.max(np.abs(Rc))),
                                      "rel_diff_mixed_gpu_vs_cpu": float(np.max(np.abs(gR - Rc)) /
                                                                         np.max(np.abs(Rc)))}}
+            cpu["single_thread"] = single_thread_leg(ms_small, args.eps)
             if args.c2_estimate and fp64 is not None:
                 cpu["c2_estimate"] = cpu_c2_estimate(m, fp64["nit"], args.cpu_seconds)
         except Exception as ex:  # the baseline must not hide the GPU line

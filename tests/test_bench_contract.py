@@ -28,6 +28,9 @@ def test_reference_arm_json_line():
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
     assert "workload" in d["config"] and "complete solves" in d["config"]["workload"]
     assert "nothing scaled" in cb["sample"]
+    # the reference's serial path beside it: the same solve with the integration on one thread
+    st = d["single_thread"]
+    assert st["cores"] == 1 and 0 < st["solves_per_s"] <= d["value"] * 1.2
     # the timed region is the run's own: steps x ms_per_step within the host time
     assert d["steps"] * d["ms_per_step"] / 1000.0 <= d["host_s"] * 1.001
 
