@@ -10,7 +10,11 @@ def reference_mesh(name):
     """Mesh dict (xyz, etype, con, bcid) of tests/golden/<name>.npz; bcid = the gmsh physical id."""
     d = np.load(os.path.join(GOLDEN, name + ".npz"))
     tris = d["tris"]
-    con = np.full((len(tris), 4), -1, np.int32)
-    con[:, :3] = tris
-    return {"xyz": np.ascontiguousarray(d["xyz"], dtype=np.float64), "etype": np.full(len(tris), 2, np.int32),
-            "con": con, "bcid": np.ascontiguousarray(d["phys"], dtype=np.int32)}
+    quads = d["quads"] if "quads" in d.files else np.zeros((0, 4), np.int32)
+    con = np.full((len(tris) + len(quads), 4), -1, np.int32)
+    con[:len(tris), :3] = tris
+    con[len(tris):] = quads
+    etype = np.concatenate([np.full(len(tris), 2, np.int32), np.full(len(quads), 3, np.int32)])
+    phys = np.concatenate([d["phys"], d["qphys"] if "qphys" in d.files else np.zeros(0, np.int32)])
+    return {"xyz": np.ascontiguousarray(d["xyz"], dtype=np.float64), "etype": etype, "con": con,
+            "bcid": np.ascontiguousarray(phys, dtype=np.int32)}

@@ -20,7 +20,8 @@ import pytest
 
 from fixtures import reference_mesh
 
-FIXTURES = ["sphere_01", "sphere_in_sphere_3678", "ellipsoid211_in_sphere_2117", "cube_624"]
+FIXTURES = ["sphere_01", "sphere_in_sphere_3678", "ellipsoid211_in_sphere_2117", "cube_624", "surf_tri_kocka",
+            "quad_kocka_150"]
 
 
 def _io():

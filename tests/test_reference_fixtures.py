@@ -23,7 +23,9 @@ the Poiseuille case (mixed boundary conditions) on the oracle; the Laplace case
 run/laplace/cube-triangles on run/mesh/surf_tri-kocka.msh with its BiC file's EDGE /
 CORNER directives (the walls of the nodes on the cube's edges and corners): the
 package's restatement of the directives against the oracle's, the oracle's fields
-against the exact linear fields, and the GPU (agb_set_node_walls) against the oracle.
+against the exact linear fields, and the GPU (agb_set_node_walls) against the oracle;
+the same directives on the quadrilateral cube of run/laplace/cube-quadrilaterals-simple
+(run/mesh/kocka-000-111-152-150_hex.msh) on the oracle.
 """
 import numpy as np
 import pytest
@@ -310,13 +312,28 @@ CUBE_CASES = {"temperatura": ({5: -0.5, 6: 0.5}, lambda p: p[:, 0] - 0.5),
               "koncentracija": ({1: 1.0, 2: 3.0}, lambda p: 3.0 - 2.0 * p[:, 2])}
 
 
-def _cube_oracle(orc, m, case, rules=True):
-    """Oracle solve of one equation of the cube case; returns (u, q, node walls, problem sizes)."""
-    dirichlet, exact = CUBE_CASES[case]
-    known = [[1 if w in dirichlet else 2 for w in CUBE_WALLS]]
-    P = orc.Problem(1, m, walls=CUBE_WALLS, known=known, itri=5)
+# run/laplace/cube-quadrilaterals-simple: run/mesh/kocka-000-111-152-150_hex.msh (walls 1
+# bottom z=0, 2 front y=0, 3 right x=1, 4 back y=1, 5 left x=0, 6 top z=1), its
+# subdomain's wall order and its EDGE / CORNER directives (kocka-1sd-prevod.bic); one
+# equation: u = -0.5 on right, 0.5 on left, no flux elsewhere (u = 0.5 - x)
+QUAD_WALLS = [2, 4, 3, 5, 1, 6]
+QUAD_RULES = [("EDGE", 6, 4, 4), ("EDGE", 6, 2, 2), ("EDGE", 6, 5, 5), ("EDGE", 6, 3, 3),
+              ("EDGE", 1, 4, 4), ("EDGE", 1, 2, 2), ("EDGE", 1, 5, 5), ("EDGE", 1, 3, 3),
+              ("EDGE", 2, 3, 3), ("EDGE", 2, 5, 5), ("EDGE", 4, 3, 3), ("EDGE", 4, 5, 5),
+              ("CORNER", 6, 2, 3, 3), ("CORNER", 6, 2, 5, 5), ("CORNER", 6, 4, 3, 3), ("CORNER", 6, 4, 3, 3),
+              ("CORNER", 1, 2, 3, 3), ("CORNER", 1, 2, 5, 5), ("CORNER", 1, 4, 3, 3), ("CORNER", 1, 4, 3, 3)]
+QUAD_CASE = ({3: -0.5, 5: 0.5}, lambda p: 0.5 - p[:, 0])
+
+
+def _cube_oracle(orc, m, case, rules=True, walls_order=None, rule_list=None):
+    """Oracle solve of one equation of a cube case; returns (u, q, node walls, problem sizes, known u)."""
+    dirichlet, exact = CUBE_CASES[case] if isinstance(case, str) else case
+    walls_order = CUBE_WALLS if walls_order is None else walls_order
+    rule_list = CUBE_RULES if rule_list is None else rule_list
+    known = [[1 if w in dirichlet else 2 for w in walls_order]]
+    P = orc.Problem(1, m, walls=walls_order, known=known, itri=5, iqud=4)
     if rules:
-        for r in CUBE_RULES:
+        for r in rule_list:
             if r[0] == "EDGE":
                 P.edge_rule(*r[1:])
             else:
@@ -352,6 +369,28 @@ def test_edge_corner_rules_match_the_oracle(orc):
     assert np.sum(walls != auto) > 0
     with pytest.raises(ValueError):
         M.edge_corner_node_walls(m, CUBE_WALLS, [("EDGE", 1, 2)])
+
+
+def test_edge_corner_rules_quadrilaterals(orc):
+    """The same on the reference's cube of quadrilaterals (cube-quadrilaterals-simple),
+    and its equation on the oracle: the Dirichlet faces' edges and corners on those
+    faces, the linear field u = 0.5 - x at every node."""
+    from andromeda_gb300 import mesh as M
+    m = reference_mesh("quad_kocka_150")
+    assert np.all(m["etype"] == 3) and len(m["etype"]) == 150
+    P = orc.Problem(1, m, walls=QUAD_WALLS, known=[[2, 2, 1, 1, 2, 2]], itri=5, iqud=4)
+    for r in QUAD_RULES:
+        (P.edge_rule if r[0] == "EDGE" else P.corner_rule)(*r[1:])
+    walls = P.node_walls()
+    P.close()
+    assert np.array_equal(walls, M.edge_corner_node_walls(m, QUAD_WALLS, QUAD_RULES))
+    x = m["xyz"][:, 0]
+    assert np.all(walls[np.isclose(x, 1.0)] == 3) and np.all(walls[np.isclose(x, 0.0)] == 5)
+    u, q, walls, sizes, u0 = _cube_oracle(orc, m, QUAD_CASE, walls_order=QUAD_WALLS, rule_list=QUAD_RULES)
+    ue = QUAD_CASE[1](m["xyz"])
+    known = np.isin(walls, [3, 5])
+    assert np.max(np.abs(u[known] - ue[known])) < 1e-14
+    assert np.max(np.abs(u - ue)) < 1e-10  # 8e-13 (5e-12 with the automatic assignment)
 
 
 @pytest.mark.parametrize("case", ["temperatura", "koncentracija"])
